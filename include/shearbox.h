@@ -1,0 +1,123 @@
+/*
+ * shearbox.h -- C-ABI of the GB300 shearing-box RK3 time stepper.
+ *
+ * Drop-in boundary for the time step of hiiragiyua/shear_nnf (r1745).  The
+ * reference has no plugin or FFI layer; its boundary is the Fortran routine
+ *     cross(vor,phi,u00,w00,hv,hg,phiwk,vorwk,dvordy,rhvc1,rhvc2,rhgc1,rhgc2,chwk)
+ * (cross.f90:3-4), called from disk3d (main.f90:279-280), calc_dns_disk3d
+ * (gmres_shear.f90:3103-3104) and shoot_shear.f90:527, with its parameters in
+ * modules ctes / running / bcs (mod.f90:1-130).  The entry points below are what
+ * an ISO_C_BINDING interface of that routine binds.
+ *
+ * Conventions
+ *   - every function returns 0 on success and a positive error code otherwise;
+ *     sb_last_error() describes the last failure of the calling thread.  Nothing
+ *     in the library stops the process (the reference's `stop` statements become
+ *     error codes or status flags).
+ *   - state arrays use the reference pencil layout: vor/phi are
+ *     complex(0:my1, 0:mx1, 0:mz1) stored as interleaved (re, im) doubles, y
+ *     fastest (cross.f90:32-33, the `buffsize` arrays of main.f90:67 with one
+ *     rank); u00/w00 are real(0:my1).  Host memory is caller-owned and copied;
+ *     device memory is owned by the handle.
+ *   - a handle holds `batch` independent boxes of one grid; it is not reentrant
+ *     and owns one CUDA stream.  No CPU fallback exists: creation fails if no
+ *     GPU is present.
+ */
+#ifndef SHEARBOX_H
+#define SHEARBOX_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SB_TRACE_RECORD 24
+
+/* Run parameters.  Mirrors hre2.dat records 1, 2 and 4 as read by initcr
+ * (initcr.f90:54-135) plus the run options of cross (running module,
+ * mod.f90:54-81).  fixed_dt > 0 selects a constant step in place of the CFL
+ * rule (the reference hard-codes ifix_dt=0, cross.f90:87,1608-1611). */
+typedef struct sb_params {
+  int mgalx, my, mgalz;        /* physical grid */
+  double Re, alp, Ly, gam;     /* 1/nu, 2pi/Lx, Ly, 2pi/Lz */
+  double s, chi, CFL;          /* shear rate, rotation, CFL number */
+  double vbulk;                /* v of the (0,0) mode (cross.f90:1276) */
+  double fixed_dt;             /* > 0: constant Delta t */
+  int readflag;                /* 0: initial umax floor as for a created i.c. */
+  double uprim;                /* hre2.dat uprime (used with readflag=0, s=0) */
+  int nhist;                   /* UNER statistics every nhist steps */
+  double etime, dumptime, dtimag; /* end time, dump time and interval */
+} sb_params;
+
+/* Per-box status after sb_step (cross.f90 istop logic, 1683-1690, 2102-2115) */
+typedef struct sb_status {
+  int istop;        /* 1 if the run was asked to stop */
+  int steps_done;   /* completed steps in the last call */
+  int ntrace;       /* statistics records written in the last call */
+  int flags;        /* 1 diverged (dt<1e-10), 2 NaN, 4 laminarised, 8 end time */
+  double time, deltat, xoffb, xofft, cfl, cflv;
+} sb_status;
+
+typedef struct sb_handle sb_handle;
+
+/* precision of sb_create */
+#define SB_FP64 0
+
+/* Creates a handle for `batch` boxes: precomputes the compact-scheme
+ * coefficients and factorisations (derivadas/prederiv1/prederiv2,
+ * diffy_shear_hepta.f90:68-296,535-573), wavenumbers and CFL constants
+ * (set_xyz_dy, initcr.f90:443-519) and allocates the device state.
+ * Replaces initcr's set-up of the time step (initcr.f90:184-307). */
+int sb_create(const sb_params *p, int batch, int precision, sb_handle **out);
+int sb_destroy(sb_handle *h);
+
+/* Per-box Reynolds number (ensembles); default p->Re. */
+int sb_set_member_re(sb_handle *h, int member, double Re);
+
+/* Copies one box's state in / out (what getfil / escru read and write,
+ * readwrite.f90:72-447,1164-1402, minus the file). */
+int sb_set_state(sb_handle *h, int member, const double *vor, const double *phi,
+                 const double *u00, const double *w00, double time, double xoffb,
+                 double xofft);
+int sb_get_state(sb_handle *h, int member, double *vor, double *phi, double *u00,
+                 double *w00, double *time, double *xoffb, double *xofft);
+
+/* Advances every box by nsteps RK3 steps on the device, with the semantics of
+ * one call of cross (cross.f90:336-1029): set_conj on entry, v from phi on the
+ * first step, Delta t from the CFL (or fixed_dt) on every step, stop on
+ * NaN / divergence / laminarisation / etime. */
+int sb_step(sb_handle *h, int nsteps);
+int sb_get_status(sb_handle *h, int member, sb_status *st);
+
+/* Statistics records of the last sb_step (the .cfbin record of
+ * cross.f90:2087): time, Deltat, uner(1:10), CFL, CFLv, umax(1:3), xoffb,
+ * xofft, umax(0), uner2(1:4). */
+int sb_get_trace(sb_handle *h, int member, double *out, int max_records, int *nrec);
+
+/* Drop-in for cross(): box 0's host state in, nstep steps, state out. */
+int sb_cross(sb_handle *h, double *vor, double *phi, double *u00, double *w00, double *time,
+             double *xoffb, double *xofft, int nstep, sb_status *st);
+
+/* CUDA stream of the handle (cudaStream_t) and a blocking wait on it. */
+void *sb_get_stream(sb_handle *h);
+int sb_sync(sb_handle *h);
+
+/* Sizes for a parameter set: out[0..7] = mx, mz, nkx(=mx/2), my, nz, mgalx,
+ * mgalz, complex entries per box (= nkx*mz*my).  Host only. */
+int sb_sizes(const sb_params *p, int *out);
+
+/* Seeded divergence-free initial field (host only): random-phase modes with
+ * E(k) ~ k^4 exp(-2 (k/k0)^2), rms velocity urms, written in the pencil layout.
+ * A synthetic stand-in for the reference's getini (initcr.f90:664-822). */
+int sb_seed_state(const sb_params *p, unsigned long long seed, double k0, double urms,
+                  double *vor, double *phi, double *u00, double *w00);
+
+/* Compact-scheme coefficients pr1, rh1*dy, pr2, rh2*dy^2 (7 each, index d+3)
+ * as computed by prederiv1/prederiv2 (diffy_shear_hepta.f90:68-296). Host only. */
+int sb_compact_coeffs(double *pr1, double *rh1h, double *pr2, double *rh2h);
+
+const char *sb_last_error(void);
+int sb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

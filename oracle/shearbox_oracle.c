@@ -1,0 +1,1510 @@
+/*
+ * shearbox_oracle.c -- CPU FP64 restatement of the reference's RK3 time step.
+ *
+ * TEST INFRASTRUCTURE ONLY (see shearbox_oracle.h).  Every routine cites the
+ * reference file:line it restates.  Operation order follows the Fortran source
+ * (left-to-right evaluation, separate multiply and add; built with
+ * -ffp-contract=off) so that the oracle is deterministic on x86 and Arm.
+ *
+ * Restated parts:
+ *   cross.f90:336-1029       RK3 step loop, explicit branch, iadd_mode=5
+ *   cross.f90:1127-1765      hvhg (non-LES)
+ *   cross.f90:1773-2121      hist, flags 'f' and 'w' (UNER record)
+ *   fou3D_thread.f:22-161    fourxz / fill00 / pack00 (FFTW semantics, own FFT)
+ *   diffy_shear_hepta.f90    prederiv1/2, derivyc, lapcdy, visc3d,
+ *                            modChol7cyclic_cmplx, modChol_addshear, solve7cyclic,
+ *                            gaussj
+ *   operators.f90:86-145     moving_frame;  operators.f90:1382-1429 set_conj
+ *   initcr.f90:191-216,443-519  sizes, wavenumbers, y grid, CFL constants
+ */
+#include "shearbox_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef struct { double re, im; } cplx;
+
+static inline cplx C(double r, double i) { cplx z = {r, i}; return z; }
+static inline cplx cadd(cplx a, cplx b) { return C(a.re + b.re, a.im + b.im); }
+static inline cplx csub(cplx a, cplx b) { return C(a.re - b.re, a.im - b.im); }
+static inline cplx cmul(cplx a, cplx b) {
+  return C(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+static inline cplx cscal(double r, cplx a) { return C(r * a.re, r * a.im); }
+static inline cplx cconj(cplx a) { return C(a.re, -a.im); }
+static inline cplx cneg(cplx a) { return C(-a.re, -a.im); }
+/* Smith division, specialised to a purely imaginary / purely real divisor */
+static inline cplx cdiv_imag(cplx a, double g) { return C(a.im / g, -a.re / g); }
+static inline cplx cdiv_real(cplx a, double k) { return C(a.re / k, a.im / k); }
+/* |z|^2 as Re(z*conjg(z)) */
+static inline double cabs2(cplx a) { return a.re * a.re + a.im * a.im; }
+/* Re(a*conjg(b)) */
+static inline double crecj(cplx a, cplx b) { return a.re * b.re + a.im * b.im; }
+
+/* ------------------------------------------------------------------------- */
+/* FFT: mixed-radix Stockham autosort (radix 4, 2, 3, 5, generic).  Stands in  */
+/* for FFTW3 (not vendored in the reference): forward e^{-i}, backward e^{+i}, */
+/* both unnormalised, as dfftw_plan_dft_* (fou3D_thread.f:14-17).              */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  int n, nst, rad[40];
+  cplx *tw; /* e^{-2 pi i t/n}, t = 0..n-1 */
+} fftplan;
+
+static void plan_init(fftplan *p, int n) {
+  p->n = n;
+  p->nst = 0;
+  int m = n;
+  while (m % 4 == 0) { p->rad[p->nst++] = 4; m /= 4; }
+  while (m % 2 == 0) { p->rad[p->nst++] = 2; m /= 2; }
+  while (m % 3 == 0) { p->rad[p->nst++] = 3; m /= 3; }
+  while (m % 5 == 0) { p->rad[p->nst++] = 5; m /= 5; }
+  if (m > 1) p->rad[p->nst++] = m; /* generic DFT stage */
+  p->tw = (cplx *)malloc(sizeof(cplx) * (size_t)n);
+  const double pi2 = 8.0 * atan(1.0);
+  for (int t = 0; t < n; t++) {
+    double a = -pi2 * (double)t / (double)n;
+    p->tw[t] = C(cos(a), sin(a));
+  }
+}
+static void plan_free(fftplan *p) { free(p->tw); p->tw = NULL; }
+
+static void dft_small(cplx *v, int R, int sign, const fftplan *p) {
+  cplx out[64];
+  if (R == 2) {
+    cplx a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+    return;
+  }
+  if (R == 4) {
+    cplx a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+    cplx b0 = cadd(v[1], v[3]), b1 = csub(v[1], v[3]);
+    /* -i*b1 for forward, +i*b1 for backward */
+    cplx jb1 = sign < 0 ? C(b1.im, -b1.re) : C(-b1.im, b1.re);
+    v[0] = cadd(a0, b0);
+    v[2] = csub(a0, b0);
+    v[1] = cadd(a1, jb1);
+    v[3] = csub(a1, jb1);
+    return;
+  }
+  if (R == 3) {
+    const double s3 = 0.86602540378443864676; /* sin(pi/3) */
+    cplx t1 = cadd(v[1], v[2]);
+    cplx t2 = C(v[0].re - 0.5 * t1.re, v[0].im - 0.5 * t1.im);
+    cplx d = csub(v[1], v[2]);
+    cplx t3 = C(s3 * d.re, s3 * d.im);
+    cplx jt3 = sign < 0 ? C(t3.im, -t3.re) : C(-t3.im, t3.re); /* -/+ i*t3 */
+    v[0] = cadd(v[0], t1);
+    v[1] = cadd(t2, jt3);
+    v[2] = csub(t2, jt3);
+    return;
+  }
+  /* generic: direct DFT with the plan's twiddles (R divides n) */
+  int stride = p->n / R;
+  for (int q = 0; q < R; q++) {
+    cplx acc = C(0.0, 0.0);
+    for (int r = 0; r < R; r++) {
+      cplx w = p->tw[((r * q) % R) * stride];
+      if (sign > 0) w = cconj(w);
+      acc = cadd(acc, cmul(v[r], w));
+    }
+    out[q] = acc;
+  }
+  for (int q = 0; q < R; q++) v[q] = out[q];
+}
+
+/* in-place transform of data[0..n-1]; work holds n entries */
+static void fft_exec(const fftplan *p, cplx *data, cplx *work, int sign) {
+  int n = p->n;
+  cplx *in = data, *out = work;
+  int Ns = 1;
+  for (int s = 0; s < p->nst; s++) {
+    int R = p->rad[s];
+    int nr = n / R;
+    for (int j = 0; j < nr; j++) {
+      cplx v[64];
+      int jm = j % Ns;
+      for (int r = 0; r < R; r++) v[r] = in[j + r * nr];
+      if (Ns > 1 && jm != 0) {
+        int step = n / (Ns * R);
+        for (int r = 1; r < R; r++) {
+          cplx w = p->tw[r * jm * step];
+          if (sign > 0) w = cconj(w);
+          v[r] = cmul(v[r], w);
+        }
+      }
+      dft_small(v, R, sign, p);
+      int idxD = (j / Ns) * Ns * R + jm;
+      for (int r = 0; r < R; r++) out[idxD + r * Ns] = v[r];
+    }
+    cplx *t = in;
+    in = out;
+    out = t;
+    Ns *= R;
+  }
+  if (in != data) memcpy(data, in, sizeof(cplx) * (size_t)n);
+}
+
+void orc_fft(int n, double *data, int sign) {
+  fftplan p;
+  plan_init(&p, n);
+  cplx *w = (cplx *)malloc(sizeof(cplx) * (size_t)n);
+  fft_exec(&p, (cplx *)data, w, sign);
+  free(w);
+  plan_free(&p);
+}
+
+/* ------------------------------------------------------------------------- */
+/* context                                                                    */
+/* ------------------------------------------------------------------------- */
+typedef struct { /* THREADPRIVATE scratch of module yderiv (diffy_shear_hepta.f90:42-43) */
+  double *ah, *bh, *ch, *dh, *dhm1;
+  cplx *eh, *fh, *gh, *ceh, *cfh, *cgh;
+  cplx *wk1, *wk2, *ur, *uc, *duc, *pc;
+  double lapmat[7];
+} ythread;
+
+typedef struct { /* per-thread plane buffers for hvhg */
+  cplx *u1c, *u2c, *u3c, *o1c, *o2c, *o3c;
+  double *u1r, *u2r, *u3r, *o1r, *o2r, *o3r;
+  cplx *wz, *col, *row, *work;
+} pthread_buf;
+
+typedef struct {
+  orc_params p;
+  int mgalx, my, mgalz, mx, mz, mx1, my1, mz1, mgx, nz, nz1, nz2, nkx;
+  double pi, pi2, dx, dy, dz, Lx, Lz, cflx, cfly, cflz, cflvv, h;
+  double *y;
+  double *xalp_im, *xgam_im, *alp2, *gam2;
+  double pr1[7], rh1[7], rh1h[7], pr2[7], rh2[7], rh2h[7];
+  double *a1, *b1, *c1, *d1, *d1m1;
+  cplx *e1, *f1, *g1, *ce1, *cf1, *cg1;
+  double *a2, *b2, *c2, *d2, *d2m1;
+  cplx *e2, *f2, *g2, *ce2, *cf2, *cg2;
+  fftplan px, pz;
+  int nthr;
+  ythread *yt;
+  pthread_buf *pt;
+} ctx;
+
+#define A7(a, d) ((a)[(d) + 3])
+
+static int g_threads = 0;
+void orc_set_threads(int n) { g_threads = n; }
+
+static int my_thread(void) {
+#ifdef _OPENMP
+  return omp_get_thread_num();
+#else
+  return 0;
+#endif
+}
+
+static double *dalloc(size_t n) { return (double *)calloc(n + 8, sizeof(double)); }
+static cplx *zalloc(size_t n) { return (cplx *)calloc(n + 8, sizeof(cplx)); }
+
+/* gaussj: Numerical Recipes Gauss-Jordan with full pivoting
+ * (diffy_shear_hepta.f90:1125-1203).  a is np x np column-major, b is np x m. */
+static void gaussj(double *a, int n, int np, double *b, int m, int mp) {
+  (void)mp;
+#define AA(r, c) a[((c)-1) * np + ((r)-1)]
+#define BB(r, c) b[((c)-1) * np + ((r)-1)]
+  int indxc[50], indxr[50], ipiv[50];
+  int irow = 0, icol = 0;
+  for (int j = 1; j <= n; j++) ipiv[j - 1] = 0;
+  for (int i = 1; i <= n; i++) {
+    double big = 0.0;
+    for (int j = 1; j <= n; j++) {
+      if (ipiv[j - 1] != 1) {
+        for (int k = 1; k <= n; k++) {
+          if (ipiv[k - 1] == 0) {
+            if (fabs(AA(j, k)) >= big) {
+              big = fabs(AA(j, k));
+              irow = j;
+              icol = k;
+            }
+          }
+        }
+      }
+    }
+    ipiv[icol - 1] += 1;
+    if (irow != icol) {
+      for (int l = 1; l <= n; l++) {
+        double d = AA(irow, l);
+        AA(irow, l) = AA(icol, l);
+        AA(icol, l) = d;
+      }
+      for (int l = 1; l <= m; l++) {
+        double d = BB(irow, l);
+        BB(irow, l) = BB(icol, l);
+        BB(icol, l) = d;
+      }
+    }
+    indxr[i - 1] = irow;
+    indxc[i - 1] = icol;
+    double pivinv = 1.0 / AA(icol, icol);
+    AA(icol, icol) = 1.0;
+    for (int l = 1; l <= n; l++) AA(icol, l) = AA(icol, l) * pivinv;
+    for (int l = 1; l <= m; l++) BB(icol, l) = BB(icol, l) * pivinv;
+    for (int ll = 1; ll <= n; ll++) {
+      if (ll != icol) {
+        double dum = AA(ll, icol);
+        AA(ll, icol) = 0.0;
+        for (int l = 1; l <= n; l++) AA(ll, l) = AA(ll, l) - AA(icol, l) * dum;
+        for (int l = 1; l <= m; l++) BB(ll, l) = BB(ll, l) - BB(icol, l) * dum;
+      }
+    }
+  }
+  for (int l = n; l >= 1; l--) {
+    if (indxr[l - 1] != indxc[l - 1]) {
+      for (int k = 1; k <= n; k++) {
+        double d = AA(k, indxr[l - 1]);
+        AA(k, indxr[l - 1]) = AA(k, indxc[l - 1]);
+        AA(k, indxc[l - 1]) = d;
+      }
+    }
+  }
+#undef AA
+#undef BB
+}
+
+/* modChol7cyclic_cmplx (diffy_shear_hepta.f90:578-755); arrays 1-based */
+static void modchol7(double *La, double *Lb, double *Lc, double *Dd, double *Ddm1,
+                     cplx *Le, cplx *Lf, cplx *Lg, cplx *cLe, cplx *cLf, cplx *cLg,
+                     const double *a, int N, cplx shp) {
+  int i, j, k;
+  double tmpr;
+  cplx tmp;
+  j = 1;
+  Dd[j] = A7(a, 0);
+  Ddm1[j] = 1.0 / A7(a, 0);
+  La[j + 1] = Ddm1[j] * A7(a, 1);
+  Lb[j + 2] = Ddm1[j] * A7(a, 2);
+  Lc[j + 3] = Ddm1[j] * A7(a, 3);
+  j = 2;
+  Dd[j] = A7(a, 0) - (La[j] * Dd[j - 1] * La[j]);
+  Ddm1[j] = 1.0 / Dd[j];
+  La[j + 1] = Ddm1[j] * (A7(a, 1) - Lb[j + 1] * Dd[j - 1] * La[j]);
+  Lb[j + 2] = Ddm1[j] * (A7(a, 2) - Lc[j + 2] * Dd[j - 1] * La[j]);
+  Lc[j + 3] = Ddm1[j] * A7(a, 3);
+  j = 3;
+  Dd[j] = A7(a, 0) - (Lb[j] * Dd[j - 2] * Lb[j] + La[j] * Dd[j - 1] * La[j]);
+  Ddm1[j] = 1.0 / Dd[j];
+  La[j + 1] = Ddm1[j] * (A7(a, 1) - (Lc[j + 1] * Dd[j - 2] * Lb[j] + Lb[j + 1] * Dd[j - 1] * La[j]));
+  Lb[j + 2] = Ddm1[j] * (A7(a, 2) - Lc[j + 2] * Dd[j - 1] * La[j]);
+  Lc[j + 3] = Ddm1[j] * A7(a, 3);
+  for (j = 4; j <= N - 6; j++) {
+    Dd[j] = A7(a, 0) - (Lc[j] * Dd[j - 3] * Lc[j] + Lb[j] * Dd[j - 2] * Lb[j] + La[j] * Dd[j - 1] * La[j]);
+    Ddm1[j] = 1.0 / Dd[j];
+    La[j + 1] = Ddm1[j] * (A7(a, 1) - (Lc[j + 1] * Dd[j - 2] * Lb[j] + Lb[j + 1] * Dd[j - 1] * La[j]));
+    Lb[j + 2] = Ddm1[j] * (A7(a, 2) - Lc[j + 2] * Dd[j - 1] * La[j]);
+    Lc[j + 3] = Ddm1[j] * A7(a, 3);
+  }
+  j = N - 5;
+  Dd[j] = A7(a, 0) - (Lc[j] * Dd[j - 3] * Lc[j] + Lb[j] * Dd[j - 2] * Lb[j] + La[j] * Dd[j - 1] * La[j]);
+  Ddm1[j] = 1.0 / Dd[j];
+  La[j + 1] = Ddm1[j] * (A7(a, 1) - (Lc[j + 1] * Dd[j - 2] * Lb[j] + Lb[j + 1] * Dd[j - 1] * La[j]));
+  Lb[j + 2] = Ddm1[j] * (A7(a, 2) - Lc[j + 2] * Dd[j - 1] * La[j]);
+  j = N - 4;
+  Dd[j] = A7(a, 0) - (Lc[j] * Dd[j - 3] * Lc[j] + Lb[j] * Dd[j - 2] * Lb[j] + La[j] * Dd[j - 1] * La[j]);
+  Ddm1[j] = 1.0 / Dd[j];
+  La[j + 1] = Ddm1[j] * (A7(a, 1) - (Lc[j + 1] * Dd[j - 2] * Lb[j] + Lb[j + 1] * Dd[j - 1] * La[j]));
+  j = N - 3;
+  Dd[j] = A7(a, 0) - (Lc[j] * Dd[j - 3] * Lc[j] + Lb[j] * Dd[j - 2] * Lb[j] + La[j] * Dd[j - 1] * La[j]);
+  Ddm1[j] = 1.0 / Dd[j];
+  /* row N-2 */
+  Le[1] = cscal(Ddm1[1] * A7(a, 3), shp);
+  i = 2;
+  Le[2] = cscal(Ddm1[i], cneg(cscal(La[i], cscal(Dd[i - 1], Le[i - 1]))));
+  i = 3;
+  Le[3] = cscal(Ddm1[i], csub(cneg(cscal(Lb[i], cscal(Dd[i - 2], Le[i - 2]))),
+                             cscal(La[i], cscal(Dd[i - 1], Le[i - 1]))));
+  for (i = 4; i <= N - 6; i++) {
+    cplx t = cneg(cscal(Lc[i], cscal(Dd[i - 3], Le[i - 3])));
+    t = csub(t, cscal(Lb[i], cscal(Dd[i - 2], Le[i - 2])));
+    t = csub(t, cscal(La[i], cscal(Dd[i - 1], Le[i - 1])));
+    Le[i] = cscal(Ddm1[i], t);
+  }
+  for (i = N - 5; i <= N - 3; i++) {
+    double ad = (i == N - 5) ? A7(a, 3) : (i == N - 4) ? A7(a, 2) : A7(a, 1);
+    cplx t = csub(C(ad, 0.0), cscal(Lc[i], cscal(Dd[i - 3], Le[i - 3])));
+    t = csub(t, cscal(Lb[i], cscal(Dd[i - 2], Le[i - 2])));
+    t = csub(t, cscal(La[i], cscal(Dd[i - 1], Le[i - 1])));
+    Le[i] = cscal(Ddm1[i], t);
+  }
+  j = N - 2;
+  tmpr = 0.0;
+  for (k = 1; k <= N - 3; k++) tmpr = tmpr + cabs2(Le[k]) * Dd[k];
+  Dd[j] = A7(a, 0) - tmpr;
+  Ddm1[j] = 1.0 / Dd[j];
+  /* row N-1 */
+  Lf[1] = cscal(Ddm1[1] * A7(a, 2), shp);
+  i = 2;
+  Lf[i] = cscal(Ddm1[i], csub(cscal(A7(a, 3), shp), cscal(La[i], cscal(Dd[i - 1], Lf[i - 1]))));
+  i = 3;
+  Lf[i] = cscal(Ddm1[i], csub(cneg(cscal(Lb[i], cscal(Dd[i - 2], Lf[i - 2]))),
+                             cscal(La[i], cscal(Dd[i - 1], Lf[i - 1]))));
+  for (i = 4; i <= N - 5; i++) {
+    cplx t = cneg(cscal(Lc[i], cscal(Dd[i - 3], Lf[i - 3])));
+    t = csub(t, cscal(Lb[i], cscal(Dd[i - 2], Lf[i - 2])));
+    t = csub(t, cscal(La[i], cscal(Dd[i - 1], Lf[i - 1])));
+    Lf[i] = cscal(Ddm1[i], t);
+  }
+  for (i = N - 4; i <= N - 3; i++) {
+    double ad = (i == N - 4) ? A7(a, 3) : A7(a, 2);
+    cplx t = csub(C(ad, 0.0), cscal(Lc[i], cscal(Dd[i - 3], Lf[i - 3])));
+    t = csub(t, cscal(Lb[i], cscal(Dd[i - 2], Lf[i - 2])));
+    t = csub(t, cscal(La[i], cscal(Dd[i - 1], Lf[i - 1])));
+    Lf[i] = cscal(Ddm1[i], t);
+  }
+  i = N - 2;
+  tmp = C(0.0, 0.0);
+  for (k = 1; k <= N - 3; k++) tmp = cadd(tmp, cscal(Dd[k], cmul(Lf[k], cconj(Le[k]))));
+  Lf[i] = cscal(Ddm1[j], csub(C(A7(a, 1), 0.0), tmp));
+  j = N - 1;
+  tmpr = 0.0;
+  for (k = 1; k <= N - 2; k++) tmpr = tmpr + cabs2(Lf[k]) * Dd[k];
+  Dd[j] = A7(a, 0) - tmpr;
+  Ddm1[j] = 1.0 / Dd[j];
+  /* row N */
+  Lg[1] = cscal(Ddm1[1] * A7(a, 1), shp);
+  i = 2;
+  Lg[i] = cscal(Ddm1[i], csub(cscal(A7(a, 2), shp), cscal(La[i], cscal(Dd[i - 1], Lg[i - 1]))));
+  i = 3;
+  {
+    cplx t = csub(cscal(A7(a, 3), shp), cscal(Lb[i], cscal(Dd[i - 2], Lg[i - 2])));
+    t = csub(t, cscal(La[i], cscal(Dd[i - 1], Lg[i - 1])));
+    Lg[i] = cscal(Ddm1[i], t);
+  }
+  for (i = 4; i <= N - 4; i++) {
+    cplx t = cneg(cscal(Lc[i], cscal(Dd[i - 3], Lg[i - 3])));
+    t = csub(t, cscal(Lb[i], cscal(Dd[i - 2], Lg[i - 2])));
+    t = csub(t, cscal(La[i], cscal(Dd[i - 1], Lg[i - 1])));
+    Lg[i] = cscal(Ddm1[i], t);
+  }
+  i = N - 3;
+  {
+    cplx t = csub(C(A7(a, 3), 0.0), cscal(Lc[i], cscal(Dd[i - 3], Lg[i - 3])));
+    t = csub(t, cscal(Lb[i], cscal(Dd[i - 2], Lg[i - 2])));
+    t = csub(t, cscal(La[i], cscal(Dd[i - 1], Lg[i - 1])));
+    Lg[i] = cscal(Ddm1[i], t);
+  }
+  i = N - 2;
+  tmp = C(0.0, 0.0);
+  for (k = 1; k <= i - 1; k++) tmp = cadd(tmp, cscal(Dd[k], cmul(Lg[k], cconj(Le[k]))));
+  Lg[i] = cscal(Ddm1[i], csub(C(A7(a, 2), 0.0), tmp));
+  i = N - 1;
+  tmp = C(0.0, 0.0);
+  for (k = 1; k <= i - 1; k++) tmp = cadd(tmp, cscal(Dd[k], cmul(Lg[k], cconj(Lf[k]))));
+  Lg[i] = cscal(Ddm1[i], csub(C(A7(a, 1), 0.0), tmp));
+  j = N;
+  tmpr = 0.0;
+  for (k = 1; k <= N - 1; k++) tmpr = tmpr + cabs2(Lg[k]) * Dd[k];
+  Dd[j] = A7(a, 0) - tmpr;
+  Ddm1[j] = 1.0 / Dd[j];
+  for (k = 1; k <= N; k++) {
+    cLe[k] = cconj(Le[k]);
+    cLf[k] = cconj(Lf[k]);
+    cLg[k] = cconj(Lg[k]);
+  }
+}
+
+/* modChol_addshear (diffy_shear_hepta.f90:760-870): recompute the shear tail */
+static void modchol_addshear(const double *La, const double *Lb, const double *Lc,
+                             double *Dd, double *Ddm1, cplx *Le, cplx *Lf, cplx *Lg,
+                             cplx *cLe, cplx *cLf, cplx *cLg, const double *a, int N) {
+  int i, j, k;
+  double tmpr;
+  cplx tmp;
+  for (i = N - 5; i <= N - 3; i++) {
+    double ad = (i == N - 5) ? A7(a, 3) : (i == N - 4) ? A7(a, 2) : A7(a, 1);
+    cplx t = csub(C(ad, 0.0), cscal(Lc[i], cscal(Dd[i - 3], Le[i - 3])));
+    t = csub(t, cscal(Lb[i], cscal(Dd[i - 2], Le[i - 2])));
+    t = csub(t, cscal(La[i], cscal(Dd[i - 1], Le[i - 1])));
+    Le[i] = cscal(Ddm1[i], t);
+  }
+  j = N - 2;
+  tmpr = 0.0;
+  for (k = 1; k <= N - 3; k++) tmpr = tmpr + cabs2(Le[k]) * Dd[k];
+  Dd[j] = A7(a, 0) - tmpr;
+  Ddm1[j] = 1.0 / Dd[j];
+  for (i = N - 4; i <= N - 3; i++) {
+    double ad = (i == N - 4) ? A7(a, 3) : A7(a, 2);
+    cplx t = csub(C(ad, 0.0), cscal(Lc[i], cscal(Dd[i - 3], Lf[i - 3])));
+    t = csub(t, cscal(Lb[i], cscal(Dd[i - 2], Lf[i - 2])));
+    t = csub(t, cscal(La[i], cscal(Dd[i - 1], Lf[i - 1])));
+    Lf[i] = cscal(Ddm1[i], t);
+  }
+  i = N - 2;
+  tmp = C(0.0, 0.0);
+  for (k = 1; k <= N - 3; k++) tmp = cadd(tmp, cscal(Dd[k], cmul(Lf[k], cconj(Le[k]))));
+  Lf[i] = cscal(Ddm1[j], csub(C(A7(a, 1), 0.0), tmp));
+  j = N - 1;
+  tmpr = 0.0;
+  for (k = 1; k <= N - 2; k++) tmpr = tmpr + cabs2(Lf[k]) * Dd[k];
+  Dd[j] = A7(a, 0) - tmpr;
+  Ddm1[j] = 1.0 / Dd[j];
+  i = N - 3;
+  {
+    cplx t = csub(C(A7(a, 3), 0.0), cscal(Lc[i], cscal(Dd[i - 3], Lg[i - 3])));
+    t = csub(t, cscal(Lb[i], cscal(Dd[i - 2], Lg[i - 2])));
+    t = csub(t, cscal(La[i], cscal(Dd[i - 1], Lg[i - 1])));
+    Lg[i] = cscal(Ddm1[i], t);
+  }
+  i = N - 2;
+  tmp = C(0.0, 0.0);
+  for (k = 1; k <= i - 1; k++) tmp = cadd(tmp, cscal(Dd[k], cmul(Lg[k], cconj(Le[k]))));
+  Lg[i] = cscal(Ddm1[i], csub(C(A7(a, 2), 0.0), tmp));
+  i = N - 1;
+  tmp = C(0.0, 0.0);
+  for (k = 1; k <= i - 1; k++) tmp = cadd(tmp, cscal(Dd[k], cmul(Lg[k], cconj(Lf[k]))));
+  Lg[i] = cscal(Ddm1[i], csub(C(A7(a, 1), 0.0), tmp));
+  j = N;
+  tmpr = 0.0;
+  for (k = 1; k <= N - 1; k++) tmpr = tmpr + cabs2(Lg[k]) * Dd[k];
+  Dd[j] = A7(a, 0) - tmpr;
+  Ddm1[j] = 1.0 / Dd[j];
+  for (k = 1; k <= N; k++) {
+    cLe[k] = cconj(Le[k]);
+    cLf[k] = cconj(Lf[k]);
+    cLg[k] = cconj(Lg[k]);
+  }
+}
+
+/* solve7cyclic (diffy_shear_hepta.f90:900-954); bb, x, y 1-based */
+static void solve7(const double *La, const double *Lb, const double *Lc,
+                   const double *Ddm1, const cplx *Le, const cplx *Lf, const cplx *Lg,
+                   const cplx *cLe, const cplx *cLf, const cplx *cLg, const cplx *bb,
+                   cplx *x, cplx *y, int nx) {
+  int i, k;
+  cplx tmp;
+  y[1] = bb[1];
+  y[2] = csub(bb[2], cscal(La[2], y[1]));
+  y[3] = csub(bb[3], cadd(cscal(Lb[3], y[1]), cscal(La[3], y[2])));
+  for (i = 4; i <= nx - 3; i++)
+    y[i] = csub(bb[i], cadd(cadd(cscal(Lc[i], y[i - 3]), cscal(Lb[i], y[i - 2])),
+                            cscal(La[i], y[i - 1])));
+  i = nx - 2;
+  tmp = C(0.0, 0.0);
+  for (k = 1; k <= i - 1; k++) tmp = cadd(tmp, cmul(Le[k], y[k]));
+  y[i] = csub(bb[i], tmp);
+  i = nx - 1;
+  tmp = C(0.0, 0.0);
+  for (k = 1; k <= i - 1; k++) tmp = cadd(tmp, cmul(Lf[k], y[k]));
+  y[i] = csub(bb[i], tmp);
+  i = nx;
+  tmp = C(0.0, 0.0);
+  for (k = 1; k <= i - 1; k++) tmp = cadd(tmp, cmul(Lg[k], y[k]));
+  y[i] = csub(bb[i], tmp);
+  x[nx] = cscal(Ddm1[nx], y[nx]);
+  x[nx - 1] = csub(cscal(Ddm1[nx - 1], y[nx - 1]), cmul(cLg[nx - 1], x[nx]));
+  x[nx - 2] = csub(csub(cscal(Ddm1[nx - 2], y[nx - 2]), cmul(cLf[nx - 2], x[nx - 1])),
+                   cmul(cLg[nx - 2], x[nx]));
+  {
+    cplx t = csub(cscal(Ddm1[nx - 3], y[nx - 3]), cmul(cLe[nx - 3], x[nx - 2]));
+    t = csub(t, cmul(cLf[nx - 3], x[nx - 1]));
+    x[nx - 3] = csub(t, cmul(cLg[nx - 3], x[nx]));
+  }
+  {
+    cplx t = csub(cscal(Ddm1[nx - 4], y[nx - 4]), cscal(La[nx - 3], x[nx - 3]));
+    t = csub(t, cmul(cLe[nx - 4], x[nx - 2]));
+    t = csub(t, cmul(cLf[nx - 4], x[nx - 1]));
+    x[nx - 4] = csub(t, cmul(cLg[nx - 4], x[nx]));
+  }
+  {
+    cplx t = csub(cscal(Ddm1[nx - 5], y[nx - 5]), cscal(La[nx - 4], x[nx - 4]));
+    t = csub(t, cscal(Lb[nx - 3], x[nx - 3]));
+    t = csub(t, cmul(cLe[nx - 5], x[nx - 2]));
+    t = csub(t, cmul(cLf[nx - 5], x[nx - 1]));
+    x[nx - 5] = csub(t, cmul(cLg[nx - 5], x[nx]));
+  }
+  for (i = nx - 6; i >= 1; i--) {
+    cplx t = csub(cscal(Ddm1[i], y[i]), cscal(La[i + 1], x[i + 1]));
+    t = csub(t, cscal(Lb[i + 2], x[i + 2]));
+    t = csub(t, cscal(Lc[i + 3], x[i + 3]));
+    t = csub(t, cmul(cLe[i], x[nx - 2]));
+    t = csub(t, cmul(cLf[i], x[nx - 1]));
+    x[i] = csub(t, cmul(cLg[i], x[nx]));
+  }
+}
+
+/* prederiv1 (diffy_shear_hepta.f90:68-162) and prederiv2 (185-296) */
+static void prederiv(ctx *c) {
+  const int N = 3, M = 3;
+  double pi = 4.0 * atan(1.0);
+  { /* first derivative */
+    double kap[3] = {0.5, 0.9, 0.0};
+    kap[2] = 5e-1 * (kap[0] + kap[1]);
+    for (int k = 0; k < M; k++) kap[k] = kap[k] * pi;
+    double mat[36], vec[6];
+    memset(mat, 0, sizeof(mat));
+    memset(vec, 0, sizeof(vec));
+#define MAT(r, cc) mat[((cc)-1) * 6 + ((r)-1)]
+    for (int k = 1; k <= 2 * N - M; k++) {
+      int kk = 2 * k - 1;
+      for (int j = 1; j <= N; j++) {
+        int p1 = 1;
+        for (int e = 0; e < kk - 1; e++) p1 *= j;
+        int p2 = 1;
+        for (int e = 0; e < kk; e++) p2 *= j;
+        MAT(k, j) = (double)(kk * p1);
+        MAT(k, N + j) = -(double)p2;
+      }
+    }
+    vec[0] = -0.5;
+    for (int k = 1; k <= M; k++) {
+      for (int j = 1; j <= N; j++) {
+        MAT(2 * N - M + k, j) = kap[k - 1] * cos(kap[k - 1] * (double)j);
+        MAT(2 * N - M + k, N + j) = -sin(kap[k - 1] * (double)j);
+      }
+      vec[2 * N - M + k - 1] = -0.5 * kap[k - 1];
+    }
+#undef MAT
+    gaussj(mat, 2 * N, 2 * N, vec, 1, 1);
+    for (int j = 1; j <= N; j++) {
+      A7(c->rh1h, j) = vec[N + j - 1];
+      A7(c->rh1h, -j) = -vec[N + j - 1];
+      A7(c->pr1, j) = vec[j - 1];
+      A7(c->pr1, -j) = vec[j - 1];
+    }
+    A7(c->rh1h, 0) = 0.0;
+    A7(c->pr1, 0) = 1.0;
+  }
+  { /* second derivative */
+    double kap[3] = {0.9, 0.5, 0.0};
+    kap[2] = 5e-1 * (kap[0] + kap[1]);
+    for (int k = 0; k < M; k++) kap[k] = kap[k] * pi;
+    double mat[49], vec[7];
+    memset(mat, 0, sizeof(mat));
+    memset(vec, 0, sizeof(vec));
+#define MAT(r, cc) mat[((cc)-1) * 7 + ((r)-1)]
+    for (int j = N + 2; j <= 2 * N + 1; j++) MAT(1, j) = 1.0;
+    MAT(1, N + 1) = 5e-1;
+    for (int k = 2; k <= 2 * N + 1 - M; k++) {
+      int kk = 2 * k - 2;
+      for (int j = 1; j <= N; j++) {
+        int p1 = 1;
+        for (int e = 0; e < kk - 2; e++) p1 *= j;
+        int p2 = 1;
+        for (int e = 0; e < kk; e++) p2 *= j;
+        MAT(k, j) = (double)(kk * (kk - 1) * p1);
+        MAT(k, N + 1 + j) = -(double)p2;
+      }
+    }
+    vec[1] = -1.0;
+    for (int k = 1; k <= M; k++) {
+      for (int j = 1; j <= N; j++) {
+        MAT(2 * N + 1 - M + k, j) = kap[k - 1] * kap[k - 1] * cos(kap[k - 1] * (double)j);
+        MAT(2 * N + 1 - M + k, N + 1 + j) = cos(kap[k - 1] * (double)j);
+      }
+    }
+    for (int r = 2 * N + 2 - M; r <= 2 * N + 1; r++) {
+      MAT(r, N + 1) = 5e-1;
+      vec[r - 1] = -0.5 * kap[r - (2 * N + 2 - M)] * kap[r - (2 * N + 2 - M)];
+    }
+#undef MAT
+    gaussj(mat, 2 * N + 1, 2 * N + 1, vec, 1, 1);
+    for (int j = 1; j <= N; j++) {
+      A7(c->rh2h, j) = vec[N + j];
+      A7(c->rh2h, -j) = vec[N + j];
+      A7(c->pr2, j) = vec[j - 1];
+      A7(c->pr2, -j) = vec[j - 1];
+    }
+    A7(c->rh2h, 0) = vec[N];
+    A7(c->pr2, 0) = 1.0;
+  }
+}
+
+/* derivyc (diffy_shear_hepta.f90:333-450); u, du are real(m, my) */
+static void derivyc(ctx *c, ythread *t, const double *u, double *du, cplx shp, cplx shm,
+                    int iord, int m, int ias) {
+  int my = c->my;
+  cplx *uc = t->uc, *ur = t->ur, *wk1 = t->wk1;
+  if (m == 1) {
+    for (int j = 1; j <= my; j++) uc[j] = C(u[j - 1], 0.0);
+    ur[1] = uc[my - 2];
+    ur[2] = uc[my - 1];
+    ur[3] = uc[my];
+    for (int j = 1; j <= my; j++) ur[3 + j] = uc[j];
+    ur[my + 4] = uc[1];
+    ur[my + 5] = uc[2];
+    ur[my + 6] = uc[3];
+  } else {
+    for (int j = 1; j <= my; j++) uc[j] = C(u[2 * (j - 1)], u[2 * (j - 1) + 1]);
+    ur[1] = cmul(uc[my - 2], shm);
+    ur[2] = cmul(uc[my - 1], shm);
+    ur[3] = cmul(uc[my], shm);
+    for (int j = 1; j <= my; j++) ur[3 + j] = uc[j];
+    ur[my + 4] = cmul(uc[1], shp);
+    ur[my + 5] = cmul(uc[2], shp);
+    ur[my + 6] = cmul(uc[3], shp);
+  }
+  const double *rh = (iord == 1) ? c->rh1 : c->rh2;
+  for (int j = 4; j <= my + 3; j++) {
+    cplx s = cscal(A7(rh, -3), ur[j - 3]);
+    s = cadd(s, cscal(A7(rh, -2), ur[j - 2]));
+    s = cadd(s, cscal(A7(rh, -1), ur[j - 1]));
+    if (iord != 1) s = cadd(s, cscal(A7(rh, 0), ur[j]));
+    s = cadd(s, cscal(A7(rh, 1), ur[j + 1]));
+    s = cadd(s, cscal(A7(rh, 2), ur[j + 2]));
+    s = cadd(s, cscal(A7(rh, 3), ur[j + 3]));
+    wk1[j - 3] = s;
+  }
+  double *a = (iord == 1) ? c->a1 : c->a2, *b = (iord == 1) ? c->b1 : c->b2;
+  double *cc = (iord == 1) ? c->c1 : c->c2, *d = (iord == 1) ? c->d1 : c->d2;
+  double *dm1 = (iord == 1) ? c->d1m1 : c->d2m1;
+  cplx *e = (iord == 1) ? c->e1 : c->e2, *f = (iord == 1) ? c->f1 : c->f2;
+  cplx *g = (iord == 1) ? c->g1 : c->g2;
+  cplx *ce = (iord == 1) ? c->ce1 : c->ce2, *cf = (iord == 1) ? c->cf1 : c->cf2;
+  cplx *cg = (iord == 1) ? c->cg1 : c->cg2;
+  const double *pr = (iord == 1) ? c->pr1 : c->pr2;
+  if (m == 1) {
+    solve7(a, b, cc, dm1, e, f, g, ce, cf, cg, wk1, t->duc, t->wk2, my);
+    for (int j = 1; j <= my; j++) du[j - 1] = t->duc[j].re;
+  } else {
+    if (ias == 1) {
+      for (int j = 1; j <= my; j++) {
+        t->dh[j] = d[j];
+        t->dhm1[j] = dm1[j];
+      }
+      for (int j = 1; j <= my; j++) {
+        t->eh[j] = (j <= my - 6) ? cscal(e[j].re, shp) : e[j];
+        t->fh[j] = (j <= my - 5) ? cscal(f[j].re, shp) : f[j];
+        t->gh[j] = (j <= my - 4) ? cscal(g[j].re, shp) : g[j];
+      }
+      modchol_addshear(a, b, cc, t->dh, t->dhm1, t->eh, t->fh, t->gh, t->ceh, t->cfh,
+                       t->cgh, pr, my);
+    }
+    cplx *x = t->duc;
+    solve7(a, b, cc, t->dhm1, t->eh, t->fh, t->gh, t->ceh, t->cfh, t->cgh, wk1, x,
+           t->wk2, my);
+    for (int j = 1; j <= my; j++) {
+      du[2 * (j - 1)] = x[j].re;
+      du[2 * (j - 1) + 1] = x[j].im;
+    }
+  }
+}
+
+/* lapcdy (diffy_shear_hepta.f90:466-525) */
+static void lapcdy(ctx *c, ythread *t, const double *u, double k2, double *p, cplx shp,
+                   cplx shm, int m) {
+  int my = c->my;
+  for (int d = -3; d <= 3; d++) A7(t->lapmat, d) = A7(c->rh2, d) - k2 * A7(c->pr2, d);
+  modchol7(t->ah, t->bh, t->ch, t->dh, t->dhm1, t->eh, t->fh, t->gh, t->ceh, t->cfh,
+           t->cgh, t->lapmat, my, shp);
+  cplx *uc = t->uc, *ur = t->ur, *wk1 = t->wk1;
+  if (m == 1) {
+    for (int j = 1; j <= my; j++) uc[j] = C(u[j - 1], 0.0);
+    ur[1] = uc[my - 2];
+    ur[2] = uc[my - 1];
+    ur[3] = uc[my];
+    for (int j = 1; j <= my; j++) ur[3 + j] = uc[j];
+    ur[my + 4] = uc[1];
+    ur[my + 5] = uc[2];
+    ur[my + 6] = uc[3];
+  } else {
+    for (int j = 1; j <= my; j++) uc[j] = C(u[2 * (j - 1)], u[2 * (j - 1) + 1]);
+    ur[1] = cmul(uc[my - 2], shm);
+    ur[2] = cmul(uc[my - 1], shm);
+    ur[3] = cmul(uc[my], shm);
+    for (int j = 1; j <= my; j++) ur[3 + j] = uc[j];
+    ur[my + 4] = cmul(uc[1], shp);
+    ur[my + 5] = cmul(uc[2], shp);
+    ur[my + 6] = cmul(uc[3], shp);
+  }
+  for (int j = 4; j <= my + 3; j++) {
+    cplx s = cscal(A7(c->pr2, -3), ur[j - 3]);
+    s = cadd(s, cscal(A7(c->pr2, -2), ur[j - 2]));
+    s = cadd(s, cscal(A7(c->pr2, -1), ur[j - 1]));
+    s = cadd(s, cscal(A7(c->pr2, 0), ur[j]));
+    s = cadd(s, cscal(A7(c->pr2, 1), ur[j + 1]));
+    s = cadd(s, cscal(A7(c->pr2, 2), ur[j + 2]));
+    s = cadd(s, cscal(A7(c->pr2, 3), ur[j + 3]));
+    wk1[j - 3] = s;
+  }
+  cplx *x = t->pc;
+  solve7(t->ah, t->bh, t->ch, t->dhm1, t->eh, t->fh, t->gh, t->ceh, t->cfh, t->cgh, wk1,
+         x, t->wk2, my);
+  if (m == 1) {
+    for (int j = 1; j <= my; j++) p[j - 1] = x[j].re;
+  } else {
+    for (int j = 1; j <= my; j++) {
+      p[2 * (j - 1)] = x[j].re;
+      p[2 * (j - 1) + 1] = x[j].im;
+    }
+  }
+}
+
+/* visc3d (diffy_shear_hepta.f90:298-318), what = '+' */
+static void visc3d(ctx *c, ythread *t, const double *u, double *visc, double *ddu,
+                   cplx shp, cplx shm, int m, double rk, double scal, int ias) {
+  derivyc(c, t, u, ddu, shp, shm, 2, m, ias);
+  int n = m * c->my;
+  for (int q = 0; q < n; q++) visc[q] = visc[q] + scal * (-(rk * u[q]) + ddu[q]);
+}
+
+/* ------------------------------------------------------------------------- */
+/* context setup: initcr.f90:191-216 (sizes), set_xyz_dy (443-519), derivadas */
+/* ------------------------------------------------------------------------- */
+static void ythread_alloc(ythread *t, int my) {
+  t->ah = dalloc(my + 1); t->bh = dalloc(my + 1); t->ch = dalloc(my + 1);
+  t->dh = dalloc(my + 1); t->dhm1 = dalloc(my + 1);
+  t->eh = zalloc(my + 1); t->fh = zalloc(my + 1); t->gh = zalloc(my + 1);
+  t->ceh = zalloc(my + 1); t->cfh = zalloc(my + 1); t->cgh = zalloc(my + 1);
+  t->wk1 = zalloc(my + 1); t->wk2 = zalloc(my + 1); t->ur = zalloc(my + 7);
+  t->uc = zalloc(my + 1); t->duc = zalloc(my + 1); t->pc = zalloc(my + 1);
+}
+static void ythread_free(ythread *t) {
+  free(t->ah); free(t->bh); free(t->ch); free(t->dh); free(t->dhm1);
+  free(t->eh); free(t->fh); free(t->gh); free(t->ceh); free(t->cfh); free(t->cgh);
+  free(t->wk1); free(t->wk2); free(t->ur); free(t->uc); free(t->duc); free(t->pc);
+}
+
+void *orc_create(const orc_params *p) {
+  ctx *c = (ctx *)calloc(1, sizeof(ctx));
+  c->p = *p;
+  c->pi = 4.0 * atan(1.0);
+  c->pi2 = 2.0 * c->pi;
+  c->mgalx = p->mgalx;
+  c->my = p->my;
+  c->mgalz = p->mgalz;
+  c->mx = 2 * (c->mgalx / 3);
+  c->mz = 2 * (c->mgalz / 3) - 1;
+  c->mx1 = c->mx / 2 - 1;
+  c->my1 = c->my - 1;
+  c->mz1 = c->mz - 1;
+  c->mgx = c->mgalx / 2;
+  c->nz = (c->mz - 1) / 2;
+  c->nz1 = c->nz;
+  c->nz2 = c->mgalz - c->nz;
+  c->nkx = c->mx1 + 1;
+  int nkx = c->nkx, mz = c->mz, my = c->my;
+  c->y = dalloc(my);
+  c->xalp_im = dalloc(nkx);
+  c->xgam_im = dalloc(mz);
+  c->alp2 = dalloc(nkx);
+  c->gam2 = dalloc(mz);
+  /* derivadas (diffy_shear_hepta.f90:535-560) */
+  prederiv(c);
+  c->a1 = dalloc(my + 1); c->b1 = dalloc(my + 1); c->c1 = dalloc(my + 1);
+  c->d1 = dalloc(my + 1); c->d1m1 = dalloc(my + 1);
+  c->e1 = zalloc(my + 1); c->f1 = zalloc(my + 1); c->g1 = zalloc(my + 1);
+  c->ce1 = zalloc(my + 1); c->cf1 = zalloc(my + 1); c->cg1 = zalloc(my + 1);
+  c->a2 = dalloc(my + 1); c->b2 = dalloc(my + 1); c->c2 = dalloc(my + 1);
+  c->d2 = dalloc(my + 1); c->d2m1 = dalloc(my + 1);
+  c->e2 = zalloc(my + 1); c->f2 = zalloc(my + 1); c->g2 = zalloc(my + 1);
+  c->ce2 = zalloc(my + 1); c->cf2 = zalloc(my + 1); c->cg2 = zalloc(my + 1);
+  modchol7(c->a1, c->b1, c->c1, c->d1, c->d1m1, c->e1, c->f1, c->g1, c->ce1, c->cf1,
+           c->cg1, c->pr1, my, C(1.0, 0.0));
+  modchol7(c->a2, c->b2, c->c2, c->d2, c->d2m1, c->e2, c->f2, c->g2, c->ce2, c->cf2,
+           c->cg2, c->pr2, my, C(1.0, 0.0));
+  /* set_xyz_dy (initcr.f90:443-519) */
+  double alp = p->alp, gam = p->gam, CFL = p->CFL;
+  c->Lx = c->pi2 / alp;
+  c->Lz = c->pi2 / gam;
+  for (int k = 0; k <= c->nz; k++) c->xgam_im[k] = gam * (double)k;
+  for (int k = c->nz + 1; k <= c->mz1; k++) c->xgam_im[k] = -gam * (double)(mz - k);
+  for (int i = 0; i <= c->mx1; i++) c->xalp_im[i] = alp * (double)i;
+  for (int i = 0; i < nkx; i++) c->alp2[i] = c->xalp_im[i] * c->xalp_im[i];
+  for (int k = 0; k < mz; k++) c->gam2[k] = c->xgam_im[k] * c->xgam_im[k];
+  c->dx = c->pi2 / alp / (double)c->mx;
+  c->dz = c->pi2 / gam / (double)mz;
+  c->dy = p->Ly / (double)my;
+  for (int j = 0; j < my; j++) c->y[j] = (double)j * c->dy - 0.5 * p->Ly;
+  c->cflx = c->pi / CFL / c->dx;
+  c->cflz = c->pi / CFL / c->dz;
+  c->cfly = 2.5 / CFL / c->dy;
+  {
+    double m1 = c->pi * c->pi / c->dx / c->dx, m2 = 6.25 / c->dy / c->dy,
+           m3 = c->pi * c->pi / c->dz / c->dz;
+    double mm = m1 > m2 ? m1 : m2;
+    mm = mm > m3 ? mm : m3;
+    c->cflvv = 1.0 / p->Re / CFL * mm;
+  }
+  /* update_dy (diffy_shear_hepta.f90:562-573) */
+  c->h = c->dy;
+  for (int d = -3; d <= 3; d++) {
+    A7(c->rh1, d) = A7(c->rh1h, d) / c->h;
+    A7(c->rh2, d) = A7(c->rh2h, d) / (c->h * c->h);
+  }
+  plan_init(&c->px, c->mgalx);
+  plan_init(&c->pz, c->mgalz);
+  int nthr = 1;
+#ifdef _OPENMP
+  if (g_threads > 0) omp_set_num_threads(g_threads);
+  nthr = omp_get_max_threads();
+#endif
+  c->nthr = nthr;
+  c->yt = (ythread *)calloc((size_t)nthr, sizeof(ythread));
+  c->pt = (pthread_buf *)calloc((size_t)nthr, sizeof(pthread_buf));
+  size_t np = (size_t)nkx * (size_t)mz;
+  size_t nr = (size_t)(c->mgalx + 2) * (size_t)c->mgalz;
+  for (int t = 0; t < nthr; t++) {
+    ythread_alloc(&c->yt[t], my);
+    pthread_buf *b = &c->pt[t];
+    b->u1c = zalloc(np); b->u2c = zalloc(np); b->u3c = zalloc(np);
+    b->o1c = zalloc(np); b->o2c = zalloc(np); b->o3c = zalloc(np);
+    b->u1r = dalloc(nr); b->u2r = dalloc(nr); b->u3r = dalloc(nr);
+    b->o1r = dalloc(nr); b->o2r = dalloc(nr); b->o3r = dalloc(nr);
+    b->wz = zalloc((size_t)c->mgalz * nkx);
+    int mm = c->mgalx > c->mgalz ? c->mgalx : c->mgalz;
+    b->col = zalloc(mm);
+    b->row = zalloc(mm);
+    b->work = zalloc(mm);
+  }
+  return c;
+}
+
+void orc_destroy(void *h) {
+  ctx *c = (ctx *)h;
+  if (!c) return;
+  for (int t = 0; t < c->nthr; t++) {
+    ythread_free(&c->yt[t]);
+    pthread_buf *b = &c->pt[t];
+    free(b->u1c); free(b->u2c); free(b->u3c); free(b->o1c); free(b->o2c); free(b->o3c);
+    free(b->u1r); free(b->u2r); free(b->u3r); free(b->o1r); free(b->o2r); free(b->o3r);
+    free(b->wz); free(b->col); free(b->row); free(b->work);
+  }
+  free(c->yt);
+  free(c->pt);
+  free(c->y); free(c->xalp_im); free(c->xgam_im); free(c->alp2); free(c->gam2);
+  free(c->a1); free(c->b1); free(c->c1); free(c->d1); free(c->d1m1);
+  free(c->e1); free(c->f1); free(c->g1); free(c->ce1); free(c->cf1); free(c->cg1);
+  free(c->a2); free(c->b2); free(c->c2); free(c->d2); free(c->d2m1);
+  free(c->e2); free(c->f2); free(c->g2); free(c->ce2); free(c->cf2); free(c->cg2);
+  plan_free(&c->px);
+  plan_free(&c->pz);
+  free(c);
+}
+
+void orc_sizes(void *h, int *out) {
+  ctx *c = (ctx *)h;
+  out[0] = c->mx; out[1] = c->mz; out[2] = c->nkx; out[3] = c->my;
+  out[4] = c->nz; out[5] = c->mgalx; out[6] = c->mgalz; out[7] = c->mx * c->mz * c->my;
+}
+
+void orc_coeffs(void *h, double *pr1, double *rh1, double *pr2, double *rh2, double *dy) {
+  ctx *c = (ctx *)h;
+  for (int d = 0; d < 7; d++) {
+    pr1[d] = c->pr1[d]; rh1[d] = c->rh1[d]; pr2[d] = c->pr2[d]; rh2[d] = c->rh2[d];
+  }
+  *dy = c->dy;
+}
+
+void orc_derivyc(void *h, const double *u, double *du, double spr, double spi, double smr,
+                 double smi, int iord, int m) {
+  ctx *c = (ctx *)h;
+  derivyc(c, &c->yt[0], u, du, C(spr, spi), C(smr, smi), iord, m, 1);
+}
+
+void orc_lapcdy(void *h, const double *u, double k2, double *p, double spr, double spi,
+                double smr, double smi, int m) {
+  ctx *c = (ctx *)h;
+  lapcdy(c, &c->yt[0], u, k2, p, C(spr, spi), C(smr, smi), m);
+}
+
+/* ------------------------------------------------------------------------- */
+/* fourxz with fill00/pack00 (fou3D_thread.f:22-161), own 2-D transform       */
+/* ------------------------------------------------------------------------- */
+/* fou: complex (0:mx1, 0:mz1), kx fastest; phys: real (mgalx+2, mgalz) */
+static void fourxz(ctx *c, pthread_buf *b, cplx *fou, double *phys, int iopt) {
+  int nkx = c->nkx, mgalx = c->mgalx, mgalz = c->mgalz, mz = c->mz;
+  int ld = mgalx + 2;
+  cplx *wz = b->wz, *col = b->col, *row = b->row, *work = b->work;
+  if (iopt > 0) {
+    /* fill00 + backward transform along z for the kx columns that are not zero */
+    for (int i = 0; i < nkx; i++) {
+      for (int kg = 0; kg < mgalz; kg++) col[kg] = C(0.0, 0.0);
+      for (int k = 0; k <= c->nz1; k++) col[k] = fou[k * nkx + i];
+      for (int kg = c->nz2; kg < mgalz; kg++) col[kg] = fou[(kg - mgalz + mz) * nkx + i];
+      fft_exec(&c->pz, col, work, +1);
+      for (int z = 0; z < mgalz; z++) wz[z * nkx + i] = col[z];
+    }
+    /* complex-to-real along x: two rows share one complex transform; the
+     * imaginary parts of the kx=0 entries are ignored as in FFTW's c2r */
+    for (int z = 0; z < mgalz; z += 2) {
+      for (int x = 0; x < mgalx; x++) row[x] = C(0.0, 0.0);
+      for (int i = 0; i < nkx; i++) {
+        cplx X1 = wz[z * nkx + i], X2 = wz[(z + 1) * nkx + i];
+        if (i == 0) {
+          X1.im = 0.0;
+          X2.im = 0.0;
+        }
+        row[i] = C(X1.re - X2.im, X1.im + X2.re);
+        if (i > 0) row[mgalx - i] = C(X1.re + X2.im, -X1.im + X2.re);
+      }
+      fft_exec(&c->px, row, work, +1);
+      for (int x = 0; x < mgalx; x++) {
+        phys[z * ld + x] = row[x].re;
+        phys[(z + 1) * ld + x] = row[x].im;
+      }
+      phys[z * ld + mgalx] = 0.0;
+      phys[z * ld + mgalx + 1] = 0.0;
+      phys[(z + 1) * ld + mgalx] = 0.0;
+      phys[(z + 1) * ld + mgalx + 1] = 0.0;
+    }
+  } else {
+    double norm = 1.0 / (double)(mgalx * mgalz);
+    for (int z = 0; z < mgalz; z += 2) {
+      for (int x = 0; x < mgalx; x++) row[x] = C(phys[z * ld + x], phys[(z + 1) * ld + x]);
+      fft_exec(&c->px, row, work, -1);
+      for (int i = 0; i < nkx; i++) {
+        cplx zk = row[i], zm = cconj(row[(mgalx - i) % mgalx]);
+        cplx s = cadd(zk, zm), d = csub(zk, zm);
+        wz[z * nkx + i] = C(0.5 * s.re, 0.5 * s.im);
+        wz[(z + 1) * nkx + i] = C(0.5 * d.im, -0.5 * d.re);
+      }
+    }
+    for (int i = 0; i < nkx; i++) {
+      for (int z = 0; z < mgalz; z++) col[z] = wz[z * nkx + i];
+      fft_exec(&c->pz, col, work, -1);
+      for (int k = 0; k <= c->nz1; k++) fou[k * nkx + i] = cscal(norm, col[k]);
+      for (int kg = c->nz2; kg < mgalz; kg++)
+        fou[(kg - mgalz + mz) * nkx + i] = cscal(norm, col[kg]);
+    }
+  }
+}
+
+void orc_fourxz(void *h, double *fou, double *phys, int iopt) {
+  ctx *c = (ctx *)h;
+  fourxz(c, &c->pt[0], (cplx *)fou, phys, iopt);
+}
+
+/* ------------------------------------------------------------------------- */
+/* cross / hvhg / hist                                                        */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+  double ener[10], ener2[4];
+  double umaxl[4];
+} plane_red;
+
+/* per-line complex pointer into a pencil array: line (i,k) */
+#define PEN(a, i, k) ((a) + 2 * (size_t)my * ((size_t)(k) * (size_t)nkx + (size_t)(i)))
+
+/* hist, flag 'f' (cross.f90:1796-1963): intensities, Pk, eps for plane j */
+static void hist_f(ctx *c, pthread_buf *b, const cplx *dv, double *ener, double *ener2) {
+  int nkx = c->nkx, mz = c->mz;
+  double s = c->p.s;
+  cplx *u1c = b->u1c, *u2c = b->u2c, *u3c = b->u3c, *o1c = b->o1c, *o2c = b->o2c,
+       *o3c = b->o3c;
+#define SUMSQ(X, out)                                                   \
+  {                                                                     \
+    double s0 = 0.0, s1 = 0.0;                                          \
+    for (int k = 0; k < mz; k++) s0 += cabs2(X[k * nkx]);               \
+    for (int k = 0; k < mz; k++)                                        \
+      for (int i = 1; i < nkx; i++) s1 += cabs2(X[k * nkx + i]);        \
+    out = s0 + 2.0 * s1;                                                \
+  }
+#define SUMCJ(X, Y, out)                                                \
+  {                                                                     \
+    double s0 = 0.0, s1 = 0.0;                                          \
+    for (int k = 0; k < mz; k++) s0 += crecj(X[k * nkx], Y[k * nkx]);   \
+    for (int k = 0; k < mz; k++)                                        \
+      for (int i = 1; i < nkx; i++) s1 += crecj(X[k * nkx + i], Y[k * nkx + i]); \
+    out = s0 + 2.0 * s1;                                                \
+  }
+  double up, vp, wp, uvr, uwr, vwr, o1p, o2p, o3p, o12p;
+  SUMSQ(u1c, up);
+  SUMSQ(u2c, vp);
+  SUMSQ(u3c, wp);
+  SUMCJ(u1c, u2c, uvr);
+  SUMCJ(u1c, u3c, uwr);
+  SUMCJ(u2c, u3c, vwr);
+  SUMSQ(o1c, o1p);
+  SUMSQ(o2c, o2p);
+  SUMSQ(o3c, o3p);
+  SUMCJ(o1c, o2c, o12p);
+#undef SUMSQ
+#undef SUMCJ
+  ener[0] += up; ener[1] += vp; ener[2] += wp;
+  ener[3] += uvr; ener[4] += uwr; ener[5] += vwr;
+  ener[6] += o1p; ener[7] += o2p; ener[8] += o3p;
+  /* add shear effect (iadd_mode = 2,3,5) */
+  cplx o3_00 = C(o3c[0].re - s, o3c[0].im);
+  double Pk = -(o3_00.re) * (-uvr) + (o3_00.re * o3_00.re - o3_00.im * o3_00.im) * (1.0 / c->p.Re);
+  ener2[0] += Pk;
+  ener2[1] += o12p;
+  /* dissipation (cross.f90:1926-1944) */
+  double eps = 0.0;
+  {
+    double sa = 0.0, sb = 0.0;
+    for (int k = 0; k < mz; k++)
+      sa += c->gam2[k] * (cabs2(u1c[k * nkx]) + cabs2(u2c[k * nkx]) + cabs2(u3c[k * nkx]));
+    for (int k = 0; k < mz; k++) {
+      cplx o3 = (k == 0) ? o3_00 : o3c[k * nkx];
+      sb += cabs2(dv[k * nkx]) + cabs2(o3);
+    }
+    eps = sa + sb;
+  }
+  for (int k = 0; k < mz; k++) {
+    double s2 = 0.0;
+    for (int i = 1; i < nkx; i++) {
+      int q = k * nkx + i;
+      s2 += (c->alp2[i] + c->gam2[k]) * (cabs2(u1c[q]) + cabs2(u2c[q]) + cabs2(u3c[q])) +
+            cabs2(dv[q]);
+    }
+    eps = eps + 2.0 * s2;
+    cplx x = u2c[k * nkx];
+    cplx cc = cadd(o1c[k * nkx], C(-c->xgam_im[k] * x.im, c->xgam_im[k] * x.re));
+    eps = eps + cabs2(cc);
+    for (int i = 1; i < nkx; i++) {
+      int q = k * nkx + i;
+      x = u2c[q];
+      cc = cadd(o1c[q], C(-c->xgam_im[k] * x.im, c->xgam_im[k] * x.re));
+      eps = eps + 2.0 * cabs2(cc);
+      cc = csub(o3c[q], C(-c->xalp_im[i] * x.im, c->xalp_im[i] * x.re));
+      eps = eps + 2.0 * cabs2(cc);
+    }
+  }
+  ener[9] += eps;
+}
+
+/* hvhg for one plane (cross.f90:1221-1587).  Plane-layout arrays point at
+ * plane j.  Writes the plane's partial reductions into red. */
+static void hvhg_plane(ctx *c, pthread_buf *b, int j, const cplx *phic, const cplx *ome2c,
+                       cplx *rhvc, cplx *rhgc, cplx *ome1c, const double *u00,
+                       const double *w00, const double *rf0u_in, const double *rf0w_in,
+                       double *rf0u_out, double *rf0w_out, int rkstep, int ihist,
+                       plane_red *red) {
+  int nkx = c->nkx, mz = c->mz, mgalx = c->mgalx, mgalz = c->mgalz;
+  int ld = mgalx + 2;
+  double s = c->p.s, chi = c->p.chi;
+  cplx *u1c = b->u1c, *u2c = b->u2c, *u3c = b->u3c, *o1c = b->o1c, *o2c = b->o2c,
+       *o3c = b->o3c;
+  u1c[0] = C(u00[j], 0.0);
+  u3c[0] = C(w00[j], 0.0);
+  o3c[0] = C(-rf0u_in[j], 0.0);
+  o1c[0] = C(rf0w_in[j], 0.0);
+  for (int k = 1; k < mz; k++) {
+    double g = c->xgam_im[k];
+    o3c[k * nkx] = cdiv_imag(cneg(ome1c[k * nkx]), g);
+    o1c[k * nkx] = cdiv_imag(cneg(phic[k * nkx]), g);
+    u3c[k * nkx] = cdiv_imag(cneg(rhvc[k * nkx]), g);
+    u1c[k * nkx] = cdiv_imag(ome2c[k * nkx], g);
+  }
+  for (int k = 0; k < mz; k++) {
+    double g = c->xgam_im[k];
+    for (int i = 1; i < nkx; i++) {
+      double a = c->xalp_im[i];
+      double kkw = c->alp2[i] + c->gam2[k];
+      int q = k * nkx + i;
+      cplx w1 = ome1c[q], ph = phic[q], dv = rhvc[q], o2 = ome2c[q];
+      /* z * (0 + i g) = (-g z.im, g z.re) */
+      cplx t;
+      t = csub(C(-g * w1.im, g * w1.re), C(-a * ph.im, a * ph.re));
+      o3c[q] = cdiv_real(t, kkw);
+      t = cadd(C(-a * w1.im, a * w1.re), C(-g * ph.im, g * ph.re));
+      o1c[q] = cdiv_real(t, kkw);
+      t = cadd(C(-g * dv.im, g * dv.re), C(-a * o2.im, a * o2.re));
+      u3c[q] = cdiv_real(t, kkw);
+      t = csub(C(-a * dv.im, a * dv.re), C(-g * o2.im, g * o2.re));
+      u1c[q] = cdiv_real(t, kkw);
+    }
+  }
+  for (int q = 0; q < nkx * mz; q++) {
+    u2c[q] = rhgc[q];
+    o2c[q] = ome2c[q];
+  }
+  u2c[0] = C(c->p.vbulk, 0.0);
+  if (ihist) hist_f(c, b, rhvc, red->ener, red->ener2);
+  fourxz(c, b, u1c, b->u1r, 1);
+  fourxz(c, b, u2c, b->u2r, 1);
+  fourxz(c, b, u3c, b->u3r, 1);
+  fourxz(c, b, o1c, b->o1r, 1);
+  fourxz(c, b, o2c, b->o2r, 1);
+  fourxz(c, b, o3c, b->o3r, 1);
+  double *u1r = b->u1r, *u2r = b->u2r, *u3r = b->u3r, *o1r = b->o1r, *o2r = b->o2r,
+         *o3r = b->o3r;
+  if (rkstep == 1) {
+    double m0 = red->umaxl[0], m1 = red->umaxl[1], m2 = red->umaxl[2], m3 = red->umaxl[3];
+    double sy = s * c->y[j];
+    for (int z = 0; z < mgalz; z++)
+      for (int x = 0; x < mgalx; x++) {
+        int q = z * ld + x;
+        double a0 = fabs(u1r[q]), a1 = fabs(u1r[q] + sy), a2 = fabs(u2r[q]),
+               a3 = fabs(u3r[q]);
+        if (a0 > m0) m0 = a0;
+        if (a1 > m1) m1 = a1;
+        if (a2 > m2) m2 = a2;
+        if (a3 > m3) m3 = a3;
+      }
+    red->umaxl[0] = m0; red->umaxl[1] = m1; red->umaxl[2] = m2; red->umaxl[3] = m3;
+  }
+  /* u x omega (cross.f90:1453-1462) */
+  double chi2 = 2.0 * chi;
+  for (int z = 0; z < mgalz; z++)
+    for (int x = 0; x < mgalx; x++) {
+      int q = z * ld + x;
+      double tmpx = u2r[q];
+      double h1 = u2r[q] * (o3r[q] + chi2) - u3r[q] * o2r[q];
+      double h2 = u3r[q] * o1r[q] - u1r[q] * (o3r[q] + chi2);
+      double h3 = u1r[q] * o2r[q] - tmpx * o1r[q];
+      u2r[q] = h1;
+      u3r[q] = h2;
+      u1r[q] = h3;
+    }
+  fourxz(c, b, u1c, u1r, -1);
+  fourxz(c, b, u2c, u2r, -1);
+  fourxz(c, b, u3c, u3r, -1);
+  rf0u_out[j] = u2c[0].re;
+  rf0w_out[j] = u1c[0].re;
+  /* iadd_mode = 5 right-hand sides (cross.f90:1536-1546) */
+  for (int k = 0; k < mz; k++) {
+    double g = c->xgam_im[k];
+    for (int i = 0; i < nkx; i++) {
+      double a = c->xalp_im[i];
+      int q = k * nkx + i;
+      cplx H3 = u1c[q], H1 = u2c[q], H2 = u3c[q], v = rhgc[q];
+      ome1c[q] = cadd(C(-a * H1.im, a * H1.re), C(-g * H3.im, g * H3.re));
+      cplx t = csub(H1, cscal(s, v));
+      rhgc[q] = cadd(cneg(C(-a * H3.im, a * H3.re)), C(-g * t.im, g * t.re));
+      rhvc[q] = cneg(cscal(c->alp2[i] + c->gam2[k], H2));
+    }
+  }
+}
+
+static const double GAMA[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};
+static const double ZETA[3] = {-17.0 / 60.0, -5.0 / 12.0, 0.0};
+static const double CA[3] = {8.0 / 15.0, 2.0 / 3.0, 1.0};
+
+/* moving_frame (operators.f90:86-145) on a pencil array */
+static void moving_frame(ctx *c, double *vor, double *phi, double mtime) {
+  int my = c->my, nkx = c->nkx, mz = c->mz;
+  cplx *sydt = zalloc((size_t)my * nkx);
+  for (int i = 0; i < nkx; i++)
+    for (int j = 0; j < my; j++) {
+      double th = (c->xalp_im[i] * c->y[j]) * mtime;
+      sydt[i * my + j] = C(cos(th), sin(th));
+    }
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < mz; k++)
+    for (int i = 0; i < nkx; i++) {
+      cplx *v = (cplx *)PEN(vor, i, k), *p = (cplx *)PEN(phi, i, k);
+      for (int j = 0; j < my; j++) {
+        v[j] = cmul(v[j], sydt[i * my + j]);
+        p[j] = cmul(p[j], sydt[i * my + j]);
+      }
+    }
+  free(sydt);
+}
+
+/* set_conj (operators.f90:1382-1429) applied to pencil arrays */
+static void set_conj_pencil(ctx *c, double *vor, double *phi) {
+  int my = c->my, nkx = c->nkx;
+  for (int k = c->nz + 1; k <= c->mz1; k++) {
+    cplx *dst = (cplx *)PEN(vor, 0, k), *src = (cplx *)PEN(vor, 0, c->mz - k);
+    for (int j = 0; j < my; j++) dst[j] = cconj(src[j]);
+    dst = (cplx *)PEN(phi, 0, k);
+    src = (cplx *)PEN(phi, 0, c->mz - k);
+    for (int j = 0; j < my; j++) dst[j] = cconj(src[j]);
+  }
+}
+
+/* pencil (j,i,k) -> plane (i,k,j) and back (the local part of
+ * chjik2ikj / chikj2jik, change.allfac_ieor.f:80-87,117-124) */
+static void to_plane(ctx *c, const double *pen, cplx *pl) {
+  int my = c->my, nkx = c->nkx, mz = c->mz;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < mz; k++)
+    for (int i = 0; i < nkx; i++) {
+      const cplx *l = (const cplx *)PEN(pen, i, k);
+      for (int j = 0; j < my; j++) pl[((size_t)j * mz + k) * nkx + i] = l[j];
+    }
+}
+static void to_pencil(ctx *c, const cplx *pl, double *pen) {
+  int my = c->my, nkx = c->nkx, mz = c->mz;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < mz; k++)
+    for (int i = 0; i < nkx; i++) {
+      cplx *l = (cplx *)PEN(pen, i, k);
+      for (int j = 0; j < my; j++) l[j] = pl[((size_t)j * mz + k) * nkx + i];
+    }
+}
+
+int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, double *ptime,
+              double *pxoffb, double *pxofft, int nstep, double *trace, int *ntrace,
+              int *pistop, double *pdeltat) {
+  ctx *c = (ctx *)h;
+  int my = c->my, nkx = c->nkx, mz = c->mz, mx1 = c->mx1;
+  size_t nfield = 2 * (size_t)my * nkx * mz; /* doubles per pencil field */
+  size_t nplane = (size_t)nkx * mz;
+  double s = c->p.s, Ly = c->p.Ly, Re = c->p.Re;
+  double time = *ptime, xoffb = *pxoffb, xofft = *pxofft;
+  double etime = c->p.etime > 0 ? c->p.etime : 1e10;
+  double dumptime = c->p.dumptime > 0 ? c->p.dumptime : 1e10;
+  double dtimag = c->p.dtimag > 0 ? c->p.dtimag : etime;
+  double Deltat = *pdeltat;
+  int nhist = c->p.nhist > 0 ? c->p.nhist : 1;
+  double *hv = dalloc(nfield), *hg = dalloc(nfield), *dvordy = dalloc(nfield);
+  double *vorwk = dalloc(nfield), *phiwk = dalloc(nfield);
+  double *ddu = dalloc(nfield);
+  cplx *b1 = zalloc(nplane * my), *b2 = zalloc(nplane * my), *phv = zalloc(nplane * my),
+       *phg = zalloc(nplane * my), *pdv = zalloc(nplane * my);
+  double *rf0u = dalloc(my), *rf0w = dalloc(my), *u00wk = dalloc(my), *w00wk = dalloc(my);
+  double *rf0u_d = dalloc(my), *rf0w_d = dalloc(my), *wk1dr = dalloc(my);
+  plane_red *red = (plane_red *)calloc((size_t)my, sizeof(plane_red));
+  cplx *shb = zalloc(nkx), *sht = zalloc(nkx), *shwkb = zalloc(nkx), *shwkt = zalloc(nkx);
+  for (int i = 0; i < nkx; i++) {
+    shb[i] = sht[i] = shwkb[i] = shwkt[i] = C(1.0, 0.0);
+  }
+  double xwkb = xoffb, xwkt = xofft;
+  int istop = 0, idump = 0, irun = 0, ihist = 1, nt = 0, done = 0;
+  double umax[4] = {0, 0, 0, 0}, CFL = c->p.CFL, CFLv = 0.0;
+  /* entry: set_conj on the state (cross.f90:283-287) */
+  set_conj_pencil(c, vor, phi);
+  for (int istep = 1; istep <= nstep; istep++) {
+    if ((istep - 1) % nhist == 0) ihist = 1;
+    xwkt = xofft;
+    xwkb = xoffb;
+    if ((istep - 1) != 1) {
+      if (istop == 1 || idump == 1) {
+        if (istop == 1) break;
+        idump = 0;
+      }
+    }
+    double u00b = s * (-Ly), u00t = s * Ly;
+    if (fabs(s) > 0.001) {
+      for (int i = 0; i <= mx1; i++) {
+        double a = c->xalp_im[i];
+        shb[i] = C(cos((-a) * xwkb), sin((-a) * xwkb));
+        sht[i] = C(cos((-a) * xwkt), sin((-a) * xwkt));
+      }
+      for (int i = 0; i <= mx1; i++) {
+        shwkt[i] = sht[i];
+        shwkb[i] = shb[i];
+      }
+    }
+    if (irun == 0) {
+      irun = 1;
+#pragma omp parallel for schedule(static)
+      for (int ik = 0; ik < nkx * mz; ik++) {
+        int i = ik % nkx, k = ik / nkx;
+        if (i != 0 || k != 0) {
+          double rk = c->gam2[k] + c->alp2[i];
+          lapcdy(c, &c->yt[my_thread()], PEN(phi, i, k), rk, PEN(hg, i, k), sht[i], shb[i], 2);
+        }
+      }
+    }
+    for (int rkstep = 1; rkstep <= 3; rkstep++) {
+#pragma omp parallel for schedule(static)
+      for (int ik = 0; ik < nkx * mz; ik++) {
+        int i = ik % nkx, k = ik / nkx;
+        ythread *t = &c->yt[my_thread()];
+        derivyc(c, t, PEN(vor, i, k), PEN(dvordy, i, k), shwkt[i], shwkb[i], 1, 2, 1);
+        derivyc(c, t, PEN(hg, i, k), PEN(hv, i, k), shwkt[i], shwkb[i], 1, 2, 0);
+      }
+      to_plane(c, phi, b1);
+      to_plane(c, vor, b2);
+      /* set_conj on the copies (cross.f90:502) */
+      for (int j = 0; j < my; j++)
+        for (int k = c->nz + 1; k <= c->mz1; k++) {
+          b2[(size_t)j * nplane + (size_t)k * nkx] = cconj(b2[(size_t)j * nplane + (size_t)(mz - k) * nkx]);
+          b1[(size_t)j * nplane + (size_t)k * nkx] = cconj(b1[(size_t)j * nplane + (size_t)(mz - k) * nkx]);
+        }
+      to_plane(c, hv, phv);
+      to_plane(c, hg, phg);
+      to_plane(c, dvordy, pdv);
+      /* ---- hvhg ---- */
+      {
+        cplx one = C(1.0, 0.0);
+        derivyc(c, &c->yt[0], u00, rf0u_d, one, one, 1, 1, 0);
+        derivyc(c, &c->yt[0], w00, rf0w_d, one, one, 1, 1, 0);
+        double uinit = 0.0;
+        if (istep == 1 && c->p.readflag == 0) uinit = (fabs(s) > 0.5) ? 1.0 : c->p.uprim;
+        for (int j = 0; j < my; j++) {
+          memset(&red[j], 0, sizeof(plane_red));
+        }
+#pragma omp parallel for schedule(static)
+        for (int j = 0; j < my; j++) {
+          pthread_buf *bb = &c->pt[my_thread()];
+          hvhg_plane(c, bb, j, b1 + (size_t)j * nplane, b2 + (size_t)j * nplane,
+                     phv + (size_t)j * nplane, phg + (size_t)j * nplane,
+                     pdv + (size_t)j * nplane, u00, w00, rf0u_d, rf0w_d, rf0u, rf0w, rkstep,
+                     ihist, &red[j]);
+        }
+        if (rkstep == 1) {
+          double ul[4] = {uinit, uinit, uinit, uinit};
+          for (int j = 0; j < my; j++)
+            for (int q = 0; q < 4; q++)
+              if (red[j].umaxl[q] > ul[q]) ul[q] = red[j].umaxl[q];
+          for (int q = 0; q < 4; q++) umax[q] = ul[q];
+          double dt;
+          if (c->p.fixed_dt > 0.0) {
+            dt = c->p.fixed_dt;
+            double m1 = umax[0] * c->pi / c->dx, m2 = umax[2] * 2.5 / c->dy,
+                   m3 = umax[3] * c->pi / c->dz;
+            double mm = m1 > m2 ? m1 : m2;
+            mm = mm > m3 ? mm : m3;
+            CFL = dt * mm;
+            double v1 = c->pi * c->pi / c->dx / c->dx, v2 = 6.25 / c->dy / c->dy,
+                   v3 = c->pi * c->pi / c->dz / c->dz;
+            double vv = v1 > v2 ? v1 : v2;
+            vv = vv > v3 ? vv : v3;
+            CFLv = (1.0 / Re) * dt * vv;
+          } else {
+            double m1 = umax[0] * c->cflx, m2 = umax[2] * c->cfly, m3 = umax[3] * c->cflz;
+            double mm = m1 > m2 ? m1 : m2;
+            mm = mm > m3 ? mm : m3;
+            dt = 1.0 / mm;
+            CFLv = CFL * c->cflvv * dt;
+            if (CFLv > CFL) dt = 1.0 / c->cflvv;
+          }
+          Deltat = dt;
+          if (Deltat < 1e-10) istop = 1;
+          if ((time + Deltat) > dumptime) {
+            Deltat = fabs(dumptime - time);
+            if (dumptime > (etime - 1e-13)) istop = 1;
+            dumptime = dumptime + dtimag;
+            idump = 1;
+          } else if ((time + Deltat) > etime) {
+            Deltat = fabs(etime - time);
+            istop = 1;
+          }
+        }
+        if (ihist) {
+          /* hist 'w' (cross.f90:2064-2118) */
+          double ener[10] = {0}, ener2[4] = {0};
+          for (int j = 0; j < my; j++) {
+            for (int q = 0; q < 10; q++) ener[q] += red[j].ener[q];
+            for (int q = 0; q < 4; q++) ener2[q] += red[j].ener2[q];
+          }
+          double uner[10], uner2[4];
+          for (int q = 0; q < 3; q++) uner[q] = sqrt(fabs(ener[q] / (double)my));
+          for (int q = 3; q < 6; q++) uner[q] = ener[q] / (double)my;
+          for (int q = 6; q < 9; q++) uner[q] = sqrt(fabs(ener[q] / (double)my));
+          uner[9] = ener[9] / (double)my;
+          for (int q = 0; q < 4; q++) uner2[q] = ener2[q] / (double)my;
+          if (trace) {
+            double *r = trace + (size_t)nt * ORC_TRACE_LEN;
+            r[0] = time; r[1] = Deltat;
+            for (int q = 0; q < 10; q++) r[2 + q] = uner[q];
+            r[12] = CFL; r[13] = CFLv;
+            r[14] = umax[1]; r[15] = umax[2]; r[16] = umax[3];
+            r[17] = xoffb; r[18] = xofft; r[19] = umax[0];
+            for (int q = 0; q < 4; q++) r[20 + q] = uner2[q];
+          }
+          nt++;
+          if (isnan(uner[0])) istop = 1;
+          if (uner[1] / c->Lz < 1e-5) istop = 1;
+          ihist = 0;
+        }
+      }
+      to_pencil(c, phv, hv);
+      to_pencil(c, phg, hg);
+      to_pencil(c, pdv, dvordy);
+#pragma omp parallel for schedule(static)
+      for (int ik = 0; ik < nkx * mz; ik++) {
+        int i = ik % nkx, k = ik / nkx;
+        ythread *t = &c->yt[my_thread()];
+        derivyc(c, t, PEN(dvordy, i, k), PEN(dvordy, i, k), shwkt[i], shwkb[i], 1, 2, 1);
+      }
+      for (size_t q = 0; q < nfield; q++) hv[q] = hv[q] - dvordy[q];
+      double r1 = CA[rkstep - 1] * Deltat;
+      double fac = 1.0 / Re;
+#pragma omp parallel for schedule(static)
+      for (int ik = 0; ik < nkx * mz; ik++) {
+        int i = ik % nkx, k = ik / nkx;
+        if (i != 0 || k != 0) {
+          ythread *t = &c->yt[my_thread()];
+          double rk = c->gam2[k] + c->alp2[i];
+          double *scr = ddu + 2 * (size_t)my * ik;
+          visc3d(c, t, PEN(vor, i, k), PEN(hg, i, k), scr, shwkt[i], shwkb[i], 2, rk, fac, 1);
+          visc3d(c, t, PEN(phi, i, k), PEN(hv, i, k), scr, shwkt[i], shwkb[i], 2, rk, fac, 0);
+        }
+      }
+      {
+        cplx one = C(1.0, 0.0);
+        visc3d(c, &c->yt[0], u00, rf0u, wk1dr, one, one, 1, 0.0, fac, 0);
+        visc3d(c, &c->yt[0], w00, rf0w, wk1dr, one, one, 1, 0.0, fac, 0);
+      }
+      double gk = GAMA[rkstep - 1];
+      if (rkstep == 1) {
+        for (size_t q = 0; q < nfield; q++) {
+          vorwk[q] = gk * hg[q];
+          phiwk[q] = gk * hv[q];
+        }
+        for (int j = 0; j < my; j++) {
+          u00wk[j] = gk * rf0u[j];
+          w00wk[j] = gk * rf0w[j];
+        }
+      } else {
+        for (size_t q = 0; q < nfield; q++) {
+          vorwk[q] = vorwk[q] + gk * hg[q];
+          phiwk[q] = phiwk[q] + gk * hv[q];
+        }
+        for (int j = 0; j < my; j++) {
+          u00wk[j] = u00wk[j] + gk * rf0u[j];
+          w00wk[j] = w00wk[j] + gk * rf0w[j];
+        }
+      }
+      for (size_t q = 0; q < nfield; q++) {
+        vor[q] = vor[q] + Deltat * vorwk[q];
+        phi[q] = phi[q] + Deltat * phiwk[q];
+      }
+      for (int j = 0; j < my; j++) {
+        u00[j] = u00[j] + Deltat * u00wk[j];
+        w00[j] = w00[j] + Deltat * w00wk[j];
+      }
+      if (fabs(s) > 0.01) {
+        xwkb = xoffb + r1 * u00b;
+        xwkt = xofft + r1 * u00t;
+        for (int i = 0; i <= mx1; i++) {
+          double a = c->xalp_im[i];
+          shwkb[i] = C(cos((-a) * xwkb), sin((-a) * xwkb));
+          shwkt[i] = C(cos((-a) * xwkt), sin((-a) * xwkt));
+        }
+      }
+      double zk = ZETA[rkstep - 1];
+      if (rkstep != 3) {
+        for (size_t q = 0; q < nfield; q++) {
+          phiwk[q] = hv[q] * zk;
+          vorwk[q] = hg[q] * zk;
+        }
+        double mf = (rkstep == 1) ? -(GAMA[0] * Deltat * s)
+                                  : -((GAMA[1] + ZETA[0]) * Deltat * s);
+        moving_frame(c, vorwk, phiwk, mf);
+        for (int j = 0; j < my; j++) {
+          u00wk[j] = rf0u[j] * zk;
+          w00wk[j] = rf0w[j] * zk;
+        }
+      }
+      {
+        double mf = (rkstep == 1) ? -(s * r1) : -(s * (CA[rkstep - 1] - CA[rkstep - 2]) * Deltat);
+        moving_frame(c, vor, phi, mf);
+      }
+#pragma omp parallel for schedule(static)
+      for (int ik = 0; ik < nkx * mz; ik++) {
+        int i = ik % nkx, k = ik / nkx;
+        if (i != 0 || k != 0) {
+          double rk = c->gam2[k] + c->alp2[i];
+          lapcdy(c, &c->yt[my_thread()], PEN(phi, i, k), rk, PEN(hg, i, k), shwkt[i],
+                 shwkb[i], 2);
+        }
+      }
+    }
+    xoffb = xwkb;
+    xofft = xwkt;
+    for (int i = 0; i < nkx; i++) {
+      sht[i] = shwkt[i];
+      shb[i] = shwkb[i];
+    }
+    time = time + Deltat;
+    done++;
+  }
+  *ptime = time;
+  *pxoffb = xoffb;
+  *pxofft = xofft;
+  *pistop = istop;
+  *pdeltat = Deltat;
+  if (ntrace) *ntrace = nt;
+  free(hv); free(hg); free(dvordy); free(vorwk); free(phiwk); free(ddu);
+  free(b1); free(b2); free(phv); free(phg); free(pdv);
+  free(rf0u); free(rf0w); free(u00wk); free(w00wk); free(rf0u_d); free(rf0w_d); free(wk1dr);
+  free(red); free(shb); free(sht); free(shwkb); free(shwkt);
+  return done;
+}

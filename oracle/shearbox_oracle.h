@@ -1,0 +1,72 @@
+/*
+ * shearbox_oracle.h -- CPU FP64 restatement of the shearing-box RK3 time step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This oracle exists so that tests/, the smoke check
+ * and the CPU-baseline leg of bench.py can check the CUDA library against the
+ * reference algorithm.  The product (shear_nnf_gb300/) never links, imports or
+ * calls it.
+ *
+ * Parity status: the reference (Fortran + FFTW + MPI) cannot be compiled in this
+ * environment and ships no golden vectors, so the oracle is pinned against the
+ * reference's own analytic checks instead: the rapid-distortion (RDT) solution
+ * rdtfunc (operators.f90:1516-1562, the check recorded in log_changes for
+ * rev.428-430), the design conditions of the compact schemes (prederiv1/2), and
+ * numpy's DFT for the x/z transforms.  It is not pinned to reference binary
+ * outputs.
+ *
+ * Layouts follow the reference exactly:
+ *   pencil   vor(0:2*my-1, 0:mx1, 0:mz1)  real, i.e. complex(0:my1,0:mx1,0:mz1),
+ *            y fastest (cross.f90:32-33);
+ *   plane    complex(0:mx1, 0:mz1, 0:my1), kx fastest (cross.f90:1144).
+ */
+#ifndef SHEARBOX_ORACLE_H
+#define SHEARBOX_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_params {
+  int mgalx, my, mgalz;   /* physical grid (hre2.dat record 1) */
+  double Re, alp, Ly, gam, s, chi, CFL; /* hre2.dat record 2 (Ly read directly) */
+  double vbulk;           /* u2c(0,0) override in hvhg (cross.f90:1276) */
+  double fixed_dt;        /* >0: fixed time step (ifix_dt branch, cross.f90:1608) */
+  int readflag;           /* 0: initial umax from s/uprim on the first step (cross.f90:1208) */
+  double uprim;           /* hre2.dat record 4 */
+  int nhist;              /* statistics every nhist steps (cross.f90:344) */
+  double etime, dumptime, dtimag; /* end/dump times (cross.f90:1694-1711) */
+} orc_params;
+
+/* one .cfbin record per statistics step (cross.f90:2087):
+ * time, Deltat, uner(1:10), CFL, CFLv, umax(1:3), xoffb, xofft, umax(0), uner2(1:4) */
+#define ORC_TRACE_LEN 24
+
+void *orc_create(const orc_params *p);
+void orc_destroy(void *h);
+/* out[0..7] = mx, mz, nkx(=mx/2), my, nz, mgalx, mgalz, buffsize(=mx*mz*my) */
+void orc_sizes(void *h, int *out);
+void orc_coeffs(void *h, double *pr1, double *rh1, double *pr2, double *rh2,
+                double *dy);
+void orc_set_threads(int n);
+
+/* cross(): nstep RK3 steps in place on pencil-layout arrays.  trace receives up
+ * to nstep records; *ntrace the count; *istop the stop flag; *deltat the last
+ * Deltat.  Returns the number of completed steps. */
+int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00,
+              double *time, double *xoffb, double *xofft, int nstep,
+              double *trace, int *ntrace, int *istop, double *deltat);
+
+/* building blocks, one y-line (complex: m=2, real: m=1) */
+void orc_derivyc(void *h, const double *u, double *du, double shp_re,
+                 double shp_im, double shm_re, double shm_im, int iord, int m);
+void orc_lapcdy(void *h, const double *u, double k2, double *p, double shp_re,
+                double shp_im, double shm_re, double shm_im, int m);
+/* one plane: iopt=+1 fou(complex 0:mx1,0:mz1) -> phys((mgalx+2) x mgalz);
+ *            iopt=-1 phys -> fou */
+void orc_fourxz(void *h, double *fou, double *phys, int iopt);
+/* plain complex FFT of length n (sign -1 forward, +1 backward, unnormalised) */
+void orc_fft(int n, double *data, int sign);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,229 @@
+"""GB300 shearing-box RK3 time stepper (Python host over the C-ABI).
+
+The product is the CUDA library ``_build/libshearbox.so`` with the C interface
+of ``include/shearbox.h``; this module is a thin ctypes host that mirrors the
+reference's ``cross`` interface (cross.f90:3-4): state in the reference pencil
+layout (complex (mz, nkx, my), y fastest), parameters of hre2.dat, and the
+``.cfbin`` statistics record.  There is no CPU fallback: importing works
+without a GPU, but creating a ``ShearBox`` fails loudly if the CUDA library or
+a GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .buildlib import LIB, build
+
+TRACE_LEN = 24
+TRACE_FIELDS = (
+    ["time", "Deltat"] + [f"uner{q}" for q in range(1, 11)] + ["CFL", "CFLv", "umax1", "umax2",
+    "umax3", "xoffb", "xofft", "umax0"] + [f"uner2_{q}" for q in range(1, 5)]
+)
+SB_FP64 = 0
+
+
+class SbParams(ctypes.Structure):
+    _fields_ = [
+        ("mgalx", ctypes.c_int), ("my", ctypes.c_int), ("mgalz", ctypes.c_int),
+        ("Re", ctypes.c_double), ("alp", ctypes.c_double), ("Ly", ctypes.c_double),
+        ("gam", ctypes.c_double), ("s", ctypes.c_double), ("chi", ctypes.c_double),
+        ("CFL", ctypes.c_double), ("vbulk", ctypes.c_double), ("fixed_dt", ctypes.c_double),
+        ("readflag", ctypes.c_int), ("uprim", ctypes.c_double), ("nhist", ctypes.c_int),
+        ("etime", ctypes.c_double), ("dumptime", ctypes.c_double), ("dtimag", ctypes.c_double),
+    ]
+
+
+class SbStatus(ctypes.Structure):
+    _fields_ = [
+        ("istop", ctypes.c_int), ("steps_done", ctypes.c_int), ("ntrace", ctypes.c_int),
+        ("flags", ctypes.c_int), ("time", ctypes.c_double), ("deltat", ctypes.c_double),
+        ("xoffb", ctypes.c_double), ("xofft", ctypes.c_double), ("cfl", ctypes.c_double),
+        ("cflv", ctypes.c_double),
+    ]
+
+
+ABI_FUNCTIONS = [
+    "sb_create", "sb_destroy", "sb_set_member_re", "sb_set_state", "sb_get_state", "sb_step",
+    "sb_get_status", "sb_get_trace", "sb_cross", "sb_get_stream", "sb_sync", "sb_sizes",
+    "sb_seed_state", "sb_compact_coeffs", "sb_last_error", "sb_version",
+]
+
+_lib = None
+
+
+def lib(auto_build: bool = False):
+    """Load the CUDA library (building it first only if asked)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if auto_build:
+        build()
+    if not os.path.exists(LIB):
+        raise RuntimeError(f"CUDA library {LIB} is missing: run __graft_entry__.build()")
+    L = ctypes.CDLL(LIB)
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    vp = ctypes.c_void_p
+    PP = ctypes.POINTER(SbParams)
+    L.sb_create.argtypes = [PP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+    L.sb_destroy.argtypes = [vp]
+    L.sb_set_member_re.argtypes = [vp, ctypes.c_int, ctypes.c_double]
+    L.sb_set_state.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp, ctypes.c_double, ctypes.c_double,
+                               ctypes.c_double]
+    L.sb_get_state.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp]
+    L.sb_step.argtypes = [vp, ctypes.c_int]
+    L.sb_get_status.argtypes = [vp, ctypes.c_int, ctypes.POINTER(SbStatus)]
+    L.sb_get_trace.argtypes = [vp, ctypes.c_int, dp, ctypes.c_int, ip]
+    L.sb_cross.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int, ctypes.POINTER(SbStatus)]
+    L.sb_get_stream.restype = vp
+    L.sb_get_stream.argtypes = [vp]
+    L.sb_sync.argtypes = [vp]
+    L.sb_sizes.argtypes = [PP, ip]
+    L.sb_seed_state.argtypes = [PP, ctypes.c_ulonglong, ctypes.c_double, ctypes.c_double, dp, dp,
+                                dp, dp]
+    L.sb_compact_coeffs.argtypes = [dp, dp, dp, dp]
+    L.sb_last_error.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+class ShearBoxError(RuntimeError):
+    pass
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise ShearBoxError(f"shearbox error {rc}: {lib().sb_last_error().decode()}")
+
+
+def _dp(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def make_params(mgalx, my, mgalz, Re, alp, Ly, gam, s=1.0, chi=0.0, CFL=0.5, vbulk=0.0,
+                fixed_dt=0.0, readflag=1, uprim=1.0, nhist=1, etime=1e10, dumptime=1e10,
+                dtimag=1e10) -> SbParams:
+    return SbParams(mgalx, my, mgalz, Re, alp, Ly, gam, s, chi, CFL, vbulk, fixed_dt, readflag,
+                    uprim, nhist, etime, dumptime, dtimag)
+
+
+def sizes(p: SbParams) -> dict:
+    out = (ctypes.c_int * 8)()
+    _check(lib().sb_sizes(ctypes.byref(p), out))
+    keys = ["mx", "mz", "nkx", "my", "nz", "mgalx", "mgalz", "n"]
+    return dict(zip(keys, list(out)))
+
+
+def seed_state(p: SbParams, seed: int, k0: float = 4.0, urms: float = None) -> dict:
+    """Seeded divergence-free initial field (pencil layout, complex128)."""
+    sz = sizes(p)
+    if urms is None:
+        urms = 0.1 * 1.0 * (2 * np.pi / p.gam)  # 0.1 * S * Lz
+    vor = np.zeros((sz["mz"], sz["nkx"], p.my), np.complex128)
+    phi = np.zeros_like(vor)
+    u00 = np.zeros(p.my)
+    w00 = np.zeros(p.my)
+    _check(lib().sb_seed_state(ctypes.byref(p), int(seed), float(k0), float(urms),
+                               _dp(vor.view(np.float64)), _dp(phi.view(np.float64)), _dp(u00),
+                               _dp(w00)))
+    return {"vor": vor, "phi": phi, "u00": u00, "w00": w00, "time": 0.0, "xoffb": 0.0,
+            "xofft": 0.0}
+
+
+def compact_coeffs():
+    a = [np.zeros(7) for _ in range(4)]
+    _check(lib().sb_compact_coeffs(*[_dp(x) for x in a]))
+    return tuple(a)
+
+
+class ShearBox:
+    """A batch of shearing boxes resident on the GPU."""
+
+    def __init__(self, p: SbParams, batch: int = 1, precision: int = SB_FP64):
+        self.p = p
+        self.batch = batch
+        self.sz = sizes(p)
+        h = ctypes.c_void_p()
+        _check(lib().sb_create(ctypes.byref(p), int(batch), int(precision), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            lib().sb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return int(lib().sb_get_stream(self.h) or 0)
+
+    def set_re(self, member: int, Re: float):
+        _check(lib().sb_set_member_re(self.h, member, float(Re)))
+
+    def set_state(self, state: dict, member: int = 0):
+        vor = np.ascontiguousarray(state["vor"], np.complex128)
+        phi = np.ascontiguousarray(state["phi"], np.complex128)
+        u00 = np.ascontiguousarray(state["u00"], np.float64)
+        w00 = np.ascontiguousarray(state["w00"], np.float64)
+        _check(lib().sb_set_state(self.h, member, _dp(vor.view(np.float64)),
+                                  _dp(phi.view(np.float64)), _dp(u00), _dp(w00),
+                                  float(state["time"]), float(state["xoffb"]),
+                                  float(state["xofft"])))
+
+    def get_state(self, member: int = 0) -> dict:
+        vor = np.zeros((self.sz["mz"], self.sz["nkx"], self.p.my), np.complex128)
+        phi = np.zeros_like(vor)
+        u00 = np.zeros(self.p.my)
+        w00 = np.zeros(self.p.my)
+        t = ctypes.c_double()
+        xb = ctypes.c_double()
+        xt = ctypes.c_double()
+        _check(lib().sb_get_state(self.h, member, _dp(vor.view(np.float64)),
+                                  _dp(phi.view(np.float64)), _dp(u00), _dp(w00), ctypes.byref(t),
+                                  ctypes.byref(xb), ctypes.byref(xt)))
+        return {"vor": vor, "phi": phi, "u00": u00, "w00": w00, "time": t.value,
+                "xoffb": xb.value, "xofft": xt.value}
+
+    def step(self, nsteps: int):
+        _check(lib().sb_step(self.h, int(nsteps)))
+
+    def sync(self):
+        _check(lib().sb_sync(self.h))
+
+    def status(self, member: int = 0) -> SbStatus:
+        st = SbStatus()
+        _check(lib().sb_get_status(self.h, member, ctypes.byref(st)))
+        return st
+
+    def trace(self, member: int = 0, max_records: int = 1 << 16) -> np.ndarray:
+        n = ctypes.c_int()
+        st = self.status(member)
+        m = min(max_records, max(st.ntrace, 0))
+        out = np.zeros((max(m, 1), TRACE_LEN))
+        _check(lib().sb_get_trace(self.h, member, _dp(out), m, ctypes.byref(n)))
+        return out[: n.value]
+
+    def cross(self, state: dict, nstep: int) -> tuple:
+        """Drop-in for the reference ``cross``: advances box 0 by nstep steps in
+        place on host arrays; returns (trace, status)."""
+        for key in ("vor", "phi"):
+            assert state[key].dtype == np.complex128 and state[key].flags["C_CONTIGUOUS"]
+        t = ctypes.c_double(state["time"])
+        xb = ctypes.c_double(state["xoffb"])
+        xt = ctypes.c_double(state["xofft"])
+        st = SbStatus()
+        _check(lib().sb_cross(self.h, _dp(state["vor"].view(np.float64)),
+                              _dp(state["phi"].view(np.float64)), _dp(state["u00"]),
+                              _dp(state["w00"]), ctypes.byref(t), ctypes.byref(xb),
+                              ctypes.byref(xt), int(nstep), ctypes.byref(st)))
+        state["time"], state["xoffb"], state["xofft"] = t.value, xb.value, xt.value
+        return self.trace(0), st

@@ -1,0 +1,513 @@
+// sb_api.cu -- C-ABI of the shearing-box time stepper (see include/shearbox.h).
+//
+// Host side of the step: owns the device state of a batch of boxes, uploads
+// the factor tables computed by sb_host.cpp, captures one RK3 step (sixteen
+// kernel launches) in a CUDA graph and replays it.  The reference's MPI/OpenMP
+// structure (cross.f90 with change.allfac_ieor.f transposes) has no
+// counterpart: one handle is one GPU, one stream.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstddef>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/shearbox.h"
+#include "sb_common.cuh"
+#include "sb_host.h"
+#include "sb_kernels.h"
+
+using namespace sb;
+
+static thread_local std::string g_err;
+static int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+#define CK(x)                                                                      \
+  do {                                                                             \
+    cudaError_t e_ = (x);                                                          \
+    if (e_ != cudaSuccess)                                                         \
+      return fail(3, "%s failed: %s (%s:%d)", #x, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+struct sb_handle {
+  sb_params p;
+  int precision;
+  Grid g;
+  Bufs bf;
+  cudaStream_t st = nullptr;
+  cudaGraphExec_t step_exec = nullptr;
+  std::vector<void *> allocs;
+  double *d_pen = nullptr;  // staging buffer, one pencil-layout field
+  int trace_cap = 0;
+  std::vector<Member> mem_init;
+};
+
+static int dalloc(sb_handle *h, double **p, size_t n) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, sizeof(double) * (n ? n : 1));
+  if (e != cudaSuccess) return fail(4, "cudaMalloc(%zu doubles): %s", n, cudaGetErrorString(e));
+  cudaMemset(q, 0, sizeof(double) * (n ? n : 1));
+  h->allocs.push_back(q);
+  *p = (double *)q;
+  return 0;
+}
+static int upload(sb_handle *h, const double **dst, const std::vector<double> &v) {
+  double *p;
+  int rc = dalloc(h, &p, v.size());
+  if (rc) return rc;
+  CK(cudaMemcpy(p, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice));
+  *dst = p;
+  return 0;
+}
+
+static int check_params(const sb_params *p) {
+  if (!p) return fail(1, "null parameters");
+  if (p->mgalx <= 0 || p->my <= 0 || p->mgalz <= 0)
+    return fail(1, "mgalx grid error %d %d %d", p->mgalx, p->my, p->mgalz);  // initcr.f90:188
+  if (!supported_grid(p->mgalx, p->mgalz))
+    return fail(1, "unsupported x/z grid %d x %d (transform lengths 32,48,64,96,192[,384])",
+                p->mgalx, p->mgalz);
+  if (p->mgalz % 2) return fail(1, "mgalz must be even");
+  if (p->my < 16 || p->my > SB_MAX_NY) return fail(1, "my=%d outside 16..%d", p->my, SB_MAX_NY);
+  if (!(p->Re != 0.0) || !(p->alp > 0) || !(p->gam > 0) || !(p->Ly > 0) || !(p->CFL > 0))
+    return fail(1, "invalid physical parameters");
+  return 0;
+}
+
+// factor tables of one band matrix, same for every line
+static int upload_uniform(sb_handle *h, Fac *F, const double a[7], int n) {
+  sbh::BaseFac b;
+  sbh::base_factor(a, n, &b);
+  int rc;
+  if ((rc = upload(h, &F->La, b.La)) || (rc = upload(h, &F->Lb, b.Lb)) ||
+      (rc = upload(h, &F->Lc, b.Lc)) || (rc = upload(h, &F->Ddm1, b.Ddm1)) ||
+      (rc = upload(h, &F->Dd, b.Dd)) || (rc = upload(h, &F->e, b.e)) ||
+      (rc = upload(h, &F->f, b.f)) || (rc = upload(h, &F->g, b.g)))
+    return rc;
+  std::vector<double> s(10);
+  for (int q = 0; q < 6; q++) s[q] = b.sums[q];
+  for (int q = 0; q < 4; q++) s[6 + q] = a[3 + q];
+  if ((rc = upload(h, &F->sums, s))) return rc;
+  F->stride = 0;
+  return 0;
+}
+
+static void member_defaults(const sb_params *p, const Grid &g, double Re, Member *m) {
+  memset(m, 0, sizeof(Member));
+  const double pi = g.pi;
+  m->Re = Re;
+  m->nu = 1.0 / Re;
+  m->CFL = p->CFL;
+  // set_xyz_dy (initcr.f90:490-498)
+  m->cflx = pi / p->CFL / g.dx;
+  m->cflz = pi / p->CFL / g.dz;
+  m->cfly = 2.5 / p->CFL / g.dy;
+  double mm = std::fmax(std::fmax(pi * pi / g.dx / g.dx, 6.25 / g.dy / g.dy), pi * pi / g.dz / g.dz);
+  m->cflvv = 1.0 / Re / p->CFL * mm;
+  m->vbulk = p->vbulk;
+  m->fixed_dt = p->fixed_dt;
+  m->uprim = p->uprim;
+  m->etime = p->etime > 0 ? p->etime : 1e10;
+  m->dumptime = p->dumptime > 0 ? p->dumptime : 1e10;
+  m->dtimag = p->dtimag > 0 ? p->dtimag : m->etime;
+  m->readflag = p->readflag;
+  m->nhist = p->nhist > 0 ? p->nhist : 1;
+}
+
+static int capture_step(sb_handle *h) {
+  if (h->step_exec) {
+    cudaGraphExecDestroy(h->step_exec);
+    h->step_exec = nullptr;
+  }
+  cudaGraph_t graph;
+  CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int rk = 1; rk <= 3 && e == cudaSuccess; rk++) {
+    if ((e = launch_plane(h->g, h->bf, 1, rk, h->st)) != cudaSuccess) break;
+    if ((e = launch_plane(h->g, h->bf, 2, rk, h->st)) != cudaSuccess) break;
+    if ((e = launch_plane(h->g, h->bf, 3, rk, h->st)) != cudaSuccess) break;
+    if ((e = launch_phase(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
+    e = launch_line(h->g, h->bf, rk, 1, h->st);
+  }
+  if (e == cudaSuccess) e = launch_finish(h->g, h->bf, h->st);
+  cudaError_t e2 = cudaStreamEndCapture(h->st, &graph);
+  if (e != cudaSuccess) return fail(3, "kernel launch during capture: %s", cudaGetErrorString(e));
+  if (e2 != cudaSuccess) return fail(3, "capture: %s", cudaGetErrorString(e2));
+  CK(cudaGraphInstantiate(&h->step_exec, graph, 0));
+  cudaGraphDestroy(graph);
+  return 0;
+}
+
+static int ensure_trace(sb_handle *h, int cap) {
+  if (cap <= h->trace_cap) return 0;
+  cap = std::max(cap, 2 * h->trace_cap);
+  double *t;
+  int rc = dalloc(h, &t, (size_t)h->g.B * cap * SB_TRACE_LEN);
+  if (rc) return rc;
+  h->bf.trace = t;
+  h->trace_cap = cap;
+  for (int b = 0; b < h->g.B; b++)
+    CK(cudaMemcpy((char *)(h->bf.mem + b) + offsetof(Member, trace_cap), &cap, sizeof(int),
+                  cudaMemcpyHostToDevice));
+  return capture_step(h);
+}
+
+extern "C" {
+
+int sb_version(void) { return 1; }
+const char *sb_last_error(void) { return g_err.c_str(); }
+
+int sb_sizes(const sb_params *p, int *out) {
+  if (!p || !out) return fail(1, "null argument");
+  int mx = 2 * (p->mgalx / 3), mz = 2 * (p->mgalz / 3) - 1;
+  out[0] = mx;
+  out[1] = mz;
+  out[2] = mx / 2;
+  out[3] = p->my;
+  out[4] = (mz - 1) / 2;
+  out[5] = p->mgalx;
+  out[6] = p->mgalz;
+  out[7] = (mx / 2) * mz * p->my;
+  return 0;
+}
+
+int sb_compact_coeffs(double *pr1, double *rh1h, double *pr2, double *rh2h) {
+  sbh::Coeffs c;
+  sbh::compact_coeffs(&c);
+  for (int d = 0; d < 7; d++) {
+    pr1[d] = c.pr1[d];
+    rh1h[d] = c.rh1h[d];
+    pr2[d] = c.pr2[d];
+    rh2h[d] = c.rh2h[d];
+  }
+  return 0;
+}
+
+int sb_seed_state(const sb_params *p, unsigned long long seed, double k0, double urms,
+                  double *vor, double *phi, double *u00, double *w00) {
+  int rc = check_params(p);
+  if (rc) return rc;
+  return sbh::seed_state(p->mgalx, p->my, p->mgalz, p->alp, p->gam, p->Ly, seed, k0, urms, vor,
+                         phi, u00, w00);
+}
+
+int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
+  if (!out) return fail(1, "null output handle");
+  *out = nullptr;
+  int rc = check_params(p);
+  if (rc) return rc;
+  if (batch < 1) return fail(1, "batch must be >= 1");
+  if (precision != SB_FP64) return fail(2, "precision %d not available", precision);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
+    return fail(5, "no CUDA device: the shearbox library has no CPU path");
+  sb_handle *h = new sb_handle();
+  h->p = *p;
+  h->precision = precision;
+  Grid &g = h->g;
+  memset(&g, 0, sizeof(g));
+  g.B = batch;
+  g.mgalx = p->mgalx;
+  g.my = p->my;
+  g.mgalz = p->mgalz;
+  g.mx = 2 * (p->mgalx / 3);
+  g.mz = 2 * (p->mgalz / 3) - 1;
+  g.nkx = g.mx / 2;
+  g.nz = (g.mz - 1) / 2;
+  g.mgx = p->mgalx / 2;
+  g.ncb = (g.nkx + plane_cb(p->mgalz) - 1) / plane_cb(p->mgalz);
+  g.pi = 4.0 * std::atan(1.0);
+  g.alp = p->alp;
+  g.gam = p->gam;
+  g.Ly = p->Ly;
+  g.s = p->s;
+  g.chi = p->chi;
+  g.dx = 2.0 * g.pi / p->alp / (double)g.mx;
+  g.dz = 2.0 * g.pi / p->gam / (double)g.mz;
+  g.dy = p->Ly / (double)p->my;
+  sbh::Coeffs co;
+  sbh::compact_coeffs(&co);
+  const double hdy = g.dy;
+  double rh1[7], rh2[7];
+  for (int d = 0; d < 7; d++) {
+    rh1[d] = co.rh1h[d] / hdy;          // update_dy (diffy_shear_hepta.f90:562-573)
+    rh2[d] = co.rh2h[d] / (hdy * hdy);
+    g.rh1[d] = rh1[d];
+    g.rh2[d] = rh2[d];
+    g.pr2[d] = co.pr2[d];
+  }
+  const int nl = g.nkx * g.mz;
+  g.plane = 2L * nl;
+  g.field = g.plane * g.my;
+  g.nlines_pad = ((2 * nl + 31) / 32) * 32;
+  g.tpm = g.nlines_pad + 32;
+  cudaError_t ce = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) {
+    delete h;
+    return fail(3, "stream: %s", cudaGetErrorString(ce));
+  }
+  Bufs &bf = h->bf;
+  const size_t B = batch, F = g.field, my = g.my;
+  auto A = [&](double **q, size_t n) { return dalloc(h, q, n); };
+  if ((rc = A(&bf.vor, B * F)) || (rc = A(&bf.phi, B * F)) || (rc = A(&bf.vorwk, B * F)) ||
+      (rc = A(&bf.phiwk, B * F)) || (rc = A(&bf.G, B * F)) || (rc = A(&bf.V, B * F)) ||
+      (rc = A(&bf.D, B * F)) || (rc = A(&bf.S, B * F + B * 2 * my * 32)) ||
+      (rc = A(&bf.mu, B * 2 * my)) || (rc = A(&bf.mwk, B * 2 * my)) ||
+      (rc = A(&bf.mrf, B * 2 * my)) || (rc = A(&bf.mdu, B * 2 * my)) ||
+      (rc = A(&bf.zbuf, B * my * g.mgalz * 6 * g.nkx * 2)) ||
+      (rc = A(&bf.xbuf, B * my * g.mgalz * 3 * g.nkx * 2)) ||
+      (rc = A(&bf.hpart, B * my * g.ncb * SB_NHIST_Q)) || (rc = A(&bf.sh_old, B * 4 * g.nkx)) ||
+      (rc = A(&bf.sh_new, B * 4 * g.nkx)) || (rc = A(&bf.mf1, B * my * g.nkx * 2)) ||
+      (rc = A(&bf.mf2, B * my * g.nkx * 2)) || (rc = A(&h->d_pen, F))) {
+    sb_destroy(h);
+    return rc;
+  }
+  {
+    void *q = nullptr;
+    ce = cudaMalloc(&q, sizeof(Member) * B);
+    if (ce != cudaSuccess) {
+      sb_destroy(h);
+      return fail(4, "cudaMalloc members: %s", cudaGetErrorString(ce));
+    }
+    h->allocs.push_back(q);
+    bf.mem = (Member *)q;
+  }
+  // twiddles e^{-2 pi i t / N}
+  auto tw = [&](int n) {
+    std::vector<double> v(2 * (size_t)n);
+    for (int t = 0; t < n; t++) {
+      double a = -2.0 * g.pi * (double)t / (double)n;
+      v[2 * t] = std::cos(a);
+      v[2 * t + 1] = std::sin(a);
+    }
+    return v;
+  };
+  std::vector<double> kinv((size_t)nl), ginv((size_t)g.mz);
+  for (int k = 0; k < g.mz; k++) {
+    int kzs = (k <= g.nz) ? k : k - g.mz;
+    double gz = g.gam * kzs;
+    ginv[k] = (k == 0) ? 0.0 : 1.0 / gz;
+    for (int i = 0; i < g.nkx; i++) {
+      double a = g.alp * i;
+      double K = gz * gz + a * a;
+      kinv[(size_t)k * g.nkx + i] = (i == 0 && k == 0) ? 0.0 : 1.0 / K;
+    }
+  }
+  if ((rc = upload(h, &bf.twz, tw(g.mgalz))) || (rc = upload(h, &bf.twx, tw(g.mgalx))) ||
+      (rc = upload(h, &bf.kinv, kinv)) || (rc = upload(h, &bf.ginv, ginv)) ||
+      (rc = upload_uniform(h, &bf.d1, co.pr1, g.my)) ||
+      (rc = upload_uniform(h, &bf.d2, co.pr2, g.my))) {
+    sb_destroy(h);
+    return rc;
+  }
+  {
+    // Helmholtz (rh2 - k^2 pr2), one base factorisation per (kx, kz) line
+    // (lapcdy, diffy_shear_hepta.f90:466-525); line (0,0) is never solved and
+    // gets a harmless k^2 = 1
+    const size_t n = g.my;
+    std::vector<double> La(n * nl), Lb(n * nl), Lc(n * nl), Dm(n * nl), Dd(n * nl), e(n * nl),
+        f(n * nl), gg(n * nl), sums(10 * (size_t)nl);
+    sbh::BaseFac bfac;
+    for (int k = 0; k < g.mz; k++)
+      for (int i = 0; i < g.nkx; i++) {
+        const size_t line = (size_t)k * g.nkx + i;
+        int kzs = (k <= g.nz) ? k : k - g.mz;
+        double gz = g.gam * kzs, a = g.alp * i;
+        double k2 = (i == 0 && k == 0) ? 1.0 : gz * gz + a * a;
+        double lap[7];
+        for (int d = 0; d < 7; d++) lap[d] = rh2[d] - k2 * co.pr2[d];
+        sbh::base_factor(lap, g.my, &bfac);
+        for (size_t q = 0; q < n; q++) {
+          La[q * nl + line] = bfac.La[q];
+          Lb[q * nl + line] = bfac.Lb[q];
+          Lc[q * nl + line] = bfac.Lc[q];
+          Dm[q * nl + line] = bfac.Ddm1[q];
+          Dd[q * nl + line] = bfac.Dd[q];
+          e[q * nl + line] = bfac.e[q];
+          f[q * nl + line] = bfac.f[q];
+          gg[q * nl + line] = bfac.g[q];
+        }
+        for (int q = 0; q < 6; q++) sums[(size_t)q * nl + line] = bfac.sums[q];
+        for (int q = 0; q < 4; q++) sums[(size_t)(6 + q) * nl + line] = lap[3 + q];
+      }
+    Fac &H = bf.hz;
+    if ((rc = upload(h, &H.La, La)) || (rc = upload(h, &H.Lb, Lb)) || (rc = upload(h, &H.Lc, Lc)) ||
+        (rc = upload(h, &H.Ddm1, Dm)) || (rc = upload(h, &H.Dd, Dd)) || (rc = upload(h, &H.e, e)) ||
+        (rc = upload(h, &H.f, f)) || (rc = upload(h, &H.g, gg)) || (rc = upload(h, &H.sums, sums))) {
+      sb_destroy(h);
+      return rc;
+    }
+    H.stride = nl;
+  }
+  h->mem_init.resize(B);
+  for (size_t b = 0; b < B; b++) member_defaults(p, g, p->Re, &h->mem_init[b]);
+  ce = cudaMemcpy(bf.mem, h->mem_init.data(), sizeof(Member) * B, cudaMemcpyHostToDevice);
+  if (ce != cudaSuccess) {
+    sb_destroy(h);
+    return fail(3, "member upload: %s", cudaGetErrorString(ce));
+  }
+  if (launch_plane(g, bf, 0, 0, h->st) != cudaSuccess) {
+    sb_destroy(h);
+    return fail(3, "kernel attributes: %s", cudaGetErrorString(cudaGetLastError()));
+  }
+  if ((rc = ensure_trace(h, 64))) {
+    sb_destroy(h);
+    return rc;
+  }
+  *out = h;
+  return 0;
+}
+
+int sb_destroy(sb_handle *h) {
+  if (!h) return 0;
+  if (h->st) cudaStreamSynchronize(h->st);
+  if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
+  for (void *q : h->allocs) cudaFree(q);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return 0;
+}
+
+int sb_set_member_re(sb_handle *h, int member, double Re) {
+  if (!h || member < 0 || member >= h->g.B) return fail(1, "bad handle or member");
+  if (!(Re != 0.0)) return fail(1, "Re must be nonzero");
+  Member m = h->mem_init[member];
+  member_defaults(&h->p, h->g, Re, &m);
+  h->mem_init[member].Re = m.Re;
+  h->mem_init[member].nu = m.nu;
+  h->mem_init[member].cflvv = m.cflvv;
+  Member *d = h->bf.mem + member;
+  CK(cudaMemcpy((char *)d + offsetof(Member, Re), &m.Re, sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy((char *)d + offsetof(Member, nu), &m.nu, sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy((char *)d + offsetof(Member, cflvv), &m.cflvv, sizeof(double), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int sb_set_state(sb_handle *h, int member, const double *vor, const double *phi, const double *u00,
+                 const double *w00, double time, double xoffb, double xofft) {
+  if (!h || member < 0 || member >= h->g.B) return fail(1, "bad handle or member");
+  if (!vor || !phi || !u00 || !w00) return fail(1, "null state array");
+  const Grid &g = h->g;
+  const size_t F = g.field;
+  CK(cudaMemcpyAsync(h->d_pen, vor, sizeof(double) * F, cudaMemcpyHostToDevice, h->st));
+  CK(launch_pencil_to_plane(g, h->d_pen, h->bf.vor + member * F, h->st));
+  CK(cudaMemcpyAsync(h->d_pen, phi, sizeof(double) * F, cudaMemcpyHostToDevice, h->st));
+  CK(launch_pencil_to_plane(g, h->d_pen, h->bf.phi + member * F, h->st));
+  std::vector<double> mu(2 * (size_t)g.my);
+  for (int j = 0; j < g.my; j++) {
+    mu[2 * j] = u00[j];
+    mu[2 * j + 1] = w00[j];
+  }
+  CK(cudaMemcpyAsync(h->bf.mu + (size_t)member * 2 * g.my, mu.data(), sizeof(double) * mu.size(),
+                     cudaMemcpyHostToDevice, h->st));
+  double sc[3] = {time, xoffb, xofft};
+  CK(cudaMemcpyAsync((char *)(h->bf.mem + member) + offsetof(Member, time), sc, sizeof(sc),
+                     cudaMemcpyHostToDevice, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  return 0;
+}
+
+int sb_get_state(sb_handle *h, int member, double *vor, double *phi, double *u00, double *w00,
+                 double *time, double *xoffb, double *xofft) {
+  if (!h || member < 0 || member >= h->g.B) return fail(1, "bad handle or member");
+  const Grid &g = h->g;
+  const size_t F = g.field;
+  if (vor) {
+    CK(launch_plane_to_pencil(g, h->bf.vor + member * F, h->d_pen, h->st));
+    CK(cudaMemcpyAsync(vor, h->d_pen, sizeof(double) * F, cudaMemcpyDeviceToHost, h->st));
+  }
+  if (phi) {
+    CK(cudaStreamSynchronize(h->st));
+    CK(launch_plane_to_pencil(g, h->bf.phi + member * F, h->d_pen, h->st));
+    CK(cudaMemcpyAsync(phi, h->d_pen, sizeof(double) * F, cudaMemcpyDeviceToHost, h->st));
+  }
+  std::vector<double> mu(2 * (size_t)g.my);
+  CK(cudaMemcpyAsync(mu.data(), h->bf.mu + (size_t)member * 2 * g.my, sizeof(double) * mu.size(),
+                     cudaMemcpyDeviceToHost, h->st));
+  double sc[3];
+  CK(cudaMemcpyAsync(sc, (char *)(h->bf.mem + member) + offsetof(Member, time), sizeof(sc),
+                     cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  for (int j = 0; j < g.my; j++) {
+    if (u00) u00[j] = mu[2 * j];
+    if (w00) w00[j] = mu[2 * j + 1];
+  }
+  if (time) *time = sc[0];
+  if (xoffb) *xoffb = sc[1];
+  if (xofft) *xofft = sc[2];
+  return 0;
+}
+
+int sb_step(sb_handle *h, int nsteps) {
+  if (!h) return fail(1, "null handle");
+  if (nsteps < 0) return fail(1, "nsteps < 0");
+  int rc = ensure_trace(h, nsteps > 0 ? nsteps : 1);
+  if (rc) return rc;
+  CK(launch_phase(h->g, h->bf, 0, h->st));
+  CK(launch_line(h->g, h->bf, 0, 1, h->st));
+  for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(h->step_exec, h->st));
+  return 0;
+}
+
+int sb_get_status(sb_handle *h, int member, sb_status *st) {
+  if (!h || !st || member < 0 || member >= h->g.B) return fail(1, "bad argument");
+  Member m;
+  CK(cudaMemcpyAsync(&m, h->bf.mem + member, sizeof(Member), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  st->istop = m.istop;
+  st->steps_done = m.istep - 1;
+  st->ntrace = m.ntrace;
+  st->flags = m.flags;
+  st->time = m.time;
+  st->deltat = m.Deltat;
+  st->xoffb = m.xoffb;
+  st->xofft = m.xofft;
+  st->cfl = m.CFLcur;
+  st->cflv = m.CFLv;
+  return 0;
+}
+
+int sb_get_trace(sb_handle *h, int member, double *out, int max_records, int *nrec) {
+  if (!h || member < 0 || member >= h->g.B) return fail(1, "bad argument");
+  Member m;
+  CK(cudaMemcpyAsync(&m, h->bf.mem + member, sizeof(Member), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  int n = std::min(std::min(m.ntrace, h->trace_cap), max_records);
+  if (n > 0 && out)
+    CK(cudaMemcpy(out, h->bf.trace + (size_t)member * h->trace_cap * SB_TRACE_LEN,
+                  sizeof(double) * n * SB_TRACE_LEN, cudaMemcpyDeviceToHost));
+  if (nrec) *nrec = n;
+  return 0;
+}
+
+int sb_cross(sb_handle *h, double *vor, double *phi, double *u00, double *w00, double *time,
+             double *xoffb, double *xofft, int nstep, sb_status *st) {
+  if (!h || !time || !xoffb || !xofft) return fail(1, "null argument");
+  int rc = sb_set_state(h, 0, vor, phi, u00, w00, *time, *xoffb, *xofft);
+  if (rc) return rc;
+  if ((rc = sb_step(h, nstep))) return rc;
+  if ((rc = sb_get_state(h, 0, vor, phi, u00, w00, time, xoffb, xofft))) return rc;
+  if (st && (rc = sb_get_status(h, 0, st))) return rc;
+  return 0;
+}
+
+void *sb_get_stream(sb_handle *h) { return h ? (void *)h->st : nullptr; }
+
+int sb_sync(sb_handle *h) {
+  if (!h) return fail(1, "null handle");
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaGetLastError());
+  return 0;
+}
+
+}  // extern "C"

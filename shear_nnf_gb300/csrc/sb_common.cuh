@@ -1,0 +1,96 @@
+// sb_common.cuh -- shared device types for the shearing-box RK3 step on GB300.
+//
+// Device layout of one spectral field of one box ("plane-major"):
+//   f[j][k][i] complex (re, im interleaved doubles), i = kx index fastest
+//   (0..nkx-1), k = kz index (0..mz-1, reference ordering: 0..nz positive,
+//   nz+1..mz-1 negative), j = y plane (0..my-1).  A batch of B boxes is
+//   [b][j][k][i].  The y-line kernels read one double per thread per plane
+//   (coalesced across kx), the plane kernels read contiguous planes, so the
+//   reference's plane<->pencil transposes (change.allfac_ieor.f) disappear.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define SB_TRACE_LEN 24
+#define SB_NHIST_Q 11   // per-plane hist partial sums
+#define SB_MAX_NY 512
+
+namespace sb {
+
+struct cd {
+  double x, y;
+};
+__host__ __device__ __forceinline__ cd mk(double a, double b) { cd z; z.x = a; z.y = b; return z; }
+__host__ __device__ __forceinline__ cd operator+(cd a, cd b) { return mk(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ cd operator-(cd a, cd b) { return mk(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ cd operator*(cd a, cd b) {
+  return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ cd operator*(double r, cd a) { return mk(r * a.x, r * a.y); }
+__host__ __device__ __forceinline__ cd cj(cd a) { return mk(a.x, -a.y); }
+__host__ __device__ __forceinline__ double abs2(cd a) { return a.x * a.x + a.y * a.y; }
+
+// Factor tables of one cyclic Hermitian heptadiagonal LDL^H factorisation with
+// the shear phase factored out (see sb_factor.cpp).  Arrays are indexed
+// [q * stride + line] with q the 0-based row; stride = 0 for the operators that
+// are the same on every line (d/dy, d2/dy2).
+struct Fac {
+  const double *La, *Lb, *Lc, *Ddm1, *e, *f, *g;  // my entries each
+  const double *Dd;    // my entries (rows my-8 .. my-4 are read)
+  const double *sums;  // 10 entries: See Sfe Sff Sge Sgf Sgg, then a(0..3)
+  long stride;
+};
+
+// Constant per-handle parameters (passed by value to every kernel)
+struct Grid {
+  int B, mgalx, my, mgalz, mx, mz, nkx, nz, mgx;
+  int ncb;               // kx column blocks per plane (plane kernels)
+  double alp, gam, Ly, s, chi, dx, dy, dz, pi;
+  double rh1[7], rh2[7], pr2[7];
+  long plane;            // doubles per plane of one field  (2*nkx*mz)
+  long field;            // doubles per field of one box   (plane*my)
+  int tpm;               // line-kernel threads per member
+  int nlines_pad;        // padded component lines per member
+};
+
+// Per-member run state, owned by the device (one per box in the batch)
+struct Member {
+  // parameters
+  double Re, nu, CFL, cflx, cfly, cflz, cflvv, vbulk, fixed_dt, uprim;
+  double etime, dumptime, dtimag;
+  int readflag, nhist;
+  // state scalars
+  double time, xoffb, xofft;
+  double xwkb, xwkt;          // offsets of the current substep (before its update)
+  double xwkb_n, xwkt_n;      // offsets after the current substep's update
+  double Deltat, CFLcur, CFLv;
+  double umax[4];
+  unsigned long long umax_bits[4];  // |u| maxima as ordered bit patterns (atomicMax)
+  int istop, idump, ihist, istep, halted, ntrace, trace_cap, flags;
+};
+
+enum { SBF_DIVERGED = 1, SBF_NAN = 2, SBF_LAMINAR = 4, SBF_ETIME = 8 };
+
+// RK3 coefficients of the low-storage Spalart-Moser-Rogers scheme
+// (cross.f90:17-24)
+__device__ __constant__ static const double kGama[3] = {8.0 / 15.0, 5.0 / 12.0, 3.0 / 4.0};
+__device__ __constant__ static const double kZeta[3] = {-17.0 / 60.0, -5.0 / 12.0, 0.0};
+__device__ __constant__ static const double kCa[3] = {8.0 / 15.0, 2.0 / 3.0, 1.0};
+
+// Device arrays of one handle
+struct Bufs {
+  double *vor, *phi, *vorwk, *phiwk, *G, *V, *D, *S;  // spectral fields [B][field]
+  double *mu, *mwk, *mrf, *mdu;  // mean lines (u00 + i w00) [B][my] complex
+  double *zbuf, *xbuf;           // plane-stage intermediates
+  double *hpart;                 // hist partials [B][my][ncb][SB_NHIST_Q]
+  double *sh_old, *sh_new;       // [B][2][nkx] complex (t then b)
+  double *mf1, *mf2;             // moving-frame phases [B][my][nkx] complex
+  double *trace;                 // [B][cap][SB_TRACE_LEN]
+  Member *mem;                   // [B]
+  const double *twz, *twx;       // FFT twiddles e^{-2 pi i t/N}
+  const double *ginv;            // 1/g per kz  (g = gam * kz_signed; 0 at k=0)
+  const double *kinv;            // 1/(alp2+gam2) per (k,i); 0 at (0,0)
+  Fac d1, d2, hz;                // d/dy, d2/dy2, Helmholtz (per line)
+};
+
+}  // namespace sb

@@ -1,0 +1,1041 @@
+// sb_kernels.cu -- FP64 kernels of the shearing-box RK3 substep on sm_103a.
+//
+// One RK3 substep of the reference (cross.f90:428-1000, explicit branch,
+// iadd_mode=5) is five launches:
+//   k_p1    per (plane, kx block): u, w, omega_x, omega_z from v, omega_y
+//           (cross.f90:1226-1276), hist sums (cross.f90:1796-1963), and the six
+//           backward z-transforms with zero padding (fill00, fou3D_thread.f:73-126)
+//   k_p2    per (plane, z row pair): backward x-transforms, |u| maxima for the CFL
+//           (cross.f90:1438-1441), u x (omega + 2 chi z) (cross.f90:1453-1462) and
+//           the three forward x-transforms
+//   k_p3    per (plane, kx block): forward z-transforms, 1/(mgalx*mgalz) scaling and
+//           truncation (pack00), right-hand sides of iadd_mode 5
+//           (cross.f90:1536-1546) and the mean-mode forcing (cross.f90:1489-1490)
+//   k_phase per box: Delta t from the CFL (cross.f90:1598-1711), the UNER record
+//           (cross.f90:2064-2118), shear offsets and phase tables
+//   k_line  per (kx, kz) y-line: every y-operator of the substep in one pass --
+//           derivyc of d(omega_y)/dy, the viscous terms (visc3d), the RK3 update
+//           (cross.f90:694-723), the zeta store and moving_frame remaps
+//           (cross.f90:752-781), the Helmholtz solve for v (lapcdy, cross.f90:784-795)
+//           and the derivatives the next substep starts from (cross.f90:434-445).
+// The per-plane/per-line split replaces the reference's plane<->pencil MPI
+// transposes (change.allfac_ieor.f): every kernel reads the same plane-major
+// layout, so no data is reordered.
+#include <cuda_runtime.h>
+
+#include "sb_common.cuh"
+#include "sb_fft.cuh"
+#include "sb_kernels.h"
+
+namespace sb {
+
+// ---------------------------------------------------------------------------
+// y-line solver
+// ---------------------------------------------------------------------------
+struct Tail {
+  cd Le5, Le4, Le3, Lf4, Lf3, Lf2, Lg3, Lg2, Lg1;
+  double Dm2, Dm1, Dm0;  // 1/D at rows N-2, N-1, N
+};
+
+struct FacView {
+  const Fac &F;
+  long line;
+  __device__ FacView(const Fac &f, long l) : F(f), line(l) {}
+  // 1-based row accessors
+  __device__ __forceinline__ double ld(const double *p, int i) const {
+    return __ldg(p + (F.stride ? (long)(i - 1) * F.stride + line : (long)(i - 1)));
+  }
+  __device__ __forceinline__ double La(int i) const { return ld(F.La, i); }
+  __device__ __forceinline__ double Lb(int i) const { return ld(F.Lb, i); }
+  __device__ __forceinline__ double Lc(int i) const { return ld(F.Lc, i); }
+  __device__ __forceinline__ double Dm(int i) const { return ld(F.Ddm1, i); }
+  __device__ __forceinline__ double Dd(int i) const { return ld(F.Dd, i); }
+  __device__ __forceinline__ double e(int i) const { return ld(F.e, i); }
+  __device__ __forceinline__ double f(int i) const { return ld(F.f, i); }
+  __device__ __forceinline__ double g(int i) const { return ld(F.g, i); }
+  __device__ __forceinline__ double sum(int q) const {
+    return __ldg(F.sums + (F.stride ? (long)q * F.stride + line : (long)q));
+  }
+};
+
+// Shear-dependent tail of the cyclic LDL^H factorisation: the entries that
+// modChol_addshear (diffy_shear_hepta.f90:760-870) recomputes, evaluated from
+// the shear-free base with the phase factored out of the border rows.
+__device__ Tail make_tail(const FacView &V, cd shp, int N) {
+  Tail T;
+  const double a0 = V.sum(6), a1 = V.sum(7), a2 = V.sum(8), a3 = V.sum(9);
+  const double shp2 = abs2(shp);
+  cd E8 = V.e(N - 8) * shp, E7 = V.e(N - 7) * shp, E6 = V.e(N - 6) * shp;
+  T.Le5 = V.Dm(N - 5) * (mk(a3, 0.0) - (V.Dd(N - 8) * V.Lc(N - 5)) * E8 -
+                         (V.Dd(N - 7) * V.Lb(N - 5)) * E7 - (V.Dd(N - 6) * V.La(N - 5)) * E6);
+  T.Le4 = V.Dm(N - 4) * (mk(a2, 0.0) - (V.Dd(N - 7) * V.Lc(N - 4)) * E7 -
+                         (V.Dd(N - 6) * V.Lb(N - 4)) * E6 - (V.Dd(N - 5) * V.La(N - 4)) * T.Le5);
+  T.Le3 = V.Dm(N - 3) * (mk(a1, 0.0) - (V.Dd(N - 6) * V.Lc(N - 3)) * E6 -
+                         (V.Dd(N - 5) * V.Lb(N - 3)) * T.Le5 - (V.Dd(N - 4) * V.La(N - 3)) * T.Le4);
+  const double DdN2 = a0 - (shp2 * V.sum(0) + abs2(T.Le5) * V.Dd(N - 5) +
+                            abs2(T.Le4) * V.Dd(N - 4) + abs2(T.Le3) * V.Dd(N - 3));
+  T.Dm2 = 1.0 / DdN2;
+  cd F7 = V.f(N - 7) * shp, F6 = V.f(N - 6) * shp, F5 = V.f(N - 5) * shp;
+  T.Lf4 = V.Dm(N - 4) * (mk(a3, 0.0) - (V.Dd(N - 7) * V.Lc(N - 4)) * F7 -
+                         (V.Dd(N - 6) * V.Lb(N - 4)) * F6 - (V.Dd(N - 5) * V.La(N - 4)) * F5);
+  T.Lf3 = V.Dm(N - 3) * (mk(a2, 0.0) - (V.Dd(N - 6) * V.Lc(N - 3)) * F6 -
+                         (V.Dd(N - 5) * V.Lb(N - 3)) * F5 - (V.Dd(N - 4) * V.La(N - 3)) * T.Lf4);
+  cd tmp = mk(shp2 * V.sum(1), 0.0) + V.Dd(N - 5) * (F5 * cj(T.Le5)) +
+           V.Dd(N - 4) * (T.Lf4 * cj(T.Le4)) + V.Dd(N - 3) * (T.Lf3 * cj(T.Le3));
+  T.Lf2 = T.Dm2 * (mk(a1, 0.0) - tmp);
+  const double DdN1 = a0 - (shp2 * V.sum(2) + abs2(T.Lf4) * V.Dd(N - 4) +
+                            abs2(T.Lf3) * V.Dd(N - 3) + abs2(T.Lf2) * DdN2);
+  T.Dm1 = 1.0 / DdN1;
+  cd G6 = V.g(N - 6) * shp, G5 = V.g(N - 5) * shp, G4 = V.g(N - 4) * shp;
+  T.Lg3 = V.Dm(N - 3) * (mk(a3, 0.0) - (V.Dd(N - 6) * V.Lc(N - 3)) * G6 -
+                         (V.Dd(N - 5) * V.Lb(N - 3)) * G5 - (V.Dd(N - 4) * V.La(N - 3)) * G4);
+  tmp = mk(shp2 * V.sum(3), 0.0) + V.Dd(N - 5) * (G5 * cj(T.Le5)) +
+        V.Dd(N - 4) * (G4 * cj(T.Le4)) + V.Dd(N - 3) * (T.Lg3 * cj(T.Le3));
+  T.Lg2 = T.Dm2 * (mk(a2, 0.0) - tmp);
+  tmp = mk(shp2 * V.sum(4), 0.0) + V.Dd(N - 4) * (G4 * cj(T.Lf4)) +
+        V.Dd(N - 3) * (T.Lg3 * cj(T.Lf3)) + DdN2 * (T.Lg2 * cj(T.Lf2));
+  T.Lg1 = T.Dm1 * (mk(a1, 0.0) - tmp);
+  const double DdN0 = a0 - (shp2 * V.sum(5) + abs2(T.Lg3) * V.Dd(N - 3) +
+                            abs2(T.Lg2) * DdN2 + abs2(T.Lg1) * DdN1);
+  T.Dm0 = 1.0 / DdN0;
+  return T;
+}
+
+// component c of a complex value held by the lane pair (c=0: re, c=1: im)
+__device__ __forceinline__ cd pair_full(double own, int c) {
+  double oth = __shfl_xor_sync(0xffffffffu, own, 1);
+  return c ? mk(oth, own) : mk(own, oth);
+}
+__device__ __forceinline__ double comp(cd z, int c) { return c ? z.y : z.x; }
+// component c of (own, other) * s
+__device__ __forceinline__ double cmul_c(double own, double oth, cd s, int c) {
+  return c ? fma(own, s.x, oth * s.y) : fma(own, s.x, -(oth * s.y));
+}
+
+// Solves B x = A u_ext on one complex y-line (this lane: component c) with the
+// shear-periodic extension u(j+my) = u(j)*shp, u(j-my) = u(j)*shm
+// (derivyc / lapcdy, diffy_shear_hepta.f90:333-525; solve7cyclic 900-954).
+// A is the 7-point stencil (r0; r1..r3) -- antisymmetric if anti -- and B the
+// factorised heptadiagonal.  u is read with stride ps; y (the forward
+// substitution) is kept in ybuf (stride ys).  epi(j, x_j) receives the
+// solution in descending j.  All 32 lanes of the warp must call this together.
+template <class EPI>
+__device__ __forceinline__ void solve_line(const double *u, long ps, double *ybuf, long ys, int N,
+                                           const FacView &V, const Tail &T, cd shp, cd shm, int c,
+                                           double r0, double r1, double r2, double r3, bool anti,
+                                           EPI epi) {
+  // wrapped values u(-3..-1) = u(N-3..N-1)*shm and u(N..N+2) = u(0..2)*shp
+  double uN3 = u[(long)(N - 3) * ps], uN2 = u[(long)(N - 2) * ps], uN1 = u[(long)(N - 1) * ps];
+  double u0 = u[0], u1 = u[ps], u2 = u[2 * ps];
+  double pN3 = __shfl_xor_sync(0xffffffffu, uN3, 1), pN2 = __shfl_xor_sync(0xffffffffu, uN2, 1),
+         pN1 = __shfl_xor_sync(0xffffffffu, uN1, 1);
+  double p0 = __shfl_xor_sync(0xffffffffu, u0, 1), p1 = __shfl_xor_sync(0xffffffffu, u1, 1),
+         p2 = __shfl_xor_sync(0xffffffffu, u2, 1);
+  const double lo3 = cmul_c(uN3, pN3, shm, c), lo2 = cmul_c(uN2, pN2, shm, c),
+               lo1 = cmul_c(uN1, pN1, shm, c);
+  const double hi0 = cmul_c(u0, p0, shp, c), hi1 = cmul_c(u1, p1, shp, c),
+               hi2 = cmul_c(u2, p2, shp, c);
+  double w0 = lo3, w1 = lo2, w2 = lo1, w3 = u0, w4 = u1, w5 = u2, w6 = u[3 * ps];
+  double y1 = 0.0, y2 = 0.0, y3 = 0.0;
+  double Se = 0.0, Sf = 0.0, Sg = 0.0;
+  double bN2 = 0.0, bN1 = 0.0, bN0 = 0.0;
+  for (int j = 0; j < N; j++) {
+    double rhs;
+    if (anti)
+      rhs = r1 * (w4 - w2) + r2 * (w5 - w1) + r3 * (w6 - w0);
+    else
+      rhs = r0 * w3 + r1 * (w4 + w2) + r2 * (w5 + w1) + r3 * (w6 + w0);
+    if (j < N - 3) {
+      const int i = j + 1;  // 1-based row
+      double y = rhs - V.Lc(i) * y3 - V.Lb(i) * y2 - V.La(i) * y1;
+      ybuf[(long)j * ys] = y;
+      Se = fma(V.e(i), y, Se);
+      Sf = fma(V.f(i), y, Sf);
+      Sg = fma(V.g(i), y, Sg);
+      y3 = y2;
+      y2 = y1;
+      y1 = y;
+    } else if (j == N - 3) {
+      bN2 = rhs;
+    } else if (j == N - 2) {
+      bN1 = rhs;
+    } else {
+      bN0 = rhs;
+    }
+    w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = w5; w5 = w6;
+    const int jn = j + 4;
+    w6 = (jn < N) ? u[(long)jn * ps] : (jn == N ? hi0 : (jn == N + 1 ? hi1 : hi2));
+  }
+  // bordered rows N-2..N and the first rows of the back substitution (complex)
+  const cd Y3 = pair_full(y1, c), Y4 = pair_full(y2, c), Y5 = pair_full(y3, c);
+  const cd cSe = pair_full(Se, c), cSf = pair_full(Sf, c), cSg = pair_full(Sg, c);
+  const cd b2 = pair_full(bN2, c), b1 = pair_full(bN1, c), b0 = pair_full(bN0, c);
+  const cd yN2 = b2 - (shp * cSe + T.Le5 * Y5 + T.Le4 * Y4 + T.Le3 * Y3);
+  const cd yN1 = b1 - (shp * cSf + T.Lf4 * Y4 + T.Lf3 * Y3 + T.Lf2 * yN2);
+  const cd yN0 = b0 - (shp * cSg + T.Lg3 * Y3 + T.Lg2 * yN2 + T.Lg1 * yN1);
+  const cd xN0 = T.Dm0 * yN0;
+  const cd xN1 = T.Dm1 * yN1 - cj(T.Lg1) * xN0;
+  const cd xN2 = T.Dm2 * yN2 - cj(T.Lf2) * xN1 - cj(T.Lg2) * xN0;
+  const cd csh = cj(shp);
+  const cd Pe = csh * xN2, Pf = csh * xN1, Pg = csh * xN0;
+  const cd x3 = V.Dm(N - 3) * Y3 - cj(T.Le3) * xN2 - cj(T.Lf3) * xN1 - cj(T.Lg3) * xN0;
+  const cd x4 = V.Dm(N - 4) * Y4 - V.La(N - 3) * x3 - cj(T.Le4) * xN2 - cj(T.Lf4) * xN1 -
+                V.g(N - 4) * Pg;
+  const cd x5 = V.Dm(N - 5) * Y5 - V.La(N - 4) * x4 - V.Lb(N - 3) * x3 - cj(T.Le5) * xN2 -
+                V.f(N - 5) * Pf - V.g(N - 5) * Pg;
+  epi(N - 1, comp(xN0, c));
+  epi(N - 2, comp(xN1, c));
+  epi(N - 3, comp(xN2, c));
+  epi(N - 4, comp(x3, c));
+  epi(N - 5, comp(x4, c));
+  epi(N - 6, comp(x5, c));
+  const double pe = comp(Pe, c), pf = comp(Pf, c), pg = comp(Pg, c);
+  double xa = comp(x5, c), xb = comp(x4, c), xc = comp(x3, c);
+  for (int j = N - 7; j >= 0; j--) {
+    const int i = j + 1;
+    double x = V.Dm(i) * ybuf[(long)j * ys] - V.La(i + 1) * xa - V.Lb(i + 2) * xb -
+               V.Lc(i + 3) * xc - V.e(i) * pe - V.f(i) * pf - V.g(i) * pg;
+    epi(j, x);
+    xc = xb;
+    xb = xa;
+    xa = x;
+  }
+}
+
+__device__ __forceinline__ cd ldc(const double *p) { return mk(p[0], p[1]); }
+
+// ---------------------------------------------------------------------------
+// k_line: all y-operators of one substep (mode 1..3) or of the step prologue
+// (mode 0: set_conj, v = lapcdy(phi), first derivatives; cross.f90:283-287,
+// 408-445).  One lane per (line, component); lane pairs hold re/im.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_line(Grid g, Bufs bf, int mode, int next) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = (int)(t / g.tpm);
+  if (b >= g.B) return;  // whole warps: tpm is a multiple of 32
+  const int r = (int)(t - (long)b * g.tpm);
+  Member &M = bf.mem[b];
+  if (M.halted) return;  // uniform per warp
+  const int N = g.my;
+  const int c = r & 1;
+  const int nl = g.nkx * g.mz;
+  const bool is_mean = r >= g.nlines_pad;
+  const int lane = threadIdx.x & 31;
+  long lc;
+  bool active;
+  if (!is_mean) {
+    lc = r >> 1;
+    active = lc < nl;
+    if (!active) lc = nl - 1;
+  } else {
+    lc = 0;
+    active = (r - g.nlines_pad) < 2;
+  }
+  const int i = (int)(lc % g.nkx), k = (int)(lc / g.nkx);
+  // scratch for the forward substitution: a field-sized array for real lines,
+  // lane-private rows for padding lanes and the mean warp
+  double *ybuf;
+  long ys;
+  if (!is_mean && active) {
+    ybuf = bf.S + (long)b * g.field + 2 * lc + c;
+    ys = g.plane;
+  } else {
+    ybuf = bf.S + (long)g.B * g.field + ((long)(2 * b + (is_mean ? 1 : 0)) * N) * 32 + lane;
+    ys = 32;
+  }
+  const FacView V1(bf.d1, 0), V2(bf.d2, 0);
+  const double Dt = M.Deltat, nu = M.nu;
+
+  if (is_mean) {
+    // ---- mean line u00 + i w00 (no shear phase) ----
+    double *mu = bf.mu + (long)b * 2 * N + c;
+    double *mwk = bf.mwk + (long)b * 2 * N + c;
+    double *mrf = bf.mrf + (long)b * 2 * N + c;
+    double *mdu = bf.mdu + (long)b * 2 * N + c;
+    const cd one = mk(1.0, 0.0);
+    const Tail T1 = make_tail(V1, one, N), T2 = make_tail(V2, one, N);
+    if (mode >= 1) {
+      const int rk = mode - 1;
+      const double gk = kGama[rk], zk = kZeta[rk];
+      // visc3d(u00, rf0u, m=1, rk=0): rf0u += nu * u00'' (cross.f90:666-672), then
+      // RK accumulate, update and zeta store (cross.f90:703-756)
+      solve_line(mu, 2, ybuf, ys, N, V2, T2, one, one, c, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6],
+                 false, [&](int j, double x) {
+                   const double rf = mrf[2 * j] + nu * (-(0.0 * mu[2 * j]) + x);
+                   double wk = (rk == 0) ? gk * rf : mwk[2 * j] + gk * rf;
+                   const double un = mu[2 * j] + Dt * wk;
+                   if (rk < 2) wk = rf * zk;
+                   if (active) {
+                     mu[2 * j] = un;
+                     mwk[2 * j] = wk;
+                   }
+                 });
+    }
+    if (mode == 0 || next) {
+      // derivyc(u00, rf0u, 1, 1, 0) used by hvhg (cross.f90:1186-1192)
+      solve_line(mu, 2, ybuf, ys, N, V1, T1, one, one, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true,
+                 [&](int j, double x) {
+                   if (active) mdu[2 * j] = x;
+                 });
+    }
+    return;
+  }
+
+  const long off = (long)b * g.field + 2 * lc + c;
+  const long ps = g.plane;
+  double *vor = bf.vor + off, *phi = bf.phi + off, *vorwk = bf.vorwk + off,
+         *phiwk = bf.phiwk + off, *G = bf.G + off, *Vv = bf.V + off, *D = bf.D + off;
+  const bool is00 = (i == 0 && k == 0);
+  const double a = g.alp * i;
+  const int kzs = (k <= g.nz) ? k : k - g.mz;
+  const double gz = g.gam * kzs;
+  const double k2 = a * a + gz * gz;
+  const double *sho = bf.sh_old + (long)b * 4 * g.nkx;
+  const double *shn = bf.sh_new + (long)b * 4 * g.nkx;
+  const FacView VH(bf.hz, lc);
+
+  if (mode == 0) {
+    // set_conj on the state for kx = 0 (operators.f90:1382-1429)
+    if (i == 0 && k > g.nz) {
+      const long src = (long)b * g.field + 2 * (long)((g.mz - k) * g.nkx) + c;
+      for (int j = 0; j < N; j++) {
+        double vv = bf.vor[src + (long)j * ps], pp = bf.phi[src + (long)j * ps];
+        if (active) {
+          vor[(long)j * ps] = c ? -vv : vv;
+          phi[(long)j * ps] = c ? -pp : pp;
+        }
+      }
+    }
+    const cd shp = ldc(sho + 2 * i), shm = ldc(sho + 2 * (g.nkx + i));
+    const Tail TH = make_tail(VH, shp, N), T1 = make_tail(V1, shp, N);
+    // v = lapcdy(phi) (cross.f90:408-426); hg(0,0) stays zero
+    solve_line(phi, ps, ybuf, ys, N, VH, TH, shp, shm, c, g.pr2[3], g.pr2[4], g.pr2[5], g.pr2[6],
+               false, [&](int j, double x) {
+                 if (active) G[(long)j * ps] = is00 ? 0.0 : x;
+               });
+    solve_line(vor, ps, ybuf, ys, N, V1, T1, shp, shm, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true,
+               [&](int j, double x) {
+                 if (active) D[(long)j * ps] = x;
+               });
+    solve_line(G, ps, ybuf, ys, N, V1, T1, shp, shm, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true,
+               [&](int j, double x) {
+                 if (active) Vv[(long)j * ps] = x;
+               });
+    return;
+  }
+
+  const int rk = mode - 1;
+  const double gk = kGama[rk], zk = kZeta[rk];
+  const cd shpo = ldc(sho + 2 * i), shmo = ldc(sho + 2 * (g.nkx + i));
+  const cd shpn = ldc(shn + 2 * i), shmn = ldc(shn + 2 * (g.nkx + i));
+  const double *mf1 = bf.mf1 + (long)b * 2 * N * g.nkx + 2 * i;
+  const double *mf2 = bf.mf2 + (long)b * 2 * N * g.nkx + 2 * i;
+  const double nuv = is00 ? 0.0 : nu;
+  {
+    // (1) dvordy <- d/dy of dH1/dx + dH3/dz  (cross.f90:565-575)
+    const Tail T1 = make_tail(V1, shpo, N);
+    solve_line(D, ps, ybuf, ys, N, V1, T1, shpo, shmo, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true,
+               [&](int j, double x) {
+                 if (active) D[(long)j * ps] = x;
+               });
+  }
+  const Tail T2 = make_tail(V2, shpo, N);
+  // (2) hg += nu*lap(vor) (visc3d), RK accumulate/update, zeta store + remap
+  solve_line(vor, ps, ybuf, ys, N, V2, T2, shpo, shmo, c, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6],
+             false, [&](int j, double x) {
+               const long q = (long)j * ps;
+               const double vo = vor[q];
+               const double hgp = G[q] + nuv * (-(k2 * vo) + x);
+               double wk = (rk == 0) ? gk * hgp : vorwk[q] + gk * hgp;
+               const double vn = vo + Dt * wk;
+               const cd m2 = ldc(mf2 + 2 * (long)j * g.nkx);
+               const double vnm = cmul_c(vn, __shfl_xor_sync(0xffffffffu, vn, 1), m2, c);
+               if (rk < 2) {
+                 const cd m1 = ldc(mf1 + 2 * (long)j * g.nkx);
+                 const double wz = hgp * zk;
+                 wk = cmul_c(wz, __shfl_xor_sync(0xffffffffu, wz, 1), m1, c);
+               }
+               if (active) {
+                 vor[q] = vnm;
+                 vorwk[q] = wk;
+               }
+             });
+  // (3) hv = hv - dvordy + nu*lap(phi), RK accumulate/update, zeta store + remap
+  solve_line(phi, ps, ybuf, ys, N, V2, T2, shpo, shmo, c, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6],
+             false, [&](int j, double x) {
+               const long q = (long)j * ps;
+               const double ph = phi[q];
+               const double hvp = (Vv[q] - D[q]) + nuv * (-(k2 * ph) + x);
+               double wk = (rk == 0) ? gk * hvp : phiwk[q] + gk * hvp;
+               const double pn = ph + Dt * wk;
+               const cd m2 = ldc(mf2 + 2 * (long)j * g.nkx);
+               const double pnm = cmul_c(pn, __shfl_xor_sync(0xffffffffu, pn, 1), m2, c);
+               if (rk < 2) {
+                 const cd m1 = ldc(mf1 + 2 * (long)j * g.nkx);
+                 const double wz = hvp * zk;
+                 wk = cmul_c(wz, __shfl_xor_sync(0xffffffffu, wz, 1), m1, c);
+               }
+               if (active) {
+                 phi[q] = pnm;
+                 phiwk[q] = wk;
+               }
+             });
+  // (4) v = lapcdy(phi) with the shear phase at t + c_k dt (cross.f90:784-795)
+  {
+    const Tail TH = make_tail(VH, shpn, N);
+    solve_line(phi, ps, ybuf, ys, N, VH, TH, shpn, shmn, c, g.pr2[3], g.pr2[4], g.pr2[5],
+               g.pr2[6], false, [&](int j, double x) {
+                 if (active && !is00) G[(long)j * ps] = x;
+               });
+  }
+  if (next) {
+    // (5) derivatives the next substep starts from (cross.f90:434-445)
+    const Tail T1 = make_tail(V1, shpn, N);
+    solve_line(vor, ps, ybuf, ys, N, V1, T1, shpn, shmn, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6],
+               true, [&](int j, double x) {
+                 if (active) D[(long)j * ps] = x;
+               });
+    solve_line(G, ps, ybuf, ys, N, V1, T1, shpn, shmn, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true,
+               [&](int j, double x) {
+                 if (active) Vv[(long)j * ps] = x;
+               });
+  }
+}
+
+// ---------------------------------------------------------------------------
+// plane stage 1: reconstruction + backward z-transforms
+// ---------------------------------------------------------------------------
+// k index -> position on the padded z grid (fill00)
+__device__ __forceinline__ int kgrid(int k, int nz, int NZ, int mz) { return k <= nz ? k : k + (NZ - mz); }
+
+template <int NZ, int CB, int T>
+__global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
+  const int cb = blockIdx.x, j = blockIdx.y, b = blockIdx.z;
+  Member &M = bf.mem[b];
+  if (M.halted) return;
+  extern __shared__ double2 smem[];
+  double2 *A = smem, *Bs = smem + 2 * CB * NZ;
+  const int nkx = g.nkx, mz = g.mz, nz = g.nz;
+  const int i0 = cb * CB;
+  const long pbase = (long)b * g.field + (long)j * g.plane;
+  const double2 *vor = (const double2 *)(bf.vor + pbase);
+  const double2 *phi = (const double2 *)(bf.phi + pbase);
+  const double2 *Dv = (const double2 *)(bf.D + pbase);
+  const double2 *Vv = (const double2 *)(bf.V + pbase);
+  const double2 *Gv = (const double2 *)(bf.G + pbase);
+  const double2 mu = ((const double2 *)bf.mu)[(long)b * g.my + j];
+  const double2 mdu = ((const double2 *)bf.mdu)[(long)b * g.my + j];
+  const double s = g.s;
+  // omega_y and phi with the kx=0 conjugate symmetry imposed (set_conj on the
+  // copies buff1/buff2, cross.f90:493-502)
+  auto ld_sym = [&](const double2 *p, int i, int k) -> double2 {
+    if (i == 0 && k > nz) {
+      double2 v = p[(mz - k) * nkx];
+      v.y = -v.y;
+      return v;
+    }
+    return p[k * nkx + i];
+  };
+  const bool do_hist = (rk == 1) && M.ihist;
+  if (do_hist) {
+    double acc[SB_NHIST_Q];
+#pragma unroll
+    for (int q = 0; q < SB_NHIST_Q; q++) acc[q] = 0.0;
+    for (int idx = threadIdx.x; idx < CB * mz; idx += T) {
+      const int ci = idx % CB, k = idx / CB, i = i0 + ci;
+      if (i >= nkx) continue;
+      const double a = g.alp * i;
+      const int kzs = (k <= nz) ? k : k - mz;
+      const double gz = g.gam * kzs;
+      const double Kk = a * a + gz * gz;
+      const double iK = bf.kinv[k * nkx + i];
+      const double2 ph = ld_sym(phi, i, k), vr = ld_sym(vor, i, k);
+      const double2 w1 = Dv[k * nkx + i], dv = Vv[k * nkx + i];
+      double2 u1, u2, u3, o1, o3;
+      if (i == 0 && k == 0) {
+        u1 = make_double2(mu.x, 0.0);
+        u3 = make_double2(mu.y, 0.0);
+        o3 = make_double2(-mdu.x, 0.0);
+        o1 = make_double2(mdu.y, 0.0);
+        u2 = make_double2(M.vbulk, 0.0);
+      } else {
+        double tx, ty;
+        tx = gz * w1.x - a * ph.x; ty = gz * w1.y - a * ph.y;
+        o3 = make_double2(-ty * iK, tx * iK);
+        tx = a * w1.x + gz * ph.x; ty = a * w1.y + gz * ph.y;
+        o1 = make_double2(-ty * iK, tx * iK);
+        tx = gz * dv.x + a * vr.x; ty = gz * dv.y + a * vr.y;
+        u3 = make_double2(-ty * iK, tx * iK);
+        tx = a * dv.x - gz * vr.x; ty = a * dv.y - gz * vr.y;
+        u1 = make_double2(-ty * iK, tx * iK);
+        u2 = Gv[k * nkx + i];
+      }
+      const double2 o2 = vr;
+      const double w = (i == 0) ? 1.0 : 2.0;
+      const double uu = u1.x * u1.x + u1.y * u1.y, vv = u2.x * u2.x + u2.y * u2.y,
+                   ww = u3.x * u3.x + u3.y * u3.y;
+      acc[0] += w * uu;
+      acc[1] += w * vv;
+      acc[2] += w * ww;
+      acc[3] += w * (u1.x * u2.x + u1.y * u2.y);
+      acc[4] += w * (u1.x * u3.x + u1.y * u3.y);
+      acc[5] += w * (u2.x * u3.x + u2.y * u3.y);
+      acc[6] += w * (o1.x * o1.x + o1.y * o1.y);
+      acc[7] += w * (o2.x * o2.x + o2.y * o2.y);
+      acc[8] += w * (o3.x * o3.x + o3.y * o3.y);
+      acc[9] += w * (o1.x * o2.x + o1.y * o2.y);
+      // dissipation (cross.f90:1926-1944); omega_z of the mean includes -s
+      double2 o3s = o3;
+      if (i == 0 && k == 0) o3s.x -= s;
+      const double c1x = o1.x - gz * u2.y, c1y = o1.y + gz * u2.x;  // o1 + i gz u2
+      const double c3x = o3s.x + a * u2.y, c3y = o3s.y - a * u2.x;  // o3 - i a u2
+      acc[10] += w * (Kk * (uu + vv + ww) + (dv.x * dv.x + dv.y * dv.y) +
+                      (c1x * c1x + c1y * c1y) + (c3x * c3x + c3y * c3y));
+    }
+    // block reduction (deterministic: fixed tree)
+    __shared__ double red[SB_NHIST_Q][T / 32];
+#pragma unroll
+    for (int q = 0; q < SB_NHIST_Q; q++) {
+      double v = acc[q];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < SB_NHIST_Q) {
+      double v = 0.0;
+      for (int w = 0; w < T / 32; w++) v += red[threadIdx.x][w];
+      bf.hpart[(((long)b * g.my + j) * g.ncb + cb) * SB_NHIST_Q + threadIdx.x] = v;
+    }
+  }
+  double2 *zb = (double2 *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * 6 * nkx;
+  for (int round = 0; round < 3; round++) {
+    // fill two fields (zero the 2/3-rule gap) on the padded z grid
+    for (int idx = threadIdx.x; idx < 2 * CB * NZ; idx += T) A[idx] = make_double2(0.0, 0.0);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < CB * mz; idx += T) {
+      const int ci = idx % CB, k = idx / CB, i = i0 + ci;
+      if (i >= nkx) continue;
+      const int kg = kgrid(k, nz, NZ, mz);
+      const double a = g.alp * i;
+      const int kzs = (k <= nz) ? k : k - mz;
+      const double gz = g.gam * kzs;
+      const double iK = bf.kinv[k * nkx + i];
+      double2 fa, fb;
+      const bool z00 = (i == 0 && k == 0);
+      if (round == 0) {  // u (f=0) and w (f=1) from dv/dy and omega_y
+        if (z00) {
+          fa = make_double2(mu.x, 0.0);
+          fb = make_double2(mu.y, 0.0);
+        } else {
+          const double2 dv = Vv[k * nkx + i], vr = ld_sym(vor, i, k);
+          double tx = a * dv.x - gz * vr.x, ty = a * dv.y - gz * vr.y;
+          fa = make_double2(-ty * iK, tx * iK);
+          tx = gz * dv.x + a * vr.x; ty = gz * dv.y + a * vr.y;
+          fb = make_double2(-ty * iK, tx * iK);
+        }
+      } else if (round == 1) {  // omega_x (f=2) and omega_z (f=3) from d(omega_y)/dy and phi
+        if (z00) {
+          fa = make_double2(mdu.y, 0.0);
+          fb = make_double2(-mdu.x, 0.0);
+        } else {
+          const double2 w1 = Dv[k * nkx + i], ph = ld_sym(phi, i, k);
+          double tx = a * w1.x + gz * ph.x, ty = a * w1.y + gz * ph.y;
+          fa = make_double2(-ty * iK, tx * iK);
+          tx = gz * w1.x - a * ph.x; ty = gz * w1.y - a * ph.y;
+          fb = make_double2(-ty * iK, tx * iK);
+        }
+      } else {  // v (f=4) and omega_y (f=5)
+        fa = z00 ? make_double2(M.vbulk, 0.0) : Gv[k * nkx + i];
+        fb = ld_sym(vor, i, k);
+      }
+      A[ci * NZ + kg] = fa;
+      A[(CB + ci) * NZ + kg] = fb;
+    }
+    double2 *res = fft_batch<NZ, +1, 2 * CB, T>(A, Bs, (const double2 *)bf.twz);
+    // store Zbuf[z][f][i]
+    for (int idx = threadIdx.x; idx < 2 * CB * NZ; idx += T) {
+      const int ci = idx % CB, rem = idx / CB;
+      const int z = rem % NZ, f = rem / NZ;
+      const int i = i0 + ci;
+      if (i < nkx) zb[((long)z * 6 + 2 * round + f) * nkx + i] = res[(f * CB + ci) * NZ + z];
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// plane stage 2: x-transforms and u x omega on pairs of z rows
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long dbits(double v) {
+  return (unsigned long long)__double_as_longlong(fabs(v));
+}
+
+template <int NX, int T>
+__global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
+  const int zp = blockIdx.x, j = blockIdx.y, b = blockIdx.z;
+  Member &M = bf.mem[b];
+  if (M.halted) return;
+  extern __shared__ double2 smem[];
+  double2 *A = smem, *Bs = smem + 6 * NX;
+  const int nkx = g.nkx, NZ = g.mgalz;
+  const int z = 2 * zp;
+  const double2 *zb = (const double2 *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * 6 * nkx;
+  // Hermitian extension of two rows into one complex sequence (c2r of both rows
+  // at once); FFTW's c2r ignores the imaginary part of the kx = 0 entry
+  for (int idx = threadIdx.x; idx < 6 * NX; idx += T) A[idx] = make_double2(0.0, 0.0);
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 6 * nkx; idx += T) {
+    const int f = idx / nkx, i = idx - f * nkx;
+    double2 X1 = zb[((long)z * 6 + f) * nkx + i];
+    double2 X2 = zb[((long)(z + 1) * 6 + f) * nkx + i];
+    if (i == 0) {
+      X1.y = 0.0;
+      X2.y = 0.0;
+    }
+    A[f * NX + i] = make_double2(X1.x - X2.y, X1.y + X2.x);
+    if (i > 0) A[f * NX + NX - i] = make_double2(X1.x + X2.y, -X1.y + X2.x);
+  }
+  double2 *P = fft_batch<NX, +1, 6, T>(A, Bs, (const double2 *)bf.twx);
+  double2 *Q = (P == A) ? Bs : A;
+  // fields: 0 u, 1 w, 2 omega_x, 3 omega_z, 4 v, 5 omega_y
+  const double chi2 = 2.0 * g.chi;
+  const double sy = g.s * ((double)j * g.dy - 0.5 * g.Ly);
+  unsigned long long m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+  for (int x = threadIdx.x; x < NX; x += T) {
+    const double2 u1 = P[0 * NX + x], u3 = P[1 * NX + x], o1 = P[2 * NX + x], o3 = P[3 * NX + x],
+                  u2 = P[4 * NX + x], o2 = P[5 * NX + x];
+    if (rk == 1) {
+      m0 = max(m0, max(dbits(u1.x), dbits(u1.y)));
+      m1 = max(m1, max(dbits(u1.x + sy), dbits(u1.y + sy)));
+      m2 = max(m2, max(dbits(u2.x), dbits(u2.y)));
+      m3 = max(m3, max(dbits(u3.x), dbits(u3.y)));
+    }
+    double2 h1, h2, h3;
+    h1.x = u2.x * (o3.x + chi2) - u3.x * o2.x;
+    h1.y = u2.y * (o3.y + chi2) - u3.y * o2.y;
+    h2.x = u3.x * o1.x - u1.x * (o3.x + chi2);
+    h2.y = u3.y * o1.y - u1.y * (o3.y + chi2);
+    h3.x = u1.x * o2.x - u2.x * o1.x;
+    h3.y = u1.y * o2.y - u2.y * o1.y;
+    Q[0 * NX + x] = h1;
+    Q[1 * NX + x] = h2;
+    Q[2 * NX + x] = h3;
+  }
+  if (rk == 1) {
+    for (int o = 16; o > 0; o >>= 1) {
+      m0 = max(m0, __shfl_xor_sync(0xffffffffu, m0, o));
+      m1 = max(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+      m2 = max(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+      m3 = max(m3, __shfl_xor_sync(0xffffffffu, m3, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMax(&M.umax_bits[0], m0);
+      atomicMax(&M.umax_bits[1], m1);
+      atomicMax(&M.umax_bits[2], m2);
+      atomicMax(&M.umax_bits[3], m3);
+    }
+  }
+  double2 *R = fft_batch<NX, -1, 3, T>(Q, P, (const double2 *)bf.twx);
+  double2 *xb = (double2 *)bf.xbuf + ((long)b * g.my + j) * (long)NZ * 3 * nkx;
+  for (int idx = threadIdx.x; idx < 3 * nkx; idx += T) {
+    const int f = idx / nkx, i = idx - f * nkx;
+    const double2 zk = R[f * NX + i];
+    double2 zm = R[f * NX + ((NX - i) % NX)];
+    zm.y = -zm.y;
+    const double sx = zk.x + zm.x, syy = zk.y + zm.y, dx = zk.x - zm.x, dy = zk.y - zm.y;
+    xb[((long)z * 3 + f) * nkx + i] = make_double2(0.5 * sx, 0.5 * syy);
+    xb[((long)(z + 1) * 3 + f) * nkx + i] = make_double2(0.5 * dy, -0.5 * dx);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// plane stage 3: forward z-transforms, truncation and right-hand sides
+// ---------------------------------------------------------------------------
+template <int NZ, int CB, int T>
+__global__ void __launch_bounds__(T) k_p3(Grid g, Bufs bf) {
+  const int cb = blockIdx.x, j = blockIdx.y, b = blockIdx.z;
+  Member &M = bf.mem[b];
+  if (M.halted) return;
+  extern __shared__ double2 smem[];
+  double2 *A = smem, *Bs = smem + 3 * CB * NZ;
+  const int nkx = g.nkx, mz = g.mz, nz = g.nz;
+  const int i0 = cb * CB;
+  const double2 *xb = (const double2 *)bf.xbuf + ((long)b * g.my + j) * (long)NZ * 3 * nkx;
+  for (int idx = threadIdx.x; idx < 3 * CB * NZ; idx += T) {
+    const int ci = idx % CB, rem = idx / CB;
+    const int f = rem % 3, z = rem / 3;
+    const int i = i0 + ci;
+    A[(f * CB + ci) * NZ + z] = (i < nkx) ? xb[((long)z * 3 + f) * nkx + i] : make_double2(0.0, 0.0);
+  }
+  double2 *P = fft_batch<NZ, -1, 3 * CB, T>(A, Bs, (const double2 *)bf.twz);
+  const long pbase = (long)b * g.field + (long)j * g.plane;
+  double2 *Dv = (double2 *)(bf.D + pbase);
+  double2 *Gv = (double2 *)(bf.G + pbase);
+  double2 *Vv = (double2 *)(bf.V + pbase);
+  const double norm = 1.0 / (double)(g.mgalx * g.mgalz);
+  const double s = g.s;
+  for (int idx = threadIdx.x; idx < CB * mz; idx += T) {
+    const int ci = idx % CB, k = idx / CB, i = i0 + ci;
+    if (i >= nkx) continue;
+    const int kg = kgrid(k, nz, NZ, mz);
+    double2 H1 = P[(0 * CB + ci) * NZ + kg], H2 = P[(1 * CB + ci) * NZ + kg],
+            H3 = P[(2 * CB + ci) * NZ + kg];
+    H1.x *= norm; H1.y *= norm;
+    H2.x *= norm; H2.y *= norm;
+    H3.x *= norm; H3.y *= norm;
+    const double a = g.alp * i;
+    const int kzs = (k <= nz) ? k : k - mz;
+    const double gz = g.gam * kzs;
+    const double Kk = a * a + gz * gz;
+    const long q = (long)k * nkx + i;
+    const double2 v = Gv[q];
+    // dvordy = i a H1 + i gz H3
+    double tx = a * H1.x + gz * H3.x, ty = a * H1.y + gz * H3.y;
+    Dv[q] = make_double2(-ty, tx);
+    // hg = -i a H3 + i gz (H1 - s v)
+    tx = gz * (H1.x - s * v.x) - a * H3.x;
+    ty = gz * (H1.y - s * v.y) - a * H3.y;
+    Gv[q] = make_double2(-ty, tx);
+    // hv = -(kx^2 + kz^2) H2
+    Vv[q] = make_double2(-(Kk * H2.x), -(Kk * H2.y));
+    if (i == 0 && k == 0) ((double2 *)bf.mrf)[(long)b * g.my + j] = make_double2(H1.x, H3.x);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// per-box scalar work: Delta t, statistics record, offsets and phase tables
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_phase(Grid g, Bufs bf, int rk) {
+  const int b = blockIdx.x;
+  Member &M = bf.mem[b];
+  __shared__ double s_xb, s_xt, s_xnb, s_xnt, s_f1, s_f2;
+  __shared__ double s_q[SB_NHIST_Q + 1];
+  __shared__ int s_halt;
+  if (threadIdx.x == 0) {
+    if (rk == 0) {  // entry of a cross() call (cross.f90:76-113)
+      M.istop = 0;
+      M.idump = 0;
+      M.halted = 0;
+      M.istep = 1;
+      M.ihist = 1;
+      M.ntrace = 0;
+      M.flags = 0;
+      for (int q = 0; q < 4; q++) M.umax_bits[q] = 0ull;
+    }
+    s_halt = M.halted;
+  }
+  __syncthreads();
+  if (s_halt) return;
+  const bool shear = fabs(g.s) > 0.01;
+  if (rk == 1 && M.ihist) {
+    // hist 'w': sums over planes of the per-block partials (cross.f90:2070-2080)
+    const int q = threadIdx.x;
+    if (q < SB_NHIST_Q) {
+      double tot = 0.0;
+      for (int j = 0; j < g.my; j++) {
+        double pl = 0.0;
+        for (int cb = 0; cb < g.ncb; cb++) pl += bf.hpart[(((long)b * g.my + j) * g.ncb + cb) * SB_NHIST_Q + q];
+        tot += pl;
+      }
+      s_q[q] = tot;
+    } else if (q == SB_NHIST_Q) {
+      // production P_k = -<omega_z>(-uv) + <omega_z>^2/Re per plane, with the
+      // mean shear -s included in <omega_z> (cross.f90:1901-1912)
+      double tot = 0.0;
+      for (int j = 0; j < g.my; j++) {
+        double uvr = 0.0;
+        for (int cb = 0; cb < g.ncb; cb++) uvr += bf.hpart[(((long)b * g.my + j) * g.ncb + cb) * SB_NHIST_Q + 3];
+        const double o3 = -bf.mdu[2 * ((long)b * g.my + j)] - g.s;
+        tot += -o3 * (-uvr) + (o3 * o3) * (1.0 / M.Re);
+      }
+      s_q[q] = tot;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (rk == 0 || rk == 1) {
+      M.xwkb = M.xoffb;
+      M.xwkt = M.xofft;
+    } else {
+      M.xwkb = M.xwkb_n;
+      M.xwkt = M.xwkt_n;
+    }
+    if (rk == 1) {
+      // umax (cross.f90:1205-1216,1436-1442) and Delta t (cross.f90:1598-1711)
+      double uinit = 0.0;
+      if (M.istep == 1 && M.readflag == 0) uinit = (fabs(g.s) > 0.5) ? 1.0 : M.uprim;
+      for (int q = 0; q < 4; q++) {
+        const double v = __longlong_as_double((long long)M.umax_bits[q]);
+        M.umax[q] = v > uinit ? v : uinit;
+      }
+      double dt;
+      if (M.fixed_dt > 0.0) {
+        dt = M.fixed_dt;
+        const double m = fmax(fmax(M.umax[0] * g.pi / g.dx, M.umax[2] * 2.5 / g.dy), M.umax[3] * g.pi / g.dz);
+        M.CFLcur = dt * m;
+        const double vv = fmax(fmax(g.pi * g.pi / g.dx / g.dx, 6.25 / g.dy / g.dy), g.pi * g.pi / g.dz / g.dz);
+        M.CFLv = (1.0 / M.Re) * dt * vv;
+      } else {
+        const double m = fmax(fmax(M.umax[0] * M.cflx, M.umax[2] * M.cfly), M.umax[3] * M.cflz);
+        dt = 1.0 / m;
+        M.CFLcur = M.CFL;
+        M.CFLv = M.CFL * M.cflvv * dt;
+        if (M.CFLv > M.CFL) dt = 1.0 / M.cflvv;
+      }
+      double Deltat = dt;
+      if (Deltat < 1e-10) {
+        M.istop = 1;
+        M.flags |= SBF_DIVERGED;
+      }
+      if ((M.time + Deltat) > M.dumptime) {
+        Deltat = fabs(M.dumptime - M.time);
+        if (M.dumptime > (M.etime - 1e-13)) {
+          M.istop = 1;
+          M.flags |= SBF_ETIME;
+        }
+        M.dumptime = M.dumptime + M.dtimag;
+        M.idump = 1;
+      } else if ((M.time + Deltat) > M.etime) {
+        Deltat = fabs(M.etime - M.time);
+        M.istop = 1;
+        M.flags |= SBF_ETIME;
+      }
+      M.Deltat = Deltat;
+      if (M.ihist) {
+        double uner[10], uner2[4];
+        const double my = (double)g.my;
+        for (int q = 0; q < 3; q++) uner[q] = sqrt(fabs(s_q[q] / my));
+        for (int q = 3; q < 6; q++) uner[q] = s_q[q] / my;
+        for (int q = 6; q < 9; q++) uner[q] = sqrt(fabs(s_q[q] / my));
+        uner[9] = s_q[10] / my;
+        uner2[0] = s_q[SB_NHIST_Q] / my;
+        uner2[1] = s_q[9] / my;
+        uner2[2] = 0.0;
+        uner2[3] = 0.0;
+        if (M.ntrace < M.trace_cap) {
+          double *rec = bf.trace + ((long)b * M.trace_cap + M.ntrace) * SB_TRACE_LEN;
+          rec[0] = M.time;
+          rec[1] = M.Deltat;
+          for (int q = 0; q < 10; q++) rec[2 + q] = uner[q];
+          rec[12] = M.CFLcur;
+          rec[13] = M.CFLv;
+          rec[14] = M.umax[1];
+          rec[15] = M.umax[2];
+          rec[16] = M.umax[3];
+          rec[17] = M.xoffb;
+          rec[18] = M.xofft;
+          rec[19] = M.umax[0];
+          for (int q = 0; q < 4; q++) rec[20 + q] = uner2[q];
+        }
+        M.ntrace++;
+        if (isnan(uner[0])) {
+          M.istop = 1;
+          M.flags |= SBF_NAN;
+        }
+        if (uner[1] / (2.0 * g.pi / g.gam) < 1e-5) {
+          M.istop = 1;
+          M.flags |= SBF_LAMINAR;
+        }
+        M.ihist = 0;
+      }
+    }
+    if (rk >= 1) {
+      const double Dt = M.Deltat;
+      const double r1 = kCa[rk - 1] * Dt;
+      if (shear) {
+        M.xwkb_n = M.xoffb + r1 * (g.s * (-g.Ly));
+        M.xwkt_n = M.xofft + r1 * (g.s * g.Ly);
+      } else {
+        M.xwkb_n = M.xwkb;
+        M.xwkt_n = M.xwkt;
+      }
+      s_f1 = (rk == 1) ? -(kGama[0] * Dt * g.s) : -((kGama[1] + kZeta[0]) * Dt * g.s);
+      s_f2 = (rk == 1) ? -(g.s * r1) : -(g.s * (kCa[rk - 1] - kCa[rk - 2]) * Dt);
+      s_xnb = M.xwkb_n;
+      s_xnt = M.xwkt_n;
+    }
+    s_xb = M.xwkb;
+    s_xt = M.xwkt;
+  }
+  __syncthreads();
+  const int nkx = g.nkx;
+  double *sho = bf.sh_old + (long)b * 4 * nkx;
+  double *shn = bf.sh_new + (long)b * 4 * nkx;
+  for (int i = threadIdx.x; i < nkx; i += blockDim.x) {
+    const double a = g.alp * i;
+    double sn, cs;
+    if (shear) {
+      sincos((-a) * s_xt, &sn, &cs);
+      sho[2 * i] = cs; sho[2 * i + 1] = sn;
+      sincos((-a) * s_xb, &sn, &cs);
+      sho[2 * (nkx + i)] = cs; sho[2 * (nkx + i) + 1] = sn;
+    } else {
+      sho[2 * i] = 1.0; sho[2 * i + 1] = 0.0;
+      sho[2 * (nkx + i)] = 1.0; sho[2 * (nkx + i) + 1] = 0.0;
+    }
+    if (rk >= 1) {
+      if (shear) {
+        sincos((-a) * s_xnt, &sn, &cs);
+        shn[2 * i] = cs; shn[2 * i + 1] = sn;
+        sincos((-a) * s_xnb, &sn, &cs);
+        shn[2 * (nkx + i)] = cs; shn[2 * (nkx + i) + 1] = sn;
+      } else {
+        shn[2 * i] = 1.0; shn[2 * i + 1] = 0.0;
+        shn[2 * (nkx + i)] = 1.0; shn[2 * (nkx + i) + 1] = 0.0;
+      }
+    }
+  }
+  if (rk >= 1) {
+    // moving_frame phases exp(i kx y_j tau) (operators.f90:119-123)
+    double *m1 = bf.mf1 + (long)b * 2 * g.my * nkx;
+    double *m2 = bf.mf2 + (long)b * 2 * g.my * nkx;
+    for (int q = threadIdx.x; q < g.my * nkx; q += blockDim.x) {
+      const int jj = q / nkx, i = q - jj * nkx;
+      const double ay = (g.alp * i) * ((double)jj * g.dy - 0.5 * g.Ly);
+      double sn, cs;
+      if (rk < 3) {
+        sincos(ay * s_f1, &sn, &cs);
+        m1[2 * q] = cs; m1[2 * q + 1] = sn;
+      }
+      sincos(ay * s_f2, &sn, &cs);
+      m2[2 * q] = cs; m2[2 * q + 1] = sn;
+    }
+  }
+}
+
+// end of a step: offsets, time, next-step flags (cross.f90:1002-1013, 336-376)
+__global__ void k_finish(Grid g, Bufs bf) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.B) return;
+  Member &M = bf.mem[b];
+  if (M.halted) return;
+  M.xoffb = M.xwkb_n;
+  M.xofft = M.xwkt_n;
+  M.time = M.time + M.Deltat;
+  M.istep += 1;
+  if ((M.istep - 1) != 1 && M.istop) M.halted = 1;
+  if ((M.istep - 1) % M.nhist == 0) M.ihist = 1;
+  for (int q = 0; q < 4; q++) M.umax_bits[q] = 0ull;
+}
+
+// pencil (j fastest, then kx, then kz) <-> plane-major layout, one box
+__global__ void k_pencil_to_plane(Grid g, const double *__restrict__ pen, double *__restrict__ dst) {
+  const long n = (long)g.my * g.nkx * g.mz;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.nkx);
+    const int k = (int)((t / g.nkx) % g.mz);
+    const int j = (int)(t / ((long)g.nkx * g.mz));
+    const long src = 2 * (((long)k * g.nkx + i) * g.my + j);
+    dst[2 * t] = pen[src];
+    dst[2 * t + 1] = pen[src + 1];
+  }
+}
+__global__ void k_plane_to_pencil(Grid g, const double *__restrict__ src, double *__restrict__ pen) {
+  const long n = (long)g.my * g.nkx * g.mz;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int j = (int)(t % g.my);
+    const int i = (int)((t / g.my) % g.nkx);
+    const int k = (int)(t / ((long)g.my * g.nkx));
+    const long s = 2 * (((long)j * g.mz + k) * g.nkx + i);
+    pen[2 * t] = src[s];
+    pen[2 * t + 1] = src[s + 1];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launch helpers
+// ---------------------------------------------------------------------------
+template <int NZ, int CB, int T>
+static cudaError_t launch_p13(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, int which,
+                              bool prep) {
+  dim3 grid(g.ncb, g.my, g.B);
+  const size_t sm1 = sizeof(double2) * 2 * (2 * CB * NZ);
+  const size_t sm3 = sizeof(double2) * 2 * (3 * CB * NZ);
+  if (prep) {
+    cudaFuncSetAttribute(k_p1<NZ, CB, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+    cudaFuncSetAttribute(k_p3<NZ, CB, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+    return cudaGetLastError();
+  }
+  if (which == 1)
+    k_p1<NZ, CB, T><<<grid, T, sm1, st>>>(g, bf, rk);
+  else
+    k_p3<NZ, CB, T><<<grid, T, sm3, st>>>(g, bf);
+  return cudaGetLastError();
+}
+
+template <int NX, int T>
+static cudaError_t launch_p2(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, bool prep) {
+  dim3 grid(g.mgalz / 2, g.my, g.B);
+  const size_t sm = sizeof(double2) * 2 * (6 * NX);
+  if (prep) {
+    cudaFuncSetAttribute(k_p2<NX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    return cudaGetLastError();
+  }
+  k_p2<NX, T><<<grid, T, sm, st>>>(g, bf, rk);
+  return cudaGetLastError();
+}
+
+int plane_cb(int mgalz) { return mgalz > 96 ? 8 : 16; }
+
+// stage 1..3: launch; stage 0: set the kernels' shared-memory limits (once)
+cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
+  const bool prep = (stage == 0);
+  if (stage == 2 || prep) {
+    cudaError_t e;
+    switch (g.mgalx) {
+      case 32: e = launch_p2<32, 64>(g, bf, rk, st, prep); break;
+      case 48: e = launch_p2<48, 64>(g, bf, rk, st, prep); break;
+      case 64: e = launch_p2<64, 96>(g, bf, rk, st, prep); break;
+      case 96: e = launch_p2<96, 96>(g, bf, rk, st, prep); break;
+      case 192: e = launch_p2<192, 128>(g, bf, rk, st, prep); break;
+      case 384: e = launch_p2<384, 256>(g, bf, rk, st, prep); break;
+      default: return cudaErrorInvalidValue;
+    }
+    if (!prep || e != cudaSuccess) return e;
+  }
+  switch (g.mgalz) {
+    case 32: return launch_p13<32, 16, 128>(g, bf, rk, st, stage, prep);
+    case 48: return launch_p13<48, 16, 128>(g, bf, rk, st, stage, prep);
+    case 64: return launch_p13<64, 16, 128>(g, bf, rk, st, stage, prep);
+    case 96: return launch_p13<96, 16, 128>(g, bf, rk, st, stage, prep);
+    case 192: return launch_p13<192, 8, 128>(g, bf, rk, st, stage, prep);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_line(const Grid &g, const Bufs &bf, int mode, int next, cudaStream_t st) {
+  const long nth = (long)g.B * g.tpm;
+  const int T = 128;
+  k_line<<<(unsigned)((nth + T - 1) / T), T, 0, st>>>(g, bf, mode, next);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_phase(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  k_phase<<<g.B, 256, 0, st>>>(g, bf, rk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finish(const Grid &g, const Bufs &bf, cudaStream_t st) {
+  k_finish<<<(g.B + 127) / 128, 128, 0, st>>>(g, bf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pencil_to_plane(const Grid &g, const double *pen, double *dst, cudaStream_t st) {
+  k_pencil_to_plane<<<256, 256, 0, st>>>(g, pen, dst);
+  return cudaGetLastError();
+}
+cudaError_t launch_plane_to_pencil(const Grid &g, const double *src, double *pen, cudaStream_t st) {
+  k_plane_to_pencil<<<256, 256, 0, st>>>(g, src, pen);
+  return cudaGetLastError();
+}
+
+bool supported_grid(int mgalx, int mgalz) {
+  const int xs[] = {32, 48, 64, 96, 192, 384};
+  const int zs[] = {32, 48, 64, 96, 192};
+  bool okx = false, okz = false;
+  for (int v : xs) okx |= (v == mgalx);
+  for (int v : zs) okz |= (v == mgalz);
+  return okx && okz;
+}
+
+}  // namespace sb

@@ -1,0 +1,16 @@
+// sb_kernels.h -- launch entry points of the device kernels (internal).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sb_common.cuh"
+
+namespace sb {
+int plane_cb(int mgalz);
+bool supported_grid(int mgalx, int mgalz);
+cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st);
+cudaError_t launch_line(const Grid &g, const Bufs &bf, int mode, int next, cudaStream_t st);
+cudaError_t launch_phase(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
+cudaError_t launch_finish(const Grid &g, const Bufs &bf, cudaStream_t st);
+cudaError_t launch_pencil_to_plane(const Grid &g, const double *pen, double *dst, cudaStream_t st);
+cudaError_t launch_plane_to_pencil(const Grid &g, const double *src, double *pen, cudaStream_t st);
+}  // namespace sb
