@@ -1,0 +1,357 @@
+"""Benchmark of the shearing-box RK3 step on GB300 (one JSON line on rank 0).
+
+Workload: one box of 192x96x96 (Lx:Ly:Lz = 2:1:1, Lz = 2pi, S = 1,
+Re_z = 4000, CFL = 0.5), FP64, seeded synthetic divergence-free field with
+E(k) ~ k^4 exp(-2 (k/k0)^2), k0 = 4, u_rms = 0.1 S Lz.  A "step" is one RK3
+step (three substeps) of that box.
+
+  value  steps/s of K consecutive steps with the state resident in HBM
+         (one sb_step call, CUDA events on the library's stream).
+  e2e    steps/s through the C-ABI drop-in sb_cross(nstep=1) with pinned host
+         buffers: host->device state, one step, device->host state, per step.
+  roofline  the dominant kernel (plane stage 2), timed alone with CUDA events:
+         FP64 rate against the FP64 FMA peak measured in the same run (the
+         binding roof on GB300) and bytes against the measured HBM copy peak.
+  cpu_baseline  the C oracle (restatement of the reference step) on the
+         host cores, a bounded sample of steps of the same workload.
+
+--impl reference times that CPU oracle alone (the reference Fortran cannot be
+built on this machine: no Fortran compiler, MPI, FFTW or HDF5).
+Multi-GPU: each rank advances its own box (replicas, no communication).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RK3 steps/s at 192x96x96 FP64 vs FP32-mixed (err vs FP64); batched Newton Jv/s"
+GRID = (192, 96, 96)
+GRIDS = {64: (64, 32, 32), 96: (96, 48, 48), 192: (192, 96, 96), 384: (384, 192, 192)}
+REZ = 4000.0
+LZ = 2 * np.pi
+
+
+def box_params():
+    return dict(mgalx=GRID[0], my=GRID[1], mgalz=GRID[2], Re=REZ / LZ ** 2, alp=0.5, Ly=LZ,
+                gam=1.0, s=1.0, chi=0.0, CFL=0.5)
+
+
+def config(extra=None):
+    c = {"workload": "shearing box 192x96x96 (Lx:Ly:Lz=2:1:1, Lz=2pi), Re_z=4000, CFL=0.5, "
+                     "1 box per GPU, FP64 RK3 step",
+         "grid": list(GRID), "boxes_per_gpu": 1, "seed": 3, "k0": 4.0,
+         "l2": "per-step working set ~156 MB (8 fields, transform buffers, line factors) "
+               "> 129 MB L2; no flush"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl"
+        dist.init_process_group(backend=backend)
+        return dist, rank, ws
+    return None, rank, ws
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev: int):
+        self.dev = dev
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.th.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) < 9:
+                continue
+            for q, nm in enumerate(names):
+                if r[5 + q].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def plane2_traffic():
+    """dram bytes per launch of plane stage 2 from the committed ncu summary
+    (profiles/k_p2_192x96x96.txt, line 'traffic_bytes_per_launch: N'), else None."""
+    path = os.path.join(ROOT, "profiles", "k_p2_192x96x96.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(nsteps_sample: int, threads: int):
+    """The C oracle on the host cores, a bounded sample of steps."""
+    import oracle
+    import shear_nnf_gb300 as sb
+    oracle.set_threads(threads)
+    pp = box_params()
+    st = sb.seed_state(sb.make_params(**pp), 3)
+    o = oracle.Oracle(**pp)
+    o.cross(st, 1)  # warm-up
+    t0 = time.perf_counter()
+    o.cross(st, nsteps_sample)
+    dt = time.perf_counter() - t0
+    return {"value": nsteps_sample / dt, "unit": "steps/s", "cores": threads, "kind": "port",
+            "sample": f"{nsteps_sample} consecutive FP64 steps of the 192x96x96 box "
+                      f"(C oracle, OpenMP, {threads} threads), after 1 warm-up step",
+            "seconds": dt}
+
+
+def run_reference(args):
+    dist, rank, ws = dist_setup()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n = max(1, min(args.steps, 20))
+    res = cpu_baseline(n, threads)
+    line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "steps/s",
+            "n_gpus": args.gpus, "steps": n, "warmup": args.warmup,
+            "ms_per_step": 1e3 / res["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config({"impl": "CPU oracle (C restatement of the reference step)"}),
+            "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": res["value"], "unit": "steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+
+    import shear_nnf_gb300 as sb
+    dist, rank, ws = dist_setup()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    torch.cuda.init()
+    pp = box_params()
+    p = sb.make_params(**pp)
+    st0 = sb.seed_state(p, 3 + rank)
+    box = sb.ShearBox(p)
+    box.set_state(st0)
+    stream = torch.cuda.ExternalStream(box.stream)
+    # warm-up
+    box.step(max(args.warmup, 1))
+    box.sync()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    barrier(dist)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    box.step(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    barrier(dist)
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    status = box.status()
+    ms_max = allmax(dist, ms)
+    steps_per_s = ws * args.steps / (ms_max * 1e-3)
+    launches = 16 * args.steps + 2
+    if args.lite:
+        # profiling runs (ncu): the timed steps only, no side measurements
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": steps_per_s, "unit": "steps/s",
+                              "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+                              "ms_per_step": ms_max / args.steps, "lite": True,
+                              "config": config({"grid": list(GRID)}), "gpu_launches": launches}))
+        return
+    # dominant kernel alone: plane stage 2 (x transforms + u x omega)
+    box.set_state(st0)
+    box.step(1)
+    box.sync()
+    nrep = 20
+    k0 = torch.cuda.Event(enable_timing=True)
+    k1 = torch.cuda.Event(enable_timing=True)
+    box.launch_stage(2, 2, 2)
+    k0.record(stream)
+    box.launch_stage(2, 2, nrep)
+    k1.record(stream)
+    k1.synchronize()
+    p2_ms = k0.elapsed_time(k1) / nrep
+    # line kernel alone, for the record
+    box.set_state(st0)
+    box.step(1)
+    box.sync()
+    k0.record(stream)
+    box.launch_stage(5, 2, 5)
+    k1.record(stream)
+    k1.synchronize()
+    line_ms = k0.elapsed_time(k1) / 5
+    fp64_peak = box.fp64_peak()
+    mgalx, my, mgalz = GRID
+    nkx = 2 * (mgalx // 3) // 2
+    # algorithmic work of plane stage 2 per launch: 9 complex FFTs of length
+    # mgalx per pair of z rows (5 N log2 N flops each), 12 flops per point of
+    # the cross product, per plane; bytes: read 6 and write 3 fields of
+    # (mgalz x nkx) complex per plane
+    fft_fl = 9 * 5 * mgalx * np.log2(mgalx) * (mgalz // 2)
+    prod_fl = 12 * mgalx * mgalz
+    p2_flops = my * (fft_fl + prod_fl)
+    p2_bytes = my * mgalz * nkx * 16 * (6 + 3)
+    hbm_peak, hbm_src = measured_peaks()
+    p2_tflops = p2_flops / (p2_ms * 1e-3) / 1e12
+    p2_gbs = p2_bytes / (p2_ms * 1e-3) / 1e9
+    traffic = plane2_traffic()
+    # end to end through the drop-in with pinned host buffers
+    nf = st0["vor"].size
+    pin = {}
+    for key in ("vor", "phi"):
+        t = torch.empty(2 * nf, dtype=torch.float64, pin_memory=True)
+        a = t.numpy().view(np.complex128).reshape(st0[key].shape)
+        a[...] = st0[key]
+        pin[key] = (t, a)
+    host = {"vor": pin["vor"][1], "phi": pin["phi"][1]}
+    for key in ("u00", "w00"):
+        t = torch.empty(my, dtype=torch.float64, pin_memory=True)
+        t.numpy()[:] = st0[key]
+        pin[key] = (t, t.numpy())
+        host[key] = t.numpy()
+    host.update(time=0.0, xoffb=0.0, xofft=0.0)
+    ne2e = max(3, min(args.steps, 20))
+    box.cross(host, 1)  # warm-up
+    torch.cuda.synchronize()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(ne2e):
+        box.cross(host, 1)
+    t1 = time.perf_counter()
+    barrier(dist)
+    e2e_s = allmax(dist, t1 - t0)
+    bytes_io = 2 * nf * 16 + 2 * my * 8 + 3 * 8
+    if rank != 0:
+        return
+    cpu = cpu_baseline(args.cpu_steps, os.cpu_count() or 1) if ws == 1 or rank == 0 else None
+    line = {
+        "metric": METRIC, "value": steps_per_s, "unit": "steps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded k^4 exp(-2(k/k0)^2) spectrum; no dataset in the reference)",
+        "config": config({"parallelism": f"replicas x{ws}", "mcell_steps_per_s":
+                          steps_per_s * mgalx * my * mgalz / 1e6,
+                          "status_after": {"istop": status.istop, "steps_done": status.steps_done,
+                                           "time": status.time}}),
+        "e2e": {"value": ws * ne2e / e2e_s, "unit": "steps/s",
+                "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io,
+                "api": "sb_cross(nstep=1), pinned host buffers"},
+        "gpu_launches": launches,
+        "roofline": {
+            "bound": "fp64", "kernel": "k_p2 (plane stage 2: x transforms, u x omega)",
+            "achieved": p2_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
+            "frac": p2_tflops / fp64_peak,
+            "peak_source": "FP64 FMA probe measured in this run (GB300 FP64 is the binding roof)",
+            "algorithmic_flops_per_launch": p2_flops, "launch_ms": p2_ms,
+            "hbm": {"achieved": p2_gbs, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": p2_gbs / hbm_peak, "peak_source": f"MEASURED_PEAKS.json ({hbm_src})",
+                    "algorithmic_bytes_per_launch": p2_bytes},
+            "traffic": traffic,
+            "line_kernel_ms": line_ms,
+        },
+        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--grid", type=int, default=192, choices=sorted(GRIDS),
+                    help="profiling only: run a different grid (the benchmark is 192)")
+    ap.add_argument("--lite", action="store_true",
+                    help="profiling only: time the steps, skip e2e / CPU / per-kernel legs")
+    args = ap.parse_args()
+    global GRID
+    GRID = GRIDS[args.grid]
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -48,7 +48,8 @@ class SbStatus(ctypes.Structure):
 ABI_FUNCTIONS = [
     "sb_create", "sb_destroy", "sb_set_member_re", "sb_set_state", "sb_get_state", "sb_step",
     "sb_get_status", "sb_get_trace", "sb_cross", "sb_get_stream", "sb_sync", "sb_sizes",
-    "sb_seed_state", "sb_compact_coeffs", "sb_last_error", "sb_version",
+    "sb_seed_state", "sb_compact_coeffs", "sb_last_error", "sb_version", "sb_launch_stage",
+    "sb_fp64_peak",
 ]
 
 _lib = None
@@ -86,6 +87,8 @@ def lib(auto_build: bool = False):
                                 dp, dp]
     L.sb_compact_coeffs.argtypes = [dp, dp, dp, dp]
     L.sb_last_error.restype = ctypes.c_char_p
+    L.sb_launch_stage.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.sb_fp64_peak.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     _lib = L
     return L
 
@@ -192,6 +195,14 @@ class ShearBox:
                                   ctypes.byref(xb), ctypes.byref(xt)))
         return {"vor": vor, "phi": phi, "u00": u00, "w00": w00, "time": t.value,
                 "xoffb": xb.value, "xofft": xt.value}
+
+    def launch_stage(self, stage: int, rk: int = 1, count: int = 1):
+        _check(lib().sb_launch_stage(self.h, int(stage), int(rk), int(count)))
+
+    def fp64_peak(self) -> float:
+        v = ctypes.c_double()
+        _check(lib().sb_fp64_peak(self.h, ctypes.byref(v)))
+        return v.value
 
     def step(self, nsteps: int):
         _check(lib().sb_step(self.h, int(nsteps)))

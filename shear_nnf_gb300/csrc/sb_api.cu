@@ -503,6 +503,28 @@ int sb_cross(sb_handle *h, double *vor, double *phi, double *u00, double *w00, d
 
 void *sb_get_stream(sb_handle *h) { return h ? (void *)h->st : nullptr; }
 
+int sb_launch_stage(sb_handle *h, int stage, int rk, int count) {
+  if (!h || count < 0) return fail(1, "bad argument");
+  if (stage < 1 || stage > 5 || rk < 1 || rk > 3) return fail(1, "stage 1..5, rk 1..3");
+  for (int q = 0; q < count; q++) {
+    cudaError_t e;
+    if (stage <= 3)
+      e = launch_plane(h->g, h->bf, stage, rk, h->st);
+    else if (stage == 4)
+      e = launch_phase(h->g, h->bf, rk, h->st);
+    else
+      e = launch_line(h->g, h->bf, rk, 1, h->st);
+    if (e != cudaSuccess) return fail(3, "launch: %s", cudaGetErrorString(e));
+  }
+  return 0;
+}
+
+int sb_fp64_peak(sb_handle *h, double *tflops) {
+  if (!h || !tflops) return fail(1, "bad argument");
+  CK(fp64_peak(tflops, h->st));
+  return 0;
+}
+
 int sb_sync(sb_handle *h) {
   if (!h) return fail(1, "null handle");
   CK(cudaStreamSynchronize(h->st));

@@ -1029,6 +1029,47 @@ cudaError_t launch_plane_to_pencil(const Grid &g, const double *src, double *pen
   return cudaGetLastError();
 }
 
+// FP64 FMA throughput probe: eight independent chains per thread
+__global__ void k_fp64_probe(double *out, int iters, double a, double b) {
+  double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5,
+         x6 = x0 + 6, x7 = x0 + 7;
+  for (int it = 0; it < iters; it++) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+cudaError_t fp64_peak(double *tflops, cudaStream_t st) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int threads = 512, blocks = 2 * sms, iters = 20000;
+  double *d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(double) * threads * blocks);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_fp64_probe<<<blocks, threads, 0, st>>>(d, 100, 0.999, 0.001);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; rep++) {
+    cudaEventRecord(e0, st);
+    k_fp64_probe<<<blocks, threads, 0, st>>>(d, iters, 0.999, 0.001);
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(d);
+  *tflops = 2.0 * 8.0 * iters * (double)threads * blocks / (best * 1e-3) / 1e12;
+  return e;
+}
+
 bool supported_grid(int mgalx, int mgalz) {
   const int xs[] = {32, 48, 64, 96, 192, 384};
   const int zs[] = {32, 48, 64, 96, 192};

@@ -13,4 +13,5 @@ cudaError_t launch_phase(const Grid &g, const Bufs &bf, int rk, cudaStream_t st)
 cudaError_t launch_finish(const Grid &g, const Bufs &bf, cudaStream_t st);
 cudaError_t launch_pencil_to_plane(const Grid &g, const double *pen, double *dst, cudaStream_t st);
 cudaError_t launch_plane_to_pencil(const Grid &g, const double *src, double *pen, cudaStream_t st);
+cudaError_t fp64_peak(double *tflops, cudaStream_t st);
 }  // namespace sb
