@@ -105,6 +105,25 @@ int sb_cross(sb_handle *h, double *vor, double *phi, double *u00, double *w00, d
 int sb_launch_stage(sb_handle *h, int stage, int rk, int count);
 int sb_fp64_peak(sb_handle *h, double *tflops);
 
+/* Standalone y-line operators on device-resident complex lines.  Line data is
+ * [j][line]: element (line, j) is the complex at u + 2*(j*ldu + line).  shp/shm
+ * (and k2) are HOST arrays with one complex (one real) entry per line: the
+ * shear phases of the upper / lower periodic images, u(y+Ly) = shp*u(y) and
+ * u(y-Ly) = shm*u(y).  A real line is a complex line with zero imaginary part
+ * and shp = shm = 1.  The work is enqueued on `stream` (a cudaStream_t, 0 for
+ * the legacy stream) and the call returns once it has completed.
+ *   sb_op_derivyc   first (iord 1) or second (iord 2) derivative in y with the
+ *                   compact heptadiagonal scheme: derivyc,
+ *                   diffy_shear_hepta.f90:333-450 (ias=1 semantics).
+ *   sb_op_lapcdy    solves (d2/dy2 - k2) p = u: lapcdy,
+ *                   diffy_shear_hepta.f90:466-525.
+ * Both allocate their scratch and factor tables with the stream-ordered
+ * allocator and free them before returning. */
+int sb_op_derivyc(int my, double Ly, int iord, int nlines, const double *u, long ldu, double *out,
+                  long ldo, const double *shp, const double *shm, void *stream);
+int sb_op_lapcdy(int my, double Ly, int nlines, const double *u, long ldu, double *out, long ldo,
+                 const double *k2, const double *shp, const double *shm, void *stream);
+
 /* CUDA stream of the handle (cudaStream_t) and a blocking wait on it. */
 void *sb_get_stream(sb_handle *h);
 int sb_sync(sb_handle *h);

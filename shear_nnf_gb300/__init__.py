@@ -49,7 +49,7 @@ ABI_FUNCTIONS = [
     "sb_create", "sb_destroy", "sb_set_member_re", "sb_set_state", "sb_get_state", "sb_step",
     "sb_get_status", "sb_get_trace", "sb_cross", "sb_get_stream", "sb_sync", "sb_sizes",
     "sb_seed_state", "sb_compact_coeffs", "sb_last_error", "sb_version", "sb_launch_stage",
-    "sb_fp64_peak",
+    "sb_fp64_peak", "sb_op_derivyc", "sb_op_lapcdy",
 ]
 
 _lib = None
@@ -89,6 +89,10 @@ def lib(auto_build: bool = False):
     L.sb_last_error.restype = ctypes.c_char_p
     L.sb_launch_stage.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.sb_fp64_peak.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+    L.sb_op_derivyc.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp,
+                                ctypes.c_long, vp, ctypes.c_long, dp, dp, vp]
+    L.sb_op_lapcdy.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, vp, ctypes.c_long, vp,
+                               ctypes.c_long, dp, dp, dp, vp]
     _lib = L
     return L
 
@@ -238,3 +242,29 @@ class ShearBox:
                               ctypes.byref(xt), int(nstep), ctypes.byref(st)))
         state["time"], state["xoffb"], state["xofft"] = t.value, xb.value, xt.value
         return self.trace(0), st
+
+
+def op_derivyc(my: int, Ly: float, iord: int, u_dev: int, out_dev: int, nlines: int,
+               shp: np.ndarray, shm: np.ndarray, ldu: int = None, ldo: int = None,
+               stream: int = 0):
+    """d/dy (iord 1) or d2/dy2 (iord 2) of nlines device-resident complex lines
+    ([j][line] layout, device pointers); shp/shm host complex arrays (nlines)."""
+    sp = np.ascontiguousarray(shp, np.complex128)
+    sm = np.ascontiguousarray(shm, np.complex128)
+    _check(lib().sb_op_derivyc(int(my), float(Ly), int(iord), int(nlines), ctypes.c_void_p(u_dev),
+                               int(ldu or nlines), ctypes.c_void_p(out_dev), int(ldo or nlines),
+                               _dp(sp.view(np.float64)), _dp(sm.view(np.float64)),
+                               ctypes.c_void_p(stream)))
+
+
+def op_lapcdy(my: int, Ly: float, u_dev: int, out_dev: int, nlines: int, k2: np.ndarray,
+              shp: np.ndarray, shm: np.ndarray, ldu: int = None, ldo: int = None,
+              stream: int = 0):
+    """Solves (d2/dy2 - k2) p = u on nlines device-resident complex lines."""
+    kk = np.ascontiguousarray(k2, np.float64)
+    sp = np.ascontiguousarray(shp, np.complex128)
+    sm = np.ascontiguousarray(shm, np.complex128)
+    _check(lib().sb_op_lapcdy(int(my), float(Ly), int(nlines), ctypes.c_void_p(u_dev),
+                              int(ldu or nlines), ctypes.c_void_p(out_dev), int(ldo or nlines),
+                              _dp(kk), _dp(sp.view(np.float64)), _dp(sm.view(np.float64)),
+                              ctypes.c_void_p(stream)))

@@ -162,6 +162,62 @@ static int ensure_trace(sb_handle *h, int cap) {
   return capture_step(h);
 }
 
+// Factor tables of one operator staged on the host, packed into one buffer so
+// that a single copy places them on the device.
+struct HostFac {
+  std::vector<double> buf;  // La Lb Lc Ddm1 Dd e f g (each n*lines) then sums (10*lines)
+  long lines = 1, n = 0;
+};
+static void host_fac_add(HostFac *h, long line, const sbh::BaseFac &b, const double a[7]) {
+  const long n = h->n, L = h->lines;
+  const std::vector<double> *arr[8] = {&b.La, &b.Lb, &b.Lc, &b.Ddm1, &b.Dd, &b.e, &b.f, &b.g};
+  for (int q = 0; q < 8; q++)
+    for (long j = 0; j < n; j++) h->buf[((long)q * n + j) * L + line] = (*arr[q])[j];
+  for (int q = 0; q < 6; q++) h->buf[(8 * n + q) * L + line] = b.sums[q];
+  for (int q = 0; q < 4; q++) h->buf[(8 * n + 6 + q) * L + line] = a[3 + q];
+}
+static void host_fac_init(HostFac *h, long n, long lines) {
+  h->n = n;
+  h->lines = lines;
+  h->buf.assign((size_t)(8 * n + 10) * lines, 0.0);
+}
+static Fac fac_bind(const HostFac &h, const double *d) {
+  Fac F;
+  const long n = h.n, L = h.lines;
+  const double **dst[8] = {&F.La, &F.Lb, &F.Lc, &F.Ddm1, &F.Dd, &F.e, &F.f, &F.g};
+  for (int q = 0; q < 8; q++) *dst[q] = d + (long)q * n * L;
+  F.sums = d + 8 * n * L;
+  F.stride = (L > 1) ? L : 0;
+  return F;
+}
+
+// common checks of the operator entry points
+static int op_check(int my, double Ly, int nlines, const void *u, const void *out, long ldu,
+                    long ldo, const double *shp, const double *shm) {
+  if (my < 16 || my > SB_MAX_NY) return fail(1, "my=%d outside 16..%d", my, SB_MAX_NY);
+  if (!(Ly > 0)) return fail(1, "Ly must be positive");
+  if (nlines < 1) return fail(1, "nlines must be >= 1");
+  if (!u || !out || !shp || !shm) return fail(1, "null argument");
+  if (ldu < nlines || ldo < nlines) return fail(1, "leading dimension smaller than nlines");
+  return 0;
+}
+
+// derivative operator d/dy (iord 1) or d2/dy2 (iord 2): band of the left-hand
+// side and right-hand-side stencil (r0; r1..r3), antisymmetric for iord 1
+static void deriv_operator(int iord, double dy, const sbh::Coeffs &co, const double **a,
+                           double r[4], int *anti) {
+  if (iord == 1) {
+    *a = co.pr1;
+    r[0] = 0.0;
+    for (int d = 1; d <= 3; d++) r[d] = co.rh1h[3 + d] / dy;
+    *anti = 1;
+  } else {
+    *a = co.pr2;
+    for (int d = 0; d <= 3; d++) r[d] = co.rh2h[3 + d] / (dy * dy);
+    *anti = 0;
+  }
+}
+
 extern "C" {
 
 int sb_version(void) { return 1; }
@@ -529,6 +585,83 @@ int sb_sync(sb_handle *h) {
   if (!h) return fail(1, "null handle");
   CK(cudaStreamSynchronize(h->st));
   CK(cudaGetLastError());
+  return 0;
+}
+
+int sb_op_derivyc(int my, double Ly, int iord, int nlines, const double *u, long ldu, double *out,
+                  long ldo, const double *shp, const double *shm, void *stream) {
+  int rc = op_check(my, Ly, nlines, u, out, ldu, ldo, shp, shm);
+  if (rc) return rc;
+  if (iord != 1 && iord != 2) return fail(1, "iord must be 1 or 2");
+  cudaStream_t st = (cudaStream_t)stream;
+  sbh::Coeffs co;
+  sbh::compact_coeffs(&co);
+  const double dy = Ly / (double)my;
+  const double *a;
+  double r[4];
+  int anti;
+  deriv_operator(iord, dy, co, &a, r, &anti);
+  HostFac hf;
+  host_fac_init(&hf, my, 1);
+  sbh::BaseFac b;
+  sbh::base_factor(a, my, &b);
+  host_fac_add(&hf, 0, b, a);
+  const size_t nfac = hf.buf.size();
+  std::vector<double> host(nfac + 4 * (size_t)nlines);
+  std::copy(hf.buf.begin(), hf.buf.end(), host.begin());
+  std::copy(shp, shp + 2 * (size_t)nlines, host.begin() + nfac);
+  std::copy(shm, shm + 2 * (size_t)nlines, host.begin() + nfac + 2 * nlines);
+  const long nthr = op_threads(nlines);
+  double *dbuf = nullptr, *ybuf = nullptr;
+  CK(cudaMallocAsync((void **)&dbuf, sizeof(double) * host.size(), st));
+  CK(cudaMallocAsync((void **)&ybuf, sizeof(double) * (size_t)my * nthr, st));
+  CK(cudaMemcpyAsync(dbuf, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice, st));
+  Fac F = fac_bind(hf, dbuf);
+  cudaError_t e = launch_op_line(nlines, my, u, ldu, out, ldo, ybuf, F, dbuf + nfac,
+                                 dbuf + nfac + 2 * nlines, r, anti, st);
+  cudaFreeAsync(ybuf, st);
+  cudaFreeAsync(dbuf, st);
+  if (e != cudaSuccess) return fail(3, "launch: %s", cudaGetErrorString(e));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int sb_op_lapcdy(int my, double Ly, int nlines, const double *u, long ldu, double *out, long ldo,
+                 const double *k2, const double *shp, const double *shm, void *stream) {
+  int rc = op_check(my, Ly, nlines, u, out, ldu, ldo, shp, shm);
+  if (rc) return rc;
+  if (!k2) return fail(1, "null k2");
+  cudaStream_t st = (cudaStream_t)stream;
+  sbh::Coeffs co;
+  sbh::compact_coeffs(&co);
+  const double dy = Ly / (double)my;
+  HostFac hf;
+  host_fac_init(&hf, my, nlines);
+  sbh::BaseFac b;
+  for (int l = 0; l < nlines; l++) {
+    double lap[7];
+    for (int d = 0; d < 7; d++) lap[d] = co.rh2h[d] / (dy * dy) - k2[l] * co.pr2[d];
+    sbh::base_factor(lap, my, &b);
+    host_fac_add(&hf, l, b, lap);
+  }
+  double r[4] = {co.pr2[3], co.pr2[4], co.pr2[5], co.pr2[6]};
+  const size_t nfac = hf.buf.size();
+  std::vector<double> host(nfac + 4 * (size_t)nlines);
+  std::copy(hf.buf.begin(), hf.buf.end(), host.begin());
+  std::copy(shp, shp + 2 * (size_t)nlines, host.begin() + nfac);
+  std::copy(shm, shm + 2 * (size_t)nlines, host.begin() + nfac + 2 * nlines);
+  const long nthr = op_threads(nlines);
+  double *dbuf = nullptr, *ybuf = nullptr;
+  CK(cudaMallocAsync((void **)&dbuf, sizeof(double) * host.size(), st));
+  CK(cudaMallocAsync((void **)&ybuf, sizeof(double) * (size_t)my * nthr, st));
+  CK(cudaMemcpyAsync(dbuf, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice, st));
+  Fac F = fac_bind(hf, dbuf);
+  cudaError_t e = launch_op_line(nlines, my, u, ldu, out, ldo, ybuf, F, dbuf + nfac,
+                                 dbuf + nfac + 2 * nlines, r, 0, st);
+  cudaFreeAsync(ybuf, st);
+  cudaFreeAsync(dbuf, st);
+  if (e != cudaSuccess) return fail(3, "launch: %s", cudaGetErrorString(e));
+  CK(cudaStreamSynchronize(st));
   return 0;
 }
 

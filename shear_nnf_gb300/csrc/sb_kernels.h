@@ -14,4 +14,8 @@ cudaError_t launch_finish(const Grid &g, const Bufs &bf, cudaStream_t st);
 cudaError_t launch_pencil_to_plane(const Grid &g, const double *pen, double *dst, cudaStream_t st);
 cudaError_t launch_plane_to_pencil(const Grid &g, const double *src, double *pen, cudaStream_t st);
 cudaError_t fp64_peak(double *tflops, cudaStream_t st);
+long op_threads(int nlines);
+cudaError_t launch_op_line(int nlines, int N, const double *u, long ldu, double *out, long ldo,
+                           double *ybuf, const Fac &F, const double *shp, const double *shm,
+                           const double r[4], int anti, cudaStream_t st);
 }  // namespace sb

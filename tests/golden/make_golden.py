@@ -1,0 +1,44 @@
+"""Generates the golden fixtures of the step tests from the C oracle.
+
+The reference ships no test vectors (its verification was by hand: RDT runs,
+log_changes rev.428-430), so these fixtures are produced by the oracle, whose
+building blocks are pinned by tests/test_oracle.py.  Inputs are not stored:
+they come from the seeded generator sb_seed_state (seed, grid below).
+
+usage: python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+import shear_nnf_gb300 as sb  # noqa: E402
+
+LZ = 2 * np.pi
+CASES = {
+    # 64x32x32, Re_z = 1000, fixed dt 0.005 (the CPU-runnable configuration), 2 steps
+    "step64_seed3": dict(params=dict(mgalx=64, my=32, mgalz=32, Re=1000.0 / LZ ** 2, alp=0.5,
+                                     Ly=LZ, gam=1.0, s=1.0, chi=0.0, CFL=0.5, fixed_dt=0.005),
+                         seed=3, nstep=2),
+}
+
+
+def main():
+    for name, c in CASES.items():
+        st = sb.seed_state(sb.make_params(**c["params"]), c["seed"])
+        o = oracle.Oracle(**c["params"])
+        tr, istop = o.cross(st, c["nstep"])
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), vor=st["vor"], phi=st["phi"],
+                            u00=st["u00"], w00=st["w00"], time=st["time"], xoffb=st["xoffb"],
+                            xofft=st["xofft"], trace=tr, seed=c["seed"], nstep=c["nstep"],
+                            **{"p_" + k: v for k, v in c["params"].items()})
+        print(name, "written")
+
+
+if __name__ == "__main__":
+    main()

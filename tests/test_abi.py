@@ -1,0 +1,99 @@
+"""The C-ABI library loads and exports every function declared in
+include/shearbox.h; host-only entry points behave (no GPU compute here)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, box_params
+
+
+def _declared():
+    txt = open(os.path.join(ROOT, "include", "shearbox.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(sb_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from shear_nnf_gb300.buildlib import LIB, build
+    build()
+    return ctypes.CDLL(LIB)
+
+
+def test_exports_every_declared_symbol(lib):
+    names = _declared()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in shearbox.h but not exported"
+
+
+def test_python_wrapper_lists_the_header():
+    import shear_nnf_gb300 as sb
+    assert sorted(sb.ABI_FUNCTIONS) == _declared()
+
+
+def test_sizes_follow_initcr():
+    import shear_nnf_gb300 as sb
+    for (gx, gy, gz), (mx, mz) in {(192, 96, 96): (128, 63), (64, 32, 32): (42, 19),
+                                    (96, 48, 48): (64, 31), (384, 192, 192): (256, 127)}.items():
+        s = sb.sizes(sb.make_params(**box_params(gx, gy, gz, rez=1000.0)))
+        assert (s["mx"], s["mz"], s["nkx"], s["nz"]) == (mx, mz, mx // 2, (mz - 1) // 2)
+
+
+def test_compact_coefficients_match_oracle_bitwise():
+    import oracle
+    import shear_nnf_gb300 as sb
+    pr1, rh1h, pr2, rh2h = sb.compact_coeffs()
+    o = oracle.Oracle(64, 32, 32, Re=10.0, alp=0.5, Ly=2 * np.pi, gam=1.0)
+    opr1, orh1, opr2, orh2, dy = o.coeffs()
+    assert np.array_equal(pr1, opr1) and np.array_equal(pr2, opr2)
+    np.testing.assert_allclose(rh1h / dy, orh1, rtol=1e-15)
+    np.testing.assert_allclose(rh2h / dy ** 2, orh2, rtol=1e-15)
+
+
+def test_seed_state_is_divergence_free_and_hermitian():
+    import shear_nnf_gb300 as sb
+    p = sb.make_params(**box_params(64, 32, 32, rez=1000.0))
+    st = sb.seed_state(p, 5)
+    s = sb.sizes(p)
+    nz, mz = s["nz"], s["mz"]
+    vor, phi = st["vor"], st["phi"]
+    # kx = 0 column: conjugate symmetric in kz (the reality condition set_conj imposes)
+    for k in range(nz + 1, mz):
+        np.testing.assert_allclose(vor[k, 0], np.conj(vor[mz - k, 0]), atol=1e-12)
+        np.testing.assert_allclose(phi[k, 0], np.conj(phi[mz - k, 0]), atol=1e-12)
+    assert np.all(vor[0, 0] == 0) and np.all(phi[0, 0] == 0)
+    # rms velocity of the seeded field is 0.1 S Lz (checked through the oracle's UNER)
+    import oracle
+    o = oracle.Oracle(**box_params(64, 32, 32, rez=1000.0, fixed_dt=1e-6))
+    tr, _ = o.cross({k: (v.copy() if hasattr(v, "copy") else v) for k, v in st.items()}, 1)
+    urms = np.sqrt((tr[0, 2] ** 2 + tr[0, 3] ** 2 + tr[0, 4] ** 2) / 3)
+    assert abs(urms / (0.1 * 2 * np.pi) - 1) < 0.05
+
+
+def test_seed_state_reproducible_and_seed_dependent():
+    import shear_nnf_gb300 as sb
+    p = sb.make_params(**box_params(64, 32, 32, rez=1000.0))
+    a, b, c = sb.seed_state(p, 1), sb.seed_state(p, 1), sb.seed_state(p, 2)
+    assert np.array_equal(a["vor"], b["vor"]) and np.array_equal(a["u00"], b["u00"])
+    assert not np.allclose(a["vor"], c["vor"])
+
+
+def test_invalid_grid_rejected_without_gpu():
+    import shear_nnf_gb300 as sb
+    p = sb.make_params(**box_params(100, 32, 32, rez=1000.0))
+    with pytest.raises(sb.ShearBoxError, match="unsupported"):
+        sb.sizes(p) and sb.seed_state(p, 1)
+
+
+def test_no_cpu_fallback(monkeypatch):
+    """Without a GPU the handle cannot be created: the library has no CPU path."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import shear_nnf_gb300 as sb
+    with pytest.raises(sb.ShearBoxError, match="no CUDA device"):
+        sb.ShearBox(sb.make_params(**box_params(64, 32, 32, rez=1000.0)))

@@ -1,0 +1,43 @@
+"""Golden fixtures (tests/golden/make_golden.py): the oracle reproduces them on
+this machine; the GPU step reproduces them on a GB300."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, rel_l2
+
+GOLD = os.path.join(ROOT, "tests", "golden", "step64_seed3.npz")
+
+
+def _case():
+    g = np.load(GOLD)
+    params = {k[2:]: g[k].item() for k in g.files if k.startswith("p_")}
+    for k in ("mgalx", "my", "mgalz"):
+        params[k] = int(params[k])
+    return g, params
+
+
+def test_oracle_reproduces_golden():
+    import oracle
+    import shear_nnf_gb300 as sb
+    g, params = _case()
+    st = sb.seed_state(sb.make_params(**params), int(g["seed"]))
+    tr, _ = oracle.Oracle(**params).cross(st, int(g["nstep"]))
+    for k in ("vor", "phi", "u00", "w00"):
+        assert rel_l2(st[k], g[k]) < 1e-13, k
+    np.testing.assert_allclose(tr, g["trace"], rtol=1e-12, atol=0)
+
+
+@pytest.mark.gpu
+def test_gpu_reproduces_golden():
+    import shear_nnf_gb300 as sb
+    g, params = _case()
+    p = sb.make_params(**params)
+    st = sb.seed_state(p, int(g["seed"]))
+    box = sb.ShearBox(p)
+    tr, status = box.cross(st, int(g["nstep"]))
+    for k in ("vor", "phi", "u00", "w00"):
+        assert rel_l2(st[k], g[k]) < 1e-12, k
+    np.testing.assert_allclose(tr, g["trace"], rtol=1e-10, atol=1e-300)
+    assert st["time"] == pytest.approx(float(g["time"]), abs=1e-15)
