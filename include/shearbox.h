@@ -124,6 +124,28 @@ int sb_op_derivyc(int my, double Ly, int iord, int nlines, const double *u, long
 int sb_op_lapcdy(int my, double Ly, int nlines, const double *u, long ldu, double *out, long ldo,
                  const double *k2, const double *shp, const double *shm, void *stream);
 
+/* Allocation-free variant of sb_op_derivyc (no counterpart in the reference).
+ * For callers that must not allocate device memory where they need the
+ * derivative -- e.g. an application whose device memory is all handed to its
+ * own pool, or a loop that must not pay the synchronisation an allocation can
+ * cause.  Same arguments and results as sb_op_derivyc; it calls no cudaMalloc,
+ * cudaFree or allocating library routine.  Its scratch is one fixed device
+ * array of the library (about 9.5 MB, held on every GPU that loads the library
+ * until the process exits), limited to nlines <= SB_NOALLOC_LINES and
+ * my * (2*nlines rounded up to a multiple of 32) <= SB_NOALLOC_YBUF doubles;
+ * larger requests return error 6 with a message.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress, with that device
+ * current); make that first call before any stream capture.  Every call
+ * overwrites the whole part of the array it uses, so nothing carries over
+ * between calls, but all calls share the one array: calls that overlap on the
+ * GPU (other streams, other host threads) race and must be serialised by the
+ * caller. */
+#define SB_NOALLOC_LINES 32768
+#define SB_NOALLOC_YBUF (1L << 20)
+int sb_op_derivyc_noalloc(int my, double Ly, int iord, int nlines, const double *u, long ldu,
+                          double *out, long ldo, const double *shp, const double *shm,
+                          void *stream);
+
 /* CUDA stream of the handle (cudaStream_t) and a blocking wait on it. */
 void *sb_get_stream(sb_handle *h);
 int sb_sync(sb_handle *h);

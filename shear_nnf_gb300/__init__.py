@@ -49,7 +49,7 @@ ABI_FUNCTIONS = [
     "sb_create", "sb_destroy", "sb_set_member_re", "sb_set_state", "sb_get_state", "sb_step",
     "sb_get_status", "sb_get_trace", "sb_cross", "sb_get_stream", "sb_sync", "sb_sizes",
     "sb_seed_state", "sb_compact_coeffs", "sb_last_error", "sb_version", "sb_launch_stage",
-    "sb_fp64_peak", "sb_op_derivyc", "sb_op_lapcdy",
+    "sb_fp64_peak", "sb_op_derivyc", "sb_op_lapcdy", "sb_op_derivyc_noalloc",
 ]
 
 _lib = None
@@ -91,6 +91,7 @@ def lib(auto_build: bool = False):
     L.sb_fp64_peak.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.sb_op_derivyc.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp,
                                 ctypes.c_long, vp, ctypes.c_long, dp, dp, vp]
+    L.sb_op_derivyc_noalloc.argtypes = list(L.sb_op_derivyc.argtypes)
     L.sb_op_lapcdy.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, vp, ctypes.c_long, vp,
                                ctypes.c_long, dp, dp, dp, vp]
     _lib = L
@@ -268,3 +269,17 @@ def op_lapcdy(my: int, Ly: float, u_dev: int, out_dev: int, nlines: int, k2: np.
                               int(ldu or nlines), ctypes.c_void_p(out_dev), int(ldo or nlines),
                               _dp(kk), _dp(sp.view(np.float64)), _dp(sm.view(np.float64)),
                               ctypes.c_void_p(stream)))
+
+
+def op_derivyc_noalloc(my: int, Ly: float, iord: int, u_dev: int, out_dev: int, nlines: int,
+                       shp: np.ndarray, shm: np.ndarray, ldu: int = None, ldo: int = None,
+                       stream: int = 0):
+    """Same as op_derivyc without any device allocation: scratch in a fixed
+    array of the library (limits and sharing rules in include/shearbox.h)."""
+    sp = np.ascontiguousarray(shp, np.complex128)
+    sm = np.ascontiguousarray(shm, np.complex128)
+    _check(lib().sb_op_derivyc_noalloc(int(my), float(Ly), int(iord), int(nlines),
+                                       ctypes.c_void_p(u_dev), int(ldu or nlines),
+                                       ctypes.c_void_p(out_dev), int(ldo or nlines),
+                                       _dp(sp.view(np.float64)), _dp(sm.view(np.float64)),
+                                       ctypes.c_void_p(stream)))

@@ -665,4 +665,13 @@ int sb_op_lapcdy(int my, double Ly, int nlines, const double *u, long ldu, doubl
   return 0;
 }
 
+int sb_op_derivyc_noalloc(int my, double Ly, int iord, int nlines, const double *u, long ldu,
+                          double *out, long ldo, const double *shp, const double *shm,
+                          void *stream) {
+  std::string err;
+  int rc = sb::noalloc_derivyc(my, Ly, iord, nlines, u, ldu, out, ldo, shp, shm, stream, &err);
+  if (rc) return fail(rc, "%s", err.c_str());
+  return 0;
+}
+
 }  // extern "C"

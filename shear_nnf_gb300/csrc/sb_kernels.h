@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "sb_common.cuh"
 
 namespace sb {
@@ -18,4 +20,7 @@ long op_threads(int nlines);
 cudaError_t launch_op_line(int nlines, int N, const double *u, long ldu, double *out, long ldo,
                            double *ybuf, const Fac &F, const double *shp, const double *shm,
                            const double r[4], int anti, cudaStream_t st);
+int noalloc_derivyc(int my, double Ly, int iord, int nlines, const double *u, long ldu,
+                    double *out, long ldo, const double *shp, const double *shm, void *stream,
+                    std::string *err);
 }  // namespace sb

@@ -1,0 +1,50 @@
+"""The allocation-free derivyc entry point (sb_op_derivyc_noalloc) against the
+allocating one (sb_op_derivyc), through the C-ABI.
+
+Callers that cannot allocate device memory where they need a y-derivative (their
+device memory is all in their own pool, or an allocation's possible
+synchronisation is not acceptable there) use the no-alloc variant; it must give
+the same results.  Two calls in a row with different inputs check that nothing
+left in the shared scratch array leaks into the next call.  This file is
+collected last so that a run stopping at the first failure has run every other
+test before it."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-13  # the tolerance of the operator tests
+
+
+def _case(nlines, my, seed):
+    rng = np.random.default_rng(seed)
+    u = rng.standard_normal((my, nlines)) + 1j * rng.standard_normal((my, nlines))
+    shp = np.exp(1j * rng.uniform(-np.pi, np.pi, nlines))
+    return u, shp, np.conj(shp)
+
+
+def test_noalloc_matches_allocating_entry_point_twice():
+    import torch
+    import shear_nnf_gb300 as sb
+    Ly = 2 * np.pi
+    for call, (nlines, my, iord) in enumerate([(4032, 96, 1), (333, 48, 2)]):
+        u, shp, shm = _case(nlines, my, 100 + call)
+        du = torch.from_numpy(u).cuda()
+        ref = torch.zeros_like(du)
+        got = torch.full_like(du, float("nan"))
+        sb.op_derivyc(my, Ly, iord, du.data_ptr(), ref.data_ptr(), nlines, shp, shm)
+        sb.op_derivyc_noalloc(my, Ly, iord, du.data_ptr(), got.data_ptr(), nlines, shp, shm)
+        r = ref.cpu().numpy()
+        g = got.cpu().numpy()
+        assert np.all(np.isfinite(g))
+        err = np.abs(g - r).max() / np.abs(r).max()
+        assert err < TOL, (call, err)
+
+
+def test_noalloc_rejects_oversized_requests():
+    import torch
+    import shear_nnf_gb300 as sb
+    my, nlines = 512, 4096  # my * 2*nlines = 4 Mi doubles > the 1 Mi scratch
+    du = torch.zeros((1, 1), dtype=torch.complex128, device="cuda")
+    one = np.ones(nlines, np.complex128)
+    with pytest.raises(sb.ShearBoxError, match="exceed the fixed scratch"):
+        sb.op_derivyc_noalloc(my, 2 * np.pi, 1, du.data_ptr(), du.data_ptr(), nlines, one, one)
