@@ -98,8 +98,8 @@ int sb_cross(sb_handle *h, double *vor, double *phi, double *u00, double *w00, d
 
 /* Measurement hooks (no counterpart in the reference; used by the benchmark).
  * sb_launch_stage enqueues `count` launches of one kernel of substep rk on the
- * handle's stream: stage 1..3 the plane stages, 4 the per-box phase kernel,
- * 5 the y-line kernel.  The launches act on the current device state, so a
+ * handle's stream: stage 1..3 the plane stages, 4 the per-box phase tables,
+ * 5 and 6 the two y-line kernels.  The launches act on the current device state, so a
  * run that used them must set the state again before stepping.
  * sb_fp64_peak measures the device's FP64 FMA throughput in TFLOP/s. */
 int sb_launch_stage(sb_handle *h, int stage, int rk, int count);

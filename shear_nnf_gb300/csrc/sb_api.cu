@@ -78,7 +78,7 @@ static int check_params(const sb_params *p) {
     return fail(1, "unsupported x/z grid %d x %d (transform lengths 32,48,64,96,192[,384])",
                 p->mgalx, p->mgalz);
   if (p->mgalz % 2) return fail(1, "mgalz must be even");
-  if (p->my < 16 || p->my > SB_MAX_NY) return fail(1, "my=%d outside 16..%d", p->my, SB_MAX_NY);
+  if (p->my < 16 || p->my > 448) return fail(1, "my=%d outside 16..448", p->my);
   if (!(p->Re != 0.0) || !(p->alp > 0) || !(p->gam > 0) || !(p->Ly > 0) || !(p->CFL > 0))
     return fail(1, "invalid physical parameters");
   return 0;
@@ -136,8 +136,10 @@ static int capture_step(sb_handle *h) {
     if ((e = launch_plane(h->g, h->bf, 1, rk, h->st)) != cudaSuccess) break;
     if ((e = launch_plane(h->g, h->bf, 2, rk, h->st)) != cudaSuccess) break;
     if ((e = launch_plane(h->g, h->bf, 3, rk, h->st)) != cudaSuccess) break;
-    if ((e = launch_phase(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
-    e = launch_line(h->g, h->bf, rk, 1, h->st);
+    if ((e = launch_scalar(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
+    if ((e = launch_tables(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
+    if ((e = launch_lineA(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
+    e = launch_lineB(h->g, h->bf, rk, h->st);
   }
   if (e == cudaSuccess) e = launch_finish(h->g, h->bf, h->st);
   cudaError_t e2 = cudaStreamEndCapture(h->st, &graph);
@@ -306,7 +308,8 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   g.plane = 2L * nl;
   g.field = g.plane * g.my;
   g.nlines_pad = ((2 * nl + 31) / 32) * 32;
-  g.tpm = g.nlines_pad + 32;
+  g.tpmA = 3 * g.nlines_pad + 32;
+  g.tpmB = 2 * g.nlines_pad + 32;
   cudaError_t ce = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
   if (ce != cudaSuccess) {
     delete h;
@@ -317,7 +320,9 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   auto A = [&](double **q, size_t n) { return dalloc(h, q, n); };
   if ((rc = A(&bf.vor, B * F)) || (rc = A(&bf.phi, B * F)) || (rc = A(&bf.vorwk, B * F)) ||
       (rc = A(&bf.phiwk, B * F)) || (rc = A(&bf.G, B * F)) || (rc = A(&bf.V, B * F)) ||
-      (rc = A(&bf.D, B * F)) || (rc = A(&bf.S, B * F + B * 2 * my * 32)) ||
+      (rc = A(&bf.D, B * F)) || (rc = A(&bf.S, B * F)) || (rc = A(&bf.T, B * F)) ||
+      (rc = A(&bf.tl1o, B * g.nkx * SB_TAIL)) || (rc = A(&bf.tl2o, B * g.nkx * SB_TAIL)) ||
+      (rc = A(&bf.tl1n, B * g.nkx * SB_TAIL)) ||
       (rc = A(&bf.mu, B * 2 * my)) || (rc = A(&bf.mwk, B * 2 * my)) ||
       (rc = A(&bf.mrf, B * 2 * my)) || (rc = A(&bf.mdu, B * 2 * my)) ||
       (rc = A(&bf.zbuf, B * my * g.mgalz * 6 * g.nkx * 2)) ||
@@ -412,7 +417,7 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
     sb_destroy(h);
     return fail(3, "member upload: %s", cudaGetErrorString(ce));
   }
-  if (launch_plane(g, bf, 0, 0, h->st) != cudaSuccess) {
+  if (launch_plane(g, bf, 0, 0, h->st) != cudaSuccess || prepare_line(g) != cudaSuccess) {
     sb_destroy(h);
     return fail(3, "kernel attributes: %s", cudaGetErrorString(cudaGetLastError()));
   }
@@ -509,8 +514,12 @@ int sb_step(sb_handle *h, int nsteps) {
   if (nsteps < 0) return fail(1, "nsteps < 0");
   int rc = ensure_trace(h, nsteps > 0 ? nsteps : 1);
   if (rc) return rc;
-  CK(launch_phase(h->g, h->bf, 0, h->st));
-  CK(launch_line(h->g, h->bf, 0, 1, h->st));
+  // entry of cross(): flags and offsets, phase tables, set_conj on the state,
+  // v from phi and the first derivatives (cross.f90:76-113,283-287,376-445)
+  CK(launch_scalar(h->g, h->bf, 0, h->st));
+  CK(launch_tables(h->g, h->bf, 0, h->st));
+  CK(launch_setconj(h->g, h->bf, h->st));
+  CK(launch_lineB(h->g, h->bf, 0, h->st));
   for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(h->step_exec, h->st));
   return 0;
 }
@@ -561,15 +570,17 @@ void *sb_get_stream(sb_handle *h) { return h ? (void *)h->st : nullptr; }
 
 int sb_launch_stage(sb_handle *h, int stage, int rk, int count) {
   if (!h || count < 0) return fail(1, "bad argument");
-  if (stage < 1 || stage > 5 || rk < 1 || rk > 3) return fail(1, "stage 1..5, rk 1..3");
+  if (stage < 1 || stage > 6 || rk < 1 || rk > 3) return fail(1, "stage 1..6, rk 1..3");
   for (int q = 0; q < count; q++) {
     cudaError_t e;
     if (stage <= 3)
       e = launch_plane(h->g, h->bf, stage, rk, h->st);
     else if (stage == 4)
-      e = launch_phase(h->g, h->bf, rk, h->st);
+      e = launch_tables(h->g, h->bf, rk, h->st);
+    else if (stage == 5)
+      e = launch_lineA(h->g, h->bf, rk, h->st);
     else
-      e = launch_line(h->g, h->bf, rk, 1, h->st);
+      e = launch_lineB(h->g, h->bf, rk, h->st);
     if (e != cudaSuccess) return fail(3, "launch: %s", cudaGetErrorString(e));
   }
   return 0;

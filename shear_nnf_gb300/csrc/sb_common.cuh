@@ -14,6 +14,7 @@
 #define SB_TRACE_LEN 24
 #define SB_NHIST_Q 11   // per-plane hist partial sums
 #define SB_MAX_NY 512
+#define SB_TAIL 24      // doubles per stored shear tail
 
 namespace sb {
 
@@ -49,8 +50,8 @@ struct Grid {
   double rh1[7], rh2[7], pr2[7];
   long plane;            // doubles per plane of one field  (2*nkx*mz)
   long field;            // doubles per field of one box   (plane*my)
-  int tpm;               // line-kernel threads per member
-  int nlines_pad;        // padded component lines per member
+  int nlines_pad;        // component lines per member, padded to whole warps
+  int tpmA, tpmB;        // threads per member of the two y-line kernels
 };
 
 // Per-member run state, owned by the device (one per box in the batch)
@@ -61,8 +62,7 @@ struct Member {
   int readflag, nhist;
   // state scalars
   double time, xoffb, xofft;
-  double xwkb, xwkt;          // offsets of the current substep (before its update)
-  double xwkb_n, xwkt_n;      // offsets after the current substep's update
+  double xwb[4], xwt[4];      // image offsets: [0] at the step start, [rk] after substep rk
   double Deltat, CFLcur, CFLv;
   double umax[4];
   unsigned long long umax_bits[4];  // |u| maxima as ordered bit patterns (atomicMax)
@@ -79,11 +79,13 @@ __device__ __constant__ static const double kCa[3] = {8.0 / 15.0, 2.0 / 3.0, 1.0
 
 // Device arrays of one handle
 struct Bufs {
-  double *vor, *phi, *vorwk, *phiwk, *G, *V, *D, *S;  // spectral fields [B][field]
+  double *vor, *phi, *vorwk, *phiwk, *G, *V, *D;  // spectral fields [B][field]
+  double *T, *S;                 // d/dy of the NL term and d2(phi)/dy2 between the line kernels
   double *mu, *mwk, *mrf, *mdu;  // mean lines (u00 + i w00) [B][my] complex
   double *zbuf, *xbuf;           // plane-stage intermediates
   double *hpart;                 // hist partials [B][my][ncb][SB_NHIST_Q]
   double *sh_old, *sh_new;       // [B][2][nkx] complex (t then b)
+  double *tl1o, *tl2o, *tl1n;    // shear tails of d/dy, d2/dy2 (old phase), d/dy (new) [B][nkx][SB_TAIL]
   double *mf1, *mf2;             // moving-frame phases [B][my][nkx] complex
   double *trace;                 // [B][cap][SB_TRACE_LEN]
   Member *mem;                   // [B]

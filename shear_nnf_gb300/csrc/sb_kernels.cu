@@ -33,204 +33,6 @@ namespace sb {
 __device__ __forceinline__ cd ldc(const double *p) { return mk(p[0], p[1]); }
 
 // ---------------------------------------------------------------------------
-// k_line: all y-operators of one substep (mode 1..3) or of the step prologue
-// (mode 0: set_conj, v = lapcdy(phi), first derivatives; cross.f90:283-287,
-// 408-445).  One lane per (line, component); lane pairs hold re/im.
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_line(Grid g, Bufs bf, int mode, int next) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int b = (int)(t / g.tpm);
-  if (b >= g.B) return;  // whole warps: tpm is a multiple of 32
-  const int r = (int)(t - (long)b * g.tpm);
-  Member &M = bf.mem[b];
-  if (M.halted) return;  // uniform per warp
-  const int N = g.my;
-  const int c = r & 1;
-  const int nl = g.nkx * g.mz;
-  const bool is_mean = r >= g.nlines_pad;
-  const int lane = threadIdx.x & 31;
-  long lc;
-  bool active;
-  if (!is_mean) {
-    lc = r >> 1;
-    active = lc < nl;
-    if (!active) lc = nl - 1;
-  } else {
-    lc = 0;
-    active = (r - g.nlines_pad) < 2;
-  }
-  const int i = (int)(lc % g.nkx), k = (int)(lc / g.nkx);
-  // scratch for the forward substitution: a field-sized array for real lines,
-  // lane-private rows for padding lanes and the mean warp
-  double *ybuf;
-  long ys;
-  if (!is_mean && active) {
-    ybuf = bf.S + (long)b * g.field + 2 * lc + c;
-    ys = g.plane;
-  } else {
-    ybuf = bf.S + (long)g.B * g.field + ((long)(2 * b + (is_mean ? 1 : 0)) * N) * 32 + lane;
-    ys = 32;
-  }
-  const FacView V1(bf.d1, 0), V2(bf.d2, 0);
-  const double Dt = M.Deltat, nu = M.nu;
-
-  if (is_mean) {
-    // ---- mean line u00 + i w00 (no shear phase) ----
-    double *mu = bf.mu + (long)b * 2 * N + c;
-    double *mwk = bf.mwk + (long)b * 2 * N + c;
-    double *mrf = bf.mrf + (long)b * 2 * N + c;
-    double *mdu = bf.mdu + (long)b * 2 * N + c;
-    const cd one = mk(1.0, 0.0);
-    const Tail T1 = make_tail(V1, one, N), T2 = make_tail(V2, one, N);
-    if (mode >= 1) {
-      const int rk = mode - 1;
-      const double gk = kGama[rk], zk = kZeta[rk];
-      // visc3d(u00, rf0u, m=1, rk=0): rf0u += nu * u00'' (cross.f90:666-672), then
-      // RK accumulate, update and zeta store (cross.f90:703-756)
-      solve_line(mu, 2, ybuf, ys, N, V2, T2, one, one, c, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6],
-                 false, [&](int j, double x) {
-                   const double rf = mrf[2 * j] + nu * (-(0.0 * mu[2 * j]) + x);
-                   double wk = (rk == 0) ? gk * rf : mwk[2 * j] + gk * rf;
-                   const double un = mu[2 * j] + Dt * wk;
-                   if (rk < 2) wk = rf * zk;
-                   if (active) {
-                     mu[2 * j] = un;
-                     mwk[2 * j] = wk;
-                   }
-                 });
-    }
-    if (mode == 0 || next) {
-      // derivyc(u00, rf0u, 1, 1, 0) used by hvhg (cross.f90:1186-1192)
-      solve_line(mu, 2, ybuf, ys, N, V1, T1, one, one, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true,
-                 [&](int j, double x) {
-                   if (active) mdu[2 * j] = x;
-                 });
-    }
-    return;
-  }
-
-  const long off = (long)b * g.field + 2 * lc + c;
-  const long ps = g.plane;
-  double *vor = bf.vor + off, *phi = bf.phi + off, *vorwk = bf.vorwk + off,
-         *phiwk = bf.phiwk + off, *G = bf.G + off, *Vv = bf.V + off, *D = bf.D + off;
-  const bool is00 = (i == 0 && k == 0);
-  const double a = g.alp * i;
-  const int kzs = (k <= g.nz) ? k : k - g.mz;
-  const double gz = g.gam * kzs;
-  const double k2 = a * a + gz * gz;
-  const double *sho = bf.sh_old + (long)b * 4 * g.nkx;
-  const double *shn = bf.sh_new + (long)b * 4 * g.nkx;
-  const FacView VH(bf.hz, lc);
-
-  if (mode == 0) {
-    // set_conj on the state for kx = 0 (operators.f90:1382-1429)
-    if (i == 0 && k > g.nz) {
-      const long src = (long)b * g.field + 2 * (long)((g.mz - k) * g.nkx) + c;
-      for (int j = 0; j < N; j++) {
-        double vv = bf.vor[src + (long)j * ps], pp = bf.phi[src + (long)j * ps];
-        if (active) {
-          vor[(long)j * ps] = c ? -vv : vv;
-          phi[(long)j * ps] = c ? -pp : pp;
-        }
-      }
-    }
-    const cd shp = ldc(sho + 2 * i), shm = ldc(sho + 2 * (g.nkx + i));
-    const Tail TH = make_tail(VH, shp, N), T1 = make_tail(V1, shp, N);
-    // v = lapcdy(phi) (cross.f90:408-426); hg(0,0) stays zero
-    solve_line(phi, ps, ybuf, ys, N, VH, TH, shp, shm, c, g.pr2[3], g.pr2[4], g.pr2[5], g.pr2[6],
-               false, [&](int j, double x) {
-                 if (active) G[(long)j * ps] = is00 ? 0.0 : x;
-               });
-    solve_line(vor, ps, ybuf, ys, N, V1, T1, shp, shm, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true,
-               [&](int j, double x) {
-                 if (active) D[(long)j * ps] = x;
-               });
-    solve_line(G, ps, ybuf, ys, N, V1, T1, shp, shm, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true,
-               [&](int j, double x) {
-                 if (active) Vv[(long)j * ps] = x;
-               });
-    return;
-  }
-
-  const int rk = mode - 1;
-  const double gk = kGama[rk], zk = kZeta[rk];
-  const cd shpo = ldc(sho + 2 * i), shmo = ldc(sho + 2 * (g.nkx + i));
-  const cd shpn = ldc(shn + 2 * i), shmn = ldc(shn + 2 * (g.nkx + i));
-  const double *mf1 = bf.mf1 + (long)b * 2 * N * g.nkx + 2 * i;
-  const double *mf2 = bf.mf2 + (long)b * 2 * N * g.nkx + 2 * i;
-  const double nuv = is00 ? 0.0 : nu;
-  {
-    // (1) dvordy <- d/dy of dH1/dx + dH3/dz  (cross.f90:565-575)
-    const Tail T1 = make_tail(V1, shpo, N);
-    solve_line(D, ps, ybuf, ys, N, V1, T1, shpo, shmo, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true,
-               [&](int j, double x) {
-                 if (active) D[(long)j * ps] = x;
-               });
-  }
-  const Tail T2 = make_tail(V2, shpo, N);
-  // (2) hg += nu*lap(vor) (visc3d), RK accumulate/update, zeta store + remap
-  solve_line(vor, ps, ybuf, ys, N, V2, T2, shpo, shmo, c, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6],
-             false, [&](int j, double x) {
-               const long q = (long)j * ps;
-               const double vo = vor[q];
-               const double hgp = G[q] + nuv * (-(k2 * vo) + x);
-               double wk = (rk == 0) ? gk * hgp : vorwk[q] + gk * hgp;
-               const double vn = vo + Dt * wk;
-               const cd m2 = ldc(mf2 + 2 * (long)j * g.nkx);
-               const double vnm = cmul_c(vn, __shfl_xor_sync(0xffffffffu, vn, 1), m2, c);
-               if (rk < 2) {
-                 const cd m1 = ldc(mf1 + 2 * (long)j * g.nkx);
-                 const double wz = hgp * zk;
-                 wk = cmul_c(wz, __shfl_xor_sync(0xffffffffu, wz, 1), m1, c);
-               }
-               if (active) {
-                 vor[q] = vnm;
-                 vorwk[q] = wk;
-               }
-             });
-  // (3) hv = hv - dvordy + nu*lap(phi), RK accumulate/update, zeta store + remap
-  solve_line(phi, ps, ybuf, ys, N, V2, T2, shpo, shmo, c, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6],
-             false, [&](int j, double x) {
-               const long q = (long)j * ps;
-               const double ph = phi[q];
-               const double hvp = (Vv[q] - D[q]) + nuv * (-(k2 * ph) + x);
-               double wk = (rk == 0) ? gk * hvp : phiwk[q] + gk * hvp;
-               const double pn = ph + Dt * wk;
-               const cd m2 = ldc(mf2 + 2 * (long)j * g.nkx);
-               const double pnm = cmul_c(pn, __shfl_xor_sync(0xffffffffu, pn, 1), m2, c);
-               if (rk < 2) {
-                 const cd m1 = ldc(mf1 + 2 * (long)j * g.nkx);
-                 const double wz = hvp * zk;
-                 wk = cmul_c(wz, __shfl_xor_sync(0xffffffffu, wz, 1), m1, c);
-               }
-               if (active) {
-                 phi[q] = pnm;
-                 phiwk[q] = wk;
-               }
-             });
-  // (4) v = lapcdy(phi) with the shear phase at t + c_k dt (cross.f90:784-795)
-  {
-    const Tail TH = make_tail(VH, shpn, N);
-    solve_line(phi, ps, ybuf, ys, N, VH, TH, shpn, shmn, c, g.pr2[3], g.pr2[4], g.pr2[5],
-               g.pr2[6], false, [&](int j, double x) {
-                 if (active && !is00) G[(long)j * ps] = x;
-               });
-  }
-  if (next) {
-    // (5) derivatives the next substep starts from (cross.f90:434-445)
-    const Tail T1 = make_tail(V1, shpn, N);
-    solve_line(vor, ps, ybuf, ys, N, V1, T1, shpn, shmn, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6],
-               true, [&](int j, double x) {
-                 if (active) D[(long)j * ps] = x;
-               });
-    solve_line(G, ps, ybuf, ys, N, V1, T1, shpn, shmn, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true,
-               [&](int j, double x) {
-                 if (active) Vv[(long)j * ps] = x;
-               });
-  }
-}
-
-// ---------------------------------------------------------------------------
 // plane stage 1: reconstruction + backward z-transforms
 // ---------------------------------------------------------------------------
 // k index -> position on the padded z grid (fill00)
@@ -530,222 +332,6 @@ __global__ void __launch_bounds__(T) k_p3(Grid g, Bufs bf) {
   }
 }
 
-// ---------------------------------------------------------------------------
-// per-box scalar work: Delta t, statistics record, offsets and phase tables
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_phase(Grid g, Bufs bf, int rk) {
-  const int b = blockIdx.x;
-  Member &M = bf.mem[b];
-  __shared__ double s_xb, s_xt, s_xnb, s_xnt, s_f1, s_f2;
-  __shared__ double s_q[SB_NHIST_Q + 1];
-  __shared__ int s_halt;
-  if (threadIdx.x == 0) {
-    if (rk == 0) {  // entry of a cross() call (cross.f90:76-113)
-      M.istop = 0;
-      M.idump = 0;
-      M.halted = 0;
-      M.istep = 1;
-      M.ihist = 1;
-      M.ntrace = 0;
-      M.flags = 0;
-      for (int q = 0; q < 4; q++) M.umax_bits[q] = 0ull;
-    }
-    s_halt = M.halted;
-  }
-  __syncthreads();
-  if (s_halt) return;
-  const bool shear = fabs(g.s) > 0.01;
-  if (rk == 1 && M.ihist) {
-    // hist 'w': sums over planes of the per-block partials (cross.f90:2070-2080)
-    const int q = threadIdx.x;
-    if (q < SB_NHIST_Q) {
-      double tot = 0.0;
-      for (int j = 0; j < g.my; j++) {
-        double pl = 0.0;
-        for (int cb = 0; cb < g.ncb; cb++) pl += bf.hpart[(((long)b * g.my + j) * g.ncb + cb) * SB_NHIST_Q + q];
-        tot += pl;
-      }
-      s_q[q] = tot;
-    } else if (q == SB_NHIST_Q) {
-      // production P_k = -<omega_z>(-uv) + <omega_z>^2/Re per plane, with the
-      // mean shear -s included in <omega_z> (cross.f90:1901-1912)
-      double tot = 0.0;
-      for (int j = 0; j < g.my; j++) {
-        double uvr = 0.0;
-        for (int cb = 0; cb < g.ncb; cb++) uvr += bf.hpart[(((long)b * g.my + j) * g.ncb + cb) * SB_NHIST_Q + 3];
-        const double o3 = -bf.mdu[2 * ((long)b * g.my + j)] - g.s;
-        tot += -o3 * (-uvr) + (o3 * o3) * (1.0 / M.Re);
-      }
-      s_q[q] = tot;
-    }
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    if (rk == 0 || rk == 1) {
-      M.xwkb = M.xoffb;
-      M.xwkt = M.xofft;
-    } else {
-      M.xwkb = M.xwkb_n;
-      M.xwkt = M.xwkt_n;
-    }
-    if (rk == 1) {
-      // umax (cross.f90:1205-1216,1436-1442) and Delta t (cross.f90:1598-1711)
-      double uinit = 0.0;
-      if (M.istep == 1 && M.readflag == 0) uinit = (fabs(g.s) > 0.5) ? 1.0 : M.uprim;
-      for (int q = 0; q < 4; q++) {
-        const double v = __longlong_as_double((long long)M.umax_bits[q]);
-        M.umax[q] = v > uinit ? v : uinit;
-      }
-      double dt;
-      if (M.fixed_dt > 0.0) {
-        dt = M.fixed_dt;
-        const double m = fmax(fmax(M.umax[0] * g.pi / g.dx, M.umax[2] * 2.5 / g.dy), M.umax[3] * g.pi / g.dz);
-        M.CFLcur = dt * m;
-        const double vv = fmax(fmax(g.pi * g.pi / g.dx / g.dx, 6.25 / g.dy / g.dy), g.pi * g.pi / g.dz / g.dz);
-        M.CFLv = (1.0 / M.Re) * dt * vv;
-      } else {
-        const double m = fmax(fmax(M.umax[0] * M.cflx, M.umax[2] * M.cfly), M.umax[3] * M.cflz);
-        dt = 1.0 / m;
-        M.CFLcur = M.CFL;
-        M.CFLv = M.CFL * M.cflvv * dt;
-        if (M.CFLv > M.CFL) dt = 1.0 / M.cflvv;
-      }
-      double Deltat = dt;
-      if (Deltat < 1e-10) {
-        M.istop = 1;
-        M.flags |= SBF_DIVERGED;
-      }
-      if ((M.time + Deltat) > M.dumptime) {
-        Deltat = fabs(M.dumptime - M.time);
-        if (M.dumptime > (M.etime - 1e-13)) {
-          M.istop = 1;
-          M.flags |= SBF_ETIME;
-        }
-        M.dumptime = M.dumptime + M.dtimag;
-        M.idump = 1;
-      } else if ((M.time + Deltat) > M.etime) {
-        Deltat = fabs(M.etime - M.time);
-        M.istop = 1;
-        M.flags |= SBF_ETIME;
-      }
-      M.Deltat = Deltat;
-      if (M.ihist) {
-        double uner[10], uner2[4];
-        const double my = (double)g.my;
-        for (int q = 0; q < 3; q++) uner[q] = sqrt(fabs(s_q[q] / my));
-        for (int q = 3; q < 6; q++) uner[q] = s_q[q] / my;
-        for (int q = 6; q < 9; q++) uner[q] = sqrt(fabs(s_q[q] / my));
-        uner[9] = s_q[10] / my;
-        uner2[0] = s_q[SB_NHIST_Q] / my;
-        uner2[1] = s_q[9] / my;
-        uner2[2] = 0.0;
-        uner2[3] = 0.0;
-        if (M.ntrace < M.trace_cap) {
-          double *rec = bf.trace + ((long)b * M.trace_cap + M.ntrace) * SB_TRACE_LEN;
-          rec[0] = M.time;
-          rec[1] = M.Deltat;
-          for (int q = 0; q < 10; q++) rec[2 + q] = uner[q];
-          rec[12] = M.CFLcur;
-          rec[13] = M.CFLv;
-          rec[14] = M.umax[1];
-          rec[15] = M.umax[2];
-          rec[16] = M.umax[3];
-          rec[17] = M.xoffb;
-          rec[18] = M.xofft;
-          rec[19] = M.umax[0];
-          for (int q = 0; q < 4; q++) rec[20 + q] = uner2[q];
-        }
-        M.ntrace++;
-        if (isnan(uner[0])) {
-          M.istop = 1;
-          M.flags |= SBF_NAN;
-        }
-        if (uner[1] / (2.0 * g.pi / g.gam) < 1e-5) {
-          M.istop = 1;
-          M.flags |= SBF_LAMINAR;
-        }
-        M.ihist = 0;
-      }
-    }
-    if (rk >= 1) {
-      const double Dt = M.Deltat;
-      const double r1 = kCa[rk - 1] * Dt;
-      if (shear) {
-        M.xwkb_n = M.xoffb + r1 * (g.s * (-g.Ly));
-        M.xwkt_n = M.xofft + r1 * (g.s * g.Ly);
-      } else {
-        M.xwkb_n = M.xwkb;
-        M.xwkt_n = M.xwkt;
-      }
-      s_f1 = (rk == 1) ? -(kGama[0] * Dt * g.s) : -((kGama[1] + kZeta[0]) * Dt * g.s);
-      s_f2 = (rk == 1) ? -(g.s * r1) : -(g.s * (kCa[rk - 1] - kCa[rk - 2]) * Dt);
-      s_xnb = M.xwkb_n;
-      s_xnt = M.xwkt_n;
-    }
-    s_xb = M.xwkb;
-    s_xt = M.xwkt;
-  }
-  __syncthreads();
-  const int nkx = g.nkx;
-  double *sho = bf.sh_old + (long)b * 4 * nkx;
-  double *shn = bf.sh_new + (long)b * 4 * nkx;
-  for (int i = threadIdx.x; i < nkx; i += blockDim.x) {
-    const double a = g.alp * i;
-    double sn, cs;
-    if (shear) {
-      sincos((-a) * s_xt, &sn, &cs);
-      sho[2 * i] = cs; sho[2 * i + 1] = sn;
-      sincos((-a) * s_xb, &sn, &cs);
-      sho[2 * (nkx + i)] = cs; sho[2 * (nkx + i) + 1] = sn;
-    } else {
-      sho[2 * i] = 1.0; sho[2 * i + 1] = 0.0;
-      sho[2 * (nkx + i)] = 1.0; sho[2 * (nkx + i) + 1] = 0.0;
-    }
-    if (rk >= 1) {
-      if (shear) {
-        sincos((-a) * s_xnt, &sn, &cs);
-        shn[2 * i] = cs; shn[2 * i + 1] = sn;
-        sincos((-a) * s_xnb, &sn, &cs);
-        shn[2 * (nkx + i)] = cs; shn[2 * (nkx + i) + 1] = sn;
-      } else {
-        shn[2 * i] = 1.0; shn[2 * i + 1] = 0.0;
-        shn[2 * (nkx + i)] = 1.0; shn[2 * (nkx + i) + 1] = 0.0;
-      }
-    }
-  }
-  if (rk >= 1) {
-    // moving_frame phases exp(i kx y_j tau) (operators.f90:119-123)
-    double *m1 = bf.mf1 + (long)b * 2 * g.my * nkx;
-    double *m2 = bf.mf2 + (long)b * 2 * g.my * nkx;
-    for (int q = threadIdx.x; q < g.my * nkx; q += blockDim.x) {
-      const int jj = q / nkx, i = q - jj * nkx;
-      const double ay = (g.alp * i) * ((double)jj * g.dy - 0.5 * g.Ly);
-      double sn, cs;
-      if (rk < 3) {
-        sincos(ay * s_f1, &sn, &cs);
-        m1[2 * q] = cs; m1[2 * q + 1] = sn;
-      }
-      sincos(ay * s_f2, &sn, &cs);
-      m2[2 * q] = cs; m2[2 * q + 1] = sn;
-    }
-  }
-}
-
-// end of a step: offsets, time, next-step flags (cross.f90:1002-1013, 336-376)
-__global__ void k_finish(Grid g, Bufs bf) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= g.B) return;
-  Member &M = bf.mem[b];
-  if (M.halted) return;
-  M.xoffb = M.xwkb_n;
-  M.xofft = M.xwkt_n;
-  M.time = M.time + M.Deltat;
-  M.istep += 1;
-  if ((M.istep - 1) != 1 && M.istop) M.halted = 1;
-  if ((M.istep - 1) % M.nhist == 0) M.ihist = 1;
-  for (int q = 0; q < 4; q++) M.umax_bits[q] = 0ull;
-}
-
 // pencil (j fastest, then kx, then kz) <-> plane-major layout, one box
 __global__ void k_pencil_to_plane(Grid g, const double *__restrict__ pen, double *__restrict__ dst) {
   const long n = (long)g.my * g.nkx * g.mz;
@@ -773,7 +359,7 @@ __global__ void k_plane_to_pencil(Grid g, const double *__restrict__ src, double
 // ---------------------------------------------------------------------------
 // launch helpers
 // ---------------------------------------------------------------------------
-template <int NZ, int CB, int T>
+template <int NZ, int CB, int T, int T3>
 static cudaError_t launch_p13(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, int which,
                               bool prep) {
   dim3 grid(g.ncb, g.my, g.B);
@@ -781,13 +367,13 @@ static cudaError_t launch_p13(const Grid &g, const Bufs &bf, int rk, cudaStream_
   const size_t sm3 = sizeof(double2) * 2 * (3 * CB * NZ);
   if (prep) {
     cudaFuncSetAttribute(k_p1<NZ, CB, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
-    cudaFuncSetAttribute(k_p3<NZ, CB, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+    cudaFuncSetAttribute(k_p3<NZ, CB, T3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
     return cudaGetLastError();
   }
   if (which == 1)
     k_p1<NZ, CB, T><<<grid, T, sm1, st>>>(g, bf, rk);
   else
-    k_p3<NZ, CB, T><<<grid, T, sm3, st>>>(g, bf);
+    k_p3<NZ, CB, T3><<<grid, T3, sm3, st>>>(g, bf);
   return cudaGetLastError();
 }
 
@@ -803,7 +389,7 @@ static cudaError_t launch_p2(const Grid &g, const Bufs &bf, int rk, cudaStream_t
   return cudaGetLastError();
 }
 
-int plane_cb(int mgalz) { return mgalz > 96 ? 8 : 16; }
+int plane_cb(int) { return 8; }
 
 // stage 1..3: launch; stage 0: set the kernels' shared-memory limits (once)
 cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
@@ -822,31 +408,17 @@ cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaS
     if (!prep || e != cudaSuccess) return e;
   }
   switch (g.mgalz) {
-    case 32: return launch_p13<32, 16, 128>(g, bf, rk, st, stage, prep);
-    case 48: return launch_p13<48, 16, 128>(g, bf, rk, st, stage, prep);
-    case 64: return launch_p13<64, 16, 128>(g, bf, rk, st, stage, prep);
-    case 96: return launch_p13<96, 16, 128>(g, bf, rk, st, stage, prep);
-    case 192: return launch_p13<192, 8, 128>(g, bf, rk, st, stage, prep);
+    case 32: return launch_p13<32, 8, 128, 96>(g, bf, rk, st, stage, prep);
+    case 48: return launch_p13<48, 8, 128, 96>(g, bf, rk, st, stage, prep);
+    case 64: return launch_p13<64, 8, 128, 96>(g, bf, rk, st, stage, prep);
+    case 96: return launch_p13<96, 8, 128, 96>(g, bf, rk, st, stage, prep);
+    case 192: return launch_p13<192, 8, 128, 96>(g, bf, rk, st, stage, prep);
     default: return cudaErrorInvalidValue;
   }
 }
 
-cudaError_t launch_line(const Grid &g, const Bufs &bf, int mode, int next, cudaStream_t st) {
-  const long nth = (long)g.B * g.tpm;
-  const int T = 128;
-  k_line<<<(unsigned)((nth + T - 1) / T), T, 0, st>>>(g, bf, mode, next);
-  return cudaGetLastError();
-}
 
-cudaError_t launch_phase(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
-  k_phase<<<g.B, 256, 0, st>>>(g, bf, rk);
-  return cudaGetLastError();
-}
 
-cudaError_t launch_finish(const Grid &g, const Bufs &bf, cudaStream_t st) {
-  k_finish<<<(g.B + 127) / 128, 128, 0, st>>>(g, bf);
-  return cudaGetLastError();
-}
 
 cudaError_t launch_pencil_to_plane(const Grid &g, const double *pen, double *dst, cudaStream_t st) {
   k_pencil_to_plane<<<256, 256, 0, st>>>(g, pen, dst);

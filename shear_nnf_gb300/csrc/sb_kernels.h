@@ -10,8 +10,13 @@ namespace sb {
 int plane_cb(int mgalz);
 bool supported_grid(int mgalx, int mgalz);
 cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st);
-cudaError_t launch_line(const Grid &g, const Bufs &bf, int mode, int next, cudaStream_t st);
-cudaError_t launch_phase(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
+cudaError_t prepare_line(const Grid &g);
+size_t line_smem(const Grid &g);
+cudaError_t launch_lineA(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
+cudaError_t launch_lineB(const Grid &g, const Bufs &bf, int mode, cudaStream_t st);
+cudaError_t launch_setconj(const Grid &g, const Bufs &bf, cudaStream_t st);
+cudaError_t launch_scalar(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
+cudaError_t launch_tables(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
 cudaError_t launch_finish(const Grid &g, const Bufs &bf, cudaStream_t st);
 cudaError_t launch_pencil_to_plane(const Grid &g, const double *pen, double *dst, cudaStream_t st);
 cudaError_t launch_plane_to_pencil(const Grid &g, const double *src, double *pen, cudaStream_t st);

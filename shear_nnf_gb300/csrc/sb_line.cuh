@@ -78,6 +78,29 @@ __device__ __forceinline__ Tail make_tail(const FacView &V, cd shp, int N) {
   return T;
 }
 
+// shear tails kept in tables (SB_TAIL doubles each)
+__device__ __forceinline__ void store_tail(double *p, const Tail &T) {
+  const cd v[9] = {T.Le5, T.Le4, T.Le3, T.Lf4, T.Lf3, T.Lf2, T.Lg3, T.Lg2, T.Lg1};
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    p[2 * q] = v[q].x;
+    p[2 * q + 1] = v[q].y;
+  }
+  p[18] = T.Dm2;
+  p[19] = T.Dm1;
+  p[20] = T.Dm0;
+}
+__device__ __forceinline__ Tail load_tail(const double *p) {
+  Tail T;
+  cd *v[9] = {&T.Le5, &T.Le4, &T.Le3, &T.Lf4, &T.Lf3, &T.Lf2, &T.Lg3, &T.Lg2, &T.Lg1};
+#pragma unroll
+  for (int q = 0; q < 9; q++) *v[q] = mk(__ldg(p + 2 * q), __ldg(p + 2 * q + 1));
+  T.Dm2 = __ldg(p + 18);
+  T.Dm1 = __ldg(p + 19);
+  T.Dm0 = __ldg(p + 20);
+  return T;
+}
+
 // component c of a complex value held by the lane pair (c=0: re, c=1: im)
 __device__ __forceinline__ cd pair_full(double own, int c) {
   double oth = __shfl_xor_sync(0xffffffffu, own, 1);
@@ -116,6 +139,7 @@ __device__ __forceinline__ void solve_line(const double *u, long ps, double *ybu
   double y1 = 0.0, y2 = 0.0, y3 = 0.0;
   double Se = 0.0, Sf = 0.0, Sg = 0.0;
   double bN2 = 0.0, bN1 = 0.0, bN0 = 0.0;
+#pragma unroll 4
   for (int j = 0; j < N; j++) {
     double rhs;
     if (anti)
@@ -168,6 +192,7 @@ __device__ __forceinline__ void solve_line(const double *u, long ps, double *ybu
   epi(N - 6, comp(x5, c));
   const double pe = comp(Pe, c), pf = comp(Pf, c), pg = comp(Pg, c);
   double xa = comp(x5, c), xb = comp(x4, c), xc = comp(x3, c);
+#pragma unroll 4
   for (int j = N - 7; j >= 0; j--) {
     const int i = j + 1;
     double x = V.Dm(i) * ybuf[(long)j * ys] - V.La(i + 1) * xa - V.Lb(i + 2) * xb -

@@ -1,0 +1,546 @@
+// sb_yline.cu -- y-line stage, per-box scalars and phase tables of the RK3 step.
+//
+// The y-operators of one substep (cross.f90:565-795 and the first derivatives of
+// the next substep, cross.f90:434-445) run as two kernels so that independent
+// solves occupy separate warps (GB300's FP64 pipe needs about one busy warp per
+// SM sub-partition, and one warp per line component is too few):
+//   k_lineA  role 0: d/dy of dH1/dx + dH3/dz                 (derivyc, -> T)
+//            role 1: nu*lap(omega_y), RK3 update of omega_y, zeta store and
+//                    moving_frame remaps                       (visc3d + update)
+//            role 2: d2(phi)/dy2                               (derivyc, -> S)
+//            mean warp: nu*u00'', RK3 update of u00, w00
+//   k_lineB  role 0: d(omega_y)/dy for the next substep         (-> D)
+//            role 1: RK3 update of phi, v = lapcdy(phi), dv/dy  (-> phi, G, V)
+//            mean warp: du00/dy, dw00/dy for the next substep
+// The same k_lineB (mode 0) is the prologue of a cross call: v from phi on the
+// first step (cross.f90:408-426) and the first derivatives.  Forward
+// substitutions are kept in shared memory, one column per thread.
+//   k_scalar per box: Delta t from the CFL (cross.f90:1598-1711), the UNER record
+//            (cross.f90:2064-2118), image offsets (cross.f90:726-746)
+//   k_tables shear phases exp(-i kx xoff), the shear tails of the d/dy and d2/dy2
+//            factorisations per kx (modChol_addshear, diffy_shear_hepta.f90:760-870)
+//            and the moving_frame phases (operators.f90:86-145)
+//   k_finish end of a step (cross.f90:1002-1013) and the stop check (cross.f90:356)
+#include <cuda_runtime.h>
+
+#include "sb_common.cuh"
+#include "sb_kernels.h"
+#include "sb_line.cuh"
+
+namespace sb {
+
+__device__ __forceinline__ cd ldc2(const double *p) { return mk(p[0], p[1]); }
+
+// thread -> (member, role, line, component) of a y-line kernel with `roles`
+// roles; the last warp of every member is the mean line u00 + i w00
+struct LineThread {
+  int b, role, c, i, k;
+  long lc;
+  bool active, mean;
+};
+__device__ __forceinline__ bool line_thread(const Grid &g, int tpm, int roles, LineThread *L) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  L->b = (int)(t / tpm);
+  if (L->b >= g.B) return false;
+  const int r = (int)(t - (long)L->b * tpm);
+  L->c = r & 1;
+  L->role = r / g.nlines_pad;
+  L->mean = L->role >= roles;
+  const int nl = g.nkx * g.mz;
+  if (L->mean) {
+    L->lc = 0;
+    L->active = (r - roles * g.nlines_pad) < 2;
+  } else {
+    L->lc = (r - L->role * g.nlines_pad) >> 1;
+    L->active = L->lc < nl;
+    if (!L->active) L->lc = nl - 1;
+  }
+  L->i = (int)(L->lc % g.nkx);
+  L->k = (int)(L->lc / g.nkx);
+  return true;
+}
+
+// one thread's column of the shared-memory forward-substitution buffer
+__device__ __forceinline__ double *ycol() {
+  extern __shared__ double sm_y[];
+  return sm_y + threadIdx.x;
+}
+
+// copy a solution kept in shared memory to a field line
+__device__ __forceinline__ void store_col(const double *ys, int ystr, double *__restrict__ dst, long ps,
+                                          int N, bool active) {
+  if (!active) return;
+#pragma unroll 4
+  for (int j = 0; j < N; j++) dst[(long)j * ps] = ys[j * ystr];
+}
+
+// RK3 accumulate/update of one field line with the zeta store and both
+// moving_frame remaps (cross.f90:694-781), fused per point.  x = d2f/dy2 in
+// the shared buffer; rhs = the nonlinear right-hand side (minus `sub` if
+// given); f, fwk the field and its RK work array.
+__device__ __forceinline__ void rk_update(const double *ys, int ystr, const double *__restrict__ rhs,
+                                          const double *__restrict__ sub, double *__restrict__ f,
+                                          double *__restrict__ fwk, long ps, int N, int rk,
+                                          double nuv, double k2, double Dt,
+                                          const double *__restrict__ mf1,
+                                          const double *__restrict__ mf2, long mfs, int c,
+                                          bool active) {
+  const double gk = kGama[rk], zk = kZeta[rk];
+#pragma unroll 2
+  for (int j = 0; j < N; j++) {
+    const long q = (long)j * ps;
+    const double x = ys[j * ystr];
+    const double fo = f[q];
+    double h = rhs[q];
+    if (sub) h = h - sub[q];
+    h = h + nuv * (-(k2 * fo) + x);
+    double wk = (rk == 0) ? gk * h : fwk[q] + gk * h;
+    const double fn = fo + Dt * wk;
+    const cd m2 = ldc2(mf2 + (long)j * mfs);
+    const double fnm = cmul_c(fn, __shfl_xor_sync(0xffffffffu, fn, 1), m2, c);
+    if (rk < 2) {
+      const cd m1 = ldc2(mf1 + (long)j * mfs);
+      const double wz = h * zk;
+      wk = cmul_c(wz, __shfl_xor_sync(0xffffffffu, wz, 1), m1, c);
+    }
+    if (active) {
+      f[q] = fnm;
+      fwk[q] = wk;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(64) k_lineA(Grid g, Bufs bf, int rk1) {
+  LineThread L;
+  if (!line_thread(g, g.tpmA, 3, &L)) return;
+  Member &M = bf.mem[L.b];
+  if (M.halted) return;  // uniform per warp (every role spans whole warps)
+  const int N = g.my, c = L.c, ystr = blockDim.x;
+  const int rk = rk1 - 1;
+  double *ys = ycol();
+  const FacView V1(bf.d1, 0), V2(bf.d2, 0);
+  const double Dt = M.Deltat, nu = M.nu;
+  if (L.mean) {
+    // visc3d(u00, rf0u, m=1, rk=0) and the RK3 update of the mean profiles
+    // (cross.f90:666-672,703-723,753-756); no shear phase, no remap
+    double *mu = bf.mu + (long)L.b * 2 * N + c;
+    double *mwk = bf.mwk + (long)L.b * 2 * N + c;
+    const double *mrf = bf.mrf + (long)L.b * 2 * N + c;
+    const cd one = mk(1.0, 0.0);
+    const Tail T2 = load_tail(bf.tl2o + (long)L.b * g.nkx * SB_TAIL);
+    solve_line(mu, 2, ys, ystr, N, V2, T2, one, one, c, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6],
+               false, [&](int j, double x) { ys[j * ystr] = x; });
+    const double gk = kGama[rk], zk = kZeta[rk];
+    for (int j = 0; j < N; j++) {
+      const double rf = mrf[2 * j] + nu * (-(0.0 * mu[2 * j]) + ys[j * ystr]);
+      double wk = (rk == 0) ? gk * rf : mwk[2 * j] + gk * rf;
+      const double un = mu[2 * j] + Dt * wk;
+      if (rk < 2) wk = rf * zk;
+      if (L.active) {
+        mu[2 * j] = un;
+        mwk[2 * j] = wk;
+      }
+    }
+    return;
+  }
+  const long off = (long)L.b * g.field + 2 * L.lc + c;
+  const long ps = g.plane;
+  const int i = L.i, k = L.k;
+  const cd shp = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * i);
+  const cd shm = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
+  if (L.role == 0) {
+    // d/dy (dH1/dx + dH3/dz) (cross.f90:565-575)
+    const Tail T1 = load_tail(bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL);
+    solve_line(bf.D + off, ps, ys, ystr, N, V1, T1, shp, shm, c, 0.0, g.rh1[4], g.rh1[5],
+               g.rh1[6], true, [&](int j, double x) { ys[j * ystr] = x; });
+    store_col(ys, ystr, bf.T + off, ps, N, L.active);
+    return;
+  }
+  const Tail T2 = load_tail(bf.tl2o + ((long)L.b * g.nkx + i) * SB_TAIL);
+  if (L.role == 2) {
+    // d2(phi)/dy2 for the viscous term of the phi equation (cross.f90:660)
+    solve_line(bf.phi + off, ps, ys, ystr, N, V2, T2, shp, shm, c, g.rh2[3], g.rh2[4], g.rh2[5],
+               g.rh2[6], false, [&](int j, double x) { ys[j * ystr] = x; });
+    store_col(ys, ystr, bf.S + off, ps, N, L.active);
+    return;
+  }
+  // role 1: hg += nu*lap(omega_y) (visc3d, cross.f90:659), RK3 update, remaps
+  solve_line(bf.vor + off, ps, ys, ystr, N, V2, T2, shp, shm, c, g.rh2[3], g.rh2[4], g.rh2[5],
+             g.rh2[6], false, [&](int j, double x) { ys[j * ystr] = x; });
+  const bool is00 = (i == 0 && k == 0);
+  const double a = g.alp * i;
+  const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
+  const double *mf1 = bf.mf1 + (long)L.b * 2 * N * g.nkx + 2 * i;
+  const double *mf2 = bf.mf2 + (long)L.b * 2 * N * g.nkx + 2 * i;
+  rk_update(ys, ystr, bf.G + off, nullptr, bf.vor + off, bf.vorwk + off, ps, N, rk,
+            is00 ? 0.0 : nu, a * a + gz * gz, Dt, mf1, mf2, 2 * g.nkx, c, L.active);
+}
+
+__global__ void __launch_bounds__(64) k_lineB(Grid g, Bufs bf, int mode) {
+  LineThread L;
+  if (!line_thread(g, g.tpmB, 2, &L)) return;
+  Member &M = bf.mem[L.b];
+  if (M.halted) return;
+  const int N = g.my, c = L.c, ystr = blockDim.x;
+  double *ys = ycol();
+  const FacView V1(bf.d1, 0);
+  if (L.mean) {
+    // derivyc(u00, rf0u, 1, 1, 0) and of w00, used by hvhg (cross.f90:1186-1192)
+    double *mu = bf.mu + (long)L.b * 2 * N + c;
+    double *mdu = bf.mdu + (long)L.b * 2 * N + c;
+    const cd one = mk(1.0, 0.0);
+    const Tail T1 = load_tail(bf.tl1o + (long)L.b * g.nkx * SB_TAIL);
+    solve_line(mu, 2, ys, ystr, N, V1, T1, one, one, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true,
+               [&](int j, double x) {
+                 if (L.active) mdu[2 * j] = x;
+               });
+    return;
+  }
+  const long off = (long)L.b * g.field + 2 * L.lc + c;
+  const long ps = g.plane;
+  const int i = L.i, k = L.k;
+  // the phase at t + c_k dt (substeps) or at t (prologue)
+  const double *sh = (mode == 0) ? bf.sh_old : bf.sh_new;
+  const double *tl1 = (mode == 0) ? bf.tl1o : bf.tl1n;
+  const cd shp = ldc2(sh + (long)L.b * 4 * g.nkx + 2 * i);
+  const cd shm = ldc2(sh + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
+  const Tail T1 = load_tail(tl1 + ((long)L.b * g.nkx + i) * SB_TAIL);
+  if (L.role == 0) {
+    // d(omega_y)/dy (cross.f90:440)
+    solve_line(bf.vor + off, ps, ys, ystr, N, V1, T1, shp, shm, c, 0.0, g.rh1[4], g.rh1[5],
+               g.rh1[6], true, [&](int j, double x) { ys[j * ystr] = x; });
+    store_col(ys, ystr, bf.D + off, ps, N, L.active);
+    return;
+  }
+  const bool is00 = (i == 0 && k == 0);
+  if (mode >= 1) {
+    // hv = hv - d/dy(dH1/dx + dH3/dz) + nu*lap(phi), RK3 update, remaps
+    // (cross.f90:607,660,694-781)
+    const int rk = mode - 1;
+    const double a = g.alp * i;
+    const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
+    const double *mf1 = bf.mf1 + (long)L.b * 2 * N * g.nkx + 2 * i;
+    const double *mf2 = bf.mf2 + (long)L.b * 2 * N * g.nkx + 2 * i;
+    // the d2(phi)/dy2 of k_lineA goes through the shared buffer
+    const double *S = bf.S + off;
+    for (int j = 0; j < N; j++) ys[j * ystr] = S[(long)j * ps];
+    rk_update(ys, ystr, bf.V + off, bf.T + off, bf.phi + off, bf.phiwk + off, ps, N, rk,
+              is00 ? 0.0 : M.nu, a * a + gz * gz, M.Deltat, mf1, mf2, 2 * g.nkx, c, L.active);
+  }
+  // v = lapcdy(phi) (cross.f90:784-795, first step: 408-426); hg(0,0) keeps
+  // the value the nonlinear stage left (zero), or zero in the prologue
+  {
+    const FacView VH(bf.hz, L.lc);
+    const Tail TH = make_tail(VH, shp, N);
+    solve_line(bf.phi + off, ps, ys, ystr, N, VH, TH, shp, shm, c, g.pr2[3], g.pr2[4], g.pr2[5],
+               g.pr2[6], false, [&](int j, double x) { ys[j * ystr] = x; });
+    if (is00) {
+      if (mode == 0 && L.active)
+        for (int j = 0; j < N; j++) bf.G[off + (long)j * ps] = 0.0;
+    } else {
+      store_col(ys, ystr, bf.G + off, ps, N, L.active);
+    }
+  }
+  // dv/dy (cross.f90:442)
+  solve_line(bf.G + off, ps, ys, ystr, N, V1, T1, shp, shm, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6],
+             true, [&](int j, double x) { ys[j * ystr] = x; });
+  store_col(ys, ystr, bf.V + off, ps, N, L.active);
+}
+
+// set_conj on the state (operators.f90:1382-1429) at entry of a cross call
+__global__ void k_setconj(Grid g, Bufs bf) {
+  const int nneg = g.mz - 1 - g.nz;
+  const long n = (long)g.B * g.my * nneg * 2;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int c = (int)(t & 1);
+    const long r = t >> 1;
+    const int kk = (int)(r % nneg);
+    const int j = (int)((r / nneg) % g.my);
+    const int b = (int)(r / ((long)nneg * g.my));
+    const int k = g.nz + 1 + kk;
+    const long base = (long)b * g.field + (long)j * g.plane;
+    const long dst = base + 2L * k * g.nkx + c, src = base + 2L * (g.mz - k) * g.nkx + c;
+    const double v = bf.vor[src], p = bf.phi[src];
+    bf.vor[dst] = c ? -v : v;
+    bf.phi[dst] = c ? -p : p;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// per-box scalars: entry flags, hist reduction and UNER record, Delta t,
+// image offsets.  One block per box.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
+  const int b = blockIdx.x;
+  Member &M = bf.mem[b];
+  __shared__ double s_q[SB_NHIST_Q + 1];
+  __shared__ double s_part[SB_NHIST_Q + 1][256 / 32];
+  __shared__ int s_halt;
+  if (threadIdx.x == 0) {
+    if (rk == 0) {  // entry of a cross() call (cross.f90:76-113)
+      M.istop = 0;
+      M.idump = 0;
+      M.halted = 0;
+      M.istep = 1;
+      M.ihist = 1;
+      M.ntrace = 0;
+      M.flags = 0;
+      for (int q = 0; q < 4; q++) M.umax_bits[q] = 0ull;
+      M.xwb[0] = M.xoffb;
+      M.xwt[0] = M.xofft;
+    }
+    s_halt = M.halted;
+  }
+  __syncthreads();
+  if (s_halt || rk == 0) return;
+  const bool shear = fabs(g.s) > 0.01;
+  const bool hist = (rk == 1) && M.ihist;
+  if (hist) {
+    // hist 'w': sum over planes of the per-block partials (cross.f90:2070-2080)
+    // and the production Pk, whose mean omega_z includes -s (cross.f90:1901-1912)
+    const int nq = SB_NHIST_Q + 1;
+    double acc[SB_NHIST_Q + 1];
+    for (int q = 0; q < nq; q++) acc[q] = 0.0;
+    for (int j = threadIdx.x; j < g.my; j += blockDim.x) {
+      const double *hp = bf.hpart + ((long)b * g.my + j) * g.ncb * SB_NHIST_Q;
+      double pl[SB_NHIST_Q];
+      for (int q = 0; q < SB_NHIST_Q; q++) pl[q] = 0.0;
+      for (int cb = 0; cb < g.ncb; cb++)
+        for (int q = 0; q < SB_NHIST_Q; q++) pl[q] += hp[cb * SB_NHIST_Q + q];
+      for (int q = 0; q < SB_NHIST_Q; q++) acc[q] += pl[q];
+      const double o3 = -bf.mdu[2 * ((long)b * g.my + j)] - g.s;
+      acc[SB_NHIST_Q] += -o3 * (-pl[3]) + (o3 * o3) * (1.0 / M.Re);
+    }
+    for (int q = 0; q < nq; q++) {
+      double v = acc[q];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if ((threadIdx.x & 31) == 0) s_part[q][threadIdx.x >> 5] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < nq) {
+      double v = 0.0;
+      for (int w = 0; w < (int)(blockDim.x / 32); w++) v += s_part[threadIdx.x][w];
+      s_q[threadIdx.x] = v;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  if (rk == 1) {
+    // umax (cross.f90:1205-1216,1436-1442) and Delta t (cross.f90:1598-1711)
+    double uinit = 0.0;
+    if (M.istep == 1 && M.readflag == 0) uinit = (fabs(g.s) > 0.5) ? 1.0 : M.uprim;
+    for (int q = 0; q < 4; q++) {
+      const double v = __longlong_as_double((long long)M.umax_bits[q]);
+      M.umax[q] = v > uinit ? v : uinit;
+    }
+    double dt;
+    if (M.fixed_dt > 0.0) {
+      dt = M.fixed_dt;
+      const double m = fmax(fmax(M.umax[0] * g.pi / g.dx, M.umax[2] * 2.5 / g.dy), M.umax[3] * g.pi / g.dz);
+      M.CFLcur = dt * m;
+      const double vv = fmax(fmax(g.pi * g.pi / g.dx / g.dx, 6.25 / g.dy / g.dy), g.pi * g.pi / g.dz / g.dz);
+      M.CFLv = (1.0 / M.Re) * dt * vv;
+    } else {
+      const double m = fmax(fmax(M.umax[0] * M.cflx, M.umax[2] * M.cfly), M.umax[3] * M.cflz);
+      dt = 1.0 / m;
+      M.CFLcur = M.CFL;
+      M.CFLv = M.CFL * M.cflvv * dt;
+      if (M.CFLv > M.CFL) dt = 1.0 / M.cflvv;
+    }
+    double Deltat = dt;
+    if (Deltat < 1e-10) {
+      M.istop = 1;
+      M.flags |= SBF_DIVERGED;
+    }
+    if ((M.time + Deltat) > M.dumptime) {
+      Deltat = fabs(M.dumptime - M.time);
+      if (M.dumptime > (M.etime - 1e-13)) {
+        M.istop = 1;
+        M.flags |= SBF_ETIME;
+      }
+      M.dumptime = M.dumptime + M.dtimag;
+      M.idump = 1;
+    } else if ((M.time + Deltat) > M.etime) {
+      Deltat = fabs(M.etime - M.time);
+      M.istop = 1;
+      M.flags |= SBF_ETIME;
+    }
+    M.Deltat = Deltat;
+    if (hist) {
+      double uner[10], uner2[4];
+      const double my = (double)g.my;
+      for (int q = 0; q < 3; q++) uner[q] = sqrt(fabs(s_q[q] / my));
+      for (int q = 3; q < 6; q++) uner[q] = s_q[q] / my;
+      for (int q = 6; q < 9; q++) uner[q] = sqrt(fabs(s_q[q] / my));
+      uner[9] = s_q[10] / my;
+      uner2[0] = s_q[SB_NHIST_Q] / my;
+      uner2[1] = s_q[9] / my;
+      uner2[2] = 0.0;
+      uner2[3] = 0.0;
+      if (M.ntrace < M.trace_cap) {
+        double *rec = bf.trace + ((long)b * M.trace_cap + M.ntrace) * SB_TRACE_LEN;
+        rec[0] = M.time;
+        rec[1] = M.Deltat;
+        for (int q = 0; q < 10; q++) rec[2 + q] = uner[q];
+        rec[12] = M.CFLcur;
+        rec[13] = M.CFLv;
+        rec[14] = M.umax[1];
+        rec[15] = M.umax[2];
+        rec[16] = M.umax[3];
+        rec[17] = M.xoffb;
+        rec[18] = M.xofft;
+        rec[19] = M.umax[0];
+        for (int q = 0; q < 4; q++) rec[20 + q] = uner2[q];
+      }
+      M.ntrace++;
+      if (isnan(uner[0])) {
+        M.istop = 1;
+        M.flags |= SBF_NAN;
+      }
+      if (uner[1] / (2.0 * g.pi / g.gam) < 1e-5) {
+        M.istop = 1;
+        M.flags |= SBF_LAMINAR;
+      }
+      M.ihist = 0;
+    }
+  }
+  // image offsets after this substep (cross.f90:728-731)
+  const double r1 = kCa[rk - 1] * M.Deltat;
+  if (shear) {
+    M.xwb[rk] = M.xoffb + r1 * (g.s * (-g.Ly));
+    M.xwt[rk] = M.xofft + r1 * (g.s * g.Ly);
+  } else {
+    M.xwb[rk] = M.xwb[rk - 1];
+    M.xwt[rk] = M.xwt[rk - 1];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// per-box tables of substep rk (0: prologue): shear phases at the offsets
+// before (old) and after (new) the substep, shear tails of the uniform
+// operators, moving_frame phases.  Grid (blocks, B).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_tables(Grid g, Bufs bf, int rk) {
+  const int b = blockIdx.y;
+  const Member &M = bf.mem[b];
+  if (M.halted) return;
+  const int nkx = g.nkx, my = g.my;
+  const bool shear = fabs(g.s) > 0.01;
+  const int ro = (rk == 0) ? 0 : rk - 1;
+  const double xob = M.xwb[ro], xot = M.xwt[ro];
+  const double xnb = M.xwb[rk], xnt = M.xwt[rk];
+  const double Dt = M.Deltat;
+  const long ntail = (rk == 0) ? 2L * nkx : 3L * nkx;
+  const long nmf = (rk == 0) ? 0 : (long)my * nkx;
+  const long n = ntail + nmf;
+  const FacView V1(bf.d1, 0), V2(bf.d2, 0);
+  for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
+    if (q < ntail) {
+      const int which = (int)(q / nkx), i = (int)(q - (long)which * nkx);
+      const double a = g.alp * i;
+      const bool nw = (which == 2);
+      const double xt = nw ? xnt : xot, xb = nw ? xnb : xob;
+      cd shp = mk(1.0, 0.0), shm = mk(1.0, 0.0);
+      if (shear) {
+        sincos((-a) * xt, &shp.y, &shp.x);
+        sincos((-a) * xb, &shm.y, &shm.x);
+      }
+      // the phase tables themselves (written once per kx)
+      double *sh = (nw ? bf.sh_new : bf.sh_old) + (long)b * 4 * nkx;
+      if (which != 1) {
+        sh[2 * i] = shp.x;
+        sh[2 * i + 1] = shp.y;
+        sh[2 * (nkx + i)] = shm.x;
+        sh[2 * (nkx + i) + 1] = shm.y;
+      }
+      const Tail T = make_tail(which == 1 ? V2 : V1, shp, my);
+      double *dst = (which == 0 ? bf.tl1o : (which == 1 ? bf.tl2o : bf.tl1n)) +
+                    ((long)b * nkx + i) * SB_TAIL;
+      store_tail(dst, T);
+    } else {
+      // moving_frame phases exp(i kx y_j tau) (operators.f90:119-123)
+      const long p = q - ntail;
+      const int jj = (int)(p / nkx), i = (int)(p - (long)jj * nkx);
+      const double f1 = (rk == 1) ? -(kGama[0] * Dt * g.s) : -((kGama[1] + kZeta[0]) * Dt * g.s);
+      const double f2 = (rk == 1) ? -(g.s * (kCa[0] * Dt)) : -(g.s * (kCa[rk - 1] - kCa[rk - 2]) * Dt);
+      const double ay = (g.alp * i) * ((double)jj * g.dy - 0.5 * g.Ly);
+      double sn, cs;
+      double *m1 = bf.mf1 + (long)b * 2 * my * nkx;
+      double *m2 = bf.mf2 + (long)b * 2 * my * nkx;
+      if (rk < 3) {
+        sincos(ay * f1, &sn, &cs);
+        m1[2 * p] = cs;
+        m1[2 * p + 1] = sn;
+      }
+      sincos(ay * f2, &sn, &cs);
+      m2[2 * p] = cs;
+      m2[2 * p + 1] = sn;
+    }
+  }
+}
+
+// end of a step: offsets, time, next-step flags (cross.f90:1002-1013, 336-376)
+__global__ void k_finish(Grid g, Bufs bf) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.B) return;
+  Member &M = bf.mem[b];
+  if (M.halted) return;
+  M.xoffb = M.xwb[3];
+  M.xofft = M.xwt[3];
+  M.xwb[0] = M.xoffb;
+  M.xwt[0] = M.xofft;
+  M.time = M.time + M.Deltat;
+  M.istep += 1;
+  if ((M.istep - 1) != 1 && M.istop) M.halted = 1;
+  if ((M.istep - 1) % M.nhist == 0) M.ihist = 1;
+  for (int q = 0; q < 4; q++) M.umax_bits[q] = 0ull;
+}
+
+// ---------------------------------------------------------------------------
+static const int kLineT = 64;
+
+size_t line_smem(const Grid &g) { return sizeof(double) * kLineT * g.my; }
+
+cudaError_t prepare_line(const Grid &g) {
+  const int sm = (int)line_smem(g);
+  cudaFuncSetAttribute(k_lineA, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_lineB, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lineA(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  const long nth = (long)g.B * g.tpmA;
+  k_lineA<<<(unsigned)((nth + kLineT - 1) / kLineT), kLineT, line_smem(g), st>>>(g, bf, rk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lineB(const Grid &g, const Bufs &bf, int mode, cudaStream_t st) {
+  const long nth = (long)g.B * g.tpmB;
+  k_lineB<<<(unsigned)((nth + kLineT - 1) / kLineT), kLineT, line_smem(g), st>>>(g, bf, mode);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_setconj(const Grid &g, const Bufs &bf, cudaStream_t st) {
+  k_setconj<<<64, 256, 0, st>>>(g, bf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scalar(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  k_scalar<<<g.B, 256, 0, st>>>(g, bf, rk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tables(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  const long n = 3L * g.nkx + (long)g.my * g.nkx;
+  const int T = 128;
+  dim3 grid((unsigned)((n + T - 1) / T), g.B);
+  k_tables<<<grid, T, 0, st>>>(g, bf, rk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finish(const Grid &g, const Bufs &bf, cudaStream_t st) {
+  k_finish<<<(g.B + 127) / 128, 128, 0, st>>>(g, bf);
+  return cudaGetLastError();
+}
+
+}  // namespace sb
