@@ -305,6 +305,43 @@ def run_ours(args):
     barrier(dist)
     e2e_s = allmax(dist, t1 - t0)
     bytes_io = 2 * nf * 16 + 2 * my * 8 + 3 * 8
+    # FP32-mixed precision form: same workload, steps/s, and the field error
+    # against the FP64 path at steps 1, 10, 100, 200 from the same initial field
+    mixed = None
+    if not args.no_mixed:
+        mbox = sb.ShearBox(p, precision=sb.SB_MIXED)
+        mbox.set_state(st0)
+        mbox.step(max(args.warmup, 1))
+        mbox.sync()
+        mstream = torch.cuda.ExternalStream(mbox.stream)
+        m0 = torch.cuda.Event(enable_timing=True)
+        m1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        m0.record(mstream)
+        mbox.step(args.steps)
+        m1.record(mstream)
+        m1.synchronize()
+        mixed_ms = allmax(dist, m0.elapsed_time(m1))
+        errs = {}
+        ref_box = box
+        ref_box.set_state(st0)
+        mbox.set_state(st0)
+        done = 0
+        for mark in (1, 10, 100, 200):
+            ref_box.step(mark - done)
+            mbox.step(mark - done)
+            done = mark
+            a = ref_box.get_state()
+            b = mbox.get_state()
+            errs[str(mark)] = max(float(np.linalg.norm(b[k] - a[k]) / np.linalg.norm(a[k]))
+                                  for k in ("vor", "phi", "u00", "w00"))
+        del mbox
+        mixed = {"value": ws * args.steps / (mixed_ms * 1e-3), "unit": "steps/s",
+                 "ms_per_step": mixed_ms / args.steps,
+                 "speedup_vs_fp64": (ws * args.steps / (mixed_ms * 1e-3)) / steps_per_s,
+                 "rel_l2_err_vs_fp64_at_step": errs,
+                 "precision": "FP32 storage, transforms, nonlinear product and RK3; FP64 "
+                              "compact y-solves, Helmholtz solve, phase factors"}
     if rank != 0:
         return
     cpu = cpu_baseline(args.cpu_steps, os.cpu_count() or 1) if ws == 1 or rank == 0 else None
@@ -333,6 +370,7 @@ def run_ours(args):
             "traffic": traffic,
             "line_kernels_ms": {"k_lineA": line_ms[0], "k_lineB": line_ms[1]},
         },
+        "mixed": mixed,
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "clocks": clk,
     }
@@ -348,6 +386,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--grid", type=int, default=192, choices=sorted(GRIDS),
                     help="profiling only: run a different grid (the benchmark is 192)")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed leg")
     ap.add_argument("--lite", action="store_true",
                     help="profiling only: time the steps, skip e2e / CPU / per-kernel legs")
     args = ap.parse_args()

@@ -58,8 +58,13 @@ typedef struct sb_status {
 
 typedef struct sb_handle sb_handle;
 
-/* precision of sb_create */
+/* precision of sb_create: SB_FP64 computes everything in FP64 (the drop-in);
+ * SB_MIXED stores the state in FP32 and runs the x/z transforms, the nonlinear
+ * product and the RK3 arithmetic in FP32, while the compact y-solves, the
+ * Helmholtz solve for v, the shear phases and the moving_frame remaps stay in
+ * FP64.  The C-ABI takes and returns FP64 arrays in both cases. */
 #define SB_FP64 0
+#define SB_MIXED 1
 
 /* Creates a handle for `batch` boxes: precomputes the compact-scheme
  * coefficients and factorisations (derivadas/prederiv1/prederiv2,

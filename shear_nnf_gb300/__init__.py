@@ -23,6 +23,7 @@ TRACE_FIELDS = (
     "umax3", "xoffb", "xofft", "umax0"] + [f"uner2_{q}" for q in range(1, 5)]
 )
 SB_FP64 = 0
+SB_MIXED = 1
 
 
 class SbParams(ctypes.Structure):

@@ -265,7 +265,8 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   int rc = check_params(p);
   if (rc) return rc;
   if (batch < 1) return fail(1, "batch must be >= 1");
-  if (precision != SB_FP64) return fail(2, "precision %d not available", precision);
+  if (precision != SB_FP64 && precision != SB_MIXED)
+    return fail(2, "precision %d not available (0: FP64, 1: FP32-mixed)", precision);
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1)
     return fail(5, "no CUDA device: the shearbox library has no CPU path");
@@ -275,6 +276,7 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   Grid &g = h->g;
   memset(&g, 0, sizeof(g));
   g.B = batch;
+  g.prec = precision;
   g.mgalx = p->mgalx;
   g.my = p->my;
   g.mgalz = p->mgalz;
@@ -364,7 +366,19 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
       kinv[(size_t)k * g.nkx + i] = (i == 0 && k == 0) ? 0.0 : 1.0 / K;
     }
   }
+  auto upload_f = [&](const float **dst, const std::vector<double> &v) -> int {
+    std::vector<float> f(v.begin(), v.end());
+    double *q;
+    int r = dalloc(h, &q, (f.size() + 1) / 2);
+    if (r) return r;
+    cudaError_t e = cudaMemcpy(q, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(3, "upload: %s", cudaGetErrorString(e));
+    *dst = (const float *)q;
+    return 0;
+  };
   if ((rc = upload(h, &bf.twz, tw(g.mgalz))) || (rc = upload(h, &bf.twx, tw(g.mgalx))) ||
+      (rc = upload_f(&bf.twzf, tw(g.mgalz))) || (rc = upload_f(&bf.twxf, tw(g.mgalx))) ||
+      (rc = upload_f(&bf.kinvf, kinv)) ||
       (rc = upload(h, &bf.kinv, kinv)) || (rc = upload(h, &bf.ginv, ginv)) ||
       (rc = upload_uniform(h, &bf.d1, co.pr1, g.my)) ||
       (rc = upload_uniform(h, &bf.d2, co.pr2, g.my))) {
@@ -461,16 +475,24 @@ int sb_set_state(sb_handle *h, int member, const double *vor, const double *phi,
   const Grid &g = h->g;
   const size_t F = g.field;
   CK(cudaMemcpyAsync(h->d_pen, vor, sizeof(double) * F, cudaMemcpyHostToDevice, h->st));
-  CK(launch_pencil_to_plane(g, h->d_pen, h->bf.vor + member * F, h->st));
+  const size_t Fd = g.prec ? F / 2 : F;  // field size in doubles of the storage type
+  CK(launch_pencil_to_plane(g, h->d_pen, h->bf.vor + member * Fd, h->st));
   CK(cudaMemcpyAsync(h->d_pen, phi, sizeof(double) * F, cudaMemcpyHostToDevice, h->st));
-  CK(launch_pencil_to_plane(g, h->d_pen, h->bf.phi + member * F, h->st));
+  CK(launch_pencil_to_plane(g, h->d_pen, h->bf.phi + member * Fd, h->st));
   std::vector<double> mu(2 * (size_t)g.my);
+  std::vector<float> muf(2 * (size_t)g.my);
   for (int j = 0; j < g.my; j++) {
     mu[2 * j] = u00[j];
     mu[2 * j + 1] = w00[j];
+    muf[2 * j] = (float)u00[j];
+    muf[2 * j + 1] = (float)w00[j];
   }
-  CK(cudaMemcpyAsync(h->bf.mu + (size_t)member * 2 * g.my, mu.data(), sizeof(double) * mu.size(),
-                     cudaMemcpyHostToDevice, h->st));
+  if (g.prec)
+    CK(cudaMemcpyAsync((float *)h->bf.mu + (size_t)member * 2 * g.my, muf.data(),
+                       sizeof(float) * muf.size(), cudaMemcpyHostToDevice, h->st));
+  else
+    CK(cudaMemcpyAsync(h->bf.mu + (size_t)member * 2 * g.my, mu.data(), sizeof(double) * mu.size(),
+                       cudaMemcpyHostToDevice, h->st));
   double sc[3] = {time, xoffb, xofft};
   CK(cudaMemcpyAsync((char *)(h->bf.mem + member) + offsetof(Member, time), sc, sizeof(sc),
                      cudaMemcpyHostToDevice, h->st));
@@ -483,22 +505,30 @@ int sb_get_state(sb_handle *h, int member, double *vor, double *phi, double *u00
   if (!h || member < 0 || member >= h->g.B) return fail(1, "bad handle or member");
   const Grid &g = h->g;
   const size_t F = g.field;
+  const size_t Fd = g.prec ? F / 2 : F;
   if (vor) {
-    CK(launch_plane_to_pencil(g, h->bf.vor + member * F, h->d_pen, h->st));
+    CK(launch_plane_to_pencil(g, h->bf.vor + member * Fd, h->d_pen, h->st));
     CK(cudaMemcpyAsync(vor, h->d_pen, sizeof(double) * F, cudaMemcpyDeviceToHost, h->st));
   }
   if (phi) {
     CK(cudaStreamSynchronize(h->st));
-    CK(launch_plane_to_pencil(g, h->bf.phi + member * F, h->d_pen, h->st));
+    CK(launch_plane_to_pencil(g, h->bf.phi + member * Fd, h->d_pen, h->st));
     CK(cudaMemcpyAsync(phi, h->d_pen, sizeof(double) * F, cudaMemcpyDeviceToHost, h->st));
   }
   std::vector<double> mu(2 * (size_t)g.my);
-  CK(cudaMemcpyAsync(mu.data(), h->bf.mu + (size_t)member * 2 * g.my, sizeof(double) * mu.size(),
-                     cudaMemcpyDeviceToHost, h->st));
+  std::vector<float> muf(2 * (size_t)g.my);
+  if (g.prec)
+    CK(cudaMemcpyAsync(muf.data(), (float *)h->bf.mu + (size_t)member * 2 * g.my,
+                       sizeof(float) * muf.size(), cudaMemcpyDeviceToHost, h->st));
+  else
+    CK(cudaMemcpyAsync(mu.data(), h->bf.mu + (size_t)member * 2 * g.my, sizeof(double) * mu.size(),
+                       cudaMemcpyDeviceToHost, h->st));
   double sc[3];
   CK(cudaMemcpyAsync(sc, (char *)(h->bf.mem + member) + offsetof(Member, time), sizeof(sc),
                      cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
+  if (g.prec)
+    for (size_t q = 0; q < mu.size(); q++) mu[q] = (double)muf[q];
   for (int j = 0; j < g.my; j++) {
     if (u00) u00[j] = mu[2 * j];
     if (w00) w00[j] = mu[2 * j + 1];

@@ -45,6 +45,7 @@ struct Fac {
 // Constant per-handle parameters (passed by value to every kernel)
 struct Grid {
   int B, mgalx, my, mgalz, mx, mz, nkx, nz, mgx;
+  int prec;              // 0: FP64 throughout; 1: FP32-mixed (FP32 storage/transforms)
   int ncb;               // kx column blocks per plane (plane kernels)
   double alp, gam, Ly, s, chi, dx, dy, dz, pi;
   double rh1[7], rh2[7], pr2[7];
@@ -79,7 +80,9 @@ __device__ __constant__ static const double kCa[3] = {8.0 / 15.0, 2.0 / 3.0, 1.0
 
 // Device arrays of one handle
 struct Bufs {
-  double *vor, *phi, *vorwk, *phiwk, *G, *V, *D;  // spectral fields [B][field]
+  // spectral fields [B][field], FP64 or FP32 storage (Grid::prec); the
+  // pointers are typed double for bookkeeping and cast by the kernels
+  double *vor, *phi, *vorwk, *phiwk, *G, *V, *D;
   double *T, *S;                 // d/dy of the NL term and d2(phi)/dy2 between the line kernels
   double *mu, *mwk, *mrf, *mdu;  // mean lines (u00 + i w00) [B][my] complex
   double *zbuf, *xbuf;           // plane-stage intermediates
@@ -90,6 +93,8 @@ struct Bufs {
   double *trace;                 // [B][cap][SB_TRACE_LEN]
   Member *mem;                   // [B]
   const double *twz, *twx;       // FFT twiddles e^{-2 pi i t/N}
+  const float *twzf, *twxf;      // the same, rounded to FP32
+  const float *kinvf;            // kinv rounded to FP32
   const double *ginv;            // 1/g per kz  (g = gam * kz_signed; 0 at k=0)
   const double *kinv;            // 1/(alp2+gam2) per (k,i); 0 at (0,0)
   Fac d1, d2, hz;                // d/dy, d2/dy2, Helmholtz (per line)

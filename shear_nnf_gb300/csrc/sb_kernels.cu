@@ -33,34 +33,58 @@ namespace sb {
 __device__ __forceinline__ cd ldc(const double *p) { return mk(p[0], p[1]); }
 
 // ---------------------------------------------------------------------------
+// storage/arithmetic types: R = double (FP64 path) or float (FP32-mixed path)
+// ---------------------------------------------------------------------------
+template <typename R> struct Vec2;
+template <> struct Vec2<double> { typedef double2 t; };
+template <> struct Vec2<float> { typedef float2 t; };
+template <typename R>
+__device__ __forceinline__ typename Vec2<R>::t mk2(R a, R b) {
+  typename Vec2<R>::t v;
+  v.x = a;
+  v.y = b;
+  return v;
+}
+template <typename R> __device__ __forceinline__ const R *tw_of(const Bufs &bf, bool z);
+template <> __device__ __forceinline__ const double *tw_of<double>(const Bufs &bf, bool z) {
+  return z ? bf.twz : bf.twx;
+}
+template <> __device__ __forceinline__ const float *tw_of<float>(const Bufs &bf, bool z) {
+  return z ? bf.twzf : bf.twxf;
+}
+template <typename R> __device__ __forceinline__ R kinv_of(const Bufs &bf, long q);
+template <> __device__ __forceinline__ double kinv_of<double>(const Bufs &bf, long q) { return bf.kinv[q]; }
+template <> __device__ __forceinline__ float kinv_of<float>(const Bufs &bf, long q) { return bf.kinvf[q]; }
+
+// ---------------------------------------------------------------------------
 // plane stage 1: reconstruction + backward z-transforms
 // ---------------------------------------------------------------------------
 // k index -> position on the padded z grid (fill00)
 __device__ __forceinline__ int kgrid(int k, int nz, int NZ, int mz) { return k <= nz ? k : k + (NZ - mz); }
 
-template <int NZ, int CB, int T>
+template <typename R, int NZ, int CB, int T>
 __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
+  typedef typename Vec2<R>::t V;
   const int cb = blockIdx.x, j = blockIdx.y, b = blockIdx.z;
   Member &M = bf.mem[b];
   if (M.halted) return;
-  extern __shared__ double2 smem[];
-  double2 *A = smem, *Bs = smem + 2 * CB * NZ;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *A = (V *)smem_raw, *Bs = A + 2 * CB * NZ;
   const int nkx = g.nkx, mz = g.mz, nz = g.nz;
   const int i0 = cb * CB;
   const long pbase = (long)b * g.field + (long)j * g.plane;
-  const double2 *vor = (const double2 *)(bf.vor + pbase);
-  const double2 *phi = (const double2 *)(bf.phi + pbase);
-  const double2 *Dv = (const double2 *)(bf.D + pbase);
-  const double2 *Vv = (const double2 *)(bf.V + pbase);
-  const double2 *Gv = (const double2 *)(bf.G + pbase);
-  const double2 mu = ((const double2 *)bf.mu)[(long)b * g.my + j];
-  const double2 mdu = ((const double2 *)bf.mdu)[(long)b * g.my + j];
-  const double s = g.s;
+  const V *vor = (const V *)((const R *)bf.vor + pbase);
+  const V *phi = (const V *)((const R *)bf.phi + pbase);
+  const V *Dv = (const V *)((const R *)bf.D + pbase);
+  const V *Vv = (const V *)((const R *)bf.V + pbase);
+  const V *Gv = (const V *)((const R *)bf.G + pbase);
+  const V mu = ((const V *)bf.mu)[(long)b * g.my + j];
+  const V mdu = ((const V *)bf.mdu)[(long)b * g.my + j];
   // omega_y and phi with the kx=0 conjugate symmetry imposed (set_conj on the
   // copies buff1/buff2, cross.f90:493-502)
-  auto ld_sym = [&](const double2 *p, int i, int k) -> double2 {
+  auto ld_sym = [&](const V *p, int i, int k) -> V {
     if (i == 0 && k > nz) {
-      double2 v = p[(mz - k) * nkx];
+      V v = p[(mz - k) * nkx];
       v.y = -v.y;
       return v;
     }
@@ -68,6 +92,8 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
   };
   const bool do_hist = (rk == 1) && M.ihist;
   if (do_hist) {
+    // statistics in FP64 whatever the storage precision
+    const double s = g.s;
     double acc[SB_NHIST_Q];
 #pragma unroll
     for (int q = 0; q < SB_NHIST_Q; q++) acc[q] = 0.0;
@@ -79,13 +105,15 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
       const double gz = g.gam * kzs;
       const double Kk = a * a + gz * gz;
       const double iK = bf.kinv[k * nkx + i];
-      const double2 ph = ld_sym(phi, i, k), vr = ld_sym(vor, i, k);
-      const double2 w1 = Dv[k * nkx + i], dv = Vv[k * nkx + i];
+      const V phr = ld_sym(phi, i, k), vrr = ld_sym(vor, i, k);
+      const V w1r = Dv[k * nkx + i], dvr = Vv[k * nkx + i];
+      const double2 ph = make_double2(phr.x, phr.y), vr = make_double2(vrr.x, vrr.y);
+      const double2 w1 = make_double2(w1r.x, w1r.y), dv = make_double2(dvr.x, dvr.y);
       double2 u1, u2, u3, o1, o3;
       if (i == 0 && k == 0) {
         u1 = make_double2(mu.x, 0.0);
         u3 = make_double2(mu.y, 0.0);
-        o3 = make_double2(-mdu.x, 0.0);
+        o3 = make_double2(-(double)mdu.x, 0.0);
         o1 = make_double2(mdu.y, 0.0);
         u2 = make_double2(M.vbulk, 0.0);
       } else {
@@ -98,7 +126,8 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
         u3 = make_double2(-ty * iK, tx * iK);
         tx = a * dv.x - gz * vr.x; ty = a * dv.y - gz * vr.y;
         u1 = make_double2(-ty * iK, tx * iK);
-        u2 = Gv[k * nkx + i];
+        const V gv = Gv[k * nkx + i];
+        u2 = make_double2(gv.x, gv.y);
       }
       const double2 o2 = vr;
       const double w = (i == 0) ? 1.0 : 2.0;
@@ -137,51 +166,52 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
       bf.hpart[(((long)b * g.my + j) * g.ncb + cb) * SB_NHIST_Q + threadIdx.x] = v;
     }
   }
-  double2 *zb = (double2 *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * 6 * nkx;
+  V *zb = (V *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * 6 * nkx;
+  const V zero = mk2<R>((R)0, (R)0);
   for (int round = 0; round < 3; round++) {
     // fill two fields (zero the 2/3-rule gap) on the padded z grid
-    for (int idx = threadIdx.x; idx < 2 * CB * NZ; idx += T) A[idx] = make_double2(0.0, 0.0);
+    for (int idx = threadIdx.x; idx < 2 * CB * NZ; idx += T) A[idx] = zero;
     __syncthreads();
     for (int idx = threadIdx.x; idx < CB * mz; idx += T) {
       const int ci = idx % CB, k = idx / CB, i = i0 + ci;
       if (i >= nkx) continue;
       const int kg = kgrid(k, nz, NZ, mz);
-      const double a = g.alp * i;
+      const R a = (R)(g.alp * i);
       const int kzs = (k <= nz) ? k : k - mz;
-      const double gz = g.gam * kzs;
-      const double iK = bf.kinv[k * nkx + i];
-      double2 fa, fb;
+      const R gz = (R)(g.gam * kzs);
+      const R iK = kinv_of<R>(bf, (long)k * nkx + i);
+      V fa, fb;
       const bool z00 = (i == 0 && k == 0);
       if (round == 0) {  // u (f=0) and w (f=1) from dv/dy and omega_y
         if (z00) {
-          fa = make_double2(mu.x, 0.0);
-          fb = make_double2(mu.y, 0.0);
+          fa = mk2<R>(mu.x, (R)0);
+          fb = mk2<R>(mu.y, (R)0);
         } else {
-          const double2 dv = Vv[k * nkx + i], vr = ld_sym(vor, i, k);
-          double tx = a * dv.x - gz * vr.x, ty = a * dv.y - gz * vr.y;
-          fa = make_double2(-ty * iK, tx * iK);
+          const V dv = Vv[k * nkx + i], vr = ld_sym(vor, i, k);
+          R tx = a * dv.x - gz * vr.x, ty = a * dv.y - gz * vr.y;
+          fa = mk2<R>(-ty * iK, tx * iK);
           tx = gz * dv.x + a * vr.x; ty = gz * dv.y + a * vr.y;
-          fb = make_double2(-ty * iK, tx * iK);
+          fb = mk2<R>(-ty * iK, tx * iK);
         }
       } else if (round == 1) {  // omega_x (f=2) and omega_z (f=3) from d(omega_y)/dy and phi
         if (z00) {
-          fa = make_double2(mdu.y, 0.0);
-          fb = make_double2(-mdu.x, 0.0);
+          fa = mk2<R>(mdu.y, (R)0);
+          fb = mk2<R>(-mdu.x, (R)0);
         } else {
-          const double2 w1 = Dv[k * nkx + i], ph = ld_sym(phi, i, k);
-          double tx = a * w1.x + gz * ph.x, ty = a * w1.y + gz * ph.y;
-          fa = make_double2(-ty * iK, tx * iK);
+          const V w1 = Dv[k * nkx + i], ph = ld_sym(phi, i, k);
+          R tx = a * w1.x + gz * ph.x, ty = a * w1.y + gz * ph.y;
+          fa = mk2<R>(-ty * iK, tx * iK);
           tx = gz * w1.x - a * ph.x; ty = gz * w1.y - a * ph.y;
-          fb = make_double2(-ty * iK, tx * iK);
+          fb = mk2<R>(-ty * iK, tx * iK);
         }
       } else {  // v (f=4) and omega_y (f=5)
-        fa = z00 ? make_double2(M.vbulk, 0.0) : Gv[k * nkx + i];
+        fa = z00 ? mk2<R>((R)M.vbulk, (R)0) : Gv[k * nkx + i];
         fb = ld_sym(vor, i, k);
       }
       A[ci * NZ + kg] = fa;
       A[(CB + ci) * NZ + kg] = fb;
     }
-    double2 *res = fft_batch<NZ, +1, 2 * CB, T>(A, Bs, (const double2 *)bf.twz);
+    V *res = fft_batch<NZ, +1, 2 * CB, T>(A, Bs, (const V *)tw_of<R>(bf, true));
     // store Zbuf[z][f][i]
     for (int idx = threadIdx.x; idx < 2 * CB * NZ; idx += T) {
       const int ci = idx % CB, rem = idx / CB;
@@ -200,47 +230,49 @@ __device__ __forceinline__ unsigned long long dbits(double v) {
   return (unsigned long long)__double_as_longlong(fabs(v));
 }
 
-template <int NX, int T>
+template <typename R, int NX, int T>
 __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
+  typedef typename Vec2<R>::t V;
   const int zp = blockIdx.x, j = blockIdx.y, b = blockIdx.z;
   Member &M = bf.mem[b];
   if (M.halted) return;
-  extern __shared__ double2 smem[];
-  double2 *A = smem, *Bs = smem + 6 * NX;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *A = (V *)smem_raw, *Bs = A + 6 * NX;
   const int nkx = g.nkx, NZ = g.mgalz;
   const int z = 2 * zp;
-  const double2 *zb = (const double2 *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * 6 * nkx;
+  const V *zb = (const V *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * 6 * nkx;
   // Hermitian extension of two rows into one complex sequence (c2r of both rows
   // at once); FFTW's c2r ignores the imaginary part of the kx = 0 entry
-  for (int idx = threadIdx.x; idx < 6 * NX; idx += T) A[idx] = make_double2(0.0, 0.0);
+  const V zero = mk2<R>((R)0, (R)0);
+  for (int idx = threadIdx.x; idx < 6 * NX; idx += T) A[idx] = zero;
   __syncthreads();
   for (int idx = threadIdx.x; idx < 6 * nkx; idx += T) {
     const int f = idx / nkx, i = idx - f * nkx;
-    double2 X1 = zb[((long)z * 6 + f) * nkx + i];
-    double2 X2 = zb[((long)(z + 1) * 6 + f) * nkx + i];
+    V X1 = zb[((long)z * 6 + f) * nkx + i];
+    V X2 = zb[((long)(z + 1) * 6 + f) * nkx + i];
     if (i == 0) {
-      X1.y = 0.0;
-      X2.y = 0.0;
+      X1.y = (R)0;
+      X2.y = (R)0;
     }
-    A[f * NX + i] = make_double2(X1.x - X2.y, X1.y + X2.x);
-    if (i > 0) A[f * NX + NX - i] = make_double2(X1.x + X2.y, -X1.y + X2.x);
+    A[f * NX + i] = mk2<R>(X1.x - X2.y, X1.y + X2.x);
+    if (i > 0) A[f * NX + NX - i] = mk2<R>(X1.x + X2.y, -X1.y + X2.x);
   }
-  double2 *P = fft_batch<NX, +1, 6, T>(A, Bs, (const double2 *)bf.twx);
-  double2 *Q = (P == A) ? Bs : A;
+  V *P = fft_batch<NX, +1, 6, T>(A, Bs, (const V *)tw_of<R>(bf, false));
+  V *Q = (P == A) ? Bs : A;
   // fields: 0 u, 1 w, 2 omega_x, 3 omega_z, 4 v, 5 omega_y
-  const double chi2 = 2.0 * g.chi;
-  const double sy = g.s * ((double)j * g.dy - 0.5 * g.Ly);
-  unsigned long long m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+  const R chi2 = (R)(2.0 * g.chi);
+  const R sy = (R)(g.s * ((double)j * g.dy - 0.5 * g.Ly));
+  R m0 = 0, m1 = 0, m2 = 0, m3 = 0;
   for (int x = threadIdx.x; x < NX; x += T) {
-    const double2 u1 = P[0 * NX + x], u3 = P[1 * NX + x], o1 = P[2 * NX + x], o3 = P[3 * NX + x],
-                  u2 = P[4 * NX + x], o2 = P[5 * NX + x];
+    const V u1 = P[0 * NX + x], u3 = P[1 * NX + x], o1 = P[2 * NX + x], o3 = P[3 * NX + x],
+            u2 = P[4 * NX + x], o2 = P[5 * NX + x];
     if (rk == 1) {
-      m0 = max(m0, max(dbits(u1.x), dbits(u1.y)));
-      m1 = max(m1, max(dbits(u1.x + sy), dbits(u1.y + sy)));
-      m2 = max(m2, max(dbits(u2.x), dbits(u2.y)));
-      m3 = max(m3, max(dbits(u3.x), dbits(u3.y)));
+      m0 = fmax(m0, fmax(fabs(u1.x), fabs(u1.y)));
+      m1 = fmax(m1, fmax(fabs(u1.x + sy), fabs(u1.y + sy)));
+      m2 = fmax(m2, fmax(fabs(u2.x), fabs(u2.y)));
+      m3 = fmax(m3, fmax(fabs(u3.x), fabs(u3.y)));
     }
-    double2 h1, h2, h3;
+    V h1, h2, h3;
     h1.x = u2.x * (o3.x + chi2) - u3.x * o2.x;
     h1.y = u2.y * (o3.y + chi2) - u3.y * o2.y;
     h2.x = u3.x * o1.x - u1.x * (o3.x + chi2);
@@ -252,180 +284,198 @@ __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
     Q[2 * NX + x] = h3;
   }
   if (rk == 1) {
+    unsigned long long b0 = dbits(m0), b1 = dbits(m1), b2 = dbits(m2), b3 = dbits(m3);
     for (int o = 16; o > 0; o >>= 1) {
-      m0 = max(m0, __shfl_xor_sync(0xffffffffu, m0, o));
-      m1 = max(m1, __shfl_xor_sync(0xffffffffu, m1, o));
-      m2 = max(m2, __shfl_xor_sync(0xffffffffu, m2, o));
-      m3 = max(m3, __shfl_xor_sync(0xffffffffu, m3, o));
+      b0 = max(b0, __shfl_xor_sync(0xffffffffu, b0, o));
+      b1 = max(b1, __shfl_xor_sync(0xffffffffu, b1, o));
+      b2 = max(b2, __shfl_xor_sync(0xffffffffu, b2, o));
+      b3 = max(b3, __shfl_xor_sync(0xffffffffu, b3, o));
     }
     if ((threadIdx.x & 31) == 0) {
-      atomicMax(&M.umax_bits[0], m0);
-      atomicMax(&M.umax_bits[1], m1);
-      atomicMax(&M.umax_bits[2], m2);
-      atomicMax(&M.umax_bits[3], m3);
+      atomicMax(&M.umax_bits[0], b0);
+      atomicMax(&M.umax_bits[1], b1);
+      atomicMax(&M.umax_bits[2], b2);
+      atomicMax(&M.umax_bits[3], b3);
     }
   }
-  double2 *R = fft_batch<NX, -1, 3, T>(Q, P, (const double2 *)bf.twx);
-  double2 *xb = (double2 *)bf.xbuf + ((long)b * g.my + j) * (long)NZ * 3 * nkx;
+  V *Rr = fft_batch<NX, -1, 3, T>(Q, P, (const V *)tw_of<R>(bf, false));
+  V *xb = (V *)bf.xbuf + ((long)b * g.my + j) * (long)NZ * 3 * nkx;
+  const R half = (R)0.5;
   for (int idx = threadIdx.x; idx < 3 * nkx; idx += T) {
     const int f = idx / nkx, i = idx - f * nkx;
-    const double2 zk = R[f * NX + i];
-    double2 zm = R[f * NX + ((NX - i) % NX)];
+    const V zk = Rr[f * NX + i];
+    V zm = Rr[f * NX + ((NX - i) % NX)];
     zm.y = -zm.y;
-    const double sx = zk.x + zm.x, syy = zk.y + zm.y, dx = zk.x - zm.x, dy = zk.y - zm.y;
-    xb[((long)z * 3 + f) * nkx + i] = make_double2(0.5 * sx, 0.5 * syy);
-    xb[((long)(z + 1) * 3 + f) * nkx + i] = make_double2(0.5 * dy, -0.5 * dx);
+    const R sx = zk.x + zm.x, syy = zk.y + zm.y, dx = zk.x - zm.x, dy = zk.y - zm.y;
+    xb[((long)z * 3 + f) * nkx + i] = mk2<R>(half * sx, half * syy);
+    xb[((long)(z + 1) * 3 + f) * nkx + i] = mk2<R>(half * dy, -half * dx);
   }
 }
 
 // ---------------------------------------------------------------------------
 // plane stage 3: forward z-transforms, truncation and right-hand sides
 // ---------------------------------------------------------------------------
-template <int NZ, int CB, int T>
+template <typename R, int NZ, int CB, int T>
 __global__ void __launch_bounds__(T) k_p3(Grid g, Bufs bf) {
+  typedef typename Vec2<R>::t V;
   const int cb = blockIdx.x, j = blockIdx.y, b = blockIdx.z;
   Member &M = bf.mem[b];
   if (M.halted) return;
-  extern __shared__ double2 smem[];
-  double2 *A = smem, *Bs = smem + 3 * CB * NZ;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *A = (V *)smem_raw, *Bs = A + 3 * CB * NZ;
   const int nkx = g.nkx, mz = g.mz, nz = g.nz;
   const int i0 = cb * CB;
-  const double2 *xb = (const double2 *)bf.xbuf + ((long)b * g.my + j) * (long)NZ * 3 * nkx;
+  const V *xb = (const V *)bf.xbuf + ((long)b * g.my + j) * (long)NZ * 3 * nkx;
+  const V zero = mk2<R>((R)0, (R)0);
   for (int idx = threadIdx.x; idx < 3 * CB * NZ; idx += T) {
     const int ci = idx % CB, rem = idx / CB;
     const int f = rem % 3, z = rem / 3;
     const int i = i0 + ci;
-    A[(f * CB + ci) * NZ + z] = (i < nkx) ? xb[((long)z * 3 + f) * nkx + i] : make_double2(0.0, 0.0);
+    A[(f * CB + ci) * NZ + z] = (i < nkx) ? xb[((long)z * 3 + f) * nkx + i] : zero;
   }
-  double2 *P = fft_batch<NZ, -1, 3 * CB, T>(A, Bs, (const double2 *)bf.twz);
+  V *P = fft_batch<NZ, -1, 3 * CB, T>(A, Bs, (const V *)tw_of<R>(bf, true));
   const long pbase = (long)b * g.field + (long)j * g.plane;
-  double2 *Dv = (double2 *)(bf.D + pbase);
-  double2 *Gv = (double2 *)(bf.G + pbase);
-  double2 *Vv = (double2 *)(bf.V + pbase);
-  const double norm = 1.0 / (double)(g.mgalx * g.mgalz);
-  const double s = g.s;
+  V *Dv = (V *)((R *)bf.D + pbase);
+  V *Gv = (V *)((R *)bf.G + pbase);
+  V *Vv = (V *)((R *)bf.V + pbase);
+  const R norm = (R)(1.0 / (double)(g.mgalx * g.mgalz));
+  const R s = (R)g.s;
   for (int idx = threadIdx.x; idx < CB * mz; idx += T) {
     const int ci = idx % CB, k = idx / CB, i = i0 + ci;
     if (i >= nkx) continue;
     const int kg = kgrid(k, nz, NZ, mz);
-    double2 H1 = P[(0 * CB + ci) * NZ + kg], H2 = P[(1 * CB + ci) * NZ + kg],
-            H3 = P[(2 * CB + ci) * NZ + kg];
+    V H1 = P[(0 * CB + ci) * NZ + kg], H2 = P[(1 * CB + ci) * NZ + kg],
+      H3 = P[(2 * CB + ci) * NZ + kg];
     H1.x *= norm; H1.y *= norm;
     H2.x *= norm; H2.y *= norm;
     H3.x *= norm; H3.y *= norm;
-    const double a = g.alp * i;
+    const R a = (R)(g.alp * i);
     const int kzs = (k <= nz) ? k : k - mz;
-    const double gz = g.gam * kzs;
-    const double Kk = a * a + gz * gz;
+    const R gz = (R)(g.gam * kzs);
+    const R Kk = a * a + gz * gz;
     const long q = (long)k * nkx + i;
-    const double2 v = Gv[q];
+    const V v = Gv[q];
     // dvordy = i a H1 + i gz H3
-    double tx = a * H1.x + gz * H3.x, ty = a * H1.y + gz * H3.y;
-    Dv[q] = make_double2(-ty, tx);
+    R tx = a * H1.x + gz * H3.x, ty = a * H1.y + gz * H3.y;
+    Dv[q] = mk2<R>(-ty, tx);
     // hg = -i a H3 + i gz (H1 - s v)
     tx = gz * (H1.x - s * v.x) - a * H3.x;
     ty = gz * (H1.y - s * v.y) - a * H3.y;
-    Gv[q] = make_double2(-ty, tx);
+    Gv[q] = mk2<R>(-ty, tx);
     // hv = -(kx^2 + kz^2) H2
-    Vv[q] = make_double2(-(Kk * H2.x), -(Kk * H2.y));
-    if (i == 0 && k == 0) ((double2 *)bf.mrf)[(long)b * g.my + j] = make_double2(H1.x, H3.x);
+    Vv[q] = mk2<R>(-(Kk * H2.x), -(Kk * H2.y));
+    if (i == 0 && k == 0) ((V *)bf.mrf)[(long)b * g.my + j] = mk2<R>(H1.x, H3.x);
   }
 }
 
-// pencil (j fastest, then kx, then kz) <-> plane-major layout, one box
-__global__ void k_pencil_to_plane(Grid g, const double *__restrict__ pen, double *__restrict__ dst) {
+// pencil (j fastest, then kx, then kz, FP64 host layout) <-> plane-major
+// device layout of storage type R, one box
+template <typename R>
+__global__ void k_pencil_to_plane(Grid g, const double *__restrict__ pen, R *__restrict__ dst) {
   const long n = (long)g.my * g.nkx * g.mz;
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
     const int i = (int)(t % g.nkx);
     const int k = (int)((t / g.nkx) % g.mz);
     const int j = (int)(t / ((long)g.nkx * g.mz));
     const long src = 2 * (((long)k * g.nkx + i) * g.my + j);
-    dst[2 * t] = pen[src];
-    dst[2 * t + 1] = pen[src + 1];
+    dst[2 * t] = (R)pen[src];
+    dst[2 * t + 1] = (R)pen[src + 1];
   }
 }
-__global__ void k_plane_to_pencil(Grid g, const double *__restrict__ src, double *__restrict__ pen) {
+template <typename R>
+__global__ void k_plane_to_pencil(Grid g, const R *__restrict__ src, double *__restrict__ pen) {
   const long n = (long)g.my * g.nkx * g.mz;
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
     const int j = (int)(t % g.my);
     const int i = (int)((t / g.my) % g.nkx);
     const int k = (int)(t / ((long)g.my * g.nkx));
     const long s = 2 * (((long)j * g.mz + k) * g.nkx + i);
-    pen[2 * t] = src[s];
-    pen[2 * t + 1] = src[s + 1];
+    pen[2 * t] = (double)src[s];
+    pen[2 * t + 1] = (double)src[s + 1];
   }
 }
 
 // ---------------------------------------------------------------------------
 // launch helpers
 // ---------------------------------------------------------------------------
-template <int NZ, int CB, int T, int T3>
+template <typename R, int NZ, int CB, int T, int T3>
 static cudaError_t launch_p13(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, int which,
                               bool prep) {
+  typedef typename Vec2<R>::t V;
   dim3 grid(g.ncb, g.my, g.B);
-  const size_t sm1 = sizeof(double2) * 2 * (2 * CB * NZ);
-  const size_t sm3 = sizeof(double2) * 2 * (3 * CB * NZ);
+  const size_t sm1 = sizeof(V) * 2 * (2 * CB * NZ);
+  const size_t sm3 = sizeof(V) * 2 * (3 * CB * NZ);
   if (prep) {
-    cudaFuncSetAttribute(k_p1<NZ, CB, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
-    cudaFuncSetAttribute(k_p3<NZ, CB, T3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+    cudaFuncSetAttribute(k_p1<R, NZ, CB, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+    cudaFuncSetAttribute(k_p3<R, NZ, CB, T3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
     return cudaGetLastError();
   }
   if (which == 1)
-    k_p1<NZ, CB, T><<<grid, T, sm1, st>>>(g, bf, rk);
+    k_p1<R, NZ, CB, T><<<grid, T, sm1, st>>>(g, bf, rk);
   else
-    k_p3<NZ, CB, T3><<<grid, T3, sm3, st>>>(g, bf);
+    k_p3<R, NZ, CB, T3><<<grid, T3, sm3, st>>>(g, bf);
   return cudaGetLastError();
 }
 
-template <int NX, int T>
+template <typename R, int NX, int T>
 static cudaError_t launch_p2(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, bool prep) {
+  typedef typename Vec2<R>::t V;
   dim3 grid(g.mgalz / 2, g.my, g.B);
-  const size_t sm = sizeof(double2) * 2 * (6 * NX);
+  const size_t sm = sizeof(V) * 2 * (6 * NX);
   if (prep) {
-    cudaFuncSetAttribute(k_p2<NX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaFuncSetAttribute(k_p2<R, NX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     return cudaGetLastError();
   }
-  k_p2<NX, T><<<grid, T, sm, st>>>(g, bf, rk);
+  k_p2<R, NX, T><<<grid, T, sm, st>>>(g, bf, rk);
   return cudaGetLastError();
 }
 
 int plane_cb(int) { return 8; }
 
-// stage 1..3: launch; stage 0: set the kernels' shared-memory limits (once)
-cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
+template <typename R>
+static cudaError_t launch_plane_t(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
   const bool prep = (stage == 0);
   if (stage == 2 || prep) {
     cudaError_t e;
     switch (g.mgalx) {
-      case 32: e = launch_p2<32, 64>(g, bf, rk, st, prep); break;
-      case 48: e = launch_p2<48, 64>(g, bf, rk, st, prep); break;
-      case 64: e = launch_p2<64, 96>(g, bf, rk, st, prep); break;
-      case 96: e = launch_p2<96, 96>(g, bf, rk, st, prep); break;
-      case 192: e = launch_p2<192, 128>(g, bf, rk, st, prep); break;
-      case 384: e = launch_p2<384, 256>(g, bf, rk, st, prep); break;
+      case 32: e = launch_p2<R, 32, 64>(g, bf, rk, st, prep); break;
+      case 48: e = launch_p2<R, 48, 64>(g, bf, rk, st, prep); break;
+      case 64: e = launch_p2<R, 64, 96>(g, bf, rk, st, prep); break;
+      case 96: e = launch_p2<R, 96, 96>(g, bf, rk, st, prep); break;
+      case 192: e = launch_p2<R, 192, 128>(g, bf, rk, st, prep); break;
+      case 384: e = launch_p2<R, 384, 256>(g, bf, rk, st, prep); break;
       default: return cudaErrorInvalidValue;
     }
     if (!prep || e != cudaSuccess) return e;
   }
   switch (g.mgalz) {
-    case 32: return launch_p13<32, 8, 128, 96>(g, bf, rk, st, stage, prep);
-    case 48: return launch_p13<48, 8, 128, 96>(g, bf, rk, st, stage, prep);
-    case 64: return launch_p13<64, 8, 128, 96>(g, bf, rk, st, stage, prep);
-    case 96: return launch_p13<96, 8, 128, 96>(g, bf, rk, st, stage, prep);
-    case 192: return launch_p13<192, 8, 128, 96>(g, bf, rk, st, stage, prep);
+    case 32: return launch_p13<R, 32, 8, 128, 96>(g, bf, rk, st, stage, prep);
+    case 48: return launch_p13<R, 48, 8, 128, 96>(g, bf, rk, st, stage, prep);
+    case 64: return launch_p13<R, 64, 8, 128, 96>(g, bf, rk, st, stage, prep);
+    case 96: return launch_p13<R, 96, 8, 128, 96>(g, bf, rk, st, stage, prep);
+    case 192: return launch_p13<R, 192, 8, 128, 96>(g, bf, rk, st, stage, prep);
     default: return cudaErrorInvalidValue;
   }
 }
 
-
-
+// stage 1..3: launch; stage 0: set the kernels' shared-memory limits (once)
+cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
+  return g.prec ? launch_plane_t<float>(g, bf, stage, rk, st)
+                : launch_plane_t<double>(g, bf, stage, rk, st);
+}
 
 cudaError_t launch_pencil_to_plane(const Grid &g, const double *pen, double *dst, cudaStream_t st) {
-  k_pencil_to_plane<<<256, 256, 0, st>>>(g, pen, dst);
+  if (g.prec)
+    k_pencil_to_plane<float><<<256, 256, 0, st>>>(g, pen, (float *)dst);
+  else
+    k_pencil_to_plane<double><<<256, 256, 0, st>>>(g, pen, dst);
   return cudaGetLastError();
 }
 cudaError_t launch_plane_to_pencil(const Grid &g, const double *src, double *pen, cudaStream_t st) {
-  k_plane_to_pencil<<<256, 256, 0, st>>>(g, src, pen);
+  if (g.prec)
+    k_plane_to_pencil<float><<<256, 256, 0, st>>>(g, (const float *)src, pen);
+  else
+    k_plane_to_pencil<double><<<256, 256, 0, st>>>(g, src, pen);
   return cudaGetLastError();
 }
 

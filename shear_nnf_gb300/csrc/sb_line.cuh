@@ -119,14 +119,15 @@ __device__ __forceinline__ double cmul_c(double own, double oth, cd s, int c) {
 // factorised heptadiagonal.  u is read with stride ps; y (the forward
 // substitution) is kept in ybuf (stride ys).  epi(j, x_j) receives the
 // solution in descending j.  All 32 lanes of the warp must call this together.
-template <class EPI>
-__device__ __forceinline__ void solve_line(const double *u, long ps, double *ybuf, long ys, int N,
+template <typename TU, class EPI>
+__device__ __forceinline__ void solve_line(const TU *u, long ps, double *ybuf, long ys, int N,
                                            const FacView &V, const Tail &T, cd shp, cd shm, int c,
                                            double r0, double r1, double r2, double r3, bool anti,
                                            EPI epi) {
   // wrapped values u(-3..-1) = u(N-3..N-1)*shm and u(N..N+2) = u(0..2)*shp
-  double uN3 = u[(long)(N - 3) * ps], uN2 = u[(long)(N - 2) * ps], uN1 = u[(long)(N - 1) * ps];
-  double u0 = u[0], u1 = u[ps], u2 = u[2 * ps];
+  double uN3 = (double)u[(long)(N - 3) * ps], uN2 = (double)u[(long)(N - 2) * ps],
+         uN1 = (double)u[(long)(N - 1) * ps];
+  double u0 = (double)u[0], u1 = (double)u[ps], u2 = (double)u[2 * ps];
   double pN3 = __shfl_xor_sync(0xffffffffu, uN3, 1), pN2 = __shfl_xor_sync(0xffffffffu, uN2, 1),
          pN1 = __shfl_xor_sync(0xffffffffu, uN1, 1);
   double p0 = __shfl_xor_sync(0xffffffffu, u0, 1), p1 = __shfl_xor_sync(0xffffffffu, u1, 1),
@@ -135,7 +136,7 @@ __device__ __forceinline__ void solve_line(const double *u, long ps, double *ybu
                lo1 = cmul_c(uN1, pN1, shm, c);
   const double hi0 = cmul_c(u0, p0, shp, c), hi1 = cmul_c(u1, p1, shp, c),
                hi2 = cmul_c(u2, p2, shp, c);
-  double w0 = lo3, w1 = lo2, w2 = lo1, w3 = u0, w4 = u1, w5 = u2, w6 = u[3 * ps];
+  double w0 = lo3, w1 = lo2, w2 = lo1, w3 = u0, w4 = u1, w5 = u2, w6 = (double)u[3 * ps];
   double y1 = 0.0, y2 = 0.0, y3 = 0.0;
   double Se = 0.0, Sf = 0.0, Sg = 0.0;
   double bN2 = 0.0, bN1 = 0.0, bN0 = 0.0;
@@ -165,7 +166,7 @@ __device__ __forceinline__ void solve_line(const double *u, long ps, double *ybu
     }
     w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = w5; w5 = w6;
     const int jn = j + 4;
-    w6 = (jn < N) ? u[(long)jn * ps] : (jn == N ? hi0 : (jn == N + 1 ? hi1 : hi2));
+    w6 = (jn < N) ? (double)u[(long)jn * ps] : (jn == N ? hi0 : (jn == N + 1 ? hi1 : hi2));
   }
   // bordered rows N-2..N and the first rows of the back substitution (complex)
   const cd Y3 = pair_full(y1, c), Y4 = pair_full(y2, c), Y5 = pair_full(y3, c);

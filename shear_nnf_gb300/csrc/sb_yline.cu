@@ -67,49 +67,53 @@ __device__ __forceinline__ double *ycol() {
 }
 
 // copy a solution kept in shared memory to a field line
-__device__ __forceinline__ void store_col(const double *ys, int ystr, double *__restrict__ dst, long ps,
+template <typename R>
+__device__ __forceinline__ void store_col(const double *ys, int ystr, R *__restrict__ dst, long ps,
                                           int N, bool active) {
   if (!active) return;
 #pragma unroll 4
-  for (int j = 0; j < N; j++) dst[(long)j * ps] = ys[j * ystr];
+  for (int j = 0; j < N; j++) dst[(long)j * ps] = (R)ys[j * ystr];
 }
 
 // RK3 accumulate/update of one field line with the zeta store and both
 // moving_frame remaps (cross.f90:694-781), fused per point.  x = d2f/dy2 in
-// the shared buffer; rhs = the nonlinear right-hand side (minus `sub` if
-// given); f, fwk the field and its RK work array.
-__device__ __forceinline__ void rk_update(const double *ys, int ystr, const double *__restrict__ rhs,
-                                          const double *__restrict__ sub, double *__restrict__ f,
-                                          double *__restrict__ fwk, long ps, int N, int rk,
-                                          double nuv, double k2, double Dt,
-                                          const double *__restrict__ mf1,
+// the shared buffer (FP64); rhs = the nonlinear right-hand side (minus `sub`
+// if given); f, fwk the field and its RK work array.  The RK arithmetic runs in
+// the storage precision R; the viscous term and the remaps (phase factors) in
+// FP64.
+template <typename R>
+__device__ __forceinline__ void rk_update(const double *ys, int ystr, const R *__restrict__ rhs,
+                                          const R *__restrict__ sub, R *__restrict__ f,
+                                          R *__restrict__ fwk, long ps, int N, int rk, double nuv,
+                                          double k2, double Dt, const double *__restrict__ mf1,
                                           const double *__restrict__ mf2, long mfs, int c,
                                           bool active) {
-  const double gk = kGama[rk], zk = kZeta[rk];
+  const R gk = (R)kGama[rk], zk = (R)kZeta[rk], dtr = (R)Dt;
 #pragma unroll 2
   for (int j = 0; j < N; j++) {
     const long q = (long)j * ps;
     const double x = ys[j * ystr];
-    const double fo = f[q];
-    double h = rhs[q];
+    const R fo = f[q];
+    R h = rhs[q];
     if (sub) h = h - sub[q];
-    h = h + nuv * (-(k2 * fo) + x);
-    double wk = (rk == 0) ? gk * h : fwk[q] + gk * h;
-    const double fn = fo + Dt * wk;
+    h = h + (R)(nuv * (-(k2 * (double)fo) + x));
+    R wk = (rk == 0) ? gk * h : fwk[q] + gk * h;
+    const double fn = (double)(fo + dtr * wk);
     const cd m2 = ldc2(mf2 + (long)j * mfs);
     const double fnm = cmul_c(fn, __shfl_xor_sync(0xffffffffu, fn, 1), m2, c);
     if (rk < 2) {
       const cd m1 = ldc2(mf1 + (long)j * mfs);
-      const double wz = h * zk;
-      wk = cmul_c(wz, __shfl_xor_sync(0xffffffffu, wz, 1), m1, c);
+      const double wz = (double)(h * zk);
+      wk = (R)cmul_c(wz, __shfl_xor_sync(0xffffffffu, wz, 1), m1, c);
     }
     if (active) {
-      f[q] = fnm;
+      f[q] = (R)fnm;
       fwk[q] = wk;
     }
   }
 }
 
+template <typename R>
 __global__ void __launch_bounds__(64) k_lineA(Grid g, Bufs bf, int rk1) {
   LineThread L;
   if (!line_thread(g, g.tpmA, 3, &L)) return;
@@ -123,18 +127,18 @@ __global__ void __launch_bounds__(64) k_lineA(Grid g, Bufs bf, int rk1) {
   if (L.mean) {
     // visc3d(u00, rf0u, m=1, rk=0) and the RK3 update of the mean profiles
     // (cross.f90:666-672,703-723,753-756); no shear phase, no remap
-    double *mu = bf.mu + (long)L.b * 2 * N + c;
-    double *mwk = bf.mwk + (long)L.b * 2 * N + c;
-    const double *mrf = bf.mrf + (long)L.b * 2 * N + c;
+    R *mu = (R *)bf.mu + (long)L.b * 2 * N + c;
+    R *mwk = (R *)bf.mwk + (long)L.b * 2 * N + c;
+    const R *mrf = (const R *)bf.mrf + (long)L.b * 2 * N + c;
     const cd one = mk(1.0, 0.0);
     const Tail T2 = load_tail(bf.tl2o + (long)L.b * g.nkx * SB_TAIL);
     solve_line(mu, 2, ys, ystr, N, V2, T2, one, one, c, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6],
                false, [&](int j, double x) { ys[j * ystr] = x; });
-    const double gk = kGama[rk], zk = kZeta[rk];
+    const R gk = (R)kGama[rk], zk = (R)kZeta[rk];
     for (int j = 0; j < N; j++) {
-      const double rf = mrf[2 * j] + nu * (-(0.0 * mu[2 * j]) + ys[j * ystr]);
-      double wk = (rk == 0) ? gk * rf : mwk[2 * j] + gk * rf;
-      const double un = mu[2 * j] + Dt * wk;
+      const R rf = mrf[2 * j] + (R)(nu * (-(0.0 * (double)mu[2 * j]) + ys[j * ystr]));
+      R wk = (rk == 0) ? gk * rf : mwk[2 * j] + gk * rf;
+      const R un = mu[2 * j] + (R)Dt * wk;
       if (rk < 2) wk = rf * zk;
       if (L.active) {
         mu[2 * j] = un;
@@ -151,31 +155,32 @@ __global__ void __launch_bounds__(64) k_lineA(Grid g, Bufs bf, int rk1) {
   if (L.role == 0) {
     // d/dy (dH1/dx + dH3/dz) (cross.f90:565-575)
     const Tail T1 = load_tail(bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL);
-    solve_line(bf.D + off, ps, ys, ystr, N, V1, T1, shp, shm, c, 0.0, g.rh1[4], g.rh1[5],
-               g.rh1[6], true, [&](int j, double x) { ys[j * ystr] = x; });
-    store_col(ys, ystr, bf.T + off, ps, N, L.active);
+    solve_line((const R *)bf.D + off, ps, ys, ystr, N, V1, T1, shp, shm, c, 0.0, g.rh1[4],
+               g.rh1[5], g.rh1[6], true, [&](int j, double x) { ys[j * ystr] = x; });
+    store_col(ys, ystr, (R *)bf.T + off, ps, N, L.active);
     return;
   }
   const Tail T2 = load_tail(bf.tl2o + ((long)L.b * g.nkx + i) * SB_TAIL);
   if (L.role == 2) {
     // d2(phi)/dy2 for the viscous term of the phi equation (cross.f90:660)
-    solve_line(bf.phi + off, ps, ys, ystr, N, V2, T2, shp, shm, c, g.rh2[3], g.rh2[4], g.rh2[5],
-               g.rh2[6], false, [&](int j, double x) { ys[j * ystr] = x; });
-    store_col(ys, ystr, bf.S + off, ps, N, L.active);
+    solve_line((const R *)bf.phi + off, ps, ys, ystr, N, V2, T2, shp, shm, c, g.rh2[3], g.rh2[4],
+               g.rh2[5], g.rh2[6], false, [&](int j, double x) { ys[j * ystr] = x; });
+    store_col(ys, ystr, (R *)bf.S + off, ps, N, L.active);
     return;
   }
   // role 1: hg += nu*lap(omega_y) (visc3d, cross.f90:659), RK3 update, remaps
-  solve_line(bf.vor + off, ps, ys, ystr, N, V2, T2, shp, shm, c, g.rh2[3], g.rh2[4], g.rh2[5],
-             g.rh2[6], false, [&](int j, double x) { ys[j * ystr] = x; });
+  solve_line((const R *)bf.vor + off, ps, ys, ystr, N, V2, T2, shp, shm, c, g.rh2[3], g.rh2[4],
+             g.rh2[5], g.rh2[6], false, [&](int j, double x) { ys[j * ystr] = x; });
   const bool is00 = (i == 0 && k == 0);
   const double a = g.alp * i;
   const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
   const double *mf1 = bf.mf1 + (long)L.b * 2 * N * g.nkx + 2 * i;
   const double *mf2 = bf.mf2 + (long)L.b * 2 * N * g.nkx + 2 * i;
-  rk_update(ys, ystr, bf.G + off, nullptr, bf.vor + off, bf.vorwk + off, ps, N, rk,
-            is00 ? 0.0 : nu, a * a + gz * gz, Dt, mf1, mf2, 2 * g.nkx, c, L.active);
+  rk_update<R>(ys, ystr, (const R *)bf.G + off, nullptr, (R *)bf.vor + off, (R *)bf.vorwk + off,
+               ps, N, rk, is00 ? 0.0 : nu, a * a + gz * gz, Dt, mf1, mf2, 2 * g.nkx, c, L.active);
 }
 
+template <typename R>
 __global__ void __launch_bounds__(64) k_lineB(Grid g, Bufs bf, int mode) {
   LineThread L;
   if (!line_thread(g, g.tpmB, 2, &L)) return;
@@ -186,13 +191,13 @@ __global__ void __launch_bounds__(64) k_lineB(Grid g, Bufs bf, int mode) {
   const FacView V1(bf.d1, 0);
   if (L.mean) {
     // derivyc(u00, rf0u, 1, 1, 0) and of w00, used by hvhg (cross.f90:1186-1192)
-    double *mu = bf.mu + (long)L.b * 2 * N + c;
-    double *mdu = bf.mdu + (long)L.b * 2 * N + c;
+    const R *mu = (const R *)bf.mu + (long)L.b * 2 * N + c;
+    R *mdu = (R *)bf.mdu + (long)L.b * 2 * N + c;
     const cd one = mk(1.0, 0.0);
     const Tail T1 = load_tail(bf.tl1o + (long)L.b * g.nkx * SB_TAIL);
     solve_line(mu, 2, ys, ystr, N, V1, T1, one, one, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true,
                [&](int j, double x) {
-                 if (L.active) mdu[2 * j] = x;
+                 if (L.active) mdu[2 * j] = (R)x;
                });
     return;
   }
@@ -207,9 +212,9 @@ __global__ void __launch_bounds__(64) k_lineB(Grid g, Bufs bf, int mode) {
   const Tail T1 = load_tail(tl1 + ((long)L.b * g.nkx + i) * SB_TAIL);
   if (L.role == 0) {
     // d(omega_y)/dy (cross.f90:440)
-    solve_line(bf.vor + off, ps, ys, ystr, N, V1, T1, shp, shm, c, 0.0, g.rh1[4], g.rh1[5],
-               g.rh1[6], true, [&](int j, double x) { ys[j * ystr] = x; });
-    store_col(ys, ystr, bf.D + off, ps, N, L.active);
+    solve_line((const R *)bf.vor + off, ps, ys, ystr, N, V1, T1, shp, shm, c, 0.0, g.rh1[4],
+               g.rh1[5], g.rh1[6], true, [&](int j, double x) { ys[j * ystr] = x; });
+    store_col(ys, ystr, (R *)bf.D + off, ps, N, L.active);
     return;
   }
   const bool is00 = (i == 0 && k == 0);
@@ -222,32 +227,34 @@ __global__ void __launch_bounds__(64) k_lineB(Grid g, Bufs bf, int mode) {
     const double *mf1 = bf.mf1 + (long)L.b * 2 * N * g.nkx + 2 * i;
     const double *mf2 = bf.mf2 + (long)L.b * 2 * N * g.nkx + 2 * i;
     // the d2(phi)/dy2 of k_lineA goes through the shared buffer
-    const double *S = bf.S + off;
-    for (int j = 0; j < N; j++) ys[j * ystr] = S[(long)j * ps];
-    rk_update(ys, ystr, bf.V + off, bf.T + off, bf.phi + off, bf.phiwk + off, ps, N, rk,
-              is00 ? 0.0 : M.nu, a * a + gz * gz, M.Deltat, mf1, mf2, 2 * g.nkx, c, L.active);
+    const R *S = (const R *)bf.S + off;
+    for (int j = 0; j < N; j++) ys[j * ystr] = (double)S[(long)j * ps];
+    rk_update<R>(ys, ystr, (const R *)bf.V + off, (const R *)bf.T + off, (R *)bf.phi + off,
+                 (R *)bf.phiwk + off, ps, N, rk, is00 ? 0.0 : M.nu, a * a + gz * gz, M.Deltat,
+                 mf1, mf2, 2 * g.nkx, c, L.active);
   }
   // v = lapcdy(phi) (cross.f90:784-795, first step: 408-426); hg(0,0) keeps
   // the value the nonlinear stage left (zero), or zero in the prologue
   {
     const FacView VH(bf.hz, L.lc);
     const Tail TH = make_tail(VH, shp, N);
-    solve_line(bf.phi + off, ps, ys, ystr, N, VH, TH, shp, shm, c, g.pr2[3], g.pr2[4], g.pr2[5],
-               g.pr2[6], false, [&](int j, double x) { ys[j * ystr] = x; });
+    solve_line((const R *)bf.phi + off, ps, ys, ystr, N, VH, TH, shp, shm, c, g.pr2[3], g.pr2[4],
+               g.pr2[5], g.pr2[6], false, [&](int j, double x) { ys[j * ystr] = x; });
     if (is00) {
       if (mode == 0 && L.active)
-        for (int j = 0; j < N; j++) bf.G[off + (long)j * ps] = 0.0;
+        for (int j = 0; j < N; j++) ((R *)bf.G)[off + (long)j * ps] = (R)0;
     } else {
-      store_col(ys, ystr, bf.G + off, ps, N, L.active);
+      store_col(ys, ystr, (R *)bf.G + off, ps, N, L.active);
     }
   }
   // dv/dy (cross.f90:442)
-  solve_line(bf.G + off, ps, ys, ystr, N, V1, T1, shp, shm, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6],
-             true, [&](int j, double x) { ys[j * ystr] = x; });
-  store_col(ys, ystr, bf.V + off, ps, N, L.active);
+  solve_line((const R *)bf.G + off, ps, ys, ystr, N, V1, T1, shp, shm, c, 0.0, g.rh1[4], g.rh1[5],
+             g.rh1[6], true, [&](int j, double x) { ys[j * ystr] = x; });
+  store_col(ys, ystr, (R *)bf.V + off, ps, N, L.active);
 }
 
 // set_conj on the state (operators.f90:1382-1429) at entry of a cross call
+template <typename R>
 __global__ void k_setconj(Grid g, Bufs bf) {
   const int nneg = g.mz - 1 - g.nz;
   const long n = (long)g.B * g.my * nneg * 2;
@@ -260,9 +267,10 @@ __global__ void k_setconj(Grid g, Bufs bf) {
     const int k = g.nz + 1 + kk;
     const long base = (long)b * g.field + (long)j * g.plane;
     const long dst = base + 2L * k * g.nkx + c, src = base + 2L * (g.mz - k) * g.nkx + c;
-    const double v = bf.vor[src], p = bf.phi[src];
-    bf.vor[dst] = c ? -v : v;
-    bf.phi[dst] = c ? -p : p;
+    R *vor = (R *)bf.vor, *phi = (R *)bf.phi;
+    const R v = vor[src], p = phi[src];
+    vor[dst] = c ? -v : v;
+    phi[dst] = c ? -p : p;
   }
 }
 
@@ -308,7 +316,9 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
       for (int cb = 0; cb < g.ncb; cb++)
         for (int q = 0; q < SB_NHIST_Q; q++) pl[q] += hp[cb * SB_NHIST_Q + q];
       for (int q = 0; q < SB_NHIST_Q; q++) acc[q] += pl[q];
-      const double o3 = -bf.mdu[2 * ((long)b * g.my + j)] - g.s;
+      const double du = g.prec ? (double)((const float *)bf.mdu)[2 * ((long)b * g.my + j)]
+                               : bf.mdu[2 * ((long)b * g.my + j)];
+      const double o3 = -du - g.s;
       acc[SB_NHIST_Q] += -o3 * (-pl[3]) + (o3 * o3) * (1.0 / M.Re);
     }
     for (int q = 0; q < nq; q++) {
@@ -503,25 +513,38 @@ size_t line_smem(const Grid &g) { return sizeof(double) * kLineT * g.my; }
 
 cudaError_t prepare_line(const Grid &g) {
   const int sm = (int)line_smem(g);
-  cudaFuncSetAttribute(k_lineA, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  cudaFuncSetAttribute(k_lineB, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_lineA<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_lineB<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_lineA<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_lineB<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   return cudaGetLastError();
 }
 
 cudaError_t launch_lineA(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
   const long nth = (long)g.B * g.tpmA;
-  k_lineA<<<(unsigned)((nth + kLineT - 1) / kLineT), kLineT, line_smem(g), st>>>(g, bf, rk);
+  const unsigned nb = (unsigned)((nth + kLineT - 1) / kLineT);
+  if (g.prec)
+    k_lineA<float><<<nb, kLineT, line_smem(g), st>>>(g, bf, rk);
+  else
+    k_lineA<double><<<nb, kLineT, line_smem(g), st>>>(g, bf, rk);
   return cudaGetLastError();
 }
 
 cudaError_t launch_lineB(const Grid &g, const Bufs &bf, int mode, cudaStream_t st) {
   const long nth = (long)g.B * g.tpmB;
-  k_lineB<<<(unsigned)((nth + kLineT - 1) / kLineT), kLineT, line_smem(g), st>>>(g, bf, mode);
+  const unsigned nb = (unsigned)((nth + kLineT - 1) / kLineT);
+  if (g.prec)
+    k_lineB<float><<<nb, kLineT, line_smem(g), st>>>(g, bf, mode);
+  else
+    k_lineB<double><<<nb, kLineT, line_smem(g), st>>>(g, bf, mode);
   return cudaGetLastError();
 }
 
 cudaError_t launch_setconj(const Grid &g, const Bufs &bf, cudaStream_t st) {
-  k_setconj<<<64, 256, 0, st>>>(g, bf);
+  if (g.prec)
+    k_setconj<float><<<64, 256, 0, st>>>(g, bf);
+  else
+    k_setconj<double><<<64, 256, 0, st>>>(g, bf);
   return cudaGetLastError();
 }
 
