@@ -88,7 +88,14 @@ static int check_params(const sb_params *p) {
 static int upload_uniform(sb_handle *h, Fac *F, const double a[7], int n) {
   sbh::BaseFac b;
   sbh::base_factor(a, n, &b);
+  sbh::SegPlan plan;
+  sbh::seg_plan(n, h->g.nseg, &plan);
+  sbh::SegFac sf;
+  sbh::seg_factor(b, n, plan, &sf);
   int rc;
+  for (int t = 0; t < 3; t++)
+    if ((rc = upload(h, &F->hf[t], sf.hf[t])) || (rc = upload(h, &F->hb[t], sf.hb[t]))) return rc;
+  if ((rc = upload(h, &F->ef, sf.ef))) return rc;
   if ((rc = upload(h, &F->La, b.La)) || (rc = upload(h, &F->Lb, b.Lb)) ||
       (rc = upload(h, &F->Lc, b.Lc)) || (rc = upload(h, &F->Ddm1, b.Ddm1)) ||
       (rc = upload(h, &F->Dd, b.Dd)) || (rc = upload(h, &F->e, b.e)) ||
@@ -310,8 +317,14 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   g.plane = 2L * nl;
   g.field = g.plane * g.my;
   g.nlines_pad = ((2 * nl + 31) / 32) * 32;
-  g.tpmA = 3 * g.nlines_pad + 32;
-  g.tpmB = 2 * g.nlines_pad + 32;
+  g.ngrp = (nl + 15) / 16;
+  sbh::SegPlan plan;
+  sbh::seg_plan(g.my, line_segments(), &plan);
+  g.nseg = plan.nseg;
+  for (int q = 0; q < plan.nseg; q++) {
+    g.slo[q] = plan.lo[q];
+    g.shi[q] = plan.hi[q];
+  }
   cudaError_t ce = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
   if (ce != cudaSuccess) {
     delete h;
@@ -392,6 +405,14 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
     const size_t n = g.my;
     std::vector<double> La(n * nl), Lb(n * nl), Lc(n * nl), Dm(n * nl), Dd(n * nl), e(n * nl),
         f(n * nl), gg(n * nl), sums(10 * (size_t)nl);
+    std::vector<double> hf[3], hb[3], ef(9 * (size_t)g.nseg * nl);
+    for (int t = 0; t < 3; t++) {
+      hf[t].assign(n * nl, 0.0);
+      hb[t].assign(n * nl, 0.0);
+    }
+    sbh::SegPlan plan;
+    sbh::seg_plan(g.my, g.nseg, &plan);
+    sbh::SegFac sfac;
     sbh::BaseFac bfac;
     for (int k = 0; k < g.mz; k++)
       for (int i = 0; i < g.nkx; i++) {
@@ -414,11 +435,22 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
         }
         for (int q = 0; q < 6; q++) sums[(size_t)q * nl + line] = bfac.sums[q];
         for (int q = 0; q < 4; q++) sums[(size_t)(6 + q) * nl + line] = lap[3 + q];
+        sbh::seg_factor(bfac, g.my, plan, &sfac);
+        for (int t = 0; t < 3; t++)
+          for (size_t q = 0; q < n; q++) {
+            hf[t][q * nl + line] = sfac.hf[t][q];
+            hb[t][q * nl + line] = sfac.hb[t][q];
+          }
+        for (size_t q = 0; q < sfac.ef.size(); q++) ef[q * nl + line] = sfac.ef[q];
       }
     Fac &H = bf.hz;
     if ((rc = upload(h, &H.La, La)) || (rc = upload(h, &H.Lb, Lb)) || (rc = upload(h, &H.Lc, Lc)) ||
         (rc = upload(h, &H.Ddm1, Dm)) || (rc = upload(h, &H.Dd, Dd)) || (rc = upload(h, &H.e, e)) ||
-        (rc = upload(h, &H.f, f)) || (rc = upload(h, &H.g, gg)) || (rc = upload(h, &H.sums, sums))) {
+        (rc = upload(h, &H.f, f)) || (rc = upload(h, &H.g, gg)) || (rc = upload(h, &H.sums, sums)) ||
+        (rc = upload(h, &H.hf[0], hf[0])) || (rc = upload(h, &H.hf[1], hf[1])) ||
+        (rc = upload(h, &H.hf[2], hf[2])) || (rc = upload(h, &H.hb[0], hb[0])) ||
+        (rc = upload(h, &H.hb[1], hb[1])) || (rc = upload(h, &H.hb[2], hb[2])) ||
+        (rc = upload(h, &H.ef, ef))) {
       sb_destroy(h);
       return rc;
     }

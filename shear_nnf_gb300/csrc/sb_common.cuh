@@ -39,6 +39,8 @@ struct Fac {
   const double *La, *Lb, *Lc, *Ddm1, *e, *f, *g;  // my entries each
   const double *Dd;    // my entries (rows my-8 .. my-4 are read)
   const double *sums;  // 10 entries: See Sfe Sff Sge Sgf Sgg, then a(0..3)
+  const double *hf[3], *hb[3];  // segment homogeneous solutions (my entries each)
+  const double *ef;             // segment border sums (9 per segment)
   long stride;
 };
 
@@ -52,7 +54,8 @@ struct Grid {
   long plane;            // doubles per plane of one field  (2*nkx*mz)
   long field;            // doubles per field of one box   (plane*my)
   int nlines_pad;        // component lines per member, padded to whole warps
-  int tpmA, tpmB;        // threads per member of the two y-line kernels
+  int nseg, slo[4], shi[4];  // segments of the banded rows of the y-solves
+  int ngrp;              // groups of 16 lines per member in the y-line kernels
 };
 
 // Per-member run state, owned by the device (one per box in the batch)

@@ -200,6 +200,57 @@ void base_factor(const double a[7], int n, BaseFac *o) {
   o->sums[5] = Sgg;
 }
 
+void seg_plan(int n, int nseg, SegPlan *p) {
+  const int m = n - 3;  // banded rows 1..n-3
+  p->nseg = nseg;
+  int lo = 1;
+  for (int s = 0; s < nseg; s++) {
+    const int size = m / nseg + (s < m % nseg ? 1 : 0);
+    p->lo[s] = lo;
+    p->hi[s] = lo + size - 1;
+    lo += size;
+  }
+}
+
+void seg_factor(const BaseFac &b, int n, const SegPlan &p, SegFac *o) {
+  auto at = [&](const std::vector<double> &v, int i) { return (i >= 1 && i <= n) ? v[i - 1] : 0.0; };
+  for (int t = 0; t < 3; t++) {
+    o->hf[t].assign(n, 0.0);
+    o->hb[t].assign(n, 0.0);
+  }
+  o->ef.assign(9 * (size_t)p.nseg, 0.0);
+  for (int s = 0; s < p.nseg; s++) {
+    const int lo = p.lo[s], hi = p.hi[s];
+    for (int t = 1; t <= 3; t++) {
+      // forward: state h[lo-1], h[lo-2], h[lo-3] with h[lo-t] = 1
+      std::vector<double> h(n + 8, 0.0);
+      auto H = [&](int i) -> double & { return h[i + 4]; };
+      H(lo - t) = 1.0;
+      for (int i = lo; i <= hi; i++)
+        H(i) = -at(b.Lc, i) * H(i - 3) - at(b.Lb, i) * H(i - 2) - at(b.La, i) * H(i - 1);
+      double se = 0, sf = 0, sg = 0;
+      for (int i = lo; i <= hi; i++) {
+        o->hf[t - 1][i - 1] = H(i);
+        se += at(b.e, i) * H(i);
+        sf += at(b.f, i) * H(i);
+        sg += at(b.g, i) * H(i);
+      }
+      o->ef[(s * 3 + 0) * 3 + t - 1] = se;
+      o->ef[(s * 3 + 1) * 3 + t - 1] = sf;
+      o->ef[(s * 3 + 2) * 3 + t - 1] = sg;
+      if (s < p.nseg - 1) {
+        std::vector<double> gq(n + 8, 0.0);
+        auto Gq = [&](int i) -> double & { return gq[i]; };
+        Gq(hi + t) = 1.0;
+        for (int i = hi; i >= lo; i--)
+          Gq(i) = -at(b.La, i + 1) * Gq(i + 1) - at(b.Lb, i + 2) * Gq(i + 2) -
+                  at(b.Lc, i + 3) * Gq(i + 3);
+        for (int i = lo; i <= hi; i++) o->hb[t - 1][i - 1] = Gq(i);
+      }
+    }
+  }
+}
+
 // SplitMix64: counter-based so that every (seed, mode) pair has its own stream
 static inline uint64_t splitmix(uint64_t x) {
   x += 0x9E3779B97F4A7C15ull;

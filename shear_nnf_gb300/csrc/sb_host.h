@@ -25,6 +25,23 @@ struct BaseFac {
 };
 void base_factor(const double a[7], int n, BaseFac *out);
 
+// Segmented solves: the banded rows 1..n-3 split into nseg consecutive
+// segments solved in parallel.  For segment s (rows lo..hi, 1-based) and
+// t = 1..3: hf[t-1][i-1] is the solution of the homogeneous forward recurrence
+// h_i = -Lc_i h_{i-3} - Lb_i h_{i-2} - La_i h_{i-1} on lo..hi started from a unit
+// value at row lo-t; hb[t-1][i-1] that of the backward recurrence
+// g_i = -La_{i+1} g_{i+1} - Lb_{i+2} g_{i+2} - Lc_{i+3} g_{i+3} on hi..lo started from
+// a unit value at row hi+t (segments below the top one only); ef[(s*3+q)*3+t-1]
+// = sum over the segment of border-row base q (e, f, g) times hf.
+struct SegPlan {
+  int nseg, lo[4], hi[4];
+};
+void seg_plan(int n, int nseg, SegPlan *p);
+struct SegFac {
+  std::vector<double> hf[3], hb[3], ef;
+};
+void seg_factor(const BaseFac &b, int n, const SegPlan &p, SegFac *out);
+
 // Seeded divergence-free initial field (synthetic stand-in for the reference's
 // getini spectrum, initcr.f90:664-822): random-phase Fourier modes with energy
 // spectrum E(k) ~ k^4 exp(-2 (k/k0)^2), rms velocity urms.  Outputs the

@@ -11,6 +11,7 @@ int plane_cb(int mgalz);
 bool supported_grid(int mgalx, int mgalz);
 cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st);
 cudaError_t prepare_line(const Grid &g);
+int line_segments();
 size_t line_smem(const Grid &g);
 cudaError_t launch_lineA(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
 cudaError_t launch_lineB(const Grid &g, const Bufs &bf, int mode, cudaStream_t st);

@@ -26,73 +26,83 @@
 #include "sb_common.cuh"
 #include "sb_kernels.h"
 #include "sb_line.cuh"
+#include "sb_seg.cuh"
 
 namespace sb {
 
 __device__ __forceinline__ cd ldc2(const double *p) { return mk(p[0], p[1]); }
 
-// thread -> (member, role, line, component) of a y-line kernel with `roles`
-// roles; the last warp of every member is the mean line u00 + i w00
+// Block -> (member, role, group of 16 lines); warp -> segment of the banded
+// rows; lane -> (line of the group, component).  The last block of every
+// member is the mean line u00 + i w00 (line slot 0).
+constexpr int kSeg = 2;  // segments per line solve (warps per block)
 struct LineThread {
-  int b, role, c, i, k;
+  int b, role, c, s, l, i, k, r0, r1;
   long lc;
   bool active, mean;
 };
-__device__ __forceinline__ bool line_thread(const Grid &g, int tpm, int roles, LineThread *L) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  L->b = (int)(t / tpm);
+__device__ __forceinline__ bool line_thread(const Grid &g, int roles, LineThread *L) {
+  const int per = roles * g.ngrp + 1;
+  L->b = blockIdx.x / per;
   if (L->b >= g.B) return false;
-  const int r = (int)(t - (long)L->b * tpm);
-  L->c = r & 1;
-  L->role = r / g.nlines_pad;
+  const int r = blockIdx.x - L->b * per;
+  L->role = r / g.ngrp;
   L->mean = L->role >= roles;
+  const int lane = threadIdx.x & 31;
+  L->s = threadIdx.x >> 5;
+  L->l = lane >> 1;
+  L->c = lane & 1;
   const int nl = g.nkx * g.mz;
   if (L->mean) {
     L->lc = 0;
-    L->active = (r - roles * g.nlines_pad) < 2;
+    L->active = (L->l == 0);
   } else {
-    L->lc = (r - L->role * g.nlines_pad) >> 1;
+    L->lc = (long)(r - L->role * g.ngrp) * 16 + L->l;
     L->active = L->lc < nl;
     if (!L->active) L->lc = nl - 1;
   }
   L->i = (int)(L->lc % g.nkx);
   L->k = (int)(L->lc / g.nkx);
+  L->r0 = g.slo[L->s];
+  L->r1 = (L->s == kSeg - 1) ? g.my : g.shi[L->s];
   return true;
 }
 
-// one thread's column of the shared-memory forward-substitution buffer
+// one thread's column of the shared-memory buffer (its segment's rows)
 __device__ __forceinline__ double *ycol() {
   extern __shared__ double sm_y[];
   return sm_y + threadIdx.x;
 }
 
-// copy a solution kept in shared memory to a field line
+// copy this segment's rows of a solution kept in shared memory to a field line
 template <typename R>
 __device__ __forceinline__ void store_col(const double *ys, int ystr, R *__restrict__ dst, long ps,
-                                          int N, bool active) {
-  if (!active) return;
+                                          const LineThread &L) {
+  if (!L.active) return;
 #pragma unroll 4
-  for (int j = 0; j < N; j++) dst[(long)j * ps] = (R)ys[j * ystr];
+  for (int i = L.r0; i <= L.r1; i++) dst[(long)(i - 1) * ps] = (R)ys[(i - L.r0) * ystr];
 }
 
-// RK3 accumulate/update of one field line with the zeta store and both
-// moving_frame remaps (cross.f90:694-781), fused per point.  x = d2f/dy2 in
-// the shared buffer (FP64); rhs = the nonlinear right-hand side (minus `sub`
-// if given); f, fwk the field and its RK work array.  The RK arithmetic runs in
-// the storage precision R; the viscous term and the remaps (phase factors) in
-// FP64.
+// RK3 accumulate/update of this segment's rows of one field line with the
+// zeta store and both moving_frame remaps (cross.f90:694-781), fused per
+// point.  x = d2f/dy2 in the shared buffer (FP64); rhs = the nonlinear
+// right-hand side (minus `sub` if given); f, fwk the field and its RK work
+// array.  The RK arithmetic runs in the storage precision R; the viscous term
+// and the remaps (phase factors) in FP64.
 template <typename R>
 __device__ __forceinline__ void rk_update(const double *ys, int ystr, const R *__restrict__ rhs,
                                           const R *__restrict__ sub, R *__restrict__ f,
-                                          R *__restrict__ fwk, long ps, int N, int rk, double nuv,
-                                          double k2, double Dt, const double *__restrict__ mf1,
-                                          const double *__restrict__ mf2, long mfs, int c,
-                                          bool active) {
+                                          R *__restrict__ fwk, long ps, const LineThread &L,
+                                          int rk, double nuv, double k2, double Dt,
+                                          const double *__restrict__ mf1,
+                                          const double *__restrict__ mf2, long mfs) {
   const R gk = (R)kGama[rk], zk = (R)kZeta[rk], dtr = (R)Dt;
+  const int c = L.c;
 #pragma unroll 2
-  for (int j = 0; j < N; j++) {
+  for (int i = L.r0; i <= L.r1; i++) {
+    const int j = i - 1;
     const long q = (long)j * ps;
-    const double x = ys[j * ystr];
+    const double x = ys[(i - L.r0) * ystr];
     const R fo = f[q];
     R h = rhs[q];
     if (sub) h = h - sub[q];
@@ -106,37 +116,43 @@ __device__ __forceinline__ void rk_update(const double *ys, int ystr, const R *_
       const double wz = (double)(h * zk);
       wk = (R)cmul_c(wz, __shfl_xor_sync(0xffffffffu, wz, 1), m1, c);
     }
-    if (active) {
+    if (L.active) {
       f[q] = (R)fnm;
       fwk[q] = wk;
     }
   }
 }
 
+#define SEG_SOLVE(U, PS, VIEW, SVIEW, TAIL, SHP, SHM, R0, R1, R2, R3, ANTI)                     \
+  solve_seg<kSeg>(U, PS, ys, ystr, N, VIEW, SVIEW, TAIL, SHP, SHM, L.c, L.s, L.l, g.slo, g.shi, \
+                  R0, R1, R2, R3, ANTI, &xch[0][0][0][0])
+
 template <typename R>
-__global__ void __launch_bounds__(64) k_lineA(Grid g, Bufs bf, int rk1) {
+__global__ void __launch_bounds__(32 * kSeg) k_lineA(Grid g, Bufs bf, int rk1) {
+  __shared__ double xch[kSeg][16][2][SB_XS];
   LineThread L;
-  if (!line_thread(g, g.tpmA, 3, &L)) return;
+  if (!line_thread(g, 3, &L)) return;  // whole blocks
   Member &M = bf.mem[L.b];
-  if (M.halted) return;  // uniform per warp (every role spans whole warps)
-  const int N = g.my, c = L.c, ystr = blockDim.x;
+  if (M.halted) return;  // uniform per block
+  const int N = g.my, ystr = blockDim.x;
   const int rk = rk1 - 1;
   double *ys = ycol();
   const FacView V1(bf.d1, 0), V2(bf.d2, 0);
+  const SegView W1(bf.d1, 0), W2(bf.d2, 0);
   const double Dt = M.Deltat, nu = M.nu;
   if (L.mean) {
     // visc3d(u00, rf0u, m=1, rk=0) and the RK3 update of the mean profiles
     // (cross.f90:666-672,703-723,753-756); no shear phase, no remap
-    R *mu = (R *)bf.mu + (long)L.b * 2 * N + c;
-    R *mwk = (R *)bf.mwk + (long)L.b * 2 * N + c;
-    const R *mrf = (const R *)bf.mrf + (long)L.b * 2 * N + c;
+    R *mu = (R *)bf.mu + (long)L.b * 2 * N + L.c;
+    R *mwk = (R *)bf.mwk + (long)L.b * 2 * N + L.c;
+    const R *mrf = (const R *)bf.mrf + (long)L.b * 2 * N + L.c;
     const cd one = mk(1.0, 0.0);
     const Tail T2 = load_tail(bf.tl2o + (long)L.b * g.nkx * SB_TAIL);
-    solve_line(mu, 2, ys, ystr, N, V2, T2, one, one, c, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6],
-               false, [&](int j, double x) { ys[j * ystr] = x; });
+    SEG_SOLVE(mu, 2, V2, W2, T2, one, one, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6], false);
     const R gk = (R)kGama[rk], zk = (R)kZeta[rk];
-    for (int j = 0; j < N; j++) {
-      const R rf = mrf[2 * j] + (R)(nu * (-(0.0 * (double)mu[2 * j]) + ys[j * ystr]));
+    for (int i = L.r0; i <= L.r1; i++) {
+      const int j = i - 1;
+      const R rf = mrf[2 * j] + (R)(nu * (-(0.0 * (double)mu[2 * j]) + ys[(i - L.r0) * ystr]));
       R wk = (rk == 0) ? gk * rf : mwk[2 * j] + gk * rf;
       const R un = mu[2 * j] + (R)Dt * wk;
       if (rk < 2) wk = rf * zk;
@@ -147,7 +163,7 @@ __global__ void __launch_bounds__(64) k_lineA(Grid g, Bufs bf, int rk1) {
     }
     return;
   }
-  const long off = (long)L.b * g.field + 2 * L.lc + c;
+  const long off = (long)L.b * g.field + 2 * L.lc + L.c;
   const long ps = g.plane;
   const int i = L.i, k = L.k;
   const cd shp = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * i);
@@ -155,53 +171,54 @@ __global__ void __launch_bounds__(64) k_lineA(Grid g, Bufs bf, int rk1) {
   if (L.role == 0) {
     // d/dy (dH1/dx + dH3/dz) (cross.f90:565-575)
     const Tail T1 = load_tail(bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL);
-    solve_line((const R *)bf.D + off, ps, ys, ystr, N, V1, T1, shp, shm, c, 0.0, g.rh1[4],
-               g.rh1[5], g.rh1[6], true, [&](int j, double x) { ys[j * ystr] = x; });
-    store_col(ys, ystr, (R *)bf.T + off, ps, N, L.active);
+    SEG_SOLVE((const R *)bf.D + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5], g.rh1[6],
+              true);
+    store_col(ys, ystr, (R *)bf.T + off, ps, L);
     return;
   }
   const Tail T2 = load_tail(bf.tl2o + ((long)L.b * g.nkx + i) * SB_TAIL);
   if (L.role == 2) {
     // d2(phi)/dy2 for the viscous term of the phi equation (cross.f90:660)
-    solve_line((const R *)bf.phi + off, ps, ys, ystr, N, V2, T2, shp, shm, c, g.rh2[3], g.rh2[4],
-               g.rh2[5], g.rh2[6], false, [&](int j, double x) { ys[j * ystr] = x; });
-    store_col(ys, ystr, (R *)bf.S + off, ps, N, L.active);
+    SEG_SOLVE((const R *)bf.phi + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
+              g.rh2[6], false);
+    store_col(ys, ystr, (R *)bf.S + off, ps, L);
     return;
   }
   // role 1: hg += nu*lap(omega_y) (visc3d, cross.f90:659), RK3 update, remaps
-  solve_line((const R *)bf.vor + off, ps, ys, ystr, N, V2, T2, shp, shm, c, g.rh2[3], g.rh2[4],
-             g.rh2[5], g.rh2[6], false, [&](int j, double x) { ys[j * ystr] = x; });
+  SEG_SOLVE((const R *)bf.vor + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
+            g.rh2[6], false);
   const bool is00 = (i == 0 && k == 0);
   const double a = g.alp * i;
   const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
   const double *mf1 = bf.mf1 + (long)L.b * 2 * N * g.nkx + 2 * i;
   const double *mf2 = bf.mf2 + (long)L.b * 2 * N * g.nkx + 2 * i;
   rk_update<R>(ys, ystr, (const R *)bf.G + off, nullptr, (R *)bf.vor + off, (R *)bf.vorwk + off,
-               ps, N, rk, is00 ? 0.0 : nu, a * a + gz * gz, Dt, mf1, mf2, 2 * g.nkx, c, L.active);
+               ps, L, rk, is00 ? 0.0 : nu, a * a + gz * gz, Dt, mf1, mf2, 2 * g.nkx);
 }
 
 template <typename R>
-__global__ void __launch_bounds__(64) k_lineB(Grid g, Bufs bf, int mode) {
+__global__ void __launch_bounds__(32 * kSeg) k_lineB(Grid g, Bufs bf, int mode) {
+  __shared__ double xch[kSeg][16][2][SB_XS];
   LineThread L;
-  if (!line_thread(g, g.tpmB, 2, &L)) return;
+  if (!line_thread(g, 2, &L)) return;
   Member &M = bf.mem[L.b];
   if (M.halted) return;
-  const int N = g.my, c = L.c, ystr = blockDim.x;
+  const int N = g.my, ystr = blockDim.x;
   double *ys = ycol();
   const FacView V1(bf.d1, 0);
+  const SegView W1(bf.d1, 0);
   if (L.mean) {
     // derivyc(u00, rf0u, 1, 1, 0) and of w00, used by hvhg (cross.f90:1186-1192)
-    const R *mu = (const R *)bf.mu + (long)L.b * 2 * N + c;
-    R *mdu = (R *)bf.mdu + (long)L.b * 2 * N + c;
+    const R *mu = (const R *)bf.mu + (long)L.b * 2 * N + L.c;
+    R *mdu = (R *)bf.mdu + (long)L.b * 2 * N + L.c;
     const cd one = mk(1.0, 0.0);
     const Tail T1 = load_tail(bf.tl1o + (long)L.b * g.nkx * SB_TAIL);
-    solve_line(mu, 2, ys, ystr, N, V1, T1, one, one, c, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true,
-               [&](int j, double x) {
-                 if (L.active) mdu[2 * j] = (R)x;
-               });
+    SEG_SOLVE(mu, 2, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true);
+    if (L.active)
+      for (int i = L.r0; i <= L.r1; i++) mdu[2 * (i - 1)] = (R)ys[(i - L.r0) * ystr];
     return;
   }
-  const long off = (long)L.b * g.field + 2 * L.lc + c;
+  const long off = (long)L.b * g.field + 2 * L.lc + L.c;
   const long ps = g.plane;
   const int i = L.i, k = L.k;
   // the phase at t + c_k dt (substeps) or at t (prologue)
@@ -212,9 +229,9 @@ __global__ void __launch_bounds__(64) k_lineB(Grid g, Bufs bf, int mode) {
   const Tail T1 = load_tail(tl1 + ((long)L.b * g.nkx + i) * SB_TAIL);
   if (L.role == 0) {
     // d(omega_y)/dy (cross.f90:440)
-    solve_line((const R *)bf.vor + off, ps, ys, ystr, N, V1, T1, shp, shm, c, 0.0, g.rh1[4],
-               g.rh1[5], g.rh1[6], true, [&](int j, double x) { ys[j * ystr] = x; });
-    store_col(ys, ystr, (R *)bf.D + off, ps, N, L.active);
+    SEG_SOLVE((const R *)bf.vor + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
+              g.rh1[6], true);
+    store_col(ys, ystr, (R *)bf.D + off, ps, L);
     return;
   }
   const bool is00 = (i == 0 && k == 0);
@@ -228,29 +245,32 @@ __global__ void __launch_bounds__(64) k_lineB(Grid g, Bufs bf, int mode) {
     const double *mf2 = bf.mf2 + (long)L.b * 2 * N * g.nkx + 2 * i;
     // the d2(phi)/dy2 of k_lineA goes through the shared buffer
     const R *S = (const R *)bf.S + off;
-    for (int j = 0; j < N; j++) ys[j * ystr] = (double)S[(long)j * ps];
+    for (int r = L.r0; r <= L.r1; r++) ys[(r - L.r0) * ystr] = (double)S[(long)(r - 1) * ps];
     rk_update<R>(ys, ystr, (const R *)bf.V + off, (const R *)bf.T + off, (R *)bf.phi + off,
-                 (R *)bf.phiwk + off, ps, N, rk, is00 ? 0.0 : M.nu, a * a + gz * gz, M.Deltat,
-                 mf1, mf2, 2 * g.nkx, c, L.active);
+                 (R *)bf.phiwk + off, ps, L, rk, is00 ? 0.0 : M.nu, a * a + gz * gz, M.Deltat,
+                 mf1, mf2, 2 * g.nkx);
+    __syncthreads();  // the whole updated line is read below
   }
   // v = lapcdy(phi) (cross.f90:784-795, first step: 408-426); hg(0,0) keeps
   // the value the nonlinear stage left (zero), or zero in the prologue
   {
     const FacView VH(bf.hz, L.lc);
+    const SegView WH(bf.hz, L.lc);
     const Tail TH = make_tail(VH, shp, N);
-    solve_line((const R *)bf.phi + off, ps, ys, ystr, N, VH, TH, shp, shm, c, g.pr2[3], g.pr2[4],
-               g.pr2[5], g.pr2[6], false, [&](int j, double x) { ys[j * ystr] = x; });
+    SEG_SOLVE((const R *)bf.phi + off, ps, VH, WH, TH, shp, shm, g.pr2[3], g.pr2[4], g.pr2[5],
+              g.pr2[6], false);
     if (is00) {
       if (mode == 0 && L.active)
-        for (int j = 0; j < N; j++) ((R *)bf.G)[off + (long)j * ps] = (R)0;
+        for (int r = L.r0; r <= L.r1; r++) ((R *)bf.G)[off + (long)(r - 1) * ps] = (R)0;
     } else {
-      store_col(ys, ystr, (R *)bf.G + off, ps, N, L.active);
+      store_col(ys, ystr, (R *)bf.G + off, ps, L);
     }
   }
+  __syncthreads();  // v of all segments is read below
   // dv/dy (cross.f90:442)
-  solve_line((const R *)bf.G + off, ps, ys, ystr, N, V1, T1, shp, shm, c, 0.0, g.rh1[4], g.rh1[5],
-             g.rh1[6], true, [&](int j, double x) { ys[j * ystr] = x; });
-  store_col(ys, ystr, (R *)bf.V + off, ps, N, L.active);
+  SEG_SOLVE((const R *)bf.G + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5], g.rh1[6],
+            true);
+  store_col(ys, ystr, (R *)bf.V + off, ps, L);
 }
 
 // set_conj on the state (operators.f90:1382-1429) at entry of a cross call
@@ -507,9 +527,16 @@ __global__ void k_finish(Grid g, Bufs bf) {
 }
 
 // ---------------------------------------------------------------------------
-static const int kLineT = 64;
+static const int kLineT = 32 * kSeg;
 
-size_t line_smem(const Grid &g) { return sizeof(double) * kLineT * g.my; }
+size_t line_smem(const Grid &g) {
+  int rows = 0;
+  for (int s = 0; s < g.nseg; s++) {
+    const int r1 = (s == g.nseg - 1) ? g.my : g.shi[s];
+    rows = rows > r1 - g.slo[s] + 1 ? rows : r1 - g.slo[s] + 1;
+  }
+  return sizeof(double) * kLineT * rows;
+}
 
 cudaError_t prepare_line(const Grid &g) {
   const int sm = (int)line_smem(g);
@@ -520,9 +547,10 @@ cudaError_t prepare_line(const Grid &g) {
   return cudaGetLastError();
 }
 
+int line_segments() { return kSeg; }
+
 cudaError_t launch_lineA(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
-  const long nth = (long)g.B * g.tpmA;
-  const unsigned nb = (unsigned)((nth + kLineT - 1) / kLineT);
+  const unsigned nb = (unsigned)(g.B * (3 * g.ngrp + 1));
   if (g.prec)
     k_lineA<float><<<nb, kLineT, line_smem(g), st>>>(g, bf, rk);
   else
@@ -531,8 +559,7 @@ cudaError_t launch_lineA(const Grid &g, const Bufs &bf, int rk, cudaStream_t st)
 }
 
 cudaError_t launch_lineB(const Grid &g, const Bufs &bf, int mode, cudaStream_t st) {
-  const long nth = (long)g.B * g.tpmB;
-  const unsigned nb = (unsigned)((nth + kLineT - 1) / kLineT);
+  const unsigned nb = (unsigned)(g.B * (2 * g.ngrp + 1));
   if (g.prec)
     k_lineB<float><<<nb, kLineT, line_smem(g), st>>>(g, bf, mode);
   else
