@@ -12,6 +12,9 @@ step (three substeps) of that box.
   roofline  the dominant kernel (plane stage 2), timed alone with CUDA events:
          FP64 rate against the FP64 FMA peak measured in the same run (the
          binding roof on GB300) and bytes against the measured HBM copy peak.
+  newton  batched Newton Jv/s: 32 finite-difference products on 96x48x48
+         (Re_z=1200, T=20/S) as one FP32-mixed batch (central differences)
+         vs one FP64 product at a time.
   cpu_baseline  the C oracle (restatement of the reference step) on the
          host cores, a bounded sample of steps of the same workload.
 
@@ -238,6 +241,56 @@ def ensemble_leg(sb, torch, dist, ws, rank, args, nbox=64, nsteps=200):
             "max_member_rel_l2_err_vs_fp64": err, "re_z_range": [500.0, 2000.0]}
 
 
+def newton_leg(sb, torch, dist, ws, rank, args, nper=32, T=20.0):
+    """Batched Newton Jv: the Jacobian-vector products of the periodic-orbit
+    search on 96x48x48 (Re_z=1200, period T=20/S) through the Newton tools'
+    public API (host vectors in, host vectors out).
+      batched         32 products as one 64-member FP32-mixed batch of central
+                      differences (eps_jacobi=3e-3: FP32 storage does not
+                      resolve the 1e-7 step of the FP64 search)
+      batched_forward 32 forward differences and the base as one 33-member
+                      FP32-mixed batch (eps_jacobi=1e-3)
+      unbatched_fp64  one forward-difference product in FP64 at eps_jacobi=1e-7,
+                      the base integration done beforehand
+    Errors are relative L2 against the FP64 product of the same direction."""
+    from shear_nnf_gb300 import newton as nw
+    pp = dict(mgalx=96, my=48, mgalz=48, Re=1200.0 / LZ ** 2, alp=0.5, Ly=LZ, gam=1.0, s=1.0,
+              chi=0.0, CFL=0.5)
+    p = sb.make_params(**pp)
+    pk = nw.Packing(p, *nw.Packing.reference_scales(p))
+    x0 = pk.pack(sb.seed_state(p, 77 + rank))
+    D = np.random.default_rng(5 + rank).standard_normal((pk.n, nper))
+    pm64 = nw.PeriodMap(p, T, batch=1, chunk=256)
+    J64 = nw.Jacobian(pm64, pk, x0, eps_jacobi=1e-7)  # base integration, untimed
+    steps_T = pm64.last_steps[0]
+    barrier(dist)
+    t0 = time.perf_counter()
+    jv64 = J64.matvec(D[:, :1])
+    t64 = allmax(dist, time.perf_counter() - t0)
+    del pm64, J64
+    out = {"grid": [96, 48, 48], "re_z": 1200.0, "period_T": T,
+           "rk3_steps_per_integration": steps_T, "unknowns": pk.n,
+           "unbatched_fp64": {"value": ws / t64, "unit": "Jv/s", "eps_jacobi": 1e-7,
+                              "seconds": t64}}
+    for key, central, eps, members in (("batched", True, 3e-3, 2 * nper),
+                                       ("batched_forward", False, 1e-3, nper + 1)):
+        pm = nw.PeriodMap(p, T, batch=members, precision=sb.SB_MIXED, chunk=256)
+        J = nw.Jacobian(pm, pk, x0, eps_jacobi=eps, central=central, base_in_batch=not central)
+        barrier(dist)
+        t0 = time.perf_counter()
+        jv = J.matvec(D)
+        t = allmax(dist, time.perf_counter() - t0)
+        out[key] = {"value": ws * nper / t, "unit": "Jv/s", "products_per_batch": nper,
+                    "members": members, "difference": "central" if central else "forward",
+                    "precision": "FP32-mixed", "eps_jacobi": eps, "seconds": t,
+                    "jv_rel_l2_err_vs_fp64": float(np.linalg.norm(jv[:, 0] - jv64[:, 0]) /
+                                                   np.linalg.norm(jv64[:, 0])),
+                    "speedup_vs_unbatched_fp64": (nper / t) * t64}
+        del pm, J
+    out["api"] = "shear_nnf_gb300.newton.Jacobian.matvec (host vectors)"
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -390,6 +443,7 @@ def run_ours(args):
                  "precision": "FP32 storage, transforms, nonlinear product and RK3; FP64 "
                               "compact y-solves, Helmholtz solve, phase factors"}
     ensemble = None if args.no_ensemble else ensemble_leg(sb, torch, dist, ws, rank, args)
+    newton = None if args.no_newton else newton_leg(sb, torch, dist, ws, rank, args)
     if rank != 0:
         return
     cpu = cpu_baseline(args.cpu_steps, os.cpu_count() or 1) if ws == 1 or rank == 0 else None
@@ -420,6 +474,7 @@ def run_ours(args):
         },
         "mixed": mixed,
         "ensemble": ensemble,
+        "newton": newton,
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "clocks": clk,
     }
@@ -437,6 +492,7 @@ def main():
                     help="profiling only: run a different grid (the benchmark is 192)")
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble leg")
+    ap.add_argument("--no-newton", action="store_true", help="skip the batched Newton Jv leg")
     ap.add_argument("--lite", action="store_true",
                     help="profiling only: time the steps, skip e2e / CPU / per-kernel legs")
     args = ap.parse_args()

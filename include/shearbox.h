@@ -45,6 +45,8 @@ typedef struct sb_params {
   double uprim;                /* hre2.dat uprime (used with readflag=0, s=0) */
   int nhist;                   /* UNER statistics every nhist steps */
   double etime, dumptime, dtimag; /* end time, dump time and interval */
+  int keep_laminar;            /* 1: no stop on laminarisation (v_rms/Lz < 1e-5,
+                                  cross.f90:2106-2115); the flag is still set */
 } sb_params;
 
 /* Per-box status after sb_step (cross.f90 istop logic, 1683-1690, 2102-2115) */
@@ -76,6 +78,12 @@ int sb_destroy(sb_handle *h);
 
 /* Per-box Reynolds number (ensembles); default p->Re. */
 int sb_set_member_re(sb_handle *h, int member, double Re);
+
+/* Per-box end time (the etime of running, mod.f90:58): a box stops at it,
+ * with the last step shortened to land on it (cross.f90:1694-1711).  The
+ * Newton/Arnoldi period map integrates every perturbation to time0 + T this way
+ * (calc_dns_disk3d, gmres_shear.f90:2951-3120). */
+int sb_set_member_etime(sb_handle *h, int member, double etime);
 
 /* Copies one box's state in / out (what getfil / escru read and write,
  * readwrite.f90:72-447,1164-1402, minus the file). */

@@ -34,6 +34,7 @@ class SbParams(ctypes.Structure):
         ("CFL", ctypes.c_double), ("vbulk", ctypes.c_double), ("fixed_dt", ctypes.c_double),
         ("readflag", ctypes.c_int), ("uprim", ctypes.c_double), ("nhist", ctypes.c_int),
         ("etime", ctypes.c_double), ("dumptime", ctypes.c_double), ("dtimag", ctypes.c_double),
+        ("keep_laminar", ctypes.c_int),
     ]
 
 
@@ -51,6 +52,7 @@ ABI_FUNCTIONS = [
     "sb_get_status", "sb_get_trace", "sb_cross", "sb_get_stream", "sb_sync", "sb_sizes",
     "sb_seed_state", "sb_compact_coeffs", "sb_last_error", "sb_version", "sb_launch_stage",
     "sb_fp64_peak", "sb_op_derivyc", "sb_op_lapcdy", "sb_op_derivyc_noalloc",
+    "sb_set_member_etime",
 ]
 
 _lib = None
@@ -73,6 +75,7 @@ def lib(auto_build: bool = False):
     L.sb_create.argtypes = [PP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
     L.sb_destroy.argtypes = [vp]
     L.sb_set_member_re.argtypes = [vp, ctypes.c_int, ctypes.c_double]
+    L.sb_set_member_etime.argtypes = [vp, ctypes.c_int, ctypes.c_double]
     L.sb_set_state.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp, ctypes.c_double, ctypes.c_double,
                                ctypes.c_double]
     L.sb_get_state.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp, dp, dp, dp]
@@ -115,9 +118,9 @@ def _dp(a: np.ndarray):
 
 def make_params(mgalx, my, mgalz, Re, alp, Ly, gam, s=1.0, chi=0.0, CFL=0.5, vbulk=0.0,
                 fixed_dt=0.0, readflag=1, uprim=1.0, nhist=1, etime=1e10, dumptime=1e10,
-                dtimag=1e10) -> SbParams:
+                dtimag=1e10, keep_laminar=0) -> SbParams:
     return SbParams(mgalx, my, mgalz, Re, alp, Ly, gam, s, chi, CFL, vbulk, fixed_dt, readflag,
-                    uprim, nhist, etime, dumptime, dtimag)
+                    uprim, nhist, etime, dumptime, dtimag, keep_laminar)
 
 
 def sizes(p: SbParams) -> dict:
@@ -177,6 +180,9 @@ class ShearBox:
 
     def set_re(self, member: int, Re: float):
         _check(lib().sb_set_member_re(self.h, member, float(Re)))
+
+    def set_etime(self, member: int, etime: float):
+        _check(lib().sb_set_member_etime(self.h, member, float(etime)))
 
     def set_state(self, state: dict, member: int = 0):
         vor = np.ascontiguousarray(state["vor"], np.complex128)

@@ -129,6 +129,7 @@ static void member_defaults(const sb_params *p, const Grid &g, double Re, Member
   m->dtimag = p->dtimag > 0 ? p->dtimag : m->etime;
   m->readflag = p->readflag;
   m->nhist = p->nhist > 0 ? p->nhist : 1;
+  m->keep_laminar = p->keep_laminar;
 }
 
 static int capture_step(sb_handle *h) {
@@ -497,6 +498,15 @@ int sb_set_member_re(sb_handle *h, int member, double Re) {
   CK(cudaMemcpy((char *)d + offsetof(Member, Re), &m.Re, sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy((char *)d + offsetof(Member, nu), &m.nu, sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy((char *)d + offsetof(Member, cflvv), &m.cflvv, sizeof(double), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int sb_set_member_etime(sb_handle *h, int member, double etime) {
+  if (!h || member < 0 || member >= h->g.B) return fail(1, "bad handle or member");
+  if (!(etime > 0)) return fail(1, "etime must be positive");
+  h->mem_init[member].etime = etime;
+  CK(cudaMemcpy((char *)(h->bf.mem + member) + offsetof(Member, etime), &etime, sizeof(double),
+                cudaMemcpyHostToDevice));
   return 0;
 }
 

@@ -63,7 +63,7 @@ struct Member {
   // parameters
   double Re, nu, CFL, cflx, cfly, cflz, cflvv, vbulk, fixed_dt, uprim;
   double etime, dumptime, dtimag;
-  int readflag, nhist;
+  int readflag, nhist, keep_laminar;
   // state scalars
   double time, xoffb, xofft;
   double xwb[4], xwt[4];      // image offsets: [0] at the step start, [rk] after substep rk

@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
         M.flags |= SBF_NAN;
       }
       if (uner[1] / (2.0 * g.pi / g.gam) < 1e-5) {
-        M.istop = 1;
+        if (!M.keep_laminar) M.istop = 1;
         M.flags |= SBF_LAMINAR;
       }
       M.ihist = 0;

@@ -1,0 +1,345 @@
+"""Newton-Krylov and Arnoldi tools over batched period maps of the shearing box.
+
+Host side of the reference's periodic-orbit search and Floquet analysis, whose
+cost is the Jacobian-vector product: each product is one integration of the
+box over the period T (matvec_dns_disk3d, gmres_shear.f90:2666-2948, through
+calc_dns_disk3d, 2951-3120).  Here every Krylov block of products is one
+batched integration on the GPU: the base state and all its perturbations are
+members of one ShearBox batch, advanced together by the graph-captured RK3
+step.  The vectors are packed as the reference's `throwing`
+(gmres_shear.f90:2229-2426, iuse_fou_mode=2); inner products, Gram-Schmidt and
+the small Hessenberg problems are FP64 on the host (numpy), a few hundred
+kilobytes per vector.
+
+Pieces:
+  Packing       state <-> unknown vector (throwing / backthrowing)
+  PeriodMap     x -> Phi_T(x) for a batch of states (calc_dns_disk3d)
+  Jacobian      forward-difference Jv with the Dennis-Schnabel step
+                (matvec_dns_disk3d, iopt_matvec=1, iuse_hej=1), optional x/z
+                phase shift (phase_shift_fou, operators.f90:488-544)
+  arnoldi       (block) Arnoldi with modified Gram-Schmidt (arnoldi_shear.f90:
+                222-330) -> Floquet multipliers and exponents log(lambda)/T
+                (arnoldi_shear.f90:371-406)
+  gmres         (block) GMRES for J dx = r (gmres_k_shear, gmres_shear.f90:
+                1905-2207), least squares on the block Hessenberg
+  Residual      F(x) = shift(Phi_T(x)) - x (- rhs) from an FP64 period map
+  newton        Newton iteration for shift(Phi_T(x)) - x = 0 at fixed T and
+                shifts (newton_shear.f90:183-597 without the period/shift
+                unknowns and the hookstep)
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import SB_FP64, ShearBox, sizes
+
+
+class Packing:
+    """Unknown vector of a state, in the order of `throwing` with
+    iuse_fou_mode=2: u00/sca_u (my), w00/sca_u (my), then for every y plane j,
+    kz index k and real index q over kx (re, im interleaved): omega_y/sca_g and
+    phi/sca_p of that entry, skipping the (0,0) mode and the kx=0 entries with
+    negative kz (the conjugates of the positive ones; gmres_shear.f90:2356-2362).
+    The second field is phi = lap(v) where the reference throws v (iuse_v=1,
+    gmres_shear.f90:51): the two differ by a fixed invertible operator per
+    mode, so the roots of F and the Floquet multipliers are the same.
+    reference_scales() gives the scalings of gmres_shear.f90:411-413."""
+
+    def __init__(self, p, sca_u=1.0, sca_g=1.0, sca_p=1.0):
+        sz = sizes(p)
+        self.my, self.nkx, self.mz, self.nz = p.my, sz["nkx"], sz["mz"], sz["nz"]
+        self.sca = (sca_u, sca_g, sca_p)
+        mask = np.ones((self.mz, 2 * self.nkx), bool)
+        mask[0, 0:2] = False
+        mask[self.nz + 1:, 0:2] = False
+        self.mask = mask
+        self.nsel = int(mask.sum())
+        self.n = 2 * self.my + self.my * self.nsel * 2
+
+    @staticmethod
+    def reference_scales(p) -> tuple:
+        lz = 2 * np.pi / p.gam
+        return (p.s * lz, p.s, p.s * lz)
+
+    def _plane_real(self, f):
+        # pencil complex (mz, nkx, my) -> plane real (my, mz, 2 nkx)
+        return np.ascontiguousarray(np.transpose(f, (2, 0, 1))).view(np.float64)
+
+    def pack(self, st: dict) -> np.ndarray:
+        su, sg, sp = self.sca
+        V = self._plane_real(st["vor"])[:, self.mask] / sg
+        P = self._plane_real(st["phi"])[:, self.mask] / sp
+        body = np.stack([V, P], axis=-1).reshape(-1)
+        return np.concatenate([st["u00"] / su, st["w00"] / su, body])
+
+    def unpack(self, x: np.ndarray, time=0.0, xoffb=0.0, xofft=0.0) -> dict:
+        su, sg, sp = self.sca
+        my, nkx, mz, nz = self.my, self.nkx, self.mz, self.nz
+        u00 = x[:my] * su
+        w00 = x[my:2 * my] * su
+        body = x[2 * my:].reshape(my, self.nsel, 2)
+        fields = []
+        for c, sca in ((0, sg), (1, sp)):
+            pl = np.zeros((my, mz, 2 * nkx))
+            pl[:, self.mask] = body[:, :, c] * sca
+            cp = pl.view(np.complex128)  # (my, mz, nkx)
+            for k in range(nz + 1, mz):  # conjugate symmetry of kx = 0
+                cp[:, k, 0] = np.conj(cp[:, mz - k, 0])
+            fields.append(np.ascontiguousarray(np.transpose(cp, (1, 2, 0))))
+        return {"vor": fields[0], "phi": fields[1], "u00": u00.copy(), "w00": w00.copy(),
+                "time": time, "xoffb": xoffb, "xofft": xofft}
+
+
+def phase_shift(st: dict, p, shiftx: float, shiftz: float) -> dict:
+    """phase_shift_fou (operators.f90:488-544): multiply each (kx, kz) mode by
+    exp(-i kx shiftx) exp(-i kz shiftz)."""
+    if shiftx == 0.0 and shiftz == 0.0:
+        return st
+    sz = sizes(p)
+    nkx, mz, nz = sz["nkx"], sz["mz"], sz["nz"]
+    kx = p.alp * np.arange(nkx)
+    kz = p.gam * np.array([k if k <= nz else k - mz for k in range(mz)], float)
+    f = np.exp(-1j * kx[None, :] * shiftx) * np.exp(-1j * kz[:, None] * shiftz)
+    out = dict(st)
+    out["vor"] = st["vor"] * f[:, :, None]
+    out["phi"] = st["phi"] * f[:, :, None]
+    return out
+
+
+class PeriodMap:
+    """x -> Phi_T(x): states integrated from their own time to time + T, all
+    members of one batch advanced together (calc_dns_disk3d).  Each member
+    stops on its own end time (the clipped last step of cross.f90:1694-1711);
+    the batch is stepped in chunks until every member has reached it."""
+
+    def __init__(self, p, T: float, batch: int, precision: int = SB_FP64, chunk: int = 64):
+        self.p, self.T, self.batch, self.chunk = p, float(T), int(batch), int(chunk)
+        self.box = ShearBox(p, batch=self.batch, precision=precision)
+        self.integrations = 0
+        self.steps = 0  # RK3 steps summed over the integrated states
+        self.last_steps = []
+
+    def __call__(self, states: list) -> list:
+        assert 1 <= len(states) <= self.batch
+        box = self.box
+        full = list(states) + [states[0]] * (self.batch - len(states))
+        for m, st in enumerate(full):
+            box.set_state(st, m)
+            box.set_etime(m, st["time"] + self.T)
+        steps = [0] * len(states)
+        fin = [False] * len(states)
+        for _ in range(1 << 20):
+            # a member already at its end time takes zero-length steps
+            box.step(self.chunk)
+            for m in range(len(states)):
+                if fin[m]:
+                    continue
+                s = box.status(m)
+                if s.flags & 3 or (s.flags & 4 and not self.p.keep_laminar):
+                    raise RuntimeError(f"period map: member {m} stopped (flags {s.flags})")
+                steps[m] += s.steps_done
+                fin[m] = bool(s.flags & 8)
+            if all(fin):
+                break
+        self.last_steps = steps
+        self.steps += sum(steps)
+        self.integrations += len(states)
+        return [box.get_state(m) for m in range(len(states))]
+
+
+class Jacobian:
+    """Finite-difference products J d of the shifted period map
+    G(x) = pack(shift(Phi_T(unpack(x)))) at x0 (matvec_dns_disk3d,
+    gmres_shear.f90:2666-2948): eps = eps_jacobi |x0| / |d| (gmres_shear.f90:1380,
+    2699), the representable step h = (x0 + eps d) - x0 (iuse_hej=1),
+    J d = (G(x0 + h) - G(x0)) / eps, or (G(x0 + h) - G(x0 - h)) / (2 eps) with
+    central=True (iopt_matvec=2).  Products are evaluated a block at a time:
+    one batched integration per block of PeriodMap.batch states.
+
+    base_in_batch=True integrates x0 again as the first member of every block
+    and differences against that copy, so that the base and the perturbed
+    states see the same arithmetic (FP32-mixed boxes)."""
+
+    def __init__(self, pmap: PeriodMap, packing: Packing, x0: np.ndarray, time0=0.0,
+                 xoff0=(0.0, 0.0), shiftx=0.0, shiftz=0.0, eps_jacobi=1e-6, central=False,
+                 base_in_batch=False):
+        self.pmap, self.pk, self.x0 = pmap, packing, np.asarray(x0, float)
+        self.time0, self.xoff0, self.shift = time0, tuple(xoff0), (shiftx, shiftz)
+        self.eps_jacobi, self.central, self.base_in_batch = eps_jacobi, central, base_in_batch
+        self.products = 0
+        self.gx0 = None if base_in_batch else self.G([self.x0])[0]
+
+    def G(self, xs: list) -> list:
+        states = [self.pk.unpack(x, self.time0, *self.xoff0) for x in xs]
+        out = []
+        for q in range(0, len(states), self.pmap.batch):
+            out += self.pmap(states[q:q + self.pmap.batch])
+        return [self.pk.pack(phase_shift(s, self.pmap.p, *self.shift)) for s in out]
+
+    @property
+    def block(self) -> int:
+        """Products per batched integration."""
+        per = 2 if self.central else 1
+        return (self.pmap.batch - (1 if self.base_in_batch else 0)) // per
+
+    def matvec(self, D: np.ndarray) -> np.ndarray:
+        D = np.asarray(D, float)
+        D = D[:, None] if D.ndim == 1 else D
+        nb = self.block
+        if nb < 1:
+            raise ValueError("matvec: batch too small for one product")
+        return np.concatenate([self._matvec_block(D[:, q:q + nb])
+                               for q in range(0, D.shape[1], nb)], axis=1)
+
+    def _matvec_block(self, D: np.ndarray) -> np.ndarray:
+        xn = np.linalg.norm(self.x0)
+        eps_j = self.eps_jacobi * (xn if xn > 0 else 1.0)
+        xs, eps = ([self.x0] if self.base_in_batch else []), []
+        for q in range(D.shape[1]):
+            dn = np.linalg.norm(D[:, q])
+            if dn == 0:
+                raise ValueError("matvec: zero direction")
+            e = eps_j / dn
+            xs.append(self.x0 + ((self.x0 + e * D[:, q]) - self.x0))
+            if self.central:
+                xs.append(self.x0 + ((self.x0 - e * D[:, q]) - self.x0))
+            eps.append(e)
+        gs = self.G(xs)
+        if self.base_in_batch:
+            g0, gs = gs[0], gs[1:]
+        else:
+            g0 = self.gx0
+        self.products += D.shape[1]
+        if self.central:
+            cols = [(gs[2 * q] - gs[2 * q + 1]) / (2 * eps[q]) for q in range(D.shape[1])]
+        else:
+            cols = [(gs[q] - g0) / eps[q] for q in range(D.shape[1])]
+        return np.stack(cols, axis=1)
+
+
+class Residual:
+    """F(x) = shift(Phi_T(x)) - x - rhs with an FP64 period map (the Newton
+    residual of newton_shear.f90:183-300; rhs = 0 there, a manufactured target
+    otherwise)."""
+
+    def __init__(self, pmap: PeriodMap, packing: Packing, time0=0.0, xoff0=(0.0, 0.0),
+                 shiftx=0.0, shiftz=0.0, rhs=None):
+        self.pmap, self.pk = pmap, packing
+        self.time0, self.xoff0, self.shift, self.rhs = time0, tuple(xoff0), (shiftx, shiftz), rhs
+
+    def G(self, x: np.ndarray) -> np.ndarray:
+        st = self.pmap([self.pk.unpack(x, self.time0, *self.xoff0)])[0]
+        return self.pk.pack(phase_shift(st, self.pmap.p, *self.shift))
+
+    def __call__(self, x: np.ndarray) -> np.ndarray:
+        F = self.G(x) - x
+        return F if self.rhs is None else F - self.rhs
+
+
+def _orthonormalize(W: np.ndarray, V: list, Hcol: list):
+    """Modified Gram-Schmidt of the block W against the blocks of V (twice, for
+    robustness), then a QR of the remainder; returns (Q, R) and appends the
+    projections to Hcol."""
+    for _ in range(2):
+        for i, Vi in enumerate(V):
+            c = Vi.T @ W
+            W = W - Vi @ c
+            if len(Hcol) <= i:
+                Hcol.append(c)
+            else:
+                Hcol[i] = Hcol[i] + c
+    return np.linalg.qr(W)
+
+
+def arnoldi(matvec, n: int, k: int, block: int = 1, seed: int = 0, start=None):
+    """Block Arnoldi: k iterations of blocks of `block` products.  Returns the
+    Ritz values (largest modulus first), their residual estimates
+    |H_{k+1,k} y_k| (unit Ritz vectors y), the block Hessenberg matrix and the
+    basis.  block=1 is the reference's Arnoldi with modified Gram-Schmidt
+    (arnoldi_shear.f90:222-330)."""
+    rng = np.random.default_rng(seed)
+    Q0 = rng.standard_normal((n, block)) if start is None else np.asarray(start, float).reshape(n, -1)
+    Q, _ = np.linalg.qr(Q0)
+    V = [Q]
+    p = Q.shape[1]
+    H = np.zeros(((k + 1) * p, k * p))
+    for it in range(k):
+        W = matvec(V[-1])
+        cols = []
+        Qn, R = _orthonormalize(W, V, cols)
+        for i, c in enumerate(cols):
+            H[i * p:(i + 1) * p, it * p:(it + 1) * p] = c
+        H[(it + 1) * p:(it + 2) * p, it * p:(it + 1) * p] = R
+        V.append(Qn)
+    Hk = H[: k * p, : k * p]
+    lam, Y = np.linalg.eig(Hk)
+    Y = Y / np.linalg.norm(Y, axis=0)
+    res = np.linalg.norm(H[k * p:, (k - 1) * p:k * p] @ Y[(k - 1) * p:, :], axis=0)
+    order = np.argsort(-np.abs(lam))
+    return lam[order], res[order], H, V
+
+
+def floquet_exponents(lam: np.ndarray, T: float) -> np.ndarray:
+    """sigma = log(lambda) / T (arnoldi_shear.f90:403-406)."""
+    return np.log(lam.astype(complex)) / T
+
+
+def gmres(matvec, b: np.ndarray, k: int, block: int = 1, tol: float = 0.0, seed: int = 0):
+    """(Block) GMRES for J x = b from x = 0: the first basis vector is b/|b|;
+    with block > 1 the other columns of the starting block are random, so every
+    iteration applies J to `block` vectors in one batched integration and the
+    solution is minimised over a larger space.  Returns (x, residual norms)."""
+    n = b.size
+    beta = np.linalg.norm(b)
+    if beta == 0:
+        return np.zeros(n), [0.0]
+    rng = np.random.default_rng(seed)
+    Q0 = np.concatenate([b[:, None], rng.standard_normal((n, block - 1))], axis=1)
+    Q, R0 = np.linalg.qr(Q0)
+    V = [Q]
+    p = Q.shape[1]
+    H = np.zeros(((k + 1) * p, k * p))
+    rhs0 = np.zeros((k + 1) * p)
+    rhs0[:p] = R0[:, 0]
+    res = [beta]
+    x = np.zeros(n)
+    for it in range(k):
+        W = matvec(V[-1])
+        cols = []
+        Qn, R = _orthonormalize(W, V, cols)
+        for i, c in enumerate(cols):
+            H[i * p:(i + 1) * p, it * p:(it + 1) * p] = c
+        H[(it + 1) * p:(it + 2) * p, it * p:(it + 1) * p] = R
+        V.append(Qn)
+        m = (it + 1) * p
+        Hm = H[: m + p, :m]
+        y, *_ = np.linalg.lstsq(Hm, rhs0[: m + p], rcond=None)
+        r = np.linalg.norm(rhs0[: m + p] - Hm @ y)
+        res.append(r)
+        Vm = np.concatenate(V[: it + 1], axis=1)
+        x = Vm @ y
+        if r <= tol * beta:
+            break
+    return x, res
+
+
+def newton(x0: np.ndarray, residual, jac_factory, k: int = 20, block: int = 1, itmax: int = 10,
+           tol: float = 1e-10, gmres_tol: float = 1e-3):
+    """Newton iteration for F(x) = 0 with F(x) = G(x) - x (- b): residual(x)
+    returns F(x) (FP64 integration); jac_factory(x) returns a Jacobian of G at x,
+    whose products may come from FP32-mixed integrations: each step solves
+    (J - I) dx = -F with GMRES to gmres_tol and the FP64 residual of the next
+    iterate corrects what the approximate Jacobian missed (iterative
+    refinement).  Returns (x, history of |F|/|x|)."""
+    x = np.asarray(x0, float).copy()
+    hist = []
+    for _ in range(itmax + 1):
+        F = residual(x)
+        rel = np.linalg.norm(F) / max(np.linalg.norm(x), 1e-300)
+        hist.append(rel)
+        if rel <= tol or len(hist) > itmax:
+            break
+        J = jac_factory(x)
+        dx, _ = gmres(lambda D: J.matvec(D) - D, -F, k, block=block, tol=gmres_tol)
+        x = x + dx
+    return x, hist

@@ -1,0 +1,204 @@
+"""Newton-Krylov / Arnoldi tools over batched period maps: packing, Krylov
+algebra (CPU), and on the GPU the Floquet multipliers of the Stokes problem
+(known answer), Jv against the oracle, batched against unbatched products, and
+Newton with FP32-mixed Jv products and an FP64 residual."""
+import numpy as np
+import pytest
+
+from conftest import box_params, rel_l2
+
+import shear_nnf_gb300 as sb
+from shear_nnf_gb300 import newton as nw
+
+
+def _params(**kw):
+    return sb.make_params(**box_params(64, 32, 32, 1000.0, **kw))
+
+
+def test_packing_roundtrip():
+    p = _params()
+    pk = nw.Packing(p, *nw.Packing.reference_scales(p))
+    st = sb.seed_state(p, 11)
+    x = pk.pack(st)
+    assert x.size == pk.n
+    back = pk.unpack(x)
+    # the (0,0) modes of vor/phi are not unknowns
+    for key in ("vor", "phi"):
+        a = st[key].copy()
+        a[0, 0, :] = 0
+        assert rel_l2(back[key], a) < 1e-15
+    assert rel_l2(back["u00"], st["u00"]) < 1e-15 and rel_l2(back["w00"], st["w00"]) < 1e-15
+    assert np.isclose(np.linalg.norm(pk.pack(back)), np.linalg.norm(x))
+
+
+def test_phase_shift_full_period():
+    p = _params()
+    st = sb.seed_state(p, 2)
+    lx, lz = 2 * np.pi / p.alp, 2 * np.pi / p.gam
+    a = nw.phase_shift(st, p, lx, lz)
+    assert rel_l2(a["vor"], st["vor"]) < 1e-13 and rel_l2(a["phi"], st["phi"]) < 1e-13
+    b = nw.phase_shift(nw.phase_shift(st, p, 0.3, -0.2), p, -0.3, 0.2)
+    assert rel_l2(b["vor"], st["vor"]) < 1e-14
+
+
+def _test_matrix(n, top, seed=1):
+    rng = np.random.default_rng(seed)
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    ev = np.concatenate([top, 0.3 * rng.random(n - len(top))])
+    return Q @ np.diag(ev) @ Q.T
+
+
+@pytest.mark.parametrize("block", [1, 4])
+def test_arnoldi_matrix(block):
+    top = [1.0, 0.9, 0.8, 0.7, 0.6]
+    A = _test_matrix(200, top)
+    lam, res, _, _ = nw.arnoldi(lambda D: A @ D, 200, 40 // block, block=block)
+    assert np.allclose(lam[:5].real, top, atol=1e-6)
+    assert np.all(res[:3] < 1e-5)
+    sig = nw.floquet_exponents(lam[:2], 2.0)
+    assert np.isclose(sig[0].real, 0.0, atol=1e-6)
+
+
+@pytest.mark.parametrize("block", [1, 4])
+def test_gmres_matrix(block):
+    A = _test_matrix(200, [1.5, 0.9, 0.8, 0.7, 0.6])
+    M = A - np.eye(200)
+    b = np.random.default_rng(3).standard_normal(200)
+    x, res = nw.gmres(lambda D: M @ D, b, 60 // block, block=block, tol=1e-10)
+    assert res[-1] <= 1e-10 * res[0]
+    assert np.linalg.norm(M @ x - b) <= 1e-9 * np.linalg.norm(b)
+
+
+def test_newton_linear_map():
+    # F(x) = A x - x - r has the root (A - I)^-1 (-r); an inexact Jacobian
+    # (A perturbed by 1e-3) still converges through the exact residual
+    A = _test_matrix(120, [1.5, 0.9, 0.8], seed=4)
+    r = np.random.default_rng(5).standard_normal(120)
+
+    class J:
+        def __init__(self, x):
+            self.A = A + 1e-3 * np.random.default_rng(6).standard_normal(A.shape) / 11
+
+        def matvec(self, D):
+            return self.A @ D
+
+    x, hist = nw.newton(np.zeros(120) + 1.0, lambda x: A @ x - x - r, J, k=60, itmax=20,
+                        tol=1e-12, gmres_tol=1e-6)
+    assert hist[-1] <= 1e-12
+    assert np.allclose(x, np.linalg.solve(A - np.eye(120), r), rtol=1e-9, atol=1e-10)
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+
+def _stokes_multipliers(p, nu, dt, nsteps):
+    """Multipliers of the linearised map at rest without shear: every Fourier
+    mode decays under explicit RK3 with amplification 1 + z + z^2/2 + z^3/6,
+    z = nu dt (lambda_y - kx^2 - kz^2), lambda_y the modified wavenumber of the
+    compact second-derivative scheme."""
+    sz = sb.sizes(p)
+    nkx, mz, nz, my = sz["nkx"], sz["mz"], sz["nz"], p.my
+    pr1, rh1, pr2, rh2 = sb.compact_coeffs()
+    h = p.Ly / my
+    d = np.arange(-3, 4)
+    ky = 2 * np.pi * np.arange(my) / p.Ly
+    num = (rh2[None, :] * np.cos(ky[:, None] * d[None, :] * h)).sum(1)
+    den = (pr2[None, :] * np.cos(ky[:, None] * d[None, :] * h)).sum(1)
+    lam_y = num / den / h ** 2
+    kx2 = (p.alp * np.arange(nkx)) ** 2
+    kz2 = (p.gam * np.array([k if k <= nz else k - mz for k in range(mz)], float)) ** 2
+    k2 = (kx2[None, :, None] + kz2[:, None, None]) - lam_y[None, None, :]
+    z = -nu * dt * k2
+    g = (1 + z + z * z / 2 + z ** 3 / 6) ** nsteps
+    assert np.all(np.abs(1 + z + z * z / 2 + z ** 3 / 6) <= 1)
+    return np.unique(np.round(g.ravel(), 13))[::-1]
+
+
+@pytest.mark.gpu
+def test_floquet_stokes_known_answer():
+    nu, dt, nsteps = 0.1, 0.01, 200
+    p = sb.make_params(64, 32, 32, 1.0 / nu, 0.7, 5.0, 1.3, s=0.0, chi=0.0, CFL=0.5,
+                       fixed_dt=dt, keep_laminar=1)
+    pk = nw.Packing(p)
+    pmap = nw.PeriodMap(p, nsteps * dt, batch=2)
+    J = nw.Jacobian(pmap, pk, np.zeros(pk.n), central=True, eps_jacobi=1e-6)
+    # 25 iterations: the multiplier 1 is double (mean u00 and w00), and longer
+    # runs split it into a pair of Ritz values with a larger residual
+    lam, res, _, _ = nw.arnoldi(J.matvec, pk.n, 25, seed=7)
+    theory = _stokes_multipliers(p, nu, dt, nsteps)
+    assert pmap.last_steps == [nsteps, nsteps]
+    for q, tol in enumerate((1e-9, 1e-9, 1e-6, 1e-6)):
+        assert abs(lam[q].imag) < 1e-10, (q, lam[:6], res[:6])
+        assert abs(lam[q].real - theory[q]) < tol * theory[q], (q, lam[:6], res[:6], theory[:6])
+    assert res[0] < 1e-10 and res[1] < 1e-9
+    sig = nw.floquet_exponents(lam[:4], nsteps * dt)
+    assert np.isclose(sig[0].real, 0.0, atol=1e-9)
+
+
+def _seeded_x(p, pk, seed, scale=1.0):
+    return scale * pk.pack(sb.seed_state(p, seed))
+
+
+@pytest.mark.gpu
+def test_jv_matches_oracle():
+    import oracle
+    kw = box_params(64, 32, 32, 1000.0)
+    p = sb.make_params(**kw)
+    T = 0.1
+    pk = nw.Packing(p, *nw.Packing.reference_scales(p))
+    x0 = _seeded_x(p, pk, 5)
+    d = np.random.default_rng(8).standard_normal(pk.n)
+    pmap = nw.PeriodMap(p, T, batch=1)
+    J = nw.Jacobian(pmap, pk, x0, eps_jacobi=1e-5)
+    jv = J.matvec(d)[:, 0]
+
+    def g_oracle(x):
+        orc = oracle.Oracle(**kw, etime=T)
+        st = pk.unpack(x)
+        orc.cross(st, 100000)
+        assert abs(st["time"] - T) < 1e-12
+        return pk.pack(st)
+
+    eps = 1e-5 * np.linalg.norm(x0) / np.linalg.norm(d)
+    xp = x0 + ((x0 + eps * d) - x0)
+    jv_o = (g_oracle(xp) - g_oracle(x0)) / eps
+    assert rel_l2(jv, jv_o) < 1e-6
+    assert pmap.steps > 2
+
+
+@pytest.mark.gpu
+def test_batched_products_equal_unbatched():
+    p = _params()
+    pk = nw.Packing(p, *nw.Packing.reference_scales(p))
+    x0 = _seeded_x(p, pk, 9)
+    D = np.random.default_rng(10).standard_normal((pk.n, 4))
+    one = nw.Jacobian(nw.PeriodMap(p, 0.05, batch=1), pk, x0)
+    four = nw.Jacobian(nw.PeriodMap(p, 0.05, batch=4), pk, x0)
+    a = one.matvec(D)
+    b = four.matvec(D)
+    assert four.pmap.integrations == 4 + 1 and one.pmap.integrations == 4 + 1
+    assert rel_l2(b, a) < 1e-12
+
+
+@pytest.mark.gpu
+def test_newton_fp32_jv_fp64_residual():
+    # manufactured root: F(x) = G(x) - x - (G(x*) - x*) vanishes at x*; products
+    # from an FP32-mixed batch (base in the batch), residual in FP64
+    p = _params()
+    T = 10.0
+    pk = nw.Packing(p, *nw.Packing.reference_scales(p))
+    xs = _seeded_x(p, pk, 12)
+    res64 = nw.Residual(nw.PeriodMap(p, T, batch=1), pk)
+    rhs = res64(xs)
+    res64.rhs = rhs
+    assert np.linalg.norm(res64(xs)) == 0.0
+    pm32 = nw.PeriodMap(p, T, batch=9, precision=sb.SB_MIXED)
+    x0 = xs + 1e-3 * np.linalg.norm(xs) / np.sqrt(pk.n) * \
+        np.random.default_rng(13).standard_normal(pk.n)
+
+    def jac(x):
+        return nw.Jacobian(pm32, pk, x, eps_jacobi=1e-3, base_in_batch=True)
+
+    x, hist = nw.newton(x0, res64, jac, k=16, block=8, itmax=12, tol=1e-10, gmres_tol=1e-4)
+    assert hist[-1] <= 1e-10, hist
