@@ -100,11 +100,17 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
         except OSError:
             self.proc = None
+            return
+        # the timed region starts once sampling runs
+        t0 = time.time()
+        while not self.rows and time.time() - t0 < 3.0 and self.proc.poll() is None:
+            time.sleep(0.01)
+        self.rows.clear()
 
     def _read(self):
         for line in self.proc.stdout:
