@@ -45,6 +45,8 @@ class OrcParams(ctypes.Structure):
         ("CFL", ctypes.c_double), ("vbulk", ctypes.c_double), ("fixed_dt", ctypes.c_double),
         ("readflag", ctypes.c_int), ("uprim", ctypes.c_double), ("nhist", ctypes.c_int),
         ("etime", ctypes.c_double), ("dumptime", ctypes.c_double), ("dtimag", ctypes.c_double),
+        ("keep_laminar", ctypes.c_int), ("les", ctypes.c_int), ("les_visc", ctypes.c_int),
+        ("cs", ctypes.c_double),
     ]
 
 
@@ -96,9 +98,11 @@ class Oracle:
 
     def __init__(self, mgalx, my, mgalz, Re, alp, Ly, gam, s=1.0, chi=0.0, CFL=0.5,
                  vbulk=0.0, fixed_dt=0.0, readflag=1, uprim=1.0, nhist=1,
-                 etime=1e10, dumptime=1e10, dtimag=1e10):
+                 etime=1e10, dumptime=1e10, dtimag=1e10, keep_laminar=0, les=0, les_visc=1,
+                 cs=0.1):
         self.p = OrcParams(mgalx, my, mgalz, Re, alp, Ly, gam, s, chi, CFL, vbulk, fixed_dt,
-                           readflag, uprim, nhist, etime, dumptime, dtimag)
+                           readflag, uprim, nhist, etime, dumptime, dtimag, keep_laminar, les,
+                           les_visc, cs)
         self.h = lib().orc_create(ctypes.byref(self.p))
         sz = (ctypes.c_int * 8)()
         lib().orc_sizes(self.h, sz)

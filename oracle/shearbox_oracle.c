@@ -173,6 +173,10 @@ typedef struct { /* per-thread plane buffers for hvhg */
   cplx *u1c, *u2c, *u3c, *o1c, *o2c, *o3c;
   double *u1r, *u2r, *u3r, *o1r, *o2r, *o3r;
   cplx *wz, *col, *row, *work;
+  /* LES block (cross.f90:1291-1406): six gradient spectra / physical planes,
+   * Sij2, its spectrum wyc, nuSGS */
+  cplx *lc[6], *wyc;
+  double *lr[6], *sij2, *nus;
 } pthread_buf;
 
 typedef struct {
@@ -190,6 +194,9 @@ typedef struct {
   int nthr;
   ythread *yt;
   pthread_buf *pt;
+  double Deltag;  /* LES grid-filter width (dx*dy*dz)^(1/3), initcr.f90:510 */
+  double max_nut; /* LES running maximum of |nuSGS| (module LES; cross.f90:1433
+                   * never resets it, so it spans every call on this context) */
 } ctx;
 
 #define A7(a, d) ((a)[(d) + 3])
@@ -816,6 +823,8 @@ void *orc_create(const orc_params *p) {
   c->dz = c->pi2 / gam / (double)mz;
   c->dy = p->Ly / (double)my;
   for (int j = 0; j < my; j++) c->y[j] = (double)j * c->dy - 0.5 * p->Ly;
+  c->Deltag = pow(c->dx * c->dy * c->dz, 1.0 / 3.0);
+  c->max_nut = 0.0;
   c->cflx = c->pi / CFL / c->dx;
   c->cflz = c->pi / CFL / c->dz;
   c->cfly = 2.5 / CFL / c->dy;
@@ -852,6 +861,15 @@ void *orc_create(const orc_params *p) {
     b->u1r = dalloc(nr); b->u2r = dalloc(nr); b->u3r = dalloc(nr);
     b->o1r = dalloc(nr); b->o2r = dalloc(nr); b->o3r = dalloc(nr);
     b->wz = zalloc((size_t)c->mgalz * nkx);
+    if (p->les) {
+      for (int f = 0; f < 6; f++) {
+        b->lc[f] = zalloc(np);
+        b->lr[f] = dalloc(nr);
+      }
+      b->wyc = zalloc(np);
+      b->sij2 = dalloc(nr);
+      b->nus = dalloc(nr);
+    }
     int mm = c->mgalx > c->mgalz ? c->mgalx : c->mgalz;
     b->col = zalloc(mm);
     b->row = zalloc(mm);
@@ -869,6 +887,11 @@ void orc_destroy(void *h) {
     free(b->u1c); free(b->u2c); free(b->u3c); free(b->o1c); free(b->o2c); free(b->o3c);
     free(b->u1r); free(b->u2r); free(b->u3r); free(b->o1r); free(b->o2r); free(b->o3r);
     free(b->wz); free(b->col); free(b->row); free(b->work);
+    for (int f = 0; f < 6; f++) {
+      free(b->lc[f]);
+      free(b->lr[f]);
+    }
+    free(b->wyc); free(b->sij2); free(b->nus);
   }
   free(c->yt);
   free(c->pt);
@@ -981,13 +1004,15 @@ void orc_fourxz(void *h, double *fou, double *phys, int iopt) {
 typedef struct {
   double ener[10], ener2[4];
   double umaxl[4];
+  double numax; /* LES: max |nuSGS| of the plane (cross.f90:1433) */
 } plane_red;
 
 /* per-line complex pointer into a pencil array: line (i,k) */
 #define PEN(a, i, k) ((a) + 2 * (size_t)my * ((size_t)(k) * (size_t)nkx + (size_t)(i)))
 
 /* hist, flag 'f' (cross.f90:1796-1963): intensities, Pk, eps for plane j */
-static void hist_f(ctx *c, pthread_buf *b, const cplx *dv, double *ener, double *ener2) {
+static void hist_f(ctx *c, pthread_buf *b, const cplx *dv, double *ener, double *ener2,
+                   double txy00j) {
   int nkx = c->nkx, mz = c->mz;
   double s = c->p.s;
   cplx *u1c = b->u1c, *u2c = b->u2c, *u3c = b->u3c, *o1c = b->o1c, *o2c = b->o2c,
@@ -1026,9 +1051,25 @@ static void hist_f(ctx *c, pthread_buf *b, const cplx *dv, double *ener, double 
   ener[6] += o1p; ener[7] += o2p; ener[8] += o3p;
   /* add shear effect (iadd_mode = 2,3,5) */
   cplx o3_00 = C(o3c[0].re - s, o3c[0].im);
-  double Pk = -(o3_00.re) * (-uvr) + (o3_00.re * o3_00.re - o3_00.im * o3_00.im) * (1.0 / c->p.Re);
-  ener2[0] += Pk;
-  ener2[1] += o12p;
+  double Pk;
+  if (c->p.les) {
+    /* cross.f90:1886-1899 (rev.1628 form) */
+    double nufac = c->p.les_visc ? (1.0 / c->p.Re) : 0.0;
+    int n = c->mgalx, ld = c->mgalx + 2;
+    double nuty = 0.0;
+    for (int z = 0; z < c->mgalz; z++)
+      for (int x = 0; x < n; x++) nuty += b->nus[z * ld + x];
+    nuty = nuty / (double)(c->mgalx * c->mgalz);
+    Pk = -(o3_00.re * (-uvr + txy00j)) +
+         nufac * (o3_00.re * o3_00.re - o3_00.im * o3_00.im);
+    ener2[0] += Pk;
+    ener2[1] += o12p;
+    ener2[2] += nuty;
+  } else {
+    Pk = -(o3_00.re) * (-uvr) + (o3_00.re * o3_00.re - o3_00.im * o3_00.im) * (1.0 / c->p.Re);
+    ener2[0] += Pk;
+    ener2[1] += o12p;
+  }
   /* dissipation (cross.f90:1926-1944) */
   double eps = 0.0;
   {
@@ -1062,6 +1103,102 @@ static void hist_f(ctx *c, pthread_buf *b, const cplx *dv, double *ener, double 
     }
   }
   ener[9] += eps;
+  if (c->p.les) {
+    /* energy transfer to the subgrid scales (cross.f90:1950-1954) */
+    int n = c->mgalx, ld = c->mgalx + 2;
+    double de = 0.0;
+    for (int z = 0; z < c->mgalz; z++)
+      for (int x = 0; x < n; x++) de += b->nus[z * ld + x] * b->sij2[z * ld + x];
+    ener2[3] += de / (double)(c->mgalx * c->mgalz);
+  }
+}
+
+/* LES block of hvhg for plane j (cross.f90:1291-1406): strain-rate gradients
+ * from the Fourier velocities and vorticities, |S|^2 with the mean shear,
+ * 2/3-dealiased (rev.1317), nu_t = (Cles Deltag)^2 |S|, the stresses T_ij back
+ * to Fourier, and the four right-hand-side pieces of the phi and omega_y
+ * equations (rhvc1, rhvc2, rhgc1, rhgc2, plane layout) plus T12, T23 of the
+ * (0,0) mode (txy00, tyz00). */
+static void les_plane(ctx *c, pthread_buf *b, const cplx *dvdy, cplx *rhvc1, cplx *rhvc2,
+                      cplx *rhgc1, cplx *rhgc2, double *txy00j, double *tyz00j, int rkstep,
+                      plane_red *red) {
+  int nkx = c->nkx, mz = c->mz, mgalx = c->mgalx, mgalz = c->mgalz, ld = mgalx + 2;
+  double s = c->p.s;
+  const cplx *u1c = b->u1c, *u2c = b->u2c, *u3c = b->u3c, *o1c = b->o1c, *o3c = b->o3c;
+  /* lc: 0 ux, 1 vy, 2 wz, 3 vz+wy, 4 uy+vx, 5 uz+wx */
+  for (int k = 0; k < mz; k++) {
+    double g = c->xgam_im[k];
+    for (int i = 0; i < nkx; i++) {
+      double a = c->xalp_im[i];
+      int q = k * nkx + i;
+      cplx u1 = u1c[q], u2 = u2c[q], u3 = u3c[q];
+      cplx uxc = C(-a * u1.im, a * u1.re), uzc = C(-g * u1.im, g * u1.re);
+      cplx vxc = C(-a * u2.im, a * u2.re), vzc = C(-g * u2.im, g * u2.re);
+      cplx wxc = C(-a * u3.im, a * u3.re), wzc = C(-g * u3.im, g * u3.re);
+      b->lc[0][q] = uxc;
+      b->lc[1][q] = dvdy[q];
+      b->lc[2][q] = wzc;
+      b->lc[3][q] = C(2.0 * vzc.re + o1c[q].re, 2.0 * vzc.im + o1c[q].im);
+      b->lc[4][q] = C(2.0 * vxc.re - o3c[q].re, 2.0 * vxc.im - o3c[q].im);
+      b->lc[5][q] = cadd(uzc, wxc);
+    }
+  }
+  for (int f = 0; f < 6; f++) fourxz(c, b, b->lc[f], b->lr[f], 1);
+  double *ux = b->lr[0], *vy = b->lr[1], *wz = b->lr[2], *vz = b->lr[3], *uy = b->lr[4],
+         *uz = b->lr[5], *S2 = b->sij2, *nu = b->nus;
+  for (int z = 0; z < mgalz; z++)
+    for (int x = 0; x < mgalx; x++) {
+      int q = z * ld + x;
+      S2[q] = 2.0 * ux[q] * ux[q] + (uy[q] + s) * (uy[q] + s) + 2.0 * vy[q] * vy[q] +
+              uz[q] * uz[q] + 2.0 * wz[q] * wz[q] + vz[q] * vz[q];
+    }
+  /* 2/3 rule on |S|^2: r2c then c2r (cross.f90:1357-1360) */
+  for (int q = 0; q < nkx * mz; q++) b->wyc[q] = C(0.0, 0.0);
+  fourxz(c, b, b->wyc, S2, -1);
+  fourxz(c, b, b->wyc, S2, 1);
+  double fac = c->p.cs * c->p.cs * c->Deltag * c->Deltag;
+  double numax = red->numax;
+  for (int z = 0; z < mgalz; z++)
+    for (int x = 0; x < mgalx; x++) {
+      int q = z * ld + x;
+      double v = fac * sqrt(fabs(S2[q]));
+      if (s < 0.0) v = -v;
+      nu[q] = v;
+      if (rkstep == 1 && fabs(v) > numax) numax = fabs(v);
+      double t11 = 2.0 * v * ux[q], t12 = v * (uy[q] + s), t13 = v * uz[q];
+      double t22 = 2.0 * v * vy[q], t23 = v * vz[q], t33 = 2.0 * v * wz[q];
+      ux[q] = t11; uy[q] = t12; uz[q] = t13;
+      vy[q] = t22; vz[q] = t23; wz[q] = t33;
+    }
+  red->numax = numax;
+  /* back to Fourier: T11 T12 T13 T22 T23 T33 */
+  cplx *T11 = b->lc[0], *T12 = b->lc[4], *T13 = b->lc[5], *T22 = b->lc[1], *T23 = b->lc[3],
+       *T33 = b->lc[2];
+  fourxz(c, b, T11, ux, -1);
+  fourxz(c, b, T12, uy, -1);
+  fourxz(c, b, T13, uz, -1);
+  fourxz(c, b, T22, vy, -1);
+  fourxz(c, b, T23, vz, -1);
+  fourxz(c, b, T33, wz, -1);
+  *txy00j = T12[0].re;
+  *tyz00j = T23[0].re;
+  for (int k = 0; k < mz; k++) {
+    double g = c->xgam_im[k], g2 = c->gam2[k];
+    for (int i = 0; i < nkx; i++) {
+      double a = c->xalp_im[i], a2 = c->alp2[i];
+      int q = k * nkx + i;
+      /* 2*xalp*xgam = -(2a)g and xalp*xgam = -a g (products of imaginaries) */
+      double m2ag = -((2.0 * a) * g), mag = -(a * g);
+      cplx t11 = T11[q], t12 = T12[q], t13 = T13[q], t22 = T22[q], t23 = T23[q], t33 = T33[q];
+      double ak = a2 + g2;
+      rhvc1[q] = C(a2 * t11.re - m2ag * t13.re + g2 * t33.re - ak * t22.re,
+                   a2 * t11.im - m2ag * t13.im + g2 * t33.im - ak * t22.im);
+      rhvc2[q] = cadd(C(-a * t12.im, a * t12.re), C(-g * t23.im, g * t23.re));
+      double ga = -g2 + a2;
+      rhgc1[q] = C(mag * (t11.re - t33.re) + ga * t13.re, mag * (t11.im - t33.im) + ga * t13.im);
+      rhgc2[q] = csub(C(-g * t12.im, g * t12.re), C(-a * t23.im, a * t23.re));
+    }
+  }
 }
 
 /* hvhg for one plane (cross.f90:1221-1587).  Plane-layout arrays point at
@@ -1070,7 +1207,8 @@ static void hvhg_plane(ctx *c, pthread_buf *b, int j, const cplx *phic, const cp
                        cplx *rhvc, cplx *rhgc, cplx *ome1c, const double *u00,
                        const double *w00, const double *rf0u_in, const double *rf0w_in,
                        double *rf0u_out, double *rf0w_out, int rkstep, int ihist,
-                       plane_red *red) {
+                       plane_red *red, cplx *rhvc1, cplx *rhvc2, cplx *rhgc1, cplx *rhgc2,
+                       double *txy00, double *tyz00) {
   int nkx = c->nkx, mz = c->mz, mgalx = c->mgalx, mgalz = c->mgalz;
   int ld = mgalx + 2;
   double s = c->p.s, chi = c->p.chi;
@@ -1111,7 +1249,9 @@ static void hvhg_plane(ctx *c, pthread_buf *b, int j, const cplx *phic, const cp
     o2c[q] = ome2c[q];
   }
   u2c[0] = C(c->p.vbulk, 0.0);
-  if (ihist) hist_f(c, b, rhvc, red->ener, red->ener2);
+  if (c->p.les)
+    les_plane(c, b, rhvc, rhvc1, rhvc2, rhgc1, rhgc2, &txy00[j], &tyz00[j], rkstep, red);
+  if (ihist) hist_f(c, b, rhvc, red->ener, red->ener2, c->p.les ? txy00[j] : 0.0);
   fourxz(c, b, u1c, b->u1r, 1);
   fourxz(c, b, u2c, b->u2r, 1);
   fourxz(c, b, u3c, b->u3r, 1);
@@ -1248,6 +1388,17 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
   double *rf0u = dalloc(my), *rf0w = dalloc(my), *u00wk = dalloc(my), *w00wk = dalloc(my);
   double *rf0u_d = dalloc(my), *rf0w_d = dalloc(my), *wk1dr = dalloc(my);
   plane_red *red = (plane_red *)calloc((size_t)my, sizeof(plane_red));
+  /* LES buffers rhvc1, rhvc2, rhgc1, rhgc2 (pencil and plane) and T12, T23 of
+   * the (0,0) mode (cross.f90:242-247) */
+  int les = c->p.les;
+  double *lp[4] = {NULL, NULL, NULL, NULL};
+  cplx *lq[4] = {NULL, NULL, NULL, NULL};
+  double *txy00 = dalloc(my), *tyz00 = dalloc(my);
+  if (les)
+    for (int f = 0; f < 4; f++) {
+      lp[f] = dalloc(nfield);
+      lq[f] = zalloc(nplane * my);
+    }
   cplx *shb = zalloc(nkx), *sht = zalloc(nkx), *shwkb = zalloc(nkx), *shwkt = zalloc(nkx);
   for (int i = 0; i < nkx; i++) {
     shb[i] = sht[i] = shwkb[i] = shwkt[i] = C(1.0, 0.0);
@@ -1322,10 +1473,11 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
 #pragma omp parallel for schedule(static)
         for (int j = 0; j < my; j++) {
           pthread_buf *bb = &c->pt[my_thread()];
-          hvhg_plane(c, bb, j, b1 + (size_t)j * nplane, b2 + (size_t)j * nplane,
-                     phv + (size_t)j * nplane, phg + (size_t)j * nplane,
-                     pdv + (size_t)j * nplane, u00, w00, rf0u_d, rf0w_d, rf0u, rf0w, rkstep,
-                     ihist, &red[j]);
+          size_t o = (size_t)j * nplane;
+          hvhg_plane(c, bb, j, b1 + o, b2 + o, phv + o, phg + o, pdv + o, u00, w00, rf0u_d,
+                     rf0w_d, rf0u, rf0w, rkstep, ihist, &red[j], les ? lq[0] + o : NULL,
+                     les ? lq[1] + o : NULL, les ? lq[2] + o : NULL, les ? lq[3] + o : NULL,
+                     txy00, tyz00);
         }
         if (rkstep == 1) {
           double ul[4] = {uinit, uinit, uinit, uinit};
@@ -1333,6 +1485,10 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
             for (int q = 0; q < 4; q++)
               if (red[j].umaxl[q] > ul[q]) ul[q] = red[j].umaxl[q];
           for (int q = 0; q < 4; q++) umax[q] = ul[q];
+          if (les)
+            for (int j = 0; j < my; j++)
+              if (red[j].numax > c->max_nut) c->max_nut = red[j].numax;
+          double nutmax = c->max_nut;
           double dt;
           if (c->p.fixed_dt > 0.0) {
             dt = c->p.fixed_dt;
@@ -1345,12 +1501,37 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
                    v3 = c->pi * c->pi / c->dz / c->dz;
             double vv = v1 > v2 ? v1 : v2;
             vv = vv > v3 ? vv : v3;
-            CFLv = (1.0 / Re) * dt * vv;
+            if (les) {
+              /* cross.f90:1620-1635 */
+              double vn = 2.0 * nutmax * dt * vv;
+              if (c->p.les_visc) {
+                double vm = fabs(1.0 / Re) * dt * vv;
+                CFLv = vm > vn ? vm : vn;
+              } else {
+                CFLv = vn;
+              }
+            } else {
+              CFLv = (1.0 / Re) * dt * vv;
+            }
           } else {
             double m1 = umax[0] * c->cflx, m2 = umax[2] * c->cfly, m3 = umax[3] * c->cflz;
             double mm = m1 > m2 ? m1 : m2;
             mm = mm > m3 ? mm : m3;
             dt = 1.0 / mm;
+            if (les) {
+              /* cross.f90:1652-1666: cflvv from the eddy viscosity */
+              double v1 = c->pi * c->pi / c->dx / c->dx, v2 = 6.25 / c->dy / c->dy,
+                     v3 = c->pi * c->pi / c->dz / c->dz;
+              double vv = v1 > v2 ? v1 : v2;
+              vv = vv > v3 ? vv : v3;
+              double vn = nutmax / CFL * vv;
+              if (c->p.les_visc) {
+                double vm = fabs(1.0 / Re) / CFL * vv;
+                c->cflvv = vm > vn ? vm : vn;
+              } else {
+                c->cflvv = vn;
+              }
+            }
             CFLv = CFL * c->cflvv * dt;
             if (CFLv > CFL) dt = 1.0 / c->cflvv;
           }
@@ -1390,34 +1571,66 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
           }
           nt++;
           if (isnan(uner[0])) istop = 1;
-          if (uner[1] / c->Lz < 1e-5) istop = 1;
+          if (uner[1] / c->Lz < 1e-5 && !c->p.keep_laminar) istop = 1;
           ihist = 0;
         }
+      }
+      if (les) {
+        /* cross.f90:537-542: the LES pieces to pencils; d(vor - rhvc1)/dy */
+        for (int f = 0; f < 4; f++) to_pencil(c, lq[f], lp[f]);
       }
       to_pencil(c, phv, hv);
       to_pencil(c, phg, hg);
       to_pencil(c, pdv, dvordy);
+      if (les)
+        for (size_t q = 0; q < nfield; q++) dvordy[q] = dvordy[q] - lp[0][q];
 #pragma omp parallel for schedule(static)
       for (int ik = 0; ik < nkx * mz; ik++) {
         int i = ik % nkx, k = ik / nkx;
         ythread *t = &c->yt[my_thread()];
         derivyc(c, t, PEN(dvordy, i, k), PEN(dvordy, i, k), shwkt[i], shwkb[i], 1, 2, 1);
+        if (les) derivyc(c, t, PEN(lp[3], i, k), PEN(lp[3], i, k), shwkt[i], shwkb[i], 1, 2, 0);
       }
-      for (size_t q = 0; q < nfield; q++) hv[q] = hv[q] - dvordy[q];
-      double r1 = CA[rkstep - 1] * Deltat;
-      double fac = 1.0 / Re;
+      if (les) {
+        /* hv += (d2/dx2 + d2/dz2 - d2/dy2) rhvc2 (cross.f90:578-595) */
 #pragma omp parallel for schedule(static)
-      for (int ik = 0; ik < nkx * mz; ik++) {
-        int i = ik % nkx, k = ik / nkx;
-        if (i != 0 || k != 0) {
-          ythread *t = &c->yt[my_thread()];
-          double rk = c->gam2[k] + c->alp2[i];
-          double *scr = ddu + 2 * (size_t)my * ik;
-          visc3d(c, t, PEN(vor, i, k), PEN(hg, i, k), scr, shwkt[i], shwkb[i], 2, rk, fac, 1);
-          visc3d(c, t, PEN(phi, i, k), PEN(hv, i, k), scr, shwkt[i], shwkb[i], 2, rk, fac, 0);
+        for (int ik = 0; ik < nkx * mz; ik++) {
+          int i = ik % nkx, k = ik / nkx;
+          if (i != 0 || k != 0) {
+            ythread *t = &c->yt[my_thread()];
+            double rk = -(c->gam2[k] + c->alp2[i]);
+            double *scr = ddu + 2 * (size_t)my * ik;
+            visc3d(c, t, PEN(lp[1], i, k), PEN(hv, i, k), scr, shwkt[i], shwkb[i], 2, rk, -1.0, 1);
+          }
         }
       }
-      {
+      for (size_t q = 0; q < nfield; q++) hv[q] = hv[q] - dvordy[q];
+      if (les)
+        for (size_t q = 0; q < nfield; q++) hg[q] = hg[q] + lp[2][q] + lp[3][q];
+      double r1 = CA[rkstep - 1] * Deltat;
+      double fac = 1.0 / Re;
+      if (les) {
+        /* mean-mode stresses (cross.f90:639-647) */
+        cplx one = C(1.0, 0.0);
+        derivyc(c, &c->yt[0], txy00, txy00, one, one, 1, 1, 0);
+        derivyc(c, &c->yt[0], tyz00, tyz00, one, one, 1, 1, 0);
+        for (int j = 0; j < my; j++) {
+          rf0u[j] = rf0u[j] + txy00[j];
+          rf0w[j] = rf0w[j] + tyz00[j];
+        }
+      }
+      if (!les || c->p.les_visc) {
+#pragma omp parallel for schedule(static)
+        for (int ik = 0; ik < nkx * mz; ik++) {
+          int i = ik % nkx, k = ik / nkx;
+          if (i != 0 || k != 0) {
+            ythread *t = &c->yt[my_thread()];
+            double rk = c->gam2[k] + c->alp2[i];
+            double *scr = ddu + 2 * (size_t)my * ik;
+            visc3d(c, t, PEN(vor, i, k), PEN(hg, i, k), scr, shwkt[i], shwkb[i], 2, rk, fac, 1);
+            visc3d(c, t, PEN(phi, i, k), PEN(hv, i, k), scr, shwkt[i], shwkb[i], 2, rk, fac, 0);
+          }
+        }
         cplx one = C(1.0, 0.0);
         visc3d(c, &c->yt[0], u00, rf0u, wk1dr, one, one, 1, 0.0, fac, 0);
         visc3d(c, &c->yt[0], w00, rf0w, wk1dr, one, one, 1, 0.0, fac, 0);
@@ -1506,5 +1719,10 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
   free(b1); free(b2); free(phv); free(phg); free(pdv);
   free(rf0u); free(rf0w); free(u00wk); free(w00wk); free(rf0u_d); free(rf0w_d); free(wk1dr);
   free(red); free(shb); free(sht); free(shwkb); free(shwkt);
+  for (int f = 0; f < 4; f++) {
+    free(lp[f]);
+    free(lq[f]);
+  }
+  free(txy00); free(tyz00);
   return done;
 }

@@ -34,6 +34,10 @@ typedef struct orc_params {
   double uprim;           /* hre2.dat record 4 */
   int nhist;              /* statistics every nhist steps (cross.f90:344) */
   double etime, dumptime, dtimag; /* end/dump times (cross.f90:1694-1711) */
+  int keep_laminar;       /* 1: no stop on laminarisation (cross.f90:2106-2115) */
+  int les;                /* iuse_LES: Smagorinsky model (cross.f90:1291-1406) */
+  int les_visc;           /* iadd_visc: molecular viscosity kept with the model */
+  double cs;              /* Cles, the Smagorinsky constant (initcr.f90:1964,2148) */
 } orc_params;
 
 /* one .cfbin record per statistics step (cross.f90:2087):
