@@ -47,6 +47,11 @@ typedef struct sb_params {
   double etime, dumptime, dtimag; /* end time, dump time and interval */
   int keep_laminar;            /* 1: no stop on laminarisation (v_rms/Lz < 1e-5,
                                   cross.f90:2106-2115); the flag is still set */
+  int les;                     /* iuse_LES: Smagorinsky eddy viscosity
+                                  (cross.f90:1291-1406, hre3.dat keyword iuse_LES) */
+  int les_visc;                /* iadd_visc: keep the molecular viscosity with the model */
+  double cs;                   /* Cles, Smagorinsky constant; filter width
+                                  (dx*dy*dz)^(1/3) (initcr.f90:510) */
 } sb_params;
 
 /* Per-box status after sb_step (cross.f90 istop logic, 1683-1690, 2102-2115) */
@@ -112,7 +117,8 @@ int sb_cross(sb_handle *h, double *vor, double *phi, double *u00, double *w00, d
 /* Measurement hooks (no counterpart in the reference; used by the benchmark).
  * sb_launch_stage enqueues `count` launches of one kernel of substep rk on the
  * handle's stream: stage 1..3 the plane stages, 4 the per-box phase tables,
- * 5 and 6 the two y-line kernels.  The launches act on the current device state, so a
+ * 5 and 6 the two y-line kernels; with LES, 7..10 the four LES plane kernels
+ * and 11 the LES y-line kernel.  The launches act on the current device state, so a
  * run that used them must set the state again before stepping.
  * sb_fp64_peak measures the device's FP64 FMA throughput in TFLOP/s. */
 int sb_launch_stage(sb_handle *h, int stage, int rk, int count);

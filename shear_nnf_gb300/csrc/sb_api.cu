@@ -113,7 +113,8 @@ static void member_defaults(const sb_params *p, const Grid &g, double Re, Member
   memset(m, 0, sizeof(Member));
   const double pi = g.pi;
   m->Re = Re;
-  m->nu = 1.0 / Re;
+  // without iadd_visc the LES run has no molecular viscous term (cross.f90:649)
+  m->nu = (p->les && !p->les_visc) ? 0.0 : 1.0 / Re;
   m->CFL = p->CFL;
   // set_xyz_dy (initcr.f90:490-498)
   m->cflx = pi / p->CFL / g.dx;
@@ -143,9 +144,14 @@ static int capture_step(sb_handle *h) {
   for (int rk = 1; rk <= 3 && e == cudaSuccess; rk++) {
     if ((e = launch_plane(h->g, h->bf, 1, rk, h->st)) != cudaSuccess) break;
     if ((e = launch_plane(h->g, h->bf, 2, rk, h->st)) != cudaSuccess) break;
+    if (h->g.les)
+      for (int q = 2; q <= 4 && e == cudaSuccess; q++) e = launch_les(h->g, h->bf, q, rk, h->st);
+    if (e != cudaSuccess) break;
     if ((e = launch_plane(h->g, h->bf, 3, rk, h->st)) != cudaSuccess) break;
+    if (h->g.les && (e = launch_les(h->g, h->bf, 5, rk, h->st)) != cudaSuccess) break;
     if ((e = launch_scalar(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
     if ((e = launch_tables(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
+    if (h->g.les && (e = launch_lineL(h->g, h->bf, h->st)) != cudaSuccess) break;
     if ((e = launch_lineA(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
     e = launch_lineB(h->g, h->bf, rk, h->st);
   }
@@ -303,6 +309,16 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   g.dx = 2.0 * g.pi / p->alp / (double)g.mx;
   g.dz = 2.0 * g.pi / p->gam / (double)g.mz;
   g.dy = p->Ly / (double)p->my;
+  g.les = p->les ? 1 : 0;
+  g.les_visc = p->les_visc ? 1 : 0;
+  g.nzf = g.les ? 10 : 6;
+  g.cbl = les_cb(p->mgalz);
+  g.ncbl = (g.nkx + g.cbl - 1) / g.cbl;
+  if (g.les) {
+    // Deltag = (dx dy dz)^(1/3) (initcr.f90:510); nu_t = Cles^2 Deltag^2 |S|
+    const double dg = std::pow(g.dx * g.dy * g.dz, 1.0 / 3.0);
+    g.les_c = p->cs * p->cs * dg * dg;
+  }
   sbh::Coeffs co;
   sbh::compact_coeffs(&co);
   const double hdy = g.dy;
@@ -341,13 +357,23 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
       (rc = A(&bf.tl1n, B * g.nkx * SB_TAIL)) ||
       (rc = A(&bf.mu, B * 2 * my)) || (rc = A(&bf.mwk, B * 2 * my)) ||
       (rc = A(&bf.mrf, B * 2 * my)) || (rc = A(&bf.mdu, B * 2 * my)) ||
-      (rc = A(&bf.zbuf, B * my * g.mgalz * 6 * g.nkx * 2)) ||
+      (rc = A(&bf.zbuf, B * my * g.mgalz * g.nzf * g.nkx * 2)) ||
       (rc = A(&bf.xbuf, B * my * g.mgalz * 3 * g.nkx * 2)) ||
       (rc = A(&bf.hpart, B * my * g.ncb * SB_NHIST_Q)) || (rc = A(&bf.sh_old, B * 4 * g.nkx)) ||
       (rc = A(&bf.sh_new, B * 4 * g.nkx)) || (rc = A(&bf.mf1, B * my * g.nkx * 2)) ||
       (rc = A(&bf.mf2, B * my * g.nkx * 2)) || (rc = A(&h->d_pen, F))) {
     sb_destroy(h);
     return rc;
+  }
+  if (g.les) {
+    const size_t NX = g.mgalx, NZ = g.mgalz, nk = g.nkx;
+    if ((rc = A(&bf.gbuf, B * my * (NZ / 2) * 12 * NX)) || (rc = A(&bf.sbuf, B * my * NZ * nk * 2)) ||
+        (rc = A(&bf.tbuf, B * my * NZ * 6 * nk * 2)) || (rc = A(&bf.L1, B * F)) ||
+        (rc = A(&bf.L2, B * F)) || (rc = A(&bf.txy, B * 2 * my)) ||
+        (rc = A(&bf.lpart, B * my * (NZ / 2) * 2))) {
+      sb_destroy(h);
+      return rc;
+    }
   }
   {
     void *q = nullptr;
@@ -464,7 +490,8 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
     sb_destroy(h);
     return fail(3, "member upload: %s", cudaGetErrorString(ce));
   }
-  if (launch_plane(g, bf, 0, 0, h->st) != cudaSuccess || prepare_line(g) != cudaSuccess) {
+  if (launch_plane(g, bf, 0, 0, h->st) != cudaSuccess || prepare_line(g) != cudaSuccess ||
+      (g.les && launch_les(g, bf, 0, 0, h->st) != cudaSuccess)) {
     sb_destroy(h);
     return fail(3, "kernel attributes: %s", cudaGetErrorString(cudaGetLastError()));
   }
@@ -538,6 +565,10 @@ int sb_set_state(sb_handle *h, int member, const double *vor, const double *phi,
   double sc[3] = {time, xoffb, xofft};
   CK(cudaMemcpyAsync((char *)(h->bf.mem + member) + offsetof(Member, time), sc, sizeof(sc),
                      cudaMemcpyHostToDevice, h->st));
+  // a new state restarts the LES running maximum of nu_t
+  static const double zero = 0.0;
+  CK(cudaMemcpyAsync((char *)(h->bf.mem + member) + offsetof(Member, max_nut), &zero,
+                     sizeof(double), cudaMemcpyHostToDevice, h->st));
   CK(cudaStreamSynchronize(h->st));
   return 0;
 }
@@ -642,7 +673,8 @@ void *sb_get_stream(sb_handle *h) { return h ? (void *)h->st : nullptr; }
 
 int sb_launch_stage(sb_handle *h, int stage, int rk, int count) {
   if (!h || count < 0) return fail(1, "bad argument");
-  if (stage < 1 || stage > 6 || rk < 1 || rk > 3) return fail(1, "stage 1..6, rk 1..3");
+  if (stage < 1 || stage > 11 || rk < 1 || rk > 3) return fail(1, "stage 1..11, rk 1..3");
+  if (stage >= 7 && !h->g.les) return fail(1, "stages 7..11 need an LES handle");
   for (int q = 0; q < count; q++) {
     cudaError_t e;
     if (stage <= 3)
@@ -651,8 +683,12 @@ int sb_launch_stage(sb_handle *h, int stage, int rk, int count) {
       e = launch_tables(h->g, h->bf, rk, h->st);
     else if (stage == 5)
       e = launch_lineA(h->g, h->bf, rk, h->st);
-    else
+    else if (stage == 6)
       e = launch_lineB(h->g, h->bf, rk, h->st);
+    else if (stage <= 10)
+      e = launch_les(h->g, h->bf, stage - 5, rk, h->st);
+    else
+      e = launch_lineL(h->g, h->bf, h->st);
     if (e != cudaSuccess) return fail(3, "launch: %s", cudaGetErrorString(e));
   }
   return 0;

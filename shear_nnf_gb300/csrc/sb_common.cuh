@@ -56,6 +56,11 @@ struct Grid {
   int nlines_pad;        // component lines per member, padded to whole warps
   int nseg, slo[4], shi[4];  // segments of the banded rows of the y-solves
   int ngrp;              // groups of 16 lines per member in the y-line kernels
+  // Smagorinsky LES (cross.f90:1291-1406): on/off, molecular viscosity kept,
+  // (Cles * Deltag)^2, fields per z row of zbuf (6, or 10 with the model),
+  // kx columns per block of the LES column kernel and their count
+  int les, les_visc, nzf, cbl, ncbl;
+  double les_c;
 };
 
 // Per-member run state, owned by the device (one per box in the batch)
@@ -70,6 +75,8 @@ struct Member {
   double Deltat, CFLcur, CFLv;
   double umax[4];
   unsigned long long umax_bits[4];  // |u| maxima as ordered bit patterns (atomicMax)
+  unsigned long long nut_bits;      // LES: max |nu_t| of this step (bit pattern)
+  double max_nut;                   // LES: running maximum of |nu_t| (cross.f90:1433)
   int istop, idump, ihist, istep, halted, ntrace, trace_cap, flags;
 };
 
@@ -101,6 +108,11 @@ struct Bufs {
   const double *ginv;            // 1/g per kz  (g = gam * kz_signed; 0 at k=0)
   const double *kinv;            // 1/(alp2+gam2) per (k,i); 0 at (0,0)
   Fac d1, d2, hz;                // d/dy, d2/dy2, Helmholtz (per line)
+  // LES buffers: physical gradient rows [B][my][mgalz/2][6][2][mgalx], |S|^2
+  // x-spectra [B][my][mgalz][nkx], stress x-spectra [B][my][mgalz][6][nkx],
+  // rhvc2 and rhgc2 fields, T12/T23 of the (0,0) mode [B][my] complex, plane
+  // partial sums of nu_t and nu_t |S|^2 [B][my][mgalz/2][2]
+  double *gbuf, *sbuf, *tbuf, *L1, *L2, *txy, *lpart;
 };
 
 }  // namespace sb

@@ -166,9 +166,10 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
       bf.hpart[(((long)b * g.my + j) * g.ncb + cb) * SB_NHIST_Q + threadIdx.x] = v;
     }
   }
-  V *zb = (V *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * 6 * nkx;
+  V *zb = (V *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * g.nzf * nkx;
   const V zero = mk2<R>((R)0, (R)0);
-  for (int round = 0; round < 3; round++) {
+  const int nround = g.les ? 5 : 3;
+  for (int round = 0; round < nround; round++) {
     // fill two fields (zero the 2/3-rule gap) on the padded z grid
     for (int idx = threadIdx.x; idx < 2 * CB * NZ; idx += T) A[idx] = zero;
     __syncthreads();
@@ -204,9 +205,37 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
           tx = gz * w1.x - a * ph.x; ty = gz * w1.y - a * ph.y;
           fb = mk2<R>(-ty * iK, tx * iK);
         }
-      } else {  // v (f=4) and omega_y (f=5)
+      } else if (round == 2) {  // v (f=4) and omega_y (f=5)
         fa = z00 ? mk2<R>((R)M.vbulk, (R)0) : Gv[k * nkx + i];
         fb = ld_sym(vor, i, k);
+      } else if (round == 3) {
+        // LES (cross.f90:1293-1325): dv/dy (f=6) and i kz w (f=7)
+        if (z00) {
+          fa = zero;
+          fb = zero;
+        } else {
+          const V dv = Vv[k * nkx + i], vr = ld_sym(vor, i, k);
+          fa = dv;
+          const R tx = gz * dv.x + a * vr.x, ty = gz * dv.y + a * vr.y;
+          const V u3 = mk2<R>(-ty * iK, tx * iK);
+          fb = mk2<R>(-gz * u3.y, gz * u3.x);
+        }
+      } else {
+        // LES: 2 i kz v + omega_x (f=8, dv/dz + dw/dy) and i kz u (f=9)
+        if (z00) {
+          fa = mk2<R>(mdu.y, (R)0);
+          fb = zero;
+        } else {
+          const V w1 = Dv[k * nkx + i], ph = ld_sym(phi, i, k);
+          R tx = a * w1.x + gz * ph.x, ty = a * w1.y + gz * ph.y;
+          const V o1 = mk2<R>(-ty * iK, tx * iK);
+          const V u2 = Gv[k * nkx + i];
+          fa = mk2<R>((R)2 * (-gz * u2.y) + o1.x, (R)2 * (gz * u2.x) + o1.y);
+          const V dv = Vv[k * nkx + i], vr = ld_sym(vor, i, k);
+          tx = a * dv.x - gz * vr.x; ty = a * dv.y - gz * vr.y;
+          const V u1 = mk2<R>(-ty * iK, tx * iK);
+          fb = mk2<R>(-gz * u1.y, gz * u1.x);
+        }
       }
       A[ci * NZ + kg] = fa;
       A[(CB + ci) * NZ + kg] = fb;
@@ -217,7 +246,7 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
       const int ci = idx % CB, rem = idx / CB;
       const int z = rem % NZ, f = rem / NZ;
       const int i = i0 + ci;
-      if (i < nkx) zb[((long)z * 6 + 2 * round + f) * nkx + i] = res[(f * CB + ci) * NZ + z];
+      if (i < nkx) zb[((long)z * g.nzf + 2 * round + f) * nkx + i] = res[(f * CB + ci) * NZ + z];
     }
     __syncthreads();
   }
@@ -240,7 +269,7 @@ __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
   V *A = (V *)smem_raw, *Bs = A + 6 * NX;
   const int nkx = g.nkx, NZ = g.mgalz;
   const int z = 2 * zp;
-  const V *zb = (const V *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * 6 * nkx;
+  const V *zb = (const V *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * g.nzf * nkx;
   // Hermitian extension of two rows into one complex sequence (c2r of both rows
   // at once); FFTW's c2r ignores the imaginary part of the kx = 0 entry
   const V zero = mk2<R>((R)0, (R)0);
@@ -248,8 +277,8 @@ __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
   __syncthreads();
   for (int idx = threadIdx.x; idx < 6 * nkx; idx += T) {
     const int f = idx / nkx, i = idx - f * nkx;
-    V X1 = zb[((long)z * 6 + f) * nkx + i];
-    V X2 = zb[((long)(z + 1) * 6 + f) * nkx + i];
+    V X1 = zb[((long)z * g.nzf + f) * nkx + i];
+    V X2 = zb[((long)(z + 1) * g.nzf + f) * nkx + i];
     if (i == 0) {
       X1.y = (R)0;
       X2.y = (R)0;
@@ -368,6 +397,285 @@ __global__ void __launch_bounds__(T) k_p3(Grid g, Bufs bf) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Smagorinsky LES stage (iuse_LES, cross.f90:1291-1406).  Per substep, after
+// k_p2 (the zbuf z-transforms also hold dv/dy, i kz w, 2 i kz v + omega_x and
+// i kz u, written by k_p1):
+//   k_les2  per (plane, z row pair): the six strain-rate combinations
+//           du/dx, dv/dy, dw/dz, dv/dz+dw/dy, du/dy+dv/dx, du/dz+dw/dx to
+//           physical x (kept in gbuf), |S|^2 with the mean shear, its
+//           forward x-transform
+//   k_les3  per (plane, kx block): forward z-transform, 2/3 truncation and
+//           backward z-transform of |S|^2 (the r2c/c2r pair of rev.1317)
+//   k_les4  per (plane, z row pair): dealiased |S|^2 to physical x,
+//           nu_t = (Cles Deltag)^2 |S|, the stresses T11..T33, nu_t maxima and
+//           statistics, forward x-transforms of the stresses
+//   k_les5  per (plane, kx block, after k_p3): forward z-transforms of the
+//           stresses, the right-hand-side pieces rhvc1 (subtracted from
+//           dH1/dx + dH3/dz), rhgc1 (added to the omega_y right-hand side),
+//           rhvc2 and rhgc2 (y-operators applied by k_lineL), T12 and T23 of
+//           the (0,0) mode
+// ---------------------------------------------------------------------------
+template <typename R, int NX, int T>
+__global__ void __launch_bounds__(T) k_les2(Grid g, Bufs bf) {
+  typedef typename Vec2<R>::t V;
+  const int zp = blockIdx.x, j = blockIdx.y, b = blockIdx.z;
+  const Member &M = bf.mem[b];
+  if (M.halted) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *A = (V *)smem_raw, *Bs = A + 6 * NX;
+  const int nkx = g.nkx, NZ = g.mgalz, nzf = g.nzf;
+  const int z = 2 * zp;
+  const V *zb = (const V *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * nzf * nkx;
+  const V zero = mk2<R>((R)0, (R)0);
+  for (int idx = threadIdx.x; idx < 6 * NX; idx += T) A[idx] = zero;
+  __syncthreads();
+  // zbuf fields: 0 u, 1 w, 2 omega_x, 3 omega_z, 4 v, 5 omega_y, 6 dv/dy,
+  // 7 i kz w, 8 2 i kz v + omega_x, 9 i kz u
+  for (int idx = threadIdx.x; idx < 6 * nkx; idx += T) {
+    const int f = idx / nkx, i = idx - f * nkx;
+    const R a = (R)(g.alp * i);
+    V X[2];
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      const V *row = zb + (long)(z + r) * nzf * nkx;
+      V x;
+      if (f == 0) {  // du/dx
+        const V u = row[i];
+        x = mk2<R>(-a * u.y, a * u.x);
+      } else if (f == 1) {  // dv/dy
+        x = row[6 * nkx + i];
+      } else if (f == 2) {  // dw/dz
+        x = row[7 * nkx + i];
+      } else if (f == 3) {  // dv/dz + dw/dy
+        x = row[8 * nkx + i];
+      } else if (f == 4) {  // du/dy + dv/dx = 2 dv/dx - omega_z
+        const V v = row[4 * nkx + i], o3 = row[3 * nkx + i];
+        x = mk2<R>((R)2 * (-a * v.y) - o3.x, (R)2 * (a * v.x) - o3.y);
+      } else {  // du/dz + dw/dx
+        const V w = row[nkx + i], izu = row[9 * nkx + i];
+        x = mk2<R>(izu.x + (-a * w.y), izu.y + a * w.x);
+      }
+      X[r] = x;
+    }
+    if (i == 0) {
+      X[0].y = (R)0;
+      X[1].y = (R)0;
+    }
+    A[f * NX + i] = mk2<R>(X[0].x - X[1].y, X[0].y + X[1].x);
+    if (i > 0) A[f * NX + NX - i] = mk2<R>(X[0].x + X[1].y, -X[0].y + X[1].x);
+  }
+  V *P = fft_batch<NX, +1, 6, T>(A, Bs, (const V *)tw_of<R>(bf, false));
+  V *Q = (P == A) ? Bs : A;
+  R *gb = (R *)bf.gbuf + (((long)b * g.my + j) * (NZ / 2) + zp) * 12L * NX;
+  const R s = (R)g.s;
+  for (int x = threadIdx.x; x < NX; x += T) {
+    const V ux = P[x], vy = P[NX + x], wz = P[2 * NX + x], vz = P[3 * NX + x],
+            uy = P[4 * NX + x], uz = P[5 * NX + x];
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+      gb[(2 * f) * NX + x] = P[f * NX + x].x;
+      gb[(2 * f + 1) * NX + x] = P[f * NX + x].y;
+    }
+    // Sij2 (cross.f90:1330-1337)
+    const R s0 = (R)2 * ux.x * ux.x + (uy.x + s) * (uy.x + s) + (R)2 * vy.x * vy.x +
+                 uz.x * uz.x + (R)2 * wz.x * wz.x + vz.x * vz.x;
+    const R s1 = (R)2 * ux.y * ux.y + (uy.y + s) * (uy.y + s) + (R)2 * vy.y * vy.y +
+                 uz.y * uz.y + (R)2 * wz.y * wz.y + vz.y * vz.y;
+    Q[x] = mk2<R>(s0, s1);
+  }
+  V *Rr = fft_batch<NX, -1, 1, T>(Q, P, (const V *)tw_of<R>(bf, false));
+  V *sbp = (V *)bf.sbuf + ((long)b * g.my + j) * (long)NZ * nkx;
+  const R half = (R)0.5;
+  for (int i = threadIdx.x; i < nkx; i += T) {
+    const V zk = Rr[i];
+    V zm = Rr[(NX - i) % NX];
+    zm.y = -zm.y;
+    sbp[(long)z * nkx + i] = mk2<R>(half * (zk.x + zm.x), half * (zk.y + zm.y));
+    sbp[(long)(z + 1) * nkx + i] = mk2<R>(half * (zk.y - zm.y), -half * (zk.x - zm.x));
+  }
+}
+
+template <typename R, int NZ, int CB, int T>
+__global__ void __launch_bounds__(T) k_les3(Grid g, Bufs bf) {
+  typedef typename Vec2<R>::t V;
+  const int cb = blockIdx.x, j = blockIdx.y, b = blockIdx.z;
+  const Member &M = bf.mem[b];
+  if (M.halted) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *A = (V *)smem_raw, *Bs = A + CB * NZ;
+  const int nkx = g.nkx, nz = g.nz, i0 = cb * CB;
+  V *sbp = (V *)bf.sbuf + ((long)b * g.my + j) * (long)NZ * nkx;
+  const V zero = mk2<R>((R)0, (R)0);
+  for (int idx = threadIdx.x; idx < CB * NZ; idx += T) {
+    const int ci = idx % CB, z = idx / CB, i = i0 + ci;
+    A[ci * NZ + z] = (i < nkx) ? sbp[(long)z * nkx + i] : zero;
+  }
+  V *P = fft_batch<NZ, -1, CB, T>(A, Bs, (const V *)tw_of<R>(bf, true));
+  const R norm = (R)(1.0 / (double)(g.mgalx * g.mgalz));
+  for (int idx = threadIdx.x; idx < CB * NZ; idx += T) {
+    const int z = idx % NZ;
+    const bool keep = (z <= nz) || (z >= NZ - nz);
+    V v = P[idx];
+    P[idx] = keep ? mk2<R>(norm * v.x, norm * v.y) : zero;
+  }
+  V *Q = fft_batch<NZ, +1, CB, T>(P, (P == A) ? Bs : A, (const V *)tw_of<R>(bf, true));
+  for (int idx = threadIdx.x; idx < CB * NZ; idx += T) {
+    const int ci = idx % CB, z = idx / CB, i = i0 + ci;
+    if (i < nkx) sbp[(long)z * nkx + i] = Q[ci * NZ + z];
+  }
+}
+
+template <typename R, int NX, int T>
+__global__ void __launch_bounds__(T) k_les4(Grid g, Bufs bf, int rk) {
+  typedef typename Vec2<R>::t V;
+  const int zp = blockIdx.x, j = blockIdx.y, b = blockIdx.z;
+  Member &M = bf.mem[b];
+  if (M.halted) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *A = (V *)smem_raw, *Bs = A + 6 * NX;
+  const int nkx = g.nkx, NZ = g.mgalz;
+  const int z = 2 * zp;
+  const V *sbp = (const V *)bf.sbuf + ((long)b * g.my + j) * (long)NZ * nkx;
+  const V zero = mk2<R>((R)0, (R)0);
+  for (int idx = threadIdx.x; idx < NX; idx += T) A[idx] = zero;
+  __syncthreads();
+  for (int i = threadIdx.x; i < nkx; i += T) {
+    V X1 = sbp[(long)z * nkx + i], X2 = sbp[(long)(z + 1) * nkx + i];
+    if (i == 0) {
+      X1.y = (R)0;
+      X2.y = (R)0;
+    }
+    A[i] = mk2<R>(X1.x - X2.y, X1.y + X2.x);
+    if (i > 0) A[NX - i] = mk2<R>(X1.x + X2.y, -X1.y + X2.x);
+  }
+  V *P = fft_batch<NX, +1, 1, T>(A, Bs, (const V *)tw_of<R>(bf, false));
+  V *Q = (P == A) ? Bs : A;
+  const R *gb = (const R *)bf.gbuf + (((long)b * g.my + j) * (NZ / 2) + zp) * 12L * NX;
+  const R C = (R)g.les_c, s = (R)g.s;
+  const bool neg = g.s < 0.0;
+  const bool stats = (rk == 1) && M.ihist;
+  R nmax = (R)0;
+  double snu = 0.0, sds = 0.0;
+  for (int x = threadIdx.x; x < NX; x += T) {
+    const V S2 = P[x];
+    R n0 = C * sqrt(fabs(S2.x)), n1 = C * sqrt(fabs(S2.y));
+    if (neg) {
+      n0 = -n0;
+      n1 = -n1;
+    }
+    if (rk == 1) nmax = fmax(nmax, fmax(fabs(n0), fabs(n1)));
+    if (stats) {
+      snu += (double)n0 + (double)n1;
+      sds += (double)n0 * (double)S2.x + (double)n1 * (double)S2.y;
+    }
+    // gradients: 0 ux, 1 vy, 2 wz, 3 vz+wy, 4 uy+vx, 5 uz+wx (two rows each)
+    const R ux0 = gb[0 * NX + x], ux1 = gb[1 * NX + x], vy0 = gb[2 * NX + x],
+            vy1 = gb[3 * NX + x], wz0 = gb[4 * NX + x], wz1 = gb[5 * NX + x],
+            vz0 = gb[6 * NX + x], vz1 = gb[7 * NX + x], uy0 = gb[8 * NX + x],
+            uy1 = gb[9 * NX + x], uz0 = gb[10 * NX + x], uz1 = gb[11 * NX + x];
+    // T11 T12 T13 T22 T23 T33 (cross.f90:1371-1376)
+    Q[0 * NX + x] = mk2<R>((R)2 * n0 * ux0, (R)2 * n1 * ux1);
+    Q[1 * NX + x] = mk2<R>(n0 * (uy0 + s), n1 * (uy1 + s));
+    Q[2 * NX + x] = mk2<R>(n0 * uz0, n1 * uz1);
+    Q[3 * NX + x] = mk2<R>((R)2 * n0 * vy0, (R)2 * n1 * vy1);
+    Q[4 * NX + x] = mk2<R>(n0 * vz0, n1 * vz1);
+    Q[5 * NX + x] = mk2<R>((R)2 * n0 * wz0, (R)2 * n1 * wz1);
+  }
+  if (rk == 1) {
+    unsigned long long bb = dbits((double)nmax);
+    for (int o = 16; o > 0; o >>= 1) bb = max(bb, __shfl_xor_sync(0xffffffffu, bb, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&M.nut_bits, bb);
+  }
+  if (stats) {
+    __shared__ double red[2][T / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+      snu += __shfl_down_sync(0xffffffffu, snu, o);
+      sds += __shfl_down_sync(0xffffffffu, sds, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red[0][threadIdx.x >> 5] = snu;
+      red[1][threadIdx.x >> 5] = sds;
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+      double v = 0.0;
+      for (int w = 0; w < T / 32; w++) v += red[threadIdx.x][w];
+      bf.lpart[(((long)b * g.my + j) * (NZ / 2) + zp) * 2 + threadIdx.x] = v;
+    }
+  }
+  V *Rr = fft_batch<NX, -1, 6, T>(Q, P, (const V *)tw_of<R>(bf, false));
+  V *tb = (V *)bf.tbuf + ((long)b * g.my + j) * (long)NZ * 6 * nkx;
+  const R half = (R)0.5;
+  for (int idx = threadIdx.x; idx < 6 * nkx; idx += T) {
+    const int f = idx / nkx, i = idx - f * nkx;
+    const V zk = Rr[f * NX + i];
+    V zm = Rr[f * NX + ((NX - i) % NX)];
+    zm.y = -zm.y;
+    tb[((long)z * 6 + f) * nkx + i] = mk2<R>(half * (zk.x + zm.x), half * (zk.y + zm.y));
+    tb[((long)(z + 1) * 6 + f) * nkx + i] = mk2<R>(half * (zk.y - zm.y), -half * (zk.x - zm.x));
+  }
+}
+
+template <typename R, int NZ, int CB, int T>
+__global__ void __launch_bounds__(T) k_les5(Grid g, Bufs bf) {
+  typedef typename Vec2<R>::t V;
+  const int cb = blockIdx.x, j = blockIdx.y, b = blockIdx.z;
+  const Member &M = bf.mem[b];
+  if (M.halted) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *A = (V *)smem_raw, *Bs = A + 6 * CB * NZ;
+  const int nkx = g.nkx, mz = g.mz, nz = g.nz, i0 = cb * CB;
+  const V *tb = (const V *)bf.tbuf + ((long)b * g.my + j) * (long)NZ * 6 * nkx;
+  const V zero = mk2<R>((R)0, (R)0);
+  for (int idx = threadIdx.x; idx < 6 * CB * NZ; idx += T) {
+    const int ci = idx % CB, rem = idx / CB;
+    const int f = rem % 6, z = rem / 6, i = i0 + ci;
+    A[(f * CB + ci) * NZ + z] = (i < nkx) ? tb[((long)z * 6 + f) * nkx + i] : zero;
+  }
+  V *P = fft_batch<NZ, -1, 6 * CB, T>(A, Bs, (const V *)tw_of<R>(bf, true));
+  const long pbase = (long)b * g.field + (long)j * g.plane;
+  V *Dv = (V *)((R *)bf.D + pbase);
+  V *Gv = (V *)((R *)bf.G + pbase);
+  V *L1 = (V *)((R *)bf.L1 + pbase);
+  V *L2 = (V *)((R *)bf.L2 + pbase);
+  const R norm = (R)(1.0 / (double)(g.mgalx * g.mgalz));
+  for (int idx = threadIdx.x; idx < CB * mz; idx += T) {
+    const int ci = idx % CB, k = idx / CB, i = i0 + ci;
+    if (i >= nkx) continue;
+    const int kg = kgrid(k, nz, NZ, mz);
+    V t[6];
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+      const V v = P[(f * CB + ci) * NZ + kg];
+      t[f] = mk2<R>(norm * v.x, norm * v.y);
+    }
+    const V t11 = t[0], t12 = t[1], t13 = t[2], t22 = t[3], t23 = t[4], t33 = t[5];
+    const R a = (R)(g.alp * i);
+    const int kzs = (k <= nz) ? k : k - mz;
+    const R gz = (R)(g.gam * kzs);
+    const R a2 = a * a, g2 = gz * gz;
+    // products of the imaginary wavenumbers: 2 xalp xgam, xalp xgam
+    const R m2ag = -(((R)2 * a) * gz), mag = -(a * gz);
+    const R ak = a2 + g2, ga = -g2 + a2;
+    const long q = (long)k * nkx + i;
+    // rhvc1, rhvc2, rhgc1, rhgc2 (cross.f90:1398-1403)
+    const V rv1 = mk2<R>(a2 * t11.x - m2ag * t13.x + g2 * t33.x - ak * t22.x,
+                         a2 * t11.y - m2ag * t13.y + g2 * t33.y - ak * t22.y);
+    const V rv2 = mk2<R>((-a * t12.y) + (-gz * t23.y), (a * t12.x) + (gz * t23.x));
+    const V rg1 = mk2<R>(mag * (t11.x - t33.x) + ga * t13.x, mag * (t11.y - t33.y) + ga * t13.y);
+    const V rg2 = mk2<R>((-gz * t12.y) - (-a * t23.y), (gz * t12.x) - (a * t23.x));
+    // dvordy - rhvc1 (cross.f90:561-564), hg + rhgc1 (cross.f90:608)
+    V d = Dv[q];
+    Dv[q] = mk2<R>(d.x - rv1.x, d.y - rv1.y);
+    V h = Gv[q];
+    Gv[q] = mk2<R>(h.x + rg1.x, h.y + rg1.y);
+    L1[q] = rv2;
+    L2[q] = rg2;
+    if (i == 0 && k == 0) ((V *)bf.txy)[(long)b * g.my + j] = mk2<R>(t12.x, t23.x);
+  }
+}
+
 // pencil (j fastest, then kx, then kz, FP64 host layout) <-> plane-major
 // device layout of storage type R, one box
 template <typename R>
@@ -462,6 +770,76 @@ static cudaError_t launch_plane_t(const Grid &g, const Bufs &bf, int stage, int 
 cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
   return g.prec ? launch_plane_t<float>(g, bf, stage, rk, st)
                 : launch_plane_t<double>(g, bf, stage, rk, st);
+}
+
+// LES launches: stage 2..5 = k_les2..k_les5 of substep rk; stage 0 sets the
+// kernels' shared-memory limits
+template <typename R, int NX, int T>
+static cudaError_t launch_les_x(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st,
+                                bool prep) {
+  typedef typename Vec2<R>::t V;
+  dim3 grid(g.mgalz / 2, g.my, g.B);
+  const size_t sm = sizeof(V) * 2 * (6 * NX);
+  if (prep) {
+    cudaFuncSetAttribute(k_les2<R, NX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaFuncSetAttribute(k_les4<R, NX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    return cudaGetLastError();
+  }
+  if (stage == 2)
+    k_les2<R, NX, T><<<grid, T, sm, st>>>(g, bf);
+  else
+    k_les4<R, NX, T><<<grid, T, sm, st>>>(g, bf, rk);
+  return cudaGetLastError();
+}
+
+template <typename R, int NZ, int CB>
+static cudaError_t launch_les_z(const Grid &g, const Bufs &bf, int stage, cudaStream_t st,
+                                bool prep) {
+  typedef typename Vec2<R>::t V;
+  const size_t sm3 = sizeof(V) * 2 * (8 * NZ), sm5 = sizeof(V) * 2 * (6 * CB * NZ);
+  if (prep) {
+    cudaFuncSetAttribute(k_les3<R, NZ, 8, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+    cudaFuncSetAttribute(k_les5<R, NZ, CB, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm5);
+    return cudaGetLastError();
+  }
+  if (stage == 3)
+    k_les3<R, NZ, 8, 128><<<dim3((g.nkx + 7) / 8, g.my, g.B), 128, sm3, st>>>(g, bf);
+  else
+    k_les5<R, NZ, CB, 128><<<dim3(g.ncbl, g.my, g.B), 128, sm5, st>>>(g, bf);
+  return cudaGetLastError();
+}
+
+int les_cb(int mgalz) { return mgalz >= 192 ? 2 : 4; }
+
+template <typename R>
+static cudaError_t launch_les_t(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
+  const bool prep = (stage == 0);
+  if (prep || stage == 2 || stage == 4) {
+    cudaError_t e;
+    switch (g.mgalx) {
+      case 32: e = launch_les_x<R, 32, 64>(g, bf, stage, rk, st, prep); break;
+      case 48: e = launch_les_x<R, 48, 64>(g, bf, stage, rk, st, prep); break;
+      case 64: e = launch_les_x<R, 64, 96>(g, bf, stage, rk, st, prep); break;
+      case 96: e = launch_les_x<R, 96, 96>(g, bf, stage, rk, st, prep); break;
+      case 192: e = launch_les_x<R, 192, 128>(g, bf, stage, rk, st, prep); break;
+      case 384: e = launch_les_x<R, 384, 256>(g, bf, stage, rk, st, prep); break;
+      default: return cudaErrorInvalidValue;
+    }
+    if (!prep || e != cudaSuccess) return e;
+  }
+  switch (g.mgalz) {
+    case 32: return launch_les_z<R, 32, 4>(g, bf, stage, st, prep);
+    case 48: return launch_les_z<R, 48, 4>(g, bf, stage, st, prep);
+    case 64: return launch_les_z<R, 64, 4>(g, bf, stage, st, prep);
+    case 96: return launch_les_z<R, 96, 4>(g, bf, stage, st, prep);
+    case 192: return launch_les_z<R, 192, 2>(g, bf, stage, st, prep);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_les(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
+  return g.prec ? launch_les_t<float>(g, bf, stage, rk, st)
+                : launch_les_t<double>(g, bf, stage, rk, st);
 }
 
 cudaError_t launch_pencil_to_plane(const Grid &g, const double *pen, double *dst, cudaStream_t st) {

@@ -273,6 +273,66 @@ __global__ void __launch_bounds__(32 * kSeg) k_lineB(Grid g, Bufs bf, int mode) 
   store_col(ys, ystr, (R *)bf.V + off, ps, L);
 }
 
+// LES y-operators (iuse_LES, cross.f90:565-608,639-647), between k_tables and
+// k_lineA:
+//   role 0: hg += d(rhgc2)/dy                       (derivyc, -> G)
+//   role 1: hv += (kx^2 + kz^2 - d2/dy2)(-rhvc2), i.e. visc3d(rhvc2, hv,
+//           rk = -(kx^2 + kz^2), fac = -1)          (-> V)
+//   mean:   rf0u += d(T12_00)/dy, rf0w += d(T23_00)/dy
+template <typename R>
+__global__ void __launch_bounds__(32 * kSeg) k_lineL(Grid g, Bufs bf) {
+  __shared__ double xch[kSeg][16][2][SB_XS];
+  LineThread L;
+  if (!line_thread(g, 2, &L)) return;
+  const Member &M = bf.mem[L.b];
+  if (M.halted) return;
+  const int N = g.my, ystr = blockDim.x;
+  double *ys = ycol();
+  const FacView V1(bf.d1, 0), V2(bf.d2, 0);
+  const SegView W1(bf.d1, 0), W2(bf.d2, 0);
+  if (L.mean) {
+    const R *tx = (const R *)bf.txy + (long)L.b * 2 * N + L.c;
+    R *mrf = (R *)bf.mrf + (long)L.b * 2 * N + L.c;
+    const cd one = mk(1.0, 0.0);
+    const Tail T1 = load_tail(bf.tl1o + (long)L.b * g.nkx * SB_TAIL);
+    SEG_SOLVE(tx, 2, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true);
+    if (L.active)
+      for (int i = L.r0; i <= L.r1; i++)
+        mrf[2 * (i - 1)] = mrf[2 * (i - 1)] + (R)ys[(i - L.r0) * ystr];
+    return;
+  }
+  const long off = (long)L.b * g.field + 2 * L.lc + L.c;
+  const long ps = g.plane;
+  const int i = L.i, k = L.k;
+  const cd shp = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * i);
+  const cd shm = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
+  if (L.role == 0) {
+    const Tail T1 = load_tail(bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL);
+    SEG_SOLVE((const R *)bf.L2 + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5], g.rh1[6],
+              true);
+    R *G = (R *)bf.G + off;
+    if (L.active)
+      for (int r = L.r0; r <= L.r1; r++) {
+        const long q = (long)(r - 1) * ps;
+        G[q] = G[q] + (R)ys[(r - L.r0) * ystr];
+      }
+    return;
+  }
+  const Tail T2 = load_tail(bf.tl2o + ((long)L.b * g.nkx + i) * SB_TAIL);
+  const R *u = (const R *)bf.L1 + off;
+  SEG_SOLVE(u, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6], false);
+  if ((i == 0 && k == 0) || !L.active) return;
+  const double a = g.alp * i;
+  const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
+  const double rk = -(gz * gz + a * a);
+  R *Vv = (R *)bf.V + off;
+  for (int r = L.r0; r <= L.r1; r++) {
+    const long q = (long)(r - 1) * ps;
+    const double t = -(rk * (double)u[q]) + ys[(r - L.r0) * ystr];
+    Vv[q] = Vv[q] + (R)(-1.0 * t);
+  }
+}
+
 // set_conj on the state (operators.f90:1382-1429) at entry of a cross call
 template <typename R>
 __global__ void k_setconj(Grid g, Bufs bf) {
@@ -301,8 +361,10 @@ __global__ void k_setconj(Grid g, Bufs bf) {
 __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
   const int b = blockIdx.x;
   Member &M = bf.mem[b];
-  __shared__ double s_q[SB_NHIST_Q + 1];
-  __shared__ double s_part[SB_NHIST_Q + 1][256 / 32];
+  // per-plane sums: SB_NHIST_Q hist partials, Pk, and with LES nu_t and nu_t |S|^2
+  constexpr int NQ = SB_NHIST_Q + 3;
+  __shared__ double s_q[NQ];
+  __shared__ double s_part[NQ][256 / 32];
   __shared__ int s_halt;
   if (threadIdx.x == 0) {
     if (rk == 0) {  // entry of a cross() call (cross.f90:76-113)
@@ -314,6 +376,7 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
       M.ntrace = 0;
       M.flags = 0;
       for (int q = 0; q < 4; q++) M.umax_bits[q] = 0ull;
+      M.nut_bits = 0ull;
       M.xwb[0] = M.xoffb;
       M.xwt[0] = M.xofft;
     }
@@ -326,9 +389,11 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
   if (hist) {
     // hist 'w': sum over planes of the per-block partials (cross.f90:2070-2080)
     // and the production Pk, whose mean omega_z includes -s (cross.f90:1901-1912)
-    const int nq = SB_NHIST_Q + 1;
-    double acc[SB_NHIST_Q + 1];
+    const int nq = NQ;
+    double acc[NQ];
     for (int q = 0; q < nq; q++) acc[q] = 0.0;
+    const double nufac = g.les_visc ? (1.0 / M.Re) : 0.0;
+    const double nxz = (double)(g.mgalx * g.mgalz);
     for (int j = threadIdx.x; j < g.my; j += blockDim.x) {
       const double *hp = bf.hpart + ((long)b * g.my + j) * g.ncb * SB_NHIST_Q;
       double pl[SB_NHIST_Q];
@@ -339,7 +404,23 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
       const double du = g.prec ? (double)((const float *)bf.mdu)[2 * ((long)b * g.my + j)]
                                : bf.mdu[2 * ((long)b * g.my + j)];
       const double o3 = -du - g.s;
-      acc[SB_NHIST_Q] += -o3 * (-pl[3]) + (o3 * o3) * (1.0 / M.Re);
+      if (g.les) {
+        // Pk with the resolved mean stress (cross.f90:1886-1899), nu_t and the
+        // energy transfer to the subgrid scales (cross.f90:1892,1950-1952)
+        const double txy = g.prec ? (double)((const float *)bf.txy)[2 * ((long)b * g.my + j)]
+                                  : bf.txy[2 * ((long)b * g.my + j)];
+        acc[SB_NHIST_Q] += -(o3 * (-pl[3] + txy)) + nufac * (o3 * o3);
+        const double *lp = bf.lpart + ((long)b * g.my + j) * (g.mgalz / 2) * 2;
+        double sn = 0.0, sd = 0.0;
+        for (int zp = 0; zp < g.mgalz / 2; zp++) {
+          sn += lp[2 * zp];
+          sd += lp[2 * zp + 1];
+        }
+        acc[SB_NHIST_Q + 1] += sn / nxz;
+        acc[SB_NHIST_Q + 2] += sd / nxz;
+      } else {
+        acc[SB_NHIST_Q] += -o3 * (-pl[3]) + (o3 * o3) * (1.0 / M.Re);
+      }
     }
     for (int q = 0; q < nq; q++) {
       double v = acc[q];
@@ -363,16 +444,33 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
       const double v = __longlong_as_double((long long)M.umax_bits[q]);
       M.umax[q] = v > uinit ? v : uinit;
     }
+    if (g.les) {
+      // running maximum of |nu_t| (cross.f90:1430-1436, 1604)
+      const double v = __longlong_as_double((long long)M.nut_bits);
+      if (v > M.max_nut) M.max_nut = v;
+    }
+    const double nutmax = M.max_nut;
+    const double vv = fmax(fmax(g.pi * g.pi / g.dx / g.dx, 6.25 / g.dy / g.dy), g.pi * g.pi / g.dz / g.dz);
     double dt;
     if (M.fixed_dt > 0.0) {
       dt = M.fixed_dt;
       const double m = fmax(fmax(M.umax[0] * g.pi / g.dx, M.umax[2] * 2.5 / g.dy), M.umax[3] * g.pi / g.dz);
       M.CFLcur = dt * m;
-      const double vv = fmax(fmax(g.pi * g.pi / g.dx / g.dx, 6.25 / g.dy / g.dy), g.pi * g.pi / g.dz / g.dz);
-      M.CFLv = (1.0 / M.Re) * dt * vv;
+      if (g.les) {
+        // cross.f90:1620-1635
+        const double vn = 2.0 * nutmax * dt * vv;
+        M.CFLv = g.les_visc ? fmax(fabs(1.0 / M.Re) * dt * vv, vn) : vn;
+      } else {
+        M.CFLv = (1.0 / M.Re) * dt * vv;
+      }
     } else {
       const double m = fmax(fmax(M.umax[0] * M.cflx, M.umax[2] * M.cfly), M.umax[3] * M.cflz);
       dt = 1.0 / m;
+      if (g.les) {
+        // cross.f90:1652-1666
+        const double vn = nutmax / M.CFL * vv;
+        M.cflvv = g.les_visc ? fmax(fabs(1.0 / M.Re) / M.CFL * vv, vn) : vn;
+      }
       M.CFLcur = M.CFL;
       M.CFLv = M.CFL * M.cflvv * dt;
       if (M.CFLv > M.CFL) dt = 1.0 / M.cflvv;
@@ -405,8 +503,8 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
       uner[9] = s_q[10] / my;
       uner2[0] = s_q[SB_NHIST_Q] / my;
       uner2[1] = s_q[9] / my;
-      uner2[2] = 0.0;
-      uner2[3] = 0.0;
+      uner2[2] = g.les ? s_q[SB_NHIST_Q + 1] / my : 0.0;
+      uner2[3] = g.les ? s_q[SB_NHIST_Q + 2] / my : 0.0;
       if (M.ntrace < M.trace_cap) {
         double *rec = bf.trace + ((long)b * M.trace_cap + M.ntrace) * SB_TRACE_LEN;
         rec[0] = M.time;
@@ -524,6 +622,7 @@ __global__ void k_finish(Grid g, Bufs bf) {
   if ((M.istep - 1) != 1 && M.istop) M.halted = 1;
   if ((M.istep - 1) % M.nhist == 0) M.ihist = 1;
   for (int q = 0; q < 4; q++) M.umax_bits[q] = 0ull;
+  M.nut_bits = 0ull;
 }
 
 // ---------------------------------------------------------------------------
@@ -544,6 +643,8 @@ cudaError_t prepare_line(const Grid &g) {
   cudaFuncSetAttribute(k_lineB<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   cudaFuncSetAttribute(k_lineA<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   cudaFuncSetAttribute(k_lineB<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_lineL<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_lineL<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   return cudaGetLastError();
 }
 
@@ -564,6 +665,15 @@ cudaError_t launch_lineB(const Grid &g, const Bufs &bf, int mode, cudaStream_t s
     k_lineB<float><<<nb, kLineT, line_smem(g), st>>>(g, bf, mode);
   else
     k_lineB<double><<<nb, kLineT, line_smem(g), st>>>(g, bf, mode);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lineL(const Grid &g, const Bufs &bf, cudaStream_t st) {
+  const unsigned nb = (unsigned)(g.B * (2 * g.ngrp + 1));
+  if (g.prec)
+    k_lineL<float><<<nb, kLineT, line_smem(g), st>>>(g, bf);
+  else
+    k_lineL<double><<<nb, kLineT, line_smem(g), st>>>(g, bf);
   return cudaGetLastError();
 }
 
