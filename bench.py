@@ -12,6 +12,7 @@ step (three substeps) of that box.
   roofline  the dominant kernel (plane stage 2), timed alone with CUDA events:
          FP64 rate against the FP64 FMA peak measured in the same run (the
          binding roof on GB300) and bytes against the measured HBM copy peak.
+  les     Smagorinsky LES on 384x192x192 (Re_z=20000), FP32-mixed vs FP64.
   newton  batched Newton Jv/s: 32 finite-difference products on 96x48x48
          (Re_z=1200, T=20/S) as one FP32-mixed batch (central differences)
          vs one FP64 product at a time.
@@ -247,6 +248,54 @@ def ensemble_leg(sb, torch, dist, ws, rank, args, nbox=64, nsteps=200):
             "max_member_rel_l2_err_vs_fp64": err, "re_z_range": [500.0, 2000.0]}
 
 
+def les_leg(sb, torch, dist, ws, rank, args):
+    """LES mode: Smagorinsky eddy viscosity (Cs = 0.1, filter width
+    (dx dy dz)^(1/3)) on 384x192x192, Re_z = 20000, k0 = 6, CFL = 0.5, FP32-mixed,
+    args.les_steps steps from the seeded field, against the same run in FP64 on
+    the GPU: steps/s of both (CUDA events, state in HBM) and the relative
+    deviation of the velocity variances (u', v', w' rms) and the Reynolds shear
+    stress <uv> of the last statistics record, plus the simulated time span
+    against the shear-periodic remesh period St = Lx/Ly."""
+    pp = dict(mgalx=384, my=192, mgalz=192, Re=20000.0 / LZ ** 2, alp=0.5, Ly=LZ, gam=1.0,
+              s=1.0, chi=0.0, CFL=0.5, les=1, les_visc=1, cs=0.1)
+    p = sb.make_params(**pp)
+    st0 = sb.seed_state(p, 6 + rank, k0=6.0)
+    n = args.les_steps
+    out = {"grid": [384, 192, 192], "re_z": 20000.0, "cs": 0.1, "k0": 6.0, "steps": n}
+    recs = {}
+    for key, prec in (("mixed", sb.SB_MIXED), ("fp64", sb.SB_FP64)):
+        box = sb.ShearBox(p, precision=prec)
+        box.set_state(st0)
+        box.step(3)
+        box.sync()
+        box.set_state(st0)
+        stream = torch.cuda.ExternalStream(box.stream)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        barrier(dist)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        box.step(n)
+        e1.record(stream)
+        e1.synchronize()
+        ms = allmax(dist, e0.elapsed_time(e1))
+        st = box.status()
+        tr = box.trace(0)
+        recs[key] = tr
+        out[key] = {"value": ws * n / (ms * 1e-3), "unit": "steps/s", "ms_per_step": ms / n,
+                    "time_span": st.time, "steps_done": st.steps_done}
+        del box
+    a, b = recs["mixed"][-1], recs["fp64"][-1]
+    out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["rel_dev_vs_fp64_last_record"] = {
+        "u_rms": float(abs(a[2] - b[2]) / abs(b[2])), "v_rms": float(abs(a[3] - b[3]) / abs(b[3])),
+        "w_rms": float(abs(a[4] - b[4]) / abs(b[4])), "uv": float(abs(a[5] - b[5]) / abs(b[5])),
+        "nu_t_mean": float(abs(a[22] - b[22]) / abs(b[22]))}
+    out["remesh_period_St"] = (2 * np.pi / 0.5) / LZ
+    out["precision"] = "FP32-mixed (FP64 y-solves, Helmholtz, phases)"
+    return out
+
+
 def newton_leg(sb, torch, dist, ws, rank, args, nper=32, T=20.0):
     """Batched Newton Jv: the Jacobian-vector products of the periodic-orbit
     search on 96x48x48 (Re_z=1200, period T=20/S) through the Newton tools'
@@ -450,6 +499,7 @@ def run_ours(args):
                               "compact y-solves, Helmholtz solve, phase factors"}
     ensemble = None if args.no_ensemble else ensemble_leg(sb, torch, dist, ws, rank, args)
     newton = None if args.no_newton else newton_leg(sb, torch, dist, ws, rank, args)
+    les = None if args.no_les else les_leg(sb, torch, dist, ws, rank, args)
     if rank != 0:
         return
     cpu = cpu_baseline(args.cpu_steps, os.cpu_count() or 1) if ws == 1 or rank == 0 else None
@@ -481,6 +531,7 @@ def run_ours(args):
         "mixed": mixed,
         "ensemble": ensemble,
         "newton": newton,
+        "les": les,
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "clocks": clk,
     }
@@ -499,6 +550,8 @@ def main():
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble leg")
     ap.add_argument("--no-newton", action="store_true", help="skip the batched Newton Jv leg")
+    ap.add_argument("--no-les", action="store_true", help="skip the LES leg")
+    ap.add_argument("--les-steps", type=int, default=500, help="steps of the LES leg")
     ap.add_argument("--lite", action="store_true",
                     help="profiling only: time the steps, skip e2e / CPU / per-kernel legs")
     args = ap.parse_args()
