@@ -52,6 +52,9 @@ typedef struct sb_params {
   int les_visc;                /* iadd_visc: keep the molecular viscosity with the model */
   double cs;                   /* Cles, Smagorinsky constant; filter width
                                   (dx*dy*dz)^(1/3) (initcr.f90:510) */
+  int ydeal;                   /* iydealiasing: 0 none (default), 3 compact y-filter
+                                  of the state at every substep (cross.f90:214-227,
+                                  476-490; filter_shear_hepta.f90:21-148) */
 } sb_params;
 
 /* Per-box status after sb_step (cross.f90 istop logic, 1683-1690, 2102-2115) */

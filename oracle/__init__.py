@@ -46,7 +46,7 @@ class OrcParams(ctypes.Structure):
         ("readflag", ctypes.c_int), ("uprim", ctypes.c_double), ("nhist", ctypes.c_int),
         ("etime", ctypes.c_double), ("dumptime", ctypes.c_double), ("dtimag", ctypes.c_double),
         ("keep_laminar", ctypes.c_int), ("les", ctypes.c_int), ("les_visc", ctypes.c_int),
-        ("cs", ctypes.c_double),
+        ("cs", ctypes.c_double), ("ydeal", ctypes.c_int),
     ]
 
 
@@ -72,6 +72,8 @@ def lib():
         L.orc_derivyc.argtypes = [ctypes.c_void_p, dp, dp] + [ctypes.c_double] * 4 + [ctypes.c_int] * 2
         L.orc_lapcdy.argtypes = [ctypes.c_void_p, dp, ctypes.c_double, dp] + [ctypes.c_double] * 4 + [ctypes.c_int]
         L.orc_fourxz.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_int]
+        L.orc_filterc.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_int]
         L.orc_fft.argtypes = [ctypes.c_int, dp, ctypes.c_int]
         _lib = L
     return _lib
@@ -99,10 +101,10 @@ class Oracle:
     def __init__(self, mgalx, my, mgalz, Re, alp, Ly, gam, s=1.0, chi=0.0, CFL=0.5,
                  vbulk=0.0, fixed_dt=0.0, readflag=1, uprim=1.0, nhist=1,
                  etime=1e10, dumptime=1e10, dtimag=1e10, keep_laminar=0, les=0, les_visc=1,
-                 cs=0.1):
+                 cs=0.1, ydeal=0):
         self.p = OrcParams(mgalx, my, mgalz, Re, alp, Ly, gam, s, chi, CFL, vbulk, fixed_dt,
                            readflag, uprim, nhist, etime, dumptime, dtimag, keep_laminar, les,
-                           les_visc, cs)
+                           les_visc, cs, ydeal)
         self.h = lib().orc_create(ctypes.byref(self.p))
         sz = (ctypes.c_int * 8)()
         lib().orc_sizes(self.h, sz)
@@ -133,6 +135,19 @@ class Oracle:
         a = np.ascontiguousarray(u, dtype=np.float64)
         out = np.zeros_like(a)
         lib().orc_derivyc(self.h, _dp(a), _dp(out), 1.0, 0.0, 1.0, 0.0, iord, 1)
+        return out
+
+    def filterc(self, u: np.ndarray, shp=1.0 + 0j) -> np.ndarray:
+        """The compact y-filter of one line (complex: shear phase shp)."""
+        if np.iscomplexobj(u):
+            a = np.ascontiguousarray(u, dtype=np.complex128)
+            out = np.zeros_like(a)
+            lib().orc_filterc(self.h, _dp(a.view(np.float64)), _dp(out.view(np.float64)),
+                              shp.real, shp.imag, 2)
+            return out
+        a = np.ascontiguousarray(u, dtype=np.float64)
+        out = np.zeros_like(a)
+        lib().orc_filterc(self.h, _dp(a), _dp(out), 1.0, 0.0, 1)
         return out
 
     def lapcdy(self, u: np.ndarray, k2: float, shp=1.0 + 0j, shm=None) -> np.ndarray:

@@ -167,6 +167,9 @@ typedef struct { /* THREADPRIVATE scratch of module yderiv (diffy_shear_hepta.f9
   cplx *eh, *fh, *gh, *ceh, *cfh, *cgh;
   cplx *wk1, *wk2, *ur, *uc, *duc, *pc;
   double lapmat[7];
+  /* scratch of module yfilter (filter_shear_hepta.f90:1-17) */
+  double *fdh, *fdhm1;
+  cplx *feh, *ffh, *fgh, *fceh, *fcfh, *fcgh, *fur, *fuc, *fwk1, *fwk2, *fduc;
 } ythread;
 
 typedef struct { /* per-thread plane buffers for hvhg */
@@ -194,6 +197,11 @@ typedef struct {
   int nthr;
   ythread *yt;
   pthread_buf *pt;
+  /* compact y-filter (prefilter, filter_shear_hepta.f90:21-100): LHS fpr(-3:3),
+   * RHS frh(-4:4) and the unshifted LDL^H factors of the LHS */
+  double fpr[7], frh[9];
+  double *fa, *fb, *fc, *fd, *fdm1;
+  cplx *fe, *ff, *fg, *fce, *fcf, *fcg;
   double Deltag;  /* LES grid-filter width (dx*dy*dz)^(1/3), initcr.f90:510 */
   double max_nut; /* LES running maximum of |nuSGS| (module LES; cross.f90:1433
                    * never resets it, so it spans every call on this context) */
@@ -747,6 +755,55 @@ static void lapcdy(ctx *c, ythread *t, const double *u, double k2, double *p, cp
   }
 }
 
+/* filterc (filter_shear_hepta.f90:104-148): 9-point symmetric right-hand side
+ * (matvecNcyclic, diffy_shear_hepta.f90:960-996, which replaces shm by
+ * conj(shp) for complex lines) over the cyclic heptadiagonal left-hand side;
+ * ias = 1 rebuilds the shear tail of the factors for shp. */
+static void filterc(ctx *c, ythread *t, const double *u, double *du, cplx shp, int m, int ias) {
+  int my = c->my;
+  cplx *uc = t->fuc, *ur = t->fur, *wk1 = t->fwk1;
+  for (int j = 1; j <= my; j++) uc[j] = (m == 1) ? C(u[j - 1], 0.0) : C(u[2 * (j - 1)], u[2 * (j - 1) + 1]);
+  cplx shm = cconj(shp);
+  for (int q = 1; q <= 4; q++) {
+    ur[q] = (m == 1) ? uc[my - 4 + q] : cmul(uc[my - 4 + q], shm);
+    ur[my + 4 + q] = (m == 1) ? uc[q] : cmul(uc[q], shp);
+  }
+  for (int j = 1; j <= my; j++) ur[4 + j] = uc[j];
+  for (int j = 5; j <= my + 4; j++) {
+    cplx s = C(0.0, 0.0);
+    for (int d = -4; d <= 4; d++) s = cadd(s, cscal(c->frh[4 + d], ur[j + d]));
+    wk1[j - 4] = s;
+  }
+  if (m == 1) {
+    solve7(c->fa, c->fb, c->fc, c->fdm1, c->fe, c->ff, c->fg, c->fce, c->fcf, c->fcg, wk1,
+           t->fduc, t->fwk2, my);
+    for (int j = 1; j <= my; j++) du[j - 1] = t->fduc[j].re;
+    return;
+  }
+  if (ias == 1) {
+    for (int j = 1; j <= my; j++) {
+      t->fdh[j] = c->fd[j];
+      t->fdhm1[j] = c->fdm1[j];
+      t->feh[j] = (j <= my - 6) ? cscal(c->fe[j].re, shp) : c->fe[j];
+      t->ffh[j] = (j <= my - 5) ? cscal(c->ff[j].re, shp) : c->ff[j];
+      t->fgh[j] = (j <= my - 4) ? cscal(c->fg[j].re, shp) : c->fg[j];
+    }
+    modchol_addshear(c->fa, c->fb, c->fc, t->fdh, t->fdhm1, t->feh, t->ffh, t->fgh, t->fceh,
+                     t->fcfh, t->fcgh, c->fpr, my);
+  }
+  solve7(c->fa, c->fb, c->fc, t->fdhm1, t->feh, t->ffh, t->fgh, t->fceh, t->fcfh, t->fcgh, wk1,
+         t->fduc, t->fwk2, my);
+  for (int j = 1; j <= my; j++) {
+    du[2 * (j - 1)] = t->fduc[j].re;
+    du[2 * (j - 1) + 1] = t->fduc[j].im;
+  }
+}
+
+void orc_filterc(void *h, const double *u, double *du, double spr, double spi, int m) {
+  ctx *c = (ctx *)h;
+  filterc(c, &c->yt[0], u, du, C(spr, spi), m, 1);
+}
+
 /* visc3d (diffy_shear_hepta.f90:298-318), what = '+' */
 static void visc3d(ctx *c, ythread *t, const double *u, double *visc, double *ddu,
                    cplx shp, cplx shm, int m, double rk, double scal, int ias) {
@@ -765,11 +822,19 @@ static void ythread_alloc(ythread *t, int my) {
   t->ceh = zalloc(my + 1); t->cfh = zalloc(my + 1); t->cgh = zalloc(my + 1);
   t->wk1 = zalloc(my + 1); t->wk2 = zalloc(my + 1); t->ur = zalloc(my + 7);
   t->uc = zalloc(my + 1); t->duc = zalloc(my + 1); t->pc = zalloc(my + 1);
+  t->fdh = dalloc(my + 1); t->fdhm1 = dalloc(my + 1);
+  t->feh = zalloc(my + 1); t->ffh = zalloc(my + 1); t->fgh = zalloc(my + 1);
+  t->fceh = zalloc(my + 1); t->fcfh = zalloc(my + 1); t->fcgh = zalloc(my + 1);
+  t->fur = zalloc(my + 9); t->fuc = zalloc(my + 1); t->fwk1 = zalloc(my + 1);
+  t->fwk2 = zalloc(my + 1); t->fduc = zalloc(my + 1);
 }
 static void ythread_free(ythread *t) {
   free(t->ah); free(t->bh); free(t->ch); free(t->dh); free(t->dhm1);
   free(t->eh); free(t->fh); free(t->gh); free(t->ceh); free(t->cfh); free(t->cgh);
   free(t->wk1); free(t->wk2); free(t->ur); free(t->uc); free(t->duc); free(t->pc);
+  free(t->fdh); free(t->fdhm1); free(t->feh); free(t->ffh); free(t->fgh);
+  free(t->fceh); free(t->fcfh); free(t->fcgh); free(t->fur); free(t->fuc); free(t->fwk1);
+  free(t->fwk2); free(t->fduc);
 }
 
 void *orc_create(const orc_params *p) {
@@ -810,6 +875,20 @@ void *orc_create(const orc_params *p) {
            c->cg1, c->pr1, my, C(1.0, 0.0));
   modchol7(c->a2, c->b2, c->c2, c->d2, c->d2m1, c->e2, c->f2, c->g2, c->ce2, c->cf2,
            c->cg2, c->pr2, my, C(1.0, 0.0));
+  /* prefilter (filter_shear_hepta.f90:55-85): fixed coefficients, unscaled */
+  {
+    static const double lhs[4] = {1.0, 0.738981897704866, 0.315003368623046, 0.053003478448814};
+    static const double rhs[5] = {0.987412035368317, 0.749052269410218, 0.309968182770373,
+                                  0.054442102978149, -0.000179828066167};
+    for (int d = 0; d <= 3; d++) c->fpr[3 + d] = c->fpr[3 - d] = lhs[d];
+    for (int d = 0; d <= 4; d++) c->frh[4 + d] = c->frh[4 - d] = rhs[d];
+    c->fa = dalloc(my + 1); c->fb = dalloc(my + 1); c->fc = dalloc(my + 1);
+    c->fd = dalloc(my + 1); c->fdm1 = dalloc(my + 1);
+    c->fe = zalloc(my + 1); c->ff = zalloc(my + 1); c->fg = zalloc(my + 1);
+    c->fce = zalloc(my + 1); c->fcf = zalloc(my + 1); c->fcg = zalloc(my + 1);
+    modchol7(c->fa, c->fb, c->fc, c->fd, c->fdm1, c->fe, c->ff, c->fg, c->fce, c->fcf, c->fcg,
+             c->fpr, my, C(1.0, 0.0));
+  }
   /* set_xyz_dy (initcr.f90:443-519) */
   double alp = p->alp, gam = p->gam, CFL = p->CFL;
   c->Lx = c->pi2 / alp;
@@ -900,6 +979,8 @@ void orc_destroy(void *h) {
   free(c->e1); free(c->f1); free(c->g1); free(c->ce1); free(c->cf1); free(c->cg1);
   free(c->a2); free(c->b2); free(c->c2); free(c->d2); free(c->d2m1);
   free(c->e2); free(c->f2); free(c->g2); free(c->ce2); free(c->cf2); free(c->cg2);
+  free(c->fa); free(c->fb); free(c->fc); free(c->fd); free(c->fdm1);
+  free(c->fe); free(c->ff); free(c->fg); free(c->fce); free(c->fcf); free(c->fcg);
   plan_free(&c->px);
   plan_free(&c->pz);
   free(c);
@@ -1366,6 +1447,21 @@ static void to_pencil(ctx *c, const cplx *pl, double *pen) {
     }
 }
 
+/* iydealiasing = 3: the compact filter on the state (cross.f90:214-227,476-490) */
+static void filter_state(ctx *c, double *vor, double *phi, double *u00, double *w00,
+                         const cplx *shwkt) {
+  int my = c->my, nkx = c->nkx, mz = c->mz;
+  filterc(c, &c->yt[0], u00, u00, C(1.0, 0.0), 1, 0);
+  filterc(c, &c->yt[0], w00, w00, C(1.0, 0.0), 1, 0);
+#pragma omp parallel for schedule(static)
+  for (int ik = 0; ik < nkx * mz; ik++) {
+    int i = ik % nkx, k = ik / nkx;
+    ythread *t = &c->yt[my_thread()];
+    filterc(c, t, PEN(vor, i, k), PEN(vor, i, k), shwkt[i], 2, 1);
+    filterc(c, t, PEN(phi, i, k), PEN(phi, i, k), shwkt[i], 2, 0);
+  }
+}
+
 int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, double *ptime,
               double *pxoffb, double *pxofft, int nstep, double *trace, int *ntrace,
               int *pistop, double *pdeltat) {
@@ -1408,6 +1504,9 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
   double umax[4] = {0, 0, 0, 0}, CFL = c->p.CFL, CFLv = 0.0;
   /* entry: set_conj on the state (cross.f90:283-287) */
   set_conj_pencil(c, vor, phi);
+  /* iydealiasing = 3 at entry (cross.f90:214-227), with the phase work array
+   * of a fresh run (initcr.f90:370) */
+  if (c->p.ydeal == 3) filter_state(c, vor, phi, u00, w00, shwkt);
   for (int istep = 1; istep <= nstep; istep++) {
     if ((istep - 1) % nhist == 0) ihist = 1;
     xwkt = xofft;
@@ -1449,6 +1548,9 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
         derivyc(c, t, PEN(vor, i, k), PEN(dvordy, i, k), shwkt[i], shwkb[i], 1, 2, 1);
         derivyc(c, t, PEN(hg, i, k), PEN(hv, i, k), shwkt[i], shwkb[i], 1, 2, 0);
       }
+      /* iydealiasing = 3 on the state after the first derivatives
+       * (cross.f90:476-490) */
+      if (c->p.ydeal == 3) filter_state(c, vor, phi, u00, w00, shwkt);
       to_plane(c, phi, b1);
       to_plane(c, vor, b2);
       /* set_conj on the copies (cross.f90:502) */

@@ -38,6 +38,7 @@ typedef struct orc_params {
   int les;                /* iuse_LES: Smagorinsky model (cross.f90:1291-1406) */
   int les_visc;           /* iadd_visc: molecular viscosity kept with the model */
   double cs;              /* Cles, the Smagorinsky constant (initcr.f90:1964,2148) */
+  int ydeal;              /* iydealiasing: 0 none, 3 compact y-filter (cross.f90:214-227,476-490) */
 } orc_params;
 
 /* one .cfbin record per statistics step (cross.f90:2087):
@@ -60,6 +61,7 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00,
               double *trace, int *ntrace, int *istop, double *deltat);
 
 /* building blocks, one y-line (complex: m=2, real: m=1) */
+void orc_filterc(void *h, const double *u, double *du, double shp_re, double shp_im, int m);
 void orc_derivyc(void *h, const double *u, double *du, double shp_re,
                  double shp_im, double shm_re, double shm_im, int iord, int m);
 void orc_lapcdy(void *h, const double *u, double k2, double *p, double shp_re,

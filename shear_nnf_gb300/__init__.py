@@ -35,7 +35,7 @@ class SbParams(ctypes.Structure):
         ("readflag", ctypes.c_int), ("uprim", ctypes.c_double), ("nhist", ctypes.c_int),
         ("etime", ctypes.c_double), ("dumptime", ctypes.c_double), ("dtimag", ctypes.c_double),
         ("keep_laminar", ctypes.c_int), ("les", ctypes.c_int), ("les_visc", ctypes.c_int),
-        ("cs", ctypes.c_double),
+        ("cs", ctypes.c_double), ("ydeal", ctypes.c_int),
     ]
 
 
@@ -119,9 +119,9 @@ def _dp(a: np.ndarray):
 
 def make_params(mgalx, my, mgalz, Re, alp, Ly, gam, s=1.0, chi=0.0, CFL=0.5, vbulk=0.0,
                 fixed_dt=0.0, readflag=1, uprim=1.0, nhist=1, etime=1e10, dumptime=1e10,
-                dtimag=1e10, keep_laminar=0, les=0, les_visc=1, cs=0.1) -> SbParams:
+                dtimag=1e10, keep_laminar=0, les=0, les_visc=1, cs=0.1, ydeal=0) -> SbParams:
     return SbParams(mgalx, my, mgalz, Re, alp, Ly, gam, s, chi, CFL, vbulk, fixed_dt, readflag,
-                    uprim, nhist, etime, dumptime, dtimag, keep_laminar, les, les_visc, cs)
+                    uprim, nhist, etime, dumptime, dtimag, keep_laminar, les, les_visc, cs, ydeal)
 
 
 def sizes(p: SbParams) -> dict:

@@ -71,6 +71,8 @@ static int upload(sb_handle *h, const double **dst, const std::vector<double> &v
 }
 
 static int check_params(const sb_params *p) {
+  if (p && p->ydeal != 0 && p->ydeal != 3)
+    return fail(2, "iydealiasing=%d not available (0, or 3: compact filter)", p->ydeal);
   if (!p) return fail(1, "null parameters");
   if (p->mgalx <= 0 || p->my <= 0 || p->mgalz <= 0)
     return fail(1, "mgalx grid error %d %d %d", p->mgalx, p->my, p->mgalz);  // initcr.f90:188
@@ -142,6 +144,7 @@ static int capture_step(sb_handle *h) {
   CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaSuccess;
   for (int rk = 1; rk <= 3 && e == cudaSuccess; rk++) {
+    if (h->g.ydeal && (e = launch_filter(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
     if ((e = launch_plane(h->g, h->bf, 1, rk, h->st)) != cudaSuccess) break;
     if ((e = launch_plane(h->g, h->bf, 2, rk, h->st)) != cudaSuccess) break;
     if (h->g.les)
@@ -314,6 +317,10 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   g.nzf = g.les ? 10 : 6;
   g.cbl = les_cb(p->mgalz);
   g.ncbl = (g.nkx + g.cbl - 1) / g.cbl;
+  g.ydeal = (p->ydeal == 3) ? 3 : 0;
+  double flhs[7], frhs[9];
+  sbh::filter_coeffs(flhs, frhs);
+  for (int d = 0; d <= 4; d++) g.frh[d] = frhs[4 + d];
   if (g.les) {
     // Deltag = (dx dy dz)^(1/3) (initcr.f90:510); nu_t = Cles^2 Deltag^2 |S|
     const double dg = std::pow(g.dx * g.dy * g.dz, 1.0 / 3.0);
@@ -421,7 +428,8 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
       (rc = upload_f(&bf.kinvf, kinv)) ||
       (rc = upload(h, &bf.kinv, kinv)) || (rc = upload(h, &bf.ginv, ginv)) ||
       (rc = upload_uniform(h, &bf.d1, co.pr1, g.my)) ||
-      (rc = upload_uniform(h, &bf.d2, co.pr2, g.my))) {
+      (rc = upload_uniform(h, &bf.d2, co.pr2, g.my)) ||
+      (g.ydeal && (rc = upload_uniform(h, &bf.flt, flhs, g.my)))) {
     sb_destroy(h);
     return rc;
   }
@@ -622,6 +630,7 @@ int sb_step(sb_handle *h, int nsteps) {
   CK(launch_scalar(h->g, h->bf, 0, h->st));
   CK(launch_tables(h->g, h->bf, 0, h->st));
   CK(launch_setconj(h->g, h->bf, h->st));
+  if (h->g.ydeal) CK(launch_filter(h->g, h->bf, 0, h->st));
   CK(launch_lineB(h->g, h->bf, 0, h->st));
   for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(h->step_exec, h->st));
   return 0;

@@ -61,6 +61,10 @@ struct Grid {
   // kx columns per block of the LES column kernel and their count
   int les, les_visc, nzf, cbl, ncbl;
   double les_c;
+  // compact y-filter (iydealiasing = 3): on/off and the symmetric 9-point
+  // right-hand side frh[0..4] (filter_shear_hepta.f90:64-73)
+  int ydeal;
+  double frh[5];
 };
 
 // Per-member run state, owned by the device (one per box in the batch)
@@ -108,6 +112,7 @@ struct Bufs {
   const double *ginv;            // 1/g per kz  (g = gam * kz_signed; 0 at k=0)
   const double *kinv;            // 1/(alp2+gam2) per (k,i); 0 at (0,0)
   Fac d1, d2, hz;                // d/dy, d2/dy2, Helmholtz (per line)
+  Fac flt;                       // left-hand side of the compact y-filter
   // LES buffers: physical gradient rows [B][my][mgalz/2][6][2][mgalx], |S|^2
   // x-spectra [B][my][mgalz][nkx], stress x-spectra [B][my][mgalz][6][nkx],
   // rhvc2 and rhgc2 fields, T12/T23 of the (0,0) mode [B][my] complex, plane

@@ -57,6 +57,16 @@ static int ipow(int b, int e) {
   return r;
 }
 
+void filter_coeffs(double lhs[7], double rhs[9]) {
+  // the filter's design (transfer 0 at pi, 0.72 at 6pi/9, 0.001 at 8.5pi/9,
+  // 0.91 at 5.5pi/9) is fixed in the reference as decimal constants
+  const double l[4] = {1.0, 0.738981897704866, 0.315003368623046, 0.053003478448814};
+  const double r[5] = {0.987412035368317, 0.749052269410218, 0.309968182770373,
+                       0.054442102978149, -0.000179828066167};
+  for (int d = 0; d <= 3; d++) lhs[3 + d] = lhs[3 - d] = l[d];
+  for (int d = 0; d <= 4; d++) rhs[4 + d] = rhs[4 - d] = r[d];
+}
+
 void compact_coeffs(Coeffs *c) {
   const int N = 3, M = 3;
   const double pi = 4.0 * std::atan(1.0);

@@ -13,6 +13,11 @@ struct Coeffs {
 };
 void compact_coeffs(Coeffs *c);
 
+// Fixed coefficients of the compact y-filter (prefilter,
+// filter_shear_hepta.f90:55-73): left-hand side lhs(-3..3) stored [d+3],
+// right-hand side rhs(-4..4) stored [d+4]; unscaled.
+void filter_coeffs(double lhs[7], double rhs[9]);
+
 // Real base of the cyclic LDL^H factorisation of the band matrix a(-3..3) of
 // size n with the shear phase factored out: for shp = 1 the factorisation of
 // modChol7cyclic_cmplx (diffy_shear_hepta.f90:578-755) is real; for a general

@@ -13,6 +13,7 @@ cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaS
 int les_cb(int mgalz);
 cudaError_t launch_les(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st);
 cudaError_t launch_lineL(const Grid &g, const Bufs &bf, cudaStream_t st);
+cudaError_t launch_filter(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
 cudaError_t prepare_line(const Grid &g);
 int line_segments();
 size_t line_smem(const Grid &g);

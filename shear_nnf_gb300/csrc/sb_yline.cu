@@ -333,6 +333,85 @@ __global__ void __launch_bounds__(32 * kSeg) k_lineL(Grid g, Bufs bf) {
   }
 }
 
+// Compact y-filter of the state (iydealiasing = 3: filterc,
+// filter_shear_hepta.f90:104-148, called at cross.f90:214-227 and 476-490) at
+// the start of substep rk (rk = 0: entry of a cross call), with the shear
+// phase of the substep's starting offsets:
+//   role 0: omega_y, role 1: phi (9-point right-hand side through the free
+//           scratch fields S and T, then the heptadiagonal solve, in place)
+//   mean:   u00, w00 (no phase), then their d/dy, which the nonlinear stage
+//           takes from the filtered profiles (cross.f90:1186-1192)
+template <typename R>
+__global__ void __launch_bounds__(32 * kSeg) k_filter(Grid g, Bufs bf, int rk) {
+  __shared__ double xch[kSeg][16][2][SB_XS];
+  LineThread L;
+  if (!line_thread(g, 2, &L)) return;
+  const Member &M = bf.mem[L.b];
+  if (M.halted) return;
+  const int N = g.my, ystr = blockDim.x;
+  double *ys = ycol();
+  const FacView VF(bf.flt, 0);
+  const SegView WF(bf.flt, 0);
+  const long ps = L.mean ? 2 : g.plane;
+  R *f, *scr;
+  cd shp = mk(1.0, 0.0);
+  if (L.mean) {
+    f = (R *)bf.mu + (long)L.b * 2 * N + L.c;
+    scr = (R *)bf.mdu + (long)L.b * 2 * N + L.c;
+  } else {
+    const long off = (long)L.b * g.field + 2 * L.lc + L.c;
+    f = (R *)(L.role == 0 ? bf.vor : bf.phi) + off;
+    scr = (R *)(L.role == 0 ? bf.S : bf.T) + off;
+    if (fabs(g.s) > 0.01) {
+      const double a = g.alp * L.i;
+      const double xt = M.xwt[rk == 0 ? 0 : rk - 1];
+      sincos((-a) * xt, &shp.y, &shp.x);
+    }
+  }
+  const cd shm = cj(shp);  // matvecNcyclic takes shm = conj(shp)
+  {
+    // u(N-3..N) shm and u(1..4) shp, this lane's component
+    double lo[4], hi[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const double a = (double)f[(long)(N - 4 + q) * ps];
+      const double b = (double)f[(long)q * ps];
+      lo[q] = cmul_c(a, __shfl_xor_sync(0xffffffffu, a, 1), shm, L.c);
+      hi[q] = cmul_c(b, __shfl_xor_sync(0xffffffffu, b, 1), shp, L.c);
+    }
+    if (L.mean) {  // two real lines, no phase
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        lo[q] = (double)f[(long)(N - 4 + q) * ps];
+        hi[q] = (double)f[(long)q * ps];
+      }
+    }
+    for (int i = L.r0; i <= L.r1; i++) {
+      double s = 0.0;
+#pragma unroll
+      for (int d = -4; d <= 4; d++) {
+        const int r = i + d;
+        const double x = (r < 1) ? lo[r + 3] : (r > N ? hi[r - N - 1] : (double)f[(long)(r - 1) * ps]);
+        s += g.frh[d < 0 ? -d : d] * x;
+      }
+      if (L.active) scr[(long)(i - 1) * ps] = (R)s;
+    }
+  }
+  __syncthreads();  // the right-hand side of all segments is read below
+  const Tail TF = make_tail(VF, shp, N);
+  SEG_SOLVE(scr, ps, VF, WF, TF, shp, shm, 1.0, 0.0, 0.0, 0.0, false);
+  store_col(ys, ystr, f, ps, L);
+  if (!L.mean) return;
+  __syncthreads();  // the filtered profiles of all segments are read below
+  const FacView V1(bf.d1, 0);
+  const SegView W1(bf.d1, 0);
+  const cd one = mk(1.0, 0.0);
+  const Tail T1 = load_tail(bf.tl1o + (long)L.b * g.nkx * SB_TAIL);
+  SEG_SOLVE(f, 2, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true);
+  if (L.active)
+    for (int i = L.r0; i <= L.r1; i++) scr[2 * (i - 1)] = (R)ys[(i - L.r0) * ystr];
+}
+
 // set_conj on the state (operators.f90:1382-1429) at entry of a cross call
 template <typename R>
 __global__ void k_setconj(Grid g, Bufs bf) {
@@ -645,6 +724,8 @@ cudaError_t prepare_line(const Grid &g) {
   cudaFuncSetAttribute(k_lineB<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   cudaFuncSetAttribute(k_lineL<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   cudaFuncSetAttribute(k_lineL<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_filter<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_filter<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   return cudaGetLastError();
 }
 
@@ -674,6 +755,15 @@ cudaError_t launch_lineL(const Grid &g, const Bufs &bf, cudaStream_t st) {
     k_lineL<float><<<nb, kLineT, line_smem(g), st>>>(g, bf);
   else
     k_lineL<double><<<nb, kLineT, line_smem(g), st>>>(g, bf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_filter(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  const unsigned nb = (unsigned)(g.B * (2 * g.ngrp + 1));
+  if (g.prec)
+    k_filter<float><<<nb, kLineT, line_smem(g), st>>>(g, bf, rk);
+  else
+    k_filter<double><<<nb, kLineT, line_smem(g), st>>>(g, bf, rk);
   return cudaGetLastError();
 }
 
