@@ -146,6 +146,26 @@ int sb_op_derivyc(int my, double Ly, int iord, int nlines, const double *u, long
 int sb_op_lapcdy(int my, double Ly, int nlines, const double *u, long ldu, double *out, long ldo,
                  const double *k2, const double *shp, const double *shm, void *stream);
 
+/* Compact y-filter of device lines, same layout and shp convention:
+ * filterc (filter_shear_hepta.f90:104-148) with the fixed coefficients of
+ * prefilter (:55-73), 9-point right-hand side over the cyclic heptadiagonal
+ * left-hand side; the lower image uses conj(shp) as matvecNcyclic does
+ * (diffy_shear_hepta.f90:978).  Allocates its scratch like sb_op_derivyc. */
+int sb_op_filterc(int my, int nlines, const double *u, long ldu, double *out, long ldo,
+                  const double *shp, void *stream);
+
+/* y-line transforms in place on device lines (FFTW conventions; forward,
+ * iopt < 0, scaled by 1/my; backward, iopt > 0, unscaled), my in
+ * {32, 48, 64, 96, 192, 384}:
+ *   sb_op_cfty  complex lines, element (line, j) at c + 2*(j*ldc + line):
+ *               cfty, cftdoublew.F:151-201
+ *   sb_op_rfty  real lines of my + 2 rows, element (line, j) at c + j*ldc + line;
+ *               forward leaves the half spectrum packed as (re, im) pairs of
+ *               modes 0..my/2 in rows 0..my+1, backward reads it and zeroes
+ *               rows my, my+1: rfty, rftdoublew.F:133-158 */
+int sb_op_cfty(int my, int nlines, double *c, long ldc, int iopt, void *stream);
+int sb_op_rfty(int my, int nlines, double *c, long ldc, int iopt, void *stream);
+
 /* Allocation-free variant of sb_op_derivyc (no counterpart in the reference).
  * For callers that must not allocate device memory where they need the
  * derivative -- e.g. an application whose device memory is all handed to its

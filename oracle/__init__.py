@@ -72,6 +72,8 @@ def lib():
         L.orc_derivyc.argtypes = [ctypes.c_void_p, dp, dp] + [ctypes.c_double] * 4 + [ctypes.c_int] * 2
         L.orc_lapcdy.argtypes = [ctypes.c_void_p, dp, ctypes.c_double, dp] + [ctypes.c_double] * 4 + [ctypes.c_int]
         L.orc_fourxz.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_int]
+        L.orc_rfty.argtypes = [ctypes.c_void_p, dp, ctypes.c_int]
+        L.orc_cfty.argtypes = [ctypes.c_void_p, dp, ctypes.c_int]
         L.orc_filterc.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_int]
         L.orc_fft.argtypes = [ctypes.c_int, dp, ctypes.c_int]
@@ -136,6 +138,17 @@ class Oracle:
         out = np.zeros_like(a)
         lib().orc_derivyc(self.h, _dp(a), _dp(out), 1.0, 0.0, 1.0, 0.0, iord, 1)
         return out
+
+    def rfty(self, u: np.ndarray, iopt: int) -> np.ndarray:
+        """rfty on one line: u of length my+2 (packed half spectrum)."""
+        a = np.ascontiguousarray(u, dtype=np.float64).copy()
+        lib().orc_rfty(self.h, _dp(a), int(iopt))
+        return a
+
+    def cfty(self, u: np.ndarray, iopt: int) -> np.ndarray:
+        a = np.ascontiguousarray(u, dtype=np.complex128).copy()
+        lib().orc_cfty(self.h, _dp(a.view(np.float64)), int(iopt))
+        return a
 
     def filterc(self, u: np.ndarray, shp=1.0 + 0j) -> np.ndarray:
         """The compact y-filter of one line (complex: shear phase shp)."""

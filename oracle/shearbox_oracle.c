@@ -193,7 +193,7 @@ typedef struct {
   cplx *e1, *f1, *g1, *ce1, *cf1, *cg1;
   double *a2, *b2, *c2, *d2, *d2m1;
   cplx *e2, *f2, *g2, *ce2, *cf2, *cg2;
-  fftplan px, pz;
+  fftplan px, pz, py;
   int nthr;
   ythread *yt;
   pthread_buf *pt;
@@ -804,6 +804,48 @@ void orc_filterc(void *h, const double *u, double *du, double spr, double spi, i
   filterc(c, &c->yt[0], u, du, C(spr, spi), m, 1);
 }
 
+/* rfty / cfty (rftdoublew.F:133-158, cftdoublew.F:151-201): FFTW conventions,
+ * forward transforms scaled by 1/n, backward unscaled.  The real transform
+ * works on the packed half spectrum c[2m], c[2m+1], m = 0..n/2 (n+2 reals). */
+static void rfty_line(ctx *c, double *u, int iopt) {
+  int n = c->my;
+  cplx *z = zalloc(n), *w = zalloc(n);
+  if (iopt < 0) {
+    for (int j = 0; j < n; j++) z[j] = C(u[j], 0.0);
+    fft_exec(&c->py, z, w, -1);
+    double dnf = 1.0 / (double)n;
+    for (int m = 0; m <= n / 2; m++) {
+      u[2 * m] = dnf * z[m].re;
+      u[2 * m + 1] = dnf * z[m].im;
+    }
+  } else {
+    for (int m = 0; m <= n / 2; m++) z[m] = C(u[2 * m], u[2 * m + 1]);
+    z[0].im = 0.0;
+    if (n % 2 == 0) z[n / 2].im = 0.0;
+    for (int m = 1; m < (n + 1) / 2; m++) z[n - m] = cconj(z[m]);
+    fft_exec(&c->py, z, w, +1);
+    for (int j = 0; j < n; j++) u[j] = z[j].re;
+    u[n] = 0.0;
+    u[n + 1] = 0.0;
+  }
+  free(z);
+  free(w);
+}
+
+static void cfty_line(ctx *c, cplx *u, int iopt) {
+  int n = c->my;
+  cplx *w = zalloc(n);
+  fft_exec(&c->py, u, w, iopt < 0 ? -1 : +1);
+  if (iopt < 0) {
+    double dnf = 1.0 / (double)n;
+    for (int j = 0; j < n; j++) u[j] = cscal(dnf, u[j]);
+  }
+  free(w);
+}
+
+void orc_cfty(void *h, double *u, int iopt) { cfty_line((ctx *)h, (cplx *)u, iopt); }
+void orc_rfty(void *h, double *u, int iopt) { rfty_line((ctx *)h, u, iopt); }
+
 /* visc3d (diffy_shear_hepta.f90:298-318), what = '+' */
 static void visc3d(ctx *c, ythread *t, const double *u, double *visc, double *ddu,
                    cplx shp, cplx shm, int m, double rk, double scal, int ias) {
@@ -922,6 +964,7 @@ void *orc_create(const orc_params *p) {
   }
   plan_init(&c->px, c->mgalx);
   plan_init(&c->pz, c->mgalz);
+  plan_init(&c->py, c->my);
   int nthr = 1;
 #ifdef _OPENMP
   if (g_threads > 0) omp_set_num_threads(g_threads);
@@ -983,6 +1026,7 @@ void orc_destroy(void *h) {
   free(c->fe); free(c->ff); free(c->fg); free(c->fce); free(c->fcf); free(c->fcg);
   plan_free(&c->px);
   plan_free(&c->pz);
+  plan_free(&c->py);
   free(c);
 }
 
@@ -1462,6 +1506,57 @@ static void filter_state(ctx *c, double *vor, double *phi, double *u00, double *
   }
 }
 
+/* dealiasing_y for iydealiasing 1 and 2 (operators.f90:352-467) */
+static void dealiasing_y(ctx *c, double *vor, double *phi, double *u00, double *w00, double fac) {
+  int my = c->my, nkx = c->nkx, mz = c->mz, mx1 = c->mx1;
+  int my23 = 2 * (my / 3), ny1 = ((my23 - 1) - 1) / 2, ny2 = my - ny1;
+  double Lx = c->Lx, Ly = c->p.Ly;
+  double *p = dalloc(my + 2);
+  double *prof[2] = {u00, w00};
+  for (int q = 0; q < 2; q++) {
+    for (int j = 0; j < my + 2; j++) p[j] = (j < my) ? prof[q][j] : 0.0;
+    rfty_line(c, p, -1);
+    for (int j = my23; j <= my + 1; j++) p[j] = 0.0;
+    rfty_line(c, p, +1);
+    for (int j = 0; j < my; j++) prof[q][j] = p[j];
+  }
+  free(p);
+  int ie = (c->p.ydeal == 1) ? 1 : nkx;
+  for (int k = 0; k < mz; k++)
+    for (int i = 0; i < ie; i++) {
+      cplx *v = (cplx *)PEN(vor, i, k), *f = (cplx *)PEN(phi, i, k);
+      cfty_line(c, v, -1);
+      cfty_line(c, f, -1);
+      double di = (double)i, r = (double)ny1 / (double)mx1;
+      double djda, djdb;
+      if (c->p.ydeal == 1 || fac <= 0.0) {
+        djda = r * (-fac - Lx / Ly) * Ly / Lx * di;
+        djdb = r * (-fac) * Ly / Lx * di;
+      } else {
+        djda = r * (-fac + Lx / Ly) * Ly / Lx * di;
+        djdb = r * (-fac) * Ly / Lx * di;
+      }
+      for (int j = 0; j < my; j++) {
+        double dj = (double)j;
+        int cut;
+        if (c->p.ydeal == 1)
+          cut = (dj > ny1 + djdb) && (dj < ny2 + djdb);
+        else
+          cut = ((dj >= ny1 + djdb) && (dj <= ny2 + djdb)) || ((dj > ny1 + djda) && (dj < ny2 + djda));
+        if (cut) {
+          v[j] = C(0.0, 0.0);
+          f[j] = C(0.0, 0.0);
+        }
+      }
+      cfty_line(c, v, +1);
+      cfty_line(c, f, +1);
+    }
+}
+
+void orc_dealiasing_y(void *h, double *vor, double *phi, double *u00, double *w00, double fac) {
+  dealiasing_y((ctx *)h, vor, phi, u00, w00, fac);
+}
+
 int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, double *ptime,
               double *pxoffb, double *pxofft, int nstep, double *trace, int *ntrace,
               int *pistop, double *pdeltat) {
@@ -1509,6 +1604,11 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
   if (c->p.ydeal == 3) filter_state(c, vor, phi, u00, w00, shwkt);
   for (int istep = 1; istep <= nstep; istep++) {
     if ((istep - 1) % nhist == 0) ihist = 1;
+    if (c->p.ydeal == 2) {
+      /* remeshing-like offsets (cross.f90:348-351) */
+      xoffb = (xoffb / c->Lx - trunc(xoffb / c->Lx)) * c->Lx;
+      xofft = -xoffb;
+    }
     xwkt = xofft;
     xwkb = xoffb;
     if ((istep - 1) != 1) {
@@ -1551,6 +1651,14 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
       /* iydealiasing = 3 on the state after the first derivatives
        * (cross.f90:476-490) */
       if (c->p.ydeal == 3) filter_state(c, vor, phi, u00, w00, shwkt);
+      if (c->p.ydeal == 1 || c->p.ydeal == 2) {
+        /* y dealiasing in the frame of the current offset (cross.f90:459-474) */
+        double fac = (xwkb / c->Lx - trunc(xwkb / c->Lx)) * c->Lx / c->p.Ly;
+        if (fac < -c->Lx / c->p.Ly * 0.5) fac = c->Lx / c->p.Ly + fac;
+        moving_frame(c, vor, phi, fac);
+        dealiasing_y(c, vor, phi, u00, w00, fac);
+        moving_frame(c, vor, phi, -fac);
+      }
       to_plane(c, phi, b1);
       to_plane(c, vor, b2);
       /* set_conj on the copies (cross.f90:502) */
@@ -1768,6 +1876,10 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
       if (fabs(s) > 0.01) {
         xwkb = xoffb + r1 * u00b;
         xwkt = xofft + r1 * u00t;
+        if (c->p.ydeal == 2) {
+          xwkb = (xwkb / c->Lx - trunc(xwkb / c->Lx)) * c->Lx;
+          xwkt = -xwkb;
+        }
         for (int i = 0; i <= mx1; i++) {
           double a = c->xalp_im[i];
           shwkb[i] = C(cos((-a) * xwkb), sin((-a) * xwkb));

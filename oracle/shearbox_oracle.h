@@ -38,7 +38,10 @@ typedef struct orc_params {
   int les;                /* iuse_LES: Smagorinsky model (cross.f90:1291-1406) */
   int les_visc;           /* iadd_visc: molecular viscosity kept with the model */
   double cs;              /* Cles, the Smagorinsky constant (initcr.f90:1964,2148) */
-  int ydeal;              /* iydealiasing: 0 none, 3 compact y-filter (cross.f90:214-227,476-490) */
+  int ydeal;              /* iydealiasing: 0 none, 1 y 2/3 rule on kx=0 and the mean modes,
+                           * 2 the moving-frame variant on every kx (dealiasing_y,
+                           * operators.f90:352-467), 3 compact y-filter
+                           * (cross.f90:214-227,476-490) */
 } orc_params;
 
 /* one .cfbin record per statistics step (cross.f90:2087):
@@ -62,6 +65,11 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00,
 
 /* building blocks, one y-line (complex: m=2, real: m=1) */
 void orc_filterc(void *h, const double *u, double *du, double shp_re, double shp_im, int m);
+/* rfty / cfty on one y-line (packed real line of my+2 doubles, or complex) */
+void orc_rfty(void *h, double *u, int iopt);
+void orc_cfty(void *h, double *u, int iopt);
+/* dealiasing_y (iydealiasing 1, 2) on pencil-layout state arrays */
+void orc_dealiasing_y(void *h, double *vor, double *phi, double *u00, double *w00, double fac);
 void orc_derivyc(void *h, const double *u, double *du, double shp_re,
                  double shp_im, double shm_re, double shm_im, int iord, int m);
 void orc_lapcdy(void *h, const double *u, double k2, double *p, double shp_re,

@@ -53,7 +53,7 @@ ABI_FUNCTIONS = [
     "sb_get_status", "sb_get_trace", "sb_cross", "sb_get_stream", "sb_sync", "sb_sizes",
     "sb_seed_state", "sb_compact_coeffs", "sb_last_error", "sb_version", "sb_launch_stage",
     "sb_fp64_peak", "sb_op_derivyc", "sb_op_lapcdy", "sb_op_derivyc_noalloc",
-    "sb_set_member_etime",
+    "sb_set_member_etime", "sb_op_filterc", "sb_op_cfty", "sb_op_rfty",
 ]
 
 _lib = None
@@ -99,6 +99,10 @@ def lib(auto_build: bool = False):
     L.sb_op_derivyc_noalloc.argtypes = list(L.sb_op_derivyc.argtypes)
     L.sb_op_lapcdy.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, vp, ctypes.c_long, vp,
                                ctypes.c_long, dp, dp, dp, vp]
+    L.sb_op_filterc.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_long, vp, ctypes.c_long,
+                                dp, vp]
+    L.sb_op_cfty.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_long, ctypes.c_int, vp]
+    L.sb_op_rfty.argtypes = list(L.sb_op_cfty.argtypes)
     _lib = L
     return L
 
@@ -277,6 +281,27 @@ def op_lapcdy(my: int, Ly: float, u_dev: int, out_dev: int, nlines: int, k2: np.
                               int(ldu or nlines), ctypes.c_void_p(out_dev), int(ldo or nlines),
                               _dp(kk), _dp(sp.view(np.float64)), _dp(sm.view(np.float64)),
                               ctypes.c_void_p(stream)))
+
+
+def op_filterc(my: int, u_dev: int, out_dev: int, nlines: int, shp: np.ndarray,
+               ldu: int = None, ldo: int = None, stream: int = 0):
+    """Compact y-filter of nlines device-resident complex lines (filterc)."""
+    sp = np.ascontiguousarray(shp, np.complex128)
+    _check(lib().sb_op_filterc(int(my), int(nlines), ctypes.c_void_p(u_dev), int(ldu or nlines),
+                               ctypes.c_void_p(out_dev), int(ldo or nlines),
+                               _dp(sp.view(np.float64)), ctypes.c_void_p(stream)))
+
+
+def op_cfty(my: int, c_dev: int, nlines: int, iopt: int, ldc: int = None, stream: int = 0):
+    """In-place y transform of complex device lines (cfty conventions)."""
+    _check(lib().sb_op_cfty(int(my), int(nlines), ctypes.c_void_p(c_dev), int(ldc or nlines),
+                            int(iopt), ctypes.c_void_p(stream)))
+
+
+def op_rfty(my: int, c_dev: int, nlines: int, iopt: int, ldc: int = None, stream: int = 0):
+    """In-place y transform of real device lines of my+2 rows (rfty)."""
+    _check(lib().sb_op_rfty(int(my), int(nlines), ctypes.c_void_p(c_dev), int(ldc or nlines),
+                            int(iopt), ctypes.c_void_p(stream)))
 
 
 def op_derivyc_noalloc(my: int, Ly: float, iord: int, u_dev: int, out_dev: int, nlines: int,

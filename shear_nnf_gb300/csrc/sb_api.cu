@@ -71,8 +71,10 @@ static int upload(sb_handle *h, const double **dst, const std::vector<double> &v
 }
 
 static int check_params(const sb_params *p) {
-  if (p && p->ydeal != 0 && p->ydeal != 3)
-    return fail(2, "iydealiasing=%d not available (0, or 3: compact filter)", p->ydeal);
+  if (p && (p->ydeal < 0 || p->ydeal > 3))
+    return fail(2, "iydealiasing=%d not available (0..3)", p->ydeal);
+  if (p && (p->ydeal == 1 || p->ydeal == 2) && !supported_ylen(p->my))
+    return fail(2, "iydealiasing=%d needs my in 32,48,64,96,192,384 (y transforms)", p->ydeal);
   if (!p) return fail(1, "null parameters");
   if (p->mgalx <= 0 || p->my <= 0 || p->mgalz <= 0)
     return fail(1, "mgalx grid error %d %d %d", p->mgalx, p->my, p->mgalz);  // initcr.f90:188
@@ -144,7 +146,11 @@ static int capture_step(sb_handle *h) {
   CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaSuccess;
   for (int rk = 1; rk <= 3 && e == cudaSuccess; rk++) {
-    if (h->g.ydeal && (e = launch_filter(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
+    if (h->g.ydeal == 3 && (e = launch_filter(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
+    if ((h->g.ydeal == 1 || h->g.ydeal == 2) &&
+        ((e = launch_ydeal(h->g, h->bf, rk, h->st)) != cudaSuccess ||
+         (e = launch_meand1(h->g, h->bf, h->st)) != cudaSuccess))
+      break;
     if ((e = launch_plane(h->g, h->bf, 1, rk, h->st)) != cudaSuccess) break;
     if ((e = launch_plane(h->g, h->bf, 2, rk, h->st)) != cudaSuccess) break;
     if (h->g.les)
@@ -317,7 +323,11 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   g.nzf = g.les ? 10 : 6;
   g.cbl = les_cb(p->mgalz);
   g.ncbl = (g.nkx + g.cbl - 1) / g.cbl;
-  g.ydeal = (p->ydeal == 3) ? 3 : 0;
+  g.ydeal = p->ydeal;
+  g.my23 = 2 * (p->my / 3);  // initcr.f90:207-210
+  g.ny1 = ((g.my23 - 1) - 1) / 2;
+  g.ny2 = p->my - g.ny1;
+  g.Lx = 2.0 * g.pi / p->alp;
   double flhs[7], frhs[9];
   sbh::filter_coeffs(flhs, frhs);
   for (int d = 0; d <= 4; d++) g.frh[d] = frhs[4 + d];
@@ -429,7 +439,9 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
       (rc = upload(h, &bf.kinv, kinv)) || (rc = upload(h, &bf.ginv, ginv)) ||
       (rc = upload_uniform(h, &bf.d1, co.pr1, g.my)) ||
       (rc = upload_uniform(h, &bf.d2, co.pr2, g.my)) ||
-      (g.ydeal && (rc = upload_uniform(h, &bf.flt, flhs, g.my)))) {
+      (g.ydeal == 3 && (rc = upload_uniform(h, &bf.flt, flhs, g.my))) ||
+      ((g.ydeal == 1 || g.ydeal == 2) &&
+       ((rc = upload(h, &bf.twy, tw(g.my))) || (rc = upload_f(&bf.twyf, tw(g.my)))))) {
     sb_destroy(h);
     return rc;
   }
@@ -499,7 +511,8 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
     return fail(3, "member upload: %s", cudaGetErrorString(ce));
   }
   if (launch_plane(g, bf, 0, 0, h->st) != cudaSuccess || prepare_line(g) != cudaSuccess ||
-      (g.les && launch_les(g, bf, 0, 0, h->st) != cudaSuccess)) {
+      (g.les && launch_les(g, bf, 0, 0, h->st) != cudaSuccess) ||
+      ((g.ydeal == 1 || g.ydeal == 2) && launch_ydeal(g, bf, 0, h->st) != cudaSuccess)) {
     sb_destroy(h);
     return fail(3, "kernel attributes: %s", cudaGetErrorString(cudaGetLastError()));
   }
@@ -630,7 +643,7 @@ int sb_step(sb_handle *h, int nsteps) {
   CK(launch_scalar(h->g, h->bf, 0, h->st));
   CK(launch_tables(h->g, h->bf, 0, h->st));
   CK(launch_setconj(h->g, h->bf, h->st));
-  if (h->g.ydeal) CK(launch_filter(h->g, h->bf, 0, h->st));
+  if (h->g.ydeal == 3) CK(launch_filter(h->g, h->bf, 0, h->st));
   CK(launch_lineB(h->g, h->bf, 0, h->st));
   for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(h->step_exec, h->st));
   return 0;
@@ -791,6 +804,65 @@ int sb_op_lapcdy(int my, double Ly, int nlines, const double *u, long ldu, doubl
   if (e != cudaSuccess) return fail(3, "launch: %s", cudaGetErrorString(e));
   CK(cudaStreamSynchronize(st));
   return 0;
+}
+
+int sb_op_filterc(int my, int nlines, const double *u, long ldu, double *out, long ldo,
+                  const double *shp, void *stream) {
+  int rc = op_check(my, 1.0, nlines, u, out, ldu, ldo, shp, shp);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  double lhs[7], rhs[9];
+  sbh::filter_coeffs(lhs, rhs);
+  HostFac hf;
+  host_fac_init(&hf, my, 1);
+  sbh::BaseFac b;
+  sbh::base_factor(lhs, my, &b);
+  host_fac_add(&hf, 0, b, lhs);
+  const size_t nfac = hf.buf.size();
+  std::vector<double> host(nfac + 4 * (size_t)nlines);
+  std::copy(hf.buf.begin(), hf.buf.end(), host.begin());
+  std::copy(shp, shp + 2 * (size_t)nlines, host.begin() + nfac);
+  for (int l = 0; l < nlines; l++) {  // the solve's lower image: conj(shp)
+    host[nfac + 2 * nlines + 2 * l] = shp[2 * l];
+    host[nfac + 2 * nlines + 2 * l + 1] = -shp[2 * l + 1];
+  }
+  const long nthr = op_threads(nlines);
+  double *dbuf = nullptr, *ybuf = nullptr, *wbuf = nullptr;
+  CK(cudaMallocAsync((void **)&dbuf, sizeof(double) * host.size(), st));
+  CK(cudaMallocAsync((void **)&ybuf, sizeof(double) * (size_t)my * nthr, st));
+  CK(cudaMallocAsync((void **)&wbuf, sizeof(double) * 2 * (size_t)my * nlines, st));
+  CK(cudaMemcpyAsync(dbuf, host.data(), sizeof(double) * host.size(), cudaMemcpyHostToDevice, st));
+  Fac F = fac_bind(hf, dbuf);
+  const double r9[5] = {rhs[4], rhs[5], rhs[6], rhs[7], rhs[8]};
+  const double one[4] = {1.0, 0.0, 0.0, 0.0};
+  cudaError_t e = launch_filter_rhs(nlines, my, u, ldu, wbuf, nlines, dbuf + nfac, r9, st);
+  if (e == cudaSuccess)
+    e = launch_op_line(nlines, my, wbuf, nlines, out, ldo, ybuf, F, dbuf + nfac,
+                       dbuf + nfac + 2 * nlines, one, 0, st);
+  cudaFreeAsync(wbuf, st);
+  cudaFreeAsync(ybuf, st);
+  cudaFreeAsync(dbuf, st);
+  if (e != cudaSuccess) return fail(3, "launch: %s", cudaGetErrorString(e));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+static int yop(int my, int nlines, double *c, long ldc, int iopt, int real, void *stream) {
+  if (!supported_ylen(my)) return fail(1, "my=%d: y transforms support 32,48,64,96,192,384", my);
+  if (nlines < 1 || !c || ldc < nlines || iopt == 0) return fail(1, "bad argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = launch_yop(my, nlines, c, ldc, iopt, real, st);
+  if (e != cudaSuccess) return fail(3, "launch: %s", cudaGetErrorString(e));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
+int sb_op_cfty(int my, int nlines, double *c, long ldc, int iopt, void *stream) {
+  return yop(my, nlines, c, ldc, iopt, 0, stream);
+}
+
+int sb_op_rfty(int my, int nlines, double *c, long ldc, int iopt, void *stream) {
+  return yop(my, nlines, c, ldc, iopt, 1, stream);
 }
 
 int sb_op_derivyc_noalloc(int my, double Ly, int iord, int nlines, const double *u, long ldu,

@@ -65,6 +65,10 @@ struct Grid {
   // right-hand side frh[0..4] (filter_shear_hepta.f90:64-73)
   int ydeal;
   double frh[5];
+  // y dealiasing (iydealiasing 1, 2; dealiasing_y, operators.f90:352-467):
+  // 2/3-rule cut indices (initcr.f90:207-210) and Lx
+  int my23, ny1, ny2;
+  double Lx;
 };
 
 // Per-member run state, owned by the device (one per box in the batch)
@@ -81,6 +85,7 @@ struct Member {
   unsigned long long umax_bits[4];  // |u| maxima as ordered bit patterns (atomicMax)
   unsigned long long nut_bits;      // LES: max |nu_t| of this step (bit pattern)
   double max_nut;                   // LES: running maximum of |nu_t| (cross.f90:1433)
+  double ydfac;                     // y dealiasing: moving-frame shift of this substep
   int istop, idump, ihist, istep, halted, ntrace, trace_cap, flags;
 };
 
@@ -113,6 +118,8 @@ struct Bufs {
   const double *kinv;            // 1/(alp2+gam2) per (k,i); 0 at (0,0)
   Fac d1, d2, hz;                // d/dy, d2/dy2, Helmholtz (per line)
   Fac flt;                       // left-hand side of the compact y-filter
+  const double *twy;             // y-transform twiddles (iydealiasing 1, 2)
+  const float *twyf;
   // LES buffers: physical gradient rows [B][my][mgalz/2][6][2][mgalx], |S|^2
   // x-spectra [B][my][mgalz][nkx], stress x-spectra [B][my][mgalz][6][nkx],
   // rhvc2 and rhgc2 fields, T12/T23 of the (0,0) mode [B][my] complex, plane

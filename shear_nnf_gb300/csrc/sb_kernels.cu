@@ -676,6 +676,173 @@ __global__ void __launch_bounds__(T) k_les5(Grid g, Bufs bf) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// y dealiasing (iydealiasing 1, 2: dealiasing_y, operators.f90:352-467, called
+// at the start of every substep, cross.f90:459-474) and the y-line transforms
+// rfty / cfty (rftdoublew.F:133-158, cftdoublew.F:151-201): forward transforms
+// scaled by 1/my, backward unscaled, FFTW sign conventions.
+// ---------------------------------------------------------------------------
+template <typename R> __device__ __forceinline__ const R *twy_of(const Bufs &bf);
+template <> __device__ __forceinline__ const double *twy_of<double>(const Bufs &bf) { return bf.twy; }
+template <> __device__ __forceinline__ const float *twy_of<float>(const Bufs &bf) { return bf.twyf; }
+
+// Mean profiles u00 + i w00 of one box: 2/3 rule of their real y-spectra
+// (modes m >= my23/2 and their conjugates).  With iydealiasing = 2 the first
+// substep of a step wraps the offsets into one box length (cross.f90:348-351);
+// every substep stores the moving-frame shift of its starting offset
+// (cross.f90:459-463).
+template <typename R, int MY, int T>
+__global__ void __launch_bounds__(T) k_ydeal_mean(Grid g, Bufs bf, int rk) {
+  typedef typename Vec2<R>::t V;
+  const int b = blockIdx.x;
+  Member &M = bf.mem[b];
+  if (M.halted) return;
+  __shared__ V A[MY], Bs[MY];
+  if (threadIdx.x == 0) {
+    if (g.ydeal == 2 && rk == 1) {
+      M.xoffb = (M.xoffb / g.Lx - trunc(M.xoffb / g.Lx)) * g.Lx;
+      M.xofft = -M.xoffb;
+      M.xwb[0] = M.xoffb;
+      M.xwt[0] = M.xofft;
+    }
+    const double xb = M.xwb[rk - 1];
+    double fac = (xb / g.Lx - trunc(xb / g.Lx)) * g.Lx / g.Ly;
+    if (fac < -g.Lx / g.Ly * 0.5) fac = g.Lx / g.Ly + fac;
+    M.ydfac = fac;
+  }
+  V *mu = (V *)bf.mu + (long)b * MY;
+  for (int j = threadIdx.x; j < MY; j += T) A[j] = mu[j];
+  V *P = fft_batch<MY, -1, 1, T>(A, Bs, (const V *)twy_of<R>(bf));
+  const int K = g.my23 / 2;
+  const R dnf = (R)(1.0 / (double)MY);
+  for (int m = threadIdx.x; m < MY; m += T) {
+    const V z = P[m];
+    P[m] = (m >= K && m <= MY - K) ? mk2<R>((R)0, (R)0) : mk2<R>(dnf * z.x, dnf * z.y);
+  }
+  V *Q = fft_batch<MY, +1, 1, T>(P, P == A ? Bs : A, (const V *)twy_of<R>(bf));
+  for (int j = threadIdx.x; j < MY; j += T) mu[j] = Q[j];
+}
+
+// CB lines (consecutive kx at one kz) of omega_y or phi of one box: moving
+// frame exp(i kx y fac) (iydealiasing 2; for 1 only kx = 0 is cut, where the
+// frame is the identity), forward y-transform, the cut of dealiasing_y,
+// backward transform, frame back.
+template <typename R, int MY, int CB, int T>
+__global__ void __launch_bounds__(T) k_ydeal(Grid g, Bufs bf) {
+  typedef typename Vec2<R>::t V;
+  const int k = blockIdx.y, b = blockIdx.z >> 1, fld = blockIdx.z & 1;
+  const Member &M = bf.mem[b];
+  if (M.halted) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *A = (V *)smem_raw, *Bs = A + CB * MY;
+  const int nkx = g.nkx, i0 = blockIdx.x * CB;
+  const int ie = (g.ydeal == 1) ? 1 : nkx;
+  V *f = (V *)((R *)(fld ? bf.phi : bf.vor) + (long)b * g.field) + (long)k * nkx;
+  const long ps = g.plane / 2;  // complex entries per plane
+  const double fac = M.ydfac;
+  const bool frame = (g.ydeal == 2);
+  for (int idx = threadIdx.x; idx < CB * MY; idx += T) {
+    const int ci = idx % CB, j = idx / CB, i = i0 + ci;
+    V v = mk2<R>((R)0, (R)0);
+    if (i < ie) {
+      v = f[(long)j * ps + i];
+      if (frame) {
+        double sn, cs;
+        sincos(((g.alp * i) * ((double)j * g.dy - 0.5 * g.Ly)) * fac, &sn, &cs);
+        v = mk2<R>((R)((double)v.x * cs - (double)v.y * sn), (R)((double)v.x * sn + (double)v.y * cs));
+      }
+    }
+    A[ci * MY + j] = v;
+  }
+  V *P = fft_batch<MY, -1, CB, T>(A, Bs, (const V *)twy_of<R>(bf));
+  const R dnf = (R)(1.0 / (double)MY);
+  const double r = (double)g.ny1 / (double)(nkx - 1);
+  const double LxLy = g.Lx / g.Ly;
+  // The band edges are compared with integers, often exactly at an integer:
+  // they are evaluated with explicitly rounded operations (no fused
+  // multiply-add) so that they round as the reference's expressions do.
+  auto edge = [&](double x, double di) {
+    return __dmul_rn(__ddiv_rn(__dmul_rn(__dmul_rn(r, x), g.Ly), g.Lx), di);
+  };
+  for (int idx = threadIdx.x; idx < CB * MY; idx += T) {
+    const int ci = idx / MY, j = idx % MY, i = i0 + ci;
+    const double di = (double)i, dj = (double)j;
+    const double xa = (g.ydeal == 1 || fac <= 0.0) ? __dsub_rn(-fac, LxLy) : __dadd_rn(-fac, LxLy);
+    const double djda = edge(xa, di), djdb = edge(-fac, di);
+    const double a1 = __dadd_rn((double)g.ny1, djda), a2 = __dadd_rn((double)g.ny2, djda);
+    const double b1 = __dadd_rn((double)g.ny1, djdb), b2 = __dadd_rn((double)g.ny2, djdb);
+    bool cut;
+    if (g.ydeal == 1)
+      cut = (dj > b1) && (dj < b2);
+    else
+      cut = ((dj >= b1) && (dj <= b2)) || ((dj > a1) && (dj < a2));
+    const V z = P[idx];
+    P[idx] = cut ? mk2<R>((R)0, (R)0) : mk2<R>(dnf * z.x, dnf * z.y);
+  }
+  V *Q = fft_batch<MY, +1, CB, T>(P, P == A ? Bs : A, (const V *)twy_of<R>(bf));
+  for (int idx = threadIdx.x; idx < CB * MY; idx += T) {
+    const int ci = idx % CB, j = idx / CB, i = i0 + ci;
+    if (i >= ie) continue;
+    V v = Q[ci * MY + j];
+    if (frame) {
+      double sn, cs;
+      sincos(((g.alp * i) * ((double)j * g.dy - 0.5 * g.Ly)) * (-fac), &sn, &cs);
+      v = mk2<R>((R)((double)v.x * cs - (double)v.y * sn), (R)((double)v.x * sn + (double)v.y * cs));
+    }
+    f[(long)j * ps + i] = v;
+  }
+}
+
+// Standalone y-line transforms on device lines [j][line] (FP64): complex lines
+// (cfty, c[2 (j ldc + l)]) or packed real lines of my + 2 rows (rfty, c[j ldc + l]).
+template <int MY, int CB, int T>
+__global__ void __launch_bounds__(T) k_yop(int nlines, double *c, long ldc, int iopt, int real) {
+  __shared__ double2 A[CB * MY], Bs[CB * MY], tw[MY];
+  for (int t = threadIdx.x; t < MY; t += T) {
+    double sn, cs;
+    sincospi(-2.0 * (double)t / (double)MY, &sn, &cs);
+    tw[t] = make_double2(cs, sn);
+  }
+  const int l0 = blockIdx.x * CB;
+  for (int idx = threadIdx.x; idx < CB * MY; idx += T) {
+    const int ci = idx % CB, j = idx / CB, l = l0 + ci;
+    double2 v = make_double2(0.0, 0.0);
+    if (l < nlines) {
+      if (!real) {
+        v = make_double2(c[2 * ((long)j * ldc + l)], c[2 * ((long)j * ldc + l) + 1]);
+      } else if (iopt < 0) {
+        v = make_double2(c[(long)j * ldc + l], 0.0);
+      } else {
+        // Hermitian extension of the packed half spectrum; c2r ignores the
+        // imaginary parts of modes 0 and my/2
+        const int m = (j <= MY / 2) ? j : MY - j;
+        double re = c[(long)(2 * m) * ldc + l], im = c[(long)(2 * m + 1) * ldc + l];
+        if (m == 0 || 2 * m == MY) im = 0.0;
+        v = make_double2(re, j <= MY / 2 ? im : -im);
+      }
+    }
+    A[ci * MY + j] = v;
+  }
+  double2 *P = (iopt < 0) ? fft_batch<MY, -1, CB, T>(A, Bs, tw) : fft_batch<MY, +1, CB, T>(A, Bs, tw);
+  const double dnf = 1.0 / (double)MY;
+  for (int idx = threadIdx.x; idx < CB * (MY + 2); idx += T) {
+    const int ci = idx % CB, j = idx / CB, l = l0 + ci;
+    if (l >= nlines) continue;
+    if (!real) {
+      if (j >= MY) continue;
+      double2 v = P[ci * MY + j];
+      if (iopt < 0) v = make_double2(dnf * v.x, dnf * v.y);
+      c[2 * ((long)j * ldc + l)] = v.x;
+      c[2 * ((long)j * ldc + l) + 1] = v.y;
+    } else if (iopt < 0) {
+      const double2 v = P[ci * MY + (j >> 1)];
+      c[(long)j * ldc + l] = dnf * ((j & 1) ? v.y : v.x);
+    } else {
+      c[(long)j * ldc + l] = (j < MY) ? P[ci * MY + j].x : 0.0;
+    }
+  }
+}
+
 // pencil (j fastest, then kx, then kz, FP64 host layout) <-> plane-major
 // device layout of storage type R, one box
 template <typename R>
@@ -840,6 +1007,65 @@ static cudaError_t launch_les_t(const Grid &g, const Bufs &bf, int stage, int rk
 cudaError_t launch_les(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
   return g.prec ? launch_les_t<float>(g, bf, stage, rk, st)
                 : launch_les_t<double>(g, bf, stage, rk, st);
+}
+
+// y dealiasing of substep rk: the mean-profile kernel (offsets, frame shift)
+// then the line kernel
+template <typename R, int MY>
+static cudaError_t launch_ydeal_t(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, bool prep) {
+  typedef typename Vec2<R>::t V;
+  constexpr int CB = MY <= 96 ? 16 : (MY == 192 ? 8 : 4);
+  const size_t sm = sizeof(V) * 2 * CB * MY;
+  if (prep) {
+    cudaFuncSetAttribute(k_ydeal<R, MY, CB, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    return cudaGetLastError();
+  }
+  k_ydeal_mean<R, MY, 128><<<g.B, 128, 0, st>>>(g, bf, rk);
+  const int nb = (g.ydeal == 1) ? 1 : (g.nkx + CB - 1) / CB;
+  k_ydeal<R, MY, CB, 128><<<dim3(nb, g.mz, 2 * g.B), 128, sm, st>>>(g, bf);
+  return cudaGetLastError();
+}
+
+template <typename R>
+static cudaError_t launch_ydeal_r(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, bool prep) {
+  switch (g.my) {
+    case 32: return launch_ydeal_t<R, 32>(g, bf, rk, st, prep);
+    case 48: return launch_ydeal_t<R, 48>(g, bf, rk, st, prep);
+    case 64: return launch_ydeal_t<R, 64>(g, bf, rk, st, prep);
+    case 96: return launch_ydeal_t<R, 96>(g, bf, rk, st, prep);
+    case 192: return launch_ydeal_t<R, 192>(g, bf, rk, st, prep);
+    case 384: return launch_ydeal_t<R, 384>(g, bf, rk, st, prep);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// rk = 1..3: launch; rk = 0: set the kernels' shared-memory limits
+cudaError_t launch_ydeal(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  return g.prec ? launch_ydeal_r<float>(g, bf, rk, st, rk == 0)
+                : launch_ydeal_r<double>(g, bf, rk, st, rk == 0);
+}
+
+bool supported_ylen(int my) {
+  return my == 32 || my == 48 || my == 64 || my == 96 || my == 192 || my == 384;
+}
+
+template <int MY>
+static cudaError_t launch_yop_t(int nlines, double *c, long ldc, int iopt, int real, cudaStream_t st) {
+  constexpr int CB = MY <= 96 ? 4 : (MY == 192 ? 2 : 1);
+  k_yop<MY, CB, 128><<<(nlines + CB - 1) / CB, 128, 0, st>>>(nlines, c, ldc, iopt, real);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_yop(int my, int nlines, double *c, long ldc, int iopt, int real, cudaStream_t st) {
+  switch (my) {
+    case 32: return launch_yop_t<32>(nlines, c, ldc, iopt, real, st);
+    case 48: return launch_yop_t<48>(nlines, c, ldc, iopt, real, st);
+    case 64: return launch_yop_t<64>(nlines, c, ldc, iopt, real, st);
+    case 96: return launch_yop_t<96>(nlines, c, ldc, iopt, real, st);
+    case 192: return launch_yop_t<192>(nlines, c, ldc, iopt, real, st);
+    case 384: return launch_yop_t<384>(nlines, c, ldc, iopt, real, st);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_pencil_to_plane(const Grid &g, const double *pen, double *dst, cudaStream_t st) {

@@ -14,6 +14,12 @@ int les_cb(int mgalz);
 cudaError_t launch_les(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st);
 cudaError_t launch_lineL(const Grid &g, const Bufs &bf, cudaStream_t st);
 cudaError_t launch_filter(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
+cudaError_t launch_ydeal(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
+cudaError_t launch_meand1(const Grid &g, const Bufs &bf, cudaStream_t st);
+bool supported_ylen(int my);
+cudaError_t launch_yop(int my, int nlines, double *c, long ldc, int iopt, int real, cudaStream_t st);
+cudaError_t launch_filter_rhs(int nlines, int N, const double *u, long ldu, double *out, long ldo,
+                              const double *shp, const double r[5], cudaStream_t st);
 cudaError_t prepare_line(const Grid &g);
 int line_segments();
 size_t line_smem(const Grid &g);

@@ -34,6 +34,44 @@ __global__ void __launch_bounds__(128) k_op_line(int nlines, int N, const double
 
 long op_threads(int nlines) { return ((2L * nlines + 31) / 32) * 32; }
 
+// right-hand side of the compact y-filter (matvecNcyclic with na = 4,
+// diffy_shear_hepta.f90:960-996): one thread per (line, row, component);
+// rows wrapped around the line take u(y-Ly) = conj(shp) u and u(y+Ly) = shp u
+__global__ void k_filter_rhs(int nlines, int N, const double *u, long ldu, double *out, long ldo,
+                             const double *shp, double r0, double r1, double r2, double r3,
+                             double r4) {
+  const long n = 2L * N * nlines;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    const int c = (int)(t & 1);
+    const long q = t >> 1;
+    const int line = (int)(q % nlines), j = (int)(q / nlines);
+    const cd sp = mk(shp[2 * line], shp[2 * line + 1]);
+    const double rr[5] = {r0, r1, r2, r3, r4};
+    double s = 0.0;
+    for (int d = -4; d <= 4; d++) {
+      int jj = j + d;
+      cd ph = mk(1.0, 0.0);
+      if (jj < 0) {
+        jj += N;
+        ph = cj(sp);
+      } else if (jj >= N) {
+        jj -= N;
+        ph = sp;
+      }
+      const cd v = mk(u[2 * ((long)jj * ldu + line)], u[2 * ((long)jj * ldu + line) + 1]);
+      const cd w = ph * v;
+      s += rr[d < 0 ? -d : d] * (c ? w.y : w.x);
+    }
+    out[2 * ((long)j * ldo + line) + c] = s;
+  }
+}
+
+cudaError_t launch_filter_rhs(int nlines, int N, const double *u, long ldu, double *out, long ldo,
+                              const double *shp, const double r[5], cudaStream_t st) {
+  k_filter_rhs<<<256, 256, 0, st>>>(nlines, N, u, ldu, out, ldo, shp, r[0], r[1], r[2], r[3], r[4]);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_op_line(int nlines, int N, const double *u, long ldu, double *out, long ldo,
                            double *ybuf, const Fac &F, const double *shp, const double *shm,
                            const double r[4], int anti, cudaStream_t st) {

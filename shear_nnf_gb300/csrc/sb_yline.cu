@@ -412,6 +412,41 @@ __global__ void __launch_bounds__(32 * kSeg) k_filter(Grid g, Bufs bf, int rk) {
     for (int i = L.r0; i <= L.r1; i++) scr[2 * (i - 1)] = (R)ys[(i - L.r0) * ystr];
 }
 
+// d/dy of the mean profiles u00, w00 (derivyc with m = 1, as hvhg computes
+// them, cross.f90:1186-1192) after the y dealiasing changed them: one block
+// per box (the mean-line slot of line_thread with a single role-less group)
+template <typename R>
+__global__ void __launch_bounds__(32 * kSeg) k_meand1(Grid g, Bufs bf) {
+  __shared__ double xch[kSeg][16][2][SB_XS];
+  const int b = blockIdx.x;
+  if (bf.mem[b].halted) return;
+  LineThread L;
+  const int lane = threadIdx.x & 31;
+  L.b = b;
+  L.role = 0;
+  L.mean = true;
+  L.s = threadIdx.x >> 5;
+  L.l = lane >> 1;
+  L.c = lane & 1;
+  L.lc = 0;
+  L.active = (L.l == 0);
+  L.i = 0;
+  L.k = 0;
+  L.r0 = g.slo[L.s];
+  L.r1 = (L.s == kSeg - 1) ? g.my : g.shi[L.s];
+  const int N = g.my, ystr = blockDim.x;
+  double *ys = ycol();
+  const FacView V1(bf.d1, 0);
+  const SegView W1(bf.d1, 0);
+  const R *mu = (const R *)bf.mu + (long)b * 2 * N + L.c;
+  R *mdu = (R *)bf.mdu + (long)b * 2 * N + L.c;
+  const cd one = mk(1.0, 0.0);
+  const Tail T1 = load_tail(bf.tl1o + (long)b * g.nkx * SB_TAIL);
+  SEG_SOLVE(mu, 2, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true);
+  if (L.active)
+    for (int i = L.r0; i <= L.r1; i++) mdu[2 * (i - 1)] = (R)ys[(i - L.r0) * ystr];
+}
+
 // set_conj on the state (operators.f90:1382-1429) at entry of a cross call
 template <typename R>
 __global__ void k_setconj(Grid g, Bufs bf) {
@@ -616,6 +651,10 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
   if (shear) {
     M.xwb[rk] = M.xoffb + r1 * (g.s * (-g.Ly));
     M.xwt[rk] = M.xofft + r1 * (g.s * g.Ly);
+    if (g.ydeal == 2) {  // cross.f90:733-736
+      M.xwb[rk] = (M.xwb[rk] / g.Lx - trunc(M.xwb[rk] / g.Lx)) * g.Lx;
+      M.xwt[rk] = -M.xwb[rk];
+    }
   } else {
     M.xwb[rk] = M.xwb[rk - 1];
     M.xwt[rk] = M.xwt[rk - 1];
@@ -726,6 +765,8 @@ cudaError_t prepare_line(const Grid &g) {
   cudaFuncSetAttribute(k_lineL<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   cudaFuncSetAttribute(k_filter<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   cudaFuncSetAttribute(k_filter<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_meand1<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_meand1<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   return cudaGetLastError();
 }
 
@@ -755,6 +796,14 @@ cudaError_t launch_lineL(const Grid &g, const Bufs &bf, cudaStream_t st) {
     k_lineL<float><<<nb, kLineT, line_smem(g), st>>>(g, bf);
   else
     k_lineL<double><<<nb, kLineT, line_smem(g), st>>>(g, bf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_meand1(const Grid &g, const Bufs &bf, cudaStream_t st) {
+  if (g.prec)
+    k_meand1<float><<<g.B, kLineT, line_smem(g), st>>>(g, bf);
+  else
+    k_meand1<double><<<g.B, kLineT, line_smem(g), st>>>(g, bf);
   return cudaGetLastError();
 }
 
