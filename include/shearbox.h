@@ -188,6 +188,35 @@ int sb_op_derivyc_noalloc(int my, double Ly, int iord, int nlines, const double 
                           double *out, long ldo, const double *shp, const double *shm,
                           void *stream);
 
+/* Restart files in the reference's binary layout (no GPU needed).
+ * sb_write_restart writes the state (pencil layout, as sb_set_state takes it)
+ * as escru does (readwrite.f90:1336-1398): Fortran unformatted sequential
+ * records with 32-bit little-endian length markers -- grid, parameters, y,
+ * offsets, u00/w00, one record per y plane (vor.re, phi.re, vor.im, phi.im for
+ * every kz, kx), then the footer CFL/uprim/vbulk/xforce, irev/nopt/nparams,
+ * the 9 switches and 13 parameters.
+ * sb_read_restart reads one as getfil does (readwrite.f90:72-447): with p NULL
+ * only *info is filled; otherwise the state is mapped on p's grid (the common
+ * kx modes and the lowest positive and negative kz modes, zeros elsewhere;
+ * the file's my must equal p->my) and set_conj is applied.  Errors: 7 I/O,
+ * 8 malformed file, 9 unsupported grid change; message in sb_last_error. */
+#define SB_RESTART_MAXOPT 32
+typedef struct sb_restart_info {
+  int mgalx, my, mgalz, numerop;         /* record 1 */
+  double time, Re, alp, Ly, gam, s, chi; /* record 2 (Ly = stored Ly/pi times pi) */
+  int mx, mye, mz;
+  double xoffb, xofft, zoffb, zofft;     /* record 4 */
+  double CFL, uprim, vbulk, xforce;      /* footer */
+  int has_footer, irev, nopt, nparams;
+  int options[SB_RESTART_MAXOPT];
+  double params[SB_RESTART_MAXOPT];
+} sb_restart_info;
+int sb_write_restart(const char *path, const sb_params *p, const double *vor, const double *phi,
+                     const double *u00, const double *w00, double time, double xoffb,
+                     double xofft, double deltat);
+int sb_read_restart(const char *path, const sb_params *p, double *vor, double *phi, double *u00,
+                    double *w00, sb_restart_info *info);
+
 /* CUDA stream of the handle (cudaStream_t) and a blocking wait on it. */
 void *sb_get_stream(sb_handle *h);
 int sb_sync(sb_handle *h);

@@ -39,6 +39,27 @@ class SbParams(ctypes.Structure):
     ]
 
 
+RESTART_MAXOPT = 32
+
+
+class SbRestartInfo(ctypes.Structure):
+    _fields_ = [
+        ("mgalx", ctypes.c_int), ("my", ctypes.c_int), ("mgalz", ctypes.c_int),
+        ("numerop", ctypes.c_int),
+        ("time", ctypes.c_double), ("Re", ctypes.c_double), ("alp", ctypes.c_double),
+        ("Ly", ctypes.c_double), ("gam", ctypes.c_double), ("s", ctypes.c_double),
+        ("chi", ctypes.c_double),
+        ("mx", ctypes.c_int), ("mye", ctypes.c_int), ("mz", ctypes.c_int),
+        ("xoffb", ctypes.c_double), ("xofft", ctypes.c_double), ("zoffb", ctypes.c_double),
+        ("zofft", ctypes.c_double),
+        ("CFL", ctypes.c_double), ("uprim", ctypes.c_double), ("vbulk", ctypes.c_double),
+        ("xforce", ctypes.c_double),
+        ("has_footer", ctypes.c_int), ("irev", ctypes.c_int), ("nopt", ctypes.c_int),
+        ("nparams", ctypes.c_int),
+        ("options", ctypes.c_int * RESTART_MAXOPT), ("params", ctypes.c_double * RESTART_MAXOPT),
+    ]
+
+
 class SbStatus(ctypes.Structure):
     _fields_ = [
         ("istop", ctypes.c_int), ("steps_done", ctypes.c_int), ("ntrace", ctypes.c_int),
@@ -53,7 +74,8 @@ ABI_FUNCTIONS = [
     "sb_get_status", "sb_get_trace", "sb_cross", "sb_get_stream", "sb_sync", "sb_sizes",
     "sb_seed_state", "sb_compact_coeffs", "sb_last_error", "sb_version", "sb_launch_stage",
     "sb_fp64_peak", "sb_op_derivyc", "sb_op_lapcdy", "sb_op_derivyc_noalloc",
-    "sb_set_member_etime", "sb_op_filterc", "sb_op_cfty", "sb_op_rfty",
+    "sb_set_member_etime", "sb_op_filterc", "sb_op_cfty", "sb_op_rfty", "sb_write_restart",
+    "sb_read_restart",
 ]
 
 _lib = None
@@ -103,6 +125,11 @@ def lib(auto_build: bool = False):
                                 dp, vp]
     L.sb_op_cfty.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.c_long, ctypes.c_int, vp]
     L.sb_op_rfty.argtypes = list(L.sb_op_cfty.argtypes)
+    L.sb_write_restart.argtypes = [ctypes.c_char_p, ctypes.POINTER(SbParams), dp, dp, dp, dp,
+                                   ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_double]
+    L.sb_read_restart.argtypes = [ctypes.c_char_p, ctypes.POINTER(SbParams), dp, dp, dp, dp,
+                                  ctypes.POINTER(SbRestartInfo)]
     _lib = L
     return L
 
@@ -281,6 +308,39 @@ def op_lapcdy(my: int, Ly: float, u_dev: int, out_dev: int, nlines: int, k2: np.
                               int(ldu or nlines), ctypes.c_void_p(out_dev), int(ldo or nlines),
                               _dp(kk), _dp(sp.view(np.float64)), _dp(sm.view(np.float64)),
                               ctypes.c_void_p(stream)))
+
+
+def write_restart(path: str, p: SbParams, state: dict, deltat: float = 0.0):
+    """Writes a state (pencil layout) as a restart file of the reference's
+    binary layout (escru)."""
+    vor = np.ascontiguousarray(state["vor"], np.complex128)
+    phi = np.ascontiguousarray(state["phi"], np.complex128)
+    u00 = np.ascontiguousarray(state["u00"], np.float64)
+    w00 = np.ascontiguousarray(state["w00"], np.float64)
+    _check(lib().sb_write_restart(str(path).encode(), ctypes.byref(p), _dp(vor.view(np.float64)),
+                                  _dp(phi.view(np.float64)), _dp(u00), _dp(w00),
+                                  float(state["time"]), float(state["xoffb"]),
+                                  float(state["xofft"]), float(deltat)))
+
+
+def read_restart(path: str, p: SbParams = None):
+    """Reads a restart file (getfil).  Returns (state on p's grid, info), or
+    (None, info) without p."""
+    info = SbRestartInfo()
+    if p is None:
+        _check(lib().sb_read_restart(str(path).encode(), None, None, None, None, None,
+                                     ctypes.byref(info)))
+        return None, info
+    sz = sizes(p)
+    vor = np.zeros((sz["mz"], sz["nkx"], p.my), np.complex128)
+    phi = np.zeros_like(vor)
+    u00 = np.zeros(p.my)
+    w00 = np.zeros(p.my)
+    _check(lib().sb_read_restart(str(path).encode(), ctypes.byref(p), _dp(vor.view(np.float64)),
+                                 _dp(phi.view(np.float64)), _dp(u00), _dp(w00),
+                                 ctypes.byref(info)))
+    return {"vor": vor, "phi": phi, "u00": u00, "w00": w00, "time": info.time,
+            "xoffb": info.xoffb, "xofft": info.xofft}, info
 
 
 def op_filterc(my: int, u_dev: int, out_dev: int, nlines: int, shp: np.ndarray,

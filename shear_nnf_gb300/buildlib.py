@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libshearbox.so")
-SOURCES = ["sb_kernels.cu", "sb_yline.cu", "sb_ops.cu", "sb_noalloc.cu", "sb_api.cu", "sb_host.cpp"]
+SOURCES = ["sb_kernels.cu", "sb_yline.cu", "sb_ops.cu", "sb_noalloc.cu", "sb_api.cu", "sb_host.cpp",
+           "sb_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC"]
 

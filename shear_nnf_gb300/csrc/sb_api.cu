@@ -23,6 +23,9 @@
 using namespace sb;
 
 static thread_local std::string g_err;
+namespace sb {
+void set_error(const std::string &msg) { g_err = msg; }
+}
 static int fail(int code, const char *fmt, ...) {
   char buf[512];
   va_list ap;

@@ -1,0 +1,277 @@
+// sb_io.cpp -- restart files in the reference's binary layout (escru writer,
+// readwrite.f90:1336-1398; getfil reader, readwrite.f90:72-447).
+//
+// The file is a Fortran unformatted sequential file: every record is framed by
+// its byte length as a little-endian 32-bit integer before and after the
+// payload (the gfortran/ifort default; the reference builds with
+// -fconvert=little-endian).  Records, in order:
+//    1  mgalx, my, mgalz, numerop                               4 int32
+//    2  time, Re, alp, Ly/pi, gam, s, chi; mx, my, mz            7 float64, 3 int32
+//    3  y(0:my-1)                                               my float64
+//    4  xoffb, xofft, zoffb, zofft                              4 float64
+//    5  u00(0:my-1), w00(0:my-1)                                2 my float64
+//    6  one record per y plane: for kz, for kx (kx fastest):
+//       vor.re, phi.re, vor.im, phi.im                          4 nkx mz float64
+//    7  CFL, uprim, vbulk, xforce                               4 float64
+//    8  irev, nopt, nparams                                     3 int32
+//    9  the nopt switches (explicit, ifix_dt, iadd_force, iadd_mode, iadd_sym,
+//       iadd_damping, iuse_LES, iadd_visc, idynamic)            nopt int32
+//   10  the nparams parameters (Deltat, force_roll, xforce, zforce, damp_aa,
+//       damp_up, Cles, Deltag, cutoffx, cutoffz, LESflt(1:3))   nparams float64
+// The state arrays of the C-ABI keep the reference pencil layout
+// complex(0:my1, 0:mx1, 0:mz1) (y fastest).
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/shearbox.h"
+
+namespace sb {
+void set_error(const std::string &msg);  // the message sb_last_error returns (sb_api.cu)
+}
+
+namespace {
+
+struct File {
+  FILE *f = nullptr;
+  ~File() {
+    if (f) fclose(f);
+  }
+};
+
+void put_u32(std::vector<unsigned char> &b, uint32_t v) {
+  for (int q = 0; q < 4; q++) b.push_back((unsigned char)((v >> (8 * q)) & 0xffu));
+}
+uint32_t get_u32(const unsigned char *p) {
+  return (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+}
+void put_i32(std::vector<unsigned char> &b, int v) { put_u32(b, (uint32_t)v); }
+void put_f64(std::vector<unsigned char> &b, double v) {
+  uint64_t u;
+  memcpy(&u, &v, 8);
+  for (int q = 0; q < 8; q++) b.push_back((unsigned char)((u >> (8 * q)) & 0xffu));
+}
+double get_f64(const unsigned char *p) {
+  uint64_t u = 0;
+  for (int q = 0; q < 8; q++) u |= (uint64_t)p[q] << (8 * q);
+  double v;
+  memcpy(&v, &u, 8);
+  return v;
+}
+int get_i32(const unsigned char *p) { return (int)get_u32(p); }
+
+bool write_record(FILE *f, const std::vector<unsigned char> &payload) {
+  std::vector<unsigned char> m;
+  put_u32(m, (uint32_t)payload.size());
+  return fwrite(m.data(), 1, 4, f) == 4 &&
+         fwrite(payload.data(), 1, payload.size(), f) == payload.size() &&
+         fwrite(m.data(), 1, 4, f) == 4;
+}
+
+// reads one record; false at end of file or on a broken frame
+bool read_record(FILE *f, std::vector<unsigned char> *payload, std::string *err) {
+  unsigned char m[4];
+  if (fread(m, 1, 4, f) != 4) return false;
+  const uint32_t n = get_u32(m);
+  if (n > (1u << 30)) {
+    *err = "record length out of range";
+    return false;
+  }
+  payload->resize(n);
+  if (n && fread(payload->data(), 1, n, f) != n) {
+    *err = "truncated record";
+    return false;
+  }
+  unsigned char e[4];
+  if (fread(e, 1, 4, f) != 4 || get_u32(e) != n) {
+    *err = "record end marker mismatch";
+    return false;
+  }
+  return true;
+}
+
+int io_fail(int code, const std::string &msg) {
+  sb::set_error(msg);
+  return code;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sb_write_restart(const char *path, const sb_params *p, const double *vor, const double *phi,
+                     const double *u00, const double *w00, double time, double xoffb,
+                     double xofft, double deltat) {
+  if (!path || !p || !vor || !phi || !u00 || !w00) return io_fail(1, "null argument");
+  const int my = p->my, mx = 2 * (p->mgalx / 3), mz = 2 * (p->mgalz / 3) - 1, nkx = mx / 2;
+  if (my < 1 || nkx < 1 || mz < 1) return io_fail(1, "bad grid");
+  const double pi = 4.0 * std::atan(1.0);
+  File fh;
+  fh.f = fopen(path, "wb");
+  if (!fh.f) return io_fail(7, std::string("cannot open ") + path);
+  std::vector<unsigned char> r;
+  bool ok = true;
+  auto flush = [&]() {
+    ok = ok && write_record(fh.f, r);
+    r.clear();
+  };
+  put_i32(r, p->mgalx); put_i32(r, my); put_i32(r, p->mgalz); put_i32(r, 1);
+  flush();
+  put_f64(r, time); put_f64(r, p->Re); put_f64(r, p->alp); put_f64(r, p->Ly / pi);
+  put_f64(r, p->gam); put_f64(r, p->s); put_f64(r, p->chi);
+  put_i32(r, mx); put_i32(r, my); put_i32(r, mz);
+  flush();
+  const double dy = p->Ly / (double)my;
+  for (int j = 0; j < my; j++) put_f64(r, (double)j * dy - 0.5 * p->Ly);  // y (initcr.f90:486-488)
+  flush();
+  put_f64(r, xoffb); put_f64(r, xofft); put_f64(r, 0.0); put_f64(r, 0.0);
+  flush();
+  for (int j = 0; j < my; j++) put_f64(r, u00[j]);
+  for (int j = 0; j < my; j++) put_f64(r, w00[j]);
+  flush();
+  for (int j = 0; j < my && ok; j++) {
+    for (int k = 0; k < mz; k++)
+      for (int i = 0; i < nkx; i++) {
+        const size_t q = 2 * (((size_t)k * nkx + i) * my + j);
+        put_f64(r, vor[q]); put_f64(r, phi[q]); put_f64(r, vor[q + 1]); put_f64(r, phi[q + 1]);
+      }
+    flush();
+  }
+  put_f64(r, p->CFL); put_f64(r, p->uprim); put_f64(r, p->vbulk); put_f64(r, 0.0);
+  flush();
+  put_i32(r, 1742); put_i32(r, 9); put_i32(r, 13);  // irev (mod.f90:45), nopt, nparams
+  flush();
+  const int opts[9] = {1, p->fixed_dt > 0 ? 1 : 0, 0, 5, 0, 0, p->les ? 1 : 0,
+                       p->les_visc ? 1 : 0, 0};
+  for (int q = 0; q < 9; q++) put_i32(r, opts[q]);
+  flush();
+  const double dx = 2.0 * pi / p->alp / (double)mx, dz = 2.0 * pi / p->gam / (double)mz;
+  const double deltag = p->les ? std::pow(dx * dy * dz, 1.0 / 3.0) : 0.0;
+  const double prm[13] = {deltat, 0.0, 0.0, 0.0, 0.0, 0.0, p->les ? p->cs : 0.0, deltag,
+                          0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int q = 0; q < 13; q++) put_f64(r, prm[q]);
+  flush();
+  if (!ok) return io_fail(7, std::string("write failed: ") + path);
+  return 0;
+}
+
+int sb_read_restart(const char *path, const sb_params *p, double *vor, double *phi, double *u00,
+                    double *w00, sb_restart_info *info) {
+  if (!path || !info) return io_fail(1, "null argument");
+  memset(info, 0, sizeof(*info));
+  File fh;
+  fh.f = fopen(path, "rb");
+  if (!fh.f) return io_fail(7, std::string("cannot open ") + path);
+  std::vector<unsigned char> r;
+  std::string err;
+  auto need = [&](size_t n, const char *what) -> int {
+    if (!read_record(fh.f, &r, &err)) return io_fail(8, std::string(what) + ": " + (err.empty() ? "missing" : err));
+    if (r.size() < n) return io_fail(8, std::string(what) + ": record too short");
+    return 0;
+  };
+  int rc;
+  if ((rc = need(16, "grid record"))) return rc;
+  info->mgalx = get_i32(&r[0]);
+  info->my = get_i32(&r[4]);
+  info->mgalz = get_i32(&r[8]);
+  info->numerop = get_i32(&r[12]);
+  if ((rc = need(68, "parameter record"))) return rc;
+  const double pi = 4.0 * std::atan(1.0);
+  info->time = get_f64(&r[0]);
+  info->Re = get_f64(&r[8]);
+  info->alp = get_f64(&r[16]);
+  info->Ly = get_f64(&r[24]) * pi;
+  info->gam = get_f64(&r[32]);
+  info->s = get_f64(&r[40]);
+  info->chi = get_f64(&r[48]);
+  info->mx = get_i32(&r[56]);
+  info->mye = get_i32(&r[60]);
+  info->mz = get_i32(&r[64]);
+  const int mye = info->mye, mxe = info->mx, mze = info->mz;
+  if (mye < 1 || mxe < 2 || mze < 1 || mye > 1 << 16 || mxe > 1 << 16 || mze > 1 << 16)
+    return io_fail(8, "sizes out of range");
+  if ((rc = need(8 * (size_t)mye, "y record"))) return rc;
+  if (std::fabs(info->Ly + 2.0 * get_f64(&r[0])) > 1e-9 * std::fmax(1.0, info->Ly))
+    return io_fail(8, "y(0) is not -Ly/2: broken file (getfil, readwrite.f90:146-149)");
+  if ((rc = need(32, "offset record"))) return rc;
+  info->xoffb = get_f64(&r[0]);
+  info->xofft = get_f64(&r[8]);
+  info->zoffb = get_f64(&r[16]);
+  info->zofft = get_f64(&r[24]);
+  if ((rc = need(16 * (size_t)mye, "mean profile record"))) return rc;
+  std::vector<double> m00(2 * (size_t)mye);
+  for (int q = 0; q < 2 * mye; q++) m00[q] = get_f64(&r[8 * (size_t)q]);
+  // the state, mapped on the caller's grid (getfil, readwrite.f90:252-305):
+  // common kx modes, the klen lowest positive and negative kz modes
+  const int nkxe = mxe / 2;
+  std::vector<std::vector<unsigned char>> planes((size_t)mye);
+  for (int j = 0; j < mye; j++) {
+    if ((rc = need(32 * (size_t)nkxe * mze, "plane record"))) return rc;
+    planes[j].swap(r);
+  }
+  // footer (optional in old files, readwrite.f90:311-323)
+  if (read_record(fh.f, &r, &err) && r.size() >= 32) {
+    info->CFL = get_f64(&r[0]);
+    info->uprim = get_f64(&r[8]);
+    info->vbulk = get_f64(&r[16]);
+    info->xforce = get_f64(&r[24]);
+    if (read_record(fh.f, &r, &err) && r.size() >= 12) {
+      info->irev = get_i32(&r[0]);
+      info->nopt = get_i32(&r[4]);
+      info->nparams = get_i32(&r[8]);
+      if (read_record(fh.f, &r, &err))
+        for (int q = 0; q < info->nopt && q < SB_RESTART_MAXOPT && 4 * (size_t)(q + 1) <= r.size(); q++)
+          info->options[q] = get_i32(&r[4 * (size_t)q]);
+      if (read_record(fh.f, &r, &err))
+        for (int q = 0; q < info->nparams && q < SB_RESTART_MAXOPT && 8 * (size_t)(q + 1) <= r.size(); q++)
+          info->params[q] = get_f64(&r[8 * (size_t)q]);
+      info->has_footer = 1;
+    }
+  }
+  if (!p) return 0;  // header only
+  if (!vor || !phi || !u00 || !w00) return io_fail(1, "null state array");
+  const int my = p->my, mx = 2 * (p->mgalx / 3), mz = 2 * (p->mgalz / 3) - 1, nkx = mx / 2;
+  const int nz = (mz - 1) / 2;
+  if (my != mye)
+    return io_fail(9, "the file has my=" + std::to_string(mye) + ", the run my=" +
+                          std::to_string(my) + " (y interpolation is not supported)");
+  memset(vor, 0, sizeof(double) * 2 * (size_t)my * nkx * mz);
+  memset(phi, 0, sizeof(double) * 2 * (size_t)my * nkx * mz);
+  for (int j = 0; j < my; j++) {
+    u00[j] = m00[j];
+    w00[j] = m00[(size_t)mye + j];
+  }
+  const int mxm = std::min(nkx, nkxe), mzm = std::min(mz, mze);
+  const int klen = (mzm + 1) / 2, kini1 = mze - klen, kini2 = mz - klen;
+  for (int j = 0; j < my; j++) {
+    const unsigned char *pl = planes[j].data();
+    auto put = [&](int ke, int k) {
+      for (int i = 0; i < mxm; i++) {
+        const unsigned char *e = pl + 32 * ((size_t)ke * nkxe + i);
+        const size_t q = 2 * (((size_t)k * nkx + i) * my + j);
+        vor[q] = get_f64(e);
+        phi[q] = get_f64(e + 8);
+        vor[q + 1] = get_f64(e + 16);
+        phi[q + 1] = get_f64(e + 24);
+      }
+    };
+    for (int k = 0; k < klen; k++) put(k, k);
+    for (int t = 1; t < klen; t++) put(kini1 + t, kini2 + t);
+  }
+  // set_conj on the read state (readwrite.f90:376; operators.f90:1382-1429)
+  for (int k = nz + 1; k < mz; k++)
+    for (int j = 0; j < my; j++) {
+      const size_t dst = 2 * ((size_t)k * nkx * my + j), src = 2 * ((size_t)(mz - k) * nkx * my + j);
+      vor[dst] = vor[src];
+      vor[dst + 1] = -vor[src + 1];
+      phi[dst] = phi[src];
+      phi[dst + 1] = -phi[src + 1];
+    }
+  return 0;
+}
+
+}  // extern "C"
