@@ -18,6 +18,8 @@ SOURCES = ["sb_kernels.cu", "sb_yline.cu", "sb_ops.cu", "sb_noalloc.cu", "sb_api
            "sb_io.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC"]
+# extra compile flags for tuning builds, e.g. SB_NVCC_EXTRA="-DSB_KSEG=4"
+EXTRA = os.environ.get("SB_NVCC_EXTRA", "").split()
 
 
 def nvcc() -> str:
@@ -43,7 +45,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     for src in SOURCES:
         obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         objs.append(obj)
-        cmd = [nvcc(), *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc(), *ARCH, *FLAGS, *EXTRA, "-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cpp"):
             cmd = [nvcc(), *FLAGS, "-x", "c++", "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:

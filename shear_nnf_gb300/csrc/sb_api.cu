@@ -364,7 +364,7 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   }
   cudaError_t ce = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
   if (ce != cudaSuccess) {
-    delete h;
+    sb_destroy(h);
     return fail(3, "stream: %s", cudaGetErrorString(ce));
   }
   Bufs &bf = h->bf;
@@ -373,8 +373,9 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   if ((rc = A(&bf.vor, B * F)) || (rc = A(&bf.phi, B * F)) || (rc = A(&bf.vorwk, B * F)) ||
       (rc = A(&bf.phiwk, B * F)) || (rc = A(&bf.G, B * F)) || (rc = A(&bf.V, B * F)) ||
       (rc = A(&bf.D, B * F)) || (rc = A(&bf.S, B * F)) || (rc = A(&bf.T, B * F)) ||
+      (rc = A(&bf.Lv, B * F)) ||
       (rc = A(&bf.tl1o, B * g.nkx * SB_TAIL)) || (rc = A(&bf.tl2o, B * g.nkx * SB_TAIL)) ||
-      (rc = A(&bf.tl1n, B * g.nkx * SB_TAIL)) ||
+      (rc = A(&bf.tl1n, B * g.nkx * SB_TAIL)) || (rc = A(&bf.tl2n, B * g.nkx * SB_TAIL)) ||
       (rc = A(&bf.mu, B * 2 * my)) || (rc = A(&bf.mwk, B * 2 * my)) ||
       (rc = A(&bf.mrf, B * 2 * my)) || (rc = A(&bf.mdu, B * 2 * my)) ||
       (rc = A(&bf.zbuf, B * my * g.mgalz * g.nzf * g.nkx * 2)) ||

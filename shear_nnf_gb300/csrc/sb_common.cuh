@@ -103,11 +103,12 @@ struct Bufs {
   // pointers are typed double for bookkeeping and cast by the kernels
   double *vor, *phi, *vorwk, *phiwk, *G, *V, *D;
   double *T, *S;                 // d/dy of the NL term and d2(phi)/dy2 between the line kernels
+  double *Lv;                    // d2(omega_y)/dy2 of the next substep's starting state
   double *mu, *mwk, *mrf, *mdu;  // mean lines (u00 + i w00) [B][my] complex
   double *zbuf, *xbuf;           // plane-stage intermediates
   double *hpart;                 // hist partials [B][my][ncb][SB_NHIST_Q]
   double *sh_old, *sh_new;       // [B][2][nkx] complex (t then b)
-  double *tl1o, *tl2o, *tl1n;    // shear tails of d/dy, d2/dy2 (old phase), d/dy (new) [B][nkx][SB_TAIL]
+  double *tl1o, *tl2o, *tl1n, *tl2n;  // shear tails of d/dy, d2/dy2 at the old and new phases [B][nkx][SB_TAIL]
   double *mf1, *mf2;             // moving-frame phases [B][my][nkx] complex
   double *trace;                 // [B][cap][SB_TRACE_LEN]
   Member *mem;                   // [B]

@@ -196,8 +196,8 @@ __device__ __forceinline__ void solve_line(const TU *u, long ps, double *ybuf, l
 #pragma unroll 4
   for (int j = N - 7; j >= 0; j--) {
     const int i = j + 1;
-    double x = V.Dm(i) * ybuf[(long)j * ys] - V.La(i + 1) * xa - V.Lb(i + 2) * xb -
-               V.Lc(i + 3) * xc - V.e(i) * pe - V.f(i) * pf - V.g(i) * pg;
+    double x = V.Dm(i) * ybuf[(long)j * ys] - V.e(i) * pe - V.f(i) * pf - V.g(i) * pg -
+               V.Lc(i + 3) * xc - V.Lb(i + 2) * xb - V.La(i + 1) * xa;
     epi(j, x);
     xc = xb;
     xb = xa;

@@ -54,16 +54,22 @@ __device__ __forceinline__ void solve_seg(const TU *u, long ps, double *ys, int 
   const double hi0 = cmul_c(u0, __shfl_xor_sync(0xffffffffu, u0, 1), shp, c),
                hi1 = cmul_c(u1, __shfl_xor_sync(0xffffffffu, u1, 1), shp, c),
                hi2 = cmul_c(u2, __shfl_xor_sync(0xffffffffu, u2, 1), shp, c);
+  const int rend = top ? N : hi;
+  // stage the segment's rows of u in the solution column: all loads issued
+  // up front instead of one per step of the recurrence; the forward sweep
+  // reads row i+4 before it overwrites row i
+#pragma unroll 8
+  for (int i = lo; i <= rend; i++) ys[(i - lo) * ystr] = (double)u[(long)(i - 1) * ps];
   auto ext = [&](int i) -> double {  // extended line, 1-based row
     if (i < 1) return i == -2 ? lo3 : (i == -1 ? lo2 : lo1);
     if (i > N) return i == N + 1 ? hi0 : (i == N + 2 ? hi1 : hi2);
+    if (i >= lo && i <= rend) return ys[(i - lo) * ystr];
     return (double)u[(long)(i - 1) * ps];
   };
   // ---- forward substitution of the segment from a zero incoming state
   double w0 = ext(lo - 3), w1 = ext(lo - 2), w2 = ext(lo - 1), w3 = ext(lo), w4 = ext(lo + 1),
          w5 = ext(lo + 2), w6 = ext(lo + 3);
   double y1 = 0.0, y2 = 0.0, y3 = 0.0, Se = 0.0, Sf = 0.0, Sg = 0.0;
-  const int rend = top ? N : hi;
   double bN2 = 0.0, bN1 = 0.0, bN0 = 0.0;
 #pragma unroll 4
   for (int i = lo; i <= rend; i++) {
@@ -172,8 +178,10 @@ __device__ __forceinline__ void solve_seg(const TU *u, long ps, double *ys, int 
 #pragma unroll 4
   for (int i = ibeg; i >= lo; i--) {
     const double y = ys[(i - lo) * ystr] + W.hf(1, i) * Ya + W.hf(2, i) * Yb + W.hf(3, i) * Yc;
-    const double x = V.Dm(i) * y - V.La(i + 1) * xa - V.Lb(i + 2) * xb - V.Lc(i + 3) * xc -
-                     V.e(i) * pe - V.f(i) * pf - V.g(i) * pg;
+    // the previous row enters last: one dependent multiply-add per row on the
+    // loop-carried path (the reference's order puts it first)
+    const double x = V.Dm(i) * y - V.e(i) * pe - V.f(i) * pf - V.g(i) * pg - V.Lc(i + 3) * xc -
+                     V.Lb(i + 2) * xb - V.La(i + 1) * xa;
     ys[(i - lo) * ystr] = x;
     xc = xb;
     xb = xa;

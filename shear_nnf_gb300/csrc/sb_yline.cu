@@ -5,11 +5,13 @@
 // solves occupy separate warps (GB300's FP64 pipe needs about one busy warp per
 // SM sub-partition, and one warp per line component is too few):
 //   k_lineA  role 0: d/dy of dH1/dx + dH3/dz                 (derivyc, -> T)
-//            role 1: nu*lap(omega_y), RK3 update of omega_y, zeta store and
+//            role 1: nu*lap(omega_y) (d2/dy2 from Lv, taken by k_lineB of the
+//                    previous substep), RK3 update of omega_y, zeta store and
 //                    moving_frame remaps                       (visc3d + update)
 //            role 2: d2(phi)/dy2                               (derivyc, -> S)
 //            mean warp: nu*u00'', RK3 update of u00, w00
-//   k_lineB  role 0: d(omega_y)/dy for the next substep         (-> D)
+//   k_lineB  role 0: d(omega_y)/dy and d2(omega_y)/dy2 for the next
+//                    substep                                   (-> D, Lv)
 //            role 1: RK3 update of phi, v = lapcdy(phi), dv/dy  (-> phi, G, V)
 //            mean warp: du00/dy, dw00/dy for the next substep
 // The same k_lineB (mode 0) is the prologue of a cross call: v from phi on the
@@ -35,7 +37,15 @@ __device__ __forceinline__ cd ldc2(const double *p) { return mk(p[0], p[1]); }
 // Block -> (member, role, group of 16 lines); warp -> segment of the banded
 // rows; lane -> (line of the group, component).  The last block of every
 // member is the mean line u00 + i w00 (line slot 0).
-constexpr int kSeg = 2;  // segments per line solve (warps per block)
+// segments per line solve (warps per block) and the blocks per SM the line
+// kernels are register-budgeted for (build-time tuning knobs)
+#ifndef SB_KSEG
+#define SB_KSEG 2
+#endif
+#ifndef SB_LINE_MINB
+#define SB_LINE_MINB 1
+#endif
+constexpr int kSeg = SB_KSEG;
 struct LineThread {
   int b, role, c, s, l, i, k, r0, r1;
   long lc;
@@ -128,7 +138,7 @@ __device__ __forceinline__ void rk_update(const double *ys, int ystr, const R *_
                   R0, R1, R2, R3, ANTI, &xch[0][0][0][0])
 
 template <typename R>
-__global__ void __launch_bounds__(32 * kSeg) k_lineA(Grid g, Bufs bf, int rk1) {
+__global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs bf, int rk1) {
   __shared__ double xch[kSeg][16][2][SB_XS];
   LineThread L;
   if (!line_thread(g, 3, &L)) return;  // whole blocks
@@ -184,9 +194,16 @@ __global__ void __launch_bounds__(32 * kSeg) k_lineA(Grid g, Bufs bf, int rk1) {
     store_col(ys, ystr, (R *)bf.S + off, ps, L);
     return;
   }
-  // role 1: hg += nu*lap(omega_y) (visc3d, cross.f90:659), RK3 update, remaps
-  SEG_SOLVE((const R *)bf.vor + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
-            g.rh2[6], false);
+  // role 1: hg += nu*lap(omega_y) (visc3d, cross.f90:659), RK3 update, remaps.
+  // d2(omega_y)/dy2 of the substep's starting state was taken by k_lineB of the
+  // previous substep, unless a y filter changed the state since
+  if (g.ydeal) {
+    SEG_SOLVE((const R *)bf.vor + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
+              g.rh2[6], false);
+  } else {
+    const R *lv = (const R *)bf.Lv + off;
+    for (int r = L.r0; r <= L.r1; r++) ys[(r - L.r0) * ystr] = (double)lv[(long)(r - 1) * ps];
+  }
   const bool is00 = (i == 0 && k == 0);
   const double a = g.alp * i;
   const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
@@ -197,7 +214,7 @@ __global__ void __launch_bounds__(32 * kSeg) k_lineA(Grid g, Bufs bf, int rk1) {
 }
 
 template <typename R>
-__global__ void __launch_bounds__(32 * kSeg) k_lineB(Grid g, Bufs bf, int mode) {
+__global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs bf, int mode) {
   __shared__ double xch[kSeg][16][2][SB_XS];
   LineThread L;
   if (!line_thread(g, 2, &L)) return;
@@ -224,6 +241,7 @@ __global__ void __launch_bounds__(32 * kSeg) k_lineB(Grid g, Bufs bf, int mode) 
   // the phase at t + c_k dt (substeps) or at t (prologue)
   const double *sh = (mode == 0) ? bf.sh_old : bf.sh_new;
   const double *tl1 = (mode == 0) ? bf.tl1o : bf.tl1n;
+  const double *tl2 = (mode == 0) ? bf.tl2o : bf.tl2n;
   const cd shp = ldc2(sh + (long)L.b * 4 * g.nkx + 2 * i);
   const cd shm = ldc2(sh + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
   const Tail T1 = load_tail(tl1 + ((long)L.b * g.nkx + i) * SB_TAIL);
@@ -232,6 +250,16 @@ __global__ void __launch_bounds__(32 * kSeg) k_lineB(Grid g, Bufs bf, int mode) 
     SEG_SOLVE((const R *)bf.vor + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
               g.rh1[6], true);
     store_col(ys, ystr, (R *)bf.D + off, ps, L);
+    if (!g.ydeal) {
+      // d2(omega_y)/dy2 of the next substep's starting state (its visc3d,
+      // cross.f90:659), same phase
+      const FacView V2(bf.d2, 0);
+      const SegView W2(bf.d2, 0);
+      const Tail T2 = load_tail(tl2 + ((long)L.b * g.nkx + i) * SB_TAIL);
+      SEG_SOLVE((const R *)bf.vor + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
+                g.rh2[6], false);
+      store_col(ys, ystr, (R *)bf.Lv + off, ps, L);
+    }
     return;
   }
   const bool is00 = (i == 0 && k == 0);
@@ -280,7 +308,7 @@ __global__ void __launch_bounds__(32 * kSeg) k_lineB(Grid g, Bufs bf, int mode) 
 //           rk = -(kx^2 + kz^2), fac = -1)          (-> V)
 //   mean:   rf0u += d(T12_00)/dy, rf0w += d(T23_00)/dy
 template <typename R>
-__global__ void __launch_bounds__(32 * kSeg) k_lineL(Grid g, Bufs bf) {
+__global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineL(Grid g, Bufs bf) {
   __shared__ double xch[kSeg][16][2][SB_XS];
   LineThread L;
   if (!line_thread(g, 2, &L)) return;
@@ -676,15 +704,16 @@ __global__ void __launch_bounds__(128) k_tables(Grid g, Bufs bf, int rk) {
   const double xob = M.xwb[ro], xot = M.xwt[ro];
   const double xnb = M.xwb[rk], xnt = M.xwt[rk];
   const double Dt = M.Deltat;
-  const long ntail = (rk == 0) ? 2L * nkx : 3L * nkx;
+  const long ntail = (rk == 0) ? 2L * nkx : 4L * nkx;
   const long nmf = (rk == 0) ? 0 : (long)my * nkx;
   const long n = ntail + nmf;
   const FacView V1(bf.d1, 0), V2(bf.d2, 0);
   for (long q = (long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long)gridDim.x * blockDim.x) {
     if (q < ntail) {
+      // which: 0 d/dy old phase, 1 d2/dy2 old, 2 d/dy new, 3 d2/dy2 new
       const int which = (int)(q / nkx), i = (int)(q - (long)which * nkx);
       const double a = g.alp * i;
-      const bool nw = (which == 2);
+      const bool nw = (which >= 2);
       const double xt = nw ? xnt : xot, xb = nw ? xnb : xob;
       cd shp = mk(1.0, 0.0), shm = mk(1.0, 0.0);
       if (shear) {
@@ -693,15 +722,15 @@ __global__ void __launch_bounds__(128) k_tables(Grid g, Bufs bf, int rk) {
       }
       // the phase tables themselves (written once per kx)
       double *sh = (nw ? bf.sh_new : bf.sh_old) + (long)b * 4 * nkx;
-      if (which != 1) {
+      if (which == 0 || which == 2) {
         sh[2 * i] = shp.x;
         sh[2 * i + 1] = shp.y;
         sh[2 * (nkx + i)] = shm.x;
         sh[2 * (nkx + i) + 1] = shm.y;
       }
-      const Tail T = make_tail(which == 1 ? V2 : V1, shp, my);
-      double *dst = (which == 0 ? bf.tl1o : (which == 1 ? bf.tl2o : bf.tl1n)) +
-                    ((long)b * nkx + i) * SB_TAIL;
+      const Tail T = make_tail((which & 1) ? V2 : V1, shp, my);
+      double *const tl[4] = {bf.tl1o, bf.tl2o, bf.tl1n, bf.tl2n};
+      double *dst = tl[which] + ((long)b * nkx + i) * SB_TAIL;
       store_tail(dst, T);
     } else {
       // moving_frame phases exp(i kx y_j tau) (operators.f90:119-123)
@@ -830,7 +859,7 @@ cudaError_t launch_scalar(const Grid &g, const Bufs &bf, int rk, cudaStream_t st
 }
 
 cudaError_t launch_tables(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
-  const long n = 3L * g.nkx + (long)g.my * g.nkx;
+  const long n = 4L * g.nkx + (long)g.my * g.nkx;
   const int T = 128;
   dim3 grid((unsigned)((n + T - 1) / T), g.B);
   k_tables<<<grid, T, 0, st>>>(g, bf, rk);
