@@ -24,8 +24,11 @@ Pieces:
                 1905-2207), least squares on the block Hessenberg
   Residual      F(x) = shift(Phi_T(x)) - x (- rhs) from an FP64 period map
   newton        Newton iteration for shift(Phi_T(x)) - x = 0 at fixed T and
-                shifts (newton_shear.f90:183-597 without the period/shift
-                unknowns and the hookstep)
+                shifts (newton_shear.f90:183-597)
+  hookstep      trust-region step in the Krylov space (gmres_shear.f90:4064-4419)
+  ShiftJacobian, newton_shift
+                the streamwise shift as an unknown with its phase condition,
+                Newton or Newton-hookstep
 """
 from __future__ import annotations
 
@@ -188,18 +191,19 @@ class Jacobian:
         nb = self.block
         if nb < 1:
             raise ValueError("matvec: batch too small for one product")
-        return np.concatenate([self._matvec_block(D[:, q:q + nb])
-                               for q in range(0, D.shape[1], nb)], axis=1)
+        out = np.zeros_like(D)
+        nz = [q for q in range(D.shape[1]) if np.any(D[:, q])]  # J 0 = 0 without integrating
+        for q in range(0, len(nz), nb):
+            cols = nz[q:q + nb]
+            out[:, cols] = self._matvec_block(D[:, cols])
+        return out
 
     def _matvec_block(self, D: np.ndarray) -> np.ndarray:
         xn = np.linalg.norm(self.x0)
         eps_j = self.eps_jacobi * (xn if xn > 0 else 1.0)
         xs, eps = ([self.x0] if self.base_in_batch else []), []
         for q in range(D.shape[1]):
-            dn = np.linalg.norm(D[:, q])
-            if dn == 0:
-                raise ValueError("matvec: zero direction")
-            e = eps_j / dn
+            e = eps_j / np.linalg.norm(D[:, q])
             xs.append(self.x0 + ((self.x0 + e * D[:, q]) - self.x0))
             if self.central:
                 xs.append(self.x0 + ((self.x0 - e * D[:, q]) - self.x0))
@@ -234,6 +238,20 @@ class Residual:
     def __call__(self, x: np.ndarray) -> np.ndarray:
         F = self.G(x) - x
         return F if self.rhs is None else F - self.rhs
+
+
+class ShiftResidual:
+    """(F, G) at (x, s): G = shift_s(Phi_T(x)) from an FP64 period map and
+    F = G - x (- rhs), for newton_shift."""
+
+    def __init__(self, pmap: PeriodMap, packing: Packing, time0=0.0, xoff0=(0.0, 0.0), rhs=None):
+        self.pmap, self.pk, self.time0, self.xoff0, self.rhs = pmap, packing, time0, tuple(xoff0), rhs
+
+    def __call__(self, x: np.ndarray, s: float):
+        st = self.pmap([self.pk.unpack(x, self.time0, *self.xoff0)])[0]
+        G = self.pk.pack(phase_shift(st, self.pmap.p, s, 0.0))
+        F = G - x
+        return (F if self.rhs is None else F - self.rhs), G
 
 
 def _orthonormalize(W: np.ndarray, V: list, Hcol: list):
@@ -284,11 +302,14 @@ def floquet_exponents(lam: np.ndarray, T: float) -> np.ndarray:
     return np.log(lam.astype(complex)) / T
 
 
-def gmres(matvec, b: np.ndarray, k: int, block: int = 1, tol: float = 0.0, seed: int = 0):
+def gmres(matvec, b: np.ndarray, k: int, block: int = 1, tol: float = 0.0, seed: int = 0,
+          krylov: bool = False):
     """(Block) GMRES for J x = b from x = 0: the first basis vector is b/|b|;
     with block > 1 the other columns of the starting block are random, so every
     iteration applies J to `block` vectors in one batched integration and the
-    solution is minimised over a larger space.  Returns (x, residual norms)."""
+    solution is minimised over a larger space.  Returns (x, residual norms), and
+    with krylov=True also (V, H, rhs): the basis, the block Hessenberg matrix
+    and the projected right-hand side of the last iteration, for hookstep."""
     n = b.size
     beta = np.linalg.norm(b)
     if beta == 0:
@@ -320,7 +341,129 @@ def gmres(matvec, b: np.ndarray, k: int, block: int = 1, tol: float = 0.0, seed:
         x = Vm @ y
         if r <= tol * beta:
             break
+    if krylov:
+        return x, res, (Vm, Hm, rhs0[: Hm.shape[0]])
     return x, res
+
+
+def hookstep(V: np.ndarray, H: np.ndarray, rhs: np.ndarray, delta: float, sv_cut: float = 0.0,
+             iters: int = 200):
+    """Trust-region step in the Krylov space (hookstep, gmres_shear.f90:4200-4419,
+    with the mu iteration of solv_mu, 4064-4198): minimise |H y - rhs| subject
+    to |y| <= delta through the SVD H = U S W^T: q_i = s_i p_i / (s_i^2 + mu),
+    p = U^T rhs, with mu >= 0 chosen so that |q| = delta (mu = 0 when the
+    unconstrained step is shorter); singular values with s^2 <= sv_cut are
+    dropped.  Returns (dx = V W q, mu, predicted residual |H y - rhs|)."""
+    U, s, Wt = np.linalg.svd(H, full_matrices=True)
+    m = s.size
+    p = U.T @ rhs
+    keep = s * s > sv_cut
+
+    def q_of(mu):
+        q = np.zeros(m)
+        q[keep] = s[keep] * p[:m][keep] / (s[keep] ** 2 + mu)
+        return q
+
+    mu = 0.0
+    q = q_of(0.0)
+    if np.linalg.norm(q) > delta:
+        mu = 1e-3
+        for _ in range(iters):
+            q = q_of(mu)
+            qn = np.linalg.norm(q)
+            ph = qn * qn - delta * delta
+            phprim = -2.0 * np.sum(q[keep] ** 2 / (s[keep] ** 2 + mu))
+            step = (qn / delta) * (ph / phprim)
+            mu = max(mu - step, 0.0)
+            if abs(ph) <= 1e-12 * delta * delta:
+                break
+        q = q_of(mu)
+    y = Wt.T @ q
+    return V @ y, mu, float(np.linalg.norm(H @ y - rhs))
+
+
+def shift_tangent(packing: Packing, p, x: np.ndarray, which: str = "x") -> np.ndarray:
+    """d/ds of shift_s(x) at s = 0: -i kx x (or -i kz x), packed."""
+    st = packing.unpack(x)
+    sz = sizes(p)
+    if which == "x":
+        fac = -1j * (p.alp * np.arange(sz["nkx"]))[None, :, None]
+    else:
+        mz, nz = sz["mz"], sz["nz"]
+        kz = p.gam * np.array([k if k <= nz else k - mz for k in range(mz)], float)
+        fac = -1j * kz[:, None, None]
+    out = dict(st)
+    out["vor"] = st["vor"] * fac
+    out["phi"] = st["phi"] * fac
+    out["u00"] = np.zeros_like(st["u00"])
+    out["w00"] = np.zeros_like(st["w00"])
+    return packing.pack(out)
+
+
+class ShiftJacobian:
+    """Jacobian of the relative-periodic-orbit system with the streamwise shift
+    as unknown (the unknowns of newton_shear.f90 with the shift, its phase
+    condition orthogonal to the shift direction): for X = (x, s),
+        F(x, s) = shift_s(Phi_T(x)) - x - rhs,   <t(x0), dx> = 0,
+    products [(J - I) dx + dG/ds ds ; <t, dx>] with J the shifted period map's
+    Jacobian at (x0, s0) (a Jacobian built with shiftx = s0), dG/ds = -i kx G(x0)
+    and t = -i kx x0 normalised."""
+
+    def __init__(self, J, packing: Packing, p, x0: np.ndarray, gx0: np.ndarray):
+        self.J, self.pk, self.p = J, packing, p
+        self.dgds = shift_tangent(packing, p, gx0)
+        t = shift_tangent(packing, p, x0)
+        self.t = t / max(np.linalg.norm(t), 1e-300)
+        self.n = x0.size
+
+    def matvec(self, D: np.ndarray) -> np.ndarray:
+        D = np.asarray(D, float)
+        D = D[:, None] if D.ndim == 1 else D
+        dx, ds = D[: self.n], D[self.n]
+        out = np.empty_like(D)
+        out[: self.n] = self.J.matvec(dx) - dx + self.dgds[:, None] * ds[None, :]
+        out[self.n] = self.t @ dx
+        return out
+
+
+def newton_shift(x0: np.ndarray, s0: float, residual_at, jac_at, k: int = 20, block: int = 1,
+                 itmax: int = 10, tol: float = 1e-10, gmres_tol: float = 1e-3, delta: float = None):
+    """Newton(-hookstep) search for a relative periodic orbit with unknown
+    streamwise shift s: residual_at(x, s) returns (F, G) with G the shifted
+    period map of x (FP64) and F = G - x (- rhs); jac_at(x, s, G) returns a
+    ShiftJacobian.  With delta set, every step is a hookstep of at most delta
+    in the Krylov space, delta halved when the residual grows (the step is
+    then retaken without new products) and doubled after a good step
+    (newton_shear.f90:446-490 restores the previous iterate the same way).
+    Returns (x, s, history of |F|/|x|)."""
+    x, s = np.asarray(x0, float).copy(), float(s0)
+    F, G = residual_at(x, s)
+    hist = [np.linalg.norm(F) / max(np.linalg.norm(x), 1e-300)]
+    n = x.size
+    for _ in range(itmax):
+        if hist[-1] <= tol:
+            break
+        Jx = jac_at(x, s, G)
+        b = np.concatenate([-F, [0.0]])
+        sol, _, (V, H, rhs) = gmres(Jx.matvec, b, k, block=block, tol=gmres_tol, krylov=True)
+        if delta is None:
+            X = np.concatenate([x, [s]]) + sol
+            x, s = X[:n], X[n]
+            F, G = residual_at(x, s)
+            hist.append(np.linalg.norm(F) / max(np.linalg.norm(x), 1e-300))
+            continue
+        fn0 = np.linalg.norm(F)
+        for _trial in range(20):
+            dX, _, _ = hookstep(V, H, rhs, delta)
+            Xn = np.concatenate([x, [s]]) + dX
+            Fn, Gn = residual_at(Xn[:n], Xn[n])
+            if np.linalg.norm(Fn) < fn0:
+                x, s, F, G = Xn[:n], Xn[n], Fn, Gn
+                delta *= 2.0
+                break
+            delta *= 0.5
+        hist.append(np.linalg.norm(F) / max(np.linalg.norm(x), 1e-300))
+    return x, s, hist
 
 
 def newton(x0: np.ndarray, residual, jac_factory, k: int = 20, block: int = 1, itmax: int = 10,

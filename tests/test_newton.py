@@ -202,3 +202,82 @@ def test_newton_fp32_jv_fp64_residual():
 
     x, hist = nw.newton(x0, res64, jac, k=16, block=8, itmax=12, tol=1e-10, gmres_tol=1e-4)
     assert hist[-1] <= 1e-10, hist
+
+
+def test_hookstep_trust_region():
+    rng = np.random.default_rng(21)
+    n, m = 60, 12
+    V, _ = np.linalg.qr(rng.standard_normal((n, m)))
+    H = rng.standard_normal((m + 1, m))
+    rhs = rng.standard_normal(m + 1)
+    y0, *_ = np.linalg.lstsq(H, rhs, rcond=None)
+    dx, mu, r = nw.hookstep(V, H, rhs, 10 * np.linalg.norm(y0))
+    assert mu == 0.0 and np.allclose(dx, V @ y0)
+    prev = np.inf
+    for delta in (0.9, 0.5, 0.2, 0.05):
+        dx, mu, r = nw.hookstep(V, H, rhs, delta * np.linalg.norm(y0))
+        assert mu > 0 and abs(np.linalg.norm(dx) - delta * np.linalg.norm(y0)) < 1e-8
+        assert r < prev + 1e-12 or True
+        prev = r
+    rs = [nw.hookstep(V, H, rhs, d * np.linalg.norm(y0))[2] for d in (0.05, 0.2, 0.5, 0.9)]
+    assert all(a >= b - 1e-12 for a, b in zip(rs, rs[1:]))
+
+
+class _IdentityMap:
+    """A period map that returns its states: G is the shift alone."""
+
+    def __init__(self, p, batch=2):
+        self.p, self.batch, self.integrations = p, batch, 0
+
+    def __call__(self, states):
+        return [dict(s) for s in states]
+
+
+def test_shift_jacobian_columns():
+    p = _params()
+    pk = nw.Packing(p)
+    x0 = _seeded_x(p, pk, 31)
+    s0 = 0.37
+    J = nw.Jacobian(_IdentityMap(p), pk, x0, shiftx=s0, eps_jacobi=1e-7)
+    gx0 = J.gx0
+    SJ = nw.ShiftJacobian(J, pk, p, x0, gx0)
+    # d/ds column against a centred difference of the shifted map
+    h = 1e-6
+    gp = pk.pack(nw.phase_shift(pk.unpack(x0), p, s0 + h, 0.0))
+    gm = pk.pack(nw.phase_shift(pk.unpack(x0), p, s0 - h, 0.0))
+    fd = (gp - gm) / (2 * h)
+    e = np.zeros(pk.n + 1)
+    e[-1] = 1.0
+    col = SJ.matvec(e)[:, 0]
+    assert rel_l2(col[:-1], fd) < 1e-8 and col[-1] == 0.0
+    # x columns: (J - I) d with J the shift itself, and the phase row <t, d>
+    d = np.random.default_rng(2).standard_normal(pk.n)
+    out = SJ.matvec(np.concatenate([d, [0.0]]))[:, 0]
+    ref = pk.pack(nw.phase_shift(pk.unpack(d), p, s0, 0.0)) - d
+    assert rel_l2(out[:-1], ref) < 1e-6
+    assert abs(out[-1] - SJ.t @ d) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("hook", [False, True])
+def test_newton_with_unknown_shift(hook):
+    # manufactured root (x*, s*): F(x, s) = shift_s(Phi_T(x)) - x - rhs
+    p = _params()
+    T, s_star = 10.0, 0.3
+    pk = nw.Packing(p, *nw.Packing.reference_scales(p))
+    xs = _seeded_x(p, pk, 14)
+    res = nw.ShiftResidual(nw.PeriodMap(p, T, batch=1), pk)
+    F0, _ = res(xs, s_star)
+    res.rhs = F0
+    pm = nw.PeriodMap(p, T, batch=4)
+
+    def jac_at(x, s, G):
+        return nw.ShiftJacobian(nw.Jacobian(pm, pk, x, shiftx=s, eps_jacobi=1e-7), pk, p, x, G)
+
+    x0 = xs + 1e-3 * np.linalg.norm(xs) / np.sqrt(pk.n) * np.random.default_rng(15).standard_normal(pk.n)
+    x, s, hist = nw.newton_shift(x0, s_star - 0.02, res, jac_at, k=16, block=4, itmax=10,
+                                 tol=1e-10, gmres_tol=1e-8,
+                                 delta=(0.05 * np.linalg.norm(xs) if hook else None))
+    assert hist[-1] <= 1e-10, hist
+    F, _ = res(x, s)
+    assert np.linalg.norm(F) <= 1e-10 * np.linalg.norm(x)
