@@ -65,7 +65,10 @@ __device__ __forceinline__ int kgrid(int k, int nz, int NZ, int mz) { return k <
 template <typename R, int NZ, int CB, int T>
 __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
   typedef typename Vec2<R>::t V;
-  const int cb = blockIdx.x, j = blockIdx.y, b = blockIdx.z;
+  // one block per (kx block, pair of fields): the three (five with LES) pairs
+  // of a column block run as separate blocks, which evens out the last wave
+  const int round = blockIdx.x / g.ncb, cb = blockIdx.x - round * g.ncb;
+  const int j = blockIdx.y, b = blockIdx.z;
   Member &M = bf.mem[b];
   if (M.halted) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -90,7 +93,7 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
     }
     return p[k * nkx + i];
   };
-  const bool do_hist = (rk == 1) && M.ihist;
+  const bool do_hist = (rk == 1) && M.ihist && round == 0;
   if (do_hist) {
     // statistics in FP64 whatever the storage precision
     const double s = g.s;
@@ -168,8 +171,7 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
   }
   V *zb = (V *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * g.nzf * nkx;
   const V zero = mk2<R>((R)0, (R)0);
-  const int nround = g.les ? 5 : 3;
-  for (int round = 0; round < nround; round++) {
+  {
     // fill two fields (zero the 2/3-rule gap) on the padded z grid
     for (int idx = threadIdx.x; idx < 2 * CB * NZ; idx += T) A[idx] = zero;
     __syncthreads();
@@ -248,7 +250,6 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
       const int i = i0 + ci;
       if (i < nkx) zb[((long)z * g.nzf + 2 * round + f) * nkx + i] = res[(f * CB + ci) * NZ + z];
     }
-    __syncthreads();
   }
 }
 
@@ -886,7 +887,7 @@ static cudaError_t launch_p13(const Grid &g, const Bufs &bf, int rk, cudaStream_
     return cudaGetLastError();
   }
   if (which == 1)
-    k_p1<R, NZ, CB, T><<<grid, T, sm1, st>>>(g, bf, rk);
+    k_p1<R, NZ, CB, T><<<dim3(g.ncb * (g.les ? 5 : 3), g.my, g.B), T, sm1, st>>>(g, bf, rk);
   else
     k_p3<R, NZ, CB, T3><<<grid, T3, sm3, st>>>(g, bf);
   return cudaGetLastError();
