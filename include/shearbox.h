@@ -125,6 +125,14 @@ int sb_cross(sb_handle *h, double *vor, double *phi, double *u00, double *w00, d
  * run that used them must set the state again before stepping.
  * sb_fp64_peak measures the device's FP64 FMA throughput in TFLOP/s. */
 int sb_launch_stage(sb_handle *h, int stage, int rk, int count);
+
+/* Autotuner of the plane stages (no counterpart in the reference): times the
+ * tile candidates of plane stages 1-3 on the handle's current state -- kx
+ * columns per block of stages 1 and 3 (4 or 8), threads per block of stage 2
+ * (the default or twice it) -- keeps the fastest and re-captures the step
+ * graph.  choice (may be NULL) receives cb1, cb3, t2.  The state itself is not
+ * changed; call it after sb_set_state and before sb_step. */
+int sb_autotune(sb_handle *h, int *choice);
 int sb_fp64_peak(sb_handle *h, double *tflops);
 
 /* Standalone y-line operators on device-resident complex lines.  Line data is

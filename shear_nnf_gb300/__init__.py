@@ -75,7 +75,7 @@ ABI_FUNCTIONS = [
     "sb_seed_state", "sb_compact_coeffs", "sb_last_error", "sb_version", "sb_launch_stage",
     "sb_fp64_peak", "sb_op_derivyc", "sb_op_lapcdy", "sb_op_derivyc_noalloc",
     "sb_set_member_etime", "sb_op_filterc", "sb_op_cfty", "sb_op_rfty", "sb_write_restart",
-    "sb_read_restart",
+    "sb_read_restart", "sb_autotune",
 ]
 
 _lib = None
@@ -116,6 +116,7 @@ def lib(auto_build: bool = False):
     L.sb_last_error.restype = ctypes.c_char_p
     L.sb_launch_stage.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.sb_fp64_peak.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+    L.sb_autotune.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     L.sb_op_derivyc.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp,
                                 ctypes.c_long, vp, ctypes.c_long, dp, dp, vp]
     L.sb_op_derivyc_noalloc.argtypes = list(L.sb_op_derivyc.argtypes)
@@ -242,6 +243,13 @@ class ShearBox:
 
     def launch_stage(self, stage: int, rk: int = 1, count: int = 1):
         _check(lib().sb_launch_stage(self.h, int(stage), int(rk), int(count)))
+
+    def autotune(self) -> dict:
+        """Picks the fastest plane-stage tiles on the current state (keep the
+        state set before calling); returns the choice."""
+        c = (ctypes.c_int * 3)()
+        _check(lib().sb_autotune(self.h, c))
+        return {"p1_cols": c[0], "p3_cols": c[1], "p2_threads": c[2]}
 
     def fp64_peak(self) -> float:
         v = ctypes.c_double()

@@ -311,7 +311,10 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   g.nkx = g.mx / 2;
   g.nz = (g.mz - 1) / 2;
   g.mgx = p->mgalx / 2;
-  g.ncb = (g.nkx + plane_cb(p->mgalz) - 1) / plane_cb(p->mgalz);
+  g.cb1 = g.cb3 = plane_cb(p->mgalz);
+  g.ncb = (g.nkx + g.cb1 - 1) / g.cb1;
+  g.ncb3 = (g.nkx + g.cb3 - 1) / g.cb3;
+  g.t2 = plane_t2_default(p->mgalx);
   g.pi = 4.0 * std::atan(1.0);
   g.alp = p->alp;
   g.gam = p->gam;
@@ -380,7 +383,7 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
       (rc = A(&bf.mrf, B * 2 * my)) || (rc = A(&bf.mdu, B * 2 * my)) ||
       (rc = A(&bf.zbuf, B * my * g.mgalz * g.nzf * g.nkx * 2)) ||
       (rc = A(&bf.xbuf, B * my * g.mgalz * 3 * g.nkx * 2)) ||
-      (rc = A(&bf.hpart, B * my * g.ncb * SB_NHIST_Q)) || (rc = A(&bf.sh_old, B * 4 * g.nkx)) ||
+      (rc = A(&bf.hpart, B * my * ((g.nkx + 3) / 4) * SB_NHIST_Q)) || (rc = A(&bf.sh_old, B * 4 * g.nkx)) ||
       (rc = A(&bf.sh_new, B * 4 * g.nkx)) || (rc = A(&bf.mf1, B * my * g.nkx * 2)) ||
       (rc = A(&bf.mf2, B * my * g.nkx * 2)) || (rc = A(&h->d_pen, F))) {
     sb_destroy(h);
@@ -718,6 +721,71 @@ int sb_launch_stage(sb_handle *h, int stage, int rk, int count) {
     if (e != cudaSuccess) return fail(3, "launch: %s", cudaGetErrorString(e));
   }
   return 0;
+}
+
+int sb_autotune(sb_handle *h, int *choice) {
+  if (!h) return fail(1, "null handle");
+  Grid &g = h->g;
+  cudaStream_t st = h->st;
+  // the derived fields of the current state, as at the entry of a call
+  CK(launch_scalar(g, h->bf, 0, st));
+  CK(launch_tables(g, h->bf, 0, st));
+  CK(launch_setconj(g, h->bf, st));
+  if (g.ydeal == 3) CK(launch_filter(g, h->bf, 0, st));
+  CK(launch_lineB(g, h->bf, 0, st));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  auto timed = [&](int stage, float *ms) -> cudaError_t {
+    cudaError_t e = cudaSuccess;
+    for (int q = 0; q < 2 && e == cudaSuccess; q++) e = launch_plane(g, h->bf, stage, 2, st);
+    if (e != cudaSuccess) return e;
+    cudaEventRecord(e0, st);
+    for (int q = 0; q < 8 && e == cudaSuccess; q++) e = launch_plane(g, h->bf, stage, 2, st);
+    cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+    return e;
+  };
+  cudaError_t e = cudaSuccess;
+  float best = 1e30f, t = 0.0f;
+  int cb1 = g.cb1, cb3 = g.cb3, t2 = g.t2;
+  for (int c : {8, 4}) {  // plane stage 1: kx columns per block
+    g.cb1 = c;
+    g.ncb = (g.nkx + c - 1) / c;
+    if ((e = timed(1, &t)) != cudaSuccess) break;
+    if (t < best) best = t, cb1 = c;
+  }
+  g.cb1 = cb1;
+  g.ncb = (g.nkx + cb1 - 1) / cb1;
+  const int t2d = plane_t2_default(g.mgalx);
+  best = 1e30f;
+  for (int c : {t2d, 2 * t2d}) {  // plane stage 2: threads per block
+    if (e != cudaSuccess) break;
+    g.t2 = c;
+    if ((e = timed(2, &t)) != cudaSuccess) break;
+    if (t < best) best = t, t2 = c;
+  }
+  g.t2 = t2;
+  best = 1e30f;
+  for (int c : {8, 4}) {  // plane stage 3: kx columns per block
+    if (e != cudaSuccess) break;
+    g.cb3 = c;
+    g.ncb3 = (g.nkx + c - 1) / c;
+    if ((e = timed(3, &t)) != cudaSuccess) break;
+    if (t < best) best = t, cb3 = c;
+  }
+  g.cb3 = cb3;
+  g.ncb3 = (g.nkx + cb3 - 1) / cb3;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return fail(3, "autotune: %s", cudaGetErrorString(e));
+  if (choice) {
+    choice[0] = g.cb1;
+    choice[1] = g.cb3;
+    choice[2] = g.t2;
+  }
+  return capture_step(h);
 }
 
 int sb_fp64_peak(sb_handle *h, double *tflops) {

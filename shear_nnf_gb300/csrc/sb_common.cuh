@@ -48,7 +48,9 @@ struct Fac {
 struct Grid {
   int B, mgalx, my, mgalz, mx, mz, nkx, nz, mgx;
   int prec;              // 0: FP64 throughout; 1: FP32-mixed (FP32 storage/transforms)
-  int ncb;               // kx column blocks per plane (plane kernels)
+  int ncb;               // kx column blocks per plane of plane stage 1 (hist partials)
+  int cb1, cb3, ncb3;    // kx columns per block of plane stages 1 and 3, stage-3 blocks
+  int t2;                // threads per block of plane stage 2
   double alp, gam, Ly, s, chi, dx, dy, dz, pi;
   double rh1[7], rh2[7], pr2[7];
   long plane;            // doubles per plane of one field  (2*nkx*mz)

@@ -878,7 +878,6 @@ template <typename R, int NZ, int CB, int T, int T3>
 static cudaError_t launch_p13(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, int which,
                               bool prep) {
   typedef typename Vec2<R>::t V;
-  dim3 grid(g.ncb, g.my, g.B);
   const size_t sm1 = sizeof(V) * 2 * (2 * CB * NZ);
   const size_t sm3 = sizeof(V) * 2 * (3 * CB * NZ);
   if (prep) {
@@ -889,8 +888,21 @@ static cudaError_t launch_p13(const Grid &g, const Bufs &bf, int rk, cudaStream_
   if (which == 1)
     k_p1<R, NZ, CB, T><<<dim3(g.ncb * (g.les ? 5 : 3), g.my, g.B), T, sm1, st>>>(g, bf, rk);
   else
-    k_p3<R, NZ, CB, T3><<<grid, T3, sm3, st>>>(g, bf);
+    k_p3<R, NZ, CB, T3><<<dim3(g.ncb3, g.my, g.B), T3, sm3, st>>>(g, bf);
   return cudaGetLastError();
+}
+
+// plane stages 1, 3 with the tuned column block (4 or 8 kx columns)
+template <typename R, int NZ>
+static cudaError_t launch_p13_cb(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, int which,
+                                 bool prep) {
+  if (prep) {
+    cudaError_t e = launch_p13<R, NZ, 8, 128, 96>(g, bf, rk, st, which, true);
+    return e != cudaSuccess ? e : launch_p13<R, NZ, 4, 128, 96>(g, bf, rk, st, which, true);
+  }
+  const int cb = (which == 1) ? g.cb1 : g.cb3;
+  return cb == 4 ? launch_p13<R, NZ, 4, 128, 96>(g, bf, rk, st, which, false)
+                 : launch_p13<R, NZ, 8, 128, 96>(g, bf, rk, st, which, false);
 }
 
 template <typename R, int NX, int T>
@@ -908,28 +920,48 @@ static cudaError_t launch_p2(const Grid &g, const Bufs &bf, int rk, cudaStream_t
 
 int plane_cb(int) { return 8; }
 
+// plane stage 2 with the tuned block size: T0 threads or 2 T0
+template <typename R, int NX, int T0>
+static cudaError_t launch_p2_t(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, bool prep) {
+  if (prep) {
+    cudaError_t e = launch_p2<R, NX, T0>(g, bf, rk, st, true);
+    return e != cudaSuccess ? e : launch_p2<R, NX, 2 * T0>(g, bf, rk, st, true);
+  }
+  return g.t2 == 2 * T0 ? launch_p2<R, NX, 2 * T0>(g, bf, rk, st, false)
+                        : launch_p2<R, NX, T0>(g, bf, rk, st, false);
+}
+
+int plane_t2_default(int mgalx) {
+  switch (mgalx) {
+    case 32: case 48: return 64;
+    case 64: case 96: return 96;
+    case 192: return 128;
+    default: return 256;
+  }
+}
+
 template <typename R>
 static cudaError_t launch_plane_t(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
   const bool prep = (stage == 0);
   if (stage == 2 || prep) {
     cudaError_t e;
     switch (g.mgalx) {
-      case 32: e = launch_p2<R, 32, 64>(g, bf, rk, st, prep); break;
-      case 48: e = launch_p2<R, 48, 64>(g, bf, rk, st, prep); break;
-      case 64: e = launch_p2<R, 64, 96>(g, bf, rk, st, prep); break;
-      case 96: e = launch_p2<R, 96, 96>(g, bf, rk, st, prep); break;
-      case 192: e = launch_p2<R, 192, 128>(g, bf, rk, st, prep); break;
-      case 384: e = launch_p2<R, 384, 256>(g, bf, rk, st, prep); break;
+      case 32: e = launch_p2_t<R, 32, 64>(g, bf, rk, st, prep); break;
+      case 48: e = launch_p2_t<R, 48, 64>(g, bf, rk, st, prep); break;
+      case 64: e = launch_p2_t<R, 64, 96>(g, bf, rk, st, prep); break;
+      case 96: e = launch_p2_t<R, 96, 96>(g, bf, rk, st, prep); break;
+      case 192: e = launch_p2_t<R, 192, 128>(g, bf, rk, st, prep); break;
+      case 384: e = launch_p2_t<R, 384, 256>(g, bf, rk, st, prep); break;
       default: return cudaErrorInvalidValue;
     }
     if (!prep || e != cudaSuccess) return e;
   }
   switch (g.mgalz) {
-    case 32: return launch_p13<R, 32, 8, 128, 96>(g, bf, rk, st, stage, prep);
-    case 48: return launch_p13<R, 48, 8, 128, 96>(g, bf, rk, st, stage, prep);
-    case 64: return launch_p13<R, 64, 8, 128, 96>(g, bf, rk, st, stage, prep);
-    case 96: return launch_p13<R, 96, 8, 128, 96>(g, bf, rk, st, stage, prep);
-    case 192: return launch_p13<R, 192, 8, 128, 96>(g, bf, rk, st, stage, prep);
+    case 32: return launch_p13_cb<R, 32>(g, bf, rk, st, stage, prep);
+    case 48: return launch_p13_cb<R, 48>(g, bf, rk, st, stage, prep);
+    case 64: return launch_p13_cb<R, 64>(g, bf, rk, st, stage, prep);
+    case 96: return launch_p13_cb<R, 96>(g, bf, rk, st, stage, prep);
+    case 192: return launch_p13_cb<R, 192>(g, bf, rk, st, stage, prep);
     default: return cudaErrorInvalidValue;
   }
 }
