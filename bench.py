@@ -65,8 +65,10 @@ def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if ws > 1:
+        import torch
         import torch.distributed as dist
-        backend = "nccl"
+        # one GPU per rank over NCCL; gloo where no GPU is visible (host tests)
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
         dist.init_process_group(backend=backend)
         return dist, rank, ws
     return None, rank, ws
@@ -81,7 +83,8 @@ def allmax(dist, v: float) -> float:
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 

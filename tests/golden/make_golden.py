@@ -25,6 +25,17 @@ CASES = {
     "step64_seed3": dict(params=dict(mgalx=64, my=32, mgalz=32, Re=1000.0 / LZ ** 2, alp=0.5,
                                      Ly=LZ, gam=1.0, s=1.0, chi=0.0, CFL=0.5, fixed_dt=0.005),
                          seed=3, nstep=2),
+    # the same box with the Smagorinsky model at Re_z = 20000 (Cs = 0.1), CFL steps
+    "les64_seed5": dict(params=dict(mgalx=64, my=32, mgalz=32, Re=20000.0 / LZ ** 2, alp=0.5,
+                                    Ly=LZ, gam=1.0, s=1.0, chi=0.0, CFL=0.5, les=1, les_visc=1,
+                                    cs=0.1), seed=5, nstep=3),
+    # the compact y-filter (iydealiasing = 3) and the y 2/3 rule (iydealiasing = 1)
+    "filt64_seed4": dict(params=dict(mgalx=64, my=32, mgalz=32, Re=4000.0 / LZ ** 2, alp=0.5,
+                                     Ly=LZ, gam=1.0, s=1.0, chi=0.0, CFL=0.5, ydeal=3),
+                         seed=4, nstep=3),
+    "ydeal64_seed6": dict(params=dict(mgalx=64, my=32, mgalz=32, Re=4000.0 / LZ ** 2, alp=0.5,
+                                      Ly=LZ, gam=1.0, s=1.0, chi=0.0, CFL=0.5, ydeal=1),
+                          seed=6, nstep=3),
 }
 
 

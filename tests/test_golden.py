@@ -7,21 +7,24 @@ import pytest
 
 from conftest import ROOT, rel_l2
 
-GOLD = os.path.join(ROOT, "tests", "golden", "step64_seed3.npz")
+CASES = ["step64_seed3", "les64_seed5", "filt64_seed4", "ydeal64_seed6"]
+INTS = ("mgalx", "my", "mgalz", "les", "les_visc", "ydeal")
 
 
-def _case():
-    g = np.load(GOLD)
+def _case(name):
+    g = np.load(os.path.join(ROOT, "tests", "golden", name + ".npz"))
     params = {k[2:]: g[k].item() for k in g.files if k.startswith("p_")}
-    for k in ("mgalx", "my", "mgalz"):
-        params[k] = int(params[k])
+    for k in INTS:
+        if k in params:
+            params[k] = int(params[k])
     return g, params
 
 
-def test_oracle_reproduces_golden():
+@pytest.mark.parametrize("name", CASES)
+def test_oracle_reproduces_golden(name):
     import oracle
     import shear_nnf_gb300 as sb
-    g, params = _case()
+    g, params = _case(name)
     st = sb.seed_state(sb.make_params(**params), int(g["seed"]))
     tr, _ = oracle.Oracle(**params).cross(st, int(g["nstep"]))
     for k in ("vor", "phi", "u00", "w00"):
@@ -30,9 +33,10 @@ def test_oracle_reproduces_golden():
 
 
 @pytest.mark.gpu
-def test_gpu_reproduces_golden():
+@pytest.mark.parametrize("name", CASES)
+def test_gpu_reproduces_golden(name):
     import shear_nnf_gb300 as sb
-    g, params = _case()
+    g, params = _case(name)
     p = sb.make_params(**params)
     st = sb.seed_state(p, int(g["seed"]))
     box = sb.ShearBox(p)

@@ -65,3 +65,14 @@ def test_hundred_steps_64():
     assert max(err.values()) < MANY_STEPS, err
     assert _trace_error(tr_g, tr_o) < TRACE_TOL
     assert status.steps_done == 100
+
+
+@pytest.mark.parametrize("les", [0, 1])
+def test_one_step_largest_grid(les):
+    # the largest transform lengths (x 384, z 192) and my = 192, with and
+    # without the LES stage
+    pp = box_params(384, 192, 192, rez=20000.0, cfl=0.5, les=les, cs=0.1)
+    st_o, tr_o, st_g, tr_g, status = _run_both(pp, 1, k0=6.0)
+    err = _field_errors(st_o, st_g)
+    assert max(err.values()) < ONE_STEP, err
+    assert _trace_error(tr_g, tr_o) < TRACE_TOL
