@@ -33,6 +33,6 @@ def _rank(rank, ws, port, out):
 
 def test_replica_timing_takes_the_slowest_rank():
     ws = 2
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()
     mp.spawn(_rank, args=(ws, _free_port(), out), nprocs=ws, join=True)
     assert dict(out) == {0: 3.5, 1: 3.5}
