@@ -126,6 +126,14 @@ int sb_cross(sb_handle *h, double *vor, double *phi, double *u00, double *w00, d
  * sb_fp64_peak measures the device's FP64 FMA throughput in TFLOP/s. */
 int sb_launch_stage(sb_handle *h, int stage, int rk, int count);
 
+/* Physical fields of a member's state as the post-processor convh5 writes
+ * them (hvhg_uvwp, convh5.f90:650-933): mask bits 0..10 select u, v, w,
+ * omega_x, omega_y, omega_z (the velocity with the laminar shear s*y and
+ * omega_z with -s), Q and R of the velocity gradient tensor, Qs and Rs of the
+ * strain tensor, Qw = |omega|^2/4.  out receives the selected fields in that
+ * order, each [my][mgalz][mgalx] doubles.  The state is not changed. */
+int sb_physical_fields(sb_handle *h, int member, unsigned mask, double *out);
+
 /* Autotuner of the plane stages (no counterpart in the reference): times the
  * tile candidates of plane stages 1-3 on the handle's current state -- kx
  * columns per block of stages 1 and 3 (4 or 8), threads per block of stage 2

@@ -72,6 +72,8 @@ def lib():
         L.orc_derivyc.argtypes = [ctypes.c_void_p, dp, dp] + [ctypes.c_double] * 4 + [ctypes.c_int] * 2
         L.orc_lapcdy.argtypes = [ctypes.c_void_p, dp, ctypes.c_double, dp] + [ctypes.c_double] * 4 + [ctypes.c_int]
         L.orc_fourxz.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_int]
+        L.orc_physical.argtypes = [ctypes.c_void_p, dp, dp, dp, dp, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_uint, dp]
         L.orc_rfty.argtypes = [ctypes.c_void_p, dp, ctypes.c_int]
         L.orc_cfty.argtypes = [ctypes.c_void_p, dp, ctypes.c_int]
         L.orc_filterc.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_double, ctypes.c_double,
@@ -137,6 +139,19 @@ class Oracle:
         a = np.ascontiguousarray(u, dtype=np.float64)
         out = np.zeros_like(a)
         lib().orc_derivyc(self.h, _dp(a), _dp(out), 1.0, 0.0, 1.0, 0.0, iord, 1)
+        return out
+
+    def physical(self, state: dict, mask: int) -> np.ndarray:
+        """convh5 fields (mask bits 0..10: u v w ox oy oz Q R Qs Rs Qw) of a
+        state: array (nfields, my, mgalz, mgalx)."""
+        nf = bin(mask & 0x7FF).count("1")
+        out = np.zeros((nf, self.my, self.p.mgalz, self.p.mgalx))
+        vor = np.ascontiguousarray(state["vor"], np.complex128)
+        phi = np.ascontiguousarray(state["phi"], np.complex128)
+        lib().orc_physical(self.h, _dp(vor.view(np.float64)), _dp(phi.view(np.float64)),
+                           _dp(np.ascontiguousarray(state["u00"], np.float64)),
+                           _dp(np.ascontiguousarray(state["w00"], np.float64)),
+                           float(state["xoffb"]), float(state["xofft"]), int(mask), _dp(out))
         return out
 
     def rfty(self, u: np.ndarray, iopt: int) -> np.ndarray:

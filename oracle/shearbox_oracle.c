@@ -1557,6 +1557,154 @@ void orc_dealiasing_y(void *h, double *vor, double *phi, double *u00, double *w0
   dealiasing_y((ctx *)h, vor, phi, u00, w00, fac);
 }
 
+/* Physical fields of a state as the post-processor convh5 computes them
+ * (pre_uvwp and hvhg_uvwp, convh5.f90:295-371,650-933): the velocity with the
+ * laminar shear s*y added, the vorticity (omega_z with -s), and the invariants
+ * Q, R of the velocity gradient tensor, Qs, Rs of the strain tensor and
+ * Qw = |omega|^2/4.  mask bit q (0..10) selects u, v, w, ox, oy, oz, Q, R, Qs,
+ * Rs, Qw; out holds the selected fields in that order, each [my][mgalz][mgalx]. */
+int orc_physical(void *h, const double *vor_in, const double *phi_in, const double *u00,
+                 const double *w00, double xoffb, double xofft, unsigned mask, double *out) {
+  ctx *c = (ctx *)h;
+  int my = c->my, nkx = c->nkx, mz = c->mz, mgalx = c->mgalx, mgalz = c->mgalz, ld = mgalx + 2;
+  size_t nfield = 2 * (size_t)my * nkx * mz, nplane = (size_t)nkx * mz;
+  double s = c->p.s;
+  double *vor = dalloc(nfield), *phi = dalloc(nfield), *hg = dalloc(nfield), *hv = dalloc(nfield),
+         *dvordy = dalloc(nfield);
+  memcpy(vor, vor_in, sizeof(double) * nfield);
+  memcpy(phi, phi_in, sizeof(double) * nfield);
+  set_conj_pencil(c, vor, phi);
+  cplx *sht = zalloc(nkx), *shb = zalloc(nkx);
+  for (int i = 0; i < nkx; i++) {
+    sht[i] = shb[i] = C(1.0, 0.0);
+    if (s > 0.5) {
+      double a = c->xalp_im[i];
+      shb[i] = C(cos((-a) * xoffb), sin((-a) * xoffb));
+      sht[i] = C(cos((-a) * xofft), sin((-a) * xofft));
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (int ik = 0; ik < nkx * mz; ik++) {
+    int i = ik % nkx, k = ik / nkx;
+    ythread *t = &c->yt[my_thread()];
+    if (i != 0 || k != 0)
+      lapcdy(c, t, PEN(phi, i, k), c->gam2[k] + c->alp2[i], PEN(hg, i, k), sht[i], shb[i], 2);
+    derivyc(c, t, PEN(vor, i, k), PEN(dvordy, i, k), sht[i], shb[i], 1, 2, 1);
+    derivyc(c, t, PEN(hg, i, k), PEN(hv, i, k), sht[i], shb[i], 1, 2, 0);
+  }
+  double *rf0u = dalloc(my), *rf0w = dalloc(my);
+  derivyc(c, &c->yt[0], u00, rf0u, C(1.0, 0.0), C(1.0, 0.0), 1, 1, 0);
+  derivyc(c, &c->yt[0], w00, rf0w, C(1.0, 0.0), C(1.0, 0.0), 1, 1, 0);
+  cplx *b1 = zalloc(nplane * my), *b2 = zalloc(nplane * my), *phv = zalloc(nplane * my),
+       *phg = zalloc(nplane * my), *pdv = zalloc(nplane * my);
+  to_plane(c, phi, b1);
+  to_plane(c, vor, b2);
+  to_plane(c, hv, phv);
+  to_plane(c, hg, phg);
+  to_plane(c, dvordy, pdv);
+  int nout = 0, slot[11];
+  for (int q = 0; q < 11; q++) slot[q] = (mask >> q & 1u) ? nout++ : -1;
+  size_t pl = (size_t)mgalx * mgalz;
+#pragma omp parallel for schedule(static)
+  for (int j = 0; j < my; j++) {
+    pthread_buf *b = &c->pt[my_thread()];
+    const cplx *phic = b1 + (size_t)j * nplane, *ome2c = b2 + (size_t)j * nplane,
+               *rhvc = phv + (size_t)j * nplane, *rhgc = phg + (size_t)j * nplane,
+               *ome1c = pdv + (size_t)j * nplane;
+    cplx *u1c = b->u1c, *u2c = b->u2c, *u3c = b->u3c, *o1c = b->o1c, *o2c = b->o2c, *o3c = b->o3c;
+    for (int q = 0; q < (int)nplane; q++) {
+      u2c[q] = rhgc[q];
+      o2c[q] = ome2c[q];
+    }
+    u1c[0] = C(u00[j] + s * c->y[j], 0.0);
+    u3c[0] = C(w00[j], 0.0);
+    o3c[0] = C(-rf0u[j] - s, 0.0);
+    o1c[0] = C(rf0w[j], 0.0);
+    for (int k = 1; k < mz; k++) {
+      double g = c->xgam_im[k];
+      o3c[k * nkx] = cdiv_imag(cneg(ome1c[k * nkx]), g);
+      o1c[k * nkx] = cdiv_imag(cneg(phic[k * nkx]), g);
+      u3c[k * nkx] = cdiv_imag(cneg(rhvc[k * nkx]), g);
+      u1c[k * nkx] = cdiv_imag(ome2c[k * nkx], g);
+    }
+    for (int k = 0; k < mz; k++) {
+      double g = c->xgam_im[k];
+      for (int i = 1; i < nkx; i++) {
+        double a = c->xalp_im[i], km1 = 1.0 / (c->alp2[i] + c->gam2[k]);
+        int q = k * nkx + i;
+        cplx w1 = ome1c[q], ph = phic[q], dv = rhvc[q], o2 = ome2c[q], t;
+        t = csub(C(-g * w1.im, g * w1.re), C(-a * ph.im, a * ph.re));
+        o3c[q] = cscal(km1, t);
+        t = cadd(C(-a * w1.im, a * w1.re), C(-g * ph.im, g * ph.re));
+        o1c[q] = cscal(km1, t);
+        t = cadd(C(-g * dv.im, g * dv.re), C(-a * o2.im, a * o2.re));
+        u3c[q] = cscal(km1, t);
+        t = csub(C(-a * dv.im, a * dv.re), C(-g * o2.im, g * o2.re));
+        u1c[q] = cscal(km1, t);
+      }
+    }
+    /* physical velocity, vorticity and gradients (c2r of each spectrum) */
+    double *r = (double *)malloc(sizeof(double) * ld * mgalz * 15);
+    cplx *f = zalloc(nplane);
+    const cplx *base[6] = {u1c, u2c, u3c, o1c, o2c, o3c};
+    for (int q = 0; q < 6; q++) {
+      memcpy(f, base[q], sizeof(cplx) * nplane);
+      fourxz(c, b, f, r + (size_t)q * ld * mgalz, 1);
+    }
+    /* 6 ux, 7 uy, 8 uz, 9 vx, 10 vy, 11 vz, 12 wx, 13 wy, 14 wz */
+    for (int q = 6; q < 15; q++) {
+      for (int k = 0; k < mz; k++) {
+        double g = c->xgam_im[k];
+        for (int i = 0; i < nkx; i++) {
+          double a = c->xalp_im[i];
+          int p = k * nkx + i;
+          cplx v;
+          switch (q) {
+            case 6: v = C(-a * u1c[p].im, a * u1c[p].re); break;
+            case 7: v = csub(C(-a * u2c[p].im, a * u2c[p].re), o3c[p]); break;
+            case 8: v = C(-g * u1c[p].im, g * u1c[p].re); break;
+            case 9: v = C(-a * u2c[p].im, a * u2c[p].re); break;
+            case 10: v = rhvc[p]; break;
+            case 11: v = C(-g * u2c[p].im, g * u2c[p].re); break;
+            case 12: v = C(-a * u3c[p].im, a * u3c[p].re); break;
+            case 13: v = cadd(C(-g * u2c[p].im, g * u2c[p].re), o1c[p]); break;
+            default: v = C(-g * u3c[p].im, g * u3c[p].re); break;
+          }
+          f[p] = v;
+        }
+      }
+      fourxz(c, b, f, r + (size_t)q * ld * mgalz, 1);
+    }
+    for (int z = 0; z < mgalz; z++)
+      for (int x = 0; x < mgalx; x++) {
+        const size_t e = (size_t)z * ld + x, st = (size_t)ld * mgalz;
+        double U[15];
+        for (int q = 0; q < 15; q++) U[q] = r[q * st + e];
+        double ux = U[6], uy = U[7], uz = U[8], vx = U[9], vy = U[10], vz = U[11], wx = U[12],
+               wy = U[13], wz = U[14];
+        double val[11];
+        for (int q = 0; q < 6; q++) val[q] = U[q];
+        double ttt = ux * ux + vy * vy + wz * wz + 2.0 * (vz * wy + uy * vx + uz * wx);
+        val[6] = -0.5 * ttt;
+        double ddd = ux * (vy * wz - wy * vz) - uy * (vx * wz - wx * vz) + uz * (vx * wy - wx * vy);
+        val[7] = -ddd;
+        double s12 = 0.5 * (uy + vx), s23 = 0.5 * (vz + wy), s13 = 0.5 * (uz + wx);
+        val[8] = -0.5 * (ux * ux + vy * vy + wz * wz) - (s12 * s12 + s13 * s13 + s23 * s23);
+        double dds = s12 * s23 * s13 + ux * (s12 * s12 + s13 * s13) + vy * (s12 * s12 + s23 * s23) +
+                     wz * (s13 * s13 + s23 * s23) + ux * vy * wz;
+        val[9] = -dds;
+        val[10] = 0.25 * (U[3] * U[3] + U[4] * U[4] + U[5] * U[5]);
+        for (int q = 0; q < 11; q++)
+          if (slot[q] >= 0) out[((size_t)slot[q] * my + j) * pl + (size_t)z * mgalx + x] = val[q];
+      }
+    free(r);
+    free(f);
+  }
+  free(vor); free(phi); free(hg); free(hv); free(dvordy); free(sht); free(shb);
+  free(rf0u); free(rf0w); free(b1); free(b2); free(phv); free(phg); free(pdv);
+  return nout;
+}
+
 int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, double *ptime,
               double *pxoffb, double *pxofft, int nstep, double *trace, int *ntrace,
               int *pistop, double *pdeltat) {

@@ -68,6 +68,10 @@ void orc_filterc(void *h, const double *u, double *du, double shp_re, double shp
 /* rfty / cfty on one y-line (packed real line of my+2 doubles, or complex) */
 void orc_rfty(void *h, double *u, int iopt);
 void orc_cfty(void *h, double *u, int iopt);
+/* physical fields of convh5 (u v w ox oy oz Q R Qs Rs Qw by mask bits 0..10),
+ * each [my][mgalz][mgalx]; returns the number of fields written */
+int orc_physical(void *h, const double *vor, const double *phi, const double *u00,
+                 const double *w00, double xoffb, double xofft, unsigned mask, double *out);
 /* dealiasing_y (iydealiasing 1, 2) on pencil-layout state arrays */
 void orc_dealiasing_y(void *h, double *vor, double *phi, double *u00, double *w00, double fac);
 void orc_derivyc(void *h, const double *u, double *du, double shp_re,

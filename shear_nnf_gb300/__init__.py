@@ -75,7 +75,7 @@ ABI_FUNCTIONS = [
     "sb_seed_state", "sb_compact_coeffs", "sb_last_error", "sb_version", "sb_launch_stage",
     "sb_fp64_peak", "sb_op_derivyc", "sb_op_lapcdy", "sb_op_derivyc_noalloc",
     "sb_set_member_etime", "sb_op_filterc", "sb_op_cfty", "sb_op_rfty", "sb_write_restart",
-    "sb_read_restart", "sb_autotune",
+    "sb_read_restart", "sb_autotune", "sb_physical_fields",
 ]
 
 _lib = None
@@ -117,6 +117,7 @@ def lib(auto_build: bool = False):
     L.sb_launch_stage.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.sb_fp64_peak.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.sb_autotune.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+    L.sb_physical_fields.argtypes = [vp, ctypes.c_int, ctypes.c_uint, dp]
     L.sb_op_derivyc.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp,
                                 ctypes.c_long, vp, ctypes.c_long, dp, dp, vp]
     L.sb_op_derivyc_noalloc.argtypes = list(L.sb_op_derivyc.argtypes)
@@ -243,6 +244,18 @@ class ShearBox:
 
     def launch_stage(self, stage: int, rk: int = 1, count: int = 1):
         _check(lib().sb_launch_stage(self.h, int(stage), int(rk), int(count)))
+
+    PHYSICAL = ("u", "v", "w", "ox", "oy", "oz", "Q", "R", "Qs", "Rs", "Qw")
+
+    def physical(self, member: int = 0, fields=PHYSICAL) -> dict:
+        """convh5 physical fields of a member's state: {name: (my, mgalz, mgalx)}."""
+        mask = 0
+        for f in fields:
+            mask |= 1 << self.PHYSICAL.index(f)
+        names = [f for f in self.PHYSICAL if mask >> self.PHYSICAL.index(f) & 1]
+        out = np.zeros((len(names), self.p.my, self.p.mgalz, self.p.mgalx))
+        _check(lib().sb_physical_fields(self.h, int(member), mask, _dp(out)))
+        return dict(zip(names, out))
 
     def autotune(self) -> dict:
         """Picks the fastest plane-stage tiles on the current state (keep the

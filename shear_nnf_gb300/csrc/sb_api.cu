@@ -788,6 +788,50 @@ int sb_autotune(sb_handle *h, int *choice) {
   return capture_step(h);
 }
 
+int sb_physical_fields(sb_handle *h, int member, unsigned mask, double *out) {
+  if (!h || member < 0 || member >= h->g.B || !out) return fail(1, "bad argument");
+  mask &= 0x7FFu;
+  int nout = 0;
+  for (int q = 0; q < 11; q++) nout += (mask >> q) & 1u;
+  if (!nout) return 0;
+  const Grid &g = h->g;
+  cudaStream_t st = h->st;
+  // the derived fields of the current state (v, dv/dy, d(omega_y)/dy, mean
+  // derivatives), as at the entry of a call
+  CK(launch_scalar(g, h->bf, 0, st));
+  CK(launch_tables(g, h->bf, 0, st));
+  CK(launch_setconj(g, h->bf, st));
+  CK(launch_lineB(g, h->bf, 0, st));
+  // one box: member-offset buffers, plane stage 1 with the extra z-transforms
+  Grid gl = g;
+  gl.B = 1;
+  gl.les = 1;
+  gl.nzf = 10;
+  Bufs bl = h->bf;
+  const long Fd = g.prec ? g.field / 2 : g.field;
+  const long Md = g.prec ? (long)g.my : 2L * g.my;
+  bl.vor += member * Fd;
+  bl.phi += member * Fd;
+  bl.D += member * Fd;
+  bl.V += member * Fd;
+  bl.G += member * Fd;
+  bl.mu += member * Md;
+  bl.mdu += member * Md;
+  bl.mem += member;
+  const size_t nout_d = (size_t)nout * g.my * g.mgalz * g.mgalx;
+  double *zb = nullptr, *od = nullptr;
+  CK(cudaMallocAsync((void **)&zb, sizeof(double) * (size_t)g.my * g.mgalz * 10 * g.nkx * 2, st));
+  CK(cudaMallocAsync((void **)&od, sizeof(double) * nout_d, st));
+  bl.zbuf = zb;
+  cudaError_t e = launch_physical(gl, bl, mask, od, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, od, sizeof(double) * nout_d, cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(zb, st);
+  cudaFreeAsync(od, st);
+  if (e != cudaSuccess) return fail(3, "physical fields: %s", cudaGetErrorString(e));
+  CK(cudaStreamSynchronize(st));
+  return 0;
+}
+
 int sb_fp64_peak(sb_handle *h, double *tflops) {
   if (!h || !tflops) return fail(1, "bad argument");
   CK(fp64_peak(tflops, h->st));

@@ -1166,4 +1166,139 @@ bool supported_grid(int mgalx, int mgalz) {
   return okx && okz;
 }
 
+// ---------------------------------------------------------------------------
+// Physical fields of the post-processor convh5 (hvhg_uvwp, convh5.f90:650-933)
+// from the z-transforms of k_p1 run with the LES rounds (zbuf fields 0 u, 1 w,
+// 2 omega_x, 3 omega_z, 4 v, 5 omega_y, 6 dv/dy, 7 i kz w, 8 2 i kz v +
+// omega_x, 9 i kz u): per (plane, z row pair), the velocity with the laminar
+// shear s y, the vorticity (omega_z with -s) and the nine velocity gradients
+// to physical x, then the selected outputs (mask bits 0..10: u v w ox oy oz
+// Q R Qs Rs Qw), each [my][mgalz][mgalx] in FP64.
+// ---------------------------------------------------------------------------
+template <typename R, int NX, int T>
+__global__ void __launch_bounds__(T) k_phys(Grid g, Bufs bf, unsigned mask, double *out) {
+  typedef typename Vec2<R>::t V;
+  const int zp = blockIdx.x, j = blockIdx.y;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *A = (V *)smem_raw, *Bs = A + 15 * NX;
+  const int nkx = g.nkx, NZ = g.mgalz, nzf = g.nzf;
+  const int z = 2 * zp;
+  const V *zb = (const V *)bf.zbuf + (long)j * NZ * nzf * nkx;
+  const V zero = mk2<R>((R)0, (R)0);
+  for (int idx = threadIdx.x; idx < 15 * NX; idx += T) A[idx] = zero;
+  __syncthreads();
+  // 0 u, 1 v, 2 w, 3 ox, 4 oy, 5 oz, 6 ux, 7 uy, 8 uz, 9 vx, 10 vy, 11 vz,
+  // 12 wx, 13 wy, 14 wz (convh5.f90:801-831)
+  for (int idx = threadIdx.x; idx < 15 * nkx; idx += T) {
+    const int f = idx / nkx, i = idx - f * nkx;
+    const R a = (R)(g.alp * i);
+    V X[2];
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      const V *row = zb + (long)(z + r) * nzf * nkx;
+      const V u = row[i], w = row[nkx + i], ox = row[2 * nkx + i], oz = row[3 * nkx + i],
+              v = row[4 * nkx + i];
+      V x;
+      switch (f) {
+        case 0: x = u; break;
+        case 1: x = v; break;
+        case 2: x = w; break;
+        case 3: x = ox; break;
+        case 4: x = row[5 * nkx + i]; break;
+        case 5: x = oz; break;
+        case 6: x = mk2<R>(-a * u.y, a * u.x); break;
+        case 7: x = mk2<R>(-a * v.y - oz.x, a * v.x - oz.y); break;
+        case 8: x = row[9 * nkx + i]; break;
+        case 9: x = mk2<R>(-a * v.y, a * v.x); break;
+        case 10: x = row[6 * nkx + i]; break;
+        case 11: {
+          const V t = row[8 * nkx + i];
+          x = mk2<R>((R)0.5 * (t.x - ox.x), (R)0.5 * (t.y - ox.y));
+          break;
+        }
+        case 12: x = mk2<R>(-a * w.y, a * w.x); break;
+        case 13: {
+          const V t = row[8 * nkx + i];
+          x = mk2<R>((R)0.5 * (t.x - ox.x) + ox.x, (R)0.5 * (t.y - ox.y) + ox.y);
+          break;
+        }
+        default: x = row[7 * nkx + i]; break;
+      }
+      X[r] = x;
+    }
+    if (i == 0) {
+      X[0].y = (R)0;
+      X[1].y = (R)0;
+    }
+    A[f * NX + i] = mk2<R>(X[0].x - X[1].y, X[0].y + X[1].x);
+    if (i > 0) A[f * NX + NX - i] = mk2<R>(X[0].x + X[1].y, -X[0].y + X[1].x);
+  }
+  V *P = fft_batch<NX, +1, 15, T>(A, Bs, (const V *)tw_of<R>(bf, false));
+  int slot[11], n = 0;
+#pragma unroll
+  for (int q = 0; q < 11; q++) slot[q] = (mask >> q & 1u) ? n++ : -1;
+  const double s = g.s, sy = g.s * ((double)j * g.dy - 0.5 * g.Ly);
+  const long pl = (long)NX * NZ;
+  for (int x = threadIdx.x; x < NX; x += T) {
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      double U[15];
+#pragma unroll
+      for (int q = 0; q < 15; q++) U[q] = r ? (double)P[q * NX + x].y : (double)P[q * NX + x].x;
+      U[0] += sy;  // laminar shear (convh5.f90:755-758)
+      U[5] -= s;
+      U[7] += s;
+      const double ux = U[6], uy = U[7], uz = U[8], vx = U[9], vy = U[10], vz = U[11],
+                   wx = U[12], wy = U[13], wz = U[14];
+      double val[11];
+#pragma unroll
+      for (int q = 0; q < 6; q++) val[q] = U[q];
+      val[6] = -0.5 * (ux * ux + vy * vy + wz * wz + 2.0 * (vz * wy + uy * vx + uz * wx));
+      val[7] = -(ux * (vy * wz - wy * vz) - uy * (vx * wz - wx * vz) + uz * (vx * wy - wx * vy));
+      const double s12 = 0.5 * (uy + vx), s23 = 0.5 * (vz + wy), s13 = 0.5 * (uz + wx);
+      val[8] = -0.5 * (ux * ux + vy * vy + wz * wz) - (s12 * s12 + s13 * s13 + s23 * s23);
+      val[9] = -(s12 * s23 * s13 + ux * (s12 * s12 + s13 * s13) + vy * (s12 * s12 + s23 * s23) +
+                 wz * (s13 * s13 + s23 * s23) + ux * vy * wz);
+      val[10] = 0.25 * (U[3] * U[3] + U[4] * U[4] + U[5] * U[5]);
+#pragma unroll
+      for (int q = 0; q < 11; q++)
+        if (slot[q] >= 0) out[((long)slot[q] * g.my + j) * pl + (long)(z + r) * NX + x] = val[q];
+    }
+  }
+}
+
+template <typename R, int NX, int T>
+static cudaError_t launch_phys_t(const Grid &g, const Bufs &bf, unsigned mask, double *out,
+                                 cudaStream_t st) {
+  typedef typename Vec2<R>::t V;
+  const size_t sm = sizeof(V) * 2 * 15 * NX;
+  cudaFuncSetAttribute(k_phys<R, NX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k_phys<R, NX, T><<<dim3(g.mgalz / 2, g.my), T, sm, st>>>(g, bf, mask, out);
+  return cudaGetLastError();
+}
+
+template <typename R>
+static cudaError_t launch_phys_r(const Grid &g, const Bufs &bf, unsigned mask, double *out,
+                                 cudaStream_t st) {
+  switch (g.mgalx) {
+    case 32: return launch_phys_t<R, 32, 64>(g, bf, mask, out, st);
+    case 48: return launch_phys_t<R, 48, 64>(g, bf, mask, out, st);
+    case 64: return launch_phys_t<R, 64, 96>(g, bf, mask, out, st);
+    case 96: return launch_phys_t<R, 96, 96>(g, bf, mask, out, st);
+    case 192: return launch_phys_t<R, 192, 128>(g, bf, mask, out, st);
+    case 384: return launch_phys_t<R, 384, 256>(g, bf, mask, out, st);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// one box (Grid with B = 1 and member-offset buffers): plane stage 1 with the
+// extra z-transforms into g's zbuf, then the physical fields
+cudaError_t launch_physical(const Grid &g, const Bufs &bf, unsigned mask, double *out,
+                            cudaStream_t st) {
+  cudaError_t e = launch_plane(g, bf, 1, 2, st);
+  if (e != cudaSuccess) return e;
+  return g.prec ? launch_phys_r<float>(g, bf, mask, out, st)
+                : launch_phys_r<double>(g, bf, mask, out, st);
+}
+
 }  // namespace sb

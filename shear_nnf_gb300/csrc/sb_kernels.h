@@ -17,6 +17,8 @@ cudaError_t launch_lineL(const Grid &g, const Bufs &bf, cudaStream_t st);
 cudaError_t launch_filter(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
 cudaError_t launch_ydeal(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
 cudaError_t launch_meand1(const Grid &g, const Bufs &bf, cudaStream_t st);
+cudaError_t launch_physical(const Grid &g, const Bufs &bf, unsigned mask, double *out,
+                            cudaStream_t st);
 bool supported_ylen(int my);
 cudaError_t launch_yop(int my, int nlines, double *c, long ldc, int iopt, int real, cudaStream_t st);
 cudaError_t launch_filter_rhs(int nlines, int N, const double *u, long ldu, double *out, long ldo,
