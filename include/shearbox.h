@@ -30,6 +30,7 @@ extern "C" {
 #endif
 
 #define SB_TRACE_RECORD 24
+#define SB_TRACE_RECORD_T 29   /* with the temperature (crosst) */
 
 /* Run parameters.  Mirrors hre2.dat records 1, 2 and 4 as read by initcr
  * (initcr.f90:54-135) plus the run options of cross (running module,
@@ -55,6 +56,12 @@ typedef struct sb_params {
   int ydeal;                   /* iydealiasing: 0 none (default), 3 compact y-filter
                                   of the state at every substep (cross.f90:214-227,
                                   476-490; filter_shear_hepta.f90:21-148) */
+  int temperature;             /* itemperature: 1 steps the Boussinesq scalar tb of
+                                  crosst (crosst.f90:3-1310) with sb_crosst or
+                                  sb_set_temperature + sb_step */
+  double fkappa, bym, gbeta;   /* its diffusivity, mean gradient d(Tbar)/dy and
+                                  buoyancy factor (hre3.dat keyword itemperature,
+                                  initcr.f90:1996-2011) */
 } sb_params;
 
 /* Per-box status after sb_step (cross.f90 istop logic, 1683-1690, 2102-2115) */
@@ -101,6 +108,13 @@ int sb_set_state(sb_handle *h, int member, const double *vor, const double *phi,
 int sb_get_state(sb_handle *h, int member, double *vor, double *phi, double *u00,
                  double *w00, double *time, double *xoffb, double *xofft);
 
+/* Temperature state of a box created with temperature = 1: tb in the pencil
+ * layout of vor, tb00 real(0:my1) (the tb, tb00 arguments of crosst,
+ * crosst.f90:3-5,47-49).  set_conj_t is applied to tb at the entry of each
+ * sb_step call (crosst.f90:333-337). */
+int sb_set_temperature(sb_handle *h, int member, const double *tb, const double *tb00);
+int sb_get_temperature(sb_handle *h, int member, double *tb, double *tb00);
+
 /* Advances every box by nsteps RK3 steps on the device, with the semantics of
  * one call of cross (cross.f90:336-1029): set_conj on entry, v from phi on the
  * first step, Delta t from the CFL (or fixed_dt) on every step, stop on
@@ -110,12 +124,20 @@ int sb_get_status(sb_handle *h, int member, sb_status *st);
 
 /* Statistics records of the last sb_step (the .cfbin record of
  * cross.f90:2087): time, Deltat, uner(1:10), CFL, CFLv, umax(1:3), xoffb,
- * xofft, umax(0), uner2(1:4). */
+ * xofft, umax(0), uner2(1:4); SB_TRACE_RECORD doubles each, or
+ * SB_TRACE_RECORD_T with the temperature, which appends tbmax, tner(1:4)
+ * (crosst.f90:2456-2458). */
 int sb_get_trace(sb_handle *h, int member, double *out, int max_records, int *nrec);
 
 /* Drop-in for cross(): box 0's host state in, nstep steps, state out. */
 int sb_cross(sb_handle *h, double *vor, double *phi, double *u00, double *w00, double *time,
              double *xoffb, double *xofft, int nstep, sb_status *st);
+
+/* Drop-in for crosst() (crosst.f90:3-5, explicit branch, iadd_mode 5): as
+ * sb_cross with the scalar tb and its mean tb00; needs temperature = 1. */
+int sb_crosst(sb_handle *h, double *vor, double *phi, double *u00, double *w00, double *tb,
+              double *tb00, double *time, double *xoffb, double *xofft, int nstep,
+              sb_status *st);
 
 /* Measurement hooks (no counterpart in the reference; used by the benchmark).
  * sb_launch_stage enqueues `count` launches of one kernel of substep rk on the

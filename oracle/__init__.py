@@ -23,6 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 TRACE_LEN = 24
+TRACE_LEN_T = 29  # crosst: the record plus tbmax, tner(1:4)
 
 
 def build(force: bool = False) -> str:
@@ -47,6 +48,8 @@ class OrcParams(ctypes.Structure):
         ("etime", ctypes.c_double), ("dumptime", ctypes.c_double), ("dtimag", ctypes.c_double),
         ("keep_laminar", ctypes.c_int), ("les", ctypes.c_int), ("les_visc", ctypes.c_int),
         ("cs", ctypes.c_double), ("ydeal", ctypes.c_int),
+        ("temperature", ctypes.c_int), ("fkappa", ctypes.c_double), ("bym", ctypes.c_double),
+        ("gbeta", ctypes.c_double),
     ]
 
 
@@ -69,6 +72,9 @@ def lib():
         L.orc_cross.restype = ctypes.c_int
         L.orc_cross.argtypes = [ctypes.c_void_p, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int,
                                 dp, ip, ip, dp]
+        L.orc_crosst.restype = ctypes.c_int
+        L.orc_crosst.argtypes = [ctypes.c_void_p, dp, dp, dp, dp, dp, dp, dp, dp, dp,
+                                 ctypes.c_int, dp, ip, ip, dp]
         L.orc_derivyc.argtypes = [ctypes.c_void_p, dp, dp] + [ctypes.c_double] * 4 + [ctypes.c_int] * 2
         L.orc_lapcdy.argtypes = [ctypes.c_void_p, dp, ctypes.c_double, dp] + [ctypes.c_double] * 4 + [ctypes.c_int]
         L.orc_fourxz.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_int]
@@ -105,10 +111,10 @@ class Oracle:
     def __init__(self, mgalx, my, mgalz, Re, alp, Ly, gam, s=1.0, chi=0.0, CFL=0.5,
                  vbulk=0.0, fixed_dt=0.0, readflag=1, uprim=1.0, nhist=1,
                  etime=1e10, dumptime=1e10, dtimag=1e10, keep_laminar=0, les=0, les_visc=1,
-                 cs=0.1, ydeal=0):
+                 cs=0.1, ydeal=0, temperature=0, fkappa=0.0, bym=0.0, gbeta=0.0):
         self.p = OrcParams(mgalx, my, mgalz, Re, alp, Ly, gam, s, chi, CFL, vbulk, fixed_dt,
                            readflag, uprim, nhist, etime, dumptime, dtimag, keep_laminar, les,
-                           les_visc, cs, ydeal)
+                           les_visc, cs, ydeal, temperature, fkappa, bym, gbeta)
         self.h = lib().orc_create(ctypes.byref(self.p))
         sz = (ctypes.c_int * 8)()
         lib().orc_sizes(self.h, sz)
@@ -203,23 +209,35 @@ class Oracle:
     def cross(self, state: dict, nstep: int):
         """Advance ``state`` in place by nstep steps.  state keys: vor, phi
         (complex (mz, nkx, my) pencil layout), u00, w00 (my,), time, xoffb,
-        xofft.  Returns (trace array (n, 24), istop)."""
+        xofft; with temperature also tb (like vor) and tb00 (my,), stepped by
+        crosst.  Returns (trace array (n, 24 or 29), istop)."""
         vor = state["vor"]
         phi = state["phi"]
-        for a in (vor, phi):
+        temp = bool(self.p.temperature)
+        fields = (vor, phi, state["tb"]) if temp else (vor, phi)
+        for a in fields:
             assert a.dtype == np.complex128 and a.flags["C_CONTIGUOUS"]
             assert a.shape == (self.mz, self.nkx, self.my)
         t = ctypes.c_double(state["time"])
         xb = ctypes.c_double(state["xoffb"])
         xt = ctypes.c_double(state["xofft"])
-        tr = np.zeros((max(nstep, 1), TRACE_LEN))
+        tr = np.zeros((max(nstep, 1), TRACE_LEN_T if temp else TRACE_LEN))
         nt = ctypes.c_int(0)
         ist = ctypes.c_int(0)
         dt = ctypes.c_double(self.deltat)
-        lib().orc_cross(self.h, _dp(vor.view(np.float64)), _dp(phi.view(np.float64)),
-                        _dp(state["u00"]), _dp(state["w00"]), ctypes.byref(t), ctypes.byref(xb),
-                        ctypes.byref(xt), int(nstep), _dp(tr), ctypes.byref(nt),
-                        ctypes.byref(ist), ctypes.byref(dt))
+        if temp:
+            rc = lib().orc_crosst(self.h, _dp(vor.view(np.float64)), _dp(phi.view(np.float64)),
+                                  _dp(state["u00"]), _dp(state["w00"]),
+                                  _dp(state["tb"].view(np.float64)), _dp(state["tb00"]),
+                                  ctypes.byref(t), ctypes.byref(xb), ctypes.byref(xt),
+                                  int(nstep), _dp(tr), ctypes.byref(nt), ctypes.byref(ist),
+                                  ctypes.byref(dt))
+            assert rc >= 0, "orc_crosst needs temperature=1, tb and tb00"
+        else:
+            lib().orc_cross(self.h, _dp(vor.view(np.float64)), _dp(phi.view(np.float64)),
+                            _dp(state["u00"]), _dp(state["w00"]), ctypes.byref(t),
+                            ctypes.byref(xb), ctypes.byref(xt), int(nstep), _dp(tr),
+                            ctypes.byref(nt), ctypes.byref(ist), ctypes.byref(dt))
         state["time"], state["xoffb"], state["xofft"] = t.value, xb.value, xt.value
         self.deltat = dt.value
         return tr[: nt.value], ist.value

@@ -180,12 +180,16 @@ typedef struct { /* per-thread plane buffers for hvhg */
    * Sij2, its spectrum wyc, nuSGS */
   cplx *lc[6], *wyc;
   double *lr[6], *sij2, *nus;
+  /* temperature (hvhgt, crosst.f90:1366-1367,301-312): tbc/tbr and the fluxes
+   * uT, vT, wT */
+  cplx *tbc, *utc, *vtc, *wtc;
+  double *tbr, *utr, *vtr, *wtr;
 } pthread_buf;
 
 typedef struct {
   orc_params p;
   int mgalx, my, mgalz, mx, mz, mx1, my1, mz1, mgx, nz, nz1, nz2, nkx;
-  double pi, pi2, dx, dy, dz, Lx, Lz, cflx, cfly, cflz, cflvv, h;
+  double pi, pi2, dx, dy, dz, Lx, Lz, cflx, cfly, cflz, cflvv, cflkk, h;
   double *y;
   double *xalp_im, *xgam_im, *alp2, *gam2;
   double pr1[7], rh1[7], rh1h[7], pr2[7], rh2[7], rh2h[7];
@@ -955,6 +959,8 @@ void *orc_create(const orc_params *p) {
     double mm = m1 > m2 ? m1 : m2;
     mm = mm > m3 ? mm : m3;
     c->cflvv = 1.0 / p->Re / CFL * mm;
+    /* thermal diffusion CFL (initcr.f90:498-502) */
+    c->cflkk = p->temperature ? p->fkappa / CFL * mm : 0.0;
   }
   /* update_dy (diffy_shear_hepta.f90:562-573) */
   c->h = c->dy;
@@ -992,6 +998,10 @@ void *orc_create(const orc_params *p) {
       b->sij2 = dalloc(nr);
       b->nus = dalloc(nr);
     }
+    if (p->temperature) {
+      b->tbc = zalloc(np); b->utc = zalloc(np); b->vtc = zalloc(np); b->wtc = zalloc(np);
+      b->tbr = dalloc(nr); b->utr = dalloc(nr); b->vtr = dalloc(nr); b->wtr = dalloc(nr);
+    }
     int mm = c->mgalx > c->mgalz ? c->mgalx : c->mgalz;
     b->col = zalloc(mm);
     b->row = zalloc(mm);
@@ -1014,6 +1024,8 @@ void orc_destroy(void *h) {
       free(b->lr[f]);
     }
     free(b->wyc); free(b->sij2); free(b->nus);
+    free(b->tbc); free(b->utc); free(b->vtc); free(b->wtc);
+    free(b->tbr); free(b->utr); free(b->vtr); free(b->wtr);
   }
   free(c->yt);
   free(c->pt);
@@ -1129,6 +1141,7 @@ void orc_fourxz(void *h, double *fou, double *phys, int iopt) {
 typedef struct {
   double ener[10], ener2[4];
   double umaxl[4];
+  double tbmaxl, enert[4]; /* temperature: max |tb| and tbp, utbp, vtbp, wtbp */
   double numax; /* LES: max |nuSGS| of the plane (cross.f90:1433) */
 } plane_red;
 
@@ -1137,7 +1150,7 @@ typedef struct {
 
 /* hist, flag 'f' (cross.f90:1796-1963): intensities, Pk, eps for plane j */
 static void hist_f(ctx *c, pthread_buf *b, const cplx *dv, double *ener, double *ener2,
-                   double txy00j) {
+                   double txy00j, const cplx *tbc, double *enert) {
   int nkx = c->nkx, mz = c->mz;
   double s = c->p.s;
   cplx *u1c = b->u1c, *u2c = b->u2c, *u3c = b->u3c, *o1c = b->o1c, *o2c = b->o2c,
@@ -1169,6 +1182,18 @@ static void hist_f(ctx *c, pthread_buf *b, const cplx *dv, double *ener, double 
   SUMSQ(o2c, o2p);
   SUMSQ(o3c, o3p);
   SUMCJ(o1c, o2c, o12p);
+  if (tbc) {
+    /* histt (crosst.f90:2151-2160, 2207-2210) */
+    double tbp, utbp, vtbp, wtbp;
+    SUMSQ(tbc, tbp);
+    SUMCJ(u1c, tbc, utbp);
+    SUMCJ(u2c, tbc, vtbp);
+    SUMCJ(u3c, tbc, wtbp);
+    enert[0] += tbp;
+    enert[1] += utbp;
+    enert[2] += vtbp;
+    enert[3] += wtbp;
+  }
 #undef SUMSQ
 #undef SUMCJ
   ener[0] += up; ener[1] += vp; ener[2] += wp;
@@ -1333,8 +1358,15 @@ static void hvhg_plane(ctx *c, pthread_buf *b, int j, const cplx *phic, const cp
                        const double *w00, const double *rf0u_in, const double *rf0w_in,
                        double *rf0u_out, double *rf0w_out, int rkstep, int ihist,
                        plane_red *red, cplx *rhvc1, cplx *rhvc2, cplx *rhgc1, cplx *rhgc2,
-                       double *txy00, double *tyz00) {
+                       double *txy00, double *tyz00, const cplx *tempc, const double *tb00,
+                       cplx *rhtc, cplx *rhtc2, double *rf0tb) {
   int nkx = c->nkx, mz = c->mz, mgalx = c->mgalx, mgalz = c->mgalz;
+  /* temperature (hvhgt, crosst.f90:1459-1462): tbc = tempc with the mean tb00 */
+  cplx *tbc = tempc ? b->tbc : NULL;
+  if (tbc) {
+    for (int q = 0; q < nkx * mz; q++) tbc[q] = tempc[q];
+    tbc[0] = C(tb00[j], 0.0);
+  }
   int ld = mgalx + 2;
   double s = c->p.s, chi = c->p.chi;
   cplx *u1c = b->u1c, *u2c = b->u2c, *u3c = b->u3c, *o1c = b->o1c, *o2c = b->o2c,
@@ -1376,13 +1408,15 @@ static void hvhg_plane(ctx *c, pthread_buf *b, int j, const cplx *phic, const cp
   u2c[0] = C(c->p.vbulk, 0.0);
   if (c->p.les)
     les_plane(c, b, rhvc, rhvc1, rhvc2, rhgc1, rhgc2, &txy00[j], &tyz00[j], rkstep, red);
-  if (ihist) hist_f(c, b, rhvc, red->ener, red->ener2, c->p.les ? txy00[j] : 0.0);
+  if (ihist)
+    hist_f(c, b, rhvc, red->ener, red->ener2, c->p.les ? txy00[j] : 0.0, tbc, red->enert);
   fourxz(c, b, u1c, b->u1r, 1);
   fourxz(c, b, u2c, b->u2r, 1);
   fourxz(c, b, u3c, b->u3r, 1);
   fourxz(c, b, o1c, b->o1r, 1);
   fourxz(c, b, o2c, b->o2r, 1);
   fourxz(c, b, o3c, b->o3r, 1);
+  if (tbc) fourxz(c, b, tbc, b->tbr, 1);
   double *u1r = b->u1r, *u2r = b->u2r, *u3r = b->u3r, *o1r = b->o1r, *o2r = b->o2r,
          *o3r = b->o3r;
   if (rkstep == 1) {
@@ -1399,6 +1433,32 @@ static void hvhg_plane(ctx *c, pthread_buf *b, int j, const cplx *phic, const cp
         if (a3 > m3) m3 = a3;
       }
     red->umaxl[0] = m0; red->umaxl[1] = m1; red->umaxl[2] = m2; red->umaxl[3] = m3;
+    if (tbc) {
+      /* crosst.f90:1674-1676 */
+      double tm = red->tbmaxl;
+      for (int z = 0; z < mgalz; z++)
+        for (int x = 0; x < mgalx; x++) {
+          double a = fabs(b->tbr[z * ld + x]);
+          if (a > tm) tm = a;
+        }
+      red->tbmaxl = tm;
+    }
+  }
+  if (tbc) {
+    /* fluxes uT, wT, vT and -vT (crosst.f90:1680-1693) */
+    double *tbr = b->tbr;
+    for (int z = 0; z < mgalz; z++)
+      for (int x = 0; x < mgalx + 2; x++) {
+        int q = z * ld + x;
+        b->utr[q] = u1r[q] * tbr[q];
+        b->wtr[q] = u3r[q] * tbr[q];
+        b->vtr[q] = u2r[q] * tbr[q];
+      }
+    fourxz(c, b, b->utc, b->utr, -1);
+    fourxz(c, b, b->wtc, b->wtr, -1);
+    fourxz(c, b, b->vtc, b->vtr, -1);
+    for (int q = 0; q < nkx * mz; q++) rhtc2[q] = cneg(b->vtc[q]);
+    rf0tb[j] = -b->vtc[0].re;
   }
   /* u x omega (cross.f90:1453-1462) */
   double chi2 = 2.0 * chi;
@@ -1418,7 +1478,19 @@ static void hvhg_plane(ctx *c, pthread_buf *b, int j, const cplx *phic, const cp
   fourxz(c, b, u3c, u3r, -1);
   rf0u_out[j] = u2c[0].re;
   rf0w_out[j] = u1c[0].re;
-  /* iadd_mode = 5 right-hand sides (cross.f90:1536-1546) */
+  /* iadd_mode = 5 right-hand sides (cross.f90:1536-1546); the temperature
+   * one first, from the input v (crosst.f90:1148-1152) */
+  if (tbc)
+    for (int k = 0; k < mz; k++) {
+      double g = c->xgam_im[k];
+      for (int i = 0; i < nkx; i++) {
+        double a = c->xalp_im[i];
+        int q = k * nkx + i;
+        cplx uT = b->utc[q], wT = b->wtc[q];
+        cplx t = csub(cneg(C(-a * uT.im, a * uT.re)), C(-g * wT.im, g * wT.re));
+        rhtc[q] = csub(t, cscal(c->p.bym, rhgc[q]));
+      }
+    }
   for (int k = 0; k < mz; k++) {
     double g = c->xgam_im[k];
     for (int i = 0; i < nkx; i++) {
@@ -1456,6 +1528,33 @@ static void moving_frame(ctx *c, double *vor, double *phi, double mtime) {
       }
     }
   free(sydt);
+}
+
+/* moving_frame_t (operators.f90:147-196): the same phase on one field */
+static void moving_frame_t(ctx *c, double *temp, double mtime) {
+  int my = c->my, nkx = c->nkx, mz = c->mz;
+  cplx *sydt = zalloc((size_t)my * nkx);
+  for (int i = 0; i < nkx; i++)
+    for (int j = 0; j < my; j++) {
+      double th = (c->xalp_im[i] * c->y[j]) * mtime;
+      sydt[i * my + j] = C(cos(th), sin(th));
+    }
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < mz; k++)
+    for (int i = 0; i < nkx; i++) {
+      cplx *v = (cplx *)PEN(temp, i, k);
+      for (int j = 0; j < my; j++) v[j] = cmul(v[j], sydt[i * my + j]);
+    }
+  free(sydt);
+}
+
+/* set_conj_t (operators.f90:1432-1472) on one pencil array */
+static void set_conj_t(ctx *c, double *f) {
+  int my = c->my, nkx = c->nkx;
+  for (int k = c->nz + 1; k <= c->mz1; k++) {
+    cplx *dst = (cplx *)PEN(f, 0, k), *src = (cplx *)PEN(f, 0, c->mz - k);
+    for (int j = 0; j < my; j++) dst[j] = cconj(src[j]);
+  }
 }
 
 /* set_conj (operators.f90:1382-1429) applied to pencil arrays */
@@ -1705,10 +1804,11 @@ int orc_physical(void *h, const double *vor_in, const double *phi_in, const doub
   return nout;
 }
 
-int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, double *ptime,
-              double *pxoffb, double *pxofft, int nstep, double *trace, int *ntrace,
-              int *pistop, double *pdeltat) {
-  ctx *c = (ctx *)h;
+/* cross (cross.f90:3-1029) or, with tb != NULL, crosst (crosst.f90:3-1310):
+ * the explicit branch with iadd_mode = 5 */
+static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00, double *tb,
+                     double *tb00, double *ptime, double *pxoffb, double *pxofft, int nstep,
+                     double *trace, int *ntrace, int *pistop, double *pdeltat) {
   int my = c->my, nkx = c->nkx, mz = c->mz, mx1 = c->mx1;
   size_t nfield = 2 * (size_t)my * nkx * mz; /* doubles per pencil field */
   size_t nplane = (size_t)nkx * mz;
@@ -1730,6 +1830,22 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
   /* LES buffers rhvc1, rhvc2, rhgc1, rhgc2 (pencil and plane) and T12, T23 of
    * the (0,0) mode (cross.f90:242-247) */
   int les = c->p.les;
+  /* temperature: tb, its RK work array, ht, rhtc2 (pencils), their plane
+   * copies, the mean-mode right-hand side rf0tb and tb00wk (crosst.f90:47-67) */
+  const int temp = (tb != NULL);
+  const int tlen = temp ? ORC_TRACE_LEN_T : ORC_TRACE_LEN;
+  double *tbwk = NULL, *ht = NULL, *rt2 = NULL;
+  cplx *b3 = NULL, *pht = NULL, *prt2 = NULL;
+  double *rf0tb = dalloc(my), *tb00wk = dalloc(my);
+  double fkappa = c->p.fkappa, gbeta = c->p.gbeta;
+  if (temp) {
+    tbwk = dalloc(nfield);
+    ht = dalloc(nfield);
+    rt2 = dalloc(nfield);
+    b3 = zalloc(nplane * my);
+    pht = zalloc(nplane * my);
+    prt2 = zalloc(nplane * my);
+  }
   double *lp[4] = {NULL, NULL, NULL, NULL};
   cplx *lq[4] = {NULL, NULL, NULL, NULL};
   double *txy00 = dalloc(my), *tyz00 = dalloc(my);
@@ -1744,9 +1860,10 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
   }
   double xwkb = xoffb, xwkt = xofft;
   int istop = 0, idump = 0, irun = 0, ihist = 1, nt = 0, done = 0;
-  double umax[4] = {0, 0, 0, 0}, CFL = c->p.CFL, CFLv = 0.0;
-  /* entry: set_conj on the state (cross.f90:283-287) */
+  double umax[4] = {0, 0, 0, 0}, CFL = c->p.CFL, CFLv = 0.0, CFLk = 0.0, tbmax = 0.0;
+  /* entry: set_conj on the state (cross.f90:283-287, crosst.f90:327-337) */
   set_conj_pencil(c, vor, phi);
+  if (temp) set_conj_t(c, tb);
   /* iydealiasing = 3 at entry (cross.f90:214-227), with the phase work array
    * of a fresh run (initcr.f90:370) */
   if (c->p.ydeal == 3) filter_state(c, vor, phi, u00, w00, shwkt);
@@ -1759,7 +1876,9 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
     }
     xwkt = xofft;
     xwkb = xoffb;
-    if ((istep - 1) != 1) {
+    /* cross checks from the third step on (cross.f90:221), crosst from the
+     * second (crosst.f90:259) */
+    if ((istep - 1) != (temp ? 0 : 1)) {
       if (istop == 1 || idump == 1) {
         if (istop == 1) break;
         idump = 0;
@@ -1815,6 +1934,8 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
           b2[(size_t)j * nplane + (size_t)k * nkx] = cconj(b2[(size_t)j * nplane + (size_t)(mz - k) * nkx]);
           b1[(size_t)j * nplane + (size_t)k * nkx] = cconj(b1[(size_t)j * nplane + (size_t)(mz - k) * nkx]);
         }
+      /* the temperature copy gets no set_conj (crosst.f90:556-559) */
+      if (temp) to_plane(c, tb, b3);
       to_plane(c, hv, phv);
       to_plane(c, hg, phg);
       to_plane(c, dvordy, pdv);
@@ -1835,7 +1956,8 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
           hvhg_plane(c, bb, j, b1 + o, b2 + o, phv + o, phg + o, pdv + o, u00, w00, rf0u_d,
                      rf0w_d, rf0u, rf0w, rkstep, ihist, &red[j], les ? lq[0] + o : NULL,
                      les ? lq[1] + o : NULL, les ? lq[2] + o : NULL, les ? lq[3] + o : NULL,
-                     txy00, tyz00);
+                     txy00, tyz00, temp ? b3 + o : NULL, tb00, temp ? pht + o : NULL,
+                     temp ? prt2 + o : NULL, rf0tb);
         }
         if (rkstep == 1) {
           double ul[4] = {uinit, uinit, uinit, uinit};
@@ -1843,6 +1965,11 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
             for (int q = 0; q < 4; q++)
               if (red[j].umaxl[q] > ul[q]) ul[q] = red[j].umaxl[q];
           for (int q = 0; q < 4; q++) umax[q] = ul[q];
+          if (temp) {
+            tbmax = 0.0;
+            for (int j = 0; j < my; j++)
+              if (red[j].tbmaxl > tbmax) tbmax = red[j].tbmaxl;
+          }
           if (les)
             for (int j = 0; j < my; j++)
               if (red[j].numax > c->max_nut) c->max_nut = red[j].numax;
@@ -1891,7 +2018,13 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
               }
             }
             CFLv = CFL * c->cflvv * dt;
-            if (CFLv > CFL) dt = 1.0 / c->cflvv;
+            if (temp) {
+              /* crosst.f90:1236-1257 */
+              CFLk = CFL * c->cflkk * dt;
+              if (CFLv > CFL) dt = (CFLk > CFLv) ? 1.0 / c->cflkk : 1.0 / c->cflvv;
+            } else if (CFLv > CFL) {
+              dt = 1.0 / c->cflvv;
+            }
           }
           Deltat = dt;
           if (Deltat < 1e-10) istop = 1;
@@ -1919,13 +2052,22 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
           uner[9] = ener[9] / (double)my;
           for (int q = 0; q < 4; q++) uner2[q] = ener2[q] / (double)my;
           if (trace) {
-            double *r = trace + (size_t)nt * ORC_TRACE_LEN;
+            double *r = trace + (size_t)nt * tlen;
             r[0] = time; r[1] = Deltat;
             for (int q = 0; q < 10; q++) r[2 + q] = uner[q];
             r[12] = CFL; r[13] = CFLv;
             r[14] = umax[1]; r[15] = umax[2]; r[16] = umax[3];
             r[17] = xoffb; r[18] = xofft; r[19] = umax[0];
             for (int q = 0; q < 4; q++) r[20 + q] = uner2[q];
+            if (temp) {
+              /* histt 'w' (crosst.f90:2446-2458) */
+              double enert[4] = {0, 0, 0, 0};
+              for (int j = 0; j < my; j++)
+                for (int q = 0; q < 4; q++) enert[q] += red[j].enert[q];
+              r[24] = tbmax;
+              r[25] = sqrt(fabs(enert[0] / (double)my));
+              for (int q = 1; q < 4; q++) r[25 + q] = enert[q] / (double)my;
+            }
           }
           nt++;
           if (isnan(uner[0])) istop = 1;
@@ -1940,6 +2082,10 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
       to_pencil(c, phv, hv);
       to_pencil(c, phg, hg);
       to_pencil(c, pdv, dvordy);
+      if (temp) {
+        to_pencil(c, pht, ht);
+        to_pencil(c, prt2, rt2);
+      }
       if (les)
         for (size_t q = 0; q < nfield; q++) dvordy[q] = dvordy[q] - lp[0][q];
 #pragma omp parallel for schedule(static)
@@ -1948,6 +2094,12 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
         ythread *t = &c->yt[my_thread()];
         derivyc(c, t, PEN(dvordy, i, k), PEN(dvordy, i, k), shwkt[i], shwkb[i], 1, 2, 1);
         if (les) derivyc(c, t, PEN(lp[3], i, k), PEN(lp[3], i, k), shwkt[i], shwkb[i], 1, 2, 0);
+        /* -d(vT)/dy (crosst.f90:633-636) */
+        if (temp) derivyc(c, t, PEN(rt2, i, k), PEN(rt2, i, k), shwkt[i], shwkb[i], 1, 2, 0);
+      }
+      if (temp) {
+        cplx one = C(1.0, 0.0);
+        derivyc(c, &c->yt[0], rf0tb, rf0tb, one, one, 1, 1, 0);
       }
       if (les) {
         /* hv += (d2/dx2 + d2/dz2 - d2/dy2) rhvc2 (cross.f90:578-595) */
@@ -1965,6 +2117,8 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
       for (size_t q = 0; q < nfield; q++) hv[q] = hv[q] - dvordy[q];
       if (les)
         for (size_t q = 0; q < nfield; q++) hg[q] = hg[q] + lp[2][q] + lp[3][q];
+      if (temp)
+        for (size_t q = 0; q < nfield; q++) ht[q] = ht[q] + rt2[q];
       double r1 = CA[rkstep - 1] * Deltat;
       double fac = 1.0 / Re;
       if (les) {
@@ -1987,11 +2141,17 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
             double *scr = ddu + 2 * (size_t)my * ik;
             visc3d(c, t, PEN(vor, i, k), PEN(hg, i, k), scr, shwkt[i], shwkb[i], 2, rk, fac, 1);
             visc3d(c, t, PEN(phi, i, k), PEN(hv, i, k), scr, shwkt[i], shwkb[i], 2, rk, fac, 0);
+            if (temp) {
+              /* thermal diffusion and buoyancy (crosst.f90:734-738) */
+              visc3d(c, t, PEN(tb, i, k), PEN(ht, i, k), scr, shwkt[i], shwkb[i], 2, rk, fkappa, 0);
+              visc3d(c, t, PEN(tb, i, k), PEN(hv, i, k), scr, shwkt[i], shwkb[i], 2, rk, gbeta, 0);
+            }
           }
         }
         cplx one = C(1.0, 0.0);
         visc3d(c, &c->yt[0], u00, rf0u, wk1dr, one, one, 1, 0.0, fac, 0);
         visc3d(c, &c->yt[0], w00, rf0w, wk1dr, one, one, 1, 0.0, fac, 0);
+        if (temp) visc3d(c, &c->yt[0], tb00, rf0tb, wk1dr, one, one, 1, 0.0, fkappa, 0);
       }
       double gk = GAMA[rkstep - 1];
       if (rkstep == 1) {
@@ -2003,6 +2163,10 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
           u00wk[j] = gk * rf0u[j];
           w00wk[j] = gk * rf0w[j];
         }
+        if (temp) {
+          for (size_t q = 0; q < nfield; q++) tbwk[q] = gk * ht[q];
+          for (int j = 0; j < my; j++) tb00wk[j] = gk * rf0tb[j];
+        }
       } else {
         for (size_t q = 0; q < nfield; q++) {
           vorwk[q] = vorwk[q] + gk * hg[q];
@@ -2012,6 +2176,10 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
           u00wk[j] = u00wk[j] + gk * rf0u[j];
           w00wk[j] = w00wk[j] + gk * rf0w[j];
         }
+        if (temp) {
+          for (size_t q = 0; q < nfield; q++) tbwk[q] = tbwk[q] + gk * ht[q];
+          for (int j = 0; j < my; j++) tb00wk[j] = tb00wk[j] + gk * rf0tb[j];
+        }
       }
       for (size_t q = 0; q < nfield; q++) {
         vor[q] = vor[q] + Deltat * vorwk[q];
@@ -2020,6 +2188,10 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
       for (int j = 0; j < my; j++) {
         u00[j] = u00[j] + Deltat * u00wk[j];
         w00[j] = w00[j] + Deltat * w00wk[j];
+      }
+      if (temp) {
+        for (size_t q = 0; q < nfield; q++) tb[q] = tb[q] + Deltat * tbwk[q];
+        for (int j = 0; j < my; j++) tb00[j] = tb00[j] + Deltat * tb00wk[j];
       }
       if (fabs(s) > 0.01) {
         xwkb = xoffb + r1 * u00b;
@@ -2043,14 +2215,21 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
         double mf = (rkstep == 1) ? -(GAMA[0] * Deltat * s)
                                   : -((GAMA[1] + ZETA[0]) * Deltat * s);
         moving_frame(c, vorwk, phiwk, mf);
+        if (temp) {
+          for (size_t q = 0; q < nfield; q++) tbwk[q] = ht[q] * zk;
+          moving_frame_t(c, tbwk, mf);
+        }
         for (int j = 0; j < my; j++) {
           u00wk[j] = rf0u[j] * zk;
           w00wk[j] = rf0w[j] * zk;
         }
+        if (temp)
+          for (int j = 0; j < my; j++) tb00wk[j] = rf0tb[j] * zk;
       }
       {
         double mf = (rkstep == 1) ? -(s * r1) : -(s * (CA[rkstep - 1] - CA[rkstep - 2]) * Deltat);
         moving_frame(c, vor, phi, mf);
+        if (temp) moving_frame_t(c, tb, mf);
       }
 #pragma omp parallel for schedule(static)
       for (int ik = 0; ik < nkx * mz; ik++) {
@@ -2086,5 +2265,22 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
     free(lq[f]);
   }
   free(txy00); free(tyz00);
+  free(rf0tb); free(tb00wk); free(tbwk); free(ht); free(rt2); free(b3); free(pht); free(prt2);
   return done;
+}
+
+int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, double *ptime,
+              double *pxoffb, double *pxofft, int nstep, double *trace, int *ntrace,
+              int *pistop, double *pdeltat) {
+  return cross_run((ctx *)h, vor, phi, u00, w00, NULL, NULL, ptime, pxoffb, pxofft, nstep,
+                   trace, ntrace, pistop, pdeltat);
+}
+
+int orc_crosst(void *h, double *vor, double *phi, double *u00, double *w00, double *tb,
+               double *tb00, double *ptime, double *pxoffb, double *pxofft, int nstep,
+               double *trace, int *ntrace, int *pistop, double *pdeltat) {
+  ctx *c = (ctx *)h;
+  if (!c->p.temperature || !tb || !tb00) return -1;
+  return cross_run(c, vor, phi, u00, w00, tb, tb00, ptime, pxoffb, pxofft, nstep, trace,
+                   ntrace, pistop, pdeltat);
 }

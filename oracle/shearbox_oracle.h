@@ -42,11 +42,16 @@ typedef struct orc_params {
                            * 2 the moving-frame variant on every kx (dealiasing_y,
                            * operators.f90:352-467), 3 compact y-filter
                            * (cross.f90:214-227,476-490) */
+  int temperature;        /* itemperature: Boussinesq scalar tb of crosst (crosst.f90:3-1310) */
+  double fkappa, bym, gbeta; /* its diffusivity, mean gradient and buoyancy factor
+                           * (hre3.dat keyword itemperature, initcr.f90:1996-2011) */
 } orc_params;
 
 /* one .cfbin record per statistics step (cross.f90:2087):
  * time, Deltat, uner(1:10), CFL, CFLv, umax(1:3), xoffb, xofft, umax(0), uner2(1:4) */
 #define ORC_TRACE_LEN 24
+/* crosst writes the same record followed by tbmax, tner(1:4) (crosst.f90:2456-2458) */
+#define ORC_TRACE_LEN_T 29
 
 void *orc_create(const orc_params *p);
 void orc_destroy(void *h);
@@ -62,6 +67,13 @@ void orc_set_threads(int n);
 int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00,
               double *time, double *xoffb, double *xofft, int nstep,
               double *trace, int *ntrace, int *istop, double *deltat);
+
+/* crosst(): cross with the scalar tb (pencil layout like vor) and its mean
+ * profile tb00(0:my1); needs temperature = 1.  Trace records have
+ * ORC_TRACE_LEN_T doubles. */
+int orc_crosst(void *h, double *vor, double *phi, double *u00, double *w00, double *tb,
+               double *tb00, double *time, double *xoffb, double *xofft, int nstep,
+               double *trace, int *ntrace, int *istop, double *deltat);
 
 /* building blocks, one y-line (complex: m=2, real: m=1) */
 void orc_filterc(void *h, const double *u, double *du, double shp_re, double shp_im, int m);

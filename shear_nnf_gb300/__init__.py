@@ -22,6 +22,9 @@ TRACE_FIELDS = (
     ["time", "Deltat"] + [f"uner{q}" for q in range(1, 11)] + ["CFL", "CFLv", "umax1", "umax2",
     "umax3", "xoffb", "xofft", "umax0"] + [f"uner2_{q}" for q in range(1, 5)]
 )
+# crosst appends tbmax and tner(1:4) (crosst.f90:2456-2458)
+TRACE_LEN_T = 29
+TRACE_FIELDS_T = TRACE_FIELDS + ["tbmax"] + [f"tner{q}" for q in range(1, 5)]
 SB_FP64 = 0
 SB_MIXED = 1
 
@@ -36,6 +39,8 @@ class SbParams(ctypes.Structure):
         ("etime", ctypes.c_double), ("dumptime", ctypes.c_double), ("dtimag", ctypes.c_double),
         ("keep_laminar", ctypes.c_int), ("les", ctypes.c_int), ("les_visc", ctypes.c_int),
         ("cs", ctypes.c_double), ("ydeal", ctypes.c_int),
+        ("temperature", ctypes.c_int), ("fkappa", ctypes.c_double), ("bym", ctypes.c_double),
+        ("gbeta", ctypes.c_double),
     ]
 
 
@@ -75,7 +80,8 @@ ABI_FUNCTIONS = [
     "sb_seed_state", "sb_compact_coeffs", "sb_last_error", "sb_version", "sb_launch_stage",
     "sb_fp64_peak", "sb_op_derivyc", "sb_op_lapcdy", "sb_op_derivyc_noalloc",
     "sb_set_member_etime", "sb_op_filterc", "sb_op_cfty", "sb_op_rfty", "sb_write_restart",
-    "sb_read_restart", "sb_autotune", "sb_physical_fields",
+    "sb_read_restart", "sb_autotune", "sb_physical_fields", "sb_set_temperature",
+    "sb_get_temperature", "sb_crosst",
 ]
 
 _lib = None
@@ -106,6 +112,10 @@ def lib(auto_build: bool = False):
     L.sb_get_status.argtypes = [vp, ctypes.c_int, ctypes.POINTER(SbStatus)]
     L.sb_get_trace.argtypes = [vp, ctypes.c_int, dp, ctypes.c_int, ip]
     L.sb_cross.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int, ctypes.POINTER(SbStatus)]
+    L.sb_crosst.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int,
+                            ctypes.POINTER(SbStatus)]
+    L.sb_set_temperature.argtypes = [vp, ctypes.c_int, dp, dp]
+    L.sb_get_temperature.argtypes = [vp, ctypes.c_int, dp, dp]
     L.sb_get_stream.restype = vp
     L.sb_get_stream.argtypes = [vp]
     L.sb_sync.argtypes = [vp]
@@ -152,9 +162,11 @@ def _dp(a: np.ndarray):
 
 def make_params(mgalx, my, mgalz, Re, alp, Ly, gam, s=1.0, chi=0.0, CFL=0.5, vbulk=0.0,
                 fixed_dt=0.0, readflag=1, uprim=1.0, nhist=1, etime=1e10, dumptime=1e10,
-                dtimag=1e10, keep_laminar=0, les=0, les_visc=1, cs=0.1, ydeal=0) -> SbParams:
+                dtimag=1e10, keep_laminar=0, les=0, les_visc=1, cs=0.1, ydeal=0, temperature=0,
+                fkappa=0.0, bym=0.0, gbeta=0.0) -> SbParams:
     return SbParams(mgalx, my, mgalz, Re, alp, Ly, gam, s, chi, CFL, vbulk, fixed_dt, readflag,
-                    uprim, nhist, etime, dumptime, dtimag, keep_laminar, les, les_visc, cs, ydeal)
+                    uprim, nhist, etime, dumptime, dtimag, keep_laminar, les, les_visc, cs, ydeal,
+                    temperature, fkappa, bym, gbeta)
 
 
 def sizes(p: SbParams) -> dict:
@@ -164,11 +176,8 @@ def sizes(p: SbParams) -> dict:
     return dict(zip(keys, list(out)))
 
 
-def seed_state(p: SbParams, seed: int, k0: float = 4.0, urms: float = None) -> dict:
-    """Seeded divergence-free initial field (pencil layout, complex128)."""
+def _seed_fields(p: SbParams, seed: int, k0: float, urms: float):
     sz = sizes(p)
-    if urms is None:
-        urms = 0.1 * 1.0 * (2 * np.pi / p.gam)  # 0.1 * S * Lz
     vor = np.zeros((sz["mz"], sz["nkx"], p.my), np.complex128)
     phi = np.zeros_like(vor)
     u00 = np.zeros(p.my)
@@ -176,8 +185,23 @@ def seed_state(p: SbParams, seed: int, k0: float = 4.0, urms: float = None) -> d
     _check(lib().sb_seed_state(ctypes.byref(p), int(seed), float(k0), float(urms),
                                _dp(vor.view(np.float64)), _dp(phi.view(np.float64)), _dp(u00),
                                _dp(w00)))
-    return {"vor": vor, "phi": phi, "u00": u00, "w00": w00, "time": 0.0, "xoffb": 0.0,
-            "xofft": 0.0}
+    return vor, phi, u00, w00
+
+
+def seed_state(p: SbParams, seed: int, k0: float = 4.0, urms: float = None) -> dict:
+    """Seeded divergence-free initial field (pencil layout, complex128).  With
+    the temperature also a seeded scalar: tb from the omega_y of a second seed
+    scaled by 1/k0 (fluctuations of order urms) and tb00 from its u00."""
+    if urms is None:
+        urms = 0.1 * 1.0 * (2 * np.pi / p.gam)  # 0.1 * S * Lz
+    vor, phi, u00, w00 = _seed_fields(p, seed, k0, urms)
+    st = {"vor": vor, "phi": phi, "u00": u00, "w00": w00, "time": 0.0, "xoffb": 0.0,
+          "xofft": 0.0}
+    if p.temperature:
+        tv, _, t00, _ = _seed_fields(p, (int(seed) * 7919 + 17) & 0xFFFFFFFF, k0, urms)
+        st["tb"] = np.ascontiguousarray(tv / k0)
+        st["tb00"] = t00
+    return st
 
 
 def compact_coeffs():
@@ -219,6 +243,12 @@ class ShearBox:
         _check(lib().sb_set_member_etime(self.h, member, float(etime)))
 
     def set_state(self, state: dict, member: int = 0):
+        """Copies a state in; with the temperature the keys tb and tb00 are
+        required."""
+        if self.p.temperature:
+            tb = np.ascontiguousarray(state["tb"], np.complex128)
+            tb00 = np.ascontiguousarray(state["tb00"], np.float64)
+            _check(lib().sb_set_temperature(self.h, member, _dp(tb.view(np.float64)), _dp(tb00)))
         vor = np.ascontiguousarray(state["vor"], np.complex128)
         phi = np.ascontiguousarray(state["phi"], np.complex128)
         u00 = np.ascontiguousarray(state["u00"], np.float64)
@@ -239,8 +269,14 @@ class ShearBox:
         _check(lib().sb_get_state(self.h, member, _dp(vor.view(np.float64)),
                                   _dp(phi.view(np.float64)), _dp(u00), _dp(w00), ctypes.byref(t),
                                   ctypes.byref(xb), ctypes.byref(xt)))
-        return {"vor": vor, "phi": phi, "u00": u00, "w00": w00, "time": t.value,
-                "xoffb": xb.value, "xofft": xt.value}
+        st = {"vor": vor, "phi": phi, "u00": u00, "w00": w00, "time": t.value,
+              "xoffb": xb.value, "xofft": xt.value}
+        if self.p.temperature:
+            tb = np.zeros_like(vor)
+            tb00 = np.zeros(self.p.my)
+            _check(lib().sb_get_temperature(self.h, member, _dp(tb.view(np.float64)), _dp(tb00)))
+            st["tb"], st["tb00"] = tb, tb00
+        return st
 
     def launch_stage(self, stage: int, rk: int = 1, count: int = 1):
         _check(lib().sb_launch_stage(self.h, int(stage), int(rk), int(count)))
@@ -284,23 +320,32 @@ class ShearBox:
         n = ctypes.c_int()
         st = self.status(member)
         m = min(max_records, max(st.ntrace, 0))
-        out = np.zeros((max(m, 1), TRACE_LEN))
+        out = np.zeros((max(m, 1), TRACE_LEN_T if self.p.temperature else TRACE_LEN))
         _check(lib().sb_get_trace(self.h, member, _dp(out), m, ctypes.byref(n)))
         return out[: n.value]
 
     def cross(self, state: dict, nstep: int) -> tuple:
-        """Drop-in for the reference ``cross``: advances box 0 by nstep steps in
-        place on host arrays; returns (trace, status)."""
-        for key in ("vor", "phi"):
+        """Drop-in for the reference ``cross`` (``crosst`` when the handle has
+        the temperature, with state keys tb and tb00): advances box 0 by nstep
+        steps in place on host arrays; returns (trace, status)."""
+        keys = ("vor", "phi", "tb") if self.p.temperature else ("vor", "phi")
+        for key in keys:
             assert state[key].dtype == np.complex128 and state[key].flags["C_CONTIGUOUS"]
         t = ctypes.c_double(state["time"])
         xb = ctypes.c_double(state["xoffb"])
         xt = ctypes.c_double(state["xofft"])
         st = SbStatus()
-        _check(lib().sb_cross(self.h, _dp(state["vor"].view(np.float64)),
-                              _dp(state["phi"].view(np.float64)), _dp(state["u00"]),
-                              _dp(state["w00"]), ctypes.byref(t), ctypes.byref(xb),
-                              ctypes.byref(xt), int(nstep), ctypes.byref(st)))
+        if self.p.temperature:
+            _check(lib().sb_crosst(self.h, _dp(state["vor"].view(np.float64)),
+                                   _dp(state["phi"].view(np.float64)), _dp(state["u00"]),
+                                   _dp(state["w00"]), _dp(state["tb"].view(np.float64)),
+                                   _dp(state["tb00"]), ctypes.byref(t), ctypes.byref(xb),
+                                   ctypes.byref(xt), int(nstep), ctypes.byref(st)))
+        else:
+            _check(lib().sb_cross(self.h, _dp(state["vor"].view(np.float64)),
+                                  _dp(state["phi"].view(np.float64)), _dp(state["u00"]),
+                                  _dp(state["w00"]), ctypes.byref(t), ctypes.byref(xb),
+                                  ctypes.byref(xt), int(nstep), ctypes.byref(st)))
         state["time"], state["xoffb"], state["xofft"] = t.value, xb.value, xt.value
         return self.trace(0), st
 

@@ -86,6 +86,8 @@ static int check_params(const sb_params *p) {
                 p->mgalx, p->mgalz);
   if (p->mgalz % 2) return fail(1, "mgalz must be even");
   if (p->my < 16 || p->my > 448) return fail(1, "my=%d outside 16..448", p->my);
+  if (p->temperature != 0 && p->temperature != 1)
+    return fail(2, "itemperature=%d not available (0, 1)", p->temperature);
   if (!(p->Re != 0.0) || !(p->alp > 0) || !(p->gam > 0) || !(p->Ly > 0) || !(p->CFL > 0))
     return fail(1, "invalid physical parameters");
   return 0;
@@ -138,6 +140,8 @@ static void member_defaults(const sb_params *p, const Grid &g, double Re, Member
   m->readflag = p->readflag;
   m->nhist = p->nhist > 0 ? p->nhist : 1;
   m->keep_laminar = p->keep_laminar;
+  // thermal diffusion CFL (initcr.f90:498-502)
+  m->cflkk = p->temperature ? p->fkappa / p->CFL * mm : 0.0;
 }
 
 static int capture_step(sb_handle *h) {
@@ -180,7 +184,7 @@ static int ensure_trace(sb_handle *h, int cap) {
   if (cap <= h->trace_cap) return 0;
   cap = std::max(cap, 2 * h->trace_cap);
   double *t;
-  int rc = dalloc(h, &t, (size_t)h->g.B * cap * SB_TRACE_LEN);
+  int rc = dalloc(h, &t, (size_t)h->g.B * cap * h->g.tlen);
   if (rc) return rc;
   h->bf.trace = t;
   h->trace_cap = cap;
@@ -327,6 +331,20 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   g.les = p->les ? 1 : 0;
   g.les_visc = p->les_visc ? 1 : 0;
   g.nzf = g.les ? 10 : 6;
+  // temperature (crosst): one more z-transform field after the others, the
+  // three fluxes in xbuf, the longer statistics record
+  g.temp = p->temperature ? 1 : 0;
+  g.tround = g.les ? 5 : 3;
+  g.tzf = g.nzf;
+  g.nzf += g.temp;
+  g.nxf = g.temp ? 6 : 3;
+  g.tlen = g.temp ? SB_TRACE_LEN_T : SB_TRACE_LEN;
+  // diffusion and buoyancy sit with the molecular viscous terms, which an LES
+  // run without iadd_visc skips (crosst.f90:717-757)
+  const bool molec = !g.les || g.les_visc;
+  g.kappa = (g.temp && molec) ? p->fkappa : 0.0;
+  g.gbeta = (g.temp && molec) ? p->gbeta : 0.0;
+  g.bym = g.temp ? p->bym : 0.0;
   g.cbl = les_cb(p->mgalz);
   g.ncbl = (g.nkx + g.cbl - 1) / g.cbl;
   g.ydeal = p->ydeal;
@@ -382,12 +400,23 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
       (rc = A(&bf.mu, B * 2 * my)) || (rc = A(&bf.mwk, B * 2 * my)) ||
       (rc = A(&bf.mrf, B * 2 * my)) || (rc = A(&bf.mdu, B * 2 * my)) ||
       (rc = A(&bf.zbuf, B * my * g.mgalz * g.nzf * g.nkx * 2)) ||
-      (rc = A(&bf.xbuf, B * my * g.mgalz * 3 * g.nkx * 2)) ||
+      (rc = A(&bf.xbuf, B * my * g.mgalz * g.nxf * g.nkx * 2)) ||
       (rc = A(&bf.hpart, B * my * ((g.nkx + 3) / 4) * SB_NHIST_Q)) || (rc = A(&bf.sh_old, B * 4 * g.nkx)) ||
       (rc = A(&bf.sh_new, B * 4 * g.nkx)) || (rc = A(&bf.mf1, B * my * g.nkx * 2)) ||
       (rc = A(&bf.mf2, B * my * g.nkx * 2)) || (rc = A(&h->d_pen, F))) {
     sb_destroy(h);
     return rc;
+  }
+  if (g.temp &&
+      ((rc = A(&bf.tb, B * F)) || (rc = A(&bf.tbwk, B * F)) || (rc = A(&bf.Ht, B * F)) ||
+       (rc = A(&bf.R2, B * F)) || (rc = A(&bf.Lt, B * F)) || (rc = A(&bf.mt, B * 2 * my)) ||
+       (rc = A(&bf.mtwk, B * 2 * my)) || (rc = A(&bf.mtr, B * 2 * my)))) {
+    sb_destroy(h);
+    return rc;
+  }
+  if (g.temp && !plane3_fits(g, g.cb3)) {
+    g.cb3 = 4;
+    g.ncb3 = (g.nkx + g.cb3 - 1) / g.cb3;
   }
   if (g.les) {
     const size_t NX = g.mgalx, NZ = g.mgalz, nk = g.nkx;
@@ -640,6 +669,68 @@ int sb_get_state(sb_handle *h, int member, double *vor, double *phi, double *u00
   return 0;
 }
 
+// mean profile of one member: [my] reals <-> the re parts of a [my] complex
+// device line in the storage precision
+static int put_mean_re(sb_handle *h, double *dev, int member, const double *v) {
+  const Grid &g = h->g;
+  if (g.prec) {
+    std::vector<float> f(2 * (size_t)g.my, 0.0f);
+    for (int j = 0; j < g.my; j++) f[2 * j] = (float)v[j];
+    CK(cudaMemcpyAsync((float *)dev + (size_t)member * 2 * g.my, f.data(), sizeof(float) * f.size(),
+                       cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  } else {
+    std::vector<double> d(2 * (size_t)g.my, 0.0);
+    for (int j = 0; j < g.my; j++) d[2 * j] = v[j];
+    CK(cudaMemcpyAsync(dev + (size_t)member * 2 * g.my, d.data(), sizeof(double) * d.size(),
+                       cudaMemcpyHostToDevice, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  return 0;
+}
+static int get_mean_re(sb_handle *h, const double *dev, int member, double *v) {
+  const Grid &g = h->g;
+  if (g.prec) {
+    std::vector<float> f(2 * (size_t)g.my);
+    CK(cudaMemcpyAsync(f.data(), (const float *)dev + (size_t)member * 2 * g.my,
+                       sizeof(float) * f.size(), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    for (int j = 0; j < g.my; j++) v[j] = (double)f[2 * j];
+  } else {
+    std::vector<double> d(2 * (size_t)g.my);
+    CK(cudaMemcpyAsync(d.data(), dev + (size_t)member * 2 * g.my, sizeof(double) * d.size(),
+                       cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    for (int j = 0; j < g.my; j++) v[j] = d[2 * j];
+  }
+  return 0;
+}
+
+int sb_set_temperature(sb_handle *h, int member, const double *tb, const double *tb00) {
+  if (!h || member < 0 || member >= h->g.B) return fail(1, "bad handle or member");
+  if (!h->g.temp) return fail(2, "the handle was created without itemperature");
+  if (!tb || !tb00) return fail(1, "null temperature array");
+  const Grid &g = h->g;
+  const size_t Fd = g.prec ? g.field / 2 : g.field;
+  CK(cudaMemcpyAsync(h->d_pen, tb, sizeof(double) * g.field, cudaMemcpyHostToDevice, h->st));
+  CK(launch_pencil_to_plane(g, h->d_pen, h->bf.tb + member * Fd, h->st));
+  return put_mean_re(h, h->bf.mt, member, tb00);
+}
+
+int sb_get_temperature(sb_handle *h, int member, double *tb, double *tb00) {
+  if (!h || member < 0 || member >= h->g.B) return fail(1, "bad handle or member");
+  if (!h->g.temp) return fail(2, "the handle was created without itemperature");
+  const Grid &g = h->g;
+  const size_t Fd = g.prec ? g.field / 2 : g.field;
+  if (tb) {
+    CK(launch_plane_to_pencil(g, h->bf.tb + member * Fd, h->d_pen, h->st));
+    CK(cudaMemcpyAsync(tb, h->d_pen, sizeof(double) * g.field, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+  }
+  if (tb00) return get_mean_re(h, h->bf.mt, member, tb00);
+  return 0;
+}
+
 int sb_step(sb_handle *h, int nsteps) {
   if (!h) return fail(1, "null handle");
   if (nsteps < 0) return fail(1, "nsteps < 0");
@@ -681,8 +772,8 @@ int sb_get_trace(sb_handle *h, int member, double *out, int max_records, int *nr
   CK(cudaStreamSynchronize(h->st));
   int n = std::min(std::min(m.ntrace, h->trace_cap), max_records);
   if (n > 0 && out)
-    CK(cudaMemcpy(out, h->bf.trace + (size_t)member * h->trace_cap * SB_TRACE_LEN,
-                  sizeof(double) * n * SB_TRACE_LEN, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(out, h->bf.trace + (size_t)member * h->trace_cap * h->g.tlen,
+                  sizeof(double) * n * h->g.tlen, cudaMemcpyDeviceToHost));
   if (nrec) *nrec = n;
   return 0;
 }
@@ -694,6 +785,20 @@ int sb_cross(sb_handle *h, double *vor, double *phi, double *u00, double *w00, d
   if (rc) return rc;
   if ((rc = sb_step(h, nstep))) return rc;
   if ((rc = sb_get_state(h, 0, vor, phi, u00, w00, time, xoffb, xofft))) return rc;
+  if (st && (rc = sb_get_status(h, 0, st))) return rc;
+  return 0;
+}
+
+int sb_crosst(sb_handle *h, double *vor, double *phi, double *u00, double *w00, double *tb,
+              double *tb00, double *time, double *xoffb, double *xofft, int nstep,
+              sb_status *st) {
+  if (!h || !time || !xoffb || !xofft) return fail(1, "null argument");
+  if (!h->g.temp) return fail(2, "crosst needs a handle created with itemperature = 1");
+  int rc = sb_set_state(h, 0, vor, phi, u00, w00, *time, *xoffb, *xofft);
+  if (rc || (rc = sb_set_temperature(h, 0, tb, tb00))) return rc;
+  if ((rc = sb_step(h, nstep))) return rc;
+  if ((rc = sb_get_state(h, 0, vor, phi, u00, w00, time, xoffb, xofft))) return rc;
+  if ((rc = sb_get_temperature(h, 0, tb, tb00))) return rc;
   if (st && (rc = sb_get_status(h, 0, st))) return rc;
   return 0;
 }
@@ -770,6 +875,7 @@ int sb_autotune(sb_handle *h, int *choice) {
   best = 1e30f;
   for (int c : {8, 4}) {  // plane stage 3: kx columns per block
     if (e != cudaSuccess) break;
+    if (!plane3_fits(g, c)) continue;
     g.cb3 = c;
     g.ncb3 = (g.nkx + c - 1) / c;
     if ((e = timed(3, &t)) != cudaSuccess) break;
@@ -807,6 +913,7 @@ int sb_physical_fields(sb_handle *h, int member, unsigned mask, double *out) {
   gl.B = 1;
   gl.les = 1;
   gl.nzf = 10;
+  gl.temp = 0;
   Bufs bl = h->bf;
   const long Fd = g.prec ? g.field / 2 : g.field;
   const long Md = g.prec ? (long)g.my : 2L * g.my;

@@ -12,7 +12,8 @@
 #include <stdint.h>
 
 #define SB_TRACE_LEN 24
-#define SB_NHIST_Q 11   // per-plane hist partial sums
+#define SB_TRACE_LEN_T 29  // with the temperature: + tbmax, tner(1:4)
+#define SB_NHIST_Q 15   // per-plane hist partial sums (11, then 4 of the temperature)
 #define SB_MAX_NY 512
 #define SB_TAIL 24      // doubles per stored shear tail
 
@@ -71,6 +72,13 @@ struct Grid {
   // 2/3-rule cut indices (initcr.f90:207-210) and Lx
   int my23, ny1, ny2;
   double Lx;
+  // Boussinesq scalar of crosst (itemperature): on/off, k_p1 round of its
+  // z-transform, its zbuf field, fields per z row of xbuf (3, or 6 with the
+  // fluxes uT wT vT), trace record length; diffusivity and buoyancy factor
+  // (zero when an LES run drops the molecular terms, crosst.f90:717-757) and
+  // the mean gradient
+  int temp, tround, tzf, nxf, tlen;
+  double kappa, gbeta, bym;
 };
 
 // Per-member run state, owned by the device (one per box in the batch)
@@ -88,6 +96,9 @@ struct Member {
   unsigned long long nut_bits;      // LES: max |nu_t| of this step (bit pattern)
   double max_nut;                   // LES: running maximum of |nu_t| (cross.f90:1433)
   double ydfac;                     // y dealiasing: moving-frame shift of this substep
+  double cflkk;                     // temperature: thermal-diffusion CFL factor (initcr.f90:498-502)
+  double tbmax;                     // temperature: max |tb| of this step
+  unsigned long long tbmax_bits;
   int istop, idump, ihist, istep, halted, ntrace, trace_cap, flags;
 };
 
@@ -128,6 +139,11 @@ struct Bufs {
   // rhvc2 and rhgc2 fields, T12/T23 of the (0,0) mode [B][my] complex, plane
   // partial sums of nu_t and nu_t |S|^2 [B][my][mgalz/2][2]
   double *gbuf, *sbuf, *tbuf, *L1, *L2, *txy, *lpart;
+  // temperature: tb and its RK work array, the right-hand side ht (plane
+  // stage: -d(uT)/dx - d(wT)/dz - bym v, then += d(-vT)/dy), -vT, the
+  // Laplacian of tb (d2/dy2 - k^2) tb; mean profile tb00 [B][my] complex (re),
+  // its RK work array and d(-vT_00)/dy
+  double *tb, *tbwk, *Ht, *R2, *Lt, *mt, *mtwk, *mtr;
 };
 
 }  // namespace sb

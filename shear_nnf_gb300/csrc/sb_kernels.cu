@@ -83,6 +83,10 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
   const V *Gv = (const V *)((const R *)bf.G + pbase);
   const V mu = ((const V *)bf.mu)[(long)b * g.my + j];
   const V mdu = ((const V *)bf.mdu)[(long)b * g.my + j];
+  // temperature: tb as stored (its copy gets no set_conj, crosst.f90:556-559)
+  // with the (0,0) mode replaced by tb00 (crosst.f90:1459-1462)
+  const V *tbv = g.temp ? (const V *)((const R *)bf.tb + pbase) : nullptr;
+  const R tb00 = g.temp ? ((const V *)bf.mt)[(long)b * g.my + j].x : (R)0;
   // omega_y and phi with the kx=0 conjugate symmetry imposed (set_conj on the
   // copies buff1/buff2, cross.f90:493-502)
   auto ld_sym = [&](const V *p, int i, int k) -> V {
@@ -153,6 +157,19 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
       const double c3x = o3s.x + a * u2.y, c3y = o3s.y - a * u2.x;  // o3 - i a u2
       acc[10] += w * (Kk * (uu + vv + ww) + (dv.x * dv.x + dv.y * dv.y) +
                       (c1x * c1x + c1y * c1y) + (c3x * c3x + c3y * c3y));
+      if (g.temp) {
+        // tbp, utbp, vtbp, wtbp of histt (crosst.f90:2151-2160)
+        double tx = (double)tb00, ty = 0.0;
+        if (!(i == 0 && k == 0)) {
+          const V t = tbv[k * nkx + i];
+          tx = (double)t.x;
+          ty = (double)t.y;
+        }
+        acc[11] += w * (tx * tx + ty * ty);
+        acc[12] += w * (u1.x * tx + u1.y * ty);
+        acc[13] += w * (u2.x * tx + u2.y * ty);
+        acc[14] += w * (u3.x * tx + u3.y * ty);
+      }
     }
     // block reduction (deterministic: fixed tree)
     __shared__ double red[SB_NHIST_Q][T / 32];
@@ -171,6 +188,22 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
   }
   V *zb = (V *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * g.nzf * nkx;
   const V zero = mk2<R>((R)0, (R)0);
+  if (g.temp && round == g.tround) {
+    // the temperature alone: CB sequences
+    for (int idx = threadIdx.x; idx < CB * NZ; idx += T) A[idx] = zero;
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < CB * mz; idx += T) {
+      const int ci = idx % CB, k = idx / CB, i = i0 + ci;
+      if (i >= nkx) continue;
+      A[ci * NZ + kgrid(k, nz, NZ, mz)] = (i == 0 && k == 0) ? mk2<R>(tb00, (R)0) : tbv[k * nkx + i];
+    }
+    V *res = fft_batch<NZ, +1, CB, T>(A, Bs, (const V *)tw_of<R>(bf, true));
+    for (int idx = threadIdx.x; idx < CB * NZ; idx += T) {
+      const int ci = idx % CB, z = idx / CB, i = i0 + ci;
+      if (i < nkx) zb[((long)z * g.nzf + g.tzf) * nkx + i] = res[ci * NZ + z];
+    }
+    return;
+  }
   {
     // fill two fields (zero the 2/3-rule gap) on the padded z grid
     for (int idx = threadIdx.x; idx < 2 * CB * NZ; idx += T) A[idx] = zero;
@@ -260,26 +293,30 @@ __device__ __forceinline__ unsigned long long dbits(double v) {
   return (unsigned long long)__double_as_longlong(fabs(v));
 }
 
-template <typename R, int NX, int T>
+// NF = 6 fields to physical x, or 7 with the temperature (then 6 products:
+// u x omega and the fluxes uT, wT, vT of crosst.f90:1680-1693)
+template <typename R, int NX, int T, int NF>
 __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
   typedef typename Vec2<R>::t V;
+  constexpr int NO = (NF == 7) ? 6 : 3;
   const int zp = blockIdx.x, j = blockIdx.y, b = blockIdx.z;
   Member &M = bf.mem[b];
   if (M.halted) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  V *A = (V *)smem_raw, *Bs = A + 6 * NX;
+  V *A = (V *)smem_raw, *Bs = A + NF * NX;
   const int nkx = g.nkx, NZ = g.mgalz;
   const int z = 2 * zp;
   const V *zb = (const V *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * g.nzf * nkx;
   // Hermitian extension of two rows into one complex sequence (c2r of both rows
   // at once); FFTW's c2r ignores the imaginary part of the kx = 0 entry
   const V zero = mk2<R>((R)0, (R)0);
-  for (int idx = threadIdx.x; idx < 6 * NX; idx += T) A[idx] = zero;
+  for (int idx = threadIdx.x; idx < NF * NX; idx += T) A[idx] = zero;
   __syncthreads();
-  for (int idx = threadIdx.x; idx < 6 * nkx; idx += T) {
+  for (int idx = threadIdx.x; idx < NF * nkx; idx += T) {
     const int f = idx / nkx, i = idx - f * nkx;
-    V X1 = zb[((long)z * g.nzf + f) * nkx + i];
-    V X2 = zb[((long)(z + 1) * g.nzf + f) * nkx + i];
+    const int zf = (f < 6) ? f : g.tzf;
+    V X1 = zb[((long)z * g.nzf + zf) * nkx + i];
+    V X2 = zb[((long)(z + 1) * g.nzf + zf) * nkx + i];
     if (i == 0) {
       X1.y = (R)0;
       X2.y = (R)0;
@@ -287,12 +324,12 @@ __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
     A[f * NX + i] = mk2<R>(X1.x - X2.y, X1.y + X2.x);
     if (i > 0) A[f * NX + NX - i] = mk2<R>(X1.x + X2.y, -X1.y + X2.x);
   }
-  V *P = fft_batch<NX, +1, 6, T>(A, Bs, (const V *)tw_of<R>(bf, false));
+  V *P = fft_batch<NX, +1, NF, T>(A, Bs, (const V *)tw_of<R>(bf, false));
   V *Q = (P == A) ? Bs : A;
-  // fields: 0 u, 1 w, 2 omega_x, 3 omega_z, 4 v, 5 omega_y
+  // fields: 0 u, 1 w, 2 omega_x, 3 omega_z, 4 v, 5 omega_y (, 6 tb)
   const R chi2 = (R)(2.0 * g.chi);
   const R sy = (R)(g.s * ((double)j * g.dy - 0.5 * g.Ly));
-  R m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+  R m0 = 0, m1 = 0, m2 = 0, m3 = 0, mt = 0;
   for (int x = threadIdx.x; x < NX; x += T) {
     const V u1 = P[0 * NX + x], u3 = P[1 * NX + x], o1 = P[2 * NX + x], o3 = P[3 * NX + x],
             u2 = P[4 * NX + x], o2 = P[5 * NX + x];
@@ -312,6 +349,13 @@ __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
     Q[0 * NX + x] = h1;
     Q[1 * NX + x] = h2;
     Q[2 * NX + x] = h3;
+    if (NF == 7) {
+      const V tb = P[6 * NX + x];
+      if (rk == 1) mt = fmax(mt, fmax(fabs(tb.x), fabs(tb.y)));
+      Q[3 * NX + x] = mk2<R>(u1.x * tb.x, u1.y * tb.y);
+      Q[4 * NX + x] = mk2<R>(u3.x * tb.x, u3.y * tb.y);
+      Q[5 * NX + x] = mk2<R>(u2.x * tb.x, u2.y * tb.y);
+    }
   }
   if (rk == 1) {
     unsigned long long b0 = dbits(m0), b1 = dbits(m1), b2 = dbits(m2), b3 = dbits(m3);
@@ -327,43 +371,49 @@ __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
       atomicMax(&M.umax_bits[2], b2);
       atomicMax(&M.umax_bits[3], b3);
     }
+    if (NF == 7) {
+      unsigned long long bt = dbits(mt);
+      for (int o = 16; o > 0; o >>= 1) bt = max(bt, __shfl_xor_sync(0xffffffffu, bt, o));
+      if ((threadIdx.x & 31) == 0) atomicMax(&M.tbmax_bits, bt);
+    }
   }
-  V *Rr = fft_batch<NX, -1, 3, T>(Q, P, (const V *)tw_of<R>(bf, false));
-  V *xb = (V *)bf.xbuf + ((long)b * g.my + j) * (long)NZ * 3 * nkx;
+  V *Rr = fft_batch<NX, -1, NO, T>(Q, P, (const V *)tw_of<R>(bf, false));
+  V *xb = (V *)bf.xbuf + ((long)b * g.my + j) * (long)NZ * NO * nkx;
   const R half = (R)0.5;
-  for (int idx = threadIdx.x; idx < 3 * nkx; idx += T) {
+  for (int idx = threadIdx.x; idx < NO * nkx; idx += T) {
     const int f = idx / nkx, i = idx - f * nkx;
     const V zk = Rr[f * NX + i];
     V zm = Rr[f * NX + ((NX - i) % NX)];
     zm.y = -zm.y;
     const R sx = zk.x + zm.x, syy = zk.y + zm.y, dx = zk.x - zm.x, dy = zk.y - zm.y;
-    xb[((long)z * 3 + f) * nkx + i] = mk2<R>(half * sx, half * syy);
-    xb[((long)(z + 1) * 3 + f) * nkx + i] = mk2<R>(half * dy, -half * dx);
+    xb[((long)z * NO + f) * nkx + i] = mk2<R>(half * sx, half * syy);
+    xb[((long)(z + 1) * NO + f) * nkx + i] = mk2<R>(half * dy, -half * dx);
   }
 }
 
 // ---------------------------------------------------------------------------
 // plane stage 3: forward z-transforms, truncation and right-hand sides
 // ---------------------------------------------------------------------------
-template <typename R, int NZ, int CB, int T>
+// NF = 3 nonlinear terms, or 6 with the temperature fluxes
+template <typename R, int NZ, int CB, int T, int NF>
 __global__ void __launch_bounds__(T) k_p3(Grid g, Bufs bf) {
   typedef typename Vec2<R>::t V;
   const int cb = blockIdx.x, j = blockIdx.y, b = blockIdx.z;
   Member &M = bf.mem[b];
   if (M.halted) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  V *A = (V *)smem_raw, *Bs = A + 3 * CB * NZ;
+  V *A = (V *)smem_raw, *Bs = A + NF * CB * NZ;
   const int nkx = g.nkx, mz = g.mz, nz = g.nz;
   const int i0 = cb * CB;
-  const V *xb = (const V *)bf.xbuf + ((long)b * g.my + j) * (long)NZ * 3 * nkx;
+  const V *xb = (const V *)bf.xbuf + ((long)b * g.my + j) * (long)NZ * NF * nkx;
   const V zero = mk2<R>((R)0, (R)0);
-  for (int idx = threadIdx.x; idx < 3 * CB * NZ; idx += T) {
+  for (int idx = threadIdx.x; idx < NF * CB * NZ; idx += T) {
     const int ci = idx % CB, rem = idx / CB;
-    const int f = rem % 3, z = rem / 3;
+    const int f = rem % NF, z = rem / NF;
     const int i = i0 + ci;
-    A[(f * CB + ci) * NZ + z] = (i < nkx) ? xb[((long)z * 3 + f) * nkx + i] : zero;
+    A[(f * CB + ci) * NZ + z] = (i < nkx) ? xb[((long)z * NF + f) * nkx + i] : zero;
   }
-  V *P = fft_batch<NZ, -1, 3 * CB, T>(A, Bs, (const V *)tw_of<R>(bf, true));
+  V *P = fft_batch<NZ, -1, NF * CB, T>(A, Bs, (const V *)tw_of<R>(bf, true));
   const long pbase = (long)b * g.field + (long)j * g.plane;
   V *Dv = (V *)((R *)bf.D + pbase);
   V *Gv = (V *)((R *)bf.G + pbase);
@@ -385,6 +435,19 @@ __global__ void __launch_bounds__(T) k_p3(Grid g, Bufs bf) {
     const R Kk = a * a + gz * gz;
     const long q = (long)k * nkx + i;
     const V v = Gv[q];
+    if (NF == 6) {
+      // ht = -i a uT - i gz wT - bym v with the input v, and -vT
+      // (crosst.f90:1148-1152,1691-1692)
+      V uT = P[(3 * CB + ci) * NZ + kg], wT = P[(4 * CB + ci) * NZ + kg],
+        vT = P[(5 * CB + ci) * NZ + kg];
+      uT.x *= norm; uT.y *= norm;
+      wT.x *= norm; wT.y *= norm;
+      vT.x *= norm; vT.y *= norm;
+      const R bym = (R)g.bym;
+      const R tx = a * uT.y + gz * wT.y, ty = -(a * uT.x) - gz * wT.x;
+      ((V *)((R *)bf.Ht + pbase))[q] = mk2<R>(tx - bym * v.x, ty - bym * v.y);
+      ((V *)((R *)bf.R2 + pbase))[q] = mk2<R>(-vT.x, -vT.y);
+    }
     // dvordy = i a H1 + i gz H3
     R tx = a * H1.x + gz * H3.x, ty = a * H1.y + gz * H3.y;
     Dv[q] = mk2<R>(-ty, tx);
@@ -874,21 +937,36 @@ __global__ void k_plane_to_pencil(Grid g, const R *__restrict__ src, double *__r
 // ---------------------------------------------------------------------------
 // launch helpers
 // ---------------------------------------------------------------------------
+static const size_t kMaxSmem = 227 * 1024;  // opt-in shared memory per block
+
+// whether plane stage 3 with cb kx columns fits in shared memory (the
+// temperature doubles its transforms)
+bool plane3_fits(const Grid &g, int cb) {
+  const size_t v = g.prec ? 8 : 16;
+  return v * 2 * ((g.temp ? 6 : 3) * (size_t)cb * g.mgalz) <= kMaxSmem;
+}
+
 template <typename R, int NZ, int CB, int T, int T3>
 static cudaError_t launch_p13(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, int which,
                               bool prep) {
   typedef typename Vec2<R>::t V;
   const size_t sm1 = sizeof(V) * 2 * (2 * CB * NZ);
-  const size_t sm3 = sizeof(V) * 2 * (3 * CB * NZ);
+  const size_t sm3 = sizeof(V) * 2 * (3 * CB * NZ), sm3t = 2 * sm3;
   if (prep) {
     cudaFuncSetAttribute(k_p1<R, NZ, CB, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
-    cudaFuncSetAttribute(k_p3<R, NZ, CB, T3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+    cudaFuncSetAttribute(k_p3<R, NZ, CB, T3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+    if (sm3t <= kMaxSmem)
+      cudaFuncSetAttribute(k_p3<R, NZ, CB, T3, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3t);
     return cudaGetLastError();
   }
+  // stage-1 rounds: 3 field pairs, 2 more with LES, the temperature alone
+  const int rounds = 3 + (g.les ? 2 : 0) + (g.temp ? 1 : 0);
   if (which == 1)
-    k_p1<R, NZ, CB, T><<<dim3(g.ncb * (g.les ? 5 : 3), g.my, g.B), T, sm1, st>>>(g, bf, rk);
+    k_p1<R, NZ, CB, T><<<dim3(g.ncb * rounds, g.my, g.B), T, sm1, st>>>(g, bf, rk);
+  else if (g.temp)
+    k_p3<R, NZ, CB, T3, 6><<<dim3(g.ncb3, g.my, g.B), T3, sm3t, st>>>(g, bf);
   else
-    k_p3<R, NZ, CB, T3><<<dim3(g.ncb3, g.my, g.B), T3, sm3, st>>>(g, bf);
+    k_p3<R, NZ, CB, T3, 3><<<dim3(g.ncb3, g.my, g.B), T3, sm3, st>>>(g, bf);
   return cudaGetLastError();
 }
 
@@ -909,12 +987,16 @@ template <typename R, int NX, int T>
 static cudaError_t launch_p2(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, bool prep) {
   typedef typename Vec2<R>::t V;
   dim3 grid(g.mgalz / 2, g.my, g.B);
-  const size_t sm = sizeof(V) * 2 * (6 * NX);
+  const size_t sm = sizeof(V) * 2 * (6 * NX), smt = sizeof(V) * 2 * (7 * NX);
   if (prep) {
-    cudaFuncSetAttribute(k_p2<R, NX, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaFuncSetAttribute(k_p2<R, NX, T, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaFuncSetAttribute(k_p2<R, NX, T, 7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
     return cudaGetLastError();
   }
-  k_p2<R, NX, T><<<grid, T, sm, st>>>(g, bf, rk);
+  if (g.temp)
+    k_p2<R, NX, T, 7><<<grid, T, smt, st>>>(g, bf, rk);
+  else
+    k_p2<R, NX, T, 6><<<grid, T, sm, st>>>(g, bf, rk);
   return cudaGetLastError();
 }
 

@@ -9,6 +9,7 @@
 namespace sb {
 int plane_cb(int mgalz);
 int plane_t2_default(int mgalx);
+bool plane3_fits(const Grid &g, int cb);
 bool supported_grid(int mgalx, int mgalz);
 cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st);
 int les_cb(int mgalz);

@@ -98,25 +98,30 @@ __device__ __forceinline__ void store_col(const double *ys, int ystr, R *__restr
 // point.  x = d2f/dy2 in the shared buffer (FP64); rhs = the nonlinear
 // right-hand side (minus `sub` if given); f, fwk the field and its RK work
 // array.  The RK arithmetic runs in the storage precision R; the viscous term
-// and the remaps (phase factors) in FP64.
+// and the remaps (phase factors) in FP64.  With `lap` the viscous term is
+// nuv * lap (a Laplacian computed before) instead of nuv (x - k2 f); `buo`
+// adds gb * buo (the buoyancy of the phi equation, crosst.f90:737).
 template <typename R>
 __device__ __forceinline__ void rk_update(const double *ys, int ystr, const R *__restrict__ rhs,
                                           const R *__restrict__ sub, R *__restrict__ f,
                                           R *__restrict__ fwk, long ps, const LineThread &L,
                                           int rk, double nuv, double k2, double Dt,
                                           const double *__restrict__ mf1,
-                                          const double *__restrict__ mf2, long mfs) {
+                                          const double *__restrict__ mf2, long mfs,
+                                          const R *__restrict__ lap = nullptr,
+                                          const R *__restrict__ buo = nullptr, double gb = 0.0) {
   const R gk = (R)kGama[rk], zk = (R)kZeta[rk], dtr = (R)Dt;
   const int c = L.c;
 #pragma unroll 2
   for (int i = L.r0; i <= L.r1; i++) {
     const int j = i - 1;
     const long q = (long)j * ps;
-    const double x = ys[(i - L.r0) * ystr];
     const R fo = f[q];
     R h = rhs[q];
     if (sub) h = h - sub[q];
-    h = h + (R)(nuv * (-(k2 * (double)fo) + x));
+    const double vis = lap ? (double)lap[q] : (-(k2 * (double)fo) + ys[(i - L.r0) * ystr]);
+    h = h + (R)(nuv * vis);
+    if (buo) h = h + (R)(gb * (double)buo[q]);
     R wk = (rk == 0) ? gk * h : fwk[q] + gk * h;
     const double fn = (double)(fo + dtr * wk);
     const cd m2 = ldc2(mf2 + (long)j * mfs);
@@ -141,7 +146,7 @@ template <typename R>
 __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs bf, int rk1) {
   __shared__ double xch[kSeg][16][2][SB_XS];
   LineThread L;
-  if (!line_thread(g, 3, &L)) return;  // whole blocks
+  if (!line_thread(g, g.temp ? 5 : 3, &L)) return;  // whole blocks
   Member &M = bf.mem[L.b];
   if (M.halted) return;  // uniform per block
   const int N = g.my, ystr = blockDim.x;
@@ -157,9 +162,43 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs 
     R *mwk = (R *)bf.mwk + (long)L.b * 2 * N + L.c;
     const R *mrf = (const R *)bf.mrf + (long)L.b * 2 * N + L.c;
     const cd one = mk(1.0, 0.0);
+    // with the temperature, line slot 1 carries tb00: rf0tb = d(-vT_00)/dy
+    // (crosst.f90:642-645) from the (0,0) line of -vT, kept in mtr; slot 0
+    // computes a d/dy of the mean that is not used
+    const bool ts = g.temp && L.l == 1;
+    if (g.temp) {
+      const Tail T1 = load_tail(bf.tl1o + (long)L.b * g.nkx * SB_TAIL);
+      const R *src = ts ? (const R *)bf.R2 + (long)L.b * g.field + L.c : (const R *)mu;
+      SEG_SOLVE(src, ts ? g.plane : 2L, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6],
+                true);
+      if (ts && L.c == 0) {
+        R *mtr = (R *)bf.mtr + (long)L.b * 2 * N;
+        for (int i = L.r0; i <= L.r1; i++) mtr[2 * (i - 1)] = (R)ys[(i - L.r0) * ystr];
+      }
+    }
     const Tail T2 = load_tail(bf.tl2o + (long)L.b * g.nkx * SB_TAIL);
-    SEG_SOLVE(mu, 2, V2, W2, T2, one, one, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6], false);
+    R *mline = ts ? (R *)bf.mt + (long)L.b * 2 * N + L.c : mu;
+    SEG_SOLVE(mline, 2, V2, W2, T2, one, one, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6], false);
     const R gk = (R)kGama[rk], zk = (R)kZeta[rk];
+    if (ts) {
+      // visc3d(tb00, rf0tb, rk=0, fkappa) and the RK3 update of tb00
+      // (crosst.f90:751-754,797-826,877-880)
+      if (L.c == 0) {
+        R *mt = mline, *mtwk = (R *)bf.mtwk + (long)L.b * 2 * N;
+        const R *mtr = (const R *)bf.mtr + (long)L.b * 2 * N;
+        for (int i = L.r0; i <= L.r1; i++) {
+          const int j = i - 1;
+          const R rf = mtr[2 * j] +
+                       (R)(g.kappa * (-(0.0 * (double)mt[2 * j]) + ys[(i - L.r0) * ystr]));
+          R wk = (rk == 0) ? gk * rf : mtwk[2 * j] + gk * rf;
+          const R tn = mt[2 * j] + (R)Dt * wk;
+          if (rk < 2) wk = rf * zk;
+          mt[2 * j] = tn;
+          mtwk[2 * j] = wk;
+        }
+      }
+      return;
+    }
     for (int i = L.r0; i <= L.r1; i++) {
       const int j = i - 1;
       const R rf = mrf[2 * j] + (R)(nu * (-(0.0 * (double)mu[2 * j]) + ys[(i - L.r0) * ystr]));
@@ -178,12 +217,27 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs 
   const int i = L.i, k = L.k;
   const cd shp = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * i);
   const cd shm = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
-  if (L.role == 0) {
-    // d/dy (dH1/dx + dH3/dz) (cross.f90:565-575)
+  const double a = g.alp * i;
+  const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
+  if (L.role == 0 || L.role == 4) {
     const Tail T1 = load_tail(bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL);
-    SEG_SOLVE((const R *)bf.D + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5], g.rh1[6],
-              true);
-    store_col(ys, ystr, (R *)bf.T + off, ps, L);
+    if (L.role == 0) {
+      // d/dy (dH1/dx + dH3/dz) (cross.f90:565-575)
+      SEG_SOLVE((const R *)bf.D + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
+                g.rh1[6], true);
+      store_col(ys, ystr, (R *)bf.T + off, ps, L);
+      return;
+    }
+    // temperature: ht += d(-vT)/dy (crosst.f90:633-636,677)
+    SEG_SOLVE((const R *)bf.R2 + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
+              g.rh1[6], true);
+    if (L.active) {
+      R *ht = (R *)bf.Ht + off;
+      for (int r = L.r0; r <= L.r1; r++) {
+        const long q = (long)(r - 1) * ps;
+        ht[q] = ht[q] + (R)ys[(r - L.r0) * ystr];
+      }
+    }
     return;
   }
   const Tail T2 = load_tail(bf.tl2o + ((long)L.b * g.nkx + i) * SB_TAIL);
@@ -192,6 +246,22 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs 
     SEG_SOLVE((const R *)bf.phi + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
               g.rh2[6], false);
     store_col(ys, ystr, (R *)bf.S + off, ps, L);
+    return;
+  }
+  if (L.role == 3) {
+    // temperature: lap(tb) = d2(tb)/dy2 - k^2 tb, shared by the thermal
+    // diffusion and the buoyancy term (visc3d, crosst.f90:734-738)
+    SEG_SOLVE((const R *)bf.tb + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
+              g.rh2[6], false);
+    if (L.active) {
+      const R *tb = (const R *)bf.tb + off;
+      R *lt = (R *)bf.Lt + off;
+      const double k2 = a * a + gz * gz;
+      for (int r = L.r0; r <= L.r1; r++) {
+        const long q = (long)(r - 1) * ps;
+        lt[q] = (R)(-(k2 * (double)tb[q]) + ys[(r - L.r0) * ystr]);
+      }
+    }
     return;
   }
   // role 1: hg += nu*lap(omega_y) (visc3d, cross.f90:659), RK3 update, remaps.
@@ -205,8 +275,6 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs 
     for (int r = L.r0; r <= L.r1; r++) ys[(r - L.r0) * ystr] = (double)lv[(long)(r - 1) * ps];
   }
   const bool is00 = (i == 0 && k == 0);
-  const double a = g.alp * i;
-  const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
   const double *mf1 = bf.mf1 + (long)L.b * 2 * N * g.nkx + 2 * i;
   const double *mf2 = bf.mf2 + (long)L.b * 2 * N * g.nkx + 2 * i;
   rk_update<R>(ys, ystr, (const R *)bf.G + off, nullptr, (R *)bf.vor + off, (R *)bf.vorwk + off,
@@ -217,7 +285,7 @@ template <typename R>
 __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs bf, int mode) {
   __shared__ double xch[kSeg][16][2][SB_XS];
   LineThread L;
-  if (!line_thread(g, 2, &L)) return;
+  if (!line_thread(g, g.temp ? 3 : 2, &L)) return;
   Member &M = bf.mem[L.b];
   if (M.halted) return;
   const int N = g.my, ystr = blockDim.x;
@@ -263,9 +331,23 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs 
     return;
   }
   const bool is00 = (i == 0 && k == 0);
+  if (L.role == 2) {
+    // temperature: ht + fkappa lap(tb), RK3 update of tb, zeta store and
+    // moving_frame_t remaps (crosst.f90:677,734-735,782-872); nothing in the
+    // prologue
+    if (mode >= 1) {
+      const double *mf1 = bf.mf1 + (long)L.b * 2 * N * g.nkx + 2 * i;
+      const double *mf2 = bf.mf2 + (long)L.b * 2 * N * g.nkx + 2 * i;
+      rk_update<R>(ys, ystr, (const R *)bf.Ht + off, nullptr, (R *)bf.tb + off,
+                   (R *)bf.tbwk + off, ps, L, mode - 1, is00 ? 0.0 : g.kappa, 0.0, M.Deltat, mf1,
+                   mf2, 2 * g.nkx, (const R *)bf.Lt + off);
+    }
+    return;
+  }
   if (mode >= 1) {
     // hv = hv - d/dy(dH1/dx + dH3/dz) + nu*lap(phi), RK3 update, remaps
-    // (cross.f90:607,660,694-781)
+    // (cross.f90:607,660,694-781); with the temperature + gbeta lap(tb)
+    // (crosst.f90:737)
     const int rk = mode - 1;
     const double a = g.alp * i;
     const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
@@ -276,7 +358,8 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs 
     for (int r = L.r0; r <= L.r1; r++) ys[(r - L.r0) * ystr] = (double)S[(long)(r - 1) * ps];
     rk_update<R>(ys, ystr, (const R *)bf.V + off, (const R *)bf.T + off, (R *)bf.phi + off,
                  (R *)bf.phiwk + off, ps, L, rk, is00 ? 0.0 : M.nu, a * a + gz * gz, M.Deltat,
-                 mf1, mf2, 2 * g.nkx);
+                 mf1, mf2, 2 * g.nkx, nullptr,
+                 (g.temp && !is00) ? (const R *)bf.Lt + off : nullptr, g.gbeta);
     __syncthreads();  // the whole updated line is read below
   }
   // v = lapcdy(phi) (cross.f90:784-795, first step: 408-426); hg(0,0) keeps
@@ -493,6 +576,11 @@ __global__ void k_setconj(Grid g, Bufs bf) {
     const R v = vor[src], p = phi[src];
     vor[dst] = c ? -v : v;
     phi[dst] = c ? -p : p;
+    if (g.temp) {  // set_conj_t (crosst.f90:333-337)
+      R *tb = (R *)bf.tb;
+      const R t = tb[src];
+      tb[dst] = c ? -t : t;
+    }
   }
 }
 
@@ -519,6 +607,7 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
       M.flags = 0;
       for (int q = 0; q < 4; q++) M.umax_bits[q] = 0ull;
       M.nut_bits = 0ull;
+      M.tbmax_bits = 0ull;
       M.xwb[0] = M.xoffb;
       M.xwt[0] = M.xofft;
     }
@@ -586,6 +675,8 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
       const double v = __longlong_as_double((long long)M.umax_bits[q]);
       M.umax[q] = v > uinit ? v : uinit;
     }
+    // max |tb| of the step (crosst.f90:1443-1445,1674-1676,1864-1867)
+    if (g.temp) M.tbmax = __longlong_as_double((long long)M.tbmax_bits);
     if (g.les) {
       // running maximum of |nu_t| (cross.f90:1430-1436, 1604)
       const double v = __longlong_as_double((long long)M.nut_bits);
@@ -615,7 +706,14 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
       }
       M.CFLcur = M.CFL;
       M.CFLv = M.CFL * M.cflvv * dt;
-      if (M.CFLv > M.CFL) dt = 1.0 / M.cflvv;
+      if (g.temp) {
+        // the thermal-diffusion limit enters only where the viscous one
+        // does (crosst.f90:1236-1257)
+        const double CFLk = M.CFL * M.cflkk * dt;
+        if (M.CFLv > M.CFL) dt = (CFLk > M.CFLv) ? 1.0 / M.cflkk : 1.0 / M.cflvv;
+      } else if (M.CFLv > M.CFL) {
+        dt = 1.0 / M.cflvv;
+      }
     }
     double Deltat = dt;
     if (Deltat < 1e-10) {
@@ -648,7 +746,7 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
       uner2[2] = g.les ? s_q[SB_NHIST_Q + 1] / my : 0.0;
       uner2[3] = g.les ? s_q[SB_NHIST_Q + 2] / my : 0.0;
       if (M.ntrace < M.trace_cap) {
-        double *rec = bf.trace + ((long)b * M.trace_cap + M.ntrace) * SB_TRACE_LEN;
+        double *rec = bf.trace + ((long)b * M.trace_cap + M.ntrace) * g.tlen;
         rec[0] = M.time;
         rec[1] = M.Deltat;
         for (int q = 0; q < 10; q++) rec[2 + q] = uner[q];
@@ -661,6 +759,12 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
         rec[18] = M.xofft;
         rec[19] = M.umax[0];
         for (int q = 0; q < 4; q++) rec[20 + q] = uner2[q];
+        if (g.temp) {
+          // tbmax, tner(1:4) of histt 'w' (crosst.f90:2446-2458)
+          rec[24] = M.tbmax;
+          rec[25] = sqrt(fabs(s_q[11] / my));
+          for (int q = 1; q < 4; q++) rec[25 + q] = s_q[11 + q] / my;
+        }
       }
       M.ntrace++;
       if (isnan(uner[0])) {
@@ -766,10 +870,13 @@ __global__ void k_finish(Grid g, Bufs bf) {
   M.xwt[0] = M.xofft;
   M.time = M.time + M.Deltat;
   M.istep += 1;
-  if ((M.istep - 1) != 1 && M.istop) M.halted = 1;
+  // cross checks the stop flag from its third step on (cross.f90:221),
+  // crosst from its second (crosst.f90:259)
+  if ((g.temp || (M.istep - 1) != 1) && M.istop) M.halted = 1;
   if ((M.istep - 1) % M.nhist == 0) M.ihist = 1;
   for (int q = 0; q < 4; q++) M.umax_bits[q] = 0ull;
   M.nut_bits = 0ull;
+  M.tbmax_bits = 0ull;
 }
 
 // ---------------------------------------------------------------------------
@@ -802,7 +909,7 @@ cudaError_t prepare_line(const Grid &g) {
 int line_segments() { return kSeg; }
 
 cudaError_t launch_lineA(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
-  const unsigned nb = (unsigned)(g.B * (3 * g.ngrp + 1));
+  const unsigned nb = (unsigned)(g.B * ((g.temp ? 5 : 3) * g.ngrp + 1));
   if (g.prec)
     k_lineA<float><<<nb, kLineT, line_smem(g), st>>>(g, bf, rk);
   else
@@ -811,7 +918,7 @@ cudaError_t launch_lineA(const Grid &g, const Bufs &bf, int rk, cudaStream_t st)
 }
 
 cudaError_t launch_lineB(const Grid &g, const Bufs &bf, int mode, cudaStream_t st) {
-  const unsigned nb = (unsigned)(g.B * (2 * g.ngrp + 1));
+  const unsigned nb = (unsigned)(g.B * ((g.temp ? 3 : 2) * g.ngrp + 1));
   if (g.prec)
     k_lineB<float><<<nb, kLineT, line_smem(g), st>>>(g, bf, mode);
   else

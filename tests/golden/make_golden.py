@@ -5,7 +5,7 @@ log_changes rev.428-430), so these fixtures are produced by the oracle, whose
 building blocks are pinned by tests/test_oracle.py.  Inputs are not stored:
 they come from the seeded generator sb_seed_state (seed, grid below).
 
-usage: python tests/golden/make_golden.py
+usage: python tests/golden/make_golden.py [case ...]   (all cases without names)
 """
 import os
 import sys
@@ -36,20 +36,28 @@ CASES = {
     "ydeal64_seed6": dict(params=dict(mgalx=64, my=32, mgalz=32, Re=4000.0 / LZ ** 2, alp=0.5,
                                       Ly=LZ, gam=1.0, s=1.0, chi=0.0, CFL=0.5, ydeal=1),
                           seed=6, nstep=3),
+    # crosst: the scalar at Pr = 0.7 with a mean gradient and buoyancy, CFL steps
+    "temp64_seed7": dict(params=dict(mgalx=64, my=32, mgalz=32, Re=4000.0 / LZ ** 2, alp=0.5,
+                                     Ly=LZ, gam=1.0, s=1.0, chi=0.0, CFL=0.5, temperature=1,
+                                     fkappa=LZ ** 2 / 4000.0 / 0.7, bym=1.0, gbeta=0.5),
+                         seed=7, nstep=3),
 }
 
 
-def main():
+def main(names):
     for name, c in CASES.items():
+        if names and name not in names:
+            continue
         st = sb.seed_state(sb.make_params(**c["params"]), c["seed"])
         o = oracle.Oracle(**c["params"])
         tr, istop = o.cross(st, c["nstep"])
+        extra = {"tb": st["tb"], "tb00": st["tb00"]} if "tb" in st else {}
         np.savez_compressed(os.path.join(HERE, name + ".npz"), vor=st["vor"], phi=st["phi"],
                             u00=st["u00"], w00=st["w00"], time=st["time"], xoffb=st["xoffb"],
                             xofft=st["xofft"], trace=tr, seed=c["seed"], nstep=c["nstep"],
-                            **{"p_" + k: v for k, v in c["params"].items()})
+                            **extra, **{"p_" + k: v for k, v in c["params"].items()})
         print(name, "written")
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

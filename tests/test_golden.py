@@ -7,8 +7,8 @@ import pytest
 
 from conftest import ROOT, rel_l2
 
-CASES = ["step64_seed3", "les64_seed5", "filt64_seed4", "ydeal64_seed6"]
-INTS = ("mgalx", "my", "mgalz", "les", "les_visc", "ydeal")
+CASES = ["step64_seed3", "les64_seed5", "filt64_seed4", "ydeal64_seed6", "temp64_seed7"]
+INTS = ("mgalx", "my", "mgalz", "les", "les_visc", "ydeal", "temperature")
 
 
 def _case(name):
@@ -20,6 +20,10 @@ def _case(name):
     return g, params
 
 
+def _keys(g):
+    return ("vor", "phi", "u00", "w00") + (("tb", "tb00") if "tb" in g.files else ())
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_oracle_reproduces_golden(name):
     import oracle
@@ -27,7 +31,7 @@ def test_oracle_reproduces_golden(name):
     g, params = _case(name)
     st = sb.seed_state(sb.make_params(**params), int(g["seed"]))
     tr, _ = oracle.Oracle(**params).cross(st, int(g["nstep"]))
-    for k in ("vor", "phi", "u00", "w00"):
+    for k in _keys(g):
         assert rel_l2(st[k], g[k]) < 1e-13, k
     np.testing.assert_allclose(tr, g["trace"], rtol=1e-12, atol=0)
 
@@ -41,7 +45,7 @@ def test_gpu_reproduces_golden(name):
     st = sb.seed_state(p, int(g["seed"]))
     box = sb.ShearBox(p)
     tr, status = box.cross(st, int(g["nstep"]))
-    for k in ("vor", "phi", "u00", "w00"):
+    for k in _keys(g):
         assert rel_l2(st[k], g[k]) < 1e-12, k
     np.testing.assert_allclose(tr, g["trace"], rtol=1e-10, atol=1e-300)
     assert st["time"] == pytest.approx(float(g["time"]), abs=1e-15)
