@@ -13,6 +13,8 @@ step (three substeps) of that box.
          FP64 rate against the FP64 FMA peak measured in the same run (the
          binding roof on GB300) and bytes against the measured HBM copy peak.
   les     Smagorinsky LES on 384x192x192 (Re_z=20000), FP32-mixed vs FP64.
+  temperature  the crosst variant (Boussinesq scalar, Pr=0.7) on the benchmark
+         box, FP64 and FP32-mixed, against the plain step.
   newton  batched Newton Jv/s: 32 finite-difference products on 96x48x48
          (Re_z=1200, T=20/S) as one FP32-mixed batch (central differences)
          vs one FP64 product at a time.
@@ -301,6 +303,46 @@ def les_leg(sb, torch, dist, ws, rank, args):
     return out
 
 
+def temperature_leg(sb, torch, dist, ws, rank, args, plain_steps_per_s):
+    """crosst: the benchmark box with the scalar (Pr = 0.7, bym = 1,
+    gbeta = 0.5), args.steps steps with the state in HBM, FP64 and FP32-mixed
+    (CUDA events); the cost against the plain FP64 step and the mixed run's
+    deviation of tb from FP64 after those steps."""
+    pp = dict(box_params(), temperature=1, fkappa=LZ ** 2 / REZ / 0.7, bym=1.0, gbeta=0.5)
+    p = sb.make_params(**pp)
+    st0 = sb.seed_state(p, 7 + rank)
+    n = args.steps
+    out = {"pr": 0.7, "bym": 1.0, "gbeta": 0.5, "steps": n}
+    finals = {}
+    for key, prec in (("fp64", sb.SB_FP64), ("mixed", sb.SB_MIXED)):
+        box = sb.ShearBox(p, precision=prec)
+        box.set_state(st0)
+        tuning = box.autotune()
+        box.set_state(st0)
+        box.step(3)
+        box.sync()
+        box.set_state(st0)
+        stream = torch.cuda.ExternalStream(box.stream)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        barrier(dist)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        box.step(n)
+        e1.record(stream)
+        e1.synchronize()
+        ms = allmax(dist, e0.elapsed_time(e1))
+        finals[key] = box.get_state()
+        out[key] = {"value": ws * n / (ms * 1e-3), "unit": "steps/s", "ms_per_step": ms / n,
+                    "tuning": tuning}
+        del box
+    out["fp64"]["cost_vs_plain_fp64"] = plain_steps_per_s / out["fp64"]["value"]
+    out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    a, b = finals["mixed"]["tb"], finals["fp64"]["tb"]
+    out["mixed"]["tb_rel_l2_err_vs_fp64"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    return out
+
+
 def newton_leg(sb, torch, dist, ws, rank, args, nper=32, T=20.0):
     """Batched Newton Jv: the Jacobian-vector products of the periodic-orbit
     search on 96x48x48 (Re_z=1200, period T=20/S) through the Newton tools'
@@ -321,7 +363,8 @@ def newton_leg(sb, torch, dist, ws, rank, args, nper=32, T=20.0):
     x0 = pk.pack(sb.seed_state(p, 77 + rank))
     D = np.random.default_rng(5 + rank).standard_normal((pk.n, nper))
     pm64 = nw.PeriodMap(p, T, batch=1, chunk=256)
-    J64 = nw.Jacobian(pm64, pk, x0, eps_jacobi=1e-7)  # base integration, untimed
+    J64 = nw.Jacobian(pm64, pk, x0, eps_jacobi=1e-7)
+    J64.gx0  # the base integration, untimed
     steps_T = pm64.last_steps[0]
     barrier(dist)
     t0 = time.perf_counter()
@@ -511,6 +554,8 @@ def run_ours(args):
     ensemble = None if args.no_ensemble else ensemble_leg(sb, torch, dist, ws, rank, args)
     newton = None if args.no_newton else newton_leg(sb, torch, dist, ws, rank, args)
     les = None if args.no_les else les_leg(sb, torch, dist, ws, rank, args)
+    temp = (None if args.no_temp else
+            temperature_leg(sb, torch, dist, ws, rank, args, steps_per_s))
     if rank != 0:
         return
     cpu = cpu_baseline(args.cpu_steps, os.cpu_count() or 1) if ws == 1 or rank == 0 else None
@@ -543,6 +588,7 @@ def run_ours(args):
         "ensemble": ensemble,
         "newton": newton,
         "les": les,
+        "temperature": temp,
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "clocks": clk,
     }
@@ -563,6 +609,7 @@ def main():
     ap.add_argument("--no-newton", action="store_true", help="skip the batched Newton Jv leg")
     ap.add_argument("--no-les", action="store_true", help="skip the LES leg")
     ap.add_argument("--les-steps", type=int, default=500, help="steps of the LES leg")
+    ap.add_argument("--no-temp", action="store_true", help="skip the temperature (crosst) leg")
     ap.add_argument("--lite", action="store_true",
                     help="profiling only: time the steps, skip e2e / CPU / per-kernel legs")
     args = ap.parse_args()

@@ -14,8 +14,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libshearbox.so")
-SOURCES = ["sb_kernels.cu", "sb_yline.cu", "sb_ops.cu", "sb_noalloc.cu", "sb_api.cu", "sb_host.cpp",
-           "sb_io.cpp"]
+# (source, extra flags): sb_kernels.cu and sb_yline.cu are compiled twice, their
+# FP64 and FP32-mixed instantiations in parallel
+UNITS = [("sb_kernels.cu", ["-DSB_FLOAT_TU=0"]), ("sb_kernels.cu", ["-DSB_FLOAT_TU=1"]),
+         ("sb_yline.cu", ["-DSB_FLOAT_TU=0"]), ("sb_yline.cu", ["-DSB_FLOAT_TU=1"]),
+         ("sb_ops.cu", []), ("sb_noalloc.cu", []), ("sb_api.cu", []), ("sb_host.cpp", []),
+         ("sb_io.cpp", [])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC"]
 # extra compile flags for tuning builds, e.g. SB_NVCC_EXTRA="-DSB_KSEG=4"
@@ -42,10 +46,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     procs = []
     objs = []
-    for src in SOURCES:
-        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
+    for src, defs in UNITS:
+        tag = "".join(d.split("=")[-1] for d in defs)
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + (f"_{tag}" if tag else "") + ".o")
         objs.append(obj)
-        cmd = [nvcc(), *ARCH, *FLAGS, *EXTRA, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc(), *ARCH, *FLAGS, *EXTRA, *defs, "-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cpp"):
             cmd = [nvcc(), *FLAGS, "-x", "c++", "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:

@@ -28,6 +28,13 @@
 #include "sb_kernels.h"
 #include "sb_line.cuh"
 
+// This file is compiled twice: SB_FLOAT_TU=0 gives the FP64 instantiations
+// and the shared entry points, SB_FLOAT_TU=1 only the FP32-mixed
+// instantiations, so that the two halves compile in parallel.
+#ifndef SB_FLOAT_TU
+#define SB_FLOAT_TU 0
+#endif
+
 namespace sb {
 
 __device__ __forceinline__ cd ldc(const double *p) { return mk(p[0], p[1]); }
@@ -62,7 +69,9 @@ template <> __device__ __forceinline__ float kinv_of<float>(const Bufs &bf, long
 // k index -> position on the padded z grid (fill00)
 __device__ __forceinline__ int kgrid(int k, int nz, int NZ, int mz) { return k <= nz ? k : k + (NZ - mz); }
 
-template <typename R, int NZ, int CB, int T>
+// TEMP: with the temperature round and statistics (a separate instantiation,
+// so that the plain step keeps its register budget)
+template <typename R, int NZ, int CB, int T, bool TEMP>
 __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
   typedef typename Vec2<R>::t V;
   // one block per (kx block, pair of fields): the three (five with LES) pairs
@@ -85,8 +94,8 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
   const V mdu = ((const V *)bf.mdu)[(long)b * g.my + j];
   // temperature: tb as stored (its copy gets no set_conj, crosst.f90:556-559)
   // with the (0,0) mode replaced by tb00 (crosst.f90:1459-1462)
-  const V *tbv = g.temp ? (const V *)((const R *)bf.tb + pbase) : nullptr;
-  const R tb00 = g.temp ? ((const V *)bf.mt)[(long)b * g.my + j].x : (R)0;
+  const V *tbv = TEMP ? (const V *)((const R *)bf.tb + pbase) : nullptr;
+  const R tb00 = TEMP ? ((const V *)bf.mt)[(long)b * g.my + j].x : (R)0;
   // omega_y and phi with the kx=0 conjugate symmetry imposed (set_conj on the
   // copies buff1/buff2, cross.f90:493-502)
   auto ld_sym = [&](const V *p, int i, int k) -> V {
@@ -157,7 +166,7 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
       const double c3x = o3s.x + a * u2.y, c3y = o3s.y - a * u2.x;  // o3 - i a u2
       acc[10] += w * (Kk * (uu + vv + ww) + (dv.x * dv.x + dv.y * dv.y) +
                       (c1x * c1x + c1y * c1y) + (c3x * c3x + c3y * c3y));
-      if (g.temp) {
+      if (TEMP) {
         // tbp, utbp, vtbp, wtbp of histt (crosst.f90:2151-2160)
         double tx = (double)tb00, ty = 0.0;
         if (!(i == 0 && k == 0)) {
@@ -188,7 +197,7 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
   }
   V *zb = (V *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * g.nzf * nkx;
   const V zero = mk2<R>((R)0, (R)0);
-  if (g.temp && round == g.tround) {
+  if (TEMP && round == g.tround) {
     // the temperature alone: CB sequences
     for (int idx = threadIdx.x; idx < CB * NZ; idx += T) A[idx] = zero;
     __syncthreads();
@@ -939,12 +948,24 @@ __global__ void k_plane_to_pencil(Grid g, const R *__restrict__ src, double *__r
 // ---------------------------------------------------------------------------
 static const size_t kMaxSmem = 227 * 1024;  // opt-in shared memory per block
 
+#if !SB_FLOAT_TU
 // whether plane stage 3 with cb kx columns fits in shared memory (the
 // temperature doubles its transforms)
 bool plane3_fits(const Grid &g, int cb) {
   const size_t v = g.prec ? 8 : 16;
   return v * 2 * ((g.temp ? 6 : 3) * (size_t)cb * g.mgalz) <= kMaxSmem;
 }
+int plane_cb(int) { return 8; }
+int plane_t2_default(int mgalx) {
+  switch (mgalx) {
+    case 32: case 48: return 64;
+    case 64: case 96: return 96;
+    case 192: return 128;
+    default: return 256;
+  }
+}
+int les_cb(int mgalz) { return mgalz >= 192 ? 2 : 4; }
+#endif
 
 template <typename R, int NZ, int CB, int T, int T3>
 static cudaError_t launch_p13(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, int which,
@@ -953,7 +974,8 @@ static cudaError_t launch_p13(const Grid &g, const Bufs &bf, int rk, cudaStream_
   const size_t sm1 = sizeof(V) * 2 * (2 * CB * NZ);
   const size_t sm3 = sizeof(V) * 2 * (3 * CB * NZ), sm3t = 2 * sm3;
   if (prep) {
-    cudaFuncSetAttribute(k_p1<R, NZ, CB, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+    cudaFuncSetAttribute(k_p1<R, NZ, CB, T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+    cudaFuncSetAttribute(k_p1<R, NZ, CB, T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
     cudaFuncSetAttribute(k_p3<R, NZ, CB, T3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
     if (sm3t <= kMaxSmem)
       cudaFuncSetAttribute(k_p3<R, NZ, CB, T3, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3t);
@@ -961,8 +983,10 @@ static cudaError_t launch_p13(const Grid &g, const Bufs &bf, int rk, cudaStream_
   }
   // stage-1 rounds: 3 field pairs, 2 more with LES, the temperature alone
   const int rounds = 3 + (g.les ? 2 : 0) + (g.temp ? 1 : 0);
-  if (which == 1)
-    k_p1<R, NZ, CB, T><<<dim3(g.ncb * rounds, g.my, g.B), T, sm1, st>>>(g, bf, rk);
+  if (which == 1 && g.temp)
+    k_p1<R, NZ, CB, T, true><<<dim3(g.ncb * rounds, g.my, g.B), T, sm1, st>>>(g, bf, rk);
+  else if (which == 1)
+    k_p1<R, NZ, CB, T, false><<<dim3(g.ncb * rounds, g.my, g.B), T, sm1, st>>>(g, bf, rk);
   else if (g.temp)
     k_p3<R, NZ, CB, T3, 6><<<dim3(g.ncb3, g.my, g.B), T3, sm3t, st>>>(g, bf);
   else
@@ -1000,8 +1024,6 @@ static cudaError_t launch_p2(const Grid &g, const Bufs &bf, int rk, cudaStream_t
   return cudaGetLastError();
 }
 
-int plane_cb(int) { return 8; }
-
 // plane stage 2 with the tuned block size: T0 threads or 2 T0
 template <typename R, int NX, int T0>
 static cudaError_t launch_p2_t(const Grid &g, const Bufs &bf, int rk, cudaStream_t st, bool prep) {
@@ -1011,15 +1033,6 @@ static cudaError_t launch_p2_t(const Grid &g, const Bufs &bf, int rk, cudaStream
   }
   return g.t2 == 2 * T0 ? launch_p2<R, NX, 2 * T0>(g, bf, rk, st, false)
                         : launch_p2<R, NX, T0>(g, bf, rk, st, false);
-}
-
-int plane_t2_default(int mgalx) {
-  switch (mgalx) {
-    case 32: case 48: return 64;
-    case 64: case 96: return 96;
-    case 192: return 128;
-    default: return 256;
-  }
 }
 
 template <typename R>
@@ -1046,12 +1059,6 @@ static cudaError_t launch_plane_t(const Grid &g, const Bufs &bf, int stage, int 
     case 192: return launch_p13_cb<R, 192>(g, bf, rk, st, stage, prep);
     default: return cudaErrorInvalidValue;
   }
-}
-
-// stage 1..3: launch; stage 0: set the kernels' shared-memory limits (once)
-cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
-  return g.prec ? launch_plane_t<float>(g, bf, stage, rk, st)
-                : launch_plane_t<double>(g, bf, stage, rk, st);
 }
 
 // LES launches: stage 2..5 = k_les2..k_les5 of substep rk; stage 0 sets the
@@ -1091,8 +1098,6 @@ static cudaError_t launch_les_z(const Grid &g, const Bufs &bf, int stage, cudaSt
   return cudaGetLastError();
 }
 
-int les_cb(int mgalz) { return mgalz >= 192 ? 2 : 4; }
-
 template <typename R>
 static cudaError_t launch_les_t(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
   const bool prep = (stage == 0);
@@ -1119,10 +1124,6 @@ static cudaError_t launch_les_t(const Grid &g, const Bufs &bf, int stage, int rk
   }
 }
 
-cudaError_t launch_les(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
-  return g.prec ? launch_les_t<float>(g, bf, stage, rk, st)
-                : launch_les_t<double>(g, bf, stage, rk, st);
-}
 
 // y dealiasing of substep rk: the mean-profile kernel (offsets, frame shift)
 // then the line kernel
@@ -1154,12 +1155,7 @@ static cudaError_t launch_ydeal_r(const Grid &g, const Bufs &bf, int rk, cudaStr
   }
 }
 
-// rk = 1..3: launch; rk = 0: set the kernels' shared-memory limits
-cudaError_t launch_ydeal(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
-  return g.prec ? launch_ydeal_r<float>(g, bf, rk, st, rk == 0)
-                : launch_ydeal_r<double>(g, bf, rk, st, rk == 0);
-}
-
+#if !SB_FLOAT_TU
 bool supported_ylen(int my) {
   return my == 32 || my == 48 || my == 64 || my == 96 || my == 192 || my == 384;
 }
@@ -1183,20 +1179,6 @@ cudaError_t launch_yop(int my, int nlines, double *c, long ldc, int iopt, int re
   }
 }
 
-cudaError_t launch_pencil_to_plane(const Grid &g, const double *pen, double *dst, cudaStream_t st) {
-  if (g.prec)
-    k_pencil_to_plane<float><<<256, 256, 0, st>>>(g, pen, (float *)dst);
-  else
-    k_pencil_to_plane<double><<<256, 256, 0, st>>>(g, pen, dst);
-  return cudaGetLastError();
-}
-cudaError_t launch_plane_to_pencil(const Grid &g, const double *src, double *pen, cudaStream_t st) {
-  if (g.prec)
-    k_plane_to_pencil<float><<<256, 256, 0, st>>>(g, (const float *)src, pen);
-  else
-    k_plane_to_pencil<double><<<256, 256, 0, st>>>(g, src, pen);
-  return cudaGetLastError();
-}
 
 // FP64 FMA throughput probe: eight independent chains per thread
 __global__ void k_fp64_probe(double *out, int iters, double a, double b) {
@@ -1247,6 +1229,7 @@ bool supported_grid(int mgalx, int mgalz) {
   for (int v : zs) okz |= (v == mgalz);
   return okx && okz;
 }
+#endif  // !SB_FLOAT_TU
 
 // ---------------------------------------------------------------------------
 // Physical fields of the post-processor convh5 (hvhg_uvwp, convh5.f90:650-933)
@@ -1373,14 +1356,73 @@ static cudaError_t launch_phys_r(const Grid &g, const Bufs &bf, unsigned mask, d
   }
 }
 
+template <typename R>
+static cudaError_t launch_p2p_t(const Grid &g, const double *pen, double *dst, cudaStream_t st) {
+  k_pencil_to_plane<R><<<256, 256, 0, st>>>(g, pen, (R *)dst);
+  return cudaGetLastError();
+}
+template <typename R>
+static cudaError_t launch_pen_t(const Grid &g, const double *src, double *pen, cudaStream_t st) {
+  k_plane_to_pencil<R><<<256, 256, 0, st>>>(g, (const R *)src, pen);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// entry points: the FP32-mixed instantiations come from the second
+// compilation of this file (SB_FLOAT_TU=1), the rest from the first
+// ---------------------------------------------------------------------------
+cudaError_t plane_f32(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st);
+cudaError_t les_f32(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st);
+cudaError_t ydeal_f32(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
+cudaError_t p2p_f32(const Grid &g, const double *pen, double *dst, cudaStream_t st);
+cudaError_t pen_f32(const Grid &g, const double *src, double *pen, cudaStream_t st);
+cudaError_t phys_f32(const Grid &g, const Bufs &bf, unsigned mask, double *out, cudaStream_t st);
+
+#if SB_FLOAT_TU
+cudaError_t plane_f32(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
+  return launch_plane_t<float>(g, bf, stage, rk, st);
+}
+cudaError_t les_f32(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
+  return launch_les_t<float>(g, bf, stage, rk, st);
+}
+cudaError_t ydeal_f32(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  return launch_ydeal_r<float>(g, bf, rk, st, rk == 0);
+}
+cudaError_t p2p_f32(const Grid &g, const double *pen, double *dst, cudaStream_t st) {
+  return launch_p2p_t<float>(g, pen, dst, st);
+}
+cudaError_t pen_f32(const Grid &g, const double *src, double *pen, cudaStream_t st) {
+  return launch_pen_t<float>(g, src, pen, st);
+}
+cudaError_t phys_f32(const Grid &g, const Bufs &bf, unsigned mask, double *out, cudaStream_t st) {
+  return launch_phys_r<float>(g, bf, mask, out, st);
+}
+#else
+// stage 1..3: launch; stage 0: set the kernels' shared-memory limits (once)
+cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
+  return g.prec ? plane_f32(g, bf, stage, rk, st) : launch_plane_t<double>(g, bf, stage, rk, st);
+}
+cudaError_t launch_les(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
+  return g.prec ? les_f32(g, bf, stage, rk, st) : launch_les_t<double>(g, bf, stage, rk, st);
+}
+// rk = 1..3: launch; rk = 0: set the kernels' shared-memory limits
+cudaError_t launch_ydeal(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  return g.prec ? ydeal_f32(g, bf, rk, st) : launch_ydeal_r<double>(g, bf, rk, st, rk == 0);
+}
+cudaError_t launch_pencil_to_plane(const Grid &g, const double *pen, double *dst, cudaStream_t st) {
+  return g.prec ? p2p_f32(g, pen, dst, st) : launch_p2p_t<double>(g, pen, dst, st);
+}
+cudaError_t launch_plane_to_pencil(const Grid &g, const double *src, double *pen, cudaStream_t st) {
+  return g.prec ? pen_f32(g, src, pen, st) : launch_pen_t<double>(g, src, pen, st);
+}
 // one box (Grid with B = 1 and member-offset buffers): plane stage 1 with the
 // extra z-transforms into g's zbuf, then the physical fields
 cudaError_t launch_physical(const Grid &g, const Bufs &bf, unsigned mask, double *out,
                             cudaStream_t st) {
   cudaError_t e = launch_plane(g, bf, 1, 2, st);
   if (e != cudaSuccess) return e;
-  return g.prec ? launch_phys_r<float>(g, bf, mask, out, st)
-                : launch_phys_r<double>(g, bf, mask, out, st);
+  return g.prec ? phys_f32(g, bf, mask, out, st) : launch_phys_r<double>(g, bf, mask, out, st);
 }
+#endif
 
 }  // namespace sb

@@ -30,6 +30,13 @@
 #include "sb_line.cuh"
 #include "sb_seg.cuh"
 
+// This file is compiled twice: SB_FLOAT_TU=0 gives the FP64 instantiations,
+// the per-box kernels and the entry points, SB_FLOAT_TU=1 only the FP32-mixed
+// instantiations, so that the two halves compile in parallel.
+#ifndef SB_FLOAT_TU
+#define SB_FLOAT_TU 0
+#endif
+
 namespace sb {
 
 __device__ __forceinline__ cd ldc2(const double *p) { return mk(p[0], p[1]); }
@@ -142,11 +149,13 @@ __device__ __forceinline__ void rk_update(const double *ys, int ystr, const R *_
   solve_seg<kSeg>(U, PS, ys, ystr, N, VIEW, SVIEW, TAIL, SHP, SHM, L.c, L.s, L.l, g.slo, g.shi, \
                   R0, R1, R2, R3, ANTI, &xch[0][0][0][0])
 
-template <typename R>
+// TEMP: the temperature roles are compiled in (a separate instantiation, so
+// that the plain step keeps its register budget)
+template <typename R, bool TEMP>
 __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs bf, int rk1) {
   __shared__ double xch[kSeg][16][2][SB_XS];
   LineThread L;
-  if (!line_thread(g, g.temp ? 5 : 3, &L)) return;  // whole blocks
+  if (!line_thread(g, TEMP ? 5 : 3, &L)) return;  // whole blocks
   Member &M = bf.mem[L.b];
   if (M.halted) return;  // uniform per block
   const int N = g.my, ystr = blockDim.x;
@@ -165,8 +174,8 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs 
     // with the temperature, line slot 1 carries tb00: rf0tb = d(-vT_00)/dy
     // (crosst.f90:642-645) from the (0,0) line of -vT, kept in mtr; slot 0
     // computes a d/dy of the mean that is not used
-    const bool ts = g.temp && L.l == 1;
-    if (g.temp) {
+    const bool ts = TEMP && L.l == 1;
+    if (TEMP) {
       const Tail T1 = load_tail(bf.tl1o + (long)L.b * g.nkx * SB_TAIL);
       const R *src = ts ? (const R *)bf.R2 + (long)L.b * g.field + L.c : (const R *)mu;
       SEG_SOLVE(src, ts ? g.plane : 2L, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6],
@@ -219,7 +228,7 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs 
   const cd shm = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
   const double a = g.alp * i;
   const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
-  if (L.role == 0 || L.role == 4) {
+  if (L.role == 0 || (TEMP && L.role == 4)) {
     const Tail T1 = load_tail(bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL);
     if (L.role == 0) {
       // d/dy (dH1/dx + dH3/dz) (cross.f90:565-575)
@@ -248,7 +257,7 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs 
     store_col(ys, ystr, (R *)bf.S + off, ps, L);
     return;
   }
-  if (L.role == 3) {
+  if (TEMP && L.role == 3) {
     // temperature: lap(tb) = d2(tb)/dy2 - k^2 tb, shared by the thermal
     // diffusion and the buoyancy term (visc3d, crosst.f90:734-738)
     SEG_SOLVE((const R *)bf.tb + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
@@ -281,11 +290,11 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs 
                ps, L, rk, is00 ? 0.0 : nu, a * a + gz * gz, Dt, mf1, mf2, 2 * g.nkx);
 }
 
-template <typename R>
+template <typename R, bool TEMP>
 __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs bf, int mode) {
   __shared__ double xch[kSeg][16][2][SB_XS];
   LineThread L;
-  if (!line_thread(g, g.temp ? 3 : 2, &L)) return;
+  if (!line_thread(g, TEMP ? 3 : 2, &L)) return;
   Member &M = bf.mem[L.b];
   if (M.halted) return;
   const int N = g.my, ystr = blockDim.x;
@@ -331,7 +340,7 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs 
     return;
   }
   const bool is00 = (i == 0 && k == 0);
-  if (L.role == 2) {
+  if (TEMP && L.role == 2) {
     // temperature: ht + fkappa lap(tb), RK3 update of tb, zeta store and
     // moving_frame_t remaps (crosst.f90:677,734-735,782-872); nothing in the
     // prologue
@@ -359,7 +368,7 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs 
     rk_update<R>(ys, ystr, (const R *)bf.V + off, (const R *)bf.T + off, (R *)bf.phi + off,
                  (R *)bf.phiwk + off, ps, L, rk, is00 ? 0.0 : M.nu, a * a + gz * gz, M.Deltat,
                  mf1, mf2, 2 * g.nkx, nullptr,
-                 (g.temp && !is00) ? (const R *)bf.Lt + off : nullptr, g.gbeta);
+                 (TEMP && !is00) ? (const R *)bf.Lt + off : nullptr, g.gbeta);
     __syncthreads();  // the whole updated line is read below
   }
   // v = lapcdy(phi) (cross.f90:784-795, first step: 408-426); hg(0,0) keeps
@@ -584,6 +593,7 @@ __global__ void k_setconj(Grid g, Bufs bf) {
   }
 }
 
+#if !SB_FLOAT_TU
 // ---------------------------------------------------------------------------
 // per-box scalars: entry flags, hist reduction and UNER record, Delta t,
 // image offsets.  One block per box.
@@ -878,11 +888,14 @@ __global__ void k_finish(Grid g, Bufs bf) {
   M.nut_bits = 0ull;
   M.tbmax_bits = 0ull;
 }
+#endif  // !SB_FLOAT_TU
 
 // ---------------------------------------------------------------------------
 static const int kLineT = 32 * kSeg;
 
-size_t line_smem(const Grid &g) {
+// shared-memory bytes of the line kernels: one column of the longest segment
+// per thread
+static size_t smem_of(const Grid &g) {
   int rows = 0;
   for (int s = 0; s < g.nseg; s++) {
     const int r1 = (s == g.nseg - 1) ? g.my : g.shi[s];
@@ -891,73 +904,118 @@ size_t line_smem(const Grid &g) {
   return sizeof(double) * kLineT * rows;
 }
 
-cudaError_t prepare_line(const Grid &g) {
-  const int sm = (int)line_smem(g);
-  cudaFuncSetAttribute(k_lineA<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  cudaFuncSetAttribute(k_lineB<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  cudaFuncSetAttribute(k_lineA<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  cudaFuncSetAttribute(k_lineB<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  cudaFuncSetAttribute(k_lineL<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  cudaFuncSetAttribute(k_lineL<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  cudaFuncSetAttribute(k_filter<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  cudaFuncSetAttribute(k_filter<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  cudaFuncSetAttribute(k_meand1<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  cudaFuncSetAttribute(k_meand1<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+template <typename R>
+static cudaError_t prepare_line_t(const Grid &g) {
+  const int sm = (int)smem_of(g);
+  cudaFuncSetAttribute(k_lineA<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_lineB<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_lineA<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_lineB<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_lineL<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_filter<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaFuncSetAttribute(k_meand1<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   return cudaGetLastError();
+}
+
+template <typename R>
+static cudaError_t lineA_t(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  const unsigned nb = (unsigned)(g.B * ((g.temp ? 5 : 3) * g.ngrp + 1));
+  if (g.temp)
+    k_lineA<R, true><<<nb, kLineT, smem_of(g), st>>>(g, bf, rk);
+  else
+    k_lineA<R, false><<<nb, kLineT, smem_of(g), st>>>(g, bf, rk);
+  return cudaGetLastError();
+}
+
+template <typename R>
+static cudaError_t lineB_t(const Grid &g, const Bufs &bf, int mode, cudaStream_t st) {
+  const unsigned nb = (unsigned)(g.B * ((g.temp ? 3 : 2) * g.ngrp + 1));
+  if (g.temp)
+    k_lineB<R, true><<<nb, kLineT, smem_of(g), st>>>(g, bf, mode);
+  else
+    k_lineB<R, false><<<nb, kLineT, smem_of(g), st>>>(g, bf, mode);
+  return cudaGetLastError();
+}
+
+template <typename R>
+static cudaError_t lineL_t(const Grid &g, const Bufs &bf, cudaStream_t st) {
+  k_lineL<R><<<(unsigned)(g.B * (2 * g.ngrp + 1)), kLineT, smem_of(g), st>>>(g, bf);
+  return cudaGetLastError();
+}
+
+template <typename R>
+static cudaError_t meand1_t(const Grid &g, const Bufs &bf, cudaStream_t st) {
+  k_meand1<R><<<g.B, kLineT, smem_of(g), st>>>(g, bf);
+  return cudaGetLastError();
+}
+
+template <typename R>
+static cudaError_t filter_t(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  k_filter<R><<<(unsigned)(g.B * (2 * g.ngrp + 1)), kLineT, smem_of(g), st>>>(g, bf, rk);
+  return cudaGetLastError();
+}
+
+template <typename R>
+static cudaError_t setconj_t(const Grid &g, const Bufs &bf, cudaStream_t st) {
+  k_setconj<R><<<64, 256, 0, st>>>(g, bf);
+  return cudaGetLastError();
+}
+
+// entry points: the FP32-mixed instantiations come from the second
+// compilation of this file (SB_FLOAT_TU=1), the rest from the first
+cudaError_t prepare_line_f32(const Grid &g);
+cudaError_t lineA_f32(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
+cudaError_t lineB_f32(const Grid &g, const Bufs &bf, int mode, cudaStream_t st);
+cudaError_t lineL_f32(const Grid &g, const Bufs &bf, cudaStream_t st);
+cudaError_t meand1_f32(const Grid &g, const Bufs &bf, cudaStream_t st);
+cudaError_t filter_f32(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
+cudaError_t setconj_f32(const Grid &g, const Bufs &bf, cudaStream_t st);
+
+#if SB_FLOAT_TU
+cudaError_t prepare_line_f32(const Grid &g) { return prepare_line_t<float>(g); }
+cudaError_t lineA_f32(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  return lineA_t<float>(g, bf, rk, st);
+}
+cudaError_t lineB_f32(const Grid &g, const Bufs &bf, int mode, cudaStream_t st) {
+  return lineB_t<float>(g, bf, mode, st);
+}
+cudaError_t lineL_f32(const Grid &g, const Bufs &bf, cudaStream_t st) { return lineL_t<float>(g, bf, st); }
+cudaError_t meand1_f32(const Grid &g, const Bufs &bf, cudaStream_t st) {
+  return meand1_t<float>(g, bf, st);
+}
+cudaError_t filter_f32(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  return filter_t<float>(g, bf, rk, st);
+}
+cudaError_t setconj_f32(const Grid &g, const Bufs &bf, cudaStream_t st) {
+  return setconj_t<float>(g, bf, st);
+}
+#else
+size_t line_smem(const Grid &g) { return smem_of(g); }
+
+cudaError_t prepare_line(const Grid &g) {
+  cudaError_t e = prepare_line_t<double>(g);
+  return e != cudaSuccess ? e : prepare_line_f32(g);
 }
 
 int line_segments() { return kSeg; }
 
 cudaError_t launch_lineA(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
-  const unsigned nb = (unsigned)(g.B * ((g.temp ? 5 : 3) * g.ngrp + 1));
-  if (g.prec)
-    k_lineA<float><<<nb, kLineT, line_smem(g), st>>>(g, bf, rk);
-  else
-    k_lineA<double><<<nb, kLineT, line_smem(g), st>>>(g, bf, rk);
-  return cudaGetLastError();
+  return g.prec ? lineA_f32(g, bf, rk, st) : lineA_t<double>(g, bf, rk, st);
 }
-
 cudaError_t launch_lineB(const Grid &g, const Bufs &bf, int mode, cudaStream_t st) {
-  const unsigned nb = (unsigned)(g.B * ((g.temp ? 3 : 2) * g.ngrp + 1));
-  if (g.prec)
-    k_lineB<float><<<nb, kLineT, line_smem(g), st>>>(g, bf, mode);
-  else
-    k_lineB<double><<<nb, kLineT, line_smem(g), st>>>(g, bf, mode);
-  return cudaGetLastError();
+  return g.prec ? lineB_f32(g, bf, mode, st) : lineB_t<double>(g, bf, mode, st);
 }
-
 cudaError_t launch_lineL(const Grid &g, const Bufs &bf, cudaStream_t st) {
-  const unsigned nb = (unsigned)(g.B * (2 * g.ngrp + 1));
-  if (g.prec)
-    k_lineL<float><<<nb, kLineT, line_smem(g), st>>>(g, bf);
-  else
-    k_lineL<double><<<nb, kLineT, line_smem(g), st>>>(g, bf);
-  return cudaGetLastError();
+  return g.prec ? lineL_f32(g, bf, st) : lineL_t<double>(g, bf, st);
 }
-
 cudaError_t launch_meand1(const Grid &g, const Bufs &bf, cudaStream_t st) {
-  if (g.prec)
-    k_meand1<float><<<g.B, kLineT, line_smem(g), st>>>(g, bf);
-  else
-    k_meand1<double><<<g.B, kLineT, line_smem(g), st>>>(g, bf);
-  return cudaGetLastError();
+  return g.prec ? meand1_f32(g, bf, st) : meand1_t<double>(g, bf, st);
 }
-
 cudaError_t launch_filter(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
-  const unsigned nb = (unsigned)(g.B * (2 * g.ngrp + 1));
-  if (g.prec)
-    k_filter<float><<<nb, kLineT, line_smem(g), st>>>(g, bf, rk);
-  else
-    k_filter<double><<<nb, kLineT, line_smem(g), st>>>(g, bf, rk);
-  return cudaGetLastError();
+  return g.prec ? filter_f32(g, bf, rk, st) : filter_t<double>(g, bf, rk, st);
 }
-
 cudaError_t launch_setconj(const Grid &g, const Bufs &bf, cudaStream_t st) {
-  if (g.prec)
-    k_setconj<float><<<64, 256, 0, st>>>(g, bf);
-  else
-    k_setconj<double><<<64, 256, 0, st>>>(g, bf);
-  return cudaGetLastError();
+  return g.prec ? setconj_f32(g, bf, st) : setconj_t<double>(g, bf, st);
 }
 
 cudaError_t launch_scalar(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
@@ -977,5 +1035,6 @@ cudaError_t launch_finish(const Grid &g, const Bufs &bf, cudaStream_t st) {
   k_finish<<<(g.B + 127) / 128, 128, 0, st>>>(g, bf);
   return cudaGetLastError();
 }
+#endif
 
 }  // namespace sb

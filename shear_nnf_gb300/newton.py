@@ -29,6 +29,12 @@ Pieces:
   ShiftJacobian, newton_shift
                 the streamwise shift as an unknown with its phase condition,
                 Newton or Newton-hookstep
+  re_derivative, ReJacobian, newton_arclength
+                pseudo-arclength continuation in the Reynolds number
+                (iarclength=1, cpara='Rez': set_arclength, set_dxda and the
+                extra row of matvec_dns_disk3d, gmres_shear.f90:1018-1147,
+                3169-3316, 2936-2942); the re-perturbed integrations are
+                members of the same batch with their own Re
 """
 from __future__ import annotations
 
@@ -122,13 +128,16 @@ class PeriodMap:
         self.steps = 0  # RK3 steps summed over the integrated states
         self.last_steps = []
 
-    def __call__(self, states: list) -> list:
+    def __call__(self, states: list, res: list = None) -> list:
+        """Integrates the states over T; res gives each state's Reynolds
+        number (1/nu), default the parameters' Re."""
         assert 1 <= len(states) <= self.batch
         box = self.box
         full = list(states) + [states[0]] * (self.batch - len(states))
         for m, st in enumerate(full):
             box.set_state(st, m)
             box.set_etime(m, st["time"] + self.T)
+            box.set_re(m, res[m] if res is not None and m < len(res) else self.p.Re)
         steps = [0] * len(states)
         fin = [False] * len(states)
         for _ in range(1 << 20):
@@ -156,8 +165,11 @@ class Jacobian:
     gmres_shear.f90:2666-2948): eps = eps_jacobi |x0| / |d| (gmres_shear.f90:1380,
     2699), the representable step h = (x0 + eps d) - x0 (iuse_hej=1),
     J d = (G(x0 + h) - G(x0)) / eps, or (G(x0 + h) - G(x0 - h)) / (2 eps) with
-    central=True (iopt_matvec=2).  Products are evaluated a block at a time:
-    one batched integration per block of PeriodMap.batch states.
+    central=True or order=2 (iopt_matvec=2), or with order=4 (iopt_matvec=4)
+    (8 (G(x0 + h) - G(x0 - h)) - (G(x0 + 2h) - G(x0 - 2h))) / (12 eps).
+    Products are evaluated a block at a time: one batched integration per
+    block of PeriodMap.batch states.  re sets the Reynolds number of the map
+    (default the parameters').
 
     base_in_batch=True integrates x0 again as the first member of every block
     and differences against that copy, so that the base and the perturbed
@@ -165,24 +177,43 @@ class Jacobian:
 
     def __init__(self, pmap: PeriodMap, packing: Packing, x0: np.ndarray, time0=0.0,
                  xoff0=(0.0, 0.0), shiftx=0.0, shiftz=0.0, eps_jacobi=1e-6, central=False,
-                 base_in_batch=False):
+                 base_in_batch=False, order=None, re=None):
         self.pmap, self.pk, self.x0 = pmap, packing, np.asarray(x0, float)
         self.time0, self.xoff0, self.shift = time0, tuple(xoff0), (shiftx, shiftz)
-        self.eps_jacobi, self.central, self.base_in_batch = eps_jacobi, central, base_in_batch
+        self.order = int(order) if order is not None else (2 if central else 1)
+        if self.order not in (1, 2, 4):
+            raise ValueError("order must be 1, 2 or 4")
+        self.central = self.order > 1
+        self.eps_jacobi, self.base_in_batch = eps_jacobi, base_in_batch
+        self.re = re
         self.products = 0
-        self.gx0 = None if base_in_batch else self.G([self.x0])[0]
+        self._gx0 = None
 
-    def G(self, xs: list) -> list:
+    @property
+    def gx0(self):
+        """G(x0), integrated on first use (the forward-difference base; None
+        when the base is integrated in every block)."""
+        if self._gx0 is None and not self.base_in_batch:
+            self._gx0 = self.G([self.x0])[0]
+        return self._gx0
+
+    def G(self, xs: list, res: list = None) -> list:
+        """Shifted period maps of the vectors xs (at Reynolds numbers res, by
+        default the Jacobian's)."""
         states = [self.pk.unpack(x, self.time0, *self.xoff0) for x in xs]
+        if res is None and self.re is not None:
+            res = [self.re] * len(xs)
         out = []
         for q in range(0, len(states), self.pmap.batch):
-            out += self.pmap(states[q:q + self.pmap.batch])
+            chunk = states[q:q + self.pmap.batch]
+            out += (self.pmap(chunk) if res is None else
+                    self.pmap(chunk, res[q:q + self.pmap.batch]))
         return [self.pk.pack(phase_shift(s, self.pmap.p, *self.shift)) for s in out]
 
     @property
     def block(self) -> int:
         """Products per batched integration."""
-        per = 2 if self.central else 1
+        per = {1: 1, 2: 2, 4: 4}[self.order]
         return (self.pmap.batch - (1 if self.base_in_batch else 0)) // per
 
     def matvec(self, D: np.ndarray) -> np.ndarray:
@@ -202,22 +233,26 @@ class Jacobian:
         xn = np.linalg.norm(self.x0)
         eps_j = self.eps_jacobi * (xn if xn > 0 else 1.0)
         xs, eps = ([self.x0] if self.base_in_batch else []), []
+        steps = {1: (1,), 2: (1, -1), 4: (1, -1, 2, -2)}[self.order]
         for q in range(D.shape[1]):
             e = eps_j / np.linalg.norm(D[:, q])
-            xs.append(self.x0 + ((self.x0 + e * D[:, q]) - self.x0))
-            if self.central:
-                xs.append(self.x0 + ((self.x0 - e * D[:, q]) - self.x0))
+            for f in steps:
+                xs.append(self.x0 + ((self.x0 + (f * e) * D[:, q]) - self.x0))
             eps.append(e)
         gs = self.G(xs)
         if self.base_in_batch:
             g0, gs = gs[0], gs[1:]
-        else:
-            g0 = self.gx0
         self.products += D.shape[1]
-        if self.central:
+        ns = len(steps)
+        if self.order == 1:
+            if not self.base_in_batch:
+                g0 = self.gx0
+            cols = [(gs[q] - g0) / eps[q] for q in range(D.shape[1])]
+        elif self.order == 2:
             cols = [(gs[2 * q] - gs[2 * q + 1]) / (2 * eps[q]) for q in range(D.shape[1])]
         else:
-            cols = [(gs[q] - g0) / eps[q] for q in range(D.shape[1])]
+            cols = [(8.0 * (gs[ns * q] - gs[ns * q + 1]) - (gs[ns * q + 2] - gs[ns * q + 3])) /
+                    (12 * eps[q]) for q in range(D.shape[1])]
         return np.stack(cols, axis=1)
 
 
@@ -486,3 +521,78 @@ def newton(x0: np.ndarray, residual, jac_factory, k: int = 20, block: int = 1, i
         dx, _ = gmres(lambda D: J.matvec(D) - D, -F, k, block=block, tol=gmres_tol)
         x = x + dx
     return x, hist
+
+
+def re_derivative(J: Jacobian, re: float, daa: float = 1e-6, central: bool = True,
+                  gx0: np.ndarray = None) -> np.ndarray:
+    """dG/dre at J.x0 by finite differences in the Reynolds number (1/nu) with
+    the absolute step daa (set_dxda, gmres_shear.f90:3169-3316: forward with
+    iopt_matvec=1, else centred); the perturbed integrations run as members of
+    one batch with their own Re."""
+    if central:
+        gp, gm = J.G([J.x0, J.x0], [re + daa, re - daa])
+        return (gp - gm) / (2.0 * daa)
+    if gx0 is None:
+        gx0 = J.G([J.x0], [re])[0]
+    return (J.G([J.x0], [re + daa])[0] - gx0) / daa
+
+
+class ReJacobian:
+    """Jacobian of the pseudo-arclength system in the Reynolds number
+    (iarclength=1, cpara='Rez'): for X = (x, re),
+        F(x, re) = G(x; re) - x - rhs,   <xstan, dx> = 0,
+    products [(J - I) dx + dG/dre dre ; <xstan, dx>] (matvec_dns_disk3d,
+    gmres_shear.f90:2936-2942: the parameter column dxda and the row
+    orthogonal to the secant xstan = x0 - xm1; sca_re = 1)."""
+
+    def __init__(self, J, dgdre: np.ndarray, xstan: np.ndarray):
+        self.J, self.dgdre, self.xstan = J, np.asarray(dgdre, float), np.asarray(xstan, float)
+        self.n = self.xstan.size
+
+    def matvec(self, D: np.ndarray) -> np.ndarray:
+        D = np.asarray(D, float)
+        D = D[:, None] if D.ndim == 1 else D
+        dx, dre = D[: self.n], D[self.n]
+        out = np.empty_like(D)
+        out[: self.n] = self.J.matvec(dx) - dx + self.dgdre[:, None] * dre[None, :]
+        out[self.n] = self.xstan @ dx
+        return out
+
+
+def arclength_predictor(xm1: np.ndarray, rem1: float, x0: np.ndarray, re0: float,
+                        arcl: float):
+    """set_arclength (gmres_shear.f90:1018-1147) for cpara='Rez': the secant
+    xstan = x0 - xm1, ptan = re0 - rem1 and the predicted point
+    (x0 + arcl xstan, re0 + arcl ptan).  Returns (x, re, xstan)."""
+    xstan = np.asarray(x0, float) - np.asarray(xm1, float)
+    ptan = float(re0) - float(rem1)
+    if np.linalg.norm(xstan) <= 0.0 or ptan == 0.0:
+        raise ValueError("arclength: the two points give no tangent")
+    if not arcl > 0.0:
+        raise ValueError("arclength: arcl must be positive")
+    return np.asarray(x0, float) + arcl * xstan, float(re0) + arcl * ptan, xstan
+
+
+def newton_arclength(xm1: np.ndarray, rem1: float, x0: np.ndarray, re0: float, arcl: float,
+                     residual_at, jac_at, k: int = 20, block: int = 1, itmax: int = 10,
+                     tol: float = 1e-10, gmres_tol: float = 1e-3):
+    """One pseudo-arclength step along the Reynolds number from the solutions
+    (xm1, rem1) and (x0, re0): the predictor of arclength_predictor, then
+    Newton corrections (dx, dre) solving [(J - I) dx + dG/dre dre = -F,
+    <xstan, dx> = 0] (the right-hand side of the extra row is zero,
+    gmres_shear.f90:1283-1285).  residual_at(x, re) returns (F, G) with
+    F = G(x; re) - x (- rhs) in FP64; jac_at(x, re, G, xstan) returns a
+    ReJacobian.  Returns (x, re, history of |F|/|x|)."""
+    x, re, xstan = arclength_predictor(xm1, rem1, x0, re0, arcl)
+    F, G = residual_at(x, re)
+    hist = [np.linalg.norm(F) / max(np.linalg.norm(x), 1e-300)]
+    n = x.size
+    for _ in range(itmax):
+        if hist[-1] <= tol:
+            break
+        Jx = jac_at(x, re, G, xstan)
+        sol, _ = gmres(Jx.matvec, np.concatenate([-F, [0.0]]), k, block=block, tol=gmres_tol)
+        x, re = x + sol[:n], re + sol[n]
+        F, G = residual_at(x, re)
+        hist.append(np.linalg.norm(F) / max(np.linalg.norm(x), 1e-300))
+    return x, re, hist

@@ -281,3 +281,144 @@ def test_newton_with_unknown_shift(hook):
     assert hist[-1] <= 1e-10, hist
     F, _ = res(x, s)
     assert np.linalg.norm(F) <= 1e-10 * np.linalg.norm(x)
+
+
+# ---------------------------------------------------------------------------
+# fourth-order products and arclength continuation in the Reynolds number
+# ---------------------------------------------------------------------------
+
+class _CubeMap:
+    """A nonlinear map on states: every entry v -> v + c v^3 (analytic, so the
+    packed Jacobian is the complex multiplication by 1 + 3 c v^2)."""
+
+    def __init__(self, p, batch=8, c=0.5):
+        self.p, self.batch, self.c = p, batch, c
+
+    def __call__(self, states, res=None):
+        out = []
+        for s in states:
+            d = dict(s)
+            for key in ("vor", "phi", "u00", "w00"):
+                d[key] = s[key] + self.c * s[key] ** 3
+            out.append(d)
+        return out
+
+
+@pytest.mark.parametrize("order,tol", [(1, 3e-2), (2, 3e-4), (4, 3e-8)])
+def test_fd_product_orders(order, tol):
+    p = _params()
+    pk = nw.Packing(p)
+    x0 = _seeded_x(p, pk, 41)
+    x0 = x0 / np.abs(x0).max()
+    cm = _CubeMap(p)
+    d = np.random.default_rng(3).standard_normal(pk.n)
+    J = nw.Jacobian(cm, pk, x0, eps_jacobi=1e-2, order=order)
+    got = J.matvec(d)[:, 0]
+    st0, dst = pk.unpack(x0), pk.unpack(d)
+    ex = {k: dst[k] * (1 + 3 * cm.c * st0[k] ** 2) for k in ("vor", "phi", "u00", "w00")}
+    exact = pk.pack(dict(st0, **ex))
+    err = rel_l2(got, exact)
+    assert err < tol, err
+    assert J.block == 8 // {1: 1, 2: 2, 4: 4}[order]
+
+
+def test_re_jacobian_columns():
+    rng = np.random.default_rng(7)
+    n = 40
+    A = rng.standard_normal((n, n))
+    b, xs = rng.standard_normal(n), rng.standard_normal(n)
+
+    class J:
+        def matvec(self, D):
+            return A @ D
+
+    RJ = nw.ReJacobian(J(), b, xs)
+    e = np.zeros(n + 1)
+    e[-1] = 1.0
+    assert np.allclose(RJ.matvec(e)[:, 0], np.concatenate([b, [0.0]]))
+    d = rng.standard_normal(n)
+    out = RJ.matvec(np.concatenate([d, [0.0]]))[:, 0]
+    assert np.allclose(out[:-1], A @ d - d) and np.isclose(out[-1], xs @ d)
+
+
+def test_newton_arclength_follows_a_curve():
+    # F(x, re) = (A - I) x + re b + c + 0.02 x^3: two converged points at
+    # re = 1.0, 1.02, then one arclength step lands on the curve in the plane
+    # through the predictor orthogonal to the secant
+    rng = np.random.default_rng(8)
+    n = 60
+    A = _test_matrix(n, [0.5, 0.4, 0.3], seed=9)
+    b, c = 0.3 * rng.standard_normal(n), 0.3 * rng.standard_normal(n)
+
+    def F(x, re):
+        return (A - np.eye(n)) @ x + re * b + c + 0.02 * x ** 3
+
+    def residual_at(x, re):
+        f = F(x, re)
+        return f, f + x
+
+    class Jx:
+        def __init__(self, x):
+            self.M = A + np.diag(0.06 * x ** 2)
+
+        def matvec(self, D):
+            return self.M @ D
+
+    def solve(re, x0):
+        x, hist = nw.newton(x0, lambda x: F(x, re), Jx, k=n, itmax=30, tol=1e-13,
+                            gmres_tol=1e-12)
+        assert hist[-1] <= 1e-13
+        return x
+
+    x1 = solve(1.0, np.zeros(n))
+    x2 = solve(1.02, x1)  # the same branch
+    xp, rep, xstan = nw.arclength_predictor(x1, 1.0, x2, 1.02, 1.0)
+    assert np.isclose(rep, 1.04)
+    x, re, hist = nw.newton_arclength(
+        x1, 1.0, x2, 1.02, 1.0, residual_at,
+        lambda x, re, G, xs: nw.ReJacobian(Jx(x), b, xs), k=n + 1, itmax=20, tol=1e-13,
+        gmres_tol=1e-12)
+    assert hist[-1] <= 1e-13, hist
+    assert abs(xstan @ (x - xp)) <= 1e-10 * np.linalg.norm(xstan) * np.linalg.norm(x)
+    assert np.linalg.norm(F(x, re)) <= 1e-12 * np.linalg.norm(x)
+    with pytest.raises(ValueError):
+        nw.arclength_predictor(x1, 1.0, x2, 1.0, 1.0)
+    assert len(hist) <= 6 and abs(re - 1.04) < 0.01
+
+
+@pytest.mark.gpu
+def test_arclength_in_re_gpu():
+    # manufactured curve through (x*, re*): F(x, re) = G(x; re) - x - rhs with
+    # rhs = G(x*; re*) - x*; a second point at 0.999 re* by Newton at fixed re,
+    # then one arclength step (arcl = 1) past x*
+    p = _params()
+    T = 10.0
+    pk = nw.Packing(p, *nw.Packing.reference_scales(p))
+    xs = _seeded_x(p, pk, 16)
+    re_s = p.Re
+    pm1 = nw.PeriodMap(p, T, batch=1)
+    rhs = pk.pack(pm1([pk.unpack(xs)], [re_s])[0]) - xs
+
+    def residual_at(x, re):
+        G = pk.pack(pm1([pk.unpack(x)], [re])[0])
+        return G - x - rhs, G
+
+    pm = nw.PeriodMap(p, T, batch=8)
+
+    def jac(x, re):
+        return nw.Jacobian(pm, pk, x, eps_jacobi=1e-7, central=True, re=re)
+
+    re1 = 0.999 * re_s
+    x1, h1 = nw.newton(xs, lambda x: residual_at(x, re1)[0], lambda x: jac(x, re1), k=16,
+                       block=4, itmax=12, tol=1e-11, gmres_tol=1e-9)
+    assert h1[-1] <= 1e-11, h1
+    def jac_at(x, re, G, xst):
+        J = jac(x, re)
+        return nw.ReJacobian(J, nw.re_derivative(J, re, daa=1e-5 * re), xst)
+
+    xp, rep, xstan = nw.arclength_predictor(x1, re1, xs, re_s, 1.0)
+    x, re, hist = nw.newton_arclength(x1, re1, xs, re_s, 1.0, residual_at, jac_at, k=16,
+                                      block=4, itmax=12, tol=1e-10, gmres_tol=1e-9)
+    assert hist[-1] <= 1e-10, hist
+    assert abs(xstan @ (x - xp)) <= 1e-8 * np.linalg.norm(xstan) * np.linalg.norm(x)
+    assert abs(re - 1.001 * re_s) < 2.5e-4 * re_s
