@@ -35,6 +35,11 @@ Pieces:
                 extra row of matvec_dns_disk3d, gmres_shear.f90:1018-1147,
                 3169-3316, 2936-2942); the re-perturbed integrations are
                 members of the same batch with their own Re
+  BorderedJacobian, period_derivative, flow_direction, newton_extended
+                any set of extra unknowns with their conditions: streamwise
+                and spanwise shifts and the period (isol_mode 4-6), the
+                period's column dG/dT and the phase row f(x0) from members
+                with their own end times
 """
 from __future__ import annotations
 
@@ -128,15 +133,17 @@ class PeriodMap:
         self.steps = 0  # RK3 steps summed over the integrated states
         self.last_steps = []
 
-    def __call__(self, states: list, res: list = None) -> list:
+    def __call__(self, states: list, res: list = None, Ts: list = None) -> list:
         """Integrates the states over T; res gives each state's Reynolds
-        number (1/nu), default the parameters' Re."""
+        number (1/nu), default the parameters' Re, and Ts each state's
+        integration time, default T."""
         assert 1 <= len(states) <= self.batch
         box = self.box
         full = list(states) + [states[0]] * (self.batch - len(states))
         for m, st in enumerate(full):
             box.set_state(st, m)
-            box.set_etime(m, st["time"] + self.T)
+            T = Ts[m] if Ts is not None and m < len(Ts) else self.T
+            box.set_etime(m, st["time"] + T)
             box.set_re(m, res[m] if res is not None and m < len(res) else self.p.Re)
         steps = [0] * len(states)
         fin = [False] * len(states)
@@ -596,3 +603,97 @@ def newton_arclength(xm1: np.ndarray, rem1: float, x0: np.ndarray, re0: float, a
         F, G = residual_at(x, re)
         hist.append(np.linalg.norm(F) / max(np.linalg.norm(x), 1e-300))
     return x, re, hist
+
+
+class BorderedJacobian:
+    """Jacobian of the periodic-orbit system with extra unknowns
+    (matvec_dns_disk3d, gmres_shear.f90:2900-2942): for X = (x, a_1..a_m),
+        [(J - I) dx + sum_k c_k da_k ; <r_k, dx>, k = 1..m]
+    with c_k = dG/da_k (shift_tangent of G for the shifts, period_derivative
+    for the period, re_derivative for the Reynolds number) and r_k the k-th
+    condition (the shift directions of x0 for the shifts, flow_direction of
+    x0 for the period: the rows of gmres_shear.f90:2915-2934)."""
+
+    def __init__(self, J, cols: list, rows: list):
+        self.J = J
+        self.cols = [np.asarray(c, float) for c in cols]
+        self.rows = [np.asarray(r, float) for r in rows]
+        assert len(self.cols) == len(self.rows)
+        self.n = self.cols[0].size if self.cols else None
+
+    def matvec(self, D: np.ndarray) -> np.ndarray:
+        D = np.asarray(D, float)
+        D = D[:, None] if D.ndim == 1 else D
+        m = len(self.cols)
+        n = D.shape[0] - m
+        dx, da = D[:n], D[n:]
+        out = np.empty_like(D)
+        out[:n] = self.J.matvec(dx) - dx
+        for k in range(m):
+            out[:n] += self.cols[k][:, None] * da[k][None, :]
+            out[n + k] = self.rows[k] @ dx
+        return out
+
+
+def period_derivative(J: Jacobian, T: float, h: float) -> np.ndarray:
+    """dG/dT at J.x0: centred difference of the shifted map over the
+    integration times T +- h, two members of one batch with their own end
+    times (the dxdt column of matvec_dns_disk3d, gmres_shear.f90:2928-2931)."""
+    st = J.pk.unpack(J.x0, J.time0, *J.xoff0)
+    gp, gm = J.pmap([st, st], Ts=[T + h, T - h])
+    gp = J.pk.pack(phase_shift(gp, J.pmap.p, *J.shift))
+    gm = J.pk.pack(phase_shift(gm, J.pmap.p, *J.shift))
+    return (gp - gm) / (2.0 * h)
+
+
+def flow_direction(pmap: PeriodMap, packing: Packing, x: np.ndarray, h: float, time0=0.0,
+                   xoff0=(0.0, 0.0)) -> np.ndarray:
+    """The time derivative of the flow at x (dxdt0 of the period's phase
+    condition <dxdt0, dx> = 0, gmres_shear.f90:2931), as the second-order
+    one-sided difference (-3 x + 4 Phi_h(x) - Phi_2h(x)) / (2h) from two
+    members with their own end times.  The reference evaluates the right-hand
+    side instead (set_dxdt); any direction transverse to the flow fixes the
+    phase, so the converged orbit is the same."""
+    st = packing.unpack(x, time0, *xoff0)
+    a, b = pmap([st, st], Ts=[h, 2.0 * h])
+    return (-3.0 * x + 4.0 * packing.pack(a) - packing.pack(b)) / (2.0 * h)
+
+
+def newton_extended(x0: np.ndarray, a0, residual_at, jac_at, k: int = 20, block: int = 1,
+                    itmax: int = 10, tol: float = 1e-10, gmres_tol: float = 1e-3,
+                    delta: float = None):
+    """Newton(-hookstep) for F(x, a) = 0 with extra unknowns a (shifts,
+    period; newton_shear.f90:183-597 with isol_mode 4-6): residual_at(x, a)
+    returns (F, G) with G the shifted period map of x over the period in a
+    (FP64) and F = G - x (- rhs); jac_at(x, a, G) returns a BorderedJacobian
+    with len(a) conditions, whose right-hand sides are zero.  With delta set,
+    every step is a Krylov hookstep of at most delta (delta halved on a failed
+    step, doubled on a good one).  Returns (x, a, history of |F|/|x|)."""
+    x, a = np.asarray(x0, float).copy(), np.atleast_1d(np.asarray(a0, float)).copy()
+    m = a.size
+    F, G = residual_at(x, a)
+    hist = [np.linalg.norm(F) / max(np.linalg.norm(x), 1e-300)]
+    n = x.size
+    for _ in range(itmax):
+        if hist[-1] <= tol:
+            break
+        Jx = jac_at(x, a, G)
+        b = np.concatenate([-F, np.zeros(m)])
+        sol, _, (V, H, rhs) = gmres(Jx.matvec, b, k, block=block, tol=gmres_tol, krylov=True)
+        if delta is None:
+            x, a = x + sol[:n], a + sol[n:]
+            F, G = residual_at(x, a)
+            hist.append(np.linalg.norm(F) / max(np.linalg.norm(x), 1e-300))
+            continue
+        fn0 = np.linalg.norm(F)
+        for _trial in range(20):
+            dX, _, _ = hookstep(V, H, rhs, delta)
+            xn, an = x + dX[:n], a + dX[n:]
+            Fn, Gn = residual_at(xn, an)
+            if np.linalg.norm(Fn) < fn0:
+                x, a, F, G = xn, an, Fn, Gn
+                delta *= 2.0
+                break
+            delta *= 0.5
+        hist.append(np.linalg.norm(F) / max(np.linalg.norm(x), 1e-300))
+    return x, a, hist

@@ -422,3 +422,125 @@ def test_arclength_in_re_gpu():
     assert hist[-1] <= 1e-10, hist
     assert abs(xstan @ (x - xp)) <= 1e-8 * np.linalg.norm(xstan) * np.linalg.norm(x)
     assert abs(re - 1.001 * re_s) < 2.5e-4 * re_s
+
+
+# ---------------------------------------------------------------------------
+# extra unknowns: bordered Jacobian, period derivative, flow direction
+# ---------------------------------------------------------------------------
+
+def test_bordered_jacobian_matches_dense():
+    rng = np.random.default_rng(11)
+    n, m = 30, 3
+    A = rng.standard_normal((n, n))
+    cols = [rng.standard_normal(n) for _ in range(m)]
+    rows = [rng.standard_normal(n) for _ in range(m)]
+
+    class J:
+        def matvec(self, D):
+            return A @ D
+
+    BJ = nw.BorderedJacobian(J(), cols, rows)
+    M = np.zeros((n + m, n + m))
+    M[:n, :n] = A - np.eye(n)
+    for q in range(m):
+        M[:n, n + q] = cols[q]
+        M[n + q, :n] = rows[q]
+    D = rng.standard_normal((n + m, 4))
+    assert np.allclose(BJ.matvec(D), M @ D)
+
+
+class _DecayMap:
+    """Phi_T(x) = exp(-lam T) x entrywise, with per-state integration times."""
+
+    def __init__(self, p, T, lam=0.3, batch=4):
+        self.p, self.T, self.lam, self.batch = p, T, lam, batch
+
+    def __call__(self, states, res=None, Ts=None):
+        out = []
+        for q, s in enumerate(states):
+            T = Ts[q] if Ts is not None else self.T
+            f = np.exp(-self.lam * T)
+            out.append(dict(s, vor=s["vor"] * f, phi=s["phi"] * f, u00=s["u00"] * f,
+                            w00=s["w00"] * f))
+        return out
+
+
+def test_period_derivative_and_flow_direction():
+    p = _params()
+    pk = nw.Packing(p)
+    x0 = _seeded_x(p, pk, 43)
+    dm = _DecayMap(p, T=2.0)
+    J = nw.Jacobian(dm, pk, x0, eps_jacobi=1e-6)
+    dgdt = nw.period_derivative(J, 2.0, h=1e-3)
+    assert rel_l2(dgdt, -0.3 * np.exp(-0.6) * x0) < 1e-6
+    f0 = nw.flow_direction(dm, pk, x0, h=1e-3)
+    assert rel_l2(f0, -0.3 * x0) < 1e-6
+
+
+def test_newton_extended_on_a_matrix_problem():
+    # F(x, a) = (A - I) x + a0 b0 + a1 b1 + c + 0.02 x^3 with the conditions
+    # <r_k, dx> = 0: the root lies on the affine plane through x0
+    rng = np.random.default_rng(12)
+    n = 50
+    A = _test_matrix(n, [0.5, 0.4, 0.3], seed=13)
+    b0, b1, c = (0.3 * rng.standard_normal(n) for _ in range(3))
+    r0, r1 = rng.standard_normal(n), rng.standard_normal(n)
+
+    def residual_at(x, a):
+        f = (A - np.eye(n)) @ x + a[0] * b0 + a[1] * b1 + c + 0.02 * x ** 3
+        return f, f + x
+
+    class Jx:
+        def __init__(self, x):
+            self.M = A + np.diag(0.06 * x ** 2)
+
+        def matvec(self, D):
+            return self.M @ D
+
+    x0 = 0.1 * rng.standard_normal(n)
+    x, a, hist = nw.newton_extended(
+        x0, [0.2, -0.1], residual_at,
+        lambda x, a, G: nw.BorderedJacobian(Jx(x), [b0, b1], [r0, r1]), k=n + 2, itmax=20,
+        tol=1e-13, gmres_tol=1e-12)
+    assert hist[-1] <= 1e-13, hist
+    assert abs(r0 @ (x - x0)) < 1e-10 and abs(r1 @ (x - x0)) < 1e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("hook", [False, True])
+def test_newton_unknown_shift_and_period_gpu(hook):
+    # manufactured family through (x*, s*, T*): F(x, s, T) = shift_s(Phi_T(x)) - x - rhs
+    p = _params()
+    T_s, s_s, h = 10.0, 0.3, 1e-3
+    pk = nw.Packing(p, *nw.Packing.reference_scales(p))
+    xs = _seeded_x(p, pk, 18)
+    pm1 = nw.PeriodMap(p, T_s, batch=2)
+
+    def G_of(x, a):
+        st = pm1([pk.unpack(x)], Ts=[a[1]])[0]
+        return pk.pack(nw.phase_shift(st, p, a[0], 0.0))
+
+    rhs = G_of(xs, [s_s, T_s]) - xs
+
+    def residual_at(x, a):
+        G = G_of(x, a)
+        return G - x - rhs, G
+
+    pm = nw.PeriodMap(p, T_s, batch=8)
+
+    def jac_at(x, a, G):
+        pm.T = float(a[1])
+        J = nw.Jacobian(pm, pk, x, shiftx=float(a[0]), eps_jacobi=1e-7, central=True)
+        tx = nw.shift_tangent(pk, p, x)
+        f0 = nw.flow_direction(pm1, pk, x, h)
+        return nw.BorderedJacobian(J, [nw.shift_tangent(pk, p, G), nw.period_derivative(J, a[1], h)],
+                                   [tx / np.linalg.norm(tx), f0 / np.linalg.norm(f0)])
+
+    x0 = xs + 1e-3 * np.linalg.norm(xs) / np.sqrt(pk.n) * \
+        np.random.default_rng(19).standard_normal(pk.n)
+    x, a, hist = nw.newton_extended(x0, [s_s - 0.02, T_s + 0.05], residual_at, jac_at, k=16,
+                                    block=4, itmax=12, tol=1e-10, gmres_tol=1e-8,
+                                    delta=(0.05 * np.linalg.norm(xs) if hook else None))
+    assert hist[-1] <= 1e-10, hist
+    F, _ = residual_at(x, a)
+    assert np.linalg.norm(F) <= 1e-10 * np.linalg.norm(x)
