@@ -139,6 +139,26 @@ int sb_crosst(sb_handle *h, double *vor, double *phi, double *u00, double *w00, 
               double *tb00, double *time, double *xoffb, double *xofft, int nstep,
               sb_status *st);
 
+/* The uner(1:10) and uner2(1:4) of the last statistics record of a member
+ * (the quantities hist 'w' writes, cross.f90:2064-2118). */
+int sb_stats(sb_handle *h, int member, double *uner, double *uner2);
+
+/* Batched finite-difference products of the period map (matvec_dns_disk3d,
+ * gmres_shear.f90:2666-2948, iopt_matvec 1 forward / 2 central):
+ *   eps_q = eps_jacobi |x0| / |d_q|,  h_q = (x0 + eps_q d_q) - x0 (iuse_hej),
+ *   out_q = (Phi_T(x0 + h_q) - Phi_T(x0)) / eps_q                 central = 0
+ *   out_q = (Phi_T(x0 + h_q) - Phi_T(x0 - h_q)) / (2 eps_q)       central = 1
+ * with Phi_T the integration from time0 (offsets xoffb, xofft) to time0 + T
+ * (calc_dns_disk3d, gmres_shear.f90:2951-3120).  Vectors are states laid out
+ * as [vor | phi | u00 | w00] (pencil layout, 4 nkx mz my + 2 my doubles),
+ * norms plain 2-norms; dirs and out hold ndir such vectors.  Every perturbed
+ * state is one member of the handle's batch, so a block of batch directions
+ * is one batched integration.  The members' states and end times are
+ * overwritten.  Not available for the temperature variant. */
+int sb_jv_batch(sb_handle *h, const double *x0, double time0, double xoffb, double xofft,
+                double T, const double *dirs, int ndir, double eps_jacobi, int central,
+                double *out);
+
 /* Measurement hooks (no counterpart in the reference; used by the benchmark).
  * sb_launch_stage enqueues `count` launches of one kernel of substep rk on the
  * handle's stream: stage 1..3 the plane stages, 4 the per-box phase tables,

@@ -81,7 +81,7 @@ ABI_FUNCTIONS = [
     "sb_fp64_peak", "sb_op_derivyc", "sb_op_lapcdy", "sb_op_derivyc_noalloc",
     "sb_set_member_etime", "sb_op_filterc", "sb_op_cfty", "sb_op_rfty", "sb_write_restart",
     "sb_read_restart", "sb_autotune", "sb_physical_fields", "sb_set_temperature",
-    "sb_get_temperature", "sb_crosst",
+    "sb_get_temperature", "sb_crosst", "sb_stats", "sb_jv_batch",
 ]
 
 _lib = None
@@ -115,6 +115,10 @@ def lib(auto_build: bool = False):
     L.sb_crosst.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int,
                             ctypes.POINTER(SbStatus)]
     L.sb_set_temperature.argtypes = [vp, ctypes.c_int, dp, dp]
+    L.sb_stats.argtypes = [vp, ctypes.c_int, dp, dp]
+    L.sb_jv_batch.argtypes = [vp, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                              ctypes.c_double, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int,
+                              dp]
     L.sb_get_temperature.argtypes = [vp, ctypes.c_int, dp, dp]
     L.sb_get_stream.restype = vp
     L.sb_get_stream.argtypes = [vp]
@@ -299,6 +303,31 @@ class ShearBox:
         c = (ctypes.c_int * 3)()
         _check(lib().sb_autotune(self.h, c))
         return {"p1_cols": c[0], "p3_cols": c[1], "p2_threads": c[2]}
+
+    def stats(self, member: int = 0):
+        """(uner[10], uner2[4]) of the member's last statistics record."""
+        u, u2 = np.zeros(10), np.zeros(4)
+        _check(lib().sb_stats(self.h, int(member), _dp(u), _dp(u2)))
+        return u, u2
+
+    def state_vector(self, st: dict) -> np.ndarray:
+        """A state as the flat [vor | phi | u00 | w00] vector of sb_jv_batch."""
+        return np.concatenate([np.ascontiguousarray(st["vor"], np.complex128).view(np.float64).ravel(),
+                               np.ascontiguousarray(st["phi"], np.complex128).view(np.float64).ravel(),
+                               np.asarray(st["u00"], np.float64), np.asarray(st["w00"], np.float64)])
+
+    def jv_batch(self, x0: np.ndarray, dirs: np.ndarray, T: float, eps_jacobi: float = 1e-7,
+                 central: bool = False, time0: float = 0.0, xoffb: float = 0.0,
+                 xofft: float = 0.0) -> np.ndarray:
+        """Batched finite-difference products of the period map on flat state
+        vectors (sb_jv_batch): x0 (n,), dirs (ndir, n) -> (ndir, n)."""
+        x0 = np.ascontiguousarray(x0, np.float64)
+        d = np.ascontiguousarray(np.atleast_2d(dirs), np.float64)
+        out = np.zeros_like(d)
+        _check(lib().sb_jv_batch(self.h, _dp(x0), float(time0), float(xoffb), float(xofft),
+                                 float(T), _dp(d), int(d.shape[0]), float(eps_jacobi),
+                                 int(bool(central)), _dp(out)))
+        return out
 
     def fp64_peak(self) -> float:
         v = ctypes.c_double()

@@ -19,7 +19,9 @@ LIB = os.path.join(BUILD, "libshearbox.so")
 UNITS = [("sb_kernels.cu", ["-DSB_FLOAT_TU=0"]), ("sb_kernels.cu", ["-DSB_FLOAT_TU=1"]),
          ("sb_yline.cu", ["-DSB_FLOAT_TU=0"]), ("sb_yline.cu", ["-DSB_FLOAT_TU=1"]),
          ("sb_ops.cu", []), ("sb_noalloc.cu", []), ("sb_api.cu", []), ("sb_host.cpp", []),
-         ("sb_io.cpp", [])]
+         ("sb_io.cpp", []),
+         # the finite-difference perturbations as written, without fused multiply-adds
+         ("sb_newton.cpp", ["-Xcompiler", "-ffp-contract=off"])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC"]
 # extra compile flags for tuning builds, e.g. SB_NVCC_EXTRA="-DSB_KSEG=4"
@@ -47,12 +49,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
     procs = []
     objs = []
     for src, defs in UNITS:
-        tag = "".join(d.split("=")[-1] for d in defs)
+        tag = "".join(d.split("=")[-1] for d in defs if d.startswith("-D"))
         obj = os.path.join(BUILD, os.path.splitext(src)[0] + (f"_{tag}" if tag else "") + ".o")
         objs.append(obj)
         cmd = [nvcc(), *ARCH, *FLAGS, *EXTRA, *defs, "-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cpp"):
-            cmd = [nvcc(), *FLAGS, "-x", "c++", "-c", os.path.join(CSRC, src), "-o", obj]
+            cmd = [nvcc(), *FLAGS, *defs, "-x", "c++", "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))

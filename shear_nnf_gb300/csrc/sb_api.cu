@@ -55,6 +55,13 @@ struct sb_handle {
   std::vector<Member> mem_init;
 };
 
+namespace sb {
+// handle accessors for the host code of sb_newton.cpp
+const sb_params *handle_params(const sb_handle *h) { return &h->p; }
+int handle_batch(const sb_handle *h) { return h->g.B; }
+int handle_trace_len(const sb_handle *h) { return h->g.tlen; }
+}  // namespace sb
+
 static int dalloc(sb_handle *h, double **p, size_t n) {
   void *q = nullptr;
   cudaError_t e = cudaMalloc(&q, sizeof(double) * (n ? n : 1));

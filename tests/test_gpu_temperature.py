@@ -1,8 +1,9 @@
 """GPU parity of the temperature variant crosst (itemperature = 1) against the
 CPU oracle through the C-ABI: FP64 one-step and twenty-step runs with and
 without shear, with the Smagorinsky stage (molecular terms kept or dropped),
-the rest-state known answer, the FP32-mixed form against FP64, a batch against
-single boxes, and the largest grid.  Tolerances as for cross: relative L2 below
+the y filter and y dealiasing (which leave tb alone), the rest-state known
+answer, the FP32-mixed form against FP64, a batch against single boxes, and
+the largest grid.  Tolerances as for cross: relative L2 below
 1e-12 after one step, statistics records to 1e-10."""
 import numpy as np
 import pytest
@@ -43,7 +44,9 @@ def _errors(st_o, st_g):
                                      ((64, 32, 32), {"s": 0.0, "fixed_dt": 0.01}),
                                      ((96, 48, 48), {"bym": -0.5, "gbeta": 2.0}),
                                      ((64, 32, 32), {"les": 1, "les_visc": 1, "cs": 0.1}),
-                                     ((64, 32, 32), {"les": 1, "les_visc": 0, "cs": 0.1})])
+                                     ((64, 32, 32), {"les": 1, "les_visc": 0, "cs": 0.1}),
+                                     ((64, 32, 32), {"ydeal": 3}),
+                                     ((64, 32, 32), {"ydeal": 2})])
 def test_temperature_one_step(grid, kw):
     pp = _temp(grid, 4000.0, **kw)
     st_o, tr_o, st_g, tr_g, status = _run_both(pp, 1)

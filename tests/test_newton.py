@@ -544,3 +544,56 @@ def test_newton_unknown_shift_and_period_gpu(hook):
     assert hist[-1] <= 1e-10, hist
     F, _ = residual_at(x, a)
     assert np.linalg.norm(F) <= 1e-10 * np.linalg.norm(x)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("central", [False, True])
+def test_jv_batch_c_abi_matches_single_integrations(central):
+    """sb_jv_batch (flat state vectors, the handle's batch as the block) gives
+    the same quotients as single integrations through the public API.  The
+    step eps is ~1e-7 |x0|, so a rounding difference of the perturbed state
+    (its norm is summed in another order by numpy) shows up ~1e9 times larger
+    in the quotient: the bar is 1e-7."""
+    p = _params()
+    T = 0.5
+    box = sb.ShearBox(p, batch=4)
+    st0 = sb.seed_state(p, 21)
+    x0 = box.state_vector(st0)
+    dirs = np.random.default_rng(4).standard_normal((5, x0.size))  # more than one block
+    out = box.jv_batch(x0, dirs, T, eps_jacobi=1e-7, central=central)
+    sz = sb.sizes(p)
+    nf = 2 * sz["nkx"] * sz["mz"] * p.my
+
+    def to_state(x):
+        shp = (sz["mz"], sz["nkx"], p.my)
+        return {"vor": x[:nf].copy().view(np.complex128).reshape(shp),
+                "phi": x[nf:2 * nf].copy().view(np.complex128).reshape(shp),
+                "u00": x[2 * nf:2 * nf + p.my].copy(), "w00": x[2 * nf + p.my:].copy(),
+                "time": 0.0, "xoffb": 0.0, "xofft": 0.0}
+
+    pm = nw.PeriodMap(p, T, batch=1)
+
+    def phi_T(x):
+        return box.state_vector(pm([to_state(x)])[0])
+
+    eps_j = 1e-7 * np.linalg.norm(x0)
+    g0 = None if central else phi_T(x0)
+    for q in range(dirs.shape[0]):
+        e = eps_j / np.linalg.norm(dirs[q])
+        xp = x0 + ((x0 + e * dirs[q]) - x0)
+        if central:
+            xm = x0 + ((x0 - e * dirs[q]) - x0)
+            ref = (phi_T(xp) - phi_T(xm)) / (2 * e)
+        else:
+            ref = (phi_T(xp) - g0) / e
+        assert rel_l2(out[q], ref) < 1e-7, q
+
+
+@pytest.mark.gpu
+def test_stats_is_the_last_record():
+    p = _params()
+    box = sb.ShearBox(p)
+    st = sb.seed_state(p, 22)
+    tr, _ = box.cross(st, 3)
+    u, u2 = box.stats()
+    assert np.array_equal(u, tr[-1, 2:12]) and np.array_equal(u2, tr[-1, 20:24])
