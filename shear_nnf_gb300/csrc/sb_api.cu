@@ -48,6 +48,10 @@ struct sb_handle {
   Grid g;
   Bufs bf;
   cudaStream_t st = nullptr;
+  // side branch of the step graph: the per-box scalars and phase tables run
+  // beside plane stage 3, which they do not depend on
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaGraphExec_t step_exec = nullptr;
   std::vector<void *> allocs;
   double *d_pen = nullptr;  // staging buffer, one pencil-layout field
@@ -170,10 +174,24 @@ static int capture_step(sb_handle *h) {
     if (h->g.les)
       for (int q = 2; q <= 4 && e == cudaSuccess; q++) e = launch_les(h->g, h->bf, q, rk, h->st);
     if (e != cudaSuccess) break;
-    if ((e = launch_plane(h->g, h->bf, 3, rk, h->st)) != cudaSuccess) break;
-    if (h->g.les && (e = launch_les(h->g, h->bf, 5, rk, h->st)) != cudaSuccess) break;
-    if ((e = launch_scalar(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
-    if ((e = launch_tables(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
+    if (!h->g.les) {
+      // k_scalar needs stages 1-2 (statistics, |u| maxima) and k_tables needs
+      // k_scalar: both run on a branch beside plane stage 3
+      if ((e = cudaEventRecord(h->ev_fork, h->st)) != cudaSuccess ||
+          (e = cudaStreamWaitEvent(h->side, h->ev_fork, 0)) != cudaSuccess ||
+          (e = launch_scalar(h->g, h->bf, rk, h->side)) != cudaSuccess ||
+          (e = launch_tables(h->g, h->bf, rk, h->side)) != cudaSuccess ||
+          (e = cudaEventRecord(h->ev_join, h->side)) != cudaSuccess ||
+          (e = launch_plane(h->g, h->bf, 3, rk, h->st)) != cudaSuccess ||
+          (e = cudaStreamWaitEvent(h->st, h->ev_join, 0)) != cudaSuccess)
+        break;
+    } else {
+      // with LES, k_scalar also takes the statistics of the LES stages
+      if ((e = launch_plane(h->g, h->bf, 3, rk, h->st)) != cudaSuccess) break;
+      if ((e = launch_les(h->g, h->bf, 5, rk, h->st)) != cudaSuccess) break;
+      if ((e = launch_scalar(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
+      if ((e = launch_tables(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
+    }
     if (h->g.les && (e = launch_lineL(h->g, h->bf, h->st)) != cudaSuccess) break;
     if ((e = launch_lineA(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
     e = launch_lineB(h->g, h->bf, rk, h->st);
@@ -391,6 +409,9 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
     g.shi[q] = plan.hi[q];
   }
   cudaError_t ce = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
   if (ce != cudaSuccess) {
     sb_destroy(h);
     return fail(3, "stream: %s", cudaGetErrorString(ce));
@@ -573,6 +594,9 @@ int sb_destroy(sb_handle *h) {
   if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
   for (void *q : h->allocs) cudaFree(q);
   if (h->st) cudaStreamDestroy(h->st);
+  if (h->side) cudaStreamDestroy(h->side);
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
   delete h;
   return 0;
 }
