@@ -403,6 +403,10 @@ def run_ours(args):
     torch.cuda.set_device(dev)
     torch.cuda.init()
     pp = box_params()
+    if args.variant == "les":
+        pp.update(les=1, les_visc=1, cs=0.1)
+    elif args.variant == "temperature":
+        pp.update(temperature=1, fkappa=LZ ** 2 / REZ / 0.7, bym=1.0, gbeta=0.5)
     p = sb.make_params(**pp)
     st0 = sb.seed_state(p, 3 + rank)
     box = sb.ShearBox(p)
@@ -430,14 +434,17 @@ def run_ours(args):
     status = box.status()
     ms_max = allmax(dist, ms)
     steps_per_s = ws * args.steps / (ms_max * 1e-3)
-    launches = 22 * args.steps + 4
+    # per step: 3 substeps x (3 plane stages, scalars, tables, 2 line kernels)
+    # + the end-of-step kernel; LES adds 5 per substep; + 4 entry launches
+    launches = (37 if args.variant == "les" else 22) * args.steps + 4
     if args.lite:
         # profiling runs (ncu): the timed steps only, no side measurements
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": steps_per_s, "unit": "steps/s",
                               "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
                               "ms_per_step": ms_max / args.steps, "lite": True,
-                              "config": config({"grid": list(GRID), "tuning": tuning}),
+                              "config": config({"grid": list(GRID), "tuning": tuning,
+                                                "variant": args.variant}),
                               "gpu_launches": launches}))
         return
     # dominant kernel alone: plane stage 2 (x transforms + u x omega)
@@ -612,7 +619,11 @@ def main():
     ap.add_argument("--no-temp", action="store_true", help="skip the temperature (crosst) leg")
     ap.add_argument("--lite", action="store_true",
                     help="profiling only: time the steps, skip e2e / CPU / per-kernel legs")
+    ap.add_argument("--variant", default="plain", choices=["plain", "les", "temperature"],
+                    help="profiling only (with --lite): step the LES or the temperature box")
     args = ap.parse_args()
+    if args.variant != "plain" and not args.lite:
+        ap.error("--variant is for profiling runs (--lite)")
     global GRID
     GRID = GRIDS[args.grid]
     if args.warmup < 3:

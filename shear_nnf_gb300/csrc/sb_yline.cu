@@ -14,6 +14,10 @@
 //                    substep                                   (-> D, Lv)
 //            role 1: RK3 update of phi, v = lapcdy(phi), dv/dy  (-> phi, G, V)
 //            mean warp: du00/dy, dw00/dy for the next substep
+// With the temperature (crosst) the same kernels carry the scalar: k_lineA
+// role 0 also adds d(-vT)/dy to ht, role 1 also takes lap(tb), the mean block
+// updates tb00; k_lineB role 1 adds the buoyancy gbeta lap(tb) to the phi
+// right-hand side and a third role updates tb.
 // The same k_lineB (mode 0) is the prologue of a cross call: v from phi on the
 // first step (cross.f90:408-426) and the first derivatives.  Forward
 // substitutions are kept in shared memory, one column per thread.
@@ -152,10 +156,10 @@ __device__ __forceinline__ void rk_update(const double *ys, int ystr, const R *_
 // TEMP: the temperature roles are compiled in (a separate instantiation, so
 // that the plain step keeps its register budget)
 template <typename R, bool TEMP>
-__global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs bf, int rk1) {
+__global__ void __launch_bounds__(32 * kSeg, TEMP ? 5 : SB_LINE_MINB) k_lineA(Grid g, Bufs bf, int rk1) {
   __shared__ double xch[kSeg][16][2][SB_XS];
   LineThread L;
-  if (!line_thread(g, TEMP ? 5 : 3, &L)) return;  // whole blocks
+  if (!line_thread(g, 3, &L)) return;  // whole blocks
   Member &M = bf.mem[L.b];
   if (M.halted) return;  // uniform per block
   const int N = g.my, ystr = blockDim.x;
@@ -228,23 +232,22 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs 
   const cd shm = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
   const double a = g.alp * i;
   const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
-  if (L.role == 0 || (TEMP && L.role == 4)) {
+  if (L.role == 0) {
     const Tail T1 = load_tail(bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL);
-    if (L.role == 0) {
-      // d/dy (dH1/dx + dH3/dz) (cross.f90:565-575)
-      SEG_SOLVE((const R *)bf.D + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
-                g.rh1[6], true);
-      store_col(ys, ystr, (R *)bf.T + off, ps, L);
-      return;
-    }
-    // temperature: ht += d(-vT)/dy (crosst.f90:633-636,677)
-    SEG_SOLVE((const R *)bf.R2 + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
+    // d/dy (dH1/dx + dH3/dz) (cross.f90:565-575)
+    SEG_SOLVE((const R *)bf.D + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
               g.rh1[6], true);
-    if (L.active) {
-      R *ht = (R *)bf.Ht + off;
-      for (int r = L.r0; r <= L.r1; r++) {
-        const long q = (long)(r - 1) * ps;
-        ht[q] = ht[q] + (R)ys[(r - L.r0) * ystr];
+    store_col(ys, ystr, (R *)bf.T + off, ps, L);
+    if (TEMP) {
+      // temperature: ht += d(-vT)/dy (crosst.f90:633-636,677)
+      SEG_SOLVE((const R *)bf.R2 + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
+                g.rh1[6], true);
+      if (L.active) {
+        R *ht = (R *)bf.Ht + off;
+        for (int r = L.r0; r <= L.r1; r++) {
+          const long q = (long)(r - 1) * ps;
+          ht[q] = ht[q] + (R)ys[(r - L.r0) * ystr];
+        }
       }
     }
     return;
@@ -257,9 +260,10 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs 
     store_col(ys, ystr, (R *)bf.S + off, ps, L);
     return;
   }
-  if (TEMP && L.role == 3) {
-    // temperature: lap(tb) = d2(tb)/dy2 - k^2 tb, shared by the thermal
-    // diffusion and the buoyancy term (visc3d, crosst.f90:734-738)
+  if (TEMP) {
+    // temperature, beside the omega_y update of this role: lap(tb) =
+    // d2(tb)/dy2 - k^2 tb, shared by the thermal diffusion and the buoyancy
+    // term (visc3d, crosst.f90:734-738)
     SEG_SOLVE((const R *)bf.tb + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
               g.rh2[6], false);
     if (L.active) {
@@ -271,7 +275,6 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineA(Grid g, Bufs 
         lt[q] = (R)(-(k2 * (double)tb[q]) + ys[(r - L.r0) * ystr]);
       }
     }
-    return;
   }
   // role 1: hg += nu*lap(omega_y) (visc3d, cross.f90:659), RK3 update, remaps.
   // d2(omega_y)/dy2 of the substep's starting state was taken by k_lineB of the
@@ -342,7 +345,7 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs 
   const bool is00 = (i == 0 && k == 0);
   if (TEMP && L.role == 2) {
     // temperature: ht + fkappa lap(tb), RK3 update of tb, zeta store and
-    // moving_frame_t remaps (crosst.f90:677,734-735,782-872); nothing in the
+    // moving_frame_t remaps (crosst.f90:734-735,782-872); nothing in the
     // prologue
     if (mode >= 1) {
       const double *mf1 = bf.mf1 + (long)L.b * 2 * N * g.nkx + 2 * i;
@@ -919,7 +922,7 @@ static cudaError_t prepare_line_t(const Grid &g) {
 
 template <typename R>
 static cudaError_t lineA_t(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
-  const unsigned nb = (unsigned)(g.B * ((g.temp ? 5 : 3) * g.ngrp + 1));
+  const unsigned nb = (unsigned)(g.B * (3 * g.ngrp + 1));
   if (g.temp)
     k_lineA<R, true><<<nb, kLineT, smem_of(g), st>>>(g, bf, rk);
   else
