@@ -139,6 +139,20 @@ int sb_crosst(sb_handle *h, double *vor, double *phi, double *u00, double *w00, 
               double *tb00, double *time, double *xoffb, double *xofft, int nstep,
               sb_status *st);
 
+/* Statistics that hist accumulated over the last sb_step call (module
+ * statistics, mod.f90:94-115; reset at the entry of every call,
+ * cross.f90:139-155): per y plane the 23 quantities of stats and their
+ * Delta t-weighted sums stats2 (hist 'f' and 'p', cross.f90:1830-1955,
+ * 2038-2048; layout [my][23]), the kx-kz spectra spl and spl2 of uu, vv, ww,
+ * uv, o1o1, o2o2, o3o3, o1o2 (cross.f90:1970-2014; layout [mz][nkx][8]), with
+ * the temperature tstats [my][5] and splt [mz][nkx][4] (crosst.f90:2201-2205,
+ * 2364-2374), the number of records nacum and their summed Delta t total_dt
+ * (cross.f90:2070-2072).  The Delta t weights of a record are those of the
+ * step before it, as in the reference.  Any pointer may be NULL. */
+int sb_get_statistics(sb_handle *h, int member, double *stats, double *stats2, double *spec,
+                      double *spec2, double *tstats, double *tspec, int *nacum,
+                      double *total_dt);
+
 /* The uner(1:10) and uner2(1:4) of the last statistics record of a member
  * (the quantities hist 'w' writes, cross.f90:2064-2118). */
 int sb_stats(sb_handle *h, int member, double *uner, double *uner2);

@@ -72,6 +72,7 @@ def lib():
         L.orc_cross.restype = ctypes.c_int
         L.orc_cross.argtypes = [ctypes.c_void_p, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int,
                                 dp, ip, ip, dp]
+        L.orc_statistics.argtypes = [ctypes.c_void_p, dp, dp, dp, dp, dp, dp, ip, dp]
         L.orc_crosst.restype = ctypes.c_int
         L.orc_crosst.argtypes = [ctypes.c_void_p, dp, dp, dp, dp, dp, dp, dp, dp, dp,
                                  ctypes.c_int, dp, ip, ip, dp]
@@ -158,6 +159,22 @@ class Oracle:
                            _dp(np.ascontiguousarray(state["u00"], np.float64)),
                            _dp(np.ascontiguousarray(state["w00"], np.float64)),
                            float(state["xoffb"]), float(state["xofft"]), int(mask), _dp(out))
+        return out
+
+    def statistics(self) -> dict:
+        """The hist accumulators of the last cross call: stats, stats2 (my, 23),
+        spec, spec2 (mz, nkx, 8), tstats (my, 5), tspec (mz, nkx, 4), nacum,
+        total_dt (reference arrays with the first index fastest)."""
+        my, nkx, mz = self.my, self.nkx, self.mz
+        out = {"stats": np.zeros((my, 23)), "stats2": np.zeros((my, 23)),
+               "spec": np.zeros((mz, nkx, 8)), "spec2": np.zeros((mz, nkx, 8)),
+               "tstats": np.zeros((my, 5)), "tspec": np.zeros((mz, nkx, 4))}
+        n = ctypes.c_int(0)
+        t = ctypes.c_double(0.0)
+        lib().orc_statistics(self.h, *[_dp(out[k]) for k in ("stats", "stats2", "spec", "spec2",
+                                                            "tstats", "tspec")],
+                             ctypes.byref(n), ctypes.byref(t))
+        out["nacum"], out["total_dt"] = n.value, t.value
         return out
 
     def rfty(self, u: np.ndarray, iopt: int) -> np.ndarray:

@@ -209,6 +209,14 @@ typedef struct {
   double Deltag;  /* LES grid-filter width (dx*dy*dz)^(1/3), initcr.f90:510 */
   double max_nut; /* LES running maximum of |nuSGS| (module LES; cross.f90:1433
                    * never resets it, so it spans every call on this context) */
+  /* statistics accumulated by hist over the last cross call (module statistics,
+   * mod.f90:94-115; reset at the call's entry, cross.f90:139-155):
+   * stats/stats2 (23, 0:my1), spectra spl/spl2 (8, 0:mx1, 0:mz1), the
+   * temperature's tstats (5, 0:my1) and splt (4, 0:mx1, 0:mz1), Fortran
+   * order (first index fastest) */
+  double *stats, *stats2, *spec, *spec2, *tstats, *tspec;
+  int nacum;
+  double total_dt;
 } ctx;
 
 #define A7(a, d) ((a)[(d) + 3])
@@ -1034,6 +1042,8 @@ void orc_destroy(void *h) {
   free(c->e1); free(c->f1); free(c->g1); free(c->ce1); free(c->cf1); free(c->cg1);
   free(c->a2); free(c->b2); free(c->c2); free(c->d2); free(c->d2m1);
   free(c->e2); free(c->f2); free(c->g2); free(c->ce2); free(c->cf2); free(c->cg2);
+  free(c->stats); free(c->stats2); free(c->spec); free(c->spec2); free(c->tstats);
+  free(c->tspec);
   free(c->fa); free(c->fb); free(c->fc); free(c->fd); free(c->fdm1);
   free(c->fe); free(c->ff); free(c->fg); free(c->fce); free(c->fcf); free(c->fcg);
   plan_free(&c->px);
@@ -1143,6 +1153,8 @@ typedef struct {
   double umaxl[4];
   double tbmaxl, enert[4]; /* temperature: max |tb| and tbp, utbp, vtbp, wtbp */
   double numax; /* LES: max |nuSGS| of the plane (cross.f90:1433) */
+  double vuu, vww, vvv; /* hist 'p' sums of the plane (cross.f90:2038-2042) */
+  double *spec, *tspec; /* the plane's spectra contributions (8 or 4, nkx, mz) */
 } plane_red;
 
 /* per-line complex pointer into a pencil array: line (i,k) */
@@ -1150,7 +1162,8 @@ typedef struct {
 
 /* hist, flag 'f' (cross.f90:1796-1963): intensities, Pk, eps for plane j */
 static void hist_f(ctx *c, pthread_buf *b, const cplx *dv, double *ener, double *ener2,
-                   double txy00j, const cplx *tbc, double *enert) {
+                   double txy00j, const cplx *tbc, double *enert, double *spec,
+                   double *tspec) {
   int nkx = c->nkx, mz = c->mz;
   double s = c->p.s;
   cplx *u1c = b->u1c, *u2c = b->u2c, *u3c = b->u3c, *o1c = b->o1c, *o2c = b->o2c,
@@ -1182,6 +1195,31 @@ static void hist_f(ctx *c, pthread_buf *b, const cplx *dv, double *ener, double 
   SUMSQ(o2c, o2p);
   SUMSQ(o3c, o3p);
   SUMCJ(o1c, o2c, o12p);
+  if (spec) {
+    /* spectra for HSF, nspec = 8 (cross.f90:1970-1994): o3c(0,0) without -s */
+    for (int k = 0; k < mz; k++)
+      for (int i = 0; i < nkx; i++) {
+        int q = k * nkx + i;
+        double w = (i == 0) ? 1.0 : 2.0;
+        double *sp = spec + 8 * (size_t)q;
+        sp[0] = w * cabs2(u1c[q]);
+        sp[1] = w * cabs2(u2c[q]);
+        sp[2] = w * cabs2(u3c[q]);
+        sp[3] = w * crecj(u1c[q], u2c[q]);
+        sp[4] = w * cabs2(o1c[q]);
+        sp[5] = w * cabs2(o2c[q]);
+        sp[6] = w * cabs2(o3c[q]);
+        sp[7] = w * crecj(o1c[q], o2c[q]);
+        if (tbc && tspec) {
+          /* splt (crosst.f90:2364-2374) */
+          double *st = tspec + 4 * (size_t)q;
+          st[0] = w * cabs2(tbc[q]);
+          st[1] = w * crecj(u1c[q], tbc[q]);
+          st[2] = w * crecj(u2c[q], tbc[q]);
+          st[3] = w * crecj(u3c[q], tbc[q]);
+        }
+      }
+  }
   if (tbc) {
     /* histt (crosst.f90:2151-2160, 2207-2210) */
     double tbp, utbp, vtbp, wtbp;
@@ -1409,7 +1447,8 @@ static void hvhg_plane(ctx *c, pthread_buf *b, int j, const cplx *phic, const cp
   if (c->p.les)
     les_plane(c, b, rhvc, rhvc1, rhvc2, rhgc1, rhgc2, &txy00[j], &tyz00[j], rkstep, red);
   if (ihist)
-    hist_f(c, b, rhvc, red->ener, red->ener2, c->p.les ? txy00[j] : 0.0, tbc, red->enert);
+    hist_f(c, b, rhvc, red->ener, red->ener2, c->p.les ? txy00[j] : 0.0, tbc, red->enert,
+           red->spec, red->tspec);
   fourxz(c, b, u1c, b->u1r, 1);
   fourxz(c, b, u2c, b->u2r, 1);
   fourxz(c, b, u3c, b->u3r, 1);
@@ -1419,6 +1458,20 @@ static void hvhg_plane(ctx *c, pthread_buf *b, int j, const cplx *phic, const cp
   if (tbc) fourxz(c, b, tbc, b->tbr, 1);
   double *u1r = b->u1r, *u2r = b->u2r, *u3r = b->u3r, *o1r = b->o1r, *o2r = b->o2r,
          *o3r = b->o3r;
+  if (ihist) {
+    /* hist 'p' (cross.f90:2038-2042): the velocity without the mean shear */
+    double a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    for (int z = 0; z < mgalz; z++)
+      for (int x = 0; x < mgalx; x++) {
+        int q = z * ld + x;
+        a1 += u2r[q] * (u1r[q] * u1r[q]);
+        a2 += u2r[q] * (u3r[q] * u3r[q]);
+        a3 += u2r[q] * u2r[q] * u2r[q];
+      }
+    red->vuu = a1;
+    red->vww = a2;
+    red->vvv = a3;
+  }
   if (rkstep == 1) {
     double m0 = red->umaxl[0], m1 = red->umaxl[1], m2 = red->umaxl[2], m3 = red->umaxl[3];
     double sy = s * c->y[j];
@@ -1827,6 +1880,18 @@ static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00,
   double *rf0u = dalloc(my), *rf0w = dalloc(my), *u00wk = dalloc(my), *w00wk = dalloc(my);
   double *rf0u_d = dalloc(my), *rf0w_d = dalloc(my), *wk1dr = dalloc(my);
   plane_red *red = (plane_red *)calloc((size_t)my, sizeof(plane_red));
+  /* per-plane spectra contributions, summed over the planes in order */
+  double *specj = dalloc((size_t)my * 8 * nplane);
+  double *tspecj = tb ? dalloc((size_t)my * 4 * nplane) : NULL;
+  /* statistics of this call start from zero (cross.f90:139-155) */
+  const size_t nst = 23 * (size_t)my, nsp = 8 * nplane;
+  free(c->stats); free(c->stats2); free(c->spec); free(c->spec2); free(c->tstats);
+  free(c->tspec);
+  c->stats = dalloc(nst); c->stats2 = dalloc(nst);
+  c->spec = dalloc(nsp); c->spec2 = dalloc(nsp);
+  c->tstats = dalloc(5 * (size_t)my); c->tspec = dalloc(4 * nplane);
+  c->nacum = 0;
+  c->total_dt = 0.0;
   /* LES buffers rhvc1, rhvc2, rhgc1, rhgc2 (pencil and plane) and T12, T23 of
    * the (0,0) mode (cross.f90:242-247) */
   int les = c->p.les;
@@ -1948,6 +2013,8 @@ static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00,
         if (istep == 1 && c->p.readflag == 0) uinit = (fabs(s) > 0.5) ? 1.0 : c->p.uprim;
         for (int j = 0; j < my; j++) {
           memset(&red[j], 0, sizeof(plane_red));
+          red[j].spec = specj + (size_t)j * 8 * nplane;
+          red[j].tspec = tspecj ? tspecj + (size_t)j * 4 * nplane : NULL;
         }
 #pragma omp parallel for schedule(static)
         for (int j = 0; j < my; j++) {
@@ -1958,6 +2025,54 @@ static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00,
                      les ? lq[1] + o : NULL, les ? lq[2] + o : NULL, les ? lq[3] + o : NULL,
                      txy00, tyz00, temp ? b3 + o : NULL, tb00, temp ? pht + o : NULL,
                      temp ? prt2 + o : NULL, rf0tb);
+        }
+        if (ihist) {
+          /* hist 'f' and 'p' accumulations with the Deltat of the previous
+           * step (cross.f90:1830-1994, 2038-2048; crosst.f90:2201-2205,
+           * 2364-2374) */
+          for (int j = 0; j < my; j++) {
+            const plane_red *r = &red[j];
+            double v[23];
+            v[0] = u00[j];
+            v[1] = c->p.vbulk;
+            v[2] = w00[j];
+            for (int q = 0; q < 6; q++) v[3 + q] = r->ener[q];
+            v[9] = rf0w_d[j];
+            v[10] = b2[(size_t)j * nplane].re;
+            v[11] = -rf0u_d[j];
+            for (int q = 0; q < 3; q++) v[12 + q] = r->ener[6 + q];
+            v[15] = r->ener[9];
+            v[16] = r->vuu;
+            v[17] = r->vww;
+            v[18] = r->vvv;
+            v[19] = r->ener2[0];
+            v[20] = r->ener2[1];
+            v[21] = les ? r->ener2[2] : 0.0;
+            v[22] = les ? r->ener2[3] : 0.0;
+            for (int q = 0; q < 23; q++) {
+              c->stats[23 * (size_t)j + q] += v[q];
+              c->stats2[23 * (size_t)j + q] += v[q] * Deltat;
+            }
+            if (temp) {
+              double *ts = c->tstats + 5 * (size_t)j;
+              ts[0] += tb00[j] * Deltat;
+              for (int q = 0; q < 4; q++) ts[1 + q] += r->enert[q] * Deltat;
+            }
+          }
+          for (size_t q = 0; q < nsp; q++) {
+            double a = 0.0, a2 = 0.0;
+            for (int j = 0; j < my; j++) {
+              a += specj[(size_t)j * nsp + q];
+              a2 += specj[(size_t)j * nsp + q] * Deltat;
+            }
+            /* spl is over (8, kx, kz) with the field fastest, as here */
+            c->spec[q] += a;
+            c->spec2[q] += a2;
+          }
+          if (temp)
+            for (size_t q = 0; q < 4 * nplane; q++)
+              for (int j = 0; j < my; j++)
+                c->tspec[q] += tspecj[(size_t)j * 4 * nplane + q] * Deltat;
         }
         if (rkstep == 1) {
           double ul[4] = {uinit, uinit, uinit, uinit};
@@ -2070,6 +2185,9 @@ static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00,
             }
           }
           nt++;
+          /* counts of the accumulated fields (cross.f90:2070-2072) */
+          c->nacum++;
+          c->total_dt += Deltat;
           if (isnan(uner[0])) istop = 1;
           if (uner[1] / c->Lz < 1e-5 && !c->p.keep_laminar) istop = 1;
           ihist = 0;
@@ -2266,6 +2384,7 @@ static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00,
   }
   free(txy00); free(tyz00);
   free(rf0tb); free(tb00wk); free(tbwk); free(ht); free(rt2); free(b3); free(pht); free(prt2);
+  free(specj); free(tspecj);
   return done;
 }
 
@@ -2274,6 +2393,25 @@ int orc_cross(void *h, double *vor, double *phi, double *u00, double *w00, doubl
               int *pistop, double *pdeltat) {
   return cross_run((ctx *)h, vor, phi, u00, w00, NULL, NULL, ptime, pxoffb, pxofft, nstep,
                    trace, ntrace, pistop, pdeltat);
+}
+
+void orc_statistics(void *h, double *stats, double *stats2, double *spec, double *spec2,
+                    double *tstats, double *tspec, int *nacum, double *total_dt) {
+  ctx *c = (ctx *)h;
+  const size_t nst = 23 * (size_t)c->my, nsp = 8 * (size_t)c->nkx * c->mz;
+  if (!c->stats) {
+    if (nacum) *nacum = 0;
+    if (total_dt) *total_dt = 0.0;
+    return;
+  }
+  if (stats) memcpy(stats, c->stats, nst * sizeof(double));
+  if (stats2) memcpy(stats2, c->stats2, nst * sizeof(double));
+  if (spec) memcpy(spec, c->spec, nsp * sizeof(double));
+  if (spec2) memcpy(spec2, c->spec2, nsp * sizeof(double));
+  if (tstats) memcpy(tstats, c->tstats, 5 * (size_t)c->my * sizeof(double));
+  if (tspec) memcpy(tspec, c->tspec, nsp / 2 * sizeof(double));
+  if (nacum) *nacum = c->nacum;
+  if (total_dt) *total_dt = c->total_dt;
 }
 
 int orc_crosst(void *h, double *vor, double *phi, double *u00, double *w00, double *tb,

@@ -75,6 +75,14 @@ int orc_crosst(void *h, double *vor, double *phi, double *u00, double *w00, doub
                double *tb00, double *time, double *xoffb, double *xofft, int nstep,
                double *trace, int *ntrace, int *istop, double *deltat);
 
+/* statistics accumulated over the last cross/crosst call (hist 'f', 'p', 'w',
+ * cross.f90:1796-2121; crosst.f90:2201-2210,2364-2374): stats and stats2
+ * (23 x my), spectra spec and spec2 (8 x nkx x mz), the temperature's tstats
+ * (5 x my) and tspec (4 x nkx x mz), first index fastest; any pointer may be
+ * NULL */
+void orc_statistics(void *h, double *stats, double *stats2, double *spec, double *spec2,
+                    double *tstats, double *tspec, int *nacum, double *total_dt);
+
 /* building blocks, one y-line (complex: m=2, real: m=1) */
 void orc_filterc(void *h, const double *u, double *du, double shp_re, double shp_im, int m);
 /* rfty / cfty on one y-line (packed real line of my+2 doubles, or complex) */

@@ -81,7 +81,7 @@ ABI_FUNCTIONS = [
     "sb_fp64_peak", "sb_op_derivyc", "sb_op_lapcdy", "sb_op_derivyc_noalloc",
     "sb_set_member_etime", "sb_op_filterc", "sb_op_cfty", "sb_op_rfty", "sb_write_restart",
     "sb_read_restart", "sb_autotune", "sb_physical_fields", "sb_set_temperature",
-    "sb_get_temperature", "sb_crosst", "sb_stats", "sb_jv_batch",
+    "sb_get_temperature", "sb_crosst", "sb_stats", "sb_jv_batch", "sb_get_statistics",
 ]
 
 _lib = None
@@ -116,6 +116,7 @@ def lib(auto_build: bool = False):
                             ctypes.POINTER(SbStatus)]
     L.sb_set_temperature.argtypes = [vp, ctypes.c_int, dp, dp]
     L.sb_stats.argtypes = [vp, ctypes.c_int, dp, dp]
+    L.sb_get_statistics.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp, dp, dp, ip, dp]
     L.sb_jv_batch.argtypes = [vp, dp, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                               ctypes.c_double, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int,
                               dp]
@@ -303,6 +304,23 @@ class ShearBox:
         c = (ctypes.c_int * 3)()
         _check(lib().sb_autotune(self.h, c))
         return {"p1_cols": c[0], "p3_cols": c[1], "p2_threads": c[2]}
+
+    def statistics(self, member: int = 0) -> dict:
+        """The hist accumulators of the last step call (sb_get_statistics):
+        stats, stats2 (my, 23), spec, spec2 (mz, nkx, 8), with the temperature
+        tstats (my, 5) and tspec (mz, nkx, 4), nacum, total_dt."""
+        my, nkx, mz = self.p.my, self.sz["nkx"], self.sz["mz"]
+        out = {"stats": np.zeros((my, 23)), "stats2": np.zeros((my, 23)),
+               "spec": np.zeros((mz, nkx, 8)), "spec2": np.zeros((mz, nkx, 8))}
+        if self.p.temperature:
+            out["tstats"], out["tspec"] = np.zeros((my, 5)), np.zeros((mz, nkx, 4))
+        n = ctypes.c_int(0)
+        t = ctypes.c_double(0.0)
+        ptr = [(_dp(out[k]) if k in out else None)
+               for k in ("stats", "stats2", "spec", "spec2", "tstats", "tspec")]
+        _check(lib().sb_get_statistics(self.h, int(member), *ptr, ctypes.byref(n), ctypes.byref(t)))
+        out["nacum"], out["total_dt"] = n.value, t.value
+        return out
 
     def stats(self, member: int = 0):
         """(uner[10], uner2[4]) of the member's last statistics record."""

@@ -52,6 +52,8 @@ struct sb_handle {
   // beside plane stage 3, which they do not depend on
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // the spectra of a statistics step run beside plane stages 1-2
+  cudaEvent_t ev_s0 = nullptr, ev_s1 = nullptr;
   cudaGraphExec_t step_exec = nullptr;
   std::vector<void *> allocs;
   double *d_pen = nullptr;  // staging buffer, one pencil-layout field
@@ -169,8 +171,16 @@ static int capture_step(sb_handle *h) {
         ((e = launch_ydeal(h->g, h->bf, rk, h->st)) != cudaSuccess ||
          (e = launch_meand1(h->g, h->bf, h->st)) != cudaSuccess))
       break;
+    if (rk == 1 &&
+        ((e = cudaEventRecord(h->ev_s0, h->st)) != cudaSuccess ||
+         (e = cudaStreamWaitEvent(h->side, h->ev_s0, 0)) != cudaSuccess ||
+         (e = launch_spectra(h->g, h->bf, h->side)) != cudaSuccess ||
+         (e = cudaEventRecord(h->ev_s1, h->side)) != cudaSuccess))
+      break;
     if ((e = launch_plane(h->g, h->bf, 1, rk, h->st)) != cudaSuccess) break;
     if ((e = launch_plane(h->g, h->bf, 2, rk, h->st)) != cudaSuccess) break;
+    // plane stage 3 overwrites inputs of the spectra
+    if (rk == 1 && (e = cudaStreamWaitEvent(h->st, h->ev_s1, 0)) != cudaSuccess) break;
     if (h->g.les)
       for (int q = 2; q <= 4 && e == cudaSuccess; q++) e = launch_les(h->g, h->bf, q, rk, h->st);
     if (e != cudaSuccess) break;
@@ -412,6 +422,8 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->ev_s0, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->ev_s1, cudaEventDisableTiming);
   if (ce != cudaSuccess) {
     sb_destroy(h);
     return fail(3, "stream: %s", cudaGetErrorString(ce));
@@ -432,6 +444,13 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
       (rc = A(&bf.hpart, B * my * ((g.nkx + 3) / 4) * SB_NHIST_Q)) || (rc = A(&bf.sh_old, B * 4 * g.nkx)) ||
       (rc = A(&bf.sh_new, B * 4 * g.nkx)) || (rc = A(&bf.mf1, B * my * g.nkx * 2)) ||
       (rc = A(&bf.mf2, B * my * g.nkx * 2)) || (rc = A(&h->d_pen, F))) {
+    sb_destroy(h);
+    return rc;
+  }
+  if ((rc = A(&bf.stats, B * my * 23)) || (rc = A(&bf.stats2, B * my * 23)) ||
+      (rc = A(&bf.spec, B * g.nkx * g.mz * 8)) || (rc = A(&bf.spec2, B * g.nkx * g.mz * 8)) ||
+      (rc = A(&bf.ppart, B * my * (g.mgalz / 2) * 3)) ||
+      (g.temp && ((rc = A(&bf.tstats, B * my * 5)) || (rc = A(&bf.tspec, B * g.nkx * g.mz * 4))))) {
     sb_destroy(h);
     return rc;
   }
@@ -597,6 +616,8 @@ int sb_destroy(sb_handle *h) {
   if (h->side) cudaStreamDestroy(h->side);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->ev_s0) cudaEventDestroy(h->ev_s0);
+  if (h->ev_s1) cudaEventDestroy(h->ev_s1);
   delete h;
   return 0;
 }
@@ -817,6 +838,34 @@ int sb_cross(sb_handle *h, double *vor, double *phi, double *u00, double *w00, d
   if ((rc = sb_step(h, nstep))) return rc;
   if ((rc = sb_get_state(h, 0, vor, phi, u00, w00, time, xoffb, xofft))) return rc;
   if (st && (rc = sb_get_status(h, 0, st))) return rc;
+  return 0;
+}
+
+int sb_get_statistics(sb_handle *h, int member, double *stats, double *stats2, double *spec,
+                      double *spec2, double *tstats, double *tspec, int *nacum,
+                      double *total_dt) {
+  if (!h || member < 0 || member >= h->g.B) return fail(1, "bad handle or member");
+  if ((tstats || tspec) && !h->g.temp) return fail(2, "the handle has no temperature");
+  const Grid &g = h->g;
+  const size_t nst = (size_t)g.my * 23, nsp = (size_t)g.nkx * g.mz * 8;
+  auto get = [&](double *dst, const double *src, size_t n) -> cudaError_t {
+    if (!dst) return cudaSuccess;
+    return cudaMemcpyAsync(dst, src + (size_t)member * n, sizeof(double) * n,
+                           cudaMemcpyDeviceToHost, h->st);
+  };
+  CK(get(stats, h->bf.stats, nst));
+  CK(get(stats2, h->bf.stats2, nst));
+  CK(get(spec, h->bf.spec, nsp));
+  CK(get(spec2, h->bf.spec2, nsp));
+  if (g.temp) {
+    CK(get(tstats, h->bf.tstats, (size_t)g.my * 5));
+    CK(get(tspec, h->bf.tspec, nsp / 2));
+  }
+  Member m;
+  CK(cudaMemcpyAsync(&m, h->bf.mem + member, sizeof(Member), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  if (nacum) *nacum = m.nacum;
+  if (total_dt) *total_dt = m.total_dt;
   return 0;
 }
 

@@ -99,6 +99,8 @@ struct Member {
   double cflkk;                     // temperature: thermal-diffusion CFL factor (initcr.f90:498-502)
   double tbmax;                     // temperature: max |tb| of this step
   unsigned long long tbmax_bits;
+  double total_dt;                  // statistics: summed Delta t of the records (cross.f90:2072)
+  int nacum;                        // statistics: records accumulated in this call
   int istop, idump, ihist, istep, halted, ntrace, trace_cap, flags;
 };
 
@@ -144,6 +146,11 @@ struct Bufs {
   // Laplacian of tb (d2/dy2 - k^2) tb; mean profile tb00 [B][my] complex (re),
   // its RK work array and d(-vT_00)/dy
   double *tb, *tbwk, *Ht, *R2, *Lt, *mt, *mtwk, *mtr;
+  // statistics accumulated by hist over one call (module statistics,
+  // mod.f90:94-115): stats, stats2 [B][my][23]; spectra spl, spl2
+  // [B][mz][nkx][8]; temperature tstats [B][my][5], splt [B][mz][nkx][4];
+  // hist 'p' plane partials [B][my][mgalz/2][3]
+  double *stats, *stats2, *spec, *spec2, *tstats, *tspec, *ppart;
 };
 
 }  // namespace sb

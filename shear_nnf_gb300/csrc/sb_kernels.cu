@@ -296,6 +296,100 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
 }
 
 // ---------------------------------------------------------------------------
+// hist spectra for HSF (nspec = 8: uu vv ww uv o1o1 o2o2 o3o3 o1o2,
+// cross.f90:1970-1994) and, with the temperature, splt (tt ut vt wt,
+// crosst.f90:2364-2374) at the first substep of a statistics step: one thread
+// per (kx, kz) mode of a box sums the products over the planes in order, from
+// the substep's starting state (the inputs of plane stage 1, reconstructed as
+// there).  Runs before the per-box scalars update Delta t: spl2 and splt are
+// weighted by the Delta t of the previous step, as in hist 'f'.
+// ---------------------------------------------------------------------------
+template <typename R, bool TEMP>
+__global__ void __launch_bounds__(128) k_spectra(Grid g, Bufs bf) {
+  typedef typename Vec2<R>::t V;
+  const int b = blockIdx.y;
+  const Member &M = bf.mem[b];
+  if (M.halted || !M.ihist) return;
+  const int nkx = g.nkx, mz = g.mz, nz = g.nz, nl = nkx * mz;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nl) return;
+  const int i = q % nkx, k = q / nkx;
+  const double a = g.alp * i;
+  const double gz = g.gam * ((k <= nz) ? k : k - mz);
+  const double iK = bf.kinv[q];
+  const double w = (i == 0) ? 1.0 : 2.0;
+  const bool z00 = (i == 0 && k == 0);
+  // set_conj of the omega_y and phi copies (cross.f90:502)
+  const int qs = (i == 0 && k > nz) ? (mz - k) * nkx : q;
+  const double cs = (i == 0 && k > nz) ? -1.0 : 1.0;
+  double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, tacc[4] = {0, 0, 0, 0};
+  for (int j = 0; j < g.my; j++) {
+    const long pb = (long)b * g.field + (long)j * g.plane;
+    const V *vor = (const V *)((const R *)bf.vor + pb), *phi = (const V *)((const R *)bf.phi + pb);
+    const V *Dv = (const V *)((const R *)bf.D + pb), *Vv = (const V *)((const R *)bf.V + pb);
+    const V *Gv = (const V *)((const R *)bf.G + pb);
+    const V vr0 = vor[qs], ph0 = phi[qs];
+    const double vrx = vr0.x, vry = cs * (double)vr0.y, phx = ph0.x, phy = cs * (double)ph0.y;
+    double u1x, u1y, u2x, u2y, u3x, u3y, o1x, o1y, o3x, o3y;
+    if (z00) {
+      const V mu = ((const V *)bf.mu)[(long)b * g.my + j];
+      const V mdu = ((const V *)bf.mdu)[(long)b * g.my + j];
+      u1x = mu.x; u1y = 0.0;
+      u3x = mu.y; u3y = 0.0;
+      o3x = -(double)mdu.x; o3y = 0.0;
+      o1x = mdu.y; o1y = 0.0;
+      u2x = M.vbulk; u2y = 0.0;
+    } else {
+      const V w1 = Dv[q], dv = Vv[q], gv = Gv[q];
+      double tx, ty;
+      tx = gz * w1.x - a * phx; ty = gz * w1.y - a * phy;
+      o3x = -ty * iK; o3y = tx * iK;
+      tx = a * w1.x + gz * phx; ty = a * w1.y + gz * phy;
+      o1x = -ty * iK; o1y = tx * iK;
+      tx = gz * dv.x + a * vrx; ty = gz * dv.y + a * vry;
+      u3x = -ty * iK; u3y = tx * iK;
+      tx = a * dv.x - gz * vrx; ty = a * dv.y - gz * vry;
+      u1x = -ty * iK; u1y = tx * iK;
+      u2x = gv.x; u2y = gv.y;
+    }
+    acc[0] += w * (u1x * u1x + u1y * u1y);
+    acc[1] += w * (u2x * u2x + u2y * u2y);
+    acc[2] += w * (u3x * u3x + u3y * u3y);
+    acc[3] += w * (u1x * u2x + u1y * u2y);
+    acc[4] += w * (o1x * o1x + o1y * o1y);
+    acc[5] += w * (vrx * vrx + vry * vry);
+    acc[6] += w * (o3x * o3x + o3y * o3y);
+    acc[7] += w * (o1x * vrx + o1y * vry);
+    if (TEMP) {
+      double tx = 0.0, ty = 0.0;
+      if (z00) {
+        tx = ((const V *)bf.mt)[(long)b * g.my + j].x;
+      } else {
+        const V t = ((const V *)((const R *)bf.tb + pb))[q];
+        tx = t.x;
+        ty = t.y;
+      }
+      tacc[0] += w * (tx * tx + ty * ty);
+      tacc[1] += w * (u1x * tx + u1y * ty);
+      tacc[2] += w * (u2x * tx + u2y * ty);
+      tacc[3] += w * (u3x * tx + u3y * ty);
+    }
+  }
+  const double dt = M.Deltat;
+  double *sp = bf.spec + ((long)b * nl + q) * 8, *sp2 = bf.spec2 + ((long)b * nl + q) * 8;
+#pragma unroll
+  for (int f = 0; f < 8; f++) {
+    sp[f] += acc[f];
+    sp2[f] += acc[f] * dt;
+  }
+  if (TEMP) {
+    double *st = bf.tspec + ((long)b * nl + q) * 4;
+#pragma unroll
+    for (int f = 0; f < 4; f++) st[f] += tacc[f] * dt;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // plane stage 2: x-transforms and u x omega on pairs of z rows
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned long long dbits(double v) {
@@ -339,9 +433,18 @@ __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
   const R chi2 = (R)(2.0 * g.chi);
   const R sy = (R)(g.s * ((double)j * g.dy - 0.5 * g.Ly));
   R m0 = 0, m1 = 0, m2 = 0, m3 = 0, mt = 0;
+  // hist 'p' (cross.f90:2038-2042): v u^2, v w^2, v^3 over the two rows
+  const bool hist = (rk == 1) && M.ihist;
+  double s1 = 0.0, s2 = 0.0, s3 = 0.0;
   for (int x = threadIdx.x; x < NX; x += T) {
     const V u1 = P[0 * NX + x], u3 = P[1 * NX + x], o1 = P[2 * NX + x], o3 = P[3 * NX + x],
             u2 = P[4 * NX + x], o2 = P[5 * NX + x];
+    if (hist) {
+      const double ax = u1.x, ay = u1.y, vx = u2.x, vy = u2.y, wx = u3.x, wy = u3.y;
+      s1 += vx * (ax * ax) + vy * (ay * ay);
+      s2 += vx * (wx * wx) + vy * (wy * wy);
+      s3 += vx * vx * vx + vy * vy * vy;
+    }
     if (rk == 1) {
       m0 = fmax(m0, fmax(fabs(u1.x), fabs(u1.y)));
       m1 = fmax(m1, fmax(fabs(u1.x + sy), fabs(u1.y + sy)));
@@ -384,6 +487,26 @@ __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
       unsigned long long bt = dbits(mt);
       for (int o = 16; o > 0; o >>= 1) bt = max(bt, __shfl_xor_sync(0xffffffffu, bt, o));
       if ((threadIdx.x & 31) == 0) atomicMax(&M.tbmax_bits, bt);
+    }
+  }
+  if (hist) {
+    // block sums in a fixed order, one triple per (plane, row pair)
+    __shared__ double sred[3][T / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+      s1 += __shfl_down_sync(0xffffffffu, s1, o);
+      s2 += __shfl_down_sync(0xffffffffu, s2, o);
+      s3 += __shfl_down_sync(0xffffffffu, s3, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      sred[0][threadIdx.x >> 5] = s1;
+      sred[1][threadIdx.x >> 5] = s2;
+      sred[2][threadIdx.x >> 5] = s3;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+      double v = 0.0;
+      for (int w = 0; w < T / 32; w++) v += sred[threadIdx.x][w];
+      bf.ppart[(((long)b * g.my + j) * (g.mgalz / 2) + zp) * 3 + threadIdx.x] = v;
     }
   }
   V *Rr = fft_batch<NX, -1, NO, T>(Q, P, (const V *)tw_of<R>(bf, false));
@@ -1357,6 +1480,17 @@ static cudaError_t launch_phys_r(const Grid &g, const Bufs &bf, unsigned mask, d
 }
 
 template <typename R>
+static cudaError_t launch_spectra_t(const Grid &g, const Bufs &bf, cudaStream_t st) {
+  const int nl = g.nkx * g.mz;
+  const dim3 grid((unsigned)((nl + 127) / 128), (unsigned)g.B);
+  if (g.temp)
+    k_spectra<R, true><<<grid, 128, 0, st>>>(g, bf);
+  else
+    k_spectra<R, false><<<grid, 128, 0, st>>>(g, bf);
+  return cudaGetLastError();
+}
+
+template <typename R>
 static cudaError_t launch_p2p_t(const Grid &g, const double *pen, double *dst, cudaStream_t st) {
   k_pencil_to_plane<R><<<256, 256, 0, st>>>(g, pen, (R *)dst);
   return cudaGetLastError();
@@ -1377,6 +1511,7 @@ cudaError_t ydeal_f32(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
 cudaError_t p2p_f32(const Grid &g, const double *pen, double *dst, cudaStream_t st);
 cudaError_t pen_f32(const Grid &g, const double *src, double *pen, cudaStream_t st);
 cudaError_t phys_f32(const Grid &g, const Bufs &bf, unsigned mask, double *out, cudaStream_t st);
+cudaError_t spectra_f32(const Grid &g, const Bufs &bf, cudaStream_t st);
 
 #if SB_FLOAT_TU
 cudaError_t plane_f32(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
@@ -1397,6 +1532,9 @@ cudaError_t pen_f32(const Grid &g, const double *src, double *pen, cudaStream_t 
 cudaError_t phys_f32(const Grid &g, const Bufs &bf, unsigned mask, double *out, cudaStream_t st) {
   return launch_phys_r<float>(g, bf, mask, out, st);
 }
+cudaError_t spectra_f32(const Grid &g, const Bufs &bf, cudaStream_t st) {
+  return launch_spectra_t<float>(g, bf, st);
+}
 #else
 // stage 1..3: launch; stage 0: set the kernels' shared-memory limits (once)
 cudaError_t launch_plane(const Grid &g, const Bufs &bf, int stage, int rk, cudaStream_t st) {
@@ -1414,6 +1552,9 @@ cudaError_t launch_pencil_to_plane(const Grid &g, const double *pen, double *dst
 }
 cudaError_t launch_plane_to_pencil(const Grid &g, const double *src, double *pen, cudaStream_t st) {
   return g.prec ? pen_f32(g, src, pen, st) : launch_pen_t<double>(g, src, pen, st);
+}
+cudaError_t launch_spectra(const Grid &g, const Bufs &bf, cudaStream_t st) {
+  return g.prec ? spectra_f32(g, bf, st) : launch_spectra_t<double>(g, bf, st);
 }
 // one box (Grid with B = 1 and member-offset buffers): plane stage 1 with the
 // extra z-transforms into g's zbuf, then the physical fields

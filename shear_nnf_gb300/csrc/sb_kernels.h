@@ -18,6 +18,7 @@ cudaError_t launch_lineL(const Grid &g, const Bufs &bf, cudaStream_t st);
 cudaError_t launch_filter(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
 cudaError_t launch_ydeal(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
 cudaError_t launch_meand1(const Grid &g, const Bufs &bf, cudaStream_t st);
+cudaError_t launch_spectra(const Grid &g, const Bufs &bf, cudaStream_t st);
 cudaError_t launch_physical(const Grid &g, const Bufs &bf, unsigned mask, double *out,
                             cudaStream_t st);
 bool supported_ylen(int my);

@@ -621,10 +621,28 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
       for (int q = 0; q < 4; q++) M.umax_bits[q] = 0ull;
       M.nut_bits = 0ull;
       M.tbmax_bits = 0ull;
+      M.nacum = 0;
+      M.total_dt = 0.0;
       M.xwb[0] = M.xoffb;
       M.xwt[0] = M.xofft;
     }
     s_halt = M.halted;
+  }
+  if (rk == 0) {
+    // the statistics of a call start from zero (cross.f90:139-155)
+    const long nst = (long)g.my * 23, nsp = (long)g.nkx * g.mz * 8;
+    for (long q = threadIdx.x; q < nst; q += blockDim.x) {
+      bf.stats[b * nst + q] = 0.0;
+      bf.stats2[b * nst + q] = 0.0;
+    }
+    for (long q = threadIdx.x; q < nsp; q += blockDim.x) {
+      bf.spec[b * nsp + q] = 0.0;
+      bf.spec2[b * nsp + q] = 0.0;
+    }
+    if (g.temp) {
+      for (long q = threadIdx.x; q < (long)g.my * 5; q += blockDim.x) bf.tstats[b * g.my * 5L + q] = 0.0;
+      for (long q = threadIdx.x; q < nsp / 2; q += blockDim.x) bf.tspec[b * (nsp / 2) + q] = 0.0;
+    }
   }
   __syncthreads();
   if (s_halt || rk == 0) return;
@@ -645,25 +663,72 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
       for (int cb = 0; cb < g.ncb; cb++)
         for (int q = 0; q < SB_NHIST_Q; q++) pl[q] += hp[cb * SB_NHIST_Q + q];
       for (int q = 0; q < SB_NHIST_Q; q++) acc[q] += pl[q];
-      const double du = g.prec ? (double)((const float *)bf.mdu)[2 * ((long)b * g.my + j)]
-                               : bf.mdu[2 * ((long)b * g.my + j)];
+      const long mj = 2 * ((long)b * g.my + j);
+      auto rdm = [&](const double *p, int c) -> double {
+        return g.prec ? (double)((const float *)p)[mj + c] : p[mj + c];
+      };
+      const double du = rdm(bf.mdu, 0);
       const double o3 = -du - g.s;
+      double Pk, nuty = 0.0, disp = 0.0;
       if (g.les) {
         // Pk with the resolved mean stress (cross.f90:1886-1899), nu_t and the
         // energy transfer to the subgrid scales (cross.f90:1892,1950-1952)
-        const double txy = g.prec ? (double)((const float *)bf.txy)[2 * ((long)b * g.my + j)]
-                                  : bf.txy[2 * ((long)b * g.my + j)];
-        acc[SB_NHIST_Q] += -(o3 * (-pl[3] + txy)) + nufac * (o3 * o3);
+        const double txy = rdm(bf.txy, 0);
+        Pk = -(o3 * (-pl[3] + txy)) + nufac * (o3 * o3);
         const double *lp = bf.lpart + ((long)b * g.my + j) * (g.mgalz / 2) * 2;
         double sn = 0.0, sd = 0.0;
         for (int zp = 0; zp < g.mgalz / 2; zp++) {
           sn += lp[2 * zp];
           sd += lp[2 * zp + 1];
         }
-        acc[SB_NHIST_Q + 1] += sn / nxz;
-        acc[SB_NHIST_Q + 2] += sd / nxz;
+        nuty = sn / nxz;
+        disp = sd / nxz;
+        acc[SB_NHIST_Q + 1] += nuty;
+        acc[SB_NHIST_Q + 2] += disp;
       } else {
-        acc[SB_NHIST_Q] += -o3 * (-pl[3]) + (o3 * o3) * (1.0 / M.Re);
+        Pk = -o3 * (-pl[3]) + (o3 * o3) * (1.0 / M.Re);
+      }
+      acc[SB_NHIST_Q] += Pk;
+      // the plane's statistics (hist 'f', 'p': cross.f90:1830-1955, 2038-2048)
+      // with the Delta t of the previous step
+      double v[23];
+      v[0] = rdm(bf.mu, 0);
+      v[1] = M.vbulk;
+      v[2] = rdm(bf.mu, 1);
+      for (int q = 0; q < 6; q++) v[3 + q] = pl[q];
+      v[9] = rdm(bf.mdu, 1);
+      v[10] = g.prec ? (double)((const float *)bf.vor)[b * g.field + j * g.plane]
+                     : bf.vor[b * g.field + j * g.plane];
+      v[11] = -du;
+      for (int q = 0; q < 3; q++) v[12 + q] = pl[6 + q];
+      v[15] = pl[10];
+      {
+        const double *pp = bf.ppart + ((long)b * g.my + j) * (g.mgalz / 2) * 3;
+        double a1 = 0.0, a2 = 0.0, a3 = 0.0;
+        for (int zp = 0; zp < g.mgalz / 2; zp++) {
+          a1 += pp[3 * zp];
+          a2 += pp[3 * zp + 1];
+          a3 += pp[3 * zp + 2];
+        }
+        v[16] = a1;
+        v[17] = a2;
+        v[18] = a3;
+      }
+      v[19] = Pk;
+      v[20] = pl[9];
+      v[21] = nuty;
+      v[22] = disp;
+      const double dto = M.Deltat;
+      double *st = bf.stats + ((long)b * g.my + j) * 23, *st2 = bf.stats2 + ((long)b * g.my + j) * 23;
+      for (int q = 0; q < 23; q++) {
+        st[q] += v[q];
+        st2[q] += v[q] * dto;
+      }
+      if (g.temp) {
+        // tstats (crosst.f90:2201-2205)
+        double *ts = bf.tstats + ((long)b * g.my + j) * 5;
+        ts[0] += rdm(bf.mt, 0) * dto;
+        for (int q = 0; q < 4; q++) ts[1 + q] += pl[11 + q] * dto;
       }
     }
     for (int q = 0; q < nq; q++) {
@@ -780,6 +845,9 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
         }
       }
       M.ntrace++;
+      // counts of the accumulated statistics (cross.f90:2070-2072)
+      M.nacum++;
+      M.total_dt += M.Deltat;
       if (isnan(uner[0])) {
         M.istop = 1;
         M.flags |= SBF_NAN;
