@@ -434,9 +434,10 @@ def run_ours(args):
     status = box.status()
     ms_max = allmax(dist, ms)
     steps_per_s = ws * args.steps / (ms_max * 1e-3)
-    # per step: 3 substeps x (3 plane stages, scalars, tables, 2 line kernels)
-    # + the end-of-step kernel; LES adds 5 per substep; + 4 entry launches
-    launches = (37 if args.variant == "les" else 22) * args.steps + 4
+    # per step: 3 substeps x (3 plane stages, scalars, tables, 2 line kernels),
+    # the spectra and plane sums of the statistics at substep 1, the
+    # end-of-step kernel; LES adds 5 per substep; + 4 entry launches
+    launches = (39 if args.variant == "les" else 24) * args.steps + 4
     if args.lite:
         # profiling runs (ncu): the timed steps only, no side measurements
         if rank == 0:

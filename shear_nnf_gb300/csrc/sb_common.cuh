@@ -121,7 +121,8 @@ struct Bufs {
   double *Lv;                    // d2(omega_y)/dy2 of the next substep's starting state
   double *mu, *mwk, *mrf, *mdu;  // mean lines (u00 + i w00) [B][my] complex
   double *zbuf, *xbuf;           // plane-stage intermediates
-  double *hpart;                 // hist partials [B][my][ncb][SB_NHIST_Q]
+  double *hpart;                 // hist partials [B][my][blocks of plane stage 1][SB_NHIST_Q]
+  double *hsum;                  // their plane sums, + hist 'p' and LES sums [B][my][SB_NHIST_Q + 5]
   double *sh_old, *sh_new;       // [B][2][nkx] complex (t then b)
   double *tl1o, *tl2o, *tl1n, *tl2n;  // shear tails of d/dy, d2/dy2 at the old and new phases [B][nkx][SB_TAIL]
   double *mf1, *mf2;             // moving-frame phases [B][my][nkx] complex
@@ -149,7 +150,7 @@ struct Bufs {
   // statistics accumulated by hist over one call (module statistics,
   // mod.f90:94-115): stats, stats2 [B][my][23]; spectra spl, spl2
   // [B][mz][nkx][8]; temperature tstats [B][my][5], splt [B][mz][nkx][4];
-  // hist 'p' plane partials [B][my][mgalz/2][3]
+  // hist 'p' partials [B][my][mgalz/2][warps of a stage-2 block][3]
   double *stats, *stats2, *spec, *spec2, *tstats, *tspec, *ppart;
 };
 

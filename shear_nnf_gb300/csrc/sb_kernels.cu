@@ -106,15 +106,19 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
     }
     return p[k * nkx + i];
   };
-  const bool do_hist = (rk == 1) && M.ihist && round == 0;
+  const bool do_hist = (rk == 1) && M.ihist;
   if (do_hist) {
-    // statistics in FP64 whatever the storage precision
+    // statistics in FP64 whatever the storage precision; the kz rows of the
+    // column block are dealt round-robin to the block's rounds, so that every
+    // block of the launch takes its share
+    const int nrounds = gridDim.x / g.ncb;
+    const int nkr = (mz - round + nrounds - 1) / nrounds;  // kz rows of this round
     const double s = g.s;
     double acc[SB_NHIST_Q];
 #pragma unroll
     for (int q = 0; q < SB_NHIST_Q; q++) acc[q] = 0.0;
-    for (int idx = threadIdx.x; idx < CB * mz; idx += T) {
-      const int ci = idx % CB, k = idx / CB, i = i0 + ci;
+    for (int idx = threadIdx.x; idx < CB * nkr; idx += T) {
+      const int ci = idx % CB, k = round + nrounds * (idx / CB), i = i0 + ci;
       if (i >= nkx) continue;
       const double a = g.alp * i;
       const int kzs = (k <= nz) ? k : k - mz;
@@ -192,7 +196,7 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
     if (threadIdx.x < SB_NHIST_Q) {
       double v = 0.0;
       for (int w = 0; w < T / 32; w++) v += red[threadIdx.x][w];
-      bf.hpart[(((long)b * g.my + j) * g.ncb + cb) * SB_NHIST_Q + threadIdx.x] = v;
+      bf.hpart[(((long)b * g.my + j) * gridDim.x + blockIdx.x) * SB_NHIST_Q + threadIdx.x] = v;
     }
   }
   V *zb = (V *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * g.nzf * nkx;
@@ -298,50 +302,57 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
 // ---------------------------------------------------------------------------
 // hist spectra for HSF (nspec = 8: uu vv ww uv o1o1 o2o2 o3o3 o1o2,
 // cross.f90:1970-1994) and, with the temperature, splt (tt ut vt wt,
-// crosst.f90:2364-2374) at the first substep of a statistics step: one thread
-// per (kx, kz) mode of a box sums the products over the planes in order, from
-// the substep's starting state (the inputs of plane stage 1, reconstructed as
-// there).  Runs before the per-box scalars update Delta t: spl2 and splt are
-// weighted by the Delta t of the previous step, as in hist 'f'.
+// crosst.f90:2364-2374) at the first substep of a statistics step, from the
+// substep's starting state (the inputs of plane stage 1, reconstructed as
+// there).  A block takes 16 modes of a box; its 8 thread slices sum every 8th
+// plane, then the slices are added in a fixed order.  Runs before the per-box
+// scalars update Delta t: spl2 and splt are weighted by the Delta t of the
+// previous step, as in hist 'f'.
 // ---------------------------------------------------------------------------
+constexpr int kSpecModes = 16, kSpecSlices = 8;
 template <typename R, bool TEMP>
-__global__ void __launch_bounds__(128) k_spectra(Grid g, Bufs bf) {
+__global__ void __launch_bounds__(kSpecModes * kSpecSlices) k_spectra(Grid g, Bufs bf) {
   typedef typename Vec2<R>::t V;
   const int b = blockIdx.y;
   const Member &M = bf.mem[b];
-  if (M.halted || !M.ihist) return;
+  if (M.halted || !M.ihist) return;  // uniform per block
   const int nkx = g.nkx, mz = g.mz, nz = g.nz, nl = nkx * mz;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nl) return;
+  const int mi = threadIdx.x % kSpecModes, sl = threadIdx.x / kSpecModes;
+  const int q0 = blockIdx.x * kSpecModes + mi;
+  const bool valid = q0 < nl;
+  const int q = valid ? q0 : nl - 1;
   const int i = q % nkx, k = q / nkx;
-  const double a = g.alp * i;
-  const double gz = g.gam * ((k <= nz) ? k : k - mz);
-  const double iK = bf.kinv[q];
-  const double w = (i == 0) ? 1.0 : 2.0;
+  // the products in the storage precision R (FP64, or FP32 in the mixed
+  // form), the sums in FP64
+  typedef R A;
+  const A a = (A)(g.alp * i);
+  const A gz = (A)(g.gam * ((k <= nz) ? k : k - mz));
+  const A iK = kinv_of<R>(bf, q);
+  const A w = (i == 0) ? (A)1 : (A)2;
   const bool z00 = (i == 0 && k == 0);
   // set_conj of the omega_y and phi copies (cross.f90:502)
   const int qs = (i == 0 && k > nz) ? (mz - k) * nkx : q;
-  const double cs = (i == 0 && k > nz) ? -1.0 : 1.0;
+  const A cs = (i == 0 && k > nz) ? (A)-1 : (A)1;
   double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, tacc[4] = {0, 0, 0, 0};
-  for (int j = 0; j < g.my; j++) {
+  for (int j = sl; j < g.my; j += kSpecSlices) {
     const long pb = (long)b * g.field + (long)j * g.plane;
     const V *vor = (const V *)((const R *)bf.vor + pb), *phi = (const V *)((const R *)bf.phi + pb);
     const V *Dv = (const V *)((const R *)bf.D + pb), *Vv = (const V *)((const R *)bf.V + pb);
     const V *Gv = (const V *)((const R *)bf.G + pb);
     const V vr0 = vor[qs], ph0 = phi[qs];
-    const double vrx = vr0.x, vry = cs * (double)vr0.y, phx = ph0.x, phy = cs * (double)ph0.y;
-    double u1x, u1y, u2x, u2y, u3x, u3y, o1x, o1y, o3x, o3y;
+    const A vrx = vr0.x, vry = cs * vr0.y, phx = ph0.x, phy = cs * ph0.y;
+    A u1x, u1y, u2x, u2y, u3x, u3y, o1x, o1y, o3x, o3y;
     if (z00) {
       const V mu = ((const V *)bf.mu)[(long)b * g.my + j];
       const V mdu = ((const V *)bf.mdu)[(long)b * g.my + j];
-      u1x = mu.x; u1y = 0.0;
-      u3x = mu.y; u3y = 0.0;
-      o3x = -(double)mdu.x; o3y = 0.0;
-      o1x = mdu.y; o1y = 0.0;
-      u2x = M.vbulk; u2y = 0.0;
+      u1x = mu.x; u1y = (A)0;
+      u3x = mu.y; u3y = (A)0;
+      o3x = -mdu.x; o3y = (A)0;
+      o1x = mdu.y; o1y = (A)0;
+      u2x = (A)M.vbulk; u2y = (A)0;
     } else {
       const V w1 = Dv[q], dv = Vv[q], gv = Gv[q];
-      double tx, ty;
+      A tx, ty;
       tx = gz * w1.x - a * phx; ty = gz * w1.y - a * phy;
       o3x = -ty * iK; o3y = tx * iK;
       tx = a * w1.x + gz * phx; ty = a * w1.y + gz * phy;
@@ -352,16 +363,16 @@ __global__ void __launch_bounds__(128) k_spectra(Grid g, Bufs bf) {
       u1x = -ty * iK; u1y = tx * iK;
       u2x = gv.x; u2y = gv.y;
     }
-    acc[0] += w * (u1x * u1x + u1y * u1y);
-    acc[1] += w * (u2x * u2x + u2y * u2y);
-    acc[2] += w * (u3x * u3x + u3y * u3y);
-    acc[3] += w * (u1x * u2x + u1y * u2y);
-    acc[4] += w * (o1x * o1x + o1y * o1y);
-    acc[5] += w * (vrx * vrx + vry * vry);
-    acc[6] += w * (o3x * o3x + o3y * o3y);
-    acc[7] += w * (o1x * vrx + o1y * vry);
+    acc[0] += (double)(w * (u1x * u1x + u1y * u1y));
+    acc[1] += (double)(w * (u2x * u2x + u2y * u2y));
+    acc[2] += (double)(w * (u3x * u3x + u3y * u3y));
+    acc[3] += (double)(w * (u1x * u2x + u1y * u2y));
+    acc[4] += (double)(w * (o1x * o1x + o1y * o1y));
+    acc[5] += (double)(w * (vrx * vrx + vry * vry));
+    acc[6] += (double)(w * (o3x * o3x + o3y * o3y));
+    acc[7] += (double)(w * (o1x * vrx + o1y * vry));
     if (TEMP) {
-      double tx = 0.0, ty = 0.0;
+      A tx = (A)0, ty = (A)0;
       if (z00) {
         tx = ((const V *)bf.mt)[(long)b * g.my + j].x;
       } else {
@@ -369,23 +380,30 @@ __global__ void __launch_bounds__(128) k_spectra(Grid g, Bufs bf) {
         tx = t.x;
         ty = t.y;
       }
-      tacc[0] += w * (tx * tx + ty * ty);
-      tacc[1] += w * (u1x * tx + u1y * ty);
-      tacc[2] += w * (u2x * tx + u2y * ty);
-      tacc[3] += w * (u3x * tx + u3y * ty);
+      tacc[0] += (double)(w * (tx * tx + ty * ty));
+      tacc[1] += (double)(w * (u1x * tx + u1y * ty));
+      tacc[2] += (double)(w * (u2x * tx + u2y * ty));
+      tacc[3] += (double)(w * (u3x * tx + u3y * ty));
     }
   }
+  __shared__ double red[kSpecSlices][12][kSpecModes];
+#pragma unroll
+  for (int f = 0; f < 8; f++) red[sl][f][mi] = acc[f];
+#pragma unroll
+  for (int f = 0; f < 4; f++) red[sl][8 + f][mi] = tacc[f];
+  __syncthreads();
+  if (sl != 0 || !valid) return;
   const double dt = M.Deltat;
   double *sp = bf.spec + ((long)b * nl + q) * 8, *sp2 = bf.spec2 + ((long)b * nl + q) * 8;
-#pragma unroll
-  for (int f = 0; f < 8; f++) {
-    sp[f] += acc[f];
-    sp2[f] += acc[f] * dt;
-  }
-  if (TEMP) {
-    double *st = bf.tspec + ((long)b * nl + q) * 4;
-#pragma unroll
-    for (int f = 0; f < 4; f++) st[f] += tacc[f] * dt;
+  for (int f = 0; f < (TEMP ? 12 : 8); f++) {
+    double a = 0.0;
+    for (int s2 = 0; s2 < kSpecSlices; s2++) a += red[s2][f][mi];
+    if (f < 8) {
+      sp[f] += a;
+      sp2[f] += a * dt;
+    } else {
+      bf.tspec[((long)b * nl + q) * 4 + (f - 8)] += a * dt;
+    }
   }
 }
 
@@ -433,17 +451,17 @@ __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
   const R chi2 = (R)(2.0 * g.chi);
   const R sy = (R)(g.s * ((double)j * g.dy - 0.5 * g.Ly));
   R m0 = 0, m1 = 0, m2 = 0, m3 = 0, mt = 0;
-  // hist 'p' (cross.f90:2038-2042): v u^2, v w^2, v^3 over the two rows
+  // hist 'p' (cross.f90:2038-2042): v u^2, v w^2, v^3 over the two rows; the
+  // products in the storage precision, the sums in FP64
   const bool hist = (rk == 1) && M.ihist;
   double s1 = 0.0, s2 = 0.0, s3 = 0.0;
   for (int x = threadIdx.x; x < NX; x += T) {
     const V u1 = P[0 * NX + x], u3 = P[1 * NX + x], o1 = P[2 * NX + x], o3 = P[3 * NX + x],
             u2 = P[4 * NX + x], o2 = P[5 * NX + x];
     if (hist) {
-      const double ax = u1.x, ay = u1.y, vx = u2.x, vy = u2.y, wx = u3.x, wy = u3.y;
-      s1 += vx * (ax * ax) + vy * (ay * ay);
-      s2 += vx * (wx * wx) + vy * (wy * wy);
-      s3 += vx * vx * vx + vy * vy * vy;
+      s1 += (double)(u2.x * (u1.x * u1.x) + u2.y * (u1.y * u1.y));
+      s2 += (double)(u2.x * (u3.x * u3.x) + u2.y * (u3.y * u3.y));
+      s3 += (double)(u2.x * u2.x * u2.x + u2.y * u2.y * u2.y);
     }
     if (rk == 1) {
       m0 = fmax(m0, fmax(fabs(u1.x), fabs(u1.y)));
@@ -490,23 +508,19 @@ __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
     }
   }
   if (hist) {
-    // block sums in a fixed order, one triple per (plane, row pair)
-    __shared__ double sred[3][T / 32];
+    // warp sums in a fixed tree, one triple per (plane, row pair, warp); the
+    // plane sums follow in k_hsum
     for (int o = 16; o > 0; o >>= 1) {
       s1 += __shfl_down_sync(0xffffffffu, s1, o);
       s2 += __shfl_down_sync(0xffffffffu, s2, o);
       s3 += __shfl_down_sync(0xffffffffu, s3, o);
     }
     if ((threadIdx.x & 31) == 0) {
-      sred[0][threadIdx.x >> 5] = s1;
-      sred[1][threadIdx.x >> 5] = s2;
-      sred[2][threadIdx.x >> 5] = s3;
-    }
-    __syncthreads();
-    if (threadIdx.x < 3) {
-      double v = 0.0;
-      for (int w = 0; w < T / 32; w++) v += sred[threadIdx.x][w];
-      bf.ppart[(((long)b * g.my + j) * (g.mgalz / 2) + zp) * 3 + threadIdx.x] = v;
+      double *pp = bf.ppart + ((((long)b * g.my + j) * (g.mgalz / 2) + zp) * (T / 32) +
+                               (threadIdx.x >> 5)) * 3;
+      pp[0] = s1;
+      pp[1] = s2;
+      pp[2] = s3;
     }
   }
   V *Rr = fft_batch<NX, -1, NO, T>(Q, P, (const V *)tw_of<R>(bf, false));
@@ -1482,11 +1496,12 @@ static cudaError_t launch_phys_r(const Grid &g, const Bufs &bf, unsigned mask, d
 template <typename R>
 static cudaError_t launch_spectra_t(const Grid &g, const Bufs &bf, cudaStream_t st) {
   const int nl = g.nkx * g.mz;
-  const dim3 grid((unsigned)((nl + 127) / 128), (unsigned)g.B);
+  const dim3 grid((unsigned)((nl + kSpecModes - 1) / kSpecModes), (unsigned)g.B);
+  const int T = kSpecModes * kSpecSlices;
   if (g.temp)
-    k_spectra<R, true><<<grid, 128, 0, st>>>(g, bf);
+    k_spectra<R, true><<<grid, T, 0, st>>>(g, bf);
   else
-    k_spectra<R, false><<<grid, 128, 0, st>>>(g, bf);
+    k_spectra<R, false><<<grid, T, 0, st>>>(g, bf);
   return cudaGetLastError();
 }
 

@@ -598,6 +598,49 @@ __global__ void k_setconj(Grid g, Bufs bf) {
 
 #if !SB_FLOAT_TU
 // ---------------------------------------------------------------------------
+// plane sums of the hist partials of plane stages 1 and 2 and of the LES
+// stage at the first substep of a statistics step: one warp per (box, plane),
+// lanes over the partials, a fixed reduction tree
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(32) k_hsum(Grid g, Bufs bf) {
+  const int j = blockIdx.x, b = blockIdx.y;
+  const Member &M = bf.mem[b];
+  if (M.halted || !M.ihist) return;
+  const int nparts = g.ncb * (3 + (g.les ? 2 : 0) + g.temp);
+  const int nzp = g.mgalz / 2;
+  const int lane = threadIdx.x;
+  constexpr int NS = SB_NHIST_Q + 5;
+  double v[NS];
+#pragma unroll
+  for (int q = 0; q < NS; q++) v[q] = 0.0;
+  const double *hp = bf.hpart + ((long)b * g.my + j) * nparts * SB_NHIST_Q;
+  for (int pp = lane; pp < nparts; pp += 32)
+#pragma unroll
+    for (int q = 0; q < SB_NHIST_Q; q++) v[q] += hp[pp * SB_NHIST_Q + q];
+  // plane stage 2 leaves one triple per (row pair, warp of its block)
+  const int np2 = nzp * (g.t2 / 32);
+  const double *ph = bf.ppart + ((long)b * g.my + j) * np2 * 3;
+  for (int z = lane; z < np2; z += 32)
+#pragma unroll
+    for (int q = 0; q < 3; q++) v[SB_NHIST_Q + q] += ph[3 * z + q];
+  if (g.les) {
+    const double *lp = bf.lpart + ((long)b * g.my + j) * nzp * 2;
+    for (int z = lane; z < nzp; z += 32) {
+      v[SB_NHIST_Q + 3] += lp[2 * z];
+      v[SB_NHIST_Q + 4] += lp[2 * z + 1];
+    }
+  }
+  double mine = 0.0;
+#pragma unroll
+  for (int q = 0; q < NS; q++) {
+    double x = v[q];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == q) mine = x;
+  }
+  if (lane < NS) bf.hsum[((long)b * g.my + j) * NS + lane] = mine;
+}
+
+// ---------------------------------------------------------------------------
 // per-box scalars: entry flags, hist reduction and UNER record, Delta t,
 // image offsets.  One block per box.
 // ---------------------------------------------------------------------------
@@ -657,11 +700,9 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
     const double nufac = g.les_visc ? (1.0 / M.Re) : 0.0;
     const double nxz = (double)(g.mgalx * g.mgalz);
     for (int j = threadIdx.x; j < g.my; j += blockDim.x) {
-      const double *hp = bf.hpart + ((long)b * g.my + j) * g.ncb * SB_NHIST_Q;
+      const double *hs = bf.hsum + ((long)b * g.my + j) * (SB_NHIST_Q + 5);
       double pl[SB_NHIST_Q];
-      for (int q = 0; q < SB_NHIST_Q; q++) pl[q] = 0.0;
-      for (int cb = 0; cb < g.ncb; cb++)
-        for (int q = 0; q < SB_NHIST_Q; q++) pl[q] += hp[cb * SB_NHIST_Q + q];
+      for (int q = 0; q < SB_NHIST_Q; q++) pl[q] = hs[q];
       for (int q = 0; q < SB_NHIST_Q; q++) acc[q] += pl[q];
       const long mj = 2 * ((long)b * g.my + j);
       auto rdm = [&](const double *p, int c) -> double {
@@ -675,14 +716,8 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
         // energy transfer to the subgrid scales (cross.f90:1892,1950-1952)
         const double txy = rdm(bf.txy, 0);
         Pk = -(o3 * (-pl[3] + txy)) + nufac * (o3 * o3);
-        const double *lp = bf.lpart + ((long)b * g.my + j) * (g.mgalz / 2) * 2;
-        double sn = 0.0, sd = 0.0;
-        for (int zp = 0; zp < g.mgalz / 2; zp++) {
-          sn += lp[2 * zp];
-          sd += lp[2 * zp + 1];
-        }
-        nuty = sn / nxz;
-        disp = sd / nxz;
+        nuty = hs[SB_NHIST_Q + 3] / nxz;
+        disp = hs[SB_NHIST_Q + 4] / nxz;
         acc[SB_NHIST_Q + 1] += nuty;
         acc[SB_NHIST_Q + 2] += disp;
       } else {
@@ -702,18 +737,9 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
       v[11] = -du;
       for (int q = 0; q < 3; q++) v[12 + q] = pl[6 + q];
       v[15] = pl[10];
-      {
-        const double *pp = bf.ppart + ((long)b * g.my + j) * (g.mgalz / 2) * 3;
-        double a1 = 0.0, a2 = 0.0, a3 = 0.0;
-        for (int zp = 0; zp < g.mgalz / 2; zp++) {
-          a1 += pp[3 * zp];
-          a2 += pp[3 * zp + 1];
-          a3 += pp[3 * zp + 2];
-        }
-        v[16] = a1;
-        v[17] = a2;
-        v[18] = a3;
-      }
+      v[16] = hs[SB_NHIST_Q];
+      v[17] = hs[SB_NHIST_Q + 1];
+      v[18] = hs[SB_NHIST_Q + 2];
       v[19] = Pk;
       v[20] = pl[9];
       v[21] = nuty;
@@ -1090,6 +1116,12 @@ cudaError_t launch_setconj(const Grid &g, const Bufs &bf, cudaStream_t st) {
 }
 
 cudaError_t launch_scalar(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  if (rk == 1) {
+    // the plane sums of a statistics step (the kernel returns at once otherwise)
+    k_hsum<<<dim3((unsigned)g.my, (unsigned)g.B), 32, 0, st>>>(g, bf);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   k_scalar<<<g.B, 256, 0, st>>>(g, bf, rk);
   return cudaGetLastError();
 }
