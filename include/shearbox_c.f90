@@ -1,0 +1,207 @@
+! shearbox_c.f90 -- Fortran 2003 ISO_C_BINDING interface of the GB300
+! shearing-box time stepper (include/shearbox.h), for the reference's drivers:
+! disk3d (main.f90:273-281), calc_dns_disk3d (gmres_shear.f90:2951-3120) and
+! shoot_shear.f90:527 call sb_cross / sb_crosst in place of cross / crosst.
+! Arrays keep the reference's own layouts (vor, phi, tb: the buffsize arrays,
+! complex(0:my1,0:mx1,0:mz1); u00, w00, tb00: real(0:my1)), so the calls copy
+! nothing on the Fortran side.  Every function returns 0 on success; the text
+! of the last error comes from sb_last_error (a C string).
+! This file is an interface only; no Fortran compiler is used by the build.
+module shearbox_c
+  use iso_c_binding
+  implicit none
+
+  integer(c_int), parameter :: SB_FP64 = 0, SB_MIXED = 1
+  integer(c_int), parameter :: SB_TRACE_RECORD = 24, SB_TRACE_RECORD_T = 29
+
+  type, bind(C) :: sb_params
+     integer(c_int)  :: mgalx, my, mgalz
+     real(c_double)  :: Re, alp, Ly, gam
+     real(c_double)  :: s, chi, CFL
+     real(c_double)  :: vbulk
+     real(c_double)  :: fixed_dt
+     integer(c_int)  :: readflag
+     real(c_double)  :: uprim
+     integer(c_int)  :: nhist
+     real(c_double)  :: etime, dumptime, dtimag
+     integer(c_int)  :: keep_laminar
+     integer(c_int)  :: les, les_visc
+     real(c_double)  :: cs
+     integer(c_int)  :: ydeal
+     integer(c_int)  :: temperature
+     real(c_double)  :: fkappa, bym, gbeta
+  end type sb_params
+
+  type, bind(C) :: sb_status
+     integer(c_int)  :: istop, steps_done, ntrace, flags
+     real(c_double)  :: time, deltat, xoffb, xofft, cfl, cflv
+  end type sb_status
+
+  interface
+     integer(c_int) function sb_create(p, batch, precision, h) bind(C, name="sb_create")
+       import :: c_int, c_ptr, sb_params
+       type(sb_params), intent(in) :: p
+       integer(c_int), value :: batch, precision
+       type(c_ptr), intent(out) :: h
+     end function sb_create
+
+     integer(c_int) function sb_destroy(h) bind(C, name="sb_destroy")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h
+     end function sb_destroy
+
+     integer(c_int) function sb_set_member_re(h, member, Re) bind(C, name="sb_set_member_re")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: member
+       real(c_double), value :: Re
+     end function sb_set_member_re
+
+     integer(c_int) function sb_set_member_etime(h, member, etime) &
+          bind(C, name="sb_set_member_etime")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: member
+       real(c_double), value :: etime
+     end function sb_set_member_etime
+
+     integer(c_int) function sb_set_state(h, member, vor, phi, u00, w00, time, xoffb, xofft) &
+          bind(C, name="sb_set_state")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: member
+       real(c_double), intent(in) :: vor(*), phi(*), u00(*), w00(*)
+       real(c_double), value :: time, xoffb, xofft
+     end function sb_set_state
+
+     integer(c_int) function sb_get_state(h, member, vor, phi, u00, w00, time, xoffb, xofft) &
+          bind(C, name="sb_get_state")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: member
+       real(c_double), intent(out) :: vor(*), phi(*), u00(*), w00(*)
+       real(c_double), intent(out) :: time, xoffb, xofft
+     end function sb_get_state
+
+     integer(c_int) function sb_set_temperature(h, member, tb, tb00) &
+          bind(C, name="sb_set_temperature")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: member
+       real(c_double), intent(in) :: tb(*), tb00(*)
+     end function sb_set_temperature
+
+     integer(c_int) function sb_get_temperature(h, member, tb, tb00) &
+          bind(C, name="sb_get_temperature")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: member
+       real(c_double), intent(out) :: tb(*), tb00(*)
+     end function sb_get_temperature
+
+     integer(c_int) function sb_step(h, nsteps) bind(C, name="sb_step")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int), value :: nsteps
+     end function sb_step
+
+     integer(c_int) function sb_get_status(h, member, st) bind(C, name="sb_get_status")
+       import :: c_int, c_ptr, sb_status
+       type(c_ptr), value :: h
+       integer(c_int), value :: member
+       type(sb_status), intent(out) :: st
+     end function sb_get_status
+
+     integer(c_int) function sb_get_trace(h, member, out, maxrec, nrec) &
+          bind(C, name="sb_get_trace")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: member, maxrec
+       real(c_double), intent(out) :: out(*)
+       integer(c_int), intent(out) :: nrec
+     end function sb_get_trace
+
+     integer(c_int) function sb_cross(h, vor, phi, u00, w00, time, xoffb, xofft, nstep, st) &
+          bind(C, name="sb_cross")
+       import :: c_int, c_ptr, c_double, sb_status
+       type(c_ptr), value :: h
+       real(c_double), intent(inout) :: vor(*), phi(*), u00(*), w00(*)
+       real(c_double), intent(inout) :: time, xoffb, xofft
+       integer(c_int), value :: nstep
+       type(sb_status), intent(out) :: st
+     end function sb_cross
+
+     integer(c_int) function sb_crosst(h, vor, phi, u00, w00, tb, tb00, time, xoffb, xofft, &
+          nstep, st) bind(C, name="sb_crosst")
+       import :: c_int, c_ptr, c_double, sb_status
+       type(c_ptr), value :: h
+       real(c_double), intent(inout) :: vor(*), phi(*), u00(*), w00(*), tb(*), tb00(*)
+       real(c_double), intent(inout) :: time, xoffb, xofft
+       integer(c_int), value :: nstep
+       type(sb_status), intent(out) :: st
+     end function sb_crosst
+
+     ! stats/stats2 (23,0:my1), spectra (8,0:mx1,0:mz1), tstats (5,0:my1),
+     ! splt (4,0:mx1,0:mz1): the arrays of module statistics (mod.f90:94-115)
+     integer(c_int) function sb_get_statistics(h, member, stats, stats2, spec, spec2, tstats, &
+          tspec, nacum, total_dt) bind(C, name="sb_get_statistics")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: member
+       real(c_double), intent(out) :: stats(*), stats2(*), spec(*), spec2(*)
+       type(c_ptr), value :: tstats, tspec   ! c_null_ptr without the temperature
+       integer(c_int), intent(out) :: nacum
+       real(c_double), intent(out) :: total_dt
+     end function sb_get_statistics
+
+     integer(c_int) function sb_stats(h, member, uner, uner2) bind(C, name="sb_stats")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: member
+       real(c_double), intent(out) :: uner(10), uner2(4)
+     end function sb_stats
+
+     ! block of period-map products for matvec_dns_disk3d: vectors are
+     ! [vor | phi | u00 | w00]
+     integer(c_int) function sb_jv_batch(h, x0, time0, xoffb, xofft, T, dirs, ndir, &
+          eps_jacobi, central, out) bind(C, name="sb_jv_batch")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       real(c_double), intent(in) :: x0(*), dirs(*)
+       real(c_double), value :: time0, xoffb, xofft, T, eps_jacobi
+       integer(c_int), value :: ndir, central
+       real(c_double), intent(out) :: out(*)
+     end function sb_jv_batch
+
+     integer(c_int) function sb_physical_fields(h, member, mask, out) &
+          bind(C, name="sb_physical_fields")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h
+       integer(c_int), value :: member, mask
+       real(c_double), intent(out) :: out(*)
+     end function sb_physical_fields
+
+     integer(c_int) function sb_write_restart(path, p, vor, phi, u00, w00, time, xoffb, &
+          xofft, deltat) bind(C, name="sb_write_restart")
+       import :: c_int, c_char, c_double, sb_params
+       character(kind=c_char), intent(in) :: path(*)   ! NUL-terminated
+       type(sb_params), intent(in) :: p
+       real(c_double), intent(in) :: vor(*), phi(*), u00(*), w00(*)
+       real(c_double), value :: time, xoffb, xofft, deltat
+     end function sb_write_restart
+
+     integer(c_int) function sb_sizes(p, out) bind(C, name="sb_sizes")
+       import :: c_int, sb_params
+       type(sb_params), intent(in) :: p
+       integer(c_int), intent(out) :: out(8)
+     end function sb_sizes
+
+     type(c_ptr) function sb_last_error() bind(C, name="sb_last_error")
+       import :: c_ptr
+     end function sb_last_error
+
+     integer(c_int) function sb_version() bind(C, name="sb_version")
+       import :: c_int
+     end function sb_version
+  end interface
+end module shearbox_c

@@ -97,3 +97,38 @@ def test_no_cpu_fallback(monkeypatch):
     import shear_nnf_gb300 as sb
     with pytest.raises(sb.ShearBoxError, match="no CUDA device"):
         sb.ShearBox(sb.make_params(**box_params(64, 32, 32, rez=1000.0)))
+
+
+def _f90():
+    txt = open(os.path.join(ROOT, "include", "shearbox_c.f90")).read()
+    return "\n".join(line.split("!")[0] for line in txt.splitlines())
+
+
+def test_fortran_interface_binds_exported_symbols(lib):
+    """Every bind(C, name=...) of include/shearbox_c.f90 is declared in the
+    header and exported (the Fortran module is not compiled here)."""
+    names = re.findall(r'bind\(C,\s*name="(sb_[a-z0-9_]+)"\)', _f90())
+    assert len(names) >= 20
+    declared = set(_declared())
+    for n in names:
+        assert n in declared and hasattr(lib, n), n
+
+
+def test_fortran_types_follow_the_c_structs():
+    """The bind(C) derived types list the C struct members in order and type."""
+    import shear_nnf_gb300 as sb
+    txt = _f90()
+
+    def fields(tname):
+        body = re.search(r"type, bind\(C\) :: %s\n(.*?)end type" % tname, txt, re.S).group(1)
+        out = []
+        for line in body.splitlines():
+            m = re.match(r"\s*(integer\(c_int\)|real\(c_double\))\s*::\s*(.*)", line)
+            if m:
+                kind = ctypes.c_int if m.group(1).startswith("integer") else ctypes.c_double
+                out += [(n.strip(), kind) for n in m.group(2).split(",")]
+        return out
+
+    for tname, cls in (("sb_params", sb.SbParams), ("sb_status", sb.SbStatus)):
+        assert [(n.lower(), t) for n, t in fields(tname)] == \
+            [(n.lower(), t) for n, t in cls._fields_], tname
