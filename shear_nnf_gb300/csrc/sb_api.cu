@@ -441,7 +441,7 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
       (rc = A(&bf.mrf, B * 2 * my)) || (rc = A(&bf.mdu, B * 2 * my)) ||
       (rc = A(&bf.zbuf, B * my * g.mgalz * g.nzf * g.nkx * 2)) ||
       (rc = A(&bf.xbuf, B * my * g.mgalz * g.nxf * g.nkx * 2)) ||
-      (rc = A(&bf.hpart, B * my * ((g.nkx + 3) / 4) * 6 * SB_NHIST_Q)) ||
+      (rc = A(&bf.hpart, B * my * ((g.nkx * g.mz + 15) / 16) * SB_NHIST_Q)) ||
       (rc = A(&bf.hsum, B * my * (SB_NHIST_Q + 5))) || (rc = A(&bf.sh_old, B * 4 * g.nkx)) ||
       (rc = A(&bf.sh_new, B * 4 * g.nkx)) || (rc = A(&bf.mf1, B * my * g.nkx * 2)) ||
       (rc = A(&bf.mf2, B * my * g.nkx * 2)) || (rc = A(&h->d_pen, F))) {

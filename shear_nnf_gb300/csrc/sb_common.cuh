@@ -121,7 +121,7 @@ struct Bufs {
   double *Lv;                    // d2(omega_y)/dy2 of the next substep's starting state
   double *mu, *mwk, *mrf, *mdu;  // mean lines (u00 + i w00) [B][my] complex
   double *zbuf, *xbuf;           // plane-stage intermediates
-  double *hpart;                 // hist partials [B][my][blocks of plane stage 1][SB_NHIST_Q]
+  double *hpart;                 // hist partials [B][my][blocks of k_spectra][SB_NHIST_Q]
   double *hsum;                  // their plane sums, + hist 'p' and LES sums [B][my][SB_NHIST_Q + 5]
   double *sh_old, *sh_new;       // [B][2][nkx] complex (t then b)
   double *tl1o, *tl2o, *tl1n, *tl2n;  // shear tails of d/dy, d2/dy2 at the old and new phases [B][nkx][SB_TAIL]

@@ -2,9 +2,11 @@
 //
 // One RK3 substep of the reference (cross.f90:428-1000, explicit branch,
 // iadd_mode=5) is five launches:
+//   k_spectra  (first substep of a statistics step, beside stages 1-2) hist
+//           plane sums and kx-kz spectra (cross.f90:1796-2014)
 //   k_p1    per (plane, kx block): u, w, omega_x, omega_z from v, omega_y
-//           (cross.f90:1226-1276), hist sums (cross.f90:1796-1963), and the six
-//           backward z-transforms with zero padding (fill00, fou3D_thread.f:73-126)
+//           (cross.f90:1226-1276) and the six backward z-transforms with zero
+//           padding (fill00, fou3D_thread.f:73-126)
 //   k_p2    per (plane, z row pair): backward x-transforms, |u| maxima for the CFL
 //           (cross.f90:1438-1441), u x (omega + 2 chi z) (cross.f90:1453-1462) and
 //           the three forward x-transforms
@@ -106,99 +108,6 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
     }
     return p[k * nkx + i];
   };
-  const bool do_hist = (rk == 1) && M.ihist;
-  if (do_hist) {
-    // statistics in FP64 whatever the storage precision; the kz rows of the
-    // column block are dealt round-robin to the block's rounds, so that every
-    // block of the launch takes its share
-    const int nrounds = gridDim.x / g.ncb;
-    const int nkr = (mz - round + nrounds - 1) / nrounds;  // kz rows of this round
-    const double s = g.s;
-    double acc[SB_NHIST_Q];
-#pragma unroll
-    for (int q = 0; q < SB_NHIST_Q; q++) acc[q] = 0.0;
-    for (int idx = threadIdx.x; idx < CB * nkr; idx += T) {
-      const int ci = idx % CB, k = round + nrounds * (idx / CB), i = i0 + ci;
-      if (i >= nkx) continue;
-      const double a = g.alp * i;
-      const int kzs = (k <= nz) ? k : k - mz;
-      const double gz = g.gam * kzs;
-      const double Kk = a * a + gz * gz;
-      const double iK = bf.kinv[k * nkx + i];
-      const V phr = ld_sym(phi, i, k), vrr = ld_sym(vor, i, k);
-      const V w1r = Dv[k * nkx + i], dvr = Vv[k * nkx + i];
-      const double2 ph = make_double2(phr.x, phr.y), vr = make_double2(vrr.x, vrr.y);
-      const double2 w1 = make_double2(w1r.x, w1r.y), dv = make_double2(dvr.x, dvr.y);
-      double2 u1, u2, u3, o1, o3;
-      if (i == 0 && k == 0) {
-        u1 = make_double2(mu.x, 0.0);
-        u3 = make_double2(mu.y, 0.0);
-        o3 = make_double2(-(double)mdu.x, 0.0);
-        o1 = make_double2(mdu.y, 0.0);
-        u2 = make_double2(M.vbulk, 0.0);
-      } else {
-        double tx, ty;
-        tx = gz * w1.x - a * ph.x; ty = gz * w1.y - a * ph.y;
-        o3 = make_double2(-ty * iK, tx * iK);
-        tx = a * w1.x + gz * ph.x; ty = a * w1.y + gz * ph.y;
-        o1 = make_double2(-ty * iK, tx * iK);
-        tx = gz * dv.x + a * vr.x; ty = gz * dv.y + a * vr.y;
-        u3 = make_double2(-ty * iK, tx * iK);
-        tx = a * dv.x - gz * vr.x; ty = a * dv.y - gz * vr.y;
-        u1 = make_double2(-ty * iK, tx * iK);
-        const V gv = Gv[k * nkx + i];
-        u2 = make_double2(gv.x, gv.y);
-      }
-      const double2 o2 = vr;
-      const double w = (i == 0) ? 1.0 : 2.0;
-      const double uu = u1.x * u1.x + u1.y * u1.y, vv = u2.x * u2.x + u2.y * u2.y,
-                   ww = u3.x * u3.x + u3.y * u3.y;
-      acc[0] += w * uu;
-      acc[1] += w * vv;
-      acc[2] += w * ww;
-      acc[3] += w * (u1.x * u2.x + u1.y * u2.y);
-      acc[4] += w * (u1.x * u3.x + u1.y * u3.y);
-      acc[5] += w * (u2.x * u3.x + u2.y * u3.y);
-      acc[6] += w * (o1.x * o1.x + o1.y * o1.y);
-      acc[7] += w * (o2.x * o2.x + o2.y * o2.y);
-      acc[8] += w * (o3.x * o3.x + o3.y * o3.y);
-      acc[9] += w * (o1.x * o2.x + o1.y * o2.y);
-      // dissipation (cross.f90:1926-1944); omega_z of the mean includes -s
-      double2 o3s = o3;
-      if (i == 0 && k == 0) o3s.x -= s;
-      const double c1x = o1.x - gz * u2.y, c1y = o1.y + gz * u2.x;  // o1 + i gz u2
-      const double c3x = o3s.x + a * u2.y, c3y = o3s.y - a * u2.x;  // o3 - i a u2
-      acc[10] += w * (Kk * (uu + vv + ww) + (dv.x * dv.x + dv.y * dv.y) +
-                      (c1x * c1x + c1y * c1y) + (c3x * c3x + c3y * c3y));
-      if (TEMP) {
-        // tbp, utbp, vtbp, wtbp of histt (crosst.f90:2151-2160)
-        double tx = (double)tb00, ty = 0.0;
-        if (!(i == 0 && k == 0)) {
-          const V t = tbv[k * nkx + i];
-          tx = (double)t.x;
-          ty = (double)t.y;
-        }
-        acc[11] += w * (tx * tx + ty * ty);
-        acc[12] += w * (u1.x * tx + u1.y * ty);
-        acc[13] += w * (u2.x * tx + u2.y * ty);
-        acc[14] += w * (u3.x * tx + u3.y * ty);
-      }
-    }
-    // block reduction (deterministic: fixed tree)
-    __shared__ double red[SB_NHIST_Q][T / 32];
-#pragma unroll
-    for (int q = 0; q < SB_NHIST_Q; q++) {
-      double v = acc[q];
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-      if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < SB_NHIST_Q) {
-      double v = 0.0;
-      for (int w = 0; w < T / 32; w++) v += red[threadIdx.x][w];
-      bf.hpart[(((long)b * g.my + j) * gridDim.x + blockIdx.x) * SB_NHIST_Q + threadIdx.x] = v;
-    }
-  }
   V *zb = (V *)bf.zbuf + ((long)b * g.my + j) * (long)NZ * g.nzf * nkx;
   const V zero = mk2<R>((R)0, (R)0);
   if (TEMP && round == g.tround) {
@@ -300,14 +209,19 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
 }
 
 // ---------------------------------------------------------------------------
-// hist spectra for HSF (nspec = 8: uu vv ww uv o1o1 o2o2 o3o3 o1o2,
-// cross.f90:1970-1994) and, with the temperature, splt (tt ut vt wt,
-// crosst.f90:2364-2374) at the first substep of a statistics step, from the
-// substep's starting state (the inputs of plane stage 1, reconstructed as
-// there).  A block takes 16 modes of a box; its 8 thread slices sum every 8th
-// plane, then the slices are added in a fixed order.  Runs before the per-box
-// scalars update Delta t: spl2 and splt are weighted by the Delta t of the
-// previous step, as in hist 'f'.
+// hist at the first substep of a statistics step (cross.f90:1796-2014;
+// crosst.f90:2151-2160,2364-2374), from the substep's starting state (the
+// inputs of plane stage 1, u, v, w and the vorticity reconstructed as
+// there, cross.f90:1226-1276): per mode the spectra for HSF (nspec = 8: uu
+// vv ww uv o1o1 o2o2 o3o3 o1o2) summed over the planes and, with the
+// temperature, splt (tt ut vt wt); per plane the partial sums over the
+// block's modes of the 11 hist quantities (up vp wp uvr uwr vwr o1p o2p o3p
+// o12p eps) and of tbp utbp vtbp wtbp, reduced per plane by k_hsum.  A block
+// takes 16 modes of a box; its 8 thread slices take every 8th plane; the
+// per-mode slices are added in a fixed order, the per-plane modes by a fixed
+// half-warp tree.  FP64 arithmetic whatever the storage precision.  Runs
+// before the per-box scalars update Delta t: spl2 and splt carry the Delta t
+// of the previous step, as in hist 'f'.
 // ---------------------------------------------------------------------------
 constexpr int kSpecModes = 16, kSpecSlices = 8;
 template <typename R, bool TEMP>
@@ -322,57 +236,88 @@ __global__ void __launch_bounds__(kSpecModes * kSpecSlices) k_spectra(Grid g, Bu
   const bool valid = q0 < nl;
   const int q = valid ? q0 : nl - 1;
   const int i = q % nkx, k = q / nkx;
-  // the products in the storage precision R (FP64, or FP32 in the mixed
-  // form), the sums in FP64
-  typedef R A;
-  const A a = (A)(g.alp * i);
-  const A gz = (A)(g.gam * ((k <= nz) ? k : k - mz));
-  const A iK = kinv_of<R>(bf, q);
-  const A w = (i == 0) ? (A)1 : (A)2;
+  const double a = g.alp * i;
+  const double gz = g.gam * ((k <= nz) ? k : k - mz);
+  const double Kk = a * a + gz * gz;
+  const double iK = bf.kinv[q];
+  // invalid threads (past the last mode) carry weight 0
+  const double wm = valid ? ((i == 0) ? 1.0 : 2.0) : 0.0;
   const bool z00 = (i == 0 && k == 0);
   // set_conj of the omega_y and phi copies (cross.f90:502)
   const int qs = (i == 0 && k > nz) ? (mz - k) * nkx : q;
-  const A cs = (i == 0 && k > nz) ? (A)-1 : (A)1;
+  const double cs = (i == 0 && k > nz) ? -1.0 : 1.0;
+  const int nblk = gridDim.x;
   double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, tacc[4] = {0, 0, 0, 0};
-  for (int j = sl; j < g.my; j += kSpecSlices) {
+  // the same number of iterations on every slice (the half-warp shuffles
+  // below need every lane of the warp): planes past the last carry weight 0
+  const int niter = (g.my + kSpecSlices - 1) / kSpecSlices;
+  for (int it = 0; it < niter; it++) {
+    const int jr = sl + kSpecSlices * it;
+    const bool jok = jr < g.my;
+    const int j = jok ? jr : g.my - 1;
+    const double w = jok ? wm : 0.0;
     const long pb = (long)b * g.field + (long)j * g.plane;
     const V *vor = (const V *)((const R *)bf.vor + pb), *phi = (const V *)((const R *)bf.phi + pb);
     const V *Dv = (const V *)((const R *)bf.D + pb), *Vv = (const V *)((const R *)bf.V + pb);
     const V *Gv = (const V *)((const R *)bf.G + pb);
     const V vr0 = vor[qs], ph0 = phi[qs];
-    const A vrx = vr0.x, vry = cs * vr0.y, phx = ph0.x, phy = cs * ph0.y;
-    A u1x, u1y, u2x, u2y, u3x, u3y, o1x, o1y, o3x, o3y;
+    const V dvr = Vv[q];
+    const double vrx = vr0.x, vry = cs * (double)vr0.y, phx = ph0.x, phy = cs * (double)ph0.y;
+    const double dvx = dvr.x, dvy = dvr.y;
+    double u1x, u1y, u2x, u2y, u3x, u3y, o1x, o1y, o3x, o3y;
     if (z00) {
       const V mu = ((const V *)bf.mu)[(long)b * g.my + j];
       const V mdu = ((const V *)bf.mdu)[(long)b * g.my + j];
-      u1x = mu.x; u1y = (A)0;
-      u3x = mu.y; u3y = (A)0;
-      o3x = -mdu.x; o3y = (A)0;
-      o1x = mdu.y; o1y = (A)0;
-      u2x = (A)M.vbulk; u2y = (A)0;
+      u1x = mu.x; u1y = 0.0;
+      u3x = mu.y; u3y = 0.0;
+      o3x = -(double)mdu.x; o3y = 0.0;
+      o1x = mdu.y; o1y = 0.0;
+      u2x = M.vbulk; u2y = 0.0;
     } else {
-      const V w1 = Dv[q], dv = Vv[q], gv = Gv[q];
-      A tx, ty;
+      const V w1 = Dv[q], gv = Gv[q];
+      double tx, ty;
       tx = gz * w1.x - a * phx; ty = gz * w1.y - a * phy;
       o3x = -ty * iK; o3y = tx * iK;
       tx = a * w1.x + gz * phx; ty = a * w1.y + gz * phy;
       o1x = -ty * iK; o1y = tx * iK;
-      tx = gz * dv.x + a * vrx; ty = gz * dv.y + a * vry;
+      tx = gz * dvx + a * vrx; ty = gz * dvy + a * vry;
       u3x = -ty * iK; u3y = tx * iK;
-      tx = a * dv.x - gz * vrx; ty = a * dv.y - gz * vry;
+      tx = a * dvx - gz * vrx; ty = a * dvy - gz * vry;
       u1x = -ty * iK; u1y = tx * iK;
       u2x = gv.x; u2y = gv.y;
     }
-    acc[0] += (double)(w * (u1x * u1x + u1y * u1y));
-    acc[1] += (double)(w * (u2x * u2x + u2y * u2y));
-    acc[2] += (double)(w * (u3x * u3x + u3y * u3y));
-    acc[3] += (double)(w * (u1x * u2x + u1y * u2y));
-    acc[4] += (double)(w * (o1x * o1x + o1y * o1y));
-    acc[5] += (double)(w * (vrx * vrx + vry * vry));
-    acc[6] += (double)(w * (o3x * o3x + o3y * o3y));
-    acc[7] += (double)(w * (o1x * vrx + o1y * vry));
+    const double uu = u1x * u1x + u1y * u1y, vv = u2x * u2x + u2y * u2y,
+                 ww = u3x * u3x + u3y * u3y;
+    double pq[SB_NHIST_Q];
+    pq[0] = w * uu;
+    pq[1] = w * vv;
+    pq[2] = w * ww;
+    pq[3] = w * (u1x * u2x + u1y * u2y);
+    pq[4] = w * (u1x * u3x + u1y * u3y);
+    pq[5] = w * (u2x * u3x + u2y * u3y);
+    pq[6] = w * (o1x * o1x + o1y * o1y);
+    pq[7] = w * (vrx * vrx + vry * vry);
+    pq[8] = w * (o3x * o3x + o3y * o3y);
+    pq[9] = w * (o1x * vrx + o1y * vry);
+    {
+      // dissipation (cross.f90:1926-1944); omega_z of the mean includes -s
+      const double o3sx = z00 ? o3x - g.s : o3x;
+      const double c1x = o1x - gz * u2y, c1y = o1y + gz * u2x;   // o1 + i gz u2
+      const double c3x = o3sx + a * u2y, c3y = o3y - a * u2x;    // o3 - i a u2
+      pq[10] = w * (Kk * (uu + vv + ww) + (dvx * dvx + dvy * dvy) + (c1x * c1x + c1y * c1y) +
+                    (c3x * c3x + c3y * c3y));
+    }
+    // spectra: omega_z of the mean without -s (cross.f90:1968)
+    acc[0] += pq[0];
+    acc[1] += pq[1];
+    acc[2] += pq[2];
+    acc[3] += pq[3];
+    acc[4] += pq[6];
+    acc[5] += pq[7];
+    acc[6] += pq[8];
+    acc[7] += pq[9];
     if (TEMP) {
-      A tx = (A)0, ty = (A)0;
+      double tx, ty = 0.0;
       if (z00) {
         tx = ((const V *)bf.mt)[(long)b * g.my + j].x;
       } else {
@@ -380,10 +325,27 @@ __global__ void __launch_bounds__(kSpecModes * kSpecSlices) k_spectra(Grid g, Bu
         tx = t.x;
         ty = t.y;
       }
-      tacc[0] += (double)(w * (tx * tx + ty * ty));
-      tacc[1] += (double)(w * (u1x * tx + u1y * ty));
-      tacc[2] += (double)(w * (u2x * tx + u2y * ty));
-      tacc[3] += (double)(w * (u3x * tx + u3y * ty));
+      pq[11] = w * (tx * tx + ty * ty);
+      pq[12] = w * (u1x * tx + u1y * ty);
+      pq[13] = w * (u2x * tx + u2y * ty);
+      pq[14] = w * (u3x * tx + u3y * ty);
+#pragma unroll
+      for (int f = 0; f < 4; f++) tacc[f] += pq[11 + f];
+    } else {
+#pragma unroll
+      for (int f = 11; f < SB_NHIST_Q; f++) pq[f] = 0.0;
+    }
+    // the plane's partial over the block's 16 modes (the lanes of one half warp)
+#pragma unroll
+    for (int f = 0; f < SB_NHIST_Q; f++) {
+      double x = pq[f];
+      for (int o = kSpecModes / 2; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+      pq[f] = x;
+    }
+    if (mi == 0 && jok) {
+      double *hp = bf.hpart + (((long)b * g.my + j) * nblk + blockIdx.x) * SB_NHIST_Q;
+#pragma unroll
+      for (int f = 0; f < SB_NHIST_Q; f++) hp[f] = pq[f];
     }
   }
   __shared__ double red[kSpecSlices][12][kSpecModes];
@@ -396,13 +358,13 @@ __global__ void __launch_bounds__(kSpecModes * kSpecSlices) k_spectra(Grid g, Bu
   const double dt = M.Deltat;
   double *sp = bf.spec + ((long)b * nl + q) * 8, *sp2 = bf.spec2 + ((long)b * nl + q) * 8;
   for (int f = 0; f < (TEMP ? 12 : 8); f++) {
-    double a = 0.0;
-    for (int s2 = 0; s2 < kSpecSlices; s2++) a += red[s2][f][mi];
+    double x = 0.0;
+    for (int s2 = 0; s2 < kSpecSlices; s2++) x += red[s2][f][mi];
     if (f < 8) {
-      sp[f] += a;
-      sp2[f] += a * dt;
+      sp[f] += x;
+      sp2[f] += x * dt;
     } else {
-      bf.tspec[((long)b * nl + q) * 4 + (f - 8)] += a * dt;
+      bf.tspec[((long)b * nl + q) * 4 + (f - 8)] += x * dt;
     }
   }
 }

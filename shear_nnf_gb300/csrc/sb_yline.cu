@@ -606,7 +606,8 @@ __global__ void __launch_bounds__(32) k_hsum(Grid g, Bufs bf) {
   const int j = blockIdx.x, b = blockIdx.y;
   const Member &M = bf.mem[b];
   if (M.halted || !M.ihist) return;
-  const int nparts = g.ncb * (3 + (g.les ? 2 : 0) + g.temp);
+  // one partial per block of k_spectra (16 modes each)
+  const int nparts = (g.nkx * g.mz + 15) / 16;
   const int nzp = g.mgalz / 2;
   const int lane = threadIdx.x;
   constexpr int NS = SB_NHIST_Q + 5;
