@@ -496,6 +496,24 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
     }
     return v;
   };
+  // the factored FP64 form of the same twiddles (sb_fft.cuh): entry t =
+  // {mx, my, tau, swap} with e^{-2 pi i t/N} = (-i)^q c (1 + i tau), q the
+  // nearest quarter turn
+  auto gtw = [&](int n) {
+    std::vector<double> v(4 * (size_t)n);
+    for (int t = 0; t < n; t++) {
+      const int q = ((8 * t + n) / (2 * n)) % 4;
+      const double a = g.pi * (double)(q * n - 4 * t) / (2.0 * (double)n);
+      const double c = std::cos(a);
+      const long long sw = q & 1;
+      const double mx = (q <= 1) ? c : -c;
+      v[4 * t] = mx;
+      v[4 * t + 1] = sw ? -mx : mx;
+      v[4 * t + 2] = std::sin(a) / c;
+      std::memcpy(&v[4 * t + 3], &sw, sizeof(double));
+    }
+    return v;
+  };
   std::vector<double> kinv((size_t)nl), ginv((size_t)g.mz);
   for (int k = 0; k < g.mz; k++) {
     int kzs = (k <= g.nz) ? k : k - g.mz;
@@ -517,7 +535,7 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
     *dst = (const float *)q;
     return 0;
   };
-  if ((rc = upload(h, &bf.twz, tw(g.mgalz))) || (rc = upload(h, &bf.twx, tw(g.mgalx))) ||
+  if ((rc = upload(h, &bf.twz, gtw(g.mgalz))) || (rc = upload(h, &bf.twx, gtw(g.mgalx))) ||
       (rc = upload_f(&bf.twzf, tw(g.mgalz))) || (rc = upload_f(&bf.twxf, tw(g.mgalx))) ||
       (rc = upload_f(&bf.kinvf, kinv)) ||
       (rc = upload(h, &bf.kinv, kinv)) || (rc = upload(h, &bf.ginv, ginv)) ||
@@ -525,7 +543,7 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
       (rc = upload_uniform(h, &bf.d2, co.pr2, g.my)) ||
       (g.ydeal == 3 && (rc = upload_uniform(h, &bf.flt, flhs, g.my))) ||
       ((g.ydeal == 1 || g.ydeal == 2) &&
-       ((rc = upload(h, &bf.twy, tw(g.my))) || (rc = upload_f(&bf.twyf, tw(g.my)))))) {
+       ((rc = upload(h, &bf.twy, gtw(g.my))) || (rc = upload_f(&bf.twyf, tw(g.my)))))) {
     sb_destroy(h);
     return rc;
   }

@@ -128,14 +128,14 @@ struct Bufs {
   double *mf1, *mf2;             // moving-frame phases [B][my][nkx] complex
   double *trace;                 // [B][cap][SB_TRACE_LEN]
   Member *mem;                   // [B]
-  const double *twz, *twx;       // FFT twiddles e^{-2 pi i t/N}
-  const float *twzf, *twxf;      // the same, rounded to FP32
+  const double *twz, *twx;       // FFT twiddles e^{-2 pi i t/N}, factored form (sb_fft.cuh)
+  const float *twzf, *twxf;      // the same as complex values, rounded to FP32
   const float *kinvf;            // kinv rounded to FP32
   const double *ginv;            // 1/g per kz  (g = gam * kz_signed; 0 at k=0)
   const double *kinv;            // 1/(alp2+gam2) per (k,i); 0 at (0,0)
   Fac d1, d2, hz;                // d/dy, d2/dy2, Helmholtz (per line)
   Fac flt;                       // left-hand side of the compact y-filter
-  const double *twy;             // y-transform twiddles (iydealiasing 1, 2)
+  const double *twy;             // y-transform twiddles (iydealiasing 1, 2), factored form
   const float *twyf;
   // LES buffers: physical gradient rows [B][my][mgalz/2][6][2][mgalx], |S|^2
   // x-spectra [B][my][mgalz][nkx], stress x-spectra [B][my][mgalz][6][nkx],

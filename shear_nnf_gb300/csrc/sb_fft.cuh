@@ -4,9 +4,28 @@
 // transforms M sequences of length N held contiguously in shared memory
 // (sequence m at [m*N]); the result lands in one of the two ping-pong buffers.
 // Conventions match FFTW: SIGN=-1 is the forward e^{-i} transform, SIGN=+1 the
-// backward e^{+i} transform, both unnormalised.  Radix 4/2/3 stages, autosort
-// (no bit reversal), twiddles from a per-length global table e^{-2 pi i t/N}.
+// backward e^{+i} transform, both unnormalised.  Autosort stages (no bit
+// reversal).
+//
+// Two forms share the stage layout:
+//  * fft_batch_std: radix 4/2/3 stages, twiddles from a per-length table of
+//    e^{-2 pi i t/N} (FP32 storage and the standalone y operators);
+//  * the FP64 form (fft_batch on double2): GB300 issues one FP64 instruction per
+//    two lanes and cycle on each SM sub-partition, so FP64 instruction count is
+//    the cost of a transform.  A twiddle w = e^{-2 pi i t/N} is stored as
+//    w = (-i)^q c (1 + i tau), with q the nearest quarter turn, so c >= cos(pi/4)
+//    and |tau| <= 1; then a +- w b is two FMAs for z = b (1 + i tau) and two per
+//    output (a + c z, a - c z) with the quarter turn a swap of the components of
+//    z (6 FP64 instructions instead of 8 for the complex product and the two
+//    sums).  The radix-4 butterfly uses w3 = w1 w2 to apply only w2 and w1 in
+//    this form (24 instead of 28 per four points), and the radix-3 stage comes
+//    first, where it has no twiddles.  Instructions per point at N = 192:
+//    22 instead of 25.3.  Table entry t: {(mx, my), (tau, swap)} with
+//    (mx, my) = the signed c of the real and imaginary output components and
+//    swap (integer bits) set for odd q.
 #pragma once
+#include <type_traits>
+
 #include "sb_common.cuh"
 
 namespace sb {
@@ -82,10 +101,10 @@ __device__ __forceinline__ void fft_stage(const R2 *__restrict__ in, R2 *__restr
   }
 }
 
-// Full transform of M length-N sequences in A (scratch B); returns the buffer
-// that holds the result.  Ends with a __syncthreads().
+// Full transform of M length-N sequences in A (scratch B), standard twiddle
+// table; returns the buffer that holds the result.  Ends with a __syncthreads().
 template <int N, int SIGN, int M, int T, typename R2>
-__device__ __forceinline__ R2 *fft_batch(R2 *A, R2 *B, const R2 *__restrict__ tw) {
+__device__ __forceinline__ R2 *fft_batch_std(R2 *A, R2 *B, const R2 *__restrict__ tw) {
   __syncthreads();
   if constexpr (N == 32) {
     fft_stage<32, 1, 4, SIGN, M, T>(A, B, tw); __syncthreads();
@@ -125,6 +144,196 @@ __device__ __forceinline__ R2 *fft_batch(R2 *A, R2 *B, const R2 *__restrict__ tw
     static_assert(N == 32, "unsupported transform length");
     return A;
   }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 form with factored twiddles
+// ---------------------------------------------------------------------------
+
+// Twiddle t of the factored table, for the direction SIGN (the backward
+// transform takes the conjugate: tau -> -tau, (mx, my) -> (my, mx)).
+struct GTw {
+  double mx, my, tau;
+  bool sw;
+};
+template <int SIGN>
+__device__ __forceinline__ GTw gtw_load(const double2 *__restrict__ G, int t) {
+  const double2 a = G[2 * t], b = G[2 * t + 1];
+  GTw w;
+  w.mx = (SIGN < 0) ? a.x : a.y;
+  w.my = (SIGN < 0) ? a.y : a.x;
+  w.tau = b.x;
+  w.sw = __double_as_longlong(b.y) != 0;
+  return w;
+}
+// z = v (1 + i tau) (forward) or v (1 - i tau) (backward), components swapped
+// for odd quarter turns: w v = (mx s.x, my s.y)
+template <int SIGN>
+__device__ __forceinline__ double2 gtw_apply(const GTw &w, double2 v) {
+  double za, zb;
+  if (SIGN < 0) {
+    za = fma(-w.tau, v.y, v.x);
+    zb = fma(w.tau, v.x, v.y);
+  } else {
+    za = fma(w.tau, v.y, v.x);
+    zb = fma(-w.tau, v.x, v.y);
+  }
+  double2 s;
+  s.x = w.sw ? zb : za;
+  s.y = w.sw ? za : zb;
+  return s;
+}
+
+// radix-3 stage without twiddles (first stage, Ns = 1): 12 FP64 instructions
+template <int N, int SIGN, int M, int T>
+__device__ __forceinline__ void gstage3(const double2 *__restrict__ in, double2 *__restrict__ out) {
+  constexpr int NR = N / 3;
+  const double s3 = (SIGN < 0) ? 0.86602540378443864676 : -0.86602540378443864676;
+  for (int bt = threadIdx.x; bt < M * NR; bt += T) {
+    const int m = bt / NR;
+    const int j = bt - m * NR;
+    const double2 *src = in + m * N;
+    double2 *dst = out + m * N + 3 * j;
+    const double2 v0 = src[j], v1 = src[j + NR], v2 = src[j + 2 * NR];
+    const double tx = v1.x + v2.x, ty = v1.y + v2.y;
+    const double dx = v1.x - v2.x, dy = v1.y - v2.y;
+    const double hx = fma(-0.5, tx, v0.x), hy = fma(-0.5, ty, v0.y);
+    dst[0] = make_double2(v0.x + tx, v0.y + ty);
+    dst[1] = make_double2(fma(s3, dy, hx), fma(-s3, dx, hy));
+    dst[2] = make_double2(fma(-s3, dy, hx), fma(s3, dx, hy));
+  }
+}
+
+// radix-4 stage without twiddles (first stage, Ns = 1): 16 FP64 instructions
+template <int N, int SIGN, int M, int T>
+__device__ __forceinline__ void gstage4_first(const double2 *__restrict__ in,
+                                              double2 *__restrict__ out) {
+  constexpr int NR = N / 4;
+  for (int bt = threadIdx.x; bt < M * NR; bt += T) {
+    const int m = bt / NR;
+    const int j = bt - m * NR;
+    const double2 *src = in + m * N;
+    double2 *dst = out + m * N + 4 * j;
+    double2 v[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) v[r] = src[j + r * NR];
+    butterfly<4, SIGN>(v);
+#pragma unroll
+    for (int r = 0; r < 4; r++) dst[r] = v[r];
+  }
+}
+
+// twiddled radix-4 stage, sub-transform size Ns: with w1 = w(jm STEP) and
+// w2 = w1^2, a = v0 +- w2 v2, e = v1 +- w2 v3, X0,2 = a0 +- w1 e0,
+// X1,3 = a1 +- J w1 e1 (J = -i forward, +i backward): 24 FP64 instructions
+template <int N, int Ns, int SIGN, int M, int T>
+__device__ __forceinline__ void gstage4(const double2 *__restrict__ in, double2 *__restrict__ out,
+                                        const double2 *__restrict__ G) {
+  constexpr int NR = N / 4;
+  constexpr int STEP = N / (Ns * 4);
+  for (int bt = threadIdx.x; bt < M * NR; bt += T) {
+    const int m = bt / NR;
+    const int j = bt - m * NR;
+    const double2 *src = in + m * N;
+    const int jm = j % Ns;
+    double2 *dst = out + m * N + (j / Ns) * Ns * 4 + jm;
+    const double2 v0 = src[j], v1 = src[j + NR], v2 = src[j + 2 * NR], v3 = src[j + 3 * NR];
+    const GTw w2 = gtw_load<SIGN>(G, 2 * jm * STEP);
+    const GTw w1 = gtw_load<SIGN>(G, jm * STEP);
+    const double2 s2 = gtw_apply<SIGN>(w2, v2);
+    const double a0x = fma(w2.mx, s2.x, v0.x), a0y = fma(w2.my, s2.y, v0.y);
+    const double a1x = fma(-w2.mx, s2.x, v0.x), a1y = fma(-w2.my, s2.y, v0.y);
+    const double2 s3 = gtw_apply<SIGN>(w2, v3);
+    const double2 e0 = make_double2(fma(w2.mx, s3.x, v1.x), fma(w2.my, s3.y, v1.y));
+    const double2 e1 = make_double2(fma(-w2.mx, s3.x, v1.x), fma(-w2.my, s3.y, v1.y));
+    const double2 p = gtw_apply<SIGN>(w1, e0);
+    dst[0] = make_double2(fma(w1.mx, p.x, a0x), fma(w1.my, p.y, a0y));
+    dst[2 * Ns] = make_double2(fma(-w1.mx, p.x, a0x), fma(-w1.my, p.y, a0y));
+    const double2 q = gtw_apply<SIGN>(w1, e1);
+    // J (w1 e1) = (my q.y, -mx q.x) forward, (-my q.y, mx q.x) backward
+    if (SIGN < 0) {
+      dst[Ns] = make_double2(fma(w1.my, q.y, a1x), fma(-w1.mx, q.x, a1y));
+      dst[3 * Ns] = make_double2(fma(-w1.my, q.y, a1x), fma(w1.mx, q.x, a1y));
+    } else {
+      dst[Ns] = make_double2(fma(-w1.my, q.y, a1x), fma(w1.mx, q.x, a1y));
+      dst[3 * Ns] = make_double2(fma(w1.my, q.y, a1x), fma(-w1.mx, q.x, a1y));
+    }
+  }
+}
+
+// twiddled radix-2 stage: X0,1 = v0 +- w1 v1, 6 FP64 instructions
+template <int N, int Ns, int SIGN, int M, int T>
+__device__ __forceinline__ void gstage2(const double2 *__restrict__ in, double2 *__restrict__ out,
+                                        const double2 *__restrict__ G) {
+  constexpr int NR = N / 2;
+  constexpr int STEP = N / (Ns * 2);
+  for (int bt = threadIdx.x; bt < M * NR; bt += T) {
+    const int m = bt / NR;
+    const int j = bt - m * NR;
+    const double2 *src = in + m * N;
+    const int jm = j % Ns;
+    double2 *dst = out + m * N + (j / Ns) * Ns * 2 + jm;
+    const double2 v0 = src[j], v1 = src[j + NR];
+    const GTw w = gtw_load<SIGN>(G, jm * STEP);
+    const double2 s = gtw_apply<SIGN>(w, v1);
+    dst[0] = make_double2(fma(w.mx, s.x, v0.x), fma(w.my, s.y, v0.y));
+    dst[Ns] = make_double2(fma(-w.mx, s.x, v0.x), fma(-w.my, s.y, v0.y));
+  }
+}
+
+// Full FP64 transform with the factored table G (2 N double2 entries).
+template <int N, int SIGN, int M, int T>
+__device__ __forceinline__ double2 *fft_batch_g(double2 *A, double2 *B,
+                                                const double2 *__restrict__ G) {
+  __syncthreads();
+  if constexpr (N == 32) {
+    gstage4_first<32, SIGN, M, T>(A, B); __syncthreads();
+    gstage4<32, 4, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage2<32, 16, SIGN, M, T>(A, B, G); __syncthreads();
+    return B;
+  } else if constexpr (N == 48) {
+    gstage3<48, SIGN, M, T>(A, B); __syncthreads();
+    gstage4<48, 3, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<48, 12, SIGN, M, T>(A, B, G); __syncthreads();
+    return B;
+  } else if constexpr (N == 64) {
+    gstage4_first<64, SIGN, M, T>(A, B); __syncthreads();
+    gstage4<64, 4, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<64, 16, SIGN, M, T>(A, B, G); __syncthreads();
+    return B;
+  } else if constexpr (N == 96) {
+    gstage3<96, SIGN, M, T>(A, B); __syncthreads();
+    gstage4<96, 3, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<96, 12, SIGN, M, T>(A, B, G); __syncthreads();
+    gstage2<96, 48, SIGN, M, T>(B, A, G); __syncthreads();
+    return A;
+  } else if constexpr (N == 192) {
+    gstage3<192, SIGN, M, T>(A, B); __syncthreads();
+    gstage4<192, 3, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<192, 12, SIGN, M, T>(A, B, G); __syncthreads();
+    gstage4<192, 48, SIGN, M, T>(B, A, G); __syncthreads();
+    return A;
+  } else if constexpr (N == 384) {
+    gstage3<384, SIGN, M, T>(A, B); __syncthreads();
+    gstage4<384, 3, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<384, 12, SIGN, M, T>(A, B, G); __syncthreads();
+    gstage4<384, 48, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage2<384, 192, SIGN, M, T>(A, B, G); __syncthreads();
+    return B;
+  } else {
+    static_assert(N == 32, "unsupported transform length");
+    return A;
+  }
+}
+
+// Transform with the device table of the storage type: the factored FP64
+// table for double2, the standard table for float2.
+template <int N, int SIGN, int M, int T, typename R2>
+__device__ __forceinline__ R2 *fft_batch(R2 *A, R2 *B, const R2 *__restrict__ tw) {
+  if constexpr (std::is_same<R2, double2>::value)
+    return fft_batch_g<N, SIGN, M, T>(A, B, tw);
+  else
+    return fft_batch_std<N, SIGN, M, T>(A, B, tw);
 }
 
 }  // namespace sb

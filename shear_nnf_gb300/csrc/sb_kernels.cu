@@ -995,7 +995,8 @@ __global__ void __launch_bounds__(T) k_yop(int nlines, double *c, long ldc, int 
     }
     A[ci * MY + j] = v;
   }
-  double2 *P = (iopt < 0) ? fft_batch<MY, -1, CB, T>(A, Bs, tw) : fft_batch<MY, +1, CB, T>(A, Bs, tw);
+  double2 *P = (iopt < 0) ? fft_batch_std<MY, -1, CB, T>(A, Bs, tw)
+                           : fft_batch_std<MY, +1, CB, T>(A, Bs, tw);
   const double dnf = 1.0 / (double)MY;
   for (int idx = threadIdx.x; idx < CB * (MY + 2); idx += T) {
     const int ci = idx % CB, j = idx / CB, l = l0 + ci;
