@@ -184,8 +184,10 @@ __device__ __forceinline__ double2 gtw_apply(const GTw &w, double2 v) {
   return s;
 }
 
-// radix-3 stage without twiddles (first stage, Ns = 1): 12 FP64 instructions
-template <int N, int SIGN, int M, int T>
+// radix-3 stage without twiddles (first stage, Ns = 1): 12 FP64 instructions.
+// GAP: the middle third of every input sequence is zero (a spectrum under the
+// 2/3 rule with N = 3 * (modes kept per sign)), v1 = 0: 8 instructions.
+template <int N, int SIGN, int M, int T, bool GAP>
 __device__ __forceinline__ void gstage3(const double2 *__restrict__ in, double2 *__restrict__ out) {
   constexpr int NR = N / 3;
   const double s3 = (SIGN < 0) ? 0.86602540378443864676 : -0.86602540378443864676;
@@ -194,13 +196,22 @@ __device__ __forceinline__ void gstage3(const double2 *__restrict__ in, double2 
     const int j = bt - m * NR;
     const double2 *src = in + m * N;
     double2 *dst = out + m * N + 3 * j;
-    const double2 v0 = src[j], v1 = src[j + NR], v2 = src[j + 2 * NR];
-    const double tx = v1.x + v2.x, ty = v1.y + v2.y;
-    const double dx = v1.x - v2.x, dy = v1.y - v2.y;
-    const double hx = fma(-0.5, tx, v0.x), hy = fma(-0.5, ty, v0.y);
-    dst[0] = make_double2(v0.x + tx, v0.y + ty);
-    dst[1] = make_double2(fma(s3, dy, hx), fma(-s3, dx, hy));
-    dst[2] = make_double2(fma(-s3, dy, hx), fma(s3, dx, hy));
+    const double2 v0 = src[j], v2 = src[j + 2 * NR];
+    if constexpr (GAP) {
+      // X0 = v0 + v2, X1,2 = v0 - v2/2 -+ J s3 v2
+      const double hx = fma(-0.5, v2.x, v0.x), hy = fma(-0.5, v2.y, v0.y);
+      dst[0] = make_double2(v0.x + v2.x, v0.y + v2.y);
+      dst[1] = make_double2(fma(-s3, v2.y, hx), fma(s3, v2.x, hy));
+      dst[2] = make_double2(fma(s3, v2.y, hx), fma(-s3, v2.x, hy));
+    } else {
+      const double2 v1 = src[j + NR];
+      const double tx = v1.x + v2.x, ty = v1.y + v2.y;
+      const double dx = v1.x - v2.x, dy = v1.y - v2.y;
+      const double hx = fma(-0.5, tx, v0.x), hy = fma(-0.5, ty, v0.y);
+      dst[0] = make_double2(v0.x + tx, v0.y + ty);
+      dst[1] = make_double2(fma(s3, dy, hx), fma(-s3, dx, hy));
+      dst[2] = make_double2(fma(-s3, dy, hx), fma(s3, dx, hy));
+    }
   }
 }
 
@@ -281,8 +292,9 @@ __device__ __forceinline__ void gstage2(const double2 *__restrict__ in, double2 
   }
 }
 
-// Full FP64 transform with the factored table G (2 N double2 entries).
-template <int N, int SIGN, int M, int T>
+// Full FP64 transform with the factored table G (2 N double2 entries); GAP as
+// for gstage3 (used where N is a multiple of 3).
+template <int N, int SIGN, int M, int T, bool GAP = false>
 __device__ __forceinline__ double2 *fft_batch_g(double2 *A, double2 *B,
                                                 const double2 *__restrict__ G) {
   __syncthreads();
@@ -292,7 +304,7 @@ __device__ __forceinline__ double2 *fft_batch_g(double2 *A, double2 *B,
     gstage2<32, 16, SIGN, M, T>(A, B, G); __syncthreads();
     return B;
   } else if constexpr (N == 48) {
-    gstage3<48, SIGN, M, T>(A, B); __syncthreads();
+    gstage3<48, SIGN, M, T, GAP>(A, B); __syncthreads();
     gstage4<48, 3, SIGN, M, T>(B, A, G); __syncthreads();
     gstage4<48, 12, SIGN, M, T>(A, B, G); __syncthreads();
     return B;
@@ -302,19 +314,19 @@ __device__ __forceinline__ double2 *fft_batch_g(double2 *A, double2 *B,
     gstage4<64, 16, SIGN, M, T>(A, B, G); __syncthreads();
     return B;
   } else if constexpr (N == 96) {
-    gstage3<96, SIGN, M, T>(A, B); __syncthreads();
+    gstage3<96, SIGN, M, T, GAP>(A, B); __syncthreads();
     gstage4<96, 3, SIGN, M, T>(B, A, G); __syncthreads();
     gstage4<96, 12, SIGN, M, T>(A, B, G); __syncthreads();
     gstage2<96, 48, SIGN, M, T>(B, A, G); __syncthreads();
     return A;
   } else if constexpr (N == 192) {
-    gstage3<192, SIGN, M, T>(A, B); __syncthreads();
+    gstage3<192, SIGN, M, T, GAP>(A, B); __syncthreads();
     gstage4<192, 3, SIGN, M, T>(B, A, G); __syncthreads();
     gstage4<192, 12, SIGN, M, T>(A, B, G); __syncthreads();
     gstage4<192, 48, SIGN, M, T>(B, A, G); __syncthreads();
     return A;
   } else if constexpr (N == 384) {
-    gstage3<384, SIGN, M, T>(A, B); __syncthreads();
+    gstage3<384, SIGN, M, T, GAP>(A, B); __syncthreads();
     gstage4<384, 3, SIGN, M, T>(B, A, G); __syncthreads();
     gstage4<384, 12, SIGN, M, T>(A, B, G); __syncthreads();
     gstage4<384, 48, SIGN, M, T>(B, A, G); __syncthreads();
@@ -327,11 +339,13 @@ __device__ __forceinline__ double2 *fft_batch_g(double2 *A, double2 *B,
 }
 
 // Transform with the device table of the storage type: the factored FP64
-// table for double2, the standard table for float2.
-template <int N, int SIGN, int M, int T, typename R2>
+// table for double2, the standard table for float2.  GAP: the caller's input
+// has the zero middle third of the 2/3 rule (backward transforms of a
+// truncated spectrum); only the FP64 form uses it.
+template <int N, int SIGN, int M, int T, bool GAP = false, typename R2>
 __device__ __forceinline__ R2 *fft_batch(R2 *A, R2 *B, const R2 *__restrict__ tw) {
   if constexpr (std::is_same<R2, double2>::value)
-    return fft_batch_g<N, SIGN, M, T>(A, B, tw);
+    return fft_batch_g<N, SIGN, M, T, GAP>(A, B, tw);
   else
     return fft_batch_std<N, SIGN, M, T>(A, B, tw);
 }

@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
       if (i >= nkx) continue;
       A[ci * NZ + kgrid(k, nz, NZ, mz)] = (i == 0 && k == 0) ? mk2<R>(tb00, (R)0) : tbv[k * nkx + i];
     }
-    V *res = fft_batch<NZ, +1, CB, T>(A, Bs, (const V *)tw_of<R>(bf, true));
+    V *res = fft_batch<NZ, +1, CB, T, true>(A, Bs, (const V *)tw_of<R>(bf, true));
     for (int idx = threadIdx.x; idx < CB * NZ; idx += T) {
       const int ci = idx % CB, z = idx / CB, i = i0 + ci;
       if (i < nkx) zb[((long)z * g.nzf + g.tzf) * nkx + i] = res[ci * NZ + z];
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
       A[ci * NZ + kg] = fa;
       A[(CB + ci) * NZ + kg] = fb;
     }
-    V *res = fft_batch<NZ, +1, 2 * CB, T>(A, Bs, (const V *)tw_of<R>(bf, true));
+    V *res = fft_batch<NZ, +1, 2 * CB, T, true>(A, Bs, (const V *)tw_of<R>(bf, true));
     // store Zbuf[z][f][i]
     for (int idx = threadIdx.x; idx < 2 * CB * NZ; idx += T) {
       const int ci = idx % CB, rem = idx / CB;
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
     A[f * NX + i] = mk2<R>(X1.x - X2.y, X1.y + X2.x);
     if (i > 0) A[f * NX + NX - i] = mk2<R>(X1.x + X2.y, -X1.y + X2.x);
   }
-  V *P = fft_batch<NX, +1, NF, T>(A, Bs, (const V *)tw_of<R>(bf, false));
+  V *P = fft_batch<NX, +1, NF, T, true>(A, Bs, (const V *)tw_of<R>(bf, false));
   V *Q = (P == A) ? Bs : A;
   // fields: 0 u, 1 w, 2 omega_x, 3 omega_z, 4 v, 5 omega_y (, 6 tb)
   const R chi2 = (R)(2.0 * g.chi);
@@ -487,15 +487,15 @@ __global__ void __launch_bounds__(T) k_p2(Grid g, Bufs bf, int rk) {
   }
   V *Rr = fft_batch<NX, -1, NO, T>(Q, P, (const V *)tw_of<R>(bf, false));
   V *xb = (V *)bf.xbuf + ((long)b * g.my + j) * (long)NZ * NO * nkx;
-  const R half = (R)0.5;
+  // the two rows' spectra, each times 2: (Z_k + conj Z_-k) and
+  // -i (Z_k - conj Z_-k); k_p3 takes the factor 1/2 with the normalisation
+  // (a power of two: the same rounding)
   for (int idx = threadIdx.x; idx < NO * nkx; idx += T) {
     const int f = idx / nkx, i = idx - f * nkx;
     const V zk = Rr[f * NX + i];
-    V zm = Rr[f * NX + ((NX - i) % NX)];
-    zm.y = -zm.y;
-    const R sx = zk.x + zm.x, syy = zk.y + zm.y, dx = zk.x - zm.x, dy = zk.y - zm.y;
-    xb[((long)z * NO + f) * nkx + i] = mk2<R>(half * sx, half * syy);
-    xb[((long)(z + 1) * NO + f) * nkx + i] = mk2<R>(half * dy, -half * dx);
+    const V zm = Rr[f * NX + ((NX - i) % NX)];
+    xb[((long)z * NO + f) * nkx + i] = mk2<R>(zk.x + zm.x, zk.y - zm.y);
+    xb[((long)(z + 1) * NO + f) * nkx + i] = mk2<R>(zk.y + zm.y, zm.x - zk.x);
   }
 }
 
@@ -526,7 +526,8 @@ __global__ void __launch_bounds__(T) k_p3(Grid g, Bufs bf) {
   V *Dv = (V *)((R *)bf.D + pbase);
   V *Gv = (V *)((R *)bf.G + pbase);
   V *Vv = (V *)((R *)bf.V + pbase);
-  const R norm = (R)(1.0 / (double)(g.mgalx * g.mgalz));
+  // 1/(mgalx mgalz) of the forward transform and the 1/2 of k_p2's row split
+  const R norm = (R)(0.5 / (double)(g.mgalx * g.mgalz));
   const R s = (R)g.s;
   for (int idx = threadIdx.x; idx < CB * mz; idx += T) {
     const int ci = idx % CB, k = idx / CB, i = i0 + ci;
