@@ -106,6 +106,29 @@ static int check_params(const sb_params *p) {
   return 0;
 }
 
+// interleaved row records of the segmented solve (Fac::rows, sb_seg.cuh):
+// row q (0-based) of line `line` of `nl` at rows[(q * nl + line) * 16] =
+// La Lb Lc e f g Dm 0 | hf1 hf2 hf3 0 | hb1 hb2 hb3 0
+static void pack_rows(const sbh::BaseFac &b, const sbh::SegFac &sf, size_t n, size_t nl,
+                      size_t line, std::vector<double> &rows) {
+  for (size_t q = 0; q < n; q++) {
+    double *r = &rows[(q * nl + line) * 16];
+    r[0] = b.La[q];
+    r[1] = b.Lb[q];
+    r[2] = b.Lc[q];
+    r[3] = b.e[q];
+    r[4] = b.f[q];
+    r[5] = b.g[q];
+    r[6] = b.Ddm1[q];
+    r[7] = 0.0;
+    for (int t = 0; t < 3; t++) {
+      r[8 + t] = sf.hf[t][q];
+      r[12 + t] = sf.hb[t][q];
+    }
+    r[11] = r[15] = 0.0;
+  }
+}
+
 // factor tables of one band matrix, same for every line
 static int upload_uniform(sb_handle *h, Fac *F, const double a[7], int n) {
   sbh::BaseFac b;
@@ -127,6 +150,9 @@ static int upload_uniform(sb_handle *h, Fac *F, const double a[7], int n) {
   for (int q = 0; q < 6; q++) s[q] = b.sums[q];
   for (int q = 0; q < 4; q++) s[6 + q] = a[3 + q];
   if ((rc = upload(h, &F->sums, s))) return rc;
+  std::vector<double> rows(16 * (size_t)n);
+  pack_rows(b, sf, (size_t)n, 1, 0, rows);
+  if ((rc = upload(h, &F->rows, rows))) return rc;
   F->stride = 0;
   return 0;
 }
@@ -554,7 +580,7 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
     const size_t n = g.my;
     std::vector<double> La(n * nl), Lb(n * nl), Lc(n * nl), Dm(n * nl), Dd(n * nl), e(n * nl),
         f(n * nl), gg(n * nl), sums(10 * (size_t)nl);
-    std::vector<double> hf[3], hb[3], ef(9 * (size_t)g.nseg * nl);
+    std::vector<double> hf[3], hb[3], ef(9 * (size_t)g.nseg * nl), rows(16 * n * nl);
     for (int t = 0; t < 3; t++) {
       hf[t].assign(n * nl, 0.0);
       hb[t].assign(n * nl, 0.0);
@@ -591,6 +617,7 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
             hb[t][q * nl + line] = sfac.hb[t][q];
           }
         for (size_t q = 0; q < sfac.ef.size(); q++) ef[q * nl + line] = sfac.ef[q];
+        pack_rows(bfac, sfac, n, nl, line, rows);
       }
     Fac &H = bf.hz;
     if ((rc = upload(h, &H.La, La)) || (rc = upload(h, &H.Lb, Lb)) || (rc = upload(h, &H.Lc, Lc)) ||
@@ -599,7 +626,7 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
         (rc = upload(h, &H.hf[0], hf[0])) || (rc = upload(h, &H.hf[1], hf[1])) ||
         (rc = upload(h, &H.hf[2], hf[2])) || (rc = upload(h, &H.hb[0], hb[0])) ||
         (rc = upload(h, &H.hb[1], hb[1])) || (rc = upload(h, &H.hb[2], hb[2])) ||
-        (rc = upload(h, &H.ef, ef))) {
+        (rc = upload(h, &H.ef, ef)) || (rc = upload(h, &H.rows, rows))) {
       sb_destroy(h);
       return rc;
     }

@@ -42,7 +42,10 @@ struct Fac {
   const double *sums;  // 10 entries: See Sfe Sff Sge Sgf Sgg, then a(0..3)
   const double *hf[3], *hb[3];  // segment homogeneous solutions (my entries each)
   const double *ef;             // segment border sums (9 per segment)
-  long stride;
+  // the same per row and line, interleaved for the segmented solve
+  // (sb_seg.cuh): 16 doubles at rows[((row-1) * lines + line) * 16]
+  const double *rows;
+  long stride;                  // lines of a per-line factor (0: one for all lines)
 };
 
 // Constant per-handle parameters (passed by value to every kernel)

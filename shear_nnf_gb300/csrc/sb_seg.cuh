@@ -31,10 +31,25 @@ struct SegView {
   __device__ __forceinline__ double ef(int s, int q, int t) const { return at(F.ef, (s * 3 + q) * 3 + t - 1); }
 };
 
+// Per-row record of the interleaved factor table (Fac::rows), 16 doubles:
+// La Lb Lc e f g Dm 0 | hf1 hf2 hf3 0 | hb1 hb2 hb3 0.  The row loops read it
+// with 16-byte loads from one pointer per line (a few load instructions per
+// row instead of one indexed load per coefficient).
+struct RowPtr {
+  const double *p;
+  long rs;  // doubles per row
+  __device__ RowPtr(const Fac &F, long line)
+      : p(F.rows + (F.stride ? line * 16 : 0)), rs(F.stride ? 16 * F.stride : 16) {}
+  __device__ __forceinline__ const double2 *row(int i) const {
+    return reinterpret_cast<const double2 *>(p + (long)(i - 1) * rs);
+  }
+};
+
 // Solves the line of lane (l, c) in segment s; on return ys[k*ystr] holds the
 // solution at row r0+k (1-based) for the rows this segment owns: lo..hi, and
 // for the top segment also lo..N.  All threads of the block must call this
-// together (it synchronises the block twice).
+// together (it synchronises the block twice).  The shared column holds
+// rend - lo + 5 rows (the segment's rows and four rows of the extension).
 template <int S, typename TU>
 __device__ __forceinline__ void solve_seg(const TU *u, long ps, double *ys, int ystr, int N,
                                           const FacView &V, const SegView &W, const Tail &T, cd shp,
@@ -44,6 +59,7 @@ __device__ __forceinline__ void solve_seg(const TU *u, long ps, double *ys, int 
   const int lo = slo[s], hi = shi[s];
   const bool top = (s == S - 1);
   double *mine = xch + ((s * 16 + l) * 2 + c) * SB_XS;
+  const RowPtr RP(V.F, V.line);
   // wrapped values u(-2..0) = u(N-2..N)*shm, u(N+1..N+3) = u(1..3)*shp (1-based)
   const double uN3 = (double)u[(long)(N - 3) * ps], uN2 = (double)u[(long)(N - 2) * ps],
                uN1 = (double)u[(long)(N - 1) * ps];
@@ -55,47 +71,52 @@ __device__ __forceinline__ void solve_seg(const TU *u, long ps, double *ys, int 
                hi1 = cmul_c(u1, __shfl_xor_sync(0xffffffffu, u1, 1), shp, c),
                hi2 = cmul_c(u2, __shfl_xor_sync(0xffffffffu, u2, 1), shp, c);
   const int rend = top ? N : hi;
-  // stage the segment's rows of u in the solution column: all loads issued
-  // up front instead of one per step of the recurrence; the forward sweep
-  // reads row i+4 before it overwrites row i
-#pragma unroll 8
-  for (int i = lo; i <= rend; i++) ys[(i - lo) * ystr] = (double)u[(long)(i - 1) * ps];
-  auto ext = [&](int i) -> double {  // extended line, 1-based row
+  auto ext = [&](int i) -> double {  // extended line, 1-based row, from the field
     if (i < 1) return i == -2 ? lo3 : (i == -1 ? lo2 : lo1);
     if (i > N) return i == N + 1 ? hi0 : (i == N + 2 ? hi1 : hi2);
-    if (i >= lo && i <= rend) return ys[(i - lo) * ystr];
     return (double)u[(long)(i - 1) * ps];
   };
+  // stage the segment's rows of u and the next four rows of the extended line
+  // in the solution column: all loads issued up front, and the forward sweep
+  // reads row i+4 from the column (before the row is overwritten)
+#pragma unroll 8
+  for (int i = lo; i <= rend; i++) ys[(i - lo) * ystr] = (double)u[(long)(i - 1) * ps];
+#pragma unroll
+  for (int t = 1; t <= 4; t++) ys[(rend - lo + t) * ystr] = ext(rend + t);
   // ---- forward substitution of the segment from a zero incoming state
-  double w0 = ext(lo - 3), w1 = ext(lo - 2), w2 = ext(lo - 1), w3 = ext(lo), w4 = ext(lo + 1),
-         w5 = ext(lo + 2), w6 = ext(lo + 3);
+  double w0 = ext(lo - 3), w1 = ext(lo - 2), w2 = ext(lo - 1), w3 = ys[0], w4 = ys[ystr],
+         w5 = ys[2 * ystr], w6 = ys[3 * ystr];
   double y1 = 0.0, y2 = 0.0, y3 = 0.0, Se = 0.0, Sf = 0.0, Sg = 0.0;
-  double bN2 = 0.0, bN1 = 0.0, bN0 = 0.0;
+  auto stencil = [&]() -> double {
+    return anti ? r1 * (w4 - w2) + r2 * (w5 - w1) + r3 * (w6 - w0)
+                : r0 * w3 + r1 * (w4 + w2) + r2 * (w5 + w1) + r3 * (w6 + w0);
+  };
 #pragma unroll 4
-  for (int i = lo; i <= rend; i++) {
-    double rhs;
-    if (anti)
-      rhs = r1 * (w4 - w2) + r2 * (w5 - w1) + r3 * (w6 - w0);
-    else
-      rhs = r0 * w3 + r1 * (w4 + w2) + r2 * (w5 + w1) + r3 * (w6 + w0);
-    if (i <= hi) {
-      const double y = rhs - V.Lc(i) * y3 - V.Lb(i) * y2 - V.La(i) * y1;
-      ys[(i - lo) * ystr] = y;
-      Se = fma(V.e(i), y, Se);
-      Sf = fma(V.f(i), y, Sf);
-      Sg = fma(V.g(i), y, Sg);
-      y3 = y2;
-      y2 = y1;
-      y1 = y;
-    } else if (i == N - 2) {
-      bN2 = rhs;
-    } else if (i == N - 1) {
-      bN1 = rhs;
-    } else {
-      bN0 = rhs;
-    }
+  for (int i = lo; i <= hi; i++) {
+    const double2 *rw = RP.row(i);
+    const double2 ab = __ldg(rw), ce = __ldg(rw + 1), fg = __ldg(rw + 2);
+    const double rhs = stencil();
+    const double y = rhs - ce.x * y3 - ab.y * y2 - ab.x * y1;
+    ys[(i - lo) * ystr] = y;
+    Se = fma(ce.y, y, Se);
+    Sf = fma(fg.x, y, Sf);
+    Sg = fma(fg.y, y, Sg);
+    y3 = y2;
+    y2 = y1;
+    y1 = y;
     w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = w5; w5 = w6;
-    w6 = ext(i + 4);
+    w6 = ys[(i + 4 - lo) * ystr];
+  }
+  // the right-hand sides of the bordered rows N-2..N (top segment)
+  double bN2 = 0.0, bN1 = 0.0, bN0 = 0.0;
+  if (top) {
+    bN2 = stencil();
+    w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = w5; w5 = w6;
+    w6 = ys[(N + 2 - lo) * ystr];
+    bN1 = stencil();
+    w0 = w1; w1 = w2; w2 = w3; w3 = w4; w4 = w5; w5 = w6;
+    w6 = ys[(N + 3 - lo) * ystr];
+    bN0 = stencil();
   }
   mine[0] = y1;  // rows hi, hi-1, hi-2
   mine[1] = y2;
@@ -175,17 +196,30 @@ __device__ __forceinline__ void solve_seg(const TU *u, long ps, double *ys, int 
     xc = comp(x3, c);
     ibeg = N - 6;
   }
+  // La(i+1), Lb(i+1..i+2), Lc(i+1..i+3) of the rows above, carried down
+  double La1 = V.La(ibeg + 1), Lb1 = V.Lb(ibeg + 1), Lb2 = V.Lb(ibeg + 2), Lc1 = V.Lc(ibeg + 1),
+         Lc2 = V.Lc(ibeg + 2), Lc3 = V.Lc(ibeg + 3);
+  // the first segment starts from the true zero state: no homogeneous part
+  const bool hom = (s > 0);
 #pragma unroll 4
   for (int i = ibeg; i >= lo; i--) {
-    const double y = ys[(i - lo) * ystr] + W.hf(1, i) * Ya + W.hf(2, i) * Yb + W.hf(3, i) * Yc;
+    const double2 *rw = RP.row(i);
+    const double2 ab = __ldg(rw), ce = __ldg(rw + 1), fg = __ldg(rw + 2), dm = __ldg(rw + 3);
+    double y = ys[(i - lo) * ystr];
+    if (hom) {
+      const double2 h12 = __ldg(rw + 4), h3 = __ldg(rw + 5);
+      y = y + h12.x * Ya + h12.y * Yb + h3.x * Yc;
+    }
     // the previous row enters last: one dependent multiply-add per row on the
     // loop-carried path (the reference's order puts it first)
-    const double x = V.Dm(i) * y - V.e(i) * pe - V.f(i) * pf - V.g(i) * pg - V.Lc(i + 3) * xc -
-                     V.Lb(i + 2) * xb - V.La(i + 1) * xa;
+    const double x = dm.x * y - ce.y * pe - fg.x * pf - fg.y * pg - Lc3 * xc - Lb2 * xb - La1 * xa;
     ys[(i - lo) * ystr] = x;
     xc = xb;
     xb = xa;
     xa = x;
+    Lc3 = Lc2; Lc2 = Lc1; Lc1 = ce.x;
+    Lb2 = Lb1; Lb1 = ab.y;
+    La1 = ab.x;
   }
   mine[9] = ys[0];  // rows lo, lo+1, lo+2
   mine[10] = ys[ystr];
@@ -212,8 +246,11 @@ __device__ __forceinline__ void solve_seg(const TU *u, long ps, double *ys, int 
     X[2] = Xn[2];
   }
 #pragma unroll 4
-  for (int i = lo; i <= hi; i++)
-    ys[(i - lo) * ystr] += W.hb(1, i) * X[0] + W.hb(2, i) * X[1] + W.hb(3, i) * X[2];
+  for (int i = lo; i <= hi; i++) {
+    const double2 *rw = RP.row(i);
+    const double2 h12 = __ldg(rw + 6), h3 = __ldg(rw + 7);
+    ys[(i - lo) * ystr] += h12.x * X[0] + h12.y * X[1] + h3.x * X[2];
+  }
 }
 
 }  // namespace sb

@@ -56,6 +56,10 @@ __device__ __forceinline__ cd ldc2(const double *p) { return mk(p[0], p[1]); }
 #ifndef SB_LINE_MINB
 #define SB_LINE_MINB 1
 #endif
+// k_lineA: six blocks per SM (170 registers) keep its three roles resident
+#ifndef SB_LINEA_MINB
+#define SB_LINEA_MINB 6
+#endif
 constexpr int kSeg = SB_KSEG;
 struct LineThread {
   int b, role, c, s, l, i, k, r0, r1;
@@ -156,7 +160,7 @@ __device__ __forceinline__ void rk_update(const double *ys, int ystr, const R *_
 // TEMP: the temperature roles are compiled in (a separate instantiation, so
 // that the plain step keeps its register budget)
 template <typename R, bool TEMP>
-__global__ void __launch_bounds__(32 * kSeg, TEMP ? 5 : SB_LINE_MINB) k_lineA(Grid g, Bufs bf, int rk1) {
+__global__ void __launch_bounds__(32 * kSeg, TEMP ? 5 : SB_LINEA_MINB) k_lineA(Grid g, Bufs bf, int rk1) {
   __shared__ double xch[kSeg][16][2][SB_XS];
   LineThread L;
   if (!line_thread(g, 3, &L)) return;  // whole blocks
@@ -991,15 +995,15 @@ __global__ void k_finish(Grid g, Bufs bf) {
 // ---------------------------------------------------------------------------
 static const int kLineT = 32 * kSeg;
 
-// shared-memory bytes of the line kernels: one column of the longest segment
-// per thread
+// shared-memory bytes of the line kernels: one column per thread of the
+// longest segment and four rows of the extended line beyond it
 static size_t smem_of(const Grid &g) {
   int rows = 0;
   for (int s = 0; s < g.nseg; s++) {
     const int r1 = (s == g.nseg - 1) ? g.my : g.shi[s];
     rows = rows > r1 - g.slo[s] + 1 ? rows : r1 - g.slo[s] + 1;
   }
-  return sizeof(double) * kLineT * rows;
+  return sizeof(double) * kLineT * (rows + 4);
 }
 
 template <typename R>
