@@ -512,12 +512,16 @@ def run_ours(args):
     box.cross(host, 1)  # warm-up
     torch.cuda.synchronize()
     barrier(dist)
+    calls = []
     t0 = time.perf_counter()
     for _ in range(ne2e):
+        c0 = time.perf_counter()
         box.cross(host, 1)
+        calls.append(time.perf_counter() - c0)
     t1 = time.perf_counter()
     barrier(dist)
     e2e_s = allmax(dist, t1 - t0)
+    calls_ms = 1e3 * np.array(calls)
     bytes_io = 2 * nf * 16 + 2 * my * 8 + 3 * 8
     # FP32-mixed precision form: same workload, steps/s, and the field error
     # against the FP64 path at steps 1, 10, 100, 200 from the same initial field
@@ -578,7 +582,9 @@ def run_ours(args):
                                            "time": status.time}}),
         "e2e": {"value": ws * ne2e / e2e_s, "unit": "steps/s",
                 "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io,
-                "api": "sb_cross(nstep=1), pinned host buffers"},
+                "api": "sb_cross(nstep=1), pinned host buffers",
+                "per_call_ms": {"median": float(np.median(calls_ms)), "min": float(calls_ms.min()),
+                                "max": float(calls_ms.max())}},
         "gpu_launches": launches,
         "roofline": {
             "bound": "fp64", "kernel": "k_p2 (plane stage 2: x transforms, u x omega)",

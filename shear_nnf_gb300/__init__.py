@@ -394,7 +394,12 @@ class ShearBox:
                                   _dp(state["w00"]), ctypes.byref(t), ctypes.byref(xb),
                                   ctypes.byref(xt), int(nstep), ctypes.byref(st)))
         state["time"], state["xoffb"], state["xofft"] = t.value, xb.value, xt.value
-        return self.trace(0), st
+        # the records of this call (the status came with the state)
+        m = max(st.ntrace, 0)
+        out = np.zeros((max(m, 1), TRACE_LEN_T if self.p.temperature else TRACE_LEN))
+        n = ctypes.c_int()
+        _check(lib().sb_get_trace(self.h, 0, _dp(out), m, ctypes.byref(n)))
+        return out[: n.value], st
 
 
 def op_derivyc(my: int, Ly: float, iord: int, u_dev: int, out_dev: int, nlines: int,

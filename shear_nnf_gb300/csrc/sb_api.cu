@@ -54,9 +54,18 @@ struct sb_handle {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // the spectra of a statistics step run beside plane stages 1-2
   cudaEvent_t ev_s0 = nullptr, ev_s1 = nullptr;
+  // the host copies of phi run on the side stream beside those of omega_y
+  cudaEvent_t ev_c0 = nullptr, ev_c1 = nullptr;
   cudaGraphExec_t step_exec = nullptr;
   std::vector<void *> allocs;
-  double *d_pen = nullptr;  // staging buffer, one pencil-layout field
+  double *d_pen = nullptr;  // staging buffers, one pencil-layout field each
+  double *d_pen2 = nullptr;
+  // pinned host staging of the small per-call values (mean profiles, time and
+  // offsets, the member record), so that a cross call synchronises once
+  struct HostSmall {
+    double mu_in[2 * 448], mu_out[2 * 448], sc_in[3], sc_out[3];
+    Member m;
+  } *hs = nullptr;
   int trace_cap = 0;
   std::vector<Member> mem_init;
 };
@@ -244,6 +253,9 @@ static int capture_step(sb_handle *h) {
 static int ensure_trace(sb_handle *h, int cap) {
   if (cap <= h->trace_cap) return 0;
   cap = std::max(cap, 2 * h->trace_cap);
+  // no copies in flight on either stream before the step graph is re-captured
+  if (h->st) CK(cudaStreamSynchronize(h->st));
+  if (h->side) CK(cudaStreamSynchronize(h->side));
   double *t;
   int rc = dalloc(h, &t, (size_t)h->g.B * cap * h->g.tlen);
   if (rc) return rc;
@@ -450,6 +462,9 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->ev_s0, cudaEventDisableTiming);
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->ev_s1, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->ev_c0, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->ev_c1, cudaEventDisableTiming);
+  if (ce == cudaSuccess) ce = cudaMallocHost((void **)&h->hs, sizeof(sb_handle::HostSmall));
   if (ce != cudaSuccess) {
     sb_destroy(h);
     return fail(3, "stream: %s", cudaGetErrorString(ce));
@@ -470,7 +485,8 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
       (rc = A(&bf.hpart, B * my * ((g.nkx * g.mz + 15) / 16) * SB_NHIST_Q)) ||
       (rc = A(&bf.hsum, B * my * (SB_NHIST_Q + 5))) || (rc = A(&bf.sh_old, B * 4 * g.nkx)) ||
       (rc = A(&bf.sh_new, B * 4 * g.nkx)) || (rc = A(&bf.mf1, B * my * g.nkx * 2)) ||
-      (rc = A(&bf.mf2, B * my * g.nkx * 2)) || (rc = A(&h->d_pen, F))) {
+      (rc = A(&bf.mf2, B * my * g.nkx * 2)) || (rc = A(&h->d_pen, F)) ||
+      (rc = A(&h->d_pen2, F))) {
     sb_destroy(h);
     return rc;
   }
@@ -658,12 +674,15 @@ int sb_destroy(sb_handle *h) {
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
   for (void *q : h->allocs) cudaFree(q);
+  if (h->hs) cudaFreeHost(h->hs);
   if (h->st) cudaStreamDestroy(h->st);
   if (h->side) cudaStreamDestroy(h->side);
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
   if (h->ev_s0) cudaEventDestroy(h->ev_s0);
   if (h->ev_s1) cudaEventDestroy(h->ev_s1);
+  if (h->ev_c0) cudaEventDestroy(h->ev_c0);
+  if (h->ev_c1) cudaEventDestroy(h->ev_c1);
   delete h;
   return 0;
 }
@@ -692,79 +711,109 @@ int sb_set_member_etime(sb_handle *h, int member, double etime) {
   return 0;
 }
 
-int sb_set_state(sb_handle *h, int member, const double *vor, const double *phi, const double *u00,
-                 const double *w00, double time, double xoffb, double xofft) {
+// State in (pencil layout -> planes) through the two staging buffers; the
+// small values go through pinned host memory, so nothing here waits for the
+// device unless `sync` (the public call: the caller may reuse its arrays).
+static int set_state_impl(sb_handle *h, int member, const double *vor, const double *phi,
+                          const double *u00, const double *w00, double time, double xoffb,
+                          double xofft, bool sync) {
   if (!h || member < 0 || member >= h->g.B) return fail(1, "bad handle or member");
   if (!vor || !phi || !u00 || !w00) return fail(1, "null state array");
   const Grid &g = h->g;
   const size_t F = g.field;
-  CK(cudaMemcpyAsync(h->d_pen, vor, sizeof(double) * F, cudaMemcpyHostToDevice, h->st));
   const size_t Fd = g.prec ? F / 2 : F;  // field size in doubles of the storage type
+  // phi on the side stream, after the work already queued on the main one
+  CK(cudaEventRecord(h->ev_c0, h->st));
+  CK(cudaStreamWaitEvent(h->side, h->ev_c0, 0));
+  CK(cudaMemcpyAsync(h->d_pen2, phi, sizeof(double) * F, cudaMemcpyHostToDevice, h->side));
+  CK(launch_pencil_to_plane(g, h->d_pen2, h->bf.phi + member * Fd, h->side));
+  CK(cudaEventRecord(h->ev_c1, h->side));
+  CK(cudaMemcpyAsync(h->d_pen, vor, sizeof(double) * F, cudaMemcpyHostToDevice, h->st));
   CK(launch_pencil_to_plane(g, h->d_pen, h->bf.vor + member * Fd, h->st));
-  CK(cudaMemcpyAsync(h->d_pen, phi, sizeof(double) * F, cudaMemcpyHostToDevice, h->st));
-  CK(launch_pencil_to_plane(g, h->d_pen, h->bf.phi + member * Fd, h->st));
-  std::vector<double> mu(2 * (size_t)g.my);
-  std::vector<float> muf(2 * (size_t)g.my);
-  for (int j = 0; j < g.my; j++) {
-    mu[2 * j] = u00[j];
-    mu[2 * j + 1] = w00[j];
-    muf[2 * j] = (float)u00[j];
-    muf[2 * j + 1] = (float)w00[j];
+  CK(cudaStreamWaitEvent(h->st, h->ev_c1, 0));
+  sb_handle::HostSmall &hs = *h->hs;
+  if (g.prec) {
+    float *muf = (float *)hs.mu_in;
+    for (int j = 0; j < g.my; j++) {
+      muf[2 * j] = (float)u00[j];
+      muf[2 * j + 1] = (float)w00[j];
+    }
+    CK(cudaMemcpyAsync((float *)h->bf.mu + (size_t)member * 2 * g.my, muf,
+                       sizeof(float) * 2 * g.my, cudaMemcpyHostToDevice, h->st));
+  } else {
+    for (int j = 0; j < g.my; j++) {
+      hs.mu_in[2 * j] = u00[j];
+      hs.mu_in[2 * j + 1] = w00[j];
+    }
+    CK(cudaMemcpyAsync(h->bf.mu + (size_t)member * 2 * g.my, hs.mu_in,
+                       sizeof(double) * 2 * g.my, cudaMemcpyHostToDevice, h->st));
   }
-  if (g.prec)
-    CK(cudaMemcpyAsync((float *)h->bf.mu + (size_t)member * 2 * g.my, muf.data(),
-                       sizeof(float) * muf.size(), cudaMemcpyHostToDevice, h->st));
-  else
-    CK(cudaMemcpyAsync(h->bf.mu + (size_t)member * 2 * g.my, mu.data(), sizeof(double) * mu.size(),
-                       cudaMemcpyHostToDevice, h->st));
-  double sc[3] = {time, xoffb, xofft};
-  CK(cudaMemcpyAsync((char *)(h->bf.mem + member) + offsetof(Member, time), sc, sizeof(sc),
-                     cudaMemcpyHostToDevice, h->st));
+  hs.sc_in[0] = time;
+  hs.sc_in[1] = xoffb;
+  hs.sc_in[2] = xofft;
+  CK(cudaMemcpyAsync((char *)(h->bf.mem + member) + offsetof(Member, time), hs.sc_in,
+                     sizeof(hs.sc_in), cudaMemcpyHostToDevice, h->st));
   // a new state restarts the LES running maximum of nu_t
-  static const double zero = 0.0;
-  CK(cudaMemcpyAsync((char *)(h->bf.mem + member) + offsetof(Member, max_nut), &zero,
-                     sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemsetAsync((char *)(h->bf.mem + member) + offsetof(Member, max_nut), 0, sizeof(double),
+                     h->st));
+  if (sync) CK(cudaStreamSynchronize(h->st));
+  return 0;
+}
+
+int sb_set_state(sb_handle *h, int member, const double *vor, const double *phi, const double *u00,
+                 const double *w00, double time, double xoffb, double xofft) {
+  return set_state_impl(h, member, vor, phi, u00, w00, time, xoffb, xofft, true);
+}
+
+// State out through the two staging buffers, one synchronisation; with `st`
+// also the member's status from the same copy.
+static void fill_status(const Member &m, sb_status *st);
+static int get_state_impl(sb_handle *h, int member, double *vor, double *phi, double *u00,
+                          double *w00, double *time, double *xoffb, double *xofft,
+                          sb_status *st) {
+  if (!h || member < 0 || member >= h->g.B) return fail(1, "bad handle or member");
+  const Grid &g = h->g;
+  const size_t F = g.field;
+  const size_t Fd = g.prec ? F / 2 : F;
+  // phi on the side stream beside omega_y
+  if (phi) {
+    CK(cudaEventRecord(h->ev_c0, h->st));
+    CK(cudaStreamWaitEvent(h->side, h->ev_c0, 0));
+    CK(launch_plane_to_pencil(g, h->bf.phi + member * Fd, h->d_pen2, h->side));
+    CK(cudaMemcpyAsync(phi, h->d_pen2, sizeof(double) * F, cudaMemcpyDeviceToHost, h->side));
+    CK(cudaEventRecord(h->ev_c1, h->side));
+  }
+  if (vor) {
+    CK(launch_plane_to_pencil(g, h->bf.vor + member * Fd, h->d_pen, h->st));
+    CK(cudaMemcpyAsync(vor, h->d_pen, sizeof(double) * F, cudaMemcpyDeviceToHost, h->st));
+  }
+  if (phi) CK(cudaStreamWaitEvent(h->st, h->ev_c1, 0));
+  sb_handle::HostSmall &hs = *h->hs;
+  const size_t mub = (g.prec ? sizeof(float) : sizeof(double)) * 2 * g.my;
+  CK(cudaMemcpyAsync(hs.mu_out, (const char *)h->bf.mu + (size_t)member * mub, mub,
+                     cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(hs.sc_out, (char *)(h->bf.mem + member) + offsetof(Member, time),
+                     sizeof(hs.sc_out), cudaMemcpyDeviceToHost, h->st));
+  if (st)
+    CK(cudaMemcpyAsync(&hs.m, h->bf.mem + member, sizeof(Member), cudaMemcpyDeviceToHost, h->st));
   CK(cudaStreamSynchronize(h->st));
+  const float *muf = (const float *)hs.mu_out;
+  for (int j = 0; j < g.my; j++) {
+    const double u = g.prec ? (double)muf[2 * j] : hs.mu_out[2 * j];
+    const double w = g.prec ? (double)muf[2 * j + 1] : hs.mu_out[2 * j + 1];
+    if (u00) u00[j] = u;
+    if (w00) w00[j] = w;
+  }
+  if (time) *time = hs.sc_out[0];
+  if (xoffb) *xoffb = hs.sc_out[1];
+  if (xofft) *xofft = hs.sc_out[2];
+  if (st) fill_status(hs.m, st);
   return 0;
 }
 
 int sb_get_state(sb_handle *h, int member, double *vor, double *phi, double *u00, double *w00,
                  double *time, double *xoffb, double *xofft) {
-  if (!h || member < 0 || member >= h->g.B) return fail(1, "bad handle or member");
-  const Grid &g = h->g;
-  const size_t F = g.field;
-  const size_t Fd = g.prec ? F / 2 : F;
-  if (vor) {
-    CK(launch_plane_to_pencil(g, h->bf.vor + member * Fd, h->d_pen, h->st));
-    CK(cudaMemcpyAsync(vor, h->d_pen, sizeof(double) * F, cudaMemcpyDeviceToHost, h->st));
-  }
-  if (phi) {
-    CK(cudaStreamSynchronize(h->st));
-    CK(launch_plane_to_pencil(g, h->bf.phi + member * Fd, h->d_pen, h->st));
-    CK(cudaMemcpyAsync(phi, h->d_pen, sizeof(double) * F, cudaMemcpyDeviceToHost, h->st));
-  }
-  std::vector<double> mu(2 * (size_t)g.my);
-  std::vector<float> muf(2 * (size_t)g.my);
-  if (g.prec)
-    CK(cudaMemcpyAsync(muf.data(), (float *)h->bf.mu + (size_t)member * 2 * g.my,
-                       sizeof(float) * muf.size(), cudaMemcpyDeviceToHost, h->st));
-  else
-    CK(cudaMemcpyAsync(mu.data(), h->bf.mu + (size_t)member * 2 * g.my, sizeof(double) * mu.size(),
-                       cudaMemcpyDeviceToHost, h->st));
-  double sc[3];
-  CK(cudaMemcpyAsync(sc, (char *)(h->bf.mem + member) + offsetof(Member, time), sizeof(sc),
-                     cudaMemcpyDeviceToHost, h->st));
-  CK(cudaStreamSynchronize(h->st));
-  if (g.prec)
-    for (size_t q = 0; q < mu.size(); q++) mu[q] = (double)muf[q];
-  for (int j = 0; j < g.my; j++) {
-    if (u00) u00[j] = mu[2 * j];
-    if (w00) w00[j] = mu[2 * j + 1];
-  }
-  if (time) *time = sc[0];
-  if (xoffb) *xoffb = sc[1];
-  if (xofft) *xofft = sc[2];
-  return 0;
+  return get_state_impl(h, member, vor, phi, u00, w00, time, xoffb, xofft, nullptr);
 }
 
 // mean profile of one member: [my] reals <-> the re parts of a [my] complex
@@ -845,11 +894,7 @@ int sb_step(sb_handle *h, int nsteps) {
   return 0;
 }
 
-int sb_get_status(sb_handle *h, int member, sb_status *st) {
-  if (!h || !st || member < 0 || member >= h->g.B) return fail(1, "bad argument");
-  Member m;
-  CK(cudaMemcpyAsync(&m, h->bf.mem + member, sizeof(Member), cudaMemcpyDeviceToHost, h->st));
-  CK(cudaStreamSynchronize(h->st));
+static void fill_status(const Member &m, sb_status *st) {
   st->istop = m.istop;
   st->steps_done = m.istep - 1;
   st->ntrace = m.ntrace;
@@ -860,6 +905,14 @@ int sb_get_status(sb_handle *h, int member, sb_status *st) {
   st->xofft = m.xofft;
   st->cfl = m.CFLcur;
   st->cflv = m.CFLv;
+}
+
+int sb_get_status(sb_handle *h, int member, sb_status *st) {
+  if (!h || !st || member < 0 || member >= h->g.B) return fail(1, "bad argument");
+  Member m;
+  CK(cudaMemcpyAsync(&m, h->bf.mem + member, sizeof(Member), cudaMemcpyDeviceToHost, h->st));
+  CK(cudaStreamSynchronize(h->st));
+  fill_status(m, st);
   return 0;
 }
 
@@ -879,12 +932,12 @@ int sb_get_trace(sb_handle *h, int member, double *out, int max_records, int *nr
 int sb_cross(sb_handle *h, double *vor, double *phi, double *u00, double *w00, double *time,
              double *xoffb, double *xofft, int nstep, sb_status *st) {
   if (!h || !time || !xoffb || !xofft) return fail(1, "null argument");
-  int rc = sb_set_state(h, 0, vor, phi, u00, w00, *time, *xoffb, *xofft);
+  // the arrays belong to the call until it returns: one synchronisation, at
+  // the end
+  int rc = set_state_impl(h, 0, vor, phi, u00, w00, *time, *xoffb, *xofft, false);
   if (rc) return rc;
   if ((rc = sb_step(h, nstep))) return rc;
-  if ((rc = sb_get_state(h, 0, vor, phi, u00, w00, time, xoffb, xofft))) return rc;
-  if (st && (rc = sb_get_status(h, 0, st))) return rc;
-  return 0;
+  return get_state_impl(h, 0, vor, phi, u00, w00, time, xoffb, xofft, st);
 }
 
 int sb_get_statistics(sb_handle *h, int member, double *stats, double *stats2, double *spec,
