@@ -50,9 +50,24 @@ struct RowPtr {
 // for the top segment also lo..N.  All threads of the block must call this
 // together (it synchronises the block twice).  The shared column holds
 // rend - lo + 5 rows (the segment's rows and four rows of the extension).
-template <int S, typename TU>
+// Sources of the shear tail (Tail) of the factorisation, evaluated only where
+// the bordered rows need it, so that its 21 values are not live through the
+// row loops: from the per-kx table of k_tables, or computed for a per-line
+// factorisation.
+struct TailLoad {
+  const double *p;
+  __device__ __forceinline__ Tail operator()() const { return load_tail(p); }
+};
+struct TailMake {
+  const FacView &V;
+  cd shp;
+  int N;
+  __device__ __forceinline__ Tail operator()() const { return make_tail(V, shp, N); }
+};
+
+template <int S, typename TU, class TF>
 __device__ __forceinline__ void solve_seg(const TU *u, long ps, double *ys, int ystr, int N,
-                                          const FacView &V, const SegView &W, const Tail &T, cd shp,
+                                          const FacView &V, const SegView &W, const TF &tailf, cd shp,
                                           cd shm, int c, int s, int l, const int *slo,
                                           const int *shi, double r0, double r1, double r2,
                                           double r3, bool anti, double *xch) {
@@ -161,6 +176,7 @@ __device__ __forceinline__ void solve_seg(const TU *u, long ps, double *ys, int 
   const double *xt0 = xch + (((S - 1) * 16 + l) * 2 + 0) * SB_XS;
   const double *xt1 = xch + (((S - 1) * 16 + l) * 2 + 1) * SB_XS;
   // ---- bordered rows N-2..N and the first back-substitution rows (complex)
+  const Tail T = tailf();
   const cd Y3 = mk(ylast[0][0], ylast[1][0]), Y4 = mk(ylast[0][1], ylast[1][1]),
            Y5 = mk(ylast[0][2], ylast[1][2]);
   const cd cSe = mk(tot[0][0], tot[1][0]), cSf = mk(tot[0][1], tot[1][1]),

@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(32 * kSeg, TEMP ? 5 : SB_LINEA_MINB) k_lineA(G
     // computes a d/dy of the mean that is not used
     const bool ts = TEMP && L.l == 1;
     if (TEMP) {
-      const Tail T1 = load_tail(bf.tl1o + (long)L.b * g.nkx * SB_TAIL);
+      const TailLoad T1{bf.tl1o + (long)L.b * g.nkx * SB_TAIL};
       const R *src = ts ? (const R *)bf.R2 + (long)L.b * g.field + L.c : (const R *)mu;
       SEG_SOLVE(src, ts ? g.plane : 2L, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6],
                 true);
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(32 * kSeg, TEMP ? 5 : SB_LINEA_MINB) k_lineA(G
         for (int i = L.r0; i <= L.r1; i++) mtr[2 * (i - 1)] = (R)ys[(i - L.r0) * ystr];
       }
     }
-    const Tail T2 = load_tail(bf.tl2o + (long)L.b * g.nkx * SB_TAIL);
+    const TailLoad T2{bf.tl2o + (long)L.b * g.nkx * SB_TAIL};
     R *mline = ts ? (R *)bf.mt + (long)L.b * 2 * N + L.c : mu;
     SEG_SOLVE(mline, 2, V2, W2, T2, one, one, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6], false);
     const R gk = (R)kGama[rk], zk = (R)kZeta[rk];
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(32 * kSeg, TEMP ? 5 : SB_LINEA_MINB) k_lineA(G
   const double a = g.alp * i;
   const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
   if (L.role == 0) {
-    const Tail T1 = load_tail(bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL);
+    const TailLoad T1{bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL};
     // d/dy (dH1/dx + dH3/dz) (cross.f90:565-575)
     SEG_SOLVE((const R *)bf.D + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
               g.rh1[6], true);
@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(32 * kSeg, TEMP ? 5 : SB_LINEA_MINB) k_lineA(G
     }
     return;
   }
-  const Tail T2 = load_tail(bf.tl2o + ((long)L.b * g.nkx + i) * SB_TAIL);
+  const TailLoad T2{bf.tl2o + ((long)L.b * g.nkx + i) * SB_TAIL};
   if (L.role == 2) {
     // d2(phi)/dy2 for the viscous term of the phi equation (cross.f90:660)
     SEG_SOLVE((const R *)bf.phi + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs 
     const R *mu = (const R *)bf.mu + (long)L.b * 2 * N + L.c;
     R *mdu = (R *)bf.mdu + (long)L.b * 2 * N + L.c;
     const cd one = mk(1.0, 0.0);
-    const Tail T1 = load_tail(bf.tl1o + (long)L.b * g.nkx * SB_TAIL);
+    const TailLoad T1{bf.tl1o + (long)L.b * g.nkx * SB_TAIL};
     SEG_SOLVE(mu, 2, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true);
     if (L.active)
       for (int i = L.r0; i <= L.r1; i++) mdu[2 * (i - 1)] = (R)ys[(i - L.r0) * ystr];
@@ -328,7 +328,7 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs 
   const double *tl2 = (mode == 0) ? bf.tl2o : bf.tl2n;
   const cd shp = ldc2(sh + (long)L.b * 4 * g.nkx + 2 * i);
   const cd shm = ldc2(sh + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
-  const Tail T1 = load_tail(tl1 + ((long)L.b * g.nkx + i) * SB_TAIL);
+  const TailLoad T1{tl1 + ((long)L.b * g.nkx + i) * SB_TAIL};
   if (L.role == 0) {
     // d(omega_y)/dy (cross.f90:440)
     SEG_SOLVE((const R *)bf.vor + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs 
       // cross.f90:659), same phase
       const FacView V2(bf.d2, 0);
       const SegView W2(bf.d2, 0);
-      const Tail T2 = load_tail(tl2 + ((long)L.b * g.nkx + i) * SB_TAIL);
+      const TailLoad T2{tl2 + ((long)L.b * g.nkx + i) * SB_TAIL};
       SEG_SOLVE((const R *)bf.vor + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
                 g.rh2[6], false);
       store_col(ys, ystr, (R *)bf.Lv + off, ps, L);
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs 
   {
     const FacView VH(bf.hz, L.lc);
     const SegView WH(bf.hz, L.lc);
-    const Tail TH = make_tail(VH, shp, N);
+    const TailMake TH{VH, shp, N};
     SEG_SOLVE((const R *)bf.phi + off, ps, VH, WH, TH, shp, shm, g.pr2[3], g.pr2[4], g.pr2[5],
               g.pr2[6], false);
     if (is00) {
@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineL(Grid g, Bufs 
     const R *tx = (const R *)bf.txy + (long)L.b * 2 * N + L.c;
     R *mrf = (R *)bf.mrf + (long)L.b * 2 * N + L.c;
     const cd one = mk(1.0, 0.0);
-    const Tail T1 = load_tail(bf.tl1o + (long)L.b * g.nkx * SB_TAIL);
+    const TailLoad T1{bf.tl1o + (long)L.b * g.nkx * SB_TAIL};
     SEG_SOLVE(tx, 2, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true);
     if (L.active)
       for (int i = L.r0; i <= L.r1; i++)
@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineL(Grid g, Bufs 
   const cd shp = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * i);
   const cd shm = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
   if (L.role == 0) {
-    const Tail T1 = load_tail(bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL);
+    const TailLoad T1{bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL};
     SEG_SOLVE((const R *)bf.L2 + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5], g.rh1[6],
               true);
     R *G = (R *)bf.G + off;
@@ -445,7 +445,7 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineL(Grid g, Bufs 
       }
     return;
   }
-  const Tail T2 = load_tail(bf.tl2o + ((long)L.b * g.nkx + i) * SB_TAIL);
+  const TailLoad T2{bf.tl2o + ((long)L.b * g.nkx + i) * SB_TAIL};
   const R *u = (const R *)bf.L1 + off;
   SEG_SOLVE(u, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6], false);
   if ((i == 0 && k == 0) || !L.active) return;
@@ -525,7 +525,7 @@ __global__ void __launch_bounds__(32 * kSeg) k_filter(Grid g, Bufs bf, int rk) {
     }
   }
   __syncthreads();  // the right-hand side of all segments is read below
-  const Tail TF = make_tail(VF, shp, N);
+  const TailMake TF{VF, shp, N};
   SEG_SOLVE(scr, ps, VF, WF, TF, shp, shm, 1.0, 0.0, 0.0, 0.0, false);
   store_col(ys, ystr, f, ps, L);
   if (!L.mean) return;
@@ -533,7 +533,7 @@ __global__ void __launch_bounds__(32 * kSeg) k_filter(Grid g, Bufs bf, int rk) {
   const FacView V1(bf.d1, 0);
   const SegView W1(bf.d1, 0);
   const cd one = mk(1.0, 0.0);
-  const Tail T1 = load_tail(bf.tl1o + (long)L.b * g.nkx * SB_TAIL);
+  const TailLoad T1{bf.tl1o + (long)L.b * g.nkx * SB_TAIL};
   SEG_SOLVE(f, 2, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true);
   if (L.active)
     for (int i = L.r0; i <= L.r1; i++) scr[2 * (i - 1)] = (R)ys[(i - L.r0) * ystr];
@@ -568,7 +568,7 @@ __global__ void __launch_bounds__(32 * kSeg) k_meand1(Grid g, Bufs bf) {
   const R *mu = (const R *)bf.mu + (long)b * 2 * N + L.c;
   R *mdu = (R *)bf.mdu + (long)b * 2 * N + L.c;
   const cd one = mk(1.0, 0.0);
-  const Tail T1 = load_tail(bf.tl1o + (long)b * g.nkx * SB_TAIL);
+  const TailLoad T1{bf.tl1o + (long)b * g.nkx * SB_TAIL};
   SEG_SOLVE(mu, 2, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true);
   if (L.active)
     for (int i = L.r0; i <= L.r1; i++) mdu[2 * (i - 1)] = (R)ys[(i - L.r0) * ystr];
