@@ -638,7 +638,7 @@ __global__ void __launch_bounds__(T) k_les2(Grid g, Bufs bf) {
     A[f * NX + i] = mk2<R>(X[0].x - X[1].y, X[0].y + X[1].x);
     if (i > 0) A[f * NX + NX - i] = mk2<R>(X[0].x + X[1].y, -X[0].y + X[1].x);
   }
-  V *P = fft_batch<NX, +1, 6, T>(A, Bs, (const V *)tw_of<R>(bf, false));
+  V *P = fft_batch<NX, +1, 6, T, true>(A, Bs, (const V *)tw_of<R>(bf, false));
   V *Q = (P == A) ? Bs : A;
   R *gb = (R *)bf.gbuf + (((long)b * g.my + j) * (NZ / 2) + zp) * 12L * NX;
   const R s = (R)g.s;
@@ -659,13 +659,12 @@ __global__ void __launch_bounds__(T) k_les2(Grid g, Bufs bf) {
   }
   V *Rr = fft_batch<NX, -1, 1, T>(Q, P, (const V *)tw_of<R>(bf, false));
   V *sbp = (V *)bf.sbuf + ((long)b * g.my + j) * (long)NZ * nkx;
-  const R half = (R)0.5;
+  // the two rows' spectra times 2 (k_les3 takes the 1/2 with the normalisation)
   for (int i = threadIdx.x; i < nkx; i += T) {
     const V zk = Rr[i];
-    V zm = Rr[(NX - i) % NX];
-    zm.y = -zm.y;
-    sbp[(long)z * nkx + i] = mk2<R>(half * (zk.x + zm.x), half * (zk.y + zm.y));
-    sbp[(long)(z + 1) * nkx + i] = mk2<R>(half * (zk.y - zm.y), -half * (zk.x - zm.x));
+    const V zm = Rr[(NX - i) % NX];
+    sbp[(long)z * nkx + i] = mk2<R>(zk.x + zm.x, zk.y - zm.y);
+    sbp[(long)(z + 1) * nkx + i] = mk2<R>(zk.y + zm.y, zm.x - zk.x);
   }
 }
 
@@ -685,14 +684,16 @@ __global__ void __launch_bounds__(T) k_les3(Grid g, Bufs bf) {
     A[ci * NZ + z] = (i < nkx) ? sbp[(long)z * nkx + i] : zero;
   }
   V *P = fft_batch<NZ, -1, CB, T>(A, Bs, (const V *)tw_of<R>(bf, true));
-  const R norm = (R)(1.0 / (double)(g.mgalx * g.mgalz));
+  // 1/(mgalx mgalz) and the 1/2 of k_les2's row split (a power of two)
+  const R norm = (R)(0.5 / (double)(g.mgalx * g.mgalz));
   for (int idx = threadIdx.x; idx < CB * NZ; idx += T) {
     const int z = idx % NZ;
     const bool keep = (z <= nz) || (z >= NZ - nz);
     V v = P[idx];
     P[idx] = keep ? mk2<R>(norm * v.x, norm * v.y) : zero;
   }
-  V *Q = fft_batch<NZ, +1, CB, T>(P, (P == A) ? Bs : A, (const V *)tw_of<R>(bf, true));
+  // the truncated spectrum has the zero middle third of the 2/3 rule
+  V *Q = fft_batch<NZ, +1, CB, T, true>(P, (P == A) ? Bs : A, (const V *)tw_of<R>(bf, true));
   for (int idx = threadIdx.x; idx < CB * NZ; idx += T) {
     const int ci = idx % CB, z = idx / CB, i = i0 + ci;
     if (i < nkx) sbp[(long)z * nkx + i] = Q[ci * NZ + z];
@@ -722,7 +723,7 @@ __global__ void __launch_bounds__(T) k_les4(Grid g, Bufs bf, int rk) {
     A[i] = mk2<R>(X1.x - X2.y, X1.y + X2.x);
     if (i > 0) A[NX - i] = mk2<R>(X1.x + X2.y, -X1.y + X2.x);
   }
-  V *P = fft_batch<NX, +1, 1, T>(A, Bs, (const V *)tw_of<R>(bf, false));
+  V *P = fft_batch<NX, +1, 1, T, true>(A, Bs, (const V *)tw_of<R>(bf, false));
   V *Q = (P == A) ? Bs : A;
   const R *gb = (const R *)bf.gbuf + (((long)b * g.my + j) * (NZ / 2) + zp) * 12L * NX;
   const R C = (R)g.les_c, s = (R)g.s;
@@ -779,14 +780,13 @@ __global__ void __launch_bounds__(T) k_les4(Grid g, Bufs bf, int rk) {
   }
   V *Rr = fft_batch<NX, -1, 6, T>(Q, P, (const V *)tw_of<R>(bf, false));
   V *tb = (V *)bf.tbuf + ((long)b * g.my + j) * (long)NZ * 6 * nkx;
-  const R half = (R)0.5;
+  // the two rows' spectra times 2 (k_les5 takes the 1/2 with the normalisation)
   for (int idx = threadIdx.x; idx < 6 * nkx; idx += T) {
     const int f = idx / nkx, i = idx - f * nkx;
     const V zk = Rr[f * NX + i];
-    V zm = Rr[f * NX + ((NX - i) % NX)];
-    zm.y = -zm.y;
-    tb[((long)z * 6 + f) * nkx + i] = mk2<R>(half * (zk.x + zm.x), half * (zk.y + zm.y));
-    tb[((long)(z + 1) * 6 + f) * nkx + i] = mk2<R>(half * (zk.y - zm.y), -half * (zk.x - zm.x));
+    const V zm = Rr[f * NX + ((NX - i) % NX)];
+    tb[((long)z * 6 + f) * nkx + i] = mk2<R>(zk.x + zm.x, zk.y - zm.y);
+    tb[((long)(z + 1) * 6 + f) * nkx + i] = mk2<R>(zk.y + zm.y, zm.x - zk.x);
   }
 }
 
@@ -812,7 +812,8 @@ __global__ void __launch_bounds__(T) k_les5(Grid g, Bufs bf) {
   V *Gv = (V *)((R *)bf.G + pbase);
   V *L1 = (V *)((R *)bf.L1 + pbase);
   V *L2 = (V *)((R *)bf.L2 + pbase);
-  const R norm = (R)(1.0 / (double)(g.mgalx * g.mgalz));
+  // 1/(mgalx mgalz) and the 1/2 of k_les4's row split (a power of two)
+  const R norm = (R)(0.5 / (double)(g.mgalx * g.mgalz));
   for (int idx = threadIdx.x; idx < CB * mz; idx += T) {
     const int ci = idx % CB, k = idx / CB, i = i0 + ci;
     if (i >= nkx) continue;
