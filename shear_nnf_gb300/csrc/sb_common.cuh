@@ -157,4 +157,20 @@ struct Bufs {
   double *stats, *stats2, *spec, *spec2, *tstats, *tspec, *ppart;
 };
 
+// Asynchronous global -> shared copy of one element of NB bytes (4, 8 or 16,
+// both addresses NB-aligned); with `valid` false the shared element is
+// zero-filled and nothing is read.  Completed by cp_async_wait_all().
+template <int NB>
+__device__ __forceinline__ void cp_async(void *smem_dst, const void *gmem_src, bool valid) {
+  static_assert(NB == 4 || NB == 8 || NB == 16, "cp.async element size");
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  const int n = valid ? NB : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(d), "l"(gmem_src),
+               "n"(NB), "r"(n)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 }  // namespace sb

@@ -514,13 +514,17 @@ __global__ void __launch_bounds__(T) k_p3(Grid g, Bufs bf) {
   const int nkx = g.nkx, mz = g.mz, nz = g.nz;
   const int i0 = cb * CB;
   const V *xb = (const V *)bf.xbuf + ((long)b * g.my + j) * (long)NZ * NF * nkx;
-  const V zero = mk2<R>((R)0, (R)0);
+  // the block's columns of the x-transformed rows, copied to shared memory
+  // asynchronously (all of a thread's copies in flight at once); columns
+  // beyond nkx are zero
   for (int idx = threadIdx.x; idx < NF * CB * NZ; idx += T) {
     const int ci = idx % CB, rem = idx / CB;
     const int f = rem % NF, z = rem / NF;
     const int i = i0 + ci;
-    A[(f * CB + ci) * NZ + z] = (i < nkx) ? xb[((long)z * NF + f) * nkx + i] : zero;
+    cp_async<sizeof(V)>(&A[(f * CB + ci) * NZ + z], xb + ((long)z * NF + f) * nkx + (i < nkx ? i : 0),
+                        i < nkx);
   }
+  cp_async_wait_all();
   V *P = fft_batch<NZ, -1, NF * CB, T>(A, Bs, (const V *)tw_of<R>(bf, true));
   const long pbase = (long)b * g.field + (long)j * g.plane;
   V *Dv = (V *)((R *)bf.D + pbase);
