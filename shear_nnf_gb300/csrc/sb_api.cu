@@ -42,6 +42,9 @@ static int fail(int code, const char *fmt, ...) {
       return fail(3, "%s failed: %s (%s:%d)", #x, cudaGetErrorString(e_), __FILE__, __LINE__); \
   } while (0)
 
+// largest my accepted by sb_create
+constexpr int kMaxMy = 448;
+
 struct sb_handle {
   sb_params p;
   int precision;
@@ -63,7 +66,7 @@ struct sb_handle {
   // pinned host staging of the small per-call values (mean profiles, time and
   // offsets, the member record), so that a cross call synchronises once
   struct HostSmall {
-    double mu_in[2 * 448], mu_out[2 * 448], sc_in[3], sc_out[3];
+    double mu_in[2 * kMaxMy], mu_out[2 * kMaxMy], sc_in[3], sc_out[3];
     Member m;
   } *hs = nullptr;
   int trace_cap = 0;
@@ -107,7 +110,7 @@ static int check_params(const sb_params *p) {
     return fail(1, "unsupported x/z grid %d x %d (transform lengths 32,48,64,96,192[,384])",
                 p->mgalx, p->mgalz);
   if (p->mgalz % 2) return fail(1, "mgalz must be even");
-  if (p->my < 16 || p->my > 448) return fail(1, "my=%d outside 16..448", p->my);
+  if (p->my < 16 || p->my > kMaxMy) return fail(1, "my=%d outside 16..%d", p->my, kMaxMy);
   if (p->temperature != 0 && p->temperature != 1)
     return fail(2, "itemperature=%d not available (0, 1)", p->temperature);
   if (!(p->Re != 0.0) || !(p->alp > 0) || !(p->gam > 0) || !(p->Ly > 0) || !(p->CFL > 0))
