@@ -45,7 +45,9 @@ from __future__ import annotations
 
 import numpy as np
 
-from . import SB_FP64, ShearBox, sizes
+from collections import OrderedDict
+
+from . import SB_FP64, SbParams, ShearBox, sizes
 
 
 class Packing:
@@ -603,6 +605,136 @@ def newton_arclength(xm1: np.ndarray, rem1: float, x0: np.ndarray, re0: float, a
         F, G = residual_at(x, re)
         hist.append(np.linalg.norm(F) / max(np.linalg.norm(x), 1e-300))
     return x, re, hist
+
+
+# pseudo-arclength parameters (cpara, gmres_shear.f90:115-160,922-975) and the
+# parameter field each one sets
+CPARA_FIELDS = {"Rez": "Re", "Ayz": "Ly", "Axz": "alp", "LES_Cs": "cs"}
+
+
+class ParamFamily:
+    """Shifted period maps G(x; a) along one pseudo-arclength parameter a
+    (cpara): 'Rez' the Reynolds number 1/nu, 'Ayz' Ly, 'Axz' alp, 'LES_Cs' the
+    Smagorinsky constant.  A value of a geometric or LES parameter gets its own
+    handle (the compact-scheme tables, wavenumbers, CFL constants and LES
+    filter width follow from it; the last few are kept); 'Rez' integrates all
+    values as members of one batch with their own Re.  With timep (shear
+    periods per orbit) the period follows 2 pi / (alp Ly s) timep, as set_dxda
+    recomputes it for Ayz and Axz (gmres_shear.f90:3204-3221), else T is
+    fixed; for Axz the image offsets keep alp xofft (xofft = xofft0 alp0 / alp,
+    xoffb = -xofft; gmres_shear.f90:3211-3220).  derivative() is dG/da by
+    finite differences with the steps of set_dxda (gmres_shear.f90:3169-3316):
+    daa = 1e-6, a tenth of it for LES_Cs, centred unless forward.
+    residual(x, a) returns (F, G) with F = G - x (- rhs) and jacobian(x, a, G,
+    xstan) the bordered operator, the two callables of newton_arclength."""
+
+    def __init__(self, p, cpara: str, packing: Packing, batch: int = 2,
+                 precision: int = SB_FP64, T: float = None, timep: float = None, time0=0.0,
+                 xoff0=(0.0, 0.0), shiftx=0.0, shiftz=0.0, rhs=None, chunk: int = 64,
+                 eps_jacobi: float = 1e-6, order: int = 2, keep: int = 3):
+        if cpara not in CPARA_FIELDS:
+            raise ValueError(f"cpara {cpara!r}: one of {sorted(CPARA_FIELDS)}")
+        if (T is None) == (timep is None):
+            raise ValueError("give the period T or the shear periods timep")
+        if cpara == "LES_Cs" and not p.les:
+            raise ValueError("cpara LES_Cs needs an LES handle (les = 1)")
+        self.p0 = SbParams.from_buffer_copy(p)
+        self.cpara, self.field = cpara, CPARA_FIELDS[cpara]
+        self.pk, self.batch, self.precision, self.chunk = packing, int(batch), precision, chunk
+        self.T, self.timep = T, timep
+        self.time0, self.xoff0, self.shift, self.rhs = time0, tuple(xoff0), (shiftx, shiftz), rhs
+        self.eps_jacobi, self.order, self.keep = eps_jacobi, order, max(int(keep), 1)
+        self._maps = OrderedDict()
+
+    @property
+    def a0(self) -> float:
+        return float(getattr(self.p0, self.field))
+
+    def params(self, a: float) -> SbParams:
+        q = SbParams.from_buffer_copy(self.p0)
+        setattr(q, self.field, float(a))
+        return q
+
+    def period(self, a: float) -> float:
+        if self.timep is None:
+            return float(self.T)
+        q = self.params(a)
+        return 2.0 * np.pi / (q.alp * q.Ly * q.s) * self.timep
+
+    def xoff(self, a: float) -> tuple:
+        xb, xt = self.xoff0
+        if self.cpara == "Axz":
+            xt = xt * self.a0 / float(a)
+            xb = -xt
+        return xb, xt
+
+    def _key(self, a: float) -> float:
+        return self.a0 if self.cpara == "Rez" else float(a)
+
+    def pmap(self, a: float) -> PeriodMap:
+        """The period map of parameter value a (one handle per value, the last
+        `keep` values kept)."""
+        key = self._key(a)
+        if key in self._maps:
+            self._maps.move_to_end(key)
+            return self._maps[key]
+        m = PeriodMap(self.params(key), self.period(a), self.batch, self.precision, self.chunk)
+        self._maps[key] = m
+        while len(self._maps) > self.keep:
+            _, old = self._maps.popitem(last=False)
+            old.box.close()
+        return m
+
+    def G(self, xs: list, avals: list) -> list:
+        """Shifted period maps of the vectors xs at the parameter values avals."""
+        out = [None] * len(xs)
+        groups = OrderedDict()
+        for q, a in enumerate(avals):
+            groups.setdefault(self._key(a), []).append(q)
+        for idx in groups.values():
+            a = avals[idx[0]]
+            m = self.pmap(a)
+            xb, xt = self.xoff(a)
+            for c in range(0, len(idx), m.batch):
+                part = idx[c:c + m.batch]
+                sts = [self.pk.unpack(xs[q], self.time0, xb, xt) for q in part]
+                if self.cpara == "Rez":
+                    gs = m(sts, [float(avals[q]) for q in part])
+                else:
+                    gs = m(sts)
+                for q, g in zip(part, gs):
+                    out[q] = self.pk.pack(phase_shift(g, m.p, *self.shift))
+        return out
+
+    def derivative(self, x: np.ndarray, a: float, daa: float = 1e-6, central: bool = True,
+                   gx: np.ndarray = None) -> np.ndarray:
+        """dG/da at (x, a) (set_dxda)."""
+        if self.cpara == "LES_Cs":
+            daa = daa / 10.0
+        if central:
+            gp, gm = self.G([x, x], [a + daa, a - daa])
+            return (gp - gm) / (2.0 * daa)
+        if gx is None:
+            gx = self.G([x], [a])[0]
+        return (self.G([x], [a + daa])[0] - gx) / daa
+
+    def residual(self, x: np.ndarray, a: float):
+        G = self.G([x], [a])[0]
+        F = G - x
+        return (F if self.rhs is None else F - self.rhs), G
+
+    def jacobian(self, x: np.ndarray, a: float, G: np.ndarray, xstan: np.ndarray) -> "ReJacobian":
+        """[(J - I) dx + dG/da da ; <xstan, dx>] at (x, a): J from the map of
+        value a (finite differences of order `order`), dG/da from derivative()
+        with the forward base G."""
+        m = self.pmap(a)
+        xb, xt = self.xoff(a)
+        J = Jacobian(m, self.pk, x, self.time0, (xb, xt), *self.shift,
+                     eps_jacobi=self.eps_jacobi, order=self.order,
+                     re=float(a) if self.cpara == "Rez" else None)
+        J._gx0 = G if self.order == 1 else None  # the forward-difference base
+        dgda = self.derivative(x, a, central=self.order > 1, gx=G)
+        return ReJacobian(J, dgda, xstan)
 
 
 class BorderedJacobian:

@@ -425,6 +425,147 @@ def test_arclength_in_re_gpu():
 
 
 # ---------------------------------------------------------------------------
+# pseudo-arclength along Ly, alp, Cs (ParamFamily)
+# ---------------------------------------------------------------------------
+
+class _FakeMap:
+    """Stands in for PeriodMap on the CPU: a smooth map of the state whose
+    coefficients depend on the handle's Ly, alp, cs and the member's Re, and
+    on the image offsets and the period it integrates over."""
+    made = []
+
+    def __init__(self, p, T, batch, precision=0, chunk=64):
+        self.p, self.T, self.batch = p, T, batch
+        self.closed = False
+        _FakeMap.made.append(self)
+
+        class _Box:
+            def close(inner):
+                self.closed = True
+        self.box = _Box()
+
+    def __call__(self, states, res=None, Ts=None):
+        out = []
+        for m, st in enumerate(states):
+            re = res[m] if res is not None else self.p.Re
+            f = (1.0 + 0.1 * self.p.Ly + 0.2 * self.p.alp + 0.3 * self.p.cs + 1e-4 * re
+                 + 0.05 * self.T + 0.01 * st["xofft"])
+            g = dict(st)
+            for key in ("vor", "phi"):
+                g[key] = st[key] * f + 0.01 * np.sin(st[key].real) * self.p.Ly
+            g["u00"] = st["u00"] * f
+            g["w00"] = st["w00"] * f
+            out.append(g)
+        return out
+
+
+def test_param_family_geometry(monkeypatch):
+    monkeypatch.setattr(nw, "PeriodMap", _FakeMap)
+    p = _params()
+    pk = nw.Packing(p, *nw.Packing.reference_scales(p))
+    fam = nw.ParamFamily(p, "Axz", pk, timep=2.0, xoff0=(-0.3, 0.3))
+    a0 = fam.a0
+    assert a0 == p.alp and fam.params(2 * a0).alp == 2 * a0 and fam.params(2 * a0).Ly == p.Ly
+    # the period follows the shear period 2 pi / (alp Ly s) timep; alp xofft kept
+    assert fam.period(a0) == pytest.approx(2 * np.pi / (p.alp * p.Ly * p.s) * 2.0, rel=1e-15)
+    assert fam.period(2 * a0) == pytest.approx(fam.period(a0) / 2, rel=1e-15)
+    assert fam.xoff(2 * a0) == pytest.approx((-0.15, 0.15), rel=1e-15)
+    ly = nw.ParamFamily(p, "Ayz", pk, T=5.0)
+    assert ly.period(3.0) == 5.0 and ly.xoff(3.0) == (0.0, 0.0)
+    with pytest.raises(ValueError):
+        nw.ParamFamily(p, "damp_up", pk, T=1.0)
+    with pytest.raises(ValueError):
+        nw.ParamFamily(p, "LES_Cs", pk, T=1.0)  # not an LES handle
+    with pytest.raises(ValueError):
+        nw.ParamFamily(p, "Ayz", pk)  # neither T nor timep
+    # one handle per value, the oldest closed beyond `keep`
+    _FakeMap.made.clear()
+    fam3 = nw.ParamFamily(p, "Ayz", pk, T=1.0, keep=2)
+    x = pk.pack(sb.seed_state(p, 3))
+    fam3.G([x, x, x], [3.0, 3.1, 3.0])
+    assert len(_FakeMap.made) == 2
+    fam3.G([x], [3.2])
+    assert len(_FakeMap.made) == 3 and _FakeMap.made[0].closed
+    # Rez: one handle, the values as member Reynolds numbers
+    _FakeMap.made.clear()
+    fre = nw.ParamFamily(p, "Rez", pk, T=1.0)
+    g1, g2 = fre.G([x, x], [p.Re, 2 * p.Re])
+    assert len(_FakeMap.made) == 1 and not np.allclose(g1, g2)
+
+
+@pytest.mark.parametrize("cpara,field", [("Ayz", "Ly"), ("Axz", "alp"), ("Rez", "Re")])
+def test_param_family_derivative_and_jacobian(monkeypatch, cpara, field):
+    monkeypatch.setattr(nw, "PeriodMap", _FakeMap)
+    p = _params()
+    pk = nw.Packing(p, *nw.Packing.reference_scales(p))
+    x = pk.pack(sb.seed_state(p, 5))
+    fam = nw.ParamFamily(p, cpara, pk, T=2.0, xoff0=(-0.2, 0.2), batch=4)
+    a = fam.a0 * 1.01
+    h = 1e-4 * fam.a0
+    # centred derivative against a wide centred difference of the same map
+    ref = (fam.G([x], [a + h])[0] - fam.G([x], [a - h])[0]) / (2 * h)
+    d = fam.derivative(x, a, daa=1e-6 * fam.a0)
+    assert rel_l2(d, ref) < 1e-6
+    fwd = fam.derivative(x, a, daa=1e-6 * fam.a0, central=False)
+    assert rel_l2(fwd, ref) < 1e-4
+    # the bordered operator: parameter column and secant row
+    F, G = fam.residual(x, a)
+    assert np.allclose(F, G - x)
+    xstan = np.random.default_rng(1).standard_normal(x.size)
+    Jx = fam.jacobian(x, a, G, xstan)
+    e = np.zeros(x.size + 1)
+    e[-1] = 1.0
+    col = Jx.matvec(e)[:, 0]
+    assert rel_l2(col[:-1], Jx.dgdre) < 1e-15 and col[-1] == 0.0
+    dx = np.random.default_rng(2).standard_normal(x.size)
+    v = Jx.matvec(np.concatenate([dx, [0.0]]))[:, 0]
+    assert v[-1] == pytest.approx(xstan @ dx, rel=1e-12)
+
+
+def test_param_family_les_cs_step(monkeypatch):
+    monkeypatch.setattr(nw, "PeriodMap", _FakeMap)
+    p = _params(les=1, les_visc=1, cs=0.1)
+    pk = nw.Packing(p, *nw.Packing.reference_scales(p))
+    x = pk.pack(sb.seed_state(p, 6))
+    fam = nw.ParamFamily(p, "LES_Cs", pk, T=1.0)
+    seen = []
+    real_G = fam.G
+
+    def spy(xs, avals):
+        seen.extend(avals)
+        return real_G(xs, avals)
+    fam.G = spy
+    fam.derivative(x, 0.1)
+    # set_dxda takes a tenth of daa for Cs
+    assert sorted(seen) == pytest.approx([0.1 - 1e-7, 0.1 + 1e-7], rel=1e-12)
+
+
+@pytest.mark.gpu
+def test_arclength_in_ly_gpu():
+    # manufactured curve through (x*, Ly*) as in the Re case, along Ly with a
+    # handle per value of Ly (ParamFamily 'Ayz'): a Newton solution at
+    # 0.999 Ly*, then one arclength step past x*
+    p = _params()
+    pk = nw.Packing(p, *nw.Packing.reference_scales(p))
+    xs = _seeded_x(p, pk, 16)
+    ly_s = p.Ly
+    probe = nw.ParamFamily(p, "Ayz", pk, T=10.0, batch=1)
+    rhs = probe.G([xs], [ly_s])[0] - xs
+    fam = nw.ParamFamily(p, "Ayz", pk, T=10.0, batch=8, rhs=rhs, eps_jacobi=1e-7)
+    ly1 = 0.999 * ly_s
+    J1 = lambda x: nw.Jacobian(fam.pmap(ly1), pk, x, eps_jacobi=1e-7, central=True)
+    x1, h1 = nw.newton(xs, lambda x: fam.residual(x, ly1)[0], J1, k=16, block=4, itmax=12,
+                       tol=1e-11, gmres_tol=1e-9)
+    assert h1[-1] <= 1e-11, h1
+    xp, lyp, xstan = nw.arclength_predictor(x1, ly1, xs, ly_s, 1.0)
+    x, ly, hist = nw.newton_arclength(x1, ly1, xs, ly_s, 1.0, fam.residual, fam.jacobian, k=16,
+                                      block=4, itmax=12, tol=1e-10, gmres_tol=1e-9)
+    assert hist[-1] <= 1e-10, hist
+    assert abs(xstan @ (x - xp)) <= 1e-8 * np.linalg.norm(xstan) * np.linalg.norm(x)
+    assert abs(ly - 1.001 * ly_s) < 2.5e-4 * ly_s
+
+
+# ---------------------------------------------------------------------------
 # extra unknowns: bordered Jacobian, period derivative, flow direction
 # ---------------------------------------------------------------------------
 
