@@ -62,6 +62,12 @@ typedef struct sb_params {
   double fkappa, bym, gbeta;   /* its diffusivity, mean gradient d(Tbar)/dy and
                                   buoyancy factor (hre3.dat keyword itemperature,
                                   initcr.f90:1996-2011) */
+  int damping;                 /* iadd_damping: 1 adds the window damping
+                                  -damp_up Hw(y) u00 to the mean forcing rf0u
+                                  (add_damping, operators.f90:42-84;
+                                  cross.f90:625-626, crosst.f90:694-695) */
+  double damp_up, damp_aa;     /* its permeability and half width / Lz
+                                  (initcr.f90:2128) */
 } sb_params;
 
 /* Per-box status after sb_step (cross.f90 istop logic, 1683-1690, 2102-2115) */

@@ -30,6 +30,8 @@ module shearbox_c
      integer(c_int)  :: ydeal
      integer(c_int)  :: temperature
      real(c_double)  :: fkappa, bym, gbeta
+     integer(c_int)  :: damping
+     real(c_double)  :: damp_up, damp_aa
   end type sb_params
 
   type, bind(C) :: sb_status

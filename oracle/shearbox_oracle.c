@@ -2239,6 +2239,17 @@ static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00,
         for (size_t q = 0; q < nfield; q++) ht[q] = ht[q] + rt2[q];
       double r1 = CA[rkstep - 1] * Deltat;
       double fac = 1.0 / Re;
+      if (c->p.damping == 1) {
+        /* window damping of the mean streamwise forcing (add_damping,
+         * operators.f90:60-78; cross.f90:625-626, crosst.f90:694-695) */
+        const double lz = c->Lz, aa = lz * c->p.damp_aa, up = c->p.damp_up;
+        for (int j = 0; j < my; j++) {
+          const double y = c->y[j];
+          const double hw = 1.0 - (0.25 * (1.0 + tanh(6.0 * (aa - y) / lz + 3.0))) *
+                                      (1.0 + tanh(6.0 * (aa + y) / lz + 3.0));
+          rf0u[j] = rf0u[j] - up * hw * u00[j];
+        }
+      }
       if (les) {
         /* mean-mode stresses (cross.f90:639-647) */
         cplx one = C(1.0, 0.0);

@@ -45,6 +45,9 @@ typedef struct orc_params {
   int temperature;        /* itemperature: Boussinesq scalar tb of crosst (crosst.f90:3-1310) */
   double fkappa, bym, gbeta; /* its diffusivity, mean gradient and buoyancy factor
                            * (hre3.dat keyword itemperature, initcr.f90:1996-2011) */
+  int damping;            /* iadd_damping: window damping of the mean forcing rf0u
+                           * (add_damping, operators.f90:42-84; cross.f90:625-626) */
+  double damp_up, damp_aa; /* its permeability and half width / Lz (initcr.f90:2128) */
 } orc_params;
 
 /* one .cfbin record per statistics step (cross.f90:2087):

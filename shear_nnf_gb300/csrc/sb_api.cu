@@ -113,6 +113,8 @@ static int check_params(const sb_params *p) {
   if (p->my < 16 || p->my > kMaxMy) return fail(1, "my=%d outside 16..%d", p->my, kMaxMy);
   if (p->temperature != 0 && p->temperature != 1)
     return fail(2, "itemperature=%d not available (0, 1)", p->temperature);
+  if (p->damping != 0 && p->damping != 1)
+    return fail(2, "iadd_damping=%d not available (0, 1)", p->damping);
   if (!(p->Re != 0.0) || !(p->alp > 0) || !(p->gam > 0) || !(p->Ly > 0) || !(p->CFL > 0))
     return fail(1, "invalid physical parameters");
   return 0;
@@ -421,6 +423,10 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   g.kappa = (g.temp && molec) ? p->fkappa : 0.0;
   g.gbeta = (g.temp && molec) ? p->gbeta : 0.0;
   g.bym = g.temp ? p->bym : 0.0;
+  g.damp = p->damping ? 1 : 0;
+  g.lz = 2.0 * g.pi / p->gam;
+  g.damp_up = p->damp_up;
+  g.damp_a = g.lz * p->damp_aa;
   g.cbl = les_cb(p->mgalz);
   g.ncbl = (g.nkx + g.cbl - 1) / g.cbl;
   g.ydeal = p->ydeal;

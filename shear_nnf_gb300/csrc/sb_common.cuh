@@ -82,6 +82,10 @@ struct Grid {
   // the mean gradient
   int temp, tround, tzf, nxf, tlen;
   double kappa, gbeta, bym;
+  // window damping of the mean forcing rf0u (iadd_damping, add_damping):
+  // on/off, permeability damp_up, half width aa = Lz damp_aa, Lz
+  int damp;
+  double damp_up, damp_a, lz;
 };
 
 // Per-member run state, owned by the device (one per box in the batch)

@@ -216,9 +216,18 @@ __global__ void __launch_bounds__(32 * kSeg, TEMP ? 5 : SB_LINEA_MINB) k_lineA(G
       }
       return;
     }
+    // window damping of rf0u (add_damping, operators.f90:60-78; cross.f90:625-626)
+    const bool damp = g.damp && L.c == 0;
     for (int i = L.r0; i <= L.r1; i++) {
       const int j = i - 1;
-      const R rf = mrf[2 * j] + (R)(nu * (-(0.0 * (double)mu[2 * j]) + ys[(i - L.r0) * ystr]));
+      R rf0 = mrf[2 * j];
+      if (damp) {
+        const double y = (double)j * g.dy - 0.5 * g.Ly;
+        const double hw = 1.0 - (0.25 * (1.0 + tanh(6.0 * (g.damp_a - y) / g.lz + 3.0))) *
+                                    (1.0 + tanh(6.0 * (g.damp_a + y) / g.lz + 3.0));
+        rf0 = (R)((double)rf0 - g.damp_up * hw * (double)mu[2 * j]);
+      }
+      const R rf = rf0 + (R)(nu * (-(0.0 * (double)mu[2 * j]) + ys[(i - L.r0) * ystr]));
       R wk = (rk == 0) ? gk * rf : mwk[2 * j] + gk * rf;
       const R un = mu[2 * j] + (R)Dt * wk;
       if (rk < 2) wk = rf * zk;

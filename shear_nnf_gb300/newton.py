@@ -609,13 +609,15 @@ def newton_arclength(xm1: np.ndarray, rem1: float, x0: np.ndarray, re0: float, a
 
 # pseudo-arclength parameters (cpara, gmres_shear.f90:115-160,922-975) and the
 # parameter field each one sets
-CPARA_FIELDS = {"Rez": "Re", "Ayz": "Ly", "Axz": "alp", "LES_Cs": "cs"}
+CPARA_FIELDS = {"Rez": "Re", "Ayz": "Ly", "Axz": "alp", "LES_Cs": "cs", "damp_up": "damp_up",
+                "damp_aa": "damp_aa"}
 
 
 class ParamFamily:
     """Shifted period maps G(x; a) along one pseudo-arclength parameter a
     (cpara): 'Rez' the Reynolds number 1/nu, 'Ayz' Ly, 'Axz' alp, 'LES_Cs' the
-    Smagorinsky constant.  A value of a geometric or LES parameter gets its own
+    Smagorinsky constant, 'damp_up'/'damp_aa' the window damping's permeability
+    and half width.  A value of a geometric, LES or damping parameter gets its own
     handle (the compact-scheme tables, wavenumbers, CFL constants and LES
     filter width follow from it; the last few are kept); 'Rez' integrates all
     values as members of one batch with their own Re.  With timep (shear
@@ -638,6 +640,8 @@ class ParamFamily:
             raise ValueError("give the period T or the shear periods timep")
         if cpara == "LES_Cs" and not p.les:
             raise ValueError("cpara LES_Cs needs an LES handle (les = 1)")
+        if cpara.startswith("damp_") and not p.damping:
+            raise ValueError(f"cpara {cpara} needs the window damping (damping = 1)")
         self.p0 = SbParams.from_buffer_copy(p)
         self.cpara, self.field = cpara, CPARA_FIELDS[cpara]
         self.pk, self.batch, self.precision, self.chunk = packing, int(batch), precision, chunk

@@ -473,7 +473,11 @@ def test_param_family_geometry(monkeypatch):
     ly = nw.ParamFamily(p, "Ayz", pk, T=5.0)
     assert ly.period(3.0) == 5.0 and ly.xoff(3.0) == (0.0, 0.0)
     with pytest.raises(ValueError):
-        nw.ParamFamily(p, "damp_up", pk, T=1.0)
+        nw.ParamFamily(p, "damp_xy", pk, T=1.0)
+    with pytest.raises(ValueError):
+        nw.ParamFamily(p, "damp_up", pk, T=1.0)  # no window damping in p
+    pd = _params(damping=1, damp_up=0.3, damp_aa=0.1)
+    assert nw.ParamFamily(pd, "damp_aa", pk, T=1.0).params(0.2).damp_aa == 0.2
     with pytest.raises(ValueError):
         nw.ParamFamily(p, "LES_Cs", pk, T=1.0)  # not an LES handle
     with pytest.raises(ValueError):
