@@ -68,6 +68,12 @@ typedef struct sb_params {
                                   cross.f90:625-626, crosst.f90:694-695) */
   double damp_up, damp_aa;     /* its permeability and half width / Lz
                                   (initcr.f90:2128) */
+  int force;                   /* iadd_force: 1 or 2 adds the one- or two-pair
+                                  streamwise-roll force to hv(kx=0, kz=1)
+                                  (add_force, operators.f90:1-40), -1 the
+                                  inertial force xforce to rf0u (cross.f90:610-624,
+                                  crosst.f90:680-693) */
+  double force_roll, xforce;   /* their amplitudes (initcr.f90:2103-2118) */
 } sb_params;
 
 /* Per-box status after sb_step (cross.f90 istop logic, 1683-1690, 2102-2115) */

@@ -32,6 +32,8 @@ module shearbox_c
      real(c_double)  :: fkappa, bym, gbeta
      integer(c_int)  :: damping
      real(c_double)  :: damp_up, damp_aa
+     integer(c_int)  :: force
+     real(c_double)  :: force_roll, xforce
   end type sb_params
 
   type, bind(C) :: sb_status

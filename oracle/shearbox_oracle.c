@@ -2239,6 +2239,20 @@ static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00,
         for (size_t q = 0; q < nfield; q++) ht[q] = ht[q] + rt2[q];
       double r1 = CA[rkstep - 1] * Deltat;
       double fac = 1.0 / Re;
+      if ((c->p.force == 1 || c->p.force == 2) && mz > 1) {
+        /* streamwise-roll force on hv(kx=0, kz=1) (add_force, operators.f90:14-37) */
+        double *h01 = PEN(hv, 0, 1);
+        const double up = c->p.force_roll, gm = c->p.gam;
+        for (int j = 0; j < my; j++) {
+          const double y = c->y[j], w = 1.0 - y * y;
+          const double f = (c->p.force == 1)
+                               ? -0.5 * up * (-4.0 * (1.0 - 3.0 * y * y) - gm * gm * w * w)
+                               : 0.5 * up * (4.0 * y * (-3.0 + 5.0 * y * y) - y * w * w * gm * gm);
+          h01[2 * j] = h01[2 * j] + f;
+        }
+      }
+      if (c->p.force == -1)
+        for (int j = 0; j < my; j++) rf0u[j] = rf0u[j] + c->p.xforce; /* cross.f90:622-624 */
       if (c->p.damping == 1) {
         /* window damping of the mean streamwise forcing (add_damping,
          * operators.f90:60-78; cross.f90:625-626, crosst.f90:694-695) */

@@ -48,6 +48,10 @@ typedef struct orc_params {
   int damping;            /* iadd_damping: window damping of the mean forcing rf0u
                            * (add_damping, operators.f90:42-84; cross.f90:625-626) */
   double damp_up, damp_aa; /* its permeability and half width / Lz (initcr.f90:2128) */
+  int force;              /* iadd_force: 1, 2 streamwise-roll force on hv(kx=0, kz=1)
+                           * (add_force, operators.f90:1-40); -1 xforce on rf0u
+                           * (cross.f90:610-624) */
+  double force_roll, xforce; /* their amplitudes (initcr.f90:2103-2118) */
 } orc_params;
 
 /* one .cfbin record per statistics step (cross.f90:2087):

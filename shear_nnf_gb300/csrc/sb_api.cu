@@ -115,6 +115,8 @@ static int check_params(const sb_params *p) {
     return fail(2, "itemperature=%d not available (0, 1)", p->temperature);
   if (p->damping != 0 && p->damping != 1)
     return fail(2, "iadd_damping=%d not available (0, 1)", p->damping);
+  if (p->force < -1 || p->force > 2)
+    return fail(2, "iadd_force=%d not available (-1, 0, 1, 2)", p->force);
   if (!(p->Re != 0.0) || !(p->alp > 0) || !(p->gam > 0) || !(p->Ly > 0) || !(p->CFL > 0))
     return fail(1, "invalid physical parameters");
   return 0;
@@ -427,6 +429,9 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   g.lz = 2.0 * g.pi / p->gam;
   g.damp_up = p->damp_up;
   g.damp_a = g.lz * p->damp_aa;
+  g.force = p->force;
+  g.force_roll = p->force_roll;
+  g.xforce = p->xforce;
   g.cbl = les_cb(p->mgalz);
   g.ncbl = (g.nkx + g.cbl - 1) / g.cbl;
   g.ydeal = p->ydeal;

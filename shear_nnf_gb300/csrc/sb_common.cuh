@@ -86,6 +86,10 @@ struct Grid {
   // on/off, permeability damp_up, half width aa = Lz damp_aa, Lz
   int damp;
   double damp_up, damp_a, lz;
+  // body forces (iadd_force): 1, 2 the streamwise-roll force on hv(kx=0,
+  // kz=1) with amplitude force_roll; -1 the inertial force xforce on rf0u
+  int force;
+  double force_roll, xforce;
 };
 
 // Per-member run state, owned by the device (one per box in the batch)

@@ -569,7 +569,16 @@ __global__ void __launch_bounds__(T) k_p3(Grid g, Bufs bf) {
     ty = gz * (H1.y - s * v.y) - a * H3.y;
     Gv[q] = mk2<R>(-ty, tx);
     // hv = -(kx^2 + kz^2) H2
-    Vv[q] = mk2<R>(-(Kk * H2.x), -(Kk * H2.y));
+    V hv = mk2<R>(-(Kk * H2.x), -(Kk * H2.y));
+    if (g.force > 0 && i == 0 && k == 1) {
+      // streamwise-roll force on hv(kx=0, kz=1) (add_force, operators.f90:14-37)
+      const double y = (double)j * g.dy - 0.5 * g.Ly, w = 1.0 - y * y, gm = g.gam;
+      const double f = (g.force == 1)
+                           ? -0.5 * g.force_roll * (-4.0 * (1.0 - 3.0 * y * y) - gm * gm * w * w)
+                           : 0.5 * g.force_roll * (4.0 * y * (-3.0 + 5.0 * y * y) - y * w * w * gm * gm);
+      hv.x = (R)((double)hv.x + f);
+    }
+    Vv[q] = hv;
     if (i == 0 && k == 0) ((V *)bf.mrf)[(long)b * g.my + j] = mk2<R>(H1.x, H3.x);
   }
 }

@@ -216,11 +216,14 @@ __global__ void __launch_bounds__(32 * kSeg, TEMP ? 5 : SB_LINEA_MINB) k_lineA(G
       }
       return;
     }
-    // window damping of rf0u (add_damping, operators.f90:60-78; cross.f90:625-626)
+    // inertial force and window damping of rf0u (cross.f90:622-626;
+    // add_damping, operators.f90:60-78)
     const bool damp = g.damp && L.c == 0;
+    const bool xf = g.force == -1 && L.c == 0;
     for (int i = L.r0; i <= L.r1; i++) {
       const int j = i - 1;
       R rf0 = mrf[2 * j];
+      if (xf) rf0 = (R)((double)rf0 + g.xforce);
       if (damp) {
         const double y = (double)j * g.dy - 0.5 * g.Ly;
         const double hw = 1.0 - (0.25 * (1.0 + tanh(6.0 * (g.damp_a - y) / g.lz + 3.0))) *
