@@ -533,6 +533,15 @@ __global__ void __launch_bounds__(T) k_p3(Grid g, Bufs bf) {
   // 1/(mgalx mgalz) of the forward transform and the 1/2 of k_p2's row split
   const R norm = (R)(0.5 / (double)(g.mgalx * g.mgalz));
   const R s = (R)g.s;
+  // streamwise-roll force of this plane on hv(kx=0, kz=1) (add_force,
+  // operators.f90:14-37)
+  const bool force = g.force > 0;
+  double fj = 0.0;
+  if (force) {
+    const double y = (double)j * g.dy - 0.5 * g.Ly, w = 1.0 - y * y, gm = g.gam;
+    fj = (g.force == 1) ? -0.5 * g.force_roll * (-4.0 * (1.0 - 3.0 * y * y) - gm * gm * w * w)
+                        : 0.5 * g.force_roll * (4.0 * y * (-3.0 + 5.0 * y * y) - y * w * w * gm * gm);
+  }
   for (int idx = threadIdx.x; idx < CB * mz; idx += T) {
     const int ci = idx % CB, k = idx / CB, i = i0 + ci;
     if (i >= nkx) continue;
@@ -570,14 +579,7 @@ __global__ void __launch_bounds__(T) k_p3(Grid g, Bufs bf) {
     Gv[q] = mk2<R>(-ty, tx);
     // hv = -(kx^2 + kz^2) H2
     V hv = mk2<R>(-(Kk * H2.x), -(Kk * H2.y));
-    if (g.force > 0 && i == 0 && k == 1) {
-      // streamwise-roll force on hv(kx=0, kz=1) (add_force, operators.f90:14-37)
-      const double y = (double)j * g.dy - 0.5 * g.Ly, w = 1.0 - y * y, gm = g.gam;
-      const double f = (g.force == 1)
-                           ? -0.5 * g.force_roll * (-4.0 * (1.0 - 3.0 * y * y) - gm * gm * w * w)
-                           : 0.5 * g.force_roll * (4.0 * y * (-3.0 + 5.0 * y * y) - y * w * w * gm * gm);
-      hv.x = (R)((double)hv.x + f);
-    }
+    if (force && i == 0 && k == 1) hv.x = (R)((double)hv.x + fj);
     Vv[q] = hv;
     if (i == 0 && k == 0) ((V *)bf.mrf)[(long)b * g.my + j] = mk2<R>(H1.x, H3.x);
   }
