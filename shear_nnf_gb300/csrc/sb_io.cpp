@@ -141,18 +141,18 @@ int sb_write_restart(const char *path, const sb_params *p, const double *vor, co
       }
     flush();
   }
-  put_f64(r, p->CFL); put_f64(r, p->uprim); put_f64(r, p->vbulk); put_f64(r, 0.0);
+  put_f64(r, p->CFL); put_f64(r, p->uprim); put_f64(r, p->vbulk); put_f64(r, p->xforce);
   flush();
   put_i32(r, 1742); put_i32(r, 9); put_i32(r, 13);  // irev (mod.f90:45), nopt, nparams
   flush();
-  const int opts[9] = {1, p->fixed_dt > 0 ? 1 : 0, 0, 5, 0, 0, p->les ? 1 : 0,
-                       p->les_visc ? 1 : 0, 0};
+  const int opts[9] = {1, p->fixed_dt > 0 ? 1 : 0, p->force, 5, 0, p->damping,
+                       p->les ? 1 : 0, p->les_visc ? 1 : 0, 0};
   for (int q = 0; q < 9; q++) put_i32(r, opts[q]);
   flush();
   const double dx = 2.0 * pi / p->alp / (double)mx, dz = 2.0 * pi / p->gam / (double)mz;
   const double deltag = p->les ? std::pow(dx * dy * dz, 1.0 / 3.0) : 0.0;
-  const double prm[13] = {deltat, 0.0, 0.0, 0.0, 0.0, 0.0, p->les ? p->cs : 0.0, deltag,
-                          0.0, 0.0, 0.0, 0.0, 0.0};
+  const double prm[13] = {deltat, p->force_roll, p->xforce, 0.0, p->damp_aa, p->damp_up,
+                          p->les ? p->cs : 0.0, deltag, 0.0, 0.0, 0.0, 0.0, 0.0};
   for (int q = 0; q < 13; q++) put_f64(r, prm[q]);
   flush();
   if (!ok) return io_fail(7, std::string("write failed: ") + path);

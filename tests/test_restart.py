@@ -77,6 +77,27 @@ def test_round_trip(tmp_path):
     assert (hdr.mgalx, hdr.my, hdr.mgalz, hdr.mx, hdr.mz) == (64, 32, 32, 42, 19)
 
 
+def test_footer_carries_forces_and_damping(tmp_path):
+    """The option switches and parameters of the footer record the body force
+    and the window damping of the run (iadd_force, iadd_damping; force_roll,
+    xforce, damp_aa, damp_up), as escru writes them."""
+    p = sb.make_params(**box_params(64, 32, 32, 1000.0, force=1, force_roll=0.25, xforce=0.0,
+                                    damping=1, damp_up=0.4, damp_aa=0.125))
+    st = sb.seed_state(p, 2)
+    f = tmp_path / "f.bin"
+    sb.write_restart(f, p, st, deltat=0.002)
+    recs = _records(f)
+    opts = struct.unpack("<9i", recs[-2])
+    assert opts[2] == 1 and opts[5] == 1 and opts[3] == 5
+    prm = struct.unpack("<13d", recs[-1])
+    assert prm[:6] == (0.002, 0.25, 0.0, 0.0, 0.125, 0.4)
+    q = sb.make_params(**box_params(64, 32, 32, 1000.0, force=-1, xforce=0.05))
+    sb.write_restart(f, q, st)
+    recs = _records(f)
+    assert struct.unpack("<4d", recs[-4])[3] == 0.05
+    assert struct.unpack("<9i", recs[-2])[2] == -1
+
+
 @pytest.mark.parametrize("target", [(96, 32, 48), (48, 32, 32)])
 def test_grid_change(tmp_path, target):
     p = sb.make_params(**box_params(64, 32, 32, 1000.0))
