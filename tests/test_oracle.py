@@ -148,7 +148,7 @@ def test_rdt_single_wave():
 
 def test_viscous_decay_without_shear():
     """s = 0: a small single wave decays as exp(-nu k^2 t) under the explicit RK3
-    viscous term (SURVEY known answer (v))."""
+    viscous term (laminar decay known answer)."""
     pp = box_params(64, 32, 32, rez=1000.0, fixed_dt=0.01, s=0.0)
     o = oracle.Oracle(**pp)
     st, kx, kz = _single_wave_state(o, 2, 1, 1e-3)
