@@ -309,6 +309,14 @@ int sb_sync(sb_handle *h);
  * mgalz, complex entries per box (= nkx*mz*my).  Host only. */
 int sb_sizes(const sb_params *p, int *out);
 
+/* The twiddle table of the length-n transforms as the device receives it:
+ * factored = 0: e^{-2 pi i t/n}, t = 0..n-1, re/im interleaved (2n doubles;
+ * the FP32 storage form); factored = 1: the FP64 form, 4n doubles per entry t
+ * {mx, my, tau, swap} with e^{-2 pi i t/n} = (-i)^q c (1 + i tau), q the
+ * nearest quarter turn, mx = (q < 2 ? c : -c), my = (odd q ? -mx : mx) and
+ * swap = q & 1 as integer bits.  Host only (inspection and tests). */
+int sb_fft_twiddles(int n, int factored, double *out);
+
 /* Seeded divergence-free initial field (host only): random-phase modes with
  * E(k) ~ k^4 exp(-2 (k/k0)^2), rms velocity urms, written in the pencil layout.
  * A synthetic stand-in for the reference's getini (initcr.f90:664-822). */

@@ -84,6 +84,7 @@ ABI_FUNCTIONS = [
     "sb_set_member_etime", "sb_op_filterc", "sb_op_cfty", "sb_op_rfty", "sb_write_restart",
     "sb_read_restart", "sb_autotune", "sb_physical_fields", "sb_set_temperature",
     "sb_get_temperature", "sb_crosst", "sb_stats", "sb_jv_batch", "sb_get_statistics",
+    "sb_fft_twiddles",
 ]
 
 _lib = None
@@ -127,6 +128,7 @@ def lib(auto_build: bool = False):
     L.sb_get_stream.argtypes = [vp]
     L.sb_sync.argtypes = [vp]
     L.sb_sizes.argtypes = [PP, ip]
+    L.sb_fft_twiddles.argtypes = [ctypes.c_int, ctypes.c_int, dp]
     L.sb_seed_state.argtypes = [PP, ctypes.c_ulonglong, ctypes.c_double, ctypes.c_double, dp, dp,
                                 dp, dp]
     L.sb_compact_coeffs.argtypes = [dp, dp, dp, dp]
@@ -183,6 +185,14 @@ def sizes(p: SbParams) -> dict:
     _check(lib().sb_sizes(ctypes.byref(p), out))
     keys = ["mx", "mz", "nkx", "my", "nz", "mgalx", "mgalz", "n"]
     return dict(zip(keys, list(out)))
+
+
+def fft_twiddles(n: int, factored: bool = True) -> np.ndarray:
+    """The device's twiddle table for transforms of length n (sb_fft_twiddles):
+    factored: (n, 4) rows {mx, my, tau, swap bits}; else (n,) complex."""
+    out = np.zeros(4 * n if factored else 2 * n)
+    _check(lib().sb_fft_twiddles(int(n), 1 if factored else 0, _dp(out)))
+    return out.reshape(n, 4) if factored else out.view(np.complex128)
 
 
 def _seed_fields(p: SbParams, seed: int, k0: float, urms: float):

@@ -335,6 +335,13 @@ extern "C" {
 int sb_version(void) { return 1; }
 const char *sb_last_error(void) { return g_err.c_str(); }
 
+int sb_fft_twiddles(int n, int factored, double *out) {
+  if (!out || n < 1) return fail(1, "bad argument");
+  const std::vector<double> v = factored ? sbh::fft_twiddles_factored(n) : sbh::fft_twiddles(n);
+  std::memcpy(out, v.data(), sizeof(double) * v.size());
+  return 0;
+}
+
 int sb_sizes(const sb_params *p, int *out) {
   if (!p || !out) return fail(1, "null argument");
   int mx = 2 * (p->mgalx / 3), mz = 2 * (p->mgalz / 3) - 1;
@@ -543,33 +550,9 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
     bf.mem = (Member *)q;
   }
   // twiddles e^{-2 pi i t / N}
-  auto tw = [&](int n) {
-    std::vector<double> v(2 * (size_t)n);
-    for (int t = 0; t < n; t++) {
-      double a = -2.0 * g.pi * (double)t / (double)n;
-      v[2 * t] = std::cos(a);
-      v[2 * t + 1] = std::sin(a);
-    }
-    return v;
-  };
-  // the factored FP64 form of the same twiddles (sb_fft.cuh): entry t =
-  // {mx, my, tau, swap} with e^{-2 pi i t/N} = (-i)^q c (1 + i tau), q the
-  // nearest quarter turn
-  auto gtw = [&](int n) {
-    std::vector<double> v(4 * (size_t)n);
-    for (int t = 0; t < n; t++) {
-      const int q = ((8 * t + n) / (2 * n)) % 4;
-      const double a = g.pi * (double)(q * n - 4 * t) / (2.0 * (double)n);
-      const double c = std::cos(a);
-      const long long sw = q & 1;
-      const double mx = (q <= 1) ? c : -c;
-      v[4 * t] = mx;
-      v[4 * t + 1] = sw ? -mx : mx;
-      v[4 * t + 2] = std::sin(a) / c;
-      std::memcpy(&v[4 * t + 3], &sw, sizeof(double));
-    }
-    return v;
-  };
+  // FFT twiddles: the complex table (FP32 storage) and the factored FP64 form
+  const auto tw = sbh::fft_twiddles;
+  const auto gtw = sbh::fft_twiddles_factored;
   std::vector<double> kinv((size_t)nl), ginv((size_t)g.mz);
   for (int k = 0; k < g.mz; k++) {
     int kzs = (k <= g.nz) ? k : k - g.mz;

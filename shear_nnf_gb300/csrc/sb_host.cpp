@@ -377,4 +377,32 @@ int seed_state(int mgalx, int my, int mgalz, double alp, double gam, double Ly, 
   return 0;
 }
 
+std::vector<double> fft_twiddles(int n) {
+  const double pi = 4.0 * std::atan(1.0);
+  std::vector<double> v(2 * (size_t)n);
+  for (int t = 0; t < n; t++) {
+    const double a = -2.0 * pi * (double)t / (double)n;
+    v[2 * t] = std::cos(a);
+    v[2 * t + 1] = std::sin(a);
+  }
+  return v;
+}
+
+std::vector<double> fft_twiddles_factored(int n) {
+  const double pi = 4.0 * std::atan(1.0);
+  std::vector<double> v(4 * (size_t)n);
+  for (int t = 0; t < n; t++) {
+    const int q = ((8 * t + n) / (2 * n)) % 4;
+    const double a = pi * (double)(q * n - 4 * t) / (2.0 * (double)n);  // -2 pi t/n + q pi/2
+    const double c = std::cos(a);
+    const long long sw = q & 1;
+    const double mx = (q <= 1) ? c : -c;
+    v[4 * t] = mx;
+    v[4 * t + 1] = sw ? -mx : mx;
+    v[4 * t + 2] = std::sin(a) / c;
+    std::memcpy(&v[4 * t + 3], &sw, sizeof(double));
+  }
+  return v;
+}
+
 }  // namespace sbh

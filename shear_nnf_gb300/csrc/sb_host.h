@@ -47,6 +47,15 @@ struct SegFac {
 };
 void seg_factor(const BaseFac &b, int n, const SegPlan &p, SegFac *out);
 
+// FFT twiddles of length n: the complex table e^{-2 pi i t/n} (t = 0..n-1,
+// re/im interleaved) and its factored FP64 form for sb_fft.cuh: entry t =
+// {mx, my, tau, swap} with e^{-2 pi i t/n} = (-i)^q c (1 + i tau), q the
+// nearest quarter turn (so c >= cos(pi/4), |tau| <= 1), mx the signed c of the
+// real output component, my = (odd q ? -mx : mx), swap = q & 1 stored as the
+// bits of an integer.
+std::vector<double> fft_twiddles(int n);
+std::vector<double> fft_twiddles_factored(int n);
+
 // Seeded divergence-free initial field (synthetic stand-in for the reference's
 // getini spectrum, initcr.f90:664-822): random-phase Fourier modes with energy
 // spectrum E(k) ~ k^4 exp(-2 (k/k0)^2), rms velocity urms.  Outputs the
