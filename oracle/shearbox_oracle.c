@@ -16,6 +16,13 @@
  *                            gaussj
  *   operators.f90:86-145     moving_frame;  operators.f90:1382-1429 set_conj
  *   initcr.f90:191-216,443-519  sizes, wavenumbers, y grid, CFL constants
+ *   cross.f90:1291-1406,537-608,639-648  Smagorinsky LES block
+ *   crosst.f90:3-1310        the temperature variant crosst (hvhgt, histt,
+ *                            moving_frame_t, set_conj_t)
+ *   filter_shear_hepta.f90:21-164  compact y filter (iydealiasing 3);
+ *   operators.f90:352-467    dealiasing_y (iydealiasing 1, 2)
+ *   cross.f90:1796-2014      hist accumulators (stats, stats2, spl, spl2)
+ *   cross.f90:610-626; operators.f90:1-84  body forces and window damping
  */
 #include "shearbox_oracle.h"
 
