@@ -41,6 +41,12 @@ CASES = {
                                      Ly=LZ, gam=1.0, s=1.0, chi=0.0, CFL=0.5, temperature=1,
                                      fkappa=LZ ** 2 / 4000.0 / 0.7, bym=1.0, gbeta=0.5),
                          seed=7, nstep=3),
+    # the two-pair roll force with the window damping of the mean (iadd_force = 2,
+    # iadd_damping = 1), CFL steps
+    "force64_seed8": dict(params=dict(mgalx=64, my=32, mgalz=32, Re=4000.0 / LZ ** 2, alp=0.5,
+                                      Ly=LZ, gam=1.0, s=1.0, chi=0.0, CFL=0.5, force=2,
+                                      force_roll=0.05, damping=1, damp_up=0.5, damp_aa=0.1),
+                          seed=8, nstep=3),
 }
 
 

@@ -7,8 +7,9 @@ import pytest
 
 from conftest import ROOT, rel_l2
 
-CASES = ["step64_seed3", "les64_seed5", "filt64_seed4", "ydeal64_seed6", "temp64_seed7"]
-INTS = ("mgalx", "my", "mgalz", "les", "les_visc", "ydeal", "temperature")
+CASES = ["step64_seed3", "les64_seed5", "filt64_seed4", "ydeal64_seed6", "temp64_seed7",
+         "force64_seed8"]
+INTS = ("mgalx", "my", "mgalz", "les", "les_visc", "ydeal", "temperature", "force", "damping")
 
 
 def _case(name):
