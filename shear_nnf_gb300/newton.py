@@ -647,7 +647,8 @@ class ParamFamily:
         self.pk, self.batch, self.precision, self.chunk = packing, int(batch), precision, chunk
         self.T, self.timep = T, timep
         self.time0, self.xoff0, self.shift, self.rhs = time0, tuple(xoff0), (shiftx, shiftz), rhs
-        self.eps_jacobi, self.order, self.keep = eps_jacobi, order, max(int(keep), 1)
+        # a Jacobian at a uses the map of a while the derivative adds a +- daa
+        self.eps_jacobi, self.order, self.keep = eps_jacobi, order, max(int(keep), 3)
         self._maps = OrderedDict()
 
     @property

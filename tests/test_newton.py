@@ -484,12 +484,12 @@ def test_param_family_geometry(monkeypatch):
         nw.ParamFamily(p, "Ayz", pk)  # neither T nor timep
     # one handle per value, the oldest closed beyond `keep`
     _FakeMap.made.clear()
-    fam3 = nw.ParamFamily(p, "Ayz", pk, T=1.0, keep=2)
+    fam3 = nw.ParamFamily(p, "Ayz", pk, T=1.0, keep=1)  # at least three are kept
     x = pk.pack(sb.seed_state(p, 3))
-    fam3.G([x, x, x], [3.0, 3.1, 3.0])
-    assert len(_FakeMap.made) == 2
-    fam3.G([x], [3.2])
-    assert len(_FakeMap.made) == 3 and _FakeMap.made[0].closed
+    fam3.G([x, x, x, x], [3.0, 3.1, 3.0, 3.2])
+    assert len(_FakeMap.made) == 3 and not any(m.closed for m in _FakeMap.made)
+    fam3.G([x], [3.3])
+    assert len(_FakeMap.made) == 4 and _FakeMap.made[0].closed
     # Rez: one handle, the values as member Reynolds numbers
     _FakeMap.made.clear()
     fre = nw.ParamFamily(p, "Rez", pk, T=1.0)
