@@ -475,6 +475,30 @@ def read_restart(path: str, p: SbParams = None):
             "xoffb": info.xoffb, "xofft": info.xofft}, info
 
 
+def params_from_restart(info: SbRestartInfo, **overrides) -> SbParams:
+    """Step parameters recorded by a restart file: grid, Re, alp, Ly, gam, s, chi
+    from the header and, with a footer, CFL, uprim, vbulk and the switches and
+    parameters escru writes (ifix_dt with the Delta t as fixed_dt, iadd_force,
+    force_roll, xforce, iadd_damping, damp_aa, damp_up, iuse_LES, iadd_visc,
+    Cles; readwrite.f90:1336-1398).  Keyword arguments override any of them
+    (the hre2.dat/hre3.dat settings of the run that reads the file)."""
+    kw = dict(mgalx=info.mgalx, my=info.my, mgalz=info.mgalz, Re=info.Re, alp=info.alp,
+              Ly=info.Ly, gam=info.gam, s=info.s, chi=info.chi)
+    if info.has_footer:
+        kw.update(CFL=info.CFL, uprim=info.uprim, vbulk=info.vbulk, xforce=info.xforce)
+        opt = list(info.options)[:info.nopt]
+        prm = list(info.params)[:info.nparams]
+        if len(opt) >= 8 and len(prm) >= 7:
+            if opt[1]:
+                kw["fixed_dt"] = prm[0]
+            kw.update(force=opt[2], force_roll=prm[1], xforce=prm[2], damping=opt[5],
+                      damp_aa=prm[4], damp_up=prm[5], les=opt[6], les_visc=opt[7])
+            if opt[6]:
+                kw["cs"] = prm[6]
+    kw.update(overrides)
+    return make_params(**kw)
+
+
 def op_filterc(my: int, u_dev: int, out_dev: int, nlines: int, shp: np.ndarray,
                ldu: int = None, ldo: int = None, stream: int = 0):
     """Compact y-filter of nlines device-resident complex lines (filterc)."""

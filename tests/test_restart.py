@@ -98,6 +98,26 @@ def test_footer_carries_forces_and_damping(tmp_path):
     assert struct.unpack("<9i", recs[-2])[2] == -1
 
 
+def test_params_from_restart(tmp_path):
+    """The parameters a restart records come back as step parameters."""
+    kw = box_params(64, 32, 32, 1000.0, fixed_dt=0.004, force=2, force_roll=0.3, damping=1,
+                    damp_up=0.2, damp_aa=0.15, les=1, les_visc=0, cs=0.12, CFL=0.4)
+    kw.pop("cfl", None)
+    p = sb.make_params(**kw)
+    st = sb.seed_state(p, 4)
+    f = tmp_path / "p.bin"
+    sb.write_restart(f, p, st, deltat=0.004)
+    _, info = sb.read_restart(f)
+    q = sb.params_from_restart(info)
+    for name, _ in sb.SbParams._fields_:
+        if name in ("mgalx", "my", "mgalz", "Re", "alp", "Ly", "gam", "s", "chi", "CFL",
+                    "uprim", "vbulk", "fixed_dt", "force", "force_roll", "xforce", "damping",
+                    "damp_up", "damp_aa", "les", "les_visc", "cs"):
+            assert getattr(q, name) == pytest.approx(getattr(p, name), rel=1e-14, abs=1e-300), name
+    r = sb.params_from_restart(info, Re=2.0, damping=0)
+    assert r.Re == 2.0 and r.damping == 0 and r.force == 2
+
+
 @pytest.mark.parametrize("target", [(96, 32, 48), (48, 32, 32)])
 def test_grid_change(tmp_path, target):
     p = sb.make_params(**box_params(64, 32, 32, 1000.0))
