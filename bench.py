@@ -106,7 +106,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "10"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
         except OSError:
@@ -171,12 +171,13 @@ def plane2_traffic():
 
 
 def cpu_baseline(nsteps_sample: int, threads: int):
-    """The C oracle on the host cores, a bounded sample of steps."""
+    """The C oracle on the host cores, a bounded sample of steps.  Loads only
+    the oracle: the seeded field comes from the oracle's own generator, which
+    the CPU tests hold bit-identical to the library's."""
     import oracle
-    import shear_nnf_gb300 as sb
     oracle.set_threads(threads)
     pp = box_params()
-    st = sb.seed_state(sb.make_params(**pp), 3)
+    st = oracle.seed_state(seed=3, **pp)
     o = oracle.Oracle(**pp)
     o.cross(st, 1)  # warm-up
     t0 = time.perf_counter()
@@ -206,15 +207,19 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def ensemble_leg(sb, torch, dist, ws, rank, args, nbox=64, nsteps=200):
+def ensemble_leg(sb, torch, dist, ws, rank, args, nbox=64, n_oracle=4):
     """Batched ensemble: 64 boxes of 64x32x32 (geometry of the 64^3/2 case),
     Re_z log-uniform in [500, 2000] and one seed per box, FP32-mixed, all boxes
-    advanced by one graph-captured step per launch sequence.  Reports box-steps/s
-    and the largest relative field error of a member against the same ensemble
-    in FP64 (the FP64 path is pinned to the oracle by the tests)."""
+    advanced by one graph-captured step per launch sequence, args.ens_steps
+    steps.  Reports box-steps/s, the HBM rate of the algorithmic bytes (72
+    complex fields per box-step, FP32 storage), the largest relative field
+    error of a member against the same ensemble in FP64 on the GPU, and for
+    the first n_oracle members the error of both against the oracle (FP64 on
+    the host cores, the members' own Re and seeds)."""
     pp = dict(mgalx=64, my=32, mgalz=32, Re=1000.0 / LZ ** 2, alp=0.5, Ly=LZ, gam=1.0, s=1.0,
               chi=0.0, CFL=0.5)
     p = sb.make_params(**pp)
+    nsteps = args.ens_steps
     rng = np.random.default_rng(1234 + rank)
     rez = np.exp(rng.uniform(np.log(500.0), np.log(2000.0), nbox))
     states = [sb.seed_state(p, 1000 * rank + m) for m in range(nbox)]
@@ -242,33 +247,62 @@ def ensemble_leg(sb, torch, dist, ws, rank, args, nbox=64, nsteps=200):
     e1.synchronize()
     ms = allmax(dist, e0.elapsed_time(e1))
     boxes[sb.SB_FP64].step(nsteps)
-    err = 0.0
-    for m in range(nbox):
-        a = boxes[sb.SB_FP64].get_state(m)
-        b = box.get_state(m)
-        err = max(err, max(float(np.linalg.norm(b[k] - a[k]) / np.linalg.norm(a[k]))
-                           for k in ("vor", "phi", "u00", "w00")))
+    keys = ("vor", "phi", "u00", "w00")
+
+    def err(a, b):
+        return max(float(np.linalg.norm(a[k] - b[k]) / np.linalg.norm(b[k])) for k in keys)
+
+    finals = {prec: [bx.get_state(m) for m in range(nbox)] for prec, bx in boxes.items()}
+    err_mixed_fp64 = max(err(finals[sb.SB_MIXED][m], finals[sb.SB_FP64][m]) for m in range(nbox))
+    steps_done = [boxes[sb.SB_MIXED].status(m).steps_done for m in range(nbox)]
+    vs_oracle = None
+    if rank == 0 and n_oracle > 0:
+        import oracle
+        oracle.set_threads(os.cpu_count() or 1)
+        e_mixed, e_fp64 = [], []
+        for m in range(n_oracle):
+            o = oracle.Oracle(**dict(pp, Re=rez[m] / LZ ** 2))
+            st = oracle.seed_state(seed=1000 * rank + m, **pp)
+            o.cross(st, nsteps)
+            e_mixed.append(err(finals[sb.SB_MIXED][m], st))
+            e_fp64.append(err(finals[sb.SB_FP64][m], st))
+        vs_oracle = {"members": n_oracle, "max_mixed": max(e_mixed), "max_fp64": max(e_fp64),
+                     "mixed": e_mixed, "fp64": e_fp64}
+    sz = sb.sizes(p)
+    alg_bytes = 72.0 * sz["n"] * 8 * nbox  # per batch step, FP32 storage (8 B per complex)
+    hbm_peak, hbm_src = measured_peaks()
+    gbs = alg_bytes * nsteps / (ms * 1e-3) / 1e9
     return {"boxes_per_gpu": nbox, "grid": [64, 32, 32], "steps": nsteps,
+            "steps_done_min": int(min(steps_done)),
             "value": ws * nbox * nsteps / (ms * 1e-3), "unit": "box-steps/s",
             "ms_per_step": ms / nsteps, "precision": "FP32-mixed",
-            "max_member_rel_l2_err_vs_fp64": err, "re_z_range": [500.0, 2000.0],
+            "max_member_rel_l2_err_vs_fp64": err_mixed_fp64,
+            "max_member_rel_l2_err_vs_oracle": vs_oracle["max_mixed"] if vs_oracle else None,
+            "vs_oracle": vs_oracle, "re_z_range": [500.0, 2000.0],
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": gbs / hbm_peak, "peak_source": f"MEASURED_PEAKS.json ({hbm_src})",
+                         "algorithmic_bytes_per_step": alg_bytes,
+                         "note": "72 complex fields per box-step (4S + 8S + 12S per substep)"},
             "tuning": tuning}
 
 
 def les_leg(sb, torch, dist, ws, rank, args):
     """LES mode: Smagorinsky eddy viscosity (Cs = 0.1, filter width
-    (dx dy dz)^(1/3)) on 384x192x192, Re_z = 20000, k0 = 6, CFL = 0.5, FP32-mixed,
-    args.les_steps steps from the seeded field, against the same run in FP64 on
-    the GPU: steps/s of both (CUDA events, state in HBM) and the relative
-    deviation of the velocity variances (u', v', w' rms) and the Reynolds shear
-    stress <uv> of the last statistics record, plus the simulated time span
-    against the shear-periodic remesh period St = Lx/Ly."""
+    (dx dy dz)^(1/3)) on 384x192x192, Re_z = 20000, k0 = 6, CFL = 0.5, from the
+    seeded field to t = args.les_tend (default 2 = Lx/(S Ly), one shear-periodic
+    remesh period; the CFL step makes that about 800 steps, so the leg runs up
+    to args.les_steps steps and stops at that time), FP32-mixed against the
+    same run in FP64 on the GPU: steps/s of both (CUDA events, state in HBM;
+    steps done over the timed call), the time reached and the relative
+    deviation of the velocity variances (u', v', w' rms), the Reynolds shear
+    stress <uv> and the mean eddy viscosity of the last statistics record."""
     pp = dict(mgalx=384, my=192, mgalz=192, Re=20000.0 / LZ ** 2, alp=0.5, Ly=LZ, gam=1.0,
               s=1.0, chi=0.0, CFL=0.5, les=1, les_visc=1, cs=0.1)
     p = sb.make_params(**pp)
     st0 = sb.seed_state(p, 6 + rank, k0=6.0)
     n = args.les_steps
-    out = {"grid": [384, 192, 192], "re_z": 20000.0, "cs": 0.1, "k0": 6.0, "steps": n}
+    out = {"grid": [384, 192, 192], "re_z": 20000.0, "cs": 0.1, "k0": 6.0, "max_steps": n,
+           "t_end": args.les_tend}
     recs = {}
     for key, prec in (("mixed", sb.SB_MIXED), ("fp64", sb.SB_FP64)):
         box = sb.ShearBox(p, precision=prec)
@@ -276,6 +310,7 @@ def les_leg(sb, torch, dist, ws, rank, args):
         box.step(3)
         box.sync()
         box.set_state(st0)
+        box.set_etime(0, args.les_tend)
         stream = torch.cuda.ExternalStream(box.stream)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -289,8 +324,10 @@ def les_leg(sb, torch, dist, ws, rank, args):
         st = box.status()
         tr = box.trace(0)
         recs[key] = tr
-        out[key] = {"value": ws * n / (ms * 1e-3), "unit": "steps/s", "ms_per_step": ms / n,
-                    "time_span": st.time, "steps_done": st.steps_done}
+        done = st.steps_done
+        out[key] = {"value": ws * done / (ms * 1e-3), "unit": "steps/s",
+                    "ms_per_step": ms / max(done, 1), "time_span": st.time,
+                    "steps_done": done, "reached_t_end": bool(st.flags & 8)}
         del box
     a, b = recs["mixed"][-1], recs["fp64"][-1]
     out["mixed"]["speedup_vs_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
@@ -299,6 +336,8 @@ def les_leg(sb, torch, dist, ws, rank, args):
         "w_rms": float(abs(a[4] - b[4]) / abs(b[4])), "uv": float(abs(a[5] - b[5]) / abs(b[5])),
         "nu_t_mean": float(abs(a[22] - b[22]) / abs(b[22]))}
     out["remesh_period_St"] = (2 * np.pi / 0.5) / LZ
+    out["spans_remesh"] = bool(out["mixed"]["time_span"] >= out["remesh_period_St"] - 1e-12 and
+                               out["fp64"]["time_span"] >= out["remesh_period_St"] - 1e-12)
     out["precision"] = "FP32-mixed (FP64 y-solves, Helmholtz, phases)"
     return out
 
@@ -402,6 +441,10 @@ def run_ours(args):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     torch.cuda.init()
+    # clocks over the whole run (all legs), beside those of the timed region
+    run_clocks = ClockSampler(dev)
+    if not args.lite and rank == 0:
+        run_clocks.start()
     pp = box_params()
     if args.variant == "les":
         pp.update(les=1, les_visc=1, cs=0.1)
@@ -542,24 +585,39 @@ def run_ours(args):
         m1.record(mstream)
         m1.synchronize()
         mixed_ms = allmax(dist, m0.elapsed_time(m1))
-        errs = {}
+        # the same marks for the FP64 GPU path against the oracle (the drop-in
+        # bar: 1e-12 after one step, 1e-9 after 100); the oracle runs on the
+        # host cores from the oracle's own seeded field
+        errs, errs64 = {}, {}
         ref_box = box
         ref_box.set_state(st0)
         mbox.set_state(st0)
+        orc = orc_st = None
+        if rank == 0 and not args.no_oracle_table:
+            import oracle
+            oracle.set_threads(os.cpu_count() or 1)
+            orc = oracle.Oracle(**pp)
+            orc_st = oracle.seed_state(seed=3, **pp)
         done = 0
         for mark in (1, 10, 100, 200):
             ref_box.step(mark - done)
             mbox.step(mark - done)
-            done = mark
             a = ref_box.get_state()
             b = mbox.get_state()
             errs[str(mark)] = max(float(np.linalg.norm(b[k] - a[k]) / np.linalg.norm(a[k]))
                                   for k in ("vor", "phi", "u00", "w00"))
+            if orc is not None:
+                orc.cross(orc_st, mark - done)
+                errs64[str(mark)] = max(
+                    float(np.linalg.norm(a[k] - orc_st[k]) / np.linalg.norm(orc_st[k]))
+                    for k in ("vor", "phi", "u00", "w00"))
+            done = mark
         del mbox
         mixed = {"value": ws * args.steps / (mixed_ms * 1e-3), "unit": "steps/s",
                  "ms_per_step": mixed_ms / args.steps,
                  "speedup_vs_fp64": (ws * args.steps / (mixed_ms * 1e-3)) / steps_per_s,
                  "rel_l2_err_vs_fp64_at_step": errs,
+                 "fp64_rel_l2_err_vs_oracle_at_step": errs64 or None,
                  "precision": "FP32 storage, transforms, nonlinear product and RK3; FP64 "
                               "compact y-solves, Helmholtz solve, phase factors",
                  "tuning": mtuning}
@@ -598,6 +656,8 @@ def run_ours(args):
             "traffic": traffic,
             "line_kernels_ms": {"k_lineA": line_ms[0], "k_lineB": line_ms[1]},
         },
+        "mixed_value": mixed["value"] if mixed else None,
+        "mixed_speedup": mixed["speedup_vs_fp64"] if mixed else None,
         "mixed": mixed,
         "ensemble": ensemble,
         "newton": newton,
@@ -605,6 +665,7 @@ def run_ours(args):
         "temperature": temp,
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "clocks": clk,
+        "clocks_all_legs": run_clocks.stop(),
     }
     print(json.dumps(line))
 
@@ -622,7 +683,13 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble leg")
     ap.add_argument("--no-newton", action="store_true", help="skip the batched Newton Jv leg")
     ap.add_argument("--no-les", action="store_true", help="skip the LES leg")
-    ap.add_argument("--les-steps", type=int, default=500, help="steps of the LES leg")
+    ap.add_argument("--les-steps", type=int, default=1000,
+                    help="most steps of the LES leg (it stops at t = 2, one remesh period)")
+    ap.add_argument("--les-tend", type=float, default=2.0,
+                    help="end time of the LES leg (the remesh period Lx/(S Ly) = 2)")
+    ap.add_argument("--ens-steps", type=int, default=1000, help="steps of the ensemble leg")
+    ap.add_argument("--no-oracle-table", action="store_true",
+                    help="skip the FP64-vs-oracle error table of the mixed leg")
     ap.add_argument("--no-temp", action="store_true", help="skip the temperature (crosst) leg")
     ap.add_argument("--lite", action="store_true",
                     help="profiling only: time the steps, skip e2e / CPU / per-kernel legs")

@@ -7,7 +7,8 @@
  * (cross.f90:3-4), called from disk3d (main.f90:279-280), calc_dns_disk3d
  * (gmres_shear.f90:3103-3104) and shoot_shear.f90:527, with its parameters in
  * modules ctes / running / bcs (mod.f90:1-130).  The entry points below are what
- * an ISO_C_BINDING interface of that routine binds.
+ * an ISO_C_BINDING interface of that routine binds (the Fortran module
+ * include/shearbox_c.f90 declares them).
  *
  * Conventions
  *   - every function returns 0 on success and a positive error code otherwise;
@@ -259,9 +260,9 @@ int sb_op_rfty(int my, int nlines, double *c, long ldc, int iopt, void *stream);
  * array of the library (about 9.5 MB, held on every GPU that loads the library
  * until the process exits), limited to nlines <= SB_NOALLOC_LINES and
  * my * (2*nlines rounded up to a multiple of 32) <= SB_NOALLOC_YBUF doubles;
- * larger requests return error 6 with a message.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress, with that device
- * current); make that first call before any stream capture.  Every call
+ * larger requests return error 6 with a message.  Every call looks up the
+ * array's address in the current device's context (cudaGetSymbolAddress, no
+ * allocation) and returns after its stream has finished the work.  Every call
  * overwrites the whole part of the array it uses, so nothing carries over
  * between calls, but all calls share the one array: calls that overlap on the
  * GPU (other streams, other host threads) race and must be serialised by the

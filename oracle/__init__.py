@@ -88,6 +88,9 @@ def lib():
         L.orc_filterc.argtypes = [ctypes.c_void_p, dp, dp, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_int]
         L.orc_fft.argtypes = [ctypes.c_int, dp, ctypes.c_int]
+        L.orc_seed_state.restype = ctypes.c_int
+        L.orc_seed_state.argtypes = [ctypes.c_int] * 3 + [ctypes.c_double] * 3 + \
+            [ctypes.c_ulonglong, ctypes.c_double, ctypes.c_double, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -99,6 +102,42 @@ def _dp(a: np.ndarray):
 
 def set_threads(n: int) -> None:
     lib().orc_set_threads(int(n))
+
+
+def _seed_fields(mgalx, my, mgalz, alp, gam, Ly, seed, k0, urms):
+    mz = 2 * (mgalz // 3) - 1
+    nkx = (2 * (mgalx // 3)) // 2
+    vor = np.zeros((mz, nkx, my), np.complex128)
+    phi = np.zeros_like(vor)
+    u00 = np.zeros(my)
+    w00 = np.zeros(my)
+    rc = lib().orc_seed_state(int(mgalx), int(my), int(mgalz), float(alp), float(gam), float(Ly),
+                              ctypes.c_ulonglong(int(seed)), float(k0), float(urms),
+                              _dp(vor.view(np.float64)), _dp(phi.view(np.float64)), _dp(u00),
+                              _dp(w00))
+    if rc != 0:
+        raise MemoryError("orc_seed_state")
+    return vor, phi, u00, w00
+
+
+def seed_state(mgalx, my, mgalz, alp, Ly, gam, seed, k0=4.0, urms=None, temperature=0,
+               **_ignored) -> dict:
+    """The seeded initial field of the benchmark configurations, generated by the
+    oracle (bit-identical to the library's sb_seed_state), as a state dict in
+    the pencil layout; with temperature=1 also tb, tb00 from a second seed as
+    the library draws them.  Extra keyword arguments (the other step
+    parameters) are accepted and ignored, so a parameter dict can be passed."""
+    if urms is None:
+        urms = 0.1 * 1.0 * (2 * np.pi / gam)  # 0.1 * S * Lz
+    vor, phi, u00, w00 = _seed_fields(mgalx, my, mgalz, alp, gam, Ly, seed, k0, urms)
+    st = {"vor": vor, "phi": phi, "u00": u00, "w00": w00, "time": 0.0, "xoffb": 0.0,
+          "xofft": 0.0}
+    if temperature:
+        tv, _, t00, _ = _seed_fields(mgalx, my, mgalz, alp, gam, Ly,
+                                     (int(seed) * 7919 + 17) & 0xFFFFFFFF, k0, urms)
+        st["tb"] = np.ascontiguousarray(tv / k0)
+        st["tb00"] = t00
+    return st
 
 
 def fft(x: np.ndarray, sign: int) -> np.ndarray:

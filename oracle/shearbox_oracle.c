@@ -2454,3 +2454,137 @@ int orc_crosst(void *h, double *vor, double *phi, double *u00, double *w00, doub
   return cross_run(c, vor, phi, u00, w00, tb, tb00, ptime, pxoffb, pxofft, nstep, trace,
                    ntrace, pistop, pdeltat);
 }
+
+/* ------------------------------------------------------------------------- */
+/* Seeded synthetic initial field.  The reference's own initial condition      */
+/* (getini, initcr.f90:664-822) draws its spectrum with an LCG; the benchmark  */
+/* configurations instead define a divergence-free random-phase field with     */
+/* E(k) ~ k^4 exp(-2 (k/k0)^2) and a given rms velocity.  This is the oracle's */
+/* restatement of that definition, so that the CPU baseline needs nothing from */
+/* the library under test: the same counter-based SplitMix64 draws per         */
+/* (seed, mode), the same arithmetic in the same order (no contraction), so    */
+/* the two generators agree bit for bit.                                       */
+/* ------------------------------------------------------------------------- */
+static inline unsigned long long seed_mix(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+static inline double seed_u01(unsigned long long seed, unsigned long long ctr) {
+  const unsigned long long r = seed_mix(seed * 0x632BE59BD9B4E019ull + seed_mix(ctr));
+  return ((double)(r >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+}
+
+int orc_seed_state(int mgalx, int my, int mgalz, double alp, double gam, double Ly,
+                   unsigned long long seed, double k0, double urms, double *vor, double *phi,
+                   double *u00, double *w00) {
+  const double pi = 4.0 * atan(1.0);
+  const int mx = 2 * (mgalx / 3), mz = 2 * (mgalz / 3) - 1;
+  const int nkx = mx / 2, nz = (mz - 1) / 2;
+  const int ny = my / 3; /* y modes |n| <= my/3 */
+  const int nyf = 2 * ny + 1;
+  const double bet = 2.0 * pi / Ly;
+  /* spectral velocity (kx_i >= 0, ky_n, kz_k, component) */
+  cplx *uh = (cplx *)calloc((size_t)nkx * nyf * mz * 3, sizeof(cplx));
+  if (!uh) return -1;
+#define UH(i, n, k, q) uh[((((size_t)(i) * nyf + ((n) + ny)) * mz + (k)) * 3 + (q))]
+  for (int i = 0; i < nkx; i++)
+    for (int n = -ny; n <= ny; n++)
+      for (int k = 0; k < mz; k++) {
+        const double kzi = (k <= nz) ? (double)k : -(double)(mz - k);
+        const double kx = alp * i, ky = bet * n, kz = gam * kzi;
+        const double kk = sqrt(kx * kx + ky * ky + kz * kz);
+        if (kk == 0.0) continue;
+        /* kx = 0: the half plane kz > 0, or kz = 0 with ky > 0; the rest by symmetry */
+        if (i == 0 && (kzi < 0 || (kzi == 0 && n <= 0))) continue;
+        const unsigned long long ctr =
+            ((unsigned long long)i * 4096 + (unsigned long long)(n + 2048)) * 4096 +
+            (unsigned long long)k;
+        const double r1 = seed_u01(seed, 4 * ctr), r2 = seed_u01(seed, 4 * ctr + 1);
+        const double r3 = seed_u01(seed, 4 * ctr + 2);
+        const double ek = pow(kk, 4.0) * exp(-2.0 * (kk / k0) * (kk / k0));
+        const double amp = sqrt(ek / (kk * kk));
+        /* an orthonormal pair (e1, e2) normal to k */
+        const double kv[3] = {kx / kk, ky / kk, kz / kk};
+        double t[3] = {0, 0, 0};
+        const int m = (fabs(kv[0]) < 0.6) ? 0 : ((fabs(kv[1]) < 0.6) ? 1 : 2);
+        t[m] = 1.0;
+        const double d = t[0] * kv[0] + t[1] * kv[1] + t[2] * kv[2];
+        double e1[3], e2[3];
+        for (int q = 0; q < 3; q++) e1[q] = t[q] - d * kv[q];
+        const double nrm = sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+        for (int q = 0; q < 3; q++) e1[q] /= nrm;
+        e2[0] = kv[1] * e1[2] - kv[2] * e1[1];
+        e2[1] = kv[2] * e1[0] - kv[0] * e1[2];
+        e2[2] = kv[0] * e1[1] - kv[1] * e1[0];
+        const double th = 2.0 * pi * r3;
+        const double a1 = 2.0 * pi * r1, a2 = 2.0 * pi * r2;
+        const cplx p1 = C(amp * cos(a1), amp * sin(a1)), p2 = C(amp * cos(a2), amp * sin(a2));
+        const double ct = cos(th), st = sin(th);
+        for (int q = 0; q < 3; q++) {
+          const cplx t1 = cscal(e1[q], cscal(ct, p1)), t2 = cscal(e2[q], cscal(st, p2));
+          UH(i, n, k, q) = cadd(t1, t2);
+        }
+      }
+  /* Hermitian completion of kx = 0: u(0, -n, -kz) = conj u(0, n, kz) */
+  for (int n = -ny; n <= ny; n++)
+    for (int k = 0; k < mz; k++) {
+      const double kzi = (k <= nz) ? (double)k : -(double)(mz - k);
+      if (kzi < 0 || (kzi == 0 && n < 0)) {
+        const int kneg = (k == 0) ? 0 : mz - k;
+        for (int q = 0; q < 3; q++) UH(0, n, k, q) = cconj(UH(0, -n, kneg, q));
+      }
+    }
+  /* rms scaling, <u.u>/3 = urms^2 (kx > 0 modes count twice) */
+  double e = 0.0;
+  for (int i = 0; i < nkx; i++)
+    for (int n = -ny; n <= ny; n++)
+      for (int k = 0; k < mz; k++)
+        for (int q = 0; q < 3; q++) e += (i == 0 ? 1.0 : 2.0) * cabs2(UH(i, n, k, q));
+  const double sc = (e > 0) ? urms / sqrt(e / 3.0) : 0.0;
+  /* y synthesis: v, omega_y = i kz u - i kx w, phi = lap v, and the mean profiles */
+  double *y = (double *)malloc(sizeof(double) * (size_t)my);
+  if (!y) {
+    free(uh);
+    return -1;
+  }
+  for (int j = 0; j < my; j++) y[j] = j * (Ly / my) - 0.5 * Ly;
+  memset(vor, 0, sizeof(double) * 2 * (size_t)my * nkx * mz);
+  memset(phi, 0, sizeof(double) * 2 * (size_t)my * nkx * mz);
+  for (int j = 0; j < my; j++) u00[j] = w00[j] = 0.0;
+  for (int k = 0; k < mz; k++)
+    for (int i = 0; i < nkx; i++) {
+      const double kx = alp * i, kz = gam * ((k <= nz) ? (double)k : -(double)(mz - k));
+      for (int j = 0; j < my; j++) {
+        cplx v = C(0, 0), om = C(0, 0), ph = C(0, 0), uu = C(0, 0), ww = C(0, 0);
+        for (int n = -ny; n <= ny; n++) {
+          const double ky = bet * n;
+          const double a = ky * (y[j] + 0.5 * Ly);
+          const cplx ex = C(1.0 * cos(a), 1.0 * sin(a));
+          const cplx h0 = cscal(sc, UH(i, n, k, 0)), h1 = cscal(sc, UH(i, n, k, 1));
+          const cplx h2 = cscal(sc, UH(i, n, k, 2));
+          v = cadd(v, cmul(h1, ex));
+          om = cadd(om, cmul(csub(cmul(C(0, kz), h0), cmul(C(0, kx), h2)), ex));
+          ph = cadd(ph, cmul(cscal(-(kx * kx + ky * ky + kz * kz), h1), ex));
+          uu = cadd(uu, cmul(h0, ex));
+          ww = cadd(ww, cmul(h2, ex));
+        }
+        (void)v;
+        const size_t o = 2 * ((size_t)my * ((size_t)k * nkx + i) + j);
+        if (i == 0 && k == 0) {
+          u00[j] = uu.re;
+          w00[j] = ww.re;
+          continue; /* v00 = 0 by continuity; the mean of omega_y is 0 */
+        }
+        vor[o] = om.re;
+        vor[o + 1] = om.im;
+        phi[o] = ph.re;
+        phi[o + 1] = ph.im;
+      }
+    }
+#undef UH
+  free(y);
+  free(uh);
+  return 0;
+}

@@ -110,6 +110,11 @@ void orc_lapcdy(void *h, const double *u, double k2, double *p, double shp_re,
 void orc_fourxz(void *h, double *fou, double *phys, int iopt);
 /* plain complex FFT of length n (sign -1 forward, +1 backward, unnormalised) */
 void orc_fft(int n, double *data, int sign);
+/* seeded divergence-free field of the benchmark configurations (E(k) ~ k^4
+ * exp(-2 (k/k0)^2), rms urms), pencil layout; returns 0, or -1 without memory */
+int orc_seed_state(int mgalx, int my, int mgalz, double alp, double gam, double Ly,
+                   unsigned long long seed, double k0, double urms, double *vor, double *phi,
+                   double *u00, double *w00);
 
 #ifdef __cplusplus
 }

@@ -416,13 +416,22 @@ class ShearBox:
         return out[: n.value], st
 
 
+def _lines(a, nlines: int, dtype, name: str) -> np.ndarray:
+    """A per-line host array of at least nlines entries (the C side reads
+    nlines of them)."""
+    a = np.ascontiguousarray(a, dtype).ravel()
+    if a.size < nlines:
+        raise ValueError(f"{name} has {a.size} entries, fewer than nlines={nlines}")
+    return a
+
+
 def op_derivyc(my: int, Ly: float, iord: int, u_dev: int, out_dev: int, nlines: int,
                shp: np.ndarray, shm: np.ndarray, ldu: int = None, ldo: int = None,
                stream: int = 0):
     """d/dy (iord 1) or d2/dy2 (iord 2) of nlines device-resident complex lines
     ([j][line] layout, device pointers); shp/shm host complex arrays (nlines)."""
-    sp = np.ascontiguousarray(shp, np.complex128)
-    sm = np.ascontiguousarray(shm, np.complex128)
+    sp = _lines(shp, nlines, np.complex128, "shp")
+    sm = _lines(shm, nlines, np.complex128, "shm")
     _check(lib().sb_op_derivyc(int(my), float(Ly), int(iord), int(nlines), ctypes.c_void_p(u_dev),
                                int(ldu or nlines), ctypes.c_void_p(out_dev), int(ldo or nlines),
                                _dp(sp.view(np.float64)), _dp(sm.view(np.float64)),
@@ -433,9 +442,9 @@ def op_lapcdy(my: int, Ly: float, u_dev: int, out_dev: int, nlines: int, k2: np.
               shp: np.ndarray, shm: np.ndarray, ldu: int = None, ldo: int = None,
               stream: int = 0):
     """Solves (d2/dy2 - k2) p = u on nlines device-resident complex lines."""
-    kk = np.ascontiguousarray(k2, np.float64)
-    sp = np.ascontiguousarray(shp, np.complex128)
-    sm = np.ascontiguousarray(shm, np.complex128)
+    kk = _lines(k2, nlines, np.float64, "k2")
+    sp = _lines(shp, nlines, np.complex128, "shp")
+    sm = _lines(shm, nlines, np.complex128, "shm")
     _check(lib().sb_op_lapcdy(int(my), float(Ly), int(nlines), ctypes.c_void_p(u_dev),
                               int(ldu or nlines), ctypes.c_void_p(out_dev), int(ldo or nlines),
                               _dp(kk), _dp(sp.view(np.float64)), _dp(sm.view(np.float64)),
@@ -502,7 +511,7 @@ def params_from_restart(info: SbRestartInfo, **overrides) -> SbParams:
 def op_filterc(my: int, u_dev: int, out_dev: int, nlines: int, shp: np.ndarray,
                ldu: int = None, ldo: int = None, stream: int = 0):
     """Compact y-filter of nlines device-resident complex lines (filterc)."""
-    sp = np.ascontiguousarray(shp, np.complex128)
+    sp = _lines(shp, nlines, np.complex128, "shp")
     _check(lib().sb_op_filterc(int(my), int(nlines), ctypes.c_void_p(u_dev), int(ldu or nlines),
                                ctypes.c_void_p(out_dev), int(ldo or nlines),
                                _dp(sp.view(np.float64)), ctypes.c_void_p(stream)))
@@ -525,8 +534,8 @@ def op_derivyc_noalloc(my: int, Ly: float, iord: int, u_dev: int, out_dev: int, 
                        stream: int = 0):
     """Same as op_derivyc without any device allocation: scratch in a fixed
     array of the library (limits and sharing rules in include/shearbox.h)."""
-    sp = np.ascontiguousarray(shp, np.complex128)
-    sm = np.ascontiguousarray(shm, np.complex128)
+    sp = _lines(shp, nlines, np.complex128, "shp")
+    sm = _lines(shm, nlines, np.complex128, "shm")
     _check(lib().sb_op_derivyc_noalloc(int(my), float(Ly), int(iord), int(nlines),
                                        ctypes.c_void_p(u_dev), int(ldu or nlines),
                                        ctypes.c_void_p(out_dev), int(ldo or nlines),

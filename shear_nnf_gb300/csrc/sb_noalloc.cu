@@ -10,12 +10,12 @@
 
 #include <cstddef>
 #include <cstdio>
-#include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/shearbox.h"
 #include "sb_common.cuh"
+#include "sb_fac.h"
 #include "sb_host.h"
 #include "sb_kernels.h"
 
@@ -32,30 +32,17 @@ constexpr long kTotal = kFac + 4 * kLines + kYbuf;
 // symbol: kernels are given the address from cudaGetSymbolAddress.
 static __device__ __align__(256) double g_noalloc_scratch[kTotal];
 
-std::mutex g_mu;
-std::vector<double *> g_addr;  // per device ordinal, nullptr until set up
-
-// Address of the scratch array on the current device (set-up once per device,
-// with that device current).
+// Address of the scratch array in the current device's context.  Looked up on
+// every call (no synchronisation, no allocation): a cached address would go
+// stale if the context were torn down and the module loaded again elsewhere.
 int scratch_address(double **out, std::string *err) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
   if (e != cudaSuccess) {
-    *err = std::string("cudaGetDevice: ") + cudaGetErrorString(e);
+    *err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
     return 3;
   }
-  std::lock_guard<std::mutex> lk(g_mu);
-  if ((int)g_addr.size() <= dev) g_addr.resize(dev + 1, nullptr);
-  if (!g_addr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) {
-      *err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
-      return 3;
-    }
-    g_addr[dev] = (double *)p;
-  }
-  *out = g_addr[dev];
+  *out = (double *)p;
   return 0;
 }
 
@@ -91,58 +78,27 @@ int noalloc_derivyc(int my, double Ly, int iord, int nlines, const double *u, lo
   int rc = scratch_address(&base, err);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
-  // host-side tables: factor arrays of the operator, then the shear phases
-  sbh::Coeffs co;
-  sbh::compact_coeffs(&co);
-  const double dy = Ly / (double)my;
-  const double *a = (iord == 1) ? co.pr1 : co.pr2;
+  // the operator's factor block and the shear phases, one copy into the scratch
+  HostFac hf;
   double r[4];
   int anti;
-  if (iord == 1) {
-    r[0] = 0.0;
-    for (int d = 1; d <= 3; d++) r[d] = co.rh1h[3 + d] / dy;
-    anti = 1;
-  } else {
-    for (int d = 0; d <= 3; d++) r[d] = co.rh2h[3 + d] / (dy * dy);
-    anti = 0;
-  }
-  sbh::BaseFac b;
-  sbh::base_factor(a, my, &b);
-  const long n = my;
-  std::vector<double> host(8 * n + 10 + 4 * (size_t)nlines, 0.0);
-  const std::vector<double> *arr[8] = {&b.La, &b.Lb, &b.Lc, &b.Ddm1, &b.Dd, &b.e, &b.f, &b.g};
-  for (int q = 0; q < 8; q++)
-    for (long j = 0; j < n; j++) host[q * n + j] = (*arr[q])[j];
-  for (int q = 0; q < 6; q++) host[8 * n + q] = b.sums[q];
-  for (int q = 0; q < 4; q++) host[8 * n + 6 + q] = a[3 + q];
+  const std::vector<double> host = derivyc_block(my, Ly, iord, nlines, shp, shm, &hf, r, &anti);
+  const size_t nfac = hf.buf.size();  // 8*my + 10 <= kFac
   double *dfac = base;
   double *dsh = base + kFac;
   double *ybuf = base + kFac + 4 * kLines;
-  for (long q = 0; q < 2L * nlines; q++) {
-    host[8 * n + 10 + q] = shp[q];
-    host[8 * n + 10 + 2L * nlines + q] = shm[q];
-  }
-  cudaError_t e = cudaMemcpyAsync(dfac, host.data(), sizeof(double) * (8 * n + 10),
+  cudaError_t e = cudaMemcpyAsync(dfac, host.data(), sizeof(double) * nfac,
                                   cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(dsh, host.data() + 8 * n + 10, sizeof(double) * 4 * (size_t)nlines,
+    e = cudaMemcpyAsync(dsh, host.data() + nfac, sizeof(double) * 4 * (size_t)nlines,
                         cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) {
     *err = std::string("cudaMemcpyAsync: ") + cudaGetErrorString(e);
     return 3;
   }
-  Fac F;
-  F.La = dfac;
-  F.Lb = dfac + n;
-  F.Lc = dfac + 2 * n;
-  F.Ddm1 = dfac + 3 * n;
-  F.Dd = dfac + 4 * n;
-  F.e = dfac + 5 * n;
-  F.f = dfac + 6 * n;
-  F.g = dfac + 7 * n;
-  F.sums = dfac + 8 * n;
-  F.stride = 0;
+  const Fac F = fac_bind(hf, dfac);
   e = launch_op_line(nlines, my, u, ldu, out, ldo, ybuf, F, dsh, dsh + 2 * nlines, r, anti, st);
+  // the copies read the pageable host block: wait before it goes out of scope
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     *err = std::string("derivyc launch: ") + cudaGetErrorString(e);

@@ -82,6 +82,49 @@ def test_seed_state_reproducible_and_seed_dependent():
     assert not np.allclose(a["vor"], c["vor"])
 
 
+@pytest.mark.parametrize("grid,seed,k0", [((64, 32, 32), 3, 4.0), ((96, 48, 48), 77, 4.0),
+                                          ((192, 96, 96), 3, 4.0), ((64, 32, 32), 11, 6.0)])
+def test_oracle_seed_matches_library_bitwise(grid, seed, k0):
+    """The oracle's restatement of the seeded field (used by the CPU baseline,
+    which must not load the library under test) equals sb_seed_state bit for
+    bit."""
+    import oracle
+    import shear_nnf_gb300 as sb
+    pp = box_params(*grid, rez=1000.0)
+    a = sb.seed_state(sb.make_params(**pp), seed, k0=k0)
+    b = oracle.seed_state(seed=seed, k0=k0, **pp)
+    for key in ("vor", "phi", "u00", "w00"):
+        assert a[key].shape == b[key].shape
+        assert np.array_equal(a[key].view(np.float64), b[key].view(np.float64)), key
+
+
+def test_oracle_seed_matches_library_with_temperature():
+    import oracle
+    import shear_nnf_gb300 as sb
+    pp = box_params(64, 32, 32, rez=1000.0, temperature=1, fkappa=0.01)
+    a = sb.seed_state(sb.make_params(**pp), 7)
+    b = oracle.seed_state(seed=7, **pp)
+    for key in ("tb", "tb00", "vor"):
+        assert np.array_equal(np.asarray(a[key]).view(np.float64),
+                              np.asarray(b[key]).view(np.float64)), key
+
+
+def test_operator_wrappers_reject_short_line_arrays():
+    """The C side reads nlines entries of each per-line host array: shorter
+    arrays are refused before any call."""
+    import shear_nnf_gb300 as sb
+    short = np.ones(3, np.complex128)
+    full = np.ones(8, np.complex128)
+    with pytest.raises(ValueError, match="shp"):
+        sb.op_derivyc(32, 2 * np.pi, 1, 0, 0, 8, short, full)
+    with pytest.raises(ValueError, match="shm"):
+        sb.op_derivyc_noalloc(32, 2 * np.pi, 1, 0, 0, 8, full, short)
+    with pytest.raises(ValueError, match="k2"):
+        sb.op_lapcdy(32, 2 * np.pi, 0, 0, 8, np.ones(2), full, full)
+    with pytest.raises(ValueError, match="shp"):
+        sb.op_filterc(32, 0, 0, 8, short)
+
+
 def test_invalid_grid_rejected_without_gpu():
     import shear_nnf_gb300 as sb
     p = sb.make_params(**box_params(100, 32, 32, rez=1000.0))

@@ -67,6 +67,30 @@ def test_hundred_steps_64():
     assert status.steps_done == 100
 
 
+def test_hundred_steps_benchmark_box():
+    """The benchmark configuration itself (192x96x96, Re_z 4000, CFL 0.5, the
+    seed of the bench): the drop-in bar after 100 steps, with every record of
+    the UNER trace."""
+    pp = box_params(192, 96, 96, rez=4000.0, cfl=0.5)
+    st_o, tr_o, st_g, tr_g, status = _run_both(pp, 100, seed=3)
+    err = _field_errors(st_o, st_g)
+    assert max(err.values()) < MANY_STEPS, err
+    assert tr_g.shape[0] == 100
+    assert _trace_error(tr_g, tr_o) < TRACE_TOL
+    assert status.steps_done == 100 and status.istop == 0
+    assert abs(st_g["time"] - st_o["time"]) < 1e-12 * st_o["time"]
+
+
+def test_twenty_steps_largest_grid():
+    """384x192x192 without LES (Re_z 20000, k0 6), 20 CFL steps."""
+    pp = box_params(384, 192, 192, rez=20000.0, cfl=0.5)
+    st_o, tr_o, st_g, tr_g, status = _run_both(pp, 20, seed=6, k0=6.0)
+    err = _field_errors(st_o, st_g)
+    assert max(err.values()) < MANY_STEPS, err
+    assert _trace_error(tr_g, tr_o) < TRACE_TOL
+    assert status.steps_done == 20
+
+
 @pytest.mark.parametrize("les", [0, 1])
 def test_one_step_largest_grid(les):
     # the largest transform lengths (x 384, z 192) and my = 192, with and

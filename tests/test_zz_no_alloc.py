@@ -40,6 +40,37 @@ def test_noalloc_matches_allocating_entry_point_twice():
         assert err < TOL, (call, err)
 
 
+def test_noalloc_exact_fit_matches_allocating_entry_point():
+    """The largest request the scratch holds: 32768 lines of 16 points fill the
+    y-buffer exactly (16 * pad32(2 * 32768) = 2**20 doubles)."""
+    import torch
+    import shear_nnf_gb300 as sb
+    nlines, my = 32768, 16
+    assert my * (((2 * nlines + 31) // 32) * 32) == 1 << 20
+    u, shp, shm = _case(nlines, my, 7)
+    du = torch.from_numpy(u).cuda()
+    ref = torch.zeros_like(du)
+    got = torch.full_like(du, float("nan"))
+    sb.op_derivyc(my, 2 * np.pi, 1, du.data_ptr(), ref.data_ptr(), nlines, shp, shm)
+    sb.op_derivyc_noalloc(my, 2 * np.pi, 1, du.data_ptr(), got.data_ptr(), nlines, shp, shm)
+    r = ref.cpu().numpy()
+    g = got.cpu().numpy()
+    assert np.all(np.isfinite(g))
+    assert np.abs(g - r).max() / np.abs(r).max() < TOL
+
+
+@pytest.mark.parametrize("nlines,my", [(32769, 16), (32768, 17)])
+def test_noalloc_rejects_one_past_the_limit(nlines, my):
+    """One line more than the limit, or one point more per line at the full
+    line count, is refused with error 6 before any device work."""
+    import torch
+    import shear_nnf_gb300 as sb
+    du = torch.zeros((1, 1), dtype=torch.complex128, device="cuda")
+    one = np.ones(nlines, np.complex128)
+    with pytest.raises(sb.ShearBoxError, match="error 6.*exceed the fixed scratch"):
+        sb.op_derivyc_noalloc(my, 2 * np.pi, 1, du.data_ptr(), du.data_ptr(), nlines, one, one)
+
+
 def test_noalloc_rejects_oversized_requests():
     import torch
     import shear_nnf_gb300 as sb
