@@ -17,7 +17,9 @@ step (three substeps) of that box.
          box, FP64 and FP32-mixed, against the plain step.
   newton  batched Newton Jv/s: 32 finite-difference products on 96x48x48
          (Re_z=1200, T=20/S) as one FP32-mixed batch (central differences)
-         vs one FP64 product at a time.
+         vs one FP64 product at a time; the search of that configuration to
+         |F|/|x| <= 1e-10 (unbatched FP64 and batched FP32-mixed, wall time)
+         and the 20 leading Floquet multipliers by block Arnoldi.
   cpu_baseline  the C oracle (restatement of the reference step) on the
          host cores, a bounded sample of steps of the same workload.
 
@@ -382,6 +384,87 @@ def temperature_leg(sb, torch, dist, ws, rank, args, plain_steps_per_s):
     return out
 
 
+def newton_search_leg(sb, torch, dist, ws, rank, args, T=20.0, s_star=0.37, pert=1e-3):
+    """The periodic-orbit search of the 96x48x48 configuration (Re_z = 1200,
+    T = 20/S, streamwise shift unknown) run to |F|/|x| <= 1e-10, every vector
+    on the device.  No orbit of this flow ships with the reference, so the
+    search targets a manufactured relative periodic orbit of the configuration's
+    own period map: x* = Phi_20(seeded field) (a developed state), s* = 0.37,
+    F(x, s) = shift_s(Phi_T(x)) - x - r with r = shift_s*(Phi_T(x*)) - x*, from
+    the start x* + 1e-3 |x*| (random direction), s* - 0.005.
+      unbatched_fp64  the reference's algorithm: GMRES one product at a time
+                      (k_gmres 50, eps_gmresk 1e-3, gmres_shear.f90:24-25,2099),
+                      FP64 forward differences at eps_jacobi 1e-7, the base
+                      taken from the residual's integration
+      batched_mixed   block GMRES, 16 forward differences (eps_jacobi 1e-3) and
+                      their base as one 17-member FP32-mixed batch per block,
+                      at most 3 blocks per Newton step, each solve after the
+                      first starting from 15 Ritz directions of the previous
+                      one (deflated restarting)
+    Both take their residuals from the same FP64 map.  Then block Arnoldi
+    (4 blocks of 32 FP32-mixed forward differences) at the converged point
+    gives the 20 leading multipliers of the shifted map's Jacobian, their
+    Ritz residual estimates and the exponents log(lambda)/T."""
+    from shear_nnf_gb300 import krylov as kr
+    from shear_nnf_gb300 import newton as nw
+    pp = dict(mgalx=96, my=48, mgalz=48, Re=1200.0 / LZ ** 2, alp=0.5, Ly=LZ, gam=1.0, s=1.0,
+              chi=0.0, CFL=0.5)
+    p = sb.make_params(**pp)
+    sca = nw.Packing.reference_scales(p)
+    pk = nw.Packing(p, *sca)
+    n = pk.n
+    ks = kr.KSpace(n + 1, 1400)
+    res64 = kr.DevPeriodMap(p, T, batch=1, sca=sca)
+    xs, rhs, x = ks.alloc(1), ks.alloc(1), ks.alloc(1)
+    ks.set(xs, pk.pack(sb.seed_state(p, 77 + rank)))
+    res64(ks, [xs], [xs])
+    res64(ks, [xs], [rhs], shift=(s_star, 0.0))
+    ks.combine(rhs, [rhs, xs], [1.0, -1.0], n)
+    xsv = ks.get(xs, 0, n)
+    d = np.random.default_rng(15 + rank).standard_normal(n)
+    x0v = np.concatenate([xsv + pert * np.linalg.norm(xsv) / np.linalg.norm(d) * d, [0.0]])
+    pm32 = kr.DevPeriodMap(p, T, batch=17, precision=sb.SB_MIXED, sca=sca)
+    cfgs = (("unbatched_fp64", dict(jac=res64, block=1, k=50, eps=1e-7, base=False, recycle=0)),
+            ("batched_mixed", dict(jac=pm32, block=16, k=3, eps=1e-3, base=True, recycle=15)))
+    out = {"grid": [96, 48, 48], "re_z": 1200.0, "period_T": T, "unknowns": n + 1,
+           "target": "manufactured relative periodic orbit (x*, s*) of the configuration's map",
+           "start_rel_perturbation": pert, "tol": 1e-10}
+    for key, c in cfgs:
+        ks.set(x, x0v)
+        barrier(dist)
+        t0 = time.perf_counter()
+        s, hist, st = kr.newton_rpo(ks, p, x, s_star - 0.005, res64, c["jac"], rhs=rhs, k=c["k"],
+                                    block=c["block"], itmax=12, tol=1e-10, gmres_tol=1e-3,
+                                    eps_jacobi=c["eps"], order=1, base_in_batch=c["base"],
+                                    recycle=c["recycle"])
+        secs = allmax(dist, time.perf_counter() - t0)
+        out[key] = {"seconds": secs, "converged": bool(hist[-1] <= 1e-10),
+                    "final_rel_residual": hist[-1], "history": hist, "shift": s,
+                    "newton_iterations": st["newton"], "gmres_iterations": st["gmres_iterations"],
+                    "products": st["products"], "fp64_residual_integrations": st["residuals"],
+                    "block": c["block"], "eps_jacobi": c["eps"],
+                    "precision_products": "FP64" if c["jac"] is res64 else "FP32-mixed"}
+    a, b = out["unbatched_fp64"], out["batched_mixed"]
+    out["speedup_batched_vs_unbatched_wall"] = a["seconds"] / b["seconds"]
+    # Floquet analysis at the point the batched search converged to
+    pmf = kr.DevPeriodMap(p, T, batch=33, precision=sb.SB_MIXED, sca=sca)
+    J = kr.DevJacobian(pmf, ks, x, shift=(b["shift"], 0.0), eps_jacobi=1e-3, order=1,
+                       base_in_batch=True)
+    t0 = time.perf_counter()
+    lam, rres, _ = kr.arnoldi_dev(ks, J.matvec, 4, block=32, rows=n, seed=5)
+    ta = time.perf_counter() - t0
+    top = lam[:20]
+    out["floquet"] = {"multipliers_abs": [float(abs(v)) for v in top],
+                      "multipliers_arg": [float(np.angle(v)) for v in top],
+                      "exponents_re": [float(np.log(abs(v)) / T) for v in top],
+                      "ritz_residual": [float(r) for r in rres[:20]],
+                      "products": J.products, "seconds": ta,
+                      "method": "block Arnoldi, 4 x 32 FP32-mixed forward differences "
+                                "(eps_jacobi 1e-3), base in every batch"}
+    del pm32, pmf, res64, ks
+    return out
+
+
 def newton_leg(sb, torch, dist, ws, rank, args, nper=32, T=20.0):
     """Batched Newton Jv: the Jacobian-vector products of the periodic-orbit
     search on 96x48x48 (Re_z=1200, period T=20/S) through the Newton tools'
@@ -623,6 +706,8 @@ def run_ours(args):
                  "tuning": mtuning}
     ensemble = None if args.no_ensemble else ensemble_leg(sb, torch, dist, ws, rank, args)
     newton = None if args.no_newton else newton_leg(sb, torch, dist, ws, rank, args)
+    if newton is not None and not args.no_search:
+        newton["search"] = newton_search_leg(sb, torch, dist, ws, rank, args)
     les = None if args.no_les else les_leg(sb, torch, dist, ws, rank, args)
     temp = (None if args.no_temp else
             temperature_leg(sb, torch, dist, ws, rank, args, steps_per_s))
@@ -682,6 +767,8 @@ def main():
     ap.add_argument("--no-mixed", action="store_true", help="skip the FP32-mixed leg")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble leg")
     ap.add_argument("--no-newton", action="store_true", help="skip the batched Newton Jv leg")
+    ap.add_argument("--no-search", action="store_true",
+                    help="skip the Newton search and Floquet analysis of the newton leg")
     ap.add_argument("--no-les", action="store_true", help="skip the LES leg")
     ap.add_argument("--les-steps", type=int, default=1000,
                     help="most steps of the LES leg (it stops at t = 2, one remesh period)")

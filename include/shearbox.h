@@ -186,6 +186,70 @@ int sb_jv_batch(sb_handle *h, const double *x0, double time0, double xoffb, doub
                 double T, const double *dirs, int ndir, double eps_jacobi, int central,
                 double *out);
 
+/* Device-resident unknown vectors of the Newton-Krylov and Arnoldi searches.
+ * A packed vector is the unknown vector of `throwing` (gmres_shear.f90:
+ * 2229-2426, iuse_fou_mode 2): u00/sca[0] (my), w00/sca[0] (my), then per y
+ * plane j, per kz index k = 0..mz-1 and kx index i (skipping (0,0) and the
+ * kx = 0 entries of negative kz, which set_conj restores) the four doubles
+ * vor.re/sca[1], phi.re/sca[2], vor.im/sca[1], phi.im/sca[2]; its length is
+ * sb_packed_length(h) = 2 my + 4 my (mz nkx - 1 - nz).  phi stands where the
+ * reference throws v (a fixed invertible map per mode).  x is a DEVICE
+ * pointer; the work is queued on the handle's stream.
+ *   sb_set_state_packed  backthrowing + set_conj into a member, with its time
+ *                        and image offsets (as sb_set_state does from host
+ *                        arrays; the LES running maximum of nu_t restarts)
+ *   sb_get_state_packed  throwing of a member's state, each mode multiplied by
+ *                        exp(-i kx shiftx) exp(-i kz shiftz) (phase_shift_fou,
+ *                        operators.f90:488-544) on the way
+ * Not available for the temperature variant. */
+long sb_packed_length(const sb_handle *h);
+int sb_set_state_packed(sb_handle *h, int member, const double *x, const double sca[3],
+                        double time, double xoffb, double xofft);
+int sb_get_state_packed(sb_handle *h, int member, double *x, const double sca[3], double shiftx,
+                        double shiftz);
+/* d/ds of phase_shift_fou at s = 0 on a packed vector (device x, out; in place
+ * allowed): every mode times -i kx (dir 0) or -i kz (dir 1), the mean profiles
+ * zero -- the shift columns dG/ds and the phase-condition rows of the
+ * relative-periodic-orbit system (gmres_shear.f90:2900-2934). */
+int sb_packed_shift_tangent(sb_handle *h, const double *x, double *out, int dir);
+
+/* A Krylov space on the device: `cols` FP64 vectors of n entries (columns
+ * 256-byte aligned), replacing the rank-0 vector algebra of the reference's
+ * GMRES and Arnoldi (dotp, vecadd, norm, gmres_shear.f90:3680-3919; the
+ * Gram-Schmidt loops of gmres_k_shear, 1905-2207, and arnoldi_shear.f90:
+ * 222-330).  Row ranges [r0, r1) select the entries an operation covers.
+ * stream NULL gives the space its own stream; pass a handle's stream
+ * (sb_get_stream) to order the space's work with that handle's.
+ *   sb_kspace_gram       C[a][b] = <col a0+a, col b0+b>, m x p, row-major host
+ *                        array; fixed-order reductions (bitwise reproducible)
+ *   sb_kspace_update     col b0+b += alpha sum_a col a0+a C[a][b] (ranges
+ *                        must not overlap; C host m x p row-major)
+ *   sb_kspace_transform  cols b0..b0+p-1 <- (cols b0..) M, p <= 64, in place
+ *   sb_kspace_combine    col dst = sum_k coef[k] col src[k], nsrc <= 8
+ *   sb_kspace_perturb    col dst = x0 + ((x0 + e d) - x0) (the representable
+ *                        step of matvec_dns_disk3d, iuse_hej)
+ *   sb_kspace_fd         finite-difference product of order 1, 2 or 4 into
+ *                        col dst from the columns g (2 or 4 of them): (g0-g1)/eps,
+ *                        (g0-g1)/(2 eps), (8 (g0-g1) - (g2-g3))/(12 eps)
+ *   sb_kspace_set/get    host <-> part of one column (synchronous)
+ *   sb_kspace_col        device address of a column (NULL if out of range) */
+typedef struct sb_kspace sb_kspace;
+int sb_kspace_create(long n, int cols, void *stream, sb_kspace **out);
+int sb_kspace_destroy(sb_kspace *ks);
+double *sb_kspace_col(sb_kspace *ks, int col);
+void *sb_kspace_stream(sb_kspace *ks);
+int sb_kspace_sync(sb_kspace *ks);
+int sb_kspace_gram(sb_kspace *ks, long r0, long r1, int a0, int m, int b0, int p, double *C);
+int sb_kspace_update(sb_kspace *ks, long r0, long r1, int a0, int m, int b0, int p,
+                     const double *C, double alpha);
+int sb_kspace_transform(sb_kspace *ks, long r0, long r1, int b0, int p, const double *M);
+int sb_kspace_combine(sb_kspace *ks, long r0, long r1, int dst, int nsrc, const int *src,
+                      const double *coef);
+int sb_kspace_perturb(sb_kspace *ks, long r0, long r1, int dst, int x0, int d, double e);
+int sb_kspace_fd(sb_kspace *ks, long r0, long r1, int dst, int order, const int *g, double eps);
+int sb_kspace_set(sb_kspace *ks, int col, long off, long len, const double *host);
+int sb_kspace_get(sb_kspace *ks, int col, long off, long len, double *host);
+
 /* Measurement hooks (no counterpart in the reference; used by the benchmark).
  * sb_launch_stage enqueues `count` launches of one kernel of substep rk on the
  * handle's stream: stage 1..3 the plane stages, 4 the per-box phase tables,

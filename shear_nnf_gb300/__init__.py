@@ -84,7 +84,11 @@ ABI_FUNCTIONS = [
     "sb_set_member_etime", "sb_op_filterc", "sb_op_cfty", "sb_op_rfty", "sb_write_restart",
     "sb_read_restart", "sb_autotune", "sb_physical_fields", "sb_set_temperature",
     "sb_get_temperature", "sb_crosst", "sb_stats", "sb_jv_batch", "sb_get_statistics",
-    "sb_fft_twiddles",
+    "sb_fft_twiddles", "sb_packed_length", "sb_set_state_packed", "sb_get_state_packed",
+    "sb_packed_shift_tangent",
+    "sb_kspace_create", "sb_kspace_destroy", "sb_kspace_col", "sb_kspace_stream",
+    "sb_kspace_sync", "sb_kspace_gram", "sb_kspace_update", "sb_kspace_transform",
+    "sb_kspace_combine", "sb_kspace_perturb", "sb_kspace_fd", "sb_kspace_set", "sb_kspace_get",
 ]
 
 _lib = None
@@ -151,6 +155,31 @@ def lib(auto_build: bool = False):
                                    ctypes.c_double]
     L.sb_read_restart.argtypes = [ctypes.c_char_p, ctypes.POINTER(SbParams), dp, dp, dp, dp,
                                   ctypes.POINTER(SbRestartInfo)]
+    L.sb_packed_length.restype = ctypes.c_long
+    L.sb_packed_length.argtypes = [vp]
+    L.sb_set_state_packed.argtypes = [vp, ctypes.c_int, vp, dp, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_double]
+    L.sb_get_state_packed.argtypes = [vp, ctypes.c_int, vp, dp, ctypes.c_double, ctypes.c_double]
+    L.sb_packed_shift_tangent.argtypes = [vp, vp, vp, ctypes.c_int]
+    lg = ctypes.c_long
+    L.sb_kspace_create.argtypes = [lg, ctypes.c_int, vp, ctypes.POINTER(vp)]
+    L.sb_kspace_destroy.argtypes = [vp]
+    L.sb_kspace_col.restype = vp
+    L.sb_kspace_col.argtypes = [vp, ctypes.c_int]
+    L.sb_kspace_stream.restype = vp
+    L.sb_kspace_stream.argtypes = [vp]
+    L.sb_kspace_sync.argtypes = [vp]
+    L.sb_kspace_gram.argtypes = [vp, lg, lg, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_int, dp]
+    L.sb_kspace_update.argtypes = [vp, lg, lg, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int, dp, ctypes.c_double]
+    L.sb_kspace_transform.argtypes = [vp, lg, lg, ctypes.c_int, ctypes.c_int, dp]
+    L.sb_kspace_combine.argtypes = [vp, lg, lg, ctypes.c_int, ctypes.c_int, ip, dp]
+    L.sb_kspace_perturb.argtypes = [vp, lg, lg, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_double]
+    L.sb_kspace_fd.argtypes = [vp, lg, lg, ctypes.c_int, ctypes.c_int, ip, ctypes.c_double]
+    L.sb_kspace_set.argtypes = [vp, ctypes.c_int, lg, lg, dp]
+    L.sb_kspace_get.argtypes = [vp, ctypes.c_int, lg, lg, dp]
     _lib = L
     return L
 
@@ -360,6 +389,31 @@ class ShearBox:
                                  float(T), _dp(d), int(d.shape[0]), float(eps_jacobi),
                                  int(bool(central)), _dp(out)))
         return out
+
+    @property
+    def packed_length(self) -> int:
+        """Length of the packed unknown vector (sb_packed_length)."""
+        return int(lib().sb_packed_length(self.h))
+
+    def set_state_packed(self, member: int, x_dev: int, sca, time=0.0, xoffb=0.0, xofft=0.0):
+        """Sets a member from a packed vector at device address x_dev
+        (sb_set_state_packed; queued on the handle's stream)."""
+        sc = np.ascontiguousarray(sca, np.float64)
+        _check(lib().sb_set_state_packed(self.h, int(member), ctypes.c_void_p(x_dev), _dp(sc),
+                                         float(time), float(xoffb), float(xofft)))
+
+    def get_state_packed(self, member: int, x_dev: int, sca, shiftx=0.0, shiftz=0.0):
+        """Writes a member's state, phase-shifted, as a packed vector at device
+        address x_dev (sb_get_state_packed; queued on the handle's stream)."""
+        sc = np.ascontiguousarray(sca, np.float64)
+        _check(lib().sb_get_state_packed(self.h, int(member), ctypes.c_void_p(x_dev), _dp(sc),
+                                         float(shiftx), float(shiftz)))
+
+    def shift_tangent_packed(self, x_dev: int, out_dev: int, which: str = "x"):
+        """d/ds of the phase shift on a packed device vector (-i kx or -i kz
+        times every mode; sb_packed_shift_tangent, handle's stream)."""
+        _check(lib().sb_packed_shift_tangent(self.h, ctypes.c_void_p(x_dev),
+                                             ctypes.c_void_p(out_dev), 0 if which == "x" else 1))
 
     def fp64_peak(self) -> float:
         v = ctypes.c_double()

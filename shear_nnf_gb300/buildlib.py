@@ -18,7 +18,7 @@ LIB = os.path.join(BUILD, "libshearbox.so")
 # FP64 and FP32-mixed instantiations in parallel
 UNITS = [("sb_kernels.cu", ["-DSB_FLOAT_TU=0"]), ("sb_kernels.cu", ["-DSB_FLOAT_TU=1"]),
          ("sb_yline.cu", ["-DSB_FLOAT_TU=0"]), ("sb_yline.cu", ["-DSB_FLOAT_TU=1"]),
-         ("sb_ops.cu", []), ("sb_noalloc.cu", []), ("sb_api.cu", []),
+         ("sb_ops.cu", []), ("sb_noalloc.cu", []), ("sb_api.cu", []), ("sb_krylov.cu", []),
          # host set-up (coefficients, factorisations, the seeded field) without
          # fused multiply-adds: the same bits on x86 and Arm hosts
          ("sb_host.cpp", ["-Xcompiler", "-ffp-contract=off"]),

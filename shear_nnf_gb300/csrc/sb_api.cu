@@ -769,6 +769,52 @@ int sb_get_state(sb_handle *h, int member, double *vor, double *phi, double *u00
   return get_state_impl(h, member, vor, phi, u00, w00, time, xoffb, xofft, nullptr);
 }
 
+long sb_packed_length(const sb_handle *h) { return h ? packed_length(h->g) : -1; }
+
+int sb_set_state_packed(sb_handle *h, int member, const double *x, const double sca[3],
+                        double time, double xoffb, double xofft) {
+  if (!h || member < 0 || member >= h->g.B) return fail(1, "bad handle or member");
+  if (!x || !sca) return fail(1, "null argument");
+  if (h->g.temp) return fail(2, "packed states carry no temperature");
+  if (!(sca[0] != 0.0 && sca[1] != 0.0 && sca[2] != 0.0)) return fail(1, "zero scale");
+  const Grid &g = h->g;
+  const size_t Fd = g.prec ? g.field / 2 : g.field;
+  const size_t mud = g.prec ? (size_t)g.my : 2 * (size_t)g.my;  // doubles per member's mean line
+  CK(launch_unpack(g, x, h->bf.vor + member * Fd, h->bf.phi + member * Fd,
+                   h->bf.mu + member * mud, sca, h->st));
+  // the pinned staging may feed an earlier copy still in flight
+  CK(cudaStreamSynchronize(h->st));
+  sb_handle::HostSmall &hs = *h->hs;
+  hs.sc_in[0] = time;
+  hs.sc_in[1] = xoffb;
+  hs.sc_in[2] = xofft;
+  CK(cudaMemcpyAsync((char *)(h->bf.mem + member) + offsetof(Member, time), hs.sc_in,
+                     sizeof(hs.sc_in), cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemsetAsync((char *)(h->bf.mem + member) + offsetof(Member, max_nut), 0, sizeof(double),
+                     h->st));
+  return 0;
+}
+
+int sb_packed_shift_tangent(sb_handle *h, const double *x, double *out, int dir) {
+  if (!h || !x || !out) return fail(1, "null argument");
+  if (dir != 0 && dir != 1) return fail(1, "dir must be 0 (x) or 1 (z)");
+  CK(launch_tangent(h->g, x, out, dir, h->st));
+  return 0;
+}
+
+int sb_get_state_packed(sb_handle *h, int member, double *x, const double sca[3], double shiftx,
+                        double shiftz) {
+  if (!h || member < 0 || member >= h->g.B) return fail(1, "bad handle or member");
+  if (!x || !sca) return fail(1, "null argument");
+  if (!(sca[0] != 0.0 && sca[1] != 0.0 && sca[2] != 0.0)) return fail(1, "zero scale");
+  const Grid &g = h->g;
+  const size_t Fd = g.prec ? g.field / 2 : g.field;
+  const size_t mud = g.prec ? (size_t)g.my : 2 * (size_t)g.my;
+  CK(launch_pack(g, h->bf.vor + member * Fd, h->bf.phi + member * Fd, h->bf.mu + member * mud, x,
+                 sca, shiftx, shiftz, h->st));
+  return 0;
+}
+
 // mean profile of one member: [my] reals <-> the re parts of a [my] complex
 // device line in the storage precision
 static int put_mean_re(sb_handle *h, double *dev, int member, const double *v) {

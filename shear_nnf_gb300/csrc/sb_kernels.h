@@ -41,6 +41,13 @@ long op_threads(int nlines);
 cudaError_t launch_op_line(int nlines, int N, const double *u, long ldu, double *out, long ldo,
                            double *ybuf, const Fac &F, const double *shp, const double *shm,
                            const double r[4], int anti, cudaStream_t st);
+long packed_length(const Grid &g);
+cudaError_t launch_pack(const Grid &g, const double *vor, const double *phi, const double *mu,
+                        double *x, const double sca[3], double sx, double sz, cudaStream_t st);
+cudaError_t launch_unpack(const Grid &g, const double *x, double *vor, double *phi, double *mu,
+                          const double sca[3], cudaStream_t st);
+cudaError_t launch_tangent(const Grid &g, const double *x, double *out, int dir,
+                           cudaStream_t st);
 int noalloc_derivyc(int my, double Ly, int iord, int nlines, const double *u, long ldu,
                     double *out, long ldo, const double *shp, const double *shm, void *stream,
                     std::string *err);
