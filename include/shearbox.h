@@ -345,10 +345,28 @@ int sb_op_derivyc_noalloc(int my, double Ly, int iord, int nlines, const double 
  * every kz, kx), then the footer CFL/uprim/vbulk/xforce, irev/nopt/nparams,
  * the 9 switches and 13 parameters.
  * sb_read_restart reads one as getfil does (readwrite.f90:72-447): with p NULL
- * only *info is filled; otherwise the state is mapped on p's grid (the common
- * kx modes and the lowest positive and negative kz modes, zeros elsewhere;
- * the file's my must equal p->my) and set_conj is applied.  Errors: 7 I/O,
- * 8 malformed file, 9 unsupported grid change; message in sb_last_error. */
+ * only *info is filled; otherwise the state is mapped on p's grid and set_conj
+ * is applied:
+ *   x, z   the common kx modes and the lowest positive and negative kz modes,
+ *          zeros elsewhere; a changed alp rescales the image offsets by
+ *          alp_file/alp, and a doubled alp with half the x points keeps the
+ *          file's even kx modes (ihalf)
+ *   y      my = file my: as read; my = file my / 2: every other plane
+ *          (ihalfy); my = 3 or 5 file my: the box stacked in y, copy n shifted
+ *          by exp(-i kx xofft n), offsets times 3 or 5 (ncopy_y); any other
+ *          my > file my: a natural cubic spline in y per mode line through the
+ *          file's planes and the wrapped first plane at Ly/2 (interp_y,
+ *          readwrite.f90:707-771; needs the file's Ly); my < file my (not
+ *          half): the first my planes, as getfil reads them
+ *   scale  a changed gam rescales u00, w00 by gam_file/gam, phi by
+ *          gam/gam_file and (without LES) vor by (gam_file/gam) sqrt(Re/Re_file);
+ *          a changed Re alone rescales vor by sqrt(Re/Re_file) (without LES and
+ *          unless flags has SB_RESTART_KEEP_VOR, as the Newton drivers read)
+ * The offsets of the mapped state are info->run_xoffb/run_xofft (info->xoffb/
+ * xofft are the file's); info->ymap says which y mapping ran (0 as read,
+ * 1 half, 2 stacked, 3 spline).  Errors: 7 I/O, 8 malformed file, 9
+ * unsupported grid change (x and y together, alp and my together, a spline
+ * with a different Ly); message in sb_last_error. */
 #define SB_RESTART_MAXOPT 32
 typedef struct sb_restart_info {
   int mgalx, my, mgalz, numerop;         /* record 1 */
@@ -359,12 +377,17 @@ typedef struct sb_restart_info {
   int has_footer, irev, nopt, nparams;
   int options[SB_RESTART_MAXOPT];
   double params[SB_RESTART_MAXOPT];
+  double run_xoffb, run_xofft;           /* offsets of the state mapped on p */
+  int ymap, ncopy, xskip;                /* y mapping, stack count, kx stride */
 } sb_restart_info;
+#define SB_RESTART_KEEP_VOR 1
 int sb_write_restart(const char *path, const sb_params *p, const double *vor, const double *phi,
                      const double *u00, const double *w00, double time, double xoffb,
                      double xofft, double deltat);
 int sb_read_restart(const char *path, const sb_params *p, double *vor, double *phi, double *u00,
                     double *w00, sb_restart_info *info);
+int sb_read_restart_ex(const char *path, const sb_params *p, int flags, double *vor, double *phi,
+                       double *u00, double *w00, sb_restart_info *info);
 
 /* CUDA stream of the handle (cudaStream_t) and a blocking wait on it. */
 void *sb_get_stream(sb_handle *h);

@@ -64,7 +64,12 @@ class SbRestartInfo(ctypes.Structure):
         ("has_footer", ctypes.c_int), ("irev", ctypes.c_int), ("nopt", ctypes.c_int),
         ("nparams", ctypes.c_int),
         ("options", ctypes.c_int * RESTART_MAXOPT), ("params", ctypes.c_double * RESTART_MAXOPT),
+        ("run_xoffb", ctypes.c_double), ("run_xofft", ctypes.c_double),
+        ("ymap", ctypes.c_int), ("ncopy", ctypes.c_int), ("xskip", ctypes.c_int),
     ]
+
+
+RESTART_KEEP_VOR = 1
 
 
 class SbStatus(ctypes.Structure):
@@ -89,6 +94,7 @@ ABI_FUNCTIONS = [
     "sb_kspace_create", "sb_kspace_destroy", "sb_kspace_col", "sb_kspace_stream",
     "sb_kspace_sync", "sb_kspace_gram", "sb_kspace_update", "sb_kspace_transform",
     "sb_kspace_combine", "sb_kspace_perturb", "sb_kspace_fd", "sb_kspace_set", "sb_kspace_get",
+    "sb_read_restart_ex",
 ]
 
 _lib = None
@@ -155,6 +161,8 @@ def lib(auto_build: bool = False):
                                    ctypes.c_double]
     L.sb_read_restart.argtypes = [ctypes.c_char_p, ctypes.POINTER(SbParams), dp, dp, dp, dp,
                                   ctypes.POINTER(SbRestartInfo)]
+    L.sb_read_restart_ex.argtypes = [ctypes.c_char_p, ctypes.POINTER(SbParams), ctypes.c_int, dp,
+                                     dp, dp, dp, ctypes.POINTER(SbRestartInfo)]
     L.sb_packed_length.restype = ctypes.c_long
     L.sb_packed_length.argtypes = [vp]
     L.sb_set_state_packed.argtypes = [vp, ctypes.c_int, vp, dp, ctypes.c_double, ctypes.c_double,
@@ -518,9 +526,12 @@ def write_restart(path: str, p: SbParams, state: dict, deltat: float = 0.0):
                                   float(state["xofft"]), float(deltat)))
 
 
-def read_restart(path: str, p: SbParams = None):
-    """Reads a restart file (getfil).  Returns (state on p's grid, info), or
-    (None, info) without p."""
+def read_restart(path: str, p: SbParams = None, keep_vor: bool = False):
+    """Reads a restart file (getfil), mapping it on p's grid: kx/kz modes,
+    the y planes (as read, every other one, stacked copies or a cubic spline
+    in y) and the gam/Re rescaling (keep_vor: no vorticity rescaling for a
+    changed Re, as the Newton drivers read).  Returns (state on p's grid with
+    its offsets, info), or (None, info) without p."""
     info = SbRestartInfo()
     if p is None:
         _check(lib().sb_read_restart(str(path).encode(), None, None, None, None, None,
@@ -531,11 +542,12 @@ def read_restart(path: str, p: SbParams = None):
     phi = np.zeros_like(vor)
     u00 = np.zeros(p.my)
     w00 = np.zeros(p.my)
-    _check(lib().sb_read_restart(str(path).encode(), ctypes.byref(p), _dp(vor.view(np.float64)),
-                                 _dp(phi.view(np.float64)), _dp(u00), _dp(w00),
-                                 ctypes.byref(info)))
+    _check(lib().sb_read_restart_ex(str(path).encode(), ctypes.byref(p),
+                                    RESTART_KEEP_VOR if keep_vor else 0,
+                                    _dp(vor.view(np.float64)), _dp(phi.view(np.float64)),
+                                    _dp(u00), _dp(w00), ctypes.byref(info)))
     return {"vor": vor, "phi": phi, "u00": u00, "w00": w00, "time": info.time,
-            "xoffb": info.xoffb, "xofft": info.xofft}, info
+            "xoffb": info.run_xoffb, "xofft": info.run_xofft}, info
 
 
 def params_from_restart(info: SbRestartInfo, **overrides) -> SbParams:

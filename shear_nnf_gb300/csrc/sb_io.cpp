@@ -99,6 +99,39 @@ int io_fail(int code, const std::string &msg) {
   return code;
 }
 
+// Natural cubic spline through (x, y), N points: the second derivatives d2
+// with zero end curvature (cubic_spline, readwrite.f90:774-812, m = 1; the
+// tridiagonal sweep of the classic natural spline), and its value at c
+// (interpolate, readwrite.f90:1131-1155: bisection for the bracketing knots).
+void natural_spline(const double *x, const double *y, int N, double *d2) {
+  std::vector<double> u((size_t)N, 0.0);
+  d2[0] = 0.0;
+  d2[N - 1] = 0.0;
+  for (int i = 1; i < N - 1; i++) {
+    const double sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
+    const double p = sig * d2[i - 1] + 2.0;
+    d2[i] = (sig - 1.0) / p;
+    u[i] = (6.0 * ((y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1])) /
+                (x[i + 1] - x[i - 1]) -
+            sig * u[i - 1]) /
+           p;
+  }
+  for (int k = N - 2; k >= 1; k--) d2[k] = d2[k] * d2[k + 1] + u[k];
+}
+double spline_at(double c, const double *x, const double *y, const double *d2, int N) {
+  int klo = 0, khi = N - 1;
+  while (khi - klo > 1) {
+    const int k = (khi + klo) / 2;
+    if (x[k] > c)
+      khi = k;
+    else
+      klo = k;
+  }
+  const double h = x[khi] - x[klo];
+  const double a = (x[khi] - c) / h, b = (c - x[klo]) / h;
+  return a * y[klo] + b * y[khi] + ((a * a * a - a) * d2[klo] + (b * b * b - b) * d2[khi]) * (h * h) / 6.0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -159,8 +192,8 @@ int sb_write_restart(const char *path, const sb_params *p, const double *vor, co
   return 0;
 }
 
-int sb_read_restart(const char *path, const sb_params *p, double *vor, double *phi, double *u00,
-                    double *w00, sb_restart_info *info) {
+int sb_read_restart_ex(const char *path, const sb_params *p, int flags, double *vor, double *phi,
+                       double *u00, double *w00, sb_restart_info *info) {
   if (!path || !info) return io_fail(1, "null argument");
   memset(info, 0, sizeof(*info));
   File fh;
@@ -195,6 +228,8 @@ int sb_read_restart(const char *path, const sb_params *p, double *vor, double *p
   if (mye < 1 || mxe < 2 || mze < 1 || mye > 1 << 16 || mxe > 1 << 16 || mze > 1 << 16)
     return io_fail(8, "sizes out of range");
   if ((rc = need(8 * (size_t)mye, "y record"))) return rc;
+  std::vector<double> yfile((size_t)mye);
+  for (int j = 0; j < mye; j++) yfile[j] = get_f64(&r[8 * (size_t)j]);
   if (std::fabs(info->Ly + 2.0 * get_f64(&r[0])) > 1e-9 * std::fmax(1.0, info->Ly))
     return io_fail(8, "y(0) is not -Ly/2: broken file (getfil, readwrite.f90:146-149)");
   if ((rc = need(32, "offset record"))) return rc;
@@ -236,22 +271,54 @@ int sb_read_restart(const char *path, const sb_params *p, double *vor, double *p
   if (!vor || !phi || !u00 || !w00) return io_fail(1, "null state array");
   const int my = p->my, mx = 2 * (p->mgalx / 3), mz = 2 * (p->mgalz / 3) - 1, nkx = mx / 2;
   const int nz = (mz - 1) / 2;
-  if (my != mye)
-    return io_fail(9, "the file has my=" + std::to_string(mye) + ", the run my=" +
-                          std::to_string(my) + " (y interpolation is not supported)");
+  const double tiny = 1e-13;  // mod.f90:41
+  // x: the offsets follow a change of Lx; a doubled alp with half the x points
+  // keeps the even modes of the file (ihalf, readwrite.f90:152-171)
+  int iskip = 1;
+  double xoffb = info->xoffb, xofft = info->xofft;
+  if (info->mgalx != p->mgalx && mye != my)
+    return io_fail(9, "x and y grids both change: getfil does not interpolate in my at the same "
+                      "time (readwrite.f90:116-120)");
+  if (info->alp != p->alp) {
+    if ((int)((p->alp + 0.00001) / info->alp) == 2 && info->mgalx / p->mgalx == 2) {
+      xoffb = xoffb * info->alp / p->alp * 2.0;
+      xofft = xofft * info->alp / p->alp * 2.0;
+      iskip = 2;
+    } else {
+      xoffb = xoffb * info->alp / p->alp;
+      xofft = xofft * info->alp / p->alp;
+    }
+    if (mye != my) return io_fail(9, "alp and my both change (readwrite.f90:172-175)");
+  }
+  // y: the file's planes as they stand, every other one (my = mye/2), copies
+  // of the box stacked in y (my = 3 or 5 mye), or a cubic spline in y
+  const int ihalfy = (my == mye / 2) ? 1 : 0;
+  int ncopy = 0;
+  if (mye == my / 3) ncopy = 3;
+  else if (mye == my / 5) ncopy = 5;
+  const bool interp = (mye < my) && (ncopy == 0);
+  if (interp && std::fabs(info->Ly - p->Ly) >= tiny)
+    return io_fail(9, "interpolation in y needs the file's Ly (readwrite.f90:404-413)");
+  const int mxm = std::min(nkx, nkxe) , mzm = std::min(mz, mze);
+  if (iskip == 2 && (mxm - 1) * 2 >= nkxe) return io_fail(9, "ihalf: not enough kx modes in the file");
   memset(vor, 0, sizeof(double) * 2 * (size_t)my * nkx * mz);
   memset(phi, 0, sizeof(double) * 2 * (size_t)my * nkx * mz);
-  for (int j = 0; j < my; j++) {
-    u00[j] = m00[j];
-    w00[j] = m00[(size_t)mye + j];
+  for (int j = 0; j < my; j++) u00[j] = w00[j] = 0.0;
+  const int mym = std::min(my, mye);
+  for (int j = 0; j < (ihalfy ? my : mym); j++) {
+    const int je = ihalfy ? 2 * j : j;
+    u00[j] = m00[je];
+    w00[j] = m00[(size_t)mye + je];
   }
-  const int mxm = std::min(nkx, nkxe), mzm = std::min(mz, mze);
+  // modes (readwrite.f90:252-305): common kx (every iskip-th of the file),
+  // the klen lowest positive and negative kz
   const int klen = (mzm + 1) / 2, kini1 = mze - klen, kini2 = mz - klen;
-  for (int j = 0; j < my; j++) {
-    const unsigned char *pl = planes[j].data();
+  const int nplanes = ihalfy ? my : mym;
+  for (int j = 0; j < nplanes; j++) {
+    const unsigned char *pl = planes[ihalfy ? 2 * j : j].data();
     auto put = [&](int ke, int k) {
       for (int i = 0; i < mxm; i++) {
-        const unsigned char *e = pl + 32 * ((size_t)ke * nkxe + i);
+        const unsigned char *e = pl + 32 * ((size_t)ke * nkxe + (size_t)i * iskip);
         const size_t q = 2 * (((size_t)k * nkx + i) * my + j);
         vor[q] = get_f64(e);
         phi[q] = get_f64(e + 8);
@@ -271,7 +338,97 @@ int sb_read_restart(const char *path, const sb_params *p, double *vor, double *p
       phi[dst] = phi[src];
       phi[dst + 1] = -phi[src + 1];
     }
+  if (interp) {
+    // interp_y (readwrite.f90:707-771): per mode line the file's mye planes
+    // and the wrapped first plane at y = Ly/2 (times exp(-i kx xofft)), a
+    // natural cubic spline through them evaluated on the run's y grid
+    std::vector<double> ye((size_t)mye + 1);
+    for (int j = 0; j < mye; j++) ye[j] = yfile[j];
+    ye[mye] = p->Ly / 2.0;
+    std::vector<double> yrun((size_t)my);
+    const double dy = p->Ly / (double)my;
+    for (int j = 0; j < my; j++) yrun[j] = (double)j * dy - 0.5 * p->Ly;  // initcr.f90:486-488
+    const int N = mye + 1;
+    std::vector<double> re(N), im(N), d2r(N), d2i(N), src(2 * (size_t)my);
+    for (int k = 0; k < mz; k++)
+      for (int i = 0; i < nkx; i++) {
+        const double ph = -(p->alp * i) * xofft;
+        const double cr = std::cos(ph), ci = std::sin(ph);  // zexp(-xalp(i)*xofft)
+        for (double *f : {vor, phi}) {
+          double *line = f + 2 * ((size_t)k * nkx + i) * my;
+          for (int j = 0; j < mye; j++) {
+            re[j] = line[2 * j];
+            im[j] = line[2 * j + 1];
+          }
+          re[mye] = line[0] * cr - line[1] * ci;
+          im[mye] = line[0] * ci + line[1] * cr;
+          natural_spline(ye.data(), re.data(), N, d2r.data());
+          natural_spline(ye.data(), im.data(), N, d2i.data());
+          for (int j = 0; j < my; j++) {
+            src[2 * j] = spline_at(yrun[j], ye.data(), re.data(), d2r.data(), N);
+            src[2 * j + 1] = spline_at(yrun[j], ye.data(), im.data(), d2i.data(), N);
+          }
+          std::copy(src.begin(), src.end(), line);
+        }
+      }
+    for (double *f : {u00, w00}) {
+      for (int j = 0; j < mye; j++) re[j] = f[j];
+      re[mye] = f[0];
+      natural_spline(ye.data(), re.data(), N, d2r.data());
+      for (int j = 0; j < my; j++) src[j] = spline_at(yrun[j], ye.data(), re.data(), d2r.data(), N);
+      std::copy(src.begin(), src.begin() + my, f);
+    }
+  } else if (mye < my && ncopy > 0) {
+    // ncopy_y (readwrite.f90:449-489): the box stacked ncopy times in y, copy
+    // inc shifted by exp(-i kx xofft inc); the offsets grow by ncopy
+    for (int k = 0; k < mz; k++)
+      for (int i = 0; i < nkx; i++)
+        for (int inc = 1; inc < ncopy; inc++) {
+          const double ph = -(p->alp * i) * xofft * inc;
+          const double cr = std::cos(ph), ci = std::sin(ph);
+          for (double *f : {vor, phi}) {
+            double *line = f + 2 * ((size_t)k * nkx + i) * my;
+            for (int j = 0; j < mye; j++) {
+              const double a = line[2 * j], b = line[2 * j + 1];
+              line[2 * (j + mye * inc)] = a * cr - b * ci;
+              line[2 * (j + mye * inc) + 1] = a * ci + b * cr;
+            }
+          }
+        }
+    xofft *= (double)ncopy;
+    xoffb *= (double)ncopy;
+    for (int inc = 1; inc < ncopy; inc++)
+      for (int j = 0; j < mye; j++) {
+        u00[j + mye * inc] = u00[j];
+        w00[j + mye * inc] = w00[j];
+      }
+  }
+  // velocity scale of a changed Lz, vorticity scale of a changed Re
+  // (readwrite.f90:427-442; the Newton drivers keep the vorticity as read)
+  const size_t nf = 2 * (size_t)my * nkx * mz;
+  if (std::fabs(info->gam - p->gam) > tiny) {
+    const double f = info->gam / p->gam;
+    for (int j = 0; j < my; j++) {
+      u00[j] *= f;
+      w00[j] *= f;
+    }
+    for (size_t q = 0; q < nf; q++) phi[q] *= p->gam / info->gam;
+    if (!p->les)
+      for (size_t q = 0; q < nf; q++) vor[q] *= f * std::sqrt(p->Re / info->Re);
+  } else if (std::fabs(info->Re - p->Re) > tiny && !p->les && !(flags & SB_RESTART_KEEP_VOR)) {
+    for (size_t q = 0; q < nf; q++) vor[q] *= (info->gam / p->gam) * std::sqrt(p->Re / info->Re);
+  }
+  info->run_xoffb = xoffb;
+  info->run_xofft = xofft;
+  info->ymap = interp ? 3 : (ncopy > 0 && mye < my ? 2 : (ihalfy ? 1 : 0));
+  info->ncopy = ncopy > 0 && mye < my ? ncopy : 0;
+  info->xskip = iskip;
   return 0;
+}
+
+int sb_read_restart(const char *path, const sb_params *p, double *vor, double *phi, double *u00,
+                    double *w00, sb_restart_info *info) {
+  return sb_read_restart_ex(path, p, 0, vor, phi, u00, w00, info);
 }
 
 }  // extern "C"

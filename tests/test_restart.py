@@ -1,6 +1,8 @@
 """Restart files in the reference's binary layout (escru / getfil,
 readwrite.f90:72-447,1336-1398): record structure, round trip, mapping onto a
-different x/z grid, header-only reads and malformed files.  Host code only."""
+different x/z grid, the y mappings of getfil (every other plane, stacked
+copies, cubic spline), the gam/Re rescaling, header-only reads and malformed
+files.  Host code only."""
 import struct
 
 import numpy as np
@@ -147,8 +149,149 @@ def test_malformed_and_unsupported(tmp_path):
     open(bad, "wb").write(data[:300])
     with pytest.raises(sb.ShearBoxError):
         sb.read_restart(bad, p)
-    q = sb.make_params(**box_params(64, 48, 32, 1000.0))
-    with pytest.raises(sb.ShearBoxError, match="my="):
-        sb.read_restart(f, q)
+    # x and y together (readwrite.f90:116-120), alp and my together (:172-175),
+    # a spline in y with another Ly (:404-413)
+    for q in (sb.make_params(**box_params(96, 48, 32, 1000.0)),
+              sb.make_params(**dict(box_params(64, 48, 32, 1000.0), alp=0.7)),
+              sb.make_params(**dict(box_params(64, 48, 32, 1000.0), Ly=5.0))):
+        with pytest.raises(sb.ShearBoxError, match="error 9"):
+            sb.read_restart(f, q)
     with pytest.raises(sb.ShearBoxError):
         sb.read_restart(tmp_path / "missing.bin", p)
+
+
+def _spline_ref(x, y, c):
+    """A numpy restatement of the natural cubic spline of getfil's interp_y
+    (cubic_spline + interpolate, readwrite.f90:774-812,1131-1155)."""
+    N = len(x)
+    d2, u = np.zeros(N), np.zeros(N)
+    for i in range(1, N - 1):
+        sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1])
+        pp = sig * d2[i - 1] + 2.0
+        d2[i] = (sig - 1.0) / pp
+        u[i] = (6.0 * ((y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1]))
+                / (x[i + 1] - x[i - 1]) - sig * u[i - 1]) / pp
+    for k in range(N - 2, 0, -1):
+        d2[k] = d2[k] * d2[k + 1] + u[k]
+    out = []
+    for cc in c:
+        klo, khi = 0, N - 1
+        while khi - klo > 1:
+            k = (khi + klo) // 2
+            if x[k] > cc:
+                khi = k
+            else:
+                klo = k
+        h = x[khi] - x[klo]
+        a, b = (x[khi] - cc) / h, (cc - x[klo]) / h
+        out.append(a * y[klo] + b * y[khi] + ((a * a * a - a) * d2[klo] + (b * b * b - b) * d2[khi])
+                   * (h * h) / 6.0)
+    return np.array(out)
+
+
+def test_y_spline_interpolation(tmp_path):
+    """my 32 -> 48 (not a 3x or 5x stack): per mode line a natural cubic spline
+    through the file's planes and the wrapped first plane at Ly/2 (shifted by
+    exp(-i kx xofft)), on the run's y grid; the same for u00, w00."""
+    p = sb.make_params(**box_params(64, 32, 32, 1000.0))
+    q = sb.make_params(**box_params(64, 48, 32, 1000.0))
+    st = _conj_state(sb.seed_state(p, 9), p)
+    st.update(xoffb=-0.3, xofft=0.3)
+    f = tmp_path / "s.bin"
+    sb.write_restart(f, p, st)
+    got, info = sb.read_restart(f, q)
+    assert info.ymap == 3 and (got["xoffb"], got["xofft"]) == (-0.3, 0.3)
+    ye = np.append(np.arange(32) * (p.Ly / 32) - p.Ly / 2, p.Ly / 2)
+    y = np.arange(48) * (q.Ly / 48) - q.Ly / 2
+    for (k, i) in [(0, 1), (2, 3), (5, 0), (17, 7)]:
+        shp = np.exp(-1j * (q.alp * i) * 0.3)
+        for key in ("vor", "phi"):
+            line = st[key][k, i]
+            ext = np.append(line, line[0] * shp)
+            want = _spline_ref(ye, ext.real, y) + 1j * _spline_ref(ye, ext.imag, y)
+            np.testing.assert_allclose(got[key][k, i], want, rtol=0, atol=1e-14 * np.abs(line).max())
+    np.testing.assert_allclose(got["u00"], _spline_ref(ye, np.append(st["u00"], st["u00"][0]), y),
+                               rtol=0, atol=1e-14 * np.abs(st["u00"]).max())
+    # a line smooth in y is reproduced to the spline's accuracy (largest next
+    # to the ends, where the natural spline's zero curvature is imposed)
+    p2 = sb.make_params(**box_params(64, 32, 32, 1000.0))
+    st2 = {key: np.zeros_like(st[key]) for key in ("vor", "phi")}
+    y32 = np.arange(32) * (p2.Ly / 32) - p2.Ly / 2
+    st2["vor"][1, 0] = np.exp(1j * 2 * np.pi / p2.Ly * y32)  # one y wave, kx = 0
+    st2["vor"][sb.sizes(p2)["mz"] - 1, 0] = np.conj(st2["vor"][1, 0])
+    st2.update(phi=st2["phi"], u00=np.cos(2 * np.pi / p2.Ly * y32), w00=np.zeros(32), time=0.0,
+               xoffb=0.0, xofft=0.0)
+    f2 = tmp_path / "s2.bin"
+    sb.write_restart(f2, p2, st2)
+    got2, _ = sb.read_restart(f2, q)
+    err = np.abs(got2["vor"][1, 0] - np.exp(1j * 2 * np.pi / q.Ly * y))
+    assert err.max() < 2e-3 and err[8:40].max() < 1e-4
+    assert np.abs(got2["u00"] - np.cos(2 * np.pi / q.Ly * y)).max() < 2e-3
+
+
+@pytest.mark.parametrize("ncopy", [3, 5])
+def test_y_stack_copies(tmp_path, ncopy):
+    """my = 3 or 5 x the file's (ncopy_y, readwrite.f90:449-489): the box
+    stacked in y, copy n times exp(-i kx xofft n), offsets times ncopy."""
+    p = sb.make_params(**box_params(64, 32, 32, 1000.0))
+    q = sb.make_params(**dict(box_params(64, 32 * ncopy, 32, 1000.0), Ly=p.Ly * ncopy))
+    st = _conj_state(sb.seed_state(p, 5), p)
+    st.update(xoffb=-0.2, xofft=0.2)
+    f = tmp_path / "c.bin"
+    sb.write_restart(f, p, st)
+    got, info = sb.read_restart(f, q)
+    assert info.ymap == 2 and info.ncopy == ncopy
+    assert np.isclose(got["xofft"], 0.2 * ncopy) and np.isclose(got["xoffb"], -0.2 * ncopy)
+    kx = q.alp * np.arange(sb.sizes(q)["nkx"])
+    for n in range(ncopy):
+        ph = np.exp(-1j * kx * 0.2 * n)[None, :, None]
+        for key in ("vor", "phi"):
+            np.testing.assert_allclose(got[key][:, :, 32 * n:32 * (n + 1)], st[key] * ph,
+                                       rtol=0, atol=1e-15 * np.abs(st[key]).max())
+        np.testing.assert_array_equal(got["u00"][32 * n:32 * (n + 1)], st["u00"])
+
+
+def test_y_half_and_x_half(tmp_path):
+    """my = file my / 2 keeps every other plane (ihalfy); a doubled alp with
+    half the x points keeps the even kx modes and the offsets (ihalf,
+    readwrite.f90:152-171,229-239)."""
+    p = sb.make_params(**box_params(64, 32, 32, 1000.0))
+    st = _conj_state(sb.seed_state(p, 6), p)
+    st.update(xoffb=-0.4, xofft=0.4)
+    f = tmp_path / "h.bin"
+    sb.write_restart(f, p, st)
+    qy = sb.make_params(**box_params(64, 16, 32, 1000.0))
+    got, info = sb.read_restart(f, qy)
+    assert info.ymap == 1
+    np.testing.assert_array_equal(got["vor"], st["vor"][:, :, ::2])
+    np.testing.assert_array_equal(got["w00"], st["w00"][::2])
+    qx = sb.make_params(**dict(box_params(32, 32, 32, 1000.0), alp=2 * p.alp))
+    got, info = sb.read_restart(f, qx)
+    nk = sb.sizes(qx)["nkx"]
+    assert info.xskip == 2 and (got["xoffb"], got["xofft"]) == (-0.4, 0.4)
+    klen = (sb.sizes(qx)["mz"] + 1) // 2
+    np.testing.assert_array_equal(got["phi"][:klen, :nk], st["phi"][:klen, 0:2 * nk:2])
+
+
+def test_rescaling_of_gam_and_re(tmp_path):
+    """getfil's rescaling (readwrite.f90:427-442): a changed gam scales u00,
+    w00 by gam_file/gam, phi by gam/gam_file and vor by (gam_file/gam)
+    sqrt(Re/Re_file); a changed Re alone scales vor by sqrt(Re/Re_file)
+    unless the vorticity is kept (the Newton drivers), and never with LES."""
+    p = sb.make_params(**box_params(64, 32, 32, 1000.0))
+    st = _conj_state(sb.seed_state(p, 8), p)
+    f = tmp_path / "r.bin"
+    sb.write_restart(f, p, st)
+    q = sb.make_params(**dict(box_params(64, 32, 32, 2000.0)))
+    got, _ = sb.read_restart(f, q)
+    np.testing.assert_allclose(got["vor"], st["vor"] * np.sqrt(q.Re / p.Re), rtol=1e-15)
+    np.testing.assert_array_equal(got["phi"], st["phi"])
+    got, _ = sb.read_restart(f, q, keep_vor=True)
+    np.testing.assert_array_equal(got["vor"], st["vor"])
+    got, _ = sb.read_restart(f, sb.make_params(**dict(box_params(64, 32, 32, 2000.0), les=1)))
+    np.testing.assert_array_equal(got["vor"], st["vor"])
+    qg = sb.make_params(**dict(box_params(64, 32, 32, 1000.0), gam=2.0))
+    got, _ = sb.read_restart(f, qg)
+    np.testing.assert_allclose(got["u00"], st["u00"] * 0.5, rtol=1e-15)
+    np.testing.assert_allclose(got["phi"], st["phi"] * 2.0, rtol=1e-15)
+    np.testing.assert_allclose(got["vor"], st["vor"] * 0.5, rtol=1e-15)
