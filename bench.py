@@ -535,10 +535,20 @@ def run_ours(args):
         pp.update(temperature=1, fkappa=LZ ** 2 / REZ / 0.7, bym=1.0, gbeta=0.5)
     p = sb.make_params(**pp)
     st0 = sb.seed_state(p, 3 + rank)
-    box = sb.ShearBox(p)
-    box.set_state(st0)
+    nbox = args.boxes if args.lite else 1
+    box = sb.ShearBox(p, batch=nbox, precision=sb.SB_MIXED if args.mixed else sb.SB_FP64)
+    states = [st0] + [sb.seed_state(p, 1000 * rank + m) for m in range(1, nbox)]
+    rez = np.exp(np.random.default_rng(1234 + rank).uniform(np.log(500.0), np.log(2000.0), nbox))
+
+    def load():
+        for m in range(nbox):
+            box.set_state(states[m], m)
+            if nbox > 1:
+                box.set_re(m, rez[m] / LZ ** 2)
+
+    load()
     tuning = box.autotune()  # plane-stage tiles for this grid (untimed set-up)
-    box.set_state(st0)
+    load()
     stream = torch.cuda.ExternalStream(box.stream)
     # warm-up
     box.step(max(args.warmup, 1))
@@ -571,7 +581,8 @@ def run_ours(args):
                               "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
                               "ms_per_step": ms_max / args.steps, "lite": True,
                               "config": config({"grid": list(GRID), "tuning": tuning,
-                                                "variant": args.variant}),
+                                                "variant": args.variant, "boxes": nbox,
+                                                "precision": "mixed" if args.mixed else "fp64"}),
                               "gpu_launches": launches}))
         return
     # dominant kernel alone: plane stage 2 (x transforms + u x omega)
@@ -782,9 +793,14 @@ def main():
                     help="profiling only: time the steps, skip e2e / CPU / per-kernel legs")
     ap.add_argument("--variant", default="plain", choices=["plain", "les", "temperature"],
                     help="profiling only (with --lite): step the LES or the temperature box")
+    ap.add_argument("--boxes", type=int, default=1,
+                    help="profiling only (with --lite): boxes in the batch (Re_z log-uniform "
+                         "in [500, 2000] beyond the first)")
+    ap.add_argument("--mixed", action="store_true",
+                    help="profiling only (with --lite): the FP32-mixed precision form")
     args = ap.parse_args()
-    if args.variant != "plain" and not args.lite:
-        ap.error("--variant is for profiling runs (--lite)")
+    if (args.variant != "plain" or args.boxes != 1 or args.mixed) and not args.lite:
+        ap.error("--variant, --boxes and --mixed are for profiling runs (--lite)")
     global GRID
     GRID = GRIDS[args.grid]
     if args.warmup < 3:
