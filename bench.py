@@ -414,7 +414,7 @@ def newton_search_leg(sb, torch, dist, ws, rank, args, T=20.0, s_star=0.37, pert
     pk = nw.Packing(p, *sca)
     n = pk.n
     ks = kr.KSpace(n + 1, 1400)
-    res64 = kr.DevPeriodMap(p, T, batch=1, sca=sca)
+    res64 = kr.DevPeriodMap(p, T, batch=1, sca=sca, autotune=True)
     xs, rhs, x = ks.alloc(1), ks.alloc(1), ks.alloc(1)
     ks.set(xs, pk.pack(sb.seed_state(p, 77 + rank)))
     res64(ks, [xs], [xs])
@@ -423,7 +423,7 @@ def newton_search_leg(sb, torch, dist, ws, rank, args, T=20.0, s_star=0.37, pert
     xsv = ks.get(xs, 0, n)
     d = np.random.default_rng(15 + rank).standard_normal(n)
     x0v = np.concatenate([xsv + pert * np.linalg.norm(xsv) / np.linalg.norm(d) * d, [0.0]])
-    pm32 = kr.DevPeriodMap(p, T, batch=17, precision=sb.SB_MIXED, sca=sca)
+    pm32 = kr.DevPeriodMap(p, T, batch=17, precision=sb.SB_MIXED, sca=sca, autotune=True)
     cfgs = (("unbatched_fp64", dict(jac=res64, block=1, k=50, eps=1e-7, base=False, recycle=0)),
             ("batched_mixed", dict(jac=pm32, block=16, k=3, eps=1e-3, base=True, recycle=15)))
     out = {"grid": [96, 48, 48], "re_z": 1200.0, "period_T": T, "unknowns": n + 1,
@@ -447,7 +447,7 @@ def newton_search_leg(sb, torch, dist, ws, rank, args, T=20.0, s_star=0.37, pert
     a, b = out["unbatched_fp64"], out["batched_mixed"]
     out["speedup_batched_vs_unbatched_wall"] = a["seconds"] / b["seconds"]
     # Floquet analysis at the point the batched search converged to
-    pmf = kr.DevPeriodMap(p, T, batch=33, precision=sb.SB_MIXED, sca=sca)
+    pmf = kr.DevPeriodMap(p, T, batch=33, precision=sb.SB_MIXED, sca=sca, autotune=True)
     J = kr.DevJacobian(pmf, ks, x, shift=(b["shift"], 0.0), eps_jacobi=1e-3, order=1,
                        base_in_batch=True)
     t0 = time.perf_counter()
@@ -484,7 +484,7 @@ def newton_leg(sb, torch, dist, ws, rank, args, nper=32, T=20.0):
     pk = nw.Packing(p, *nw.Packing.reference_scales(p))
     x0 = pk.pack(sb.seed_state(p, 77 + rank))
     D = np.random.default_rng(5 + rank).standard_normal((pk.n, nper))
-    pm64 = nw.PeriodMap(p, T, batch=1, chunk=256)
+    pm64 = nw.PeriodMap(p, T, batch=1, chunk=256, autotune=True)
     J64 = nw.Jacobian(pm64, pk, x0, eps_jacobi=1e-7)
     J64.gx0  # the base integration, untimed
     steps_T = pm64.last_steps[0]
@@ -499,7 +499,7 @@ def newton_leg(sb, torch, dist, ws, rank, args, nper=32, T=20.0):
                               "seconds": t64}}
     for key, central, eps, members in (("batched", True, 3e-3, 2 * nper),
                                        ("batched_forward", False, 1e-3, nper + 1)):
-        pm = nw.PeriodMap(p, T, batch=members, precision=sb.SB_MIXED, chunk=256)
+        pm = nw.PeriodMap(p, T, batch=members, precision=sb.SB_MIXED, chunk=256, autotune=True)
         J = nw.Jacobian(pm, pk, x0, eps_jacobi=eps, central=central, base_in_batch=not central)
         barrier(dist)
         t0 = time.perf_counter()

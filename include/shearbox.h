@@ -267,13 +267,19 @@ int sb_launch_stage(sb_handle *h, int stage, int rk, int count);
  * order, each [my][mgalz][mgalx] doubles.  The state is not changed. */
 int sb_physical_fields(sb_handle *h, int member, unsigned mask, double *out);
 
-/* Autotuner of the plane stages (no counterpart in the reference): times the
+/* Autotuner of the step's tiles (no counterpart in the reference): times the
  * tile candidates of plane stages 1-3 on the handle's current state -- kx
  * columns per block of stages 1 and 3 (4 or 8), threads per block of stage 2
- * (the default or twice it) -- keeps the fastest and re-captures the step
- * graph.  choice (may be NULL) receives cb1, cb3, t2.  The state itself is not
- * changed; call it after sb_set_state and before sb_step. */
+ * (the default or twice it) -- and the y-line tile, 1, 2 or 3 warps per line
+ * solve (segments of the banded rows solved at once; each choice has its own
+ * factor tables), keeps the fastest and re-captures the step graph.  choice
+ * (may be NULL) receives cb1, cb3, t2; sb_get_tuning gives cb1, cb3, t2 and
+ * the warps per line solve.  The state itself is not changed; call it after
+ * sb_set_state and before sb_step.  sb_set_line_segments sets the warps per
+ * line solve directly (1..3; my - 3 >= 6 rows per segment). */
 int sb_autotune(sb_handle *h, int *choice);
+int sb_get_tuning(sb_handle *h, int *out);
+int sb_set_line_segments(sb_handle *h, int nseg);
 int sb_fp64_peak(sb_handle *h, double *tflops);
 
 /* Standalone y-line operators on device-resident complex lines.  Line data is

@@ -14,10 +14,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libshearbox.so")
-# (source, extra flags): sb_kernels.cu and sb_yline.cu are compiled twice, their
-# FP64 and FP32-mixed instantiations in parallel
+# (source, extra flags): sb_kernels.cu is compiled twice (its FP64 and
+# FP32-mixed instantiations in parallel), sb_yline.cu six times (1, 2 or 3
+# warps per line solve, each precision)
 UNITS = [("sb_kernels.cu", ["-DSB_FLOAT_TU=0"]), ("sb_kernels.cu", ["-DSB_FLOAT_TU=1"]),
-         ("sb_yline.cu", ["-DSB_FLOAT_TU=0"]), ("sb_yline.cu", ["-DSB_FLOAT_TU=1"]),
+         # the y-line kernels once per (warps per line solve, precision)
+         *[("sb_yline.cu", [f"-DSB_FLOAT_TU={f}", f"-DSB_KSEG={k}"]) for k in (1, 2, 3)
+           for f in (0, 1)],
+         ("sb_box.cu", []),
          ("sb_ops.cu", []), ("sb_noalloc.cu", []), ("sb_api.cu", []), ("sb_krylov.cu", []),
          # host set-up (coefficients, factorisations, the seeded field) without
          # fused multiply-adds: the same bits on x86 and Arm hosts

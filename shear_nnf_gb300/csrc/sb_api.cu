@@ -62,6 +62,11 @@ struct sb_handle {
   cudaEvent_t ev_c0 = nullptr, ev_c1 = nullptr;
   cudaGraphExec_t step_exec = nullptr;
   std::vector<void *> allocs;
+  // the factor tables of the y-line solves depend on the segment plan: kept
+  // apart so that a new plan (sb_set_line_segments, the autotuner) can
+  // replace them
+  std::vector<void *> line_allocs;
+  std::vector<void *> *alloc_to = nullptr;
   double *d_pen = nullptr;  // staging buffers, one pencil-layout field each
   double *d_pen2 = nullptr;
   // pinned host staging of the small per-call values (mean profiles, time and
@@ -86,7 +91,7 @@ static int dalloc(sb_handle *h, double **p, size_t n) {
   cudaError_t e = cudaMalloc(&q, sizeof(double) * (n ? n : 1));
   if (e != cudaSuccess) return fail(4, "cudaMalloc(%zu doubles): %s", n, cudaGetErrorString(e));
   cudaMemset(q, 0, sizeof(double) * (n ? n : 1));
-  h->allocs.push_back(q);
+  (h->alloc_to ? *h->alloc_to : h->allocs).push_back(q);
   *p = (double *)q;
   return 0;
 }
@@ -173,6 +178,103 @@ static int upload_uniform(sb_handle *h, Fac *F, const double a[7], int n) {
   F->stride = 0;
   return 0;
 }
+
+// The factor tables of the y-line solves for a segment plan of nseg warps per
+// line: d/dy and d2/dy2 (and the y-filter), each the same for every line, and
+// the Helmholtz operator (rh2 - k^2 pr2) per (kx, kz) line (lapcdy,
+// diffy_shear_hepta.f90:466-525; line (0,0) is never solved and gets a
+// harmless k^2 = 1).  Replaces the tables of an earlier plan.
+static int build_line_tables(sb_handle *h, int nseg) {
+  Grid &g = h->g;
+  Bufs &bf = h->bf;
+  if (!line_segments_supported(nseg)) return fail(1, "%d warps per line solve not available", nseg);
+  if ((g.my - 3) / nseg < 6) return fail(1, "my=%d too short for %d segments", g.my, nseg);
+  sbh::SegPlan plan0;
+  sbh::seg_plan(g.my, nseg, &plan0);
+  g.nseg = plan0.nseg;
+  for (int q = 0; q < plan0.nseg; q++) {
+    g.slo[q] = plan0.lo[q];
+    g.shi[q] = plan0.hi[q];
+  }
+  if (h->st) cudaStreamSynchronize(h->st);
+  for (void *q : h->line_allocs) cudaFree(q);
+  h->line_allocs.clear();
+  h->alloc_to = &h->line_allocs;
+  struct Reset {
+    sb_handle *h;
+    ~Reset() { h->alloc_to = nullptr; }
+  } reset{h};
+  sbh::Coeffs co;
+  sbh::compact_coeffs(&co);
+  double flhs[7], frhs[9];
+  sbh::filter_coeffs(flhs, frhs);
+  const double *rh2 = g.rh2;
+  const int nl = g.nkx * g.mz;
+  int rc;
+  if ((rc = upload_uniform(h, &bf.d1, co.pr1, g.my)) ||
+      (rc = upload_uniform(h, &bf.d2, co.pr2, g.my)) ||
+      (g.ydeal == 3 && (rc = upload_uniform(h, &bf.flt, flhs, g.my))))
+    return rc;
+  {
+    const size_t n = g.my;
+    std::vector<double> La(n * nl), Lb(n * nl), Lc(n * nl), Dm(n * nl), Dd(n * nl), e(n * nl),
+        f(n * nl), gg(n * nl), sums(10 * (size_t)nl);
+    std::vector<double> hf[3], hb[3], ef(9 * (size_t)g.nseg * nl), rows(16 * n * nl);
+    for (int t = 0; t < 3; t++) {
+      hf[t].assign(n * nl, 0.0);
+      hb[t].assign(n * nl, 0.0);
+    }
+    sbh::SegPlan plan;
+    sbh::seg_plan(g.my, g.nseg, &plan);
+    sbh::SegFac sfac;
+    sbh::BaseFac bfac;
+    for (int k = 0; k < g.mz; k++)
+      for (int i = 0; i < g.nkx; i++) {
+        const size_t line = (size_t)k * g.nkx + i;
+        int kzs = (k <= g.nz) ? k : k - g.mz;
+        double gz = g.gam * kzs, a = g.alp * i;
+        double k2 = (i == 0 && k == 0) ? 1.0 : gz * gz + a * a;
+        double lap[7];
+        for (int d = 0; d < 7; d++) lap[d] = rh2[d] - k2 * co.pr2[d];
+        sbh::base_factor(lap, g.my, &bfac);
+        for (size_t q = 0; q < n; q++) {
+          La[q * nl + line] = bfac.La[q];
+          Lb[q * nl + line] = bfac.Lb[q];
+          Lc[q * nl + line] = bfac.Lc[q];
+          Dm[q * nl + line] = bfac.Ddm1[q];
+          Dd[q * nl + line] = bfac.Dd[q];
+          e[q * nl + line] = bfac.e[q];
+          f[q * nl + line] = bfac.f[q];
+          gg[q * nl + line] = bfac.g[q];
+        }
+        for (int q = 0; q < 6; q++) sums[(size_t)q * nl + line] = bfac.sums[q];
+        for (int q = 0; q < 4; q++) sums[(size_t)(6 + q) * nl + line] = lap[3 + q];
+        sbh::seg_factor(bfac, g.my, plan, &sfac);
+        for (int t = 0; t < 3; t++)
+          for (size_t q = 0; q < n; q++) {
+            hf[t][q * nl + line] = sfac.hf[t][q];
+            hb[t][q * nl + line] = sfac.hb[t][q];
+          }
+        for (size_t q = 0; q < sfac.ef.size(); q++) ef[q * nl + line] = sfac.ef[q];
+        pack_rows(bfac, sfac, n, nl, line, rows);
+      }
+    Fac &H = bf.hz;
+    if ((rc = upload(h, &H.La, La)) || (rc = upload(h, &H.Lb, Lb)) || (rc = upload(h, &H.Lc, Lc)) ||
+        (rc = upload(h, &H.Ddm1, Dm)) || (rc = upload(h, &H.Dd, Dd)) || (rc = upload(h, &H.e, e)) ||
+        (rc = upload(h, &H.f, f)) || (rc = upload(h, &H.g, gg)) || (rc = upload(h, &H.sums, sums)) ||
+        (rc = upload(h, &H.hf[0], hf[0])) || (rc = upload(h, &H.hf[1], hf[1])) ||
+        (rc = upload(h, &H.hf[2], hf[2])) || (rc = upload(h, &H.hb[0], hb[0])) ||
+        (rc = upload(h, &H.hb[1], hb[1])) || (rc = upload(h, &H.hb[2], hb[2])) ||
+        (rc = upload(h, &H.ef, ef)) || (rc = upload(h, &H.rows, rows))) {
+      return rc;
+    }
+    H.stride = nl;
+  }
+  if (prepare_line(g) != cudaSuccess)
+    return fail(3, "line kernel attributes: %s", cudaGetErrorString(cudaGetLastError()));
+  return 0;
+}
+
 
 static void member_defaults(const sb_params *p, const Grid &g, double Re, Member *m) {
   memset(m, 0, sizeof(Member));
@@ -534,72 +636,14 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
       (rc = upload_f(&bf.twzf, tw(g.mgalz))) || (rc = upload_f(&bf.twxf, tw(g.mgalx))) ||
       (rc = upload_f(&bf.kinvf, kinv)) ||
       (rc = upload(h, &bf.kinv, kinv)) || (rc = upload(h, &bf.ginv, ginv)) ||
-      (rc = upload_uniform(h, &bf.d1, co.pr1, g.my)) ||
-      (rc = upload_uniform(h, &bf.d2, co.pr2, g.my)) ||
-      (g.ydeal == 3 && (rc = upload_uniform(h, &bf.flt, flhs, g.my))) ||
       ((g.ydeal == 1 || g.ydeal == 2) &&
        ((rc = upload(h, &bf.twy, gtw(g.my))) || (rc = upload_f(&bf.twyf, tw(g.my)))))) {
     sb_destroy(h);
     return rc;
   }
-  {
-    // Helmholtz (rh2 - k^2 pr2), one base factorisation per (kx, kz) line
-    // (lapcdy, diffy_shear_hepta.f90:466-525); line (0,0) is never solved and
-    // gets a harmless k^2 = 1
-    const size_t n = g.my;
-    std::vector<double> La(n * nl), Lb(n * nl), Lc(n * nl), Dm(n * nl), Dd(n * nl), e(n * nl),
-        f(n * nl), gg(n * nl), sums(10 * (size_t)nl);
-    std::vector<double> hf[3], hb[3], ef(9 * (size_t)g.nseg * nl), rows(16 * n * nl);
-    for (int t = 0; t < 3; t++) {
-      hf[t].assign(n * nl, 0.0);
-      hb[t].assign(n * nl, 0.0);
-    }
-    sbh::SegPlan plan;
-    sbh::seg_plan(g.my, g.nseg, &plan);
-    sbh::SegFac sfac;
-    sbh::BaseFac bfac;
-    for (int k = 0; k < g.mz; k++)
-      for (int i = 0; i < g.nkx; i++) {
-        const size_t line = (size_t)k * g.nkx + i;
-        int kzs = (k <= g.nz) ? k : k - g.mz;
-        double gz = g.gam * kzs, a = g.alp * i;
-        double k2 = (i == 0 && k == 0) ? 1.0 : gz * gz + a * a;
-        double lap[7];
-        for (int d = 0; d < 7; d++) lap[d] = rh2[d] - k2 * co.pr2[d];
-        sbh::base_factor(lap, g.my, &bfac);
-        for (size_t q = 0; q < n; q++) {
-          La[q * nl + line] = bfac.La[q];
-          Lb[q * nl + line] = bfac.Lb[q];
-          Lc[q * nl + line] = bfac.Lc[q];
-          Dm[q * nl + line] = bfac.Ddm1[q];
-          Dd[q * nl + line] = bfac.Dd[q];
-          e[q * nl + line] = bfac.e[q];
-          f[q * nl + line] = bfac.f[q];
-          gg[q * nl + line] = bfac.g[q];
-        }
-        for (int q = 0; q < 6; q++) sums[(size_t)q * nl + line] = bfac.sums[q];
-        for (int q = 0; q < 4; q++) sums[(size_t)(6 + q) * nl + line] = lap[3 + q];
-        sbh::seg_factor(bfac, g.my, plan, &sfac);
-        for (int t = 0; t < 3; t++)
-          for (size_t q = 0; q < n; q++) {
-            hf[t][q * nl + line] = sfac.hf[t][q];
-            hb[t][q * nl + line] = sfac.hb[t][q];
-          }
-        for (size_t q = 0; q < sfac.ef.size(); q++) ef[q * nl + line] = sfac.ef[q];
-        pack_rows(bfac, sfac, n, nl, line, rows);
-      }
-    Fac &H = bf.hz;
-    if ((rc = upload(h, &H.La, La)) || (rc = upload(h, &H.Lb, Lb)) || (rc = upload(h, &H.Lc, Lc)) ||
-        (rc = upload(h, &H.Ddm1, Dm)) || (rc = upload(h, &H.Dd, Dd)) || (rc = upload(h, &H.e, e)) ||
-        (rc = upload(h, &H.f, f)) || (rc = upload(h, &H.g, gg)) || (rc = upload(h, &H.sums, sums)) ||
-        (rc = upload(h, &H.hf[0], hf[0])) || (rc = upload(h, &H.hf[1], hf[1])) ||
-        (rc = upload(h, &H.hf[2], hf[2])) || (rc = upload(h, &H.hb[0], hb[0])) ||
-        (rc = upload(h, &H.hb[1], hb[1])) || (rc = upload(h, &H.hb[2], hb[2])) ||
-        (rc = upload(h, &H.ef, ef)) || (rc = upload(h, &H.rows, rows))) {
-      sb_destroy(h);
-      return rc;
-    }
-    H.stride = nl;
+  if ((rc = build_line_tables(h, g.nseg))) {
+    sb_destroy(h);
+    return rc;
   }
   h->mem_init.resize(B);
   for (size_t b = 0; b < B; b++) member_defaults(p, g, p->Re, &h->mem_init[b]);
@@ -627,6 +671,7 @@ int sb_destroy(sb_handle *h) {
   if (h->st) cudaStreamSynchronize(h->st);
   if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
   for (void *q : h->allocs) cudaFree(q);
+  for (void *q : h->line_allocs) cudaFree(q);
   if (h->hs) cudaFreeHost(h->hs);
   if (h->st) cudaStreamDestroy(h->st);
   if (h->side) cudaStreamDestroy(h->side);
@@ -1006,6 +1051,59 @@ int sb_launch_stage(sb_handle *h, int stage, int rk, int count) {
   return 0;
 }
 
+// A copy of what a step changes and the next step reads: the state fields,
+// the mean lines, the members' scalars (and the temperature).
+struct Snapshot {
+  std::vector<std::pair<void *, size_t>> parts;  // (device field, bytes)
+  std::vector<void *> copies;
+  int take(sb_handle *h) {
+    const Grid &g = h->g;
+    const size_t es = g.prec ? sizeof(float) : sizeof(double);
+    const size_t Fb = es * g.field * (size_t)g.B, Mb = es * 2 * (size_t)g.my * g.B;
+    parts = {{h->bf.vor, Fb}, {h->bf.phi, Fb}, {h->bf.mu, Mb},
+             {h->bf.mem, sizeof(Member) * (size_t)g.B}};
+    if (g.temp) {
+      parts.push_back({h->bf.tb, Fb});
+      parts.push_back({h->bf.mt, Mb});
+    }
+    for (auto &pt : parts) {
+      void *q = nullptr;
+      if (cudaMalloc(&q, pt.second) != cudaSuccess) {
+        release();
+        return fail(4, "autotune: no memory for the state snapshot");
+      }
+      copies.push_back(q);
+      if (cudaMemcpyAsync(q, pt.first, pt.second, cudaMemcpyDeviceToDevice, h->st) != cudaSuccess)
+        return fail(3, "autotune: snapshot copy failed");
+    }
+    return 0;
+  }
+  int restore(sb_handle *h) {
+    for (size_t q = 0; q < copies.size(); q++)
+      if (cudaMemcpyAsync(parts[q].first, copies[q], parts[q].second, cudaMemcpyDeviceToDevice,
+                          h->st) != cudaSuccess)
+        return fail(3, "autotune: snapshot restore failed");
+    return 0;
+  }
+  void release() {
+    for (void *q : copies) cudaFree(q);
+    copies.clear();
+  }
+};
+
+// the launches of one sb_step call of nsteps steps (without the trace check)
+static cudaError_t launch_step_call(sb_handle *h, int nsteps) {
+  cudaError_t e;
+  if ((e = launch_scalar(h->g, h->bf, 0, h->st)) != cudaSuccess ||
+      (e = launch_tables(h->g, h->bf, 0, h->st)) != cudaSuccess ||
+      (e = launch_setconj(h->g, h->bf, h->st)) != cudaSuccess ||
+      (h->g.ydeal == 3 && (e = launch_filter(h->g, h->bf, 0, h->st)) != cudaSuccess) ||
+      (e = launch_lineB(h->g, h->bf, 0, h->st)) != cudaSuccess)
+    return e;
+  for (int s = 0; s < nsteps && e == cudaSuccess; s++) e = cudaGraphLaunch(h->step_exec, h->st);
+  return e;
+}
+
 int sb_autotune(sb_handle *h, int *choice) {
   if (!h) return fail(1, "null handle");
   Grid &g = h->g;
@@ -1061,15 +1159,60 @@ int sb_autotune(sb_handle *h, int *choice) {
   }
   g.cb3 = cb3;
   g.ncb3 = (g.nkx + cb3 - 1) / cb3;
+  // the y-line tile: warps per line solve (the segment plan and its factor
+  // tables), timed on whole captured steps -- the solves of a step differ in
+  // kind and count per kernel, so no single kernel stands for them -- from a
+  // snapshot of the state that is put back afterwards
+  int nseg = g.nseg;
+  best = 1e30f;
+  Snapshot snap;
+  int rc = snap.take(h);
+  for (int c : {1, 2, 3}) {
+    if (rc || e != cudaSuccess) break;
+    if ((g.my - 3) / c < 6) continue;
+    if ((rc = build_line_tables(h, c)) || (rc = capture_step(h))) break;
+    for (int q = 0; q < 3 && e == cudaSuccess; q++) {
+      if ((rc = snap.restore(h))) break;
+      if (q) cudaEventRecord(e0, st);
+      e = launch_step_call(h, 2);
+      if (q) cudaEventRecord(e1, st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float tq = 0.0f;
+      if (q && e == cudaSuccess) e = cudaEventElapsedTime(&tq, e0, e1);
+      if (q == 1) t = tq;
+      if (q == 2) t = t < tq ? t : tq;
+    }
+    if (!rc && e == cudaSuccess && t < best) best = t, nseg = c;
+  }
+  if (!rc) rc = snap.restore(h);
+  snap.release();
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (rc) return rc;
   if (e != cudaSuccess) return fail(3, "autotune: %s", cudaGetErrorString(e));
+  if (g.nseg != nseg && (rc = build_line_tables(h, nseg))) return rc;
   if (choice) {
     choice[0] = g.cb1;
     choice[1] = g.cb3;
     choice[2] = g.t2;
   }
   return capture_step(h);
+}
+
+int sb_set_line_segments(sb_handle *h, int nseg) {
+  if (!h) return fail(1, "null handle");
+  const int rc = build_line_tables(h, nseg);
+  if (rc) return rc;
+  return capture_step(h);
+}
+
+int sb_get_tuning(sb_handle *h, int *out) {
+  if (!h || !out) return fail(1, "null argument");
+  out[0] = h->g.cb1;
+  out[1] = h->g.cb3;
+  out[2] = h->g.t2;
+  out[3] = h->g.nseg;
+  return 0;
 }
 
 int sb_physical_fields(sb_handle *h, int member, unsigned mask, double *out) {

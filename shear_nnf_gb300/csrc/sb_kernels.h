@@ -27,6 +27,7 @@ cudaError_t launch_filter_rhs(int nlines, int N, const double *u, long ldu, doub
                               const double *shp, const double r[5], cudaStream_t st);
 cudaError_t prepare_line(const Grid &g);
 int line_segments();
+bool line_segments_supported(int nseg);
 size_t line_smem(const Grid &g);
 cudaError_t launch_lineA(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
 cudaError_t launch_lineB(const Grid &g, const Bufs &bf, int mode, cudaStream_t st);

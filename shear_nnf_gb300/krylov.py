@@ -157,11 +157,14 @@ class DevPeriodMap:
     """x -> shift(Phi_T(x)) on packed columns, the members of one batch
     advanced together (calc_dns_disk3d).  Each member stops on its own end
     time; members beyond the block get their start time as end time and stop
-    at once.  sca: the scalings of the packed vector (Packing.reference_scales)."""
+    at once.  sca: the scalings of the packed vector (Packing.reference_scales).
+    With autotune the handle's tiles (plane stages, warps per y-line solve)
+    are timed on the states of the first call (sb_autotune)."""
 
     def __init__(self, p, T: float, batch: int, precision: int = SB_FP64, chunk: int = 256,
-                 sca=(1.0, 1.0, 1.0)):
+                 sca=(1.0, 1.0, 1.0), autotune: bool = False):
         self.p, self.T, self.batch, self.chunk = p, float(T), int(batch), int(chunk)
+        self.autotune, self.tuning = autotune, None
         self.box = ShearBox(p, batch=self.batch, precision=precision)
         self.sca = np.asarray(sca, np.float64)
         self.n = self.box.packed_length
@@ -194,6 +197,9 @@ class DevPeriodMap:
                     # padding: an end time just past the start stops it at once
                     box.set_etime(m, time0 + max(1e-12, 1e-15 * abs(time0)))
                     box.set_re(m, self.p.Re)
+            if self.autotune and not self.tuning:
+                # tiles for this batch, timed on its first states (left as set)
+                self.tuning = box.autotune()
             done = [0] * len(grp)
             fin = [False] * len(grp)
             for _ in range(1 << 20):

@@ -128,8 +128,10 @@ class PeriodMap:
     stops on its own end time (the clipped last step of cross.f90:1694-1711);
     the batch is stepped in chunks until every member has reached it."""
 
-    def __init__(self, p, T: float, batch: int, precision: int = SB_FP64, chunk: int = 64):
+    def __init__(self, p, T: float, batch: int, precision: int = SB_FP64, chunk: int = 64,
+                 autotune: bool = False):
         self.p, self.T, self.batch, self.chunk = p, float(T), int(batch), int(chunk)
+        self.autotune, self.tuning = autotune, None
         self.box = ShearBox(p, batch=self.batch, precision=precision)
         self.integrations = 0
         self.steps = 0  # RK3 steps summed over the integrated states
@@ -147,6 +149,9 @@ class PeriodMap:
             T = Ts[m] if Ts is not None and m < len(Ts) else self.T
             box.set_etime(m, st["time"] + T)
             box.set_re(m, res[m] if res is not None and m < len(res) else self.p.Re)
+        if self.autotune and not self.tuning:
+            # tiles for this batch, timed on its first states (left as set)
+            self.tuning = box.autotune()
         steps = [0] * len(states)
         fin = [False] * len(states)
         for _ in range(1 << 20):
