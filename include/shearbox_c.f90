@@ -194,6 +194,155 @@ module shearbox_c
        real(c_double), value :: time, xoffb, xofft, deltat
      end function sb_write_restart
 
+     ! device-resident unknown vectors of the Newton / Arnoldi drivers: x is a
+     ! device address (for example a column of a Krylov space, sb_kspace_col);
+     ! sca = (sca_u, sca_g, sca_p) of throwing (gmres_shear.f90:411-413)
+     integer(c_long) function sb_packed_length(h) bind(C, name="sb_packed_length")
+       import :: c_long, c_ptr
+       type(c_ptr), value :: h
+     end function sb_packed_length
+
+     integer(c_int) function sb_set_state_packed(h, member, x, sca, time, xoffb, xofft) &
+          bind(C, name="sb_set_state_packed")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h, x
+       integer(c_int), value :: member
+       real(c_double), intent(in) :: sca(3)
+       real(c_double), value :: time, xoffb, xofft
+     end function sb_set_state_packed
+
+     integer(c_int) function sb_get_state_packed(h, member, x, sca, shiftx, shiftz) &
+          bind(C, name="sb_get_state_packed")
+       import :: c_int, c_ptr, c_double
+       type(c_ptr), value :: h, x
+       integer(c_int), value :: member
+       real(c_double), intent(in) :: sca(3)
+       real(c_double), value :: shiftx, shiftz
+     end function sb_get_state_packed
+
+     integer(c_int) function sb_packed_shift_tangent(h, x, out, dir) &
+          bind(C, name="sb_packed_shift_tangent")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h, x, out
+       integer(c_int), value :: dir
+     end function sb_packed_shift_tangent
+
+     ! a Krylov space of FP64 device columns: the vv(nl, k_gmres+1) of
+     ! gmres_k_shear with its dotp / vecadd / norm on the GPU
+     integer(c_int) function sb_kspace_create(n, cols, stream, ks) bind(C, name="sb_kspace_create")
+       import :: c_int, c_long, c_ptr
+       integer(c_long), value :: n
+       integer(c_int), value :: cols
+       type(c_ptr), value :: stream
+       type(c_ptr), intent(out) :: ks
+     end function sb_kspace_create
+
+     integer(c_int) function sb_kspace_destroy(ks) bind(C, name="sb_kspace_destroy")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ks
+     end function sb_kspace_destroy
+
+     type(c_ptr) function sb_kspace_col(ks, col) bind(C, name="sb_kspace_col")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ks
+       integer(c_int), value :: col
+     end function sb_kspace_col
+
+     integer(c_int) function sb_kspace_gram(ks, r0, r1, a0, m, b0, p, C) &
+          bind(C, name="sb_kspace_gram")
+       import :: c_int, c_long, c_ptr, c_double
+       type(c_ptr), value :: ks
+       integer(c_long), value :: r0, r1
+       integer(c_int), value :: a0, m, b0, p
+       real(c_double), intent(out) :: C(*)   ! m x p, row-major (C(p,m) in Fortran order)
+     end function sb_kspace_gram
+
+     integer(c_int) function sb_kspace_update(ks, r0, r1, a0, m, b0, p, C, alpha) &
+          bind(C, name="sb_kspace_update")
+       import :: c_int, c_long, c_ptr, c_double
+       type(c_ptr), value :: ks
+       integer(c_long), value :: r0, r1
+       integer(c_int), value :: a0, m, b0, p
+       real(c_double), intent(in) :: C(*)
+       real(c_double), value :: alpha
+     end function sb_kspace_update
+
+     integer(c_int) function sb_kspace_combine(ks, r0, r1, dst, nsrc, src, coef) &
+          bind(C, name="sb_kspace_combine")
+       import :: c_int, c_long, c_ptr, c_double
+       type(c_ptr), value :: ks
+       integer(c_long), value :: r0, r1
+       integer(c_int), value :: dst, nsrc
+       integer(c_int), intent(in) :: src(*)
+       real(c_double), intent(in) :: coef(*)
+     end function sb_kspace_combine
+
+     integer(c_int) function sb_kspace_perturb(ks, r0, r1, dst, x0, d, e) &
+          bind(C, name="sb_kspace_perturb")
+       import :: c_int, c_long, c_ptr, c_double
+       type(c_ptr), value :: ks
+       integer(c_long), value :: r0, r1
+       integer(c_int), value :: dst, x0, d
+       real(c_double), value :: e
+     end function sb_kspace_perturb
+
+     integer(c_int) function sb_kspace_fd(ks, r0, r1, dst, order, g, eps) &
+          bind(C, name="sb_kspace_fd")
+       import :: c_int, c_long, c_ptr, c_double
+       type(c_ptr), value :: ks
+       integer(c_long), value :: r0, r1
+       integer(c_int), value :: dst, order
+       integer(c_int), intent(in) :: g(*)
+       real(c_double), value :: eps
+     end function sb_kspace_fd
+
+     integer(c_int) function sb_kspace_set(ks, col, off, len, host) bind(C, name="sb_kspace_set")
+       import :: c_int, c_long, c_ptr, c_double
+       type(c_ptr), value :: ks
+       integer(c_int), value :: col
+       integer(c_long), value :: off, len
+       real(c_double), intent(in) :: host(*)
+     end function sb_kspace_set
+
+     integer(c_int) function sb_kspace_get(ks, col, off, len, host) bind(C, name="sb_kspace_get")
+       import :: c_int, c_long, c_ptr, c_double
+       type(c_ptr), value :: ks
+       integer(c_int), value :: col
+       integer(c_long), value :: off, len
+       real(c_double), intent(out) :: host(*)
+     end function sb_kspace_get
+
+     ! tiles of the step (plane stages, warps per y-line solve)
+     integer(c_int) function sb_autotune(h, choice) bind(C, name="sb_autotune")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int), intent(out) :: choice(3)
+     end function sb_autotune
+
+     integer(c_int) function sb_get_tuning(h, out) bind(C, name="sb_get_tuning")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int), intent(out) :: out(4)
+     end function sb_get_tuning
+
+     integer(c_int) function sb_set_line_segments(h, nseg) bind(C, name="sb_set_line_segments")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int), value :: nseg
+     end function sb_set_line_segments
+
+     ! getfil on the run's grid; info: pass a buffer of at least 584 bytes
+     ! (sb_restart_info), flags = 1 keeps the vorticity of a changed Re
+     integer(c_int) function sb_read_restart_ex(path, p, flags, vor, phi, u00, w00, info) &
+          bind(C, name="sb_read_restart_ex")
+       import :: c_int, c_char, c_double, c_ptr, sb_params
+       character(kind=c_char), intent(in) :: path(*)   ! NUL-terminated
+       type(sb_params), intent(in) :: p
+       integer(c_int), value :: flags
+       real(c_double), intent(out) :: vor(*), phi(*), u00(*), w00(*)
+       type(c_ptr), value :: info
+     end function sb_read_restart_ex
+
      integer(c_int) function sb_sizes(p, out) bind(C, name="sb_sizes")
        import :: c_int, sb_params
        type(sb_params), intent(in) :: p
