@@ -548,6 +548,11 @@ def run_ours(args):
 
     load()
     tuning = box.autotune()  # plane-stage tiles for this grid (untimed set-up)
+    if args.line_segments:
+        box.set_line_segments(args.line_segments)
+    if args.line_form != "auto":
+        box.set_line_form(args.line_form)
+    tuning = box.tuning()
     load()
     stream = torch.cuda.ExternalStream(box.stream)
     # warm-up
@@ -572,8 +577,11 @@ def run_ours(args):
     steps_per_s = ws * args.steps / (ms_max * 1e-3)
     # per step: 3 substeps x (3 plane stages, scalars, tables, 2 line kernels),
     # the spectra and plane sums of the statistics at substep 1, the
-    # end-of-step kernel; LES adds 5 per substep; + 4 entry launches
-    launches = (39 if args.variant == "les" else 24) * args.steps + 4
+    # end-of-step kernel; LES adds 5 per substep; the fused y-line form runs
+    # one line kernel per substep instead of two; + 4 entry launches
+    per_step = (39 if args.variant == "les" else 24) - (3 if tuning.get("line_form") == "fused"
+                                                         else 0)
+    launches = per_step * args.steps + 4
     if args.lite:
         # profiling runs (ncu): the timed steps only, no side measurements
         if rank == 0:
@@ -615,6 +623,17 @@ def run_ours(args):
     k1.record(stream)
     k1.synchronize()
     line_ms = (line_ms, k0.elapsed_time(k1) / 5)
+    # the fused y-line kernel (the step's default form where available)
+    lineF_ms = None
+    if box.tuning()["line_form"] == "fused":
+        box.set_state(st0)
+        box.step(1)
+        box.sync()
+        k0.record(stream)
+        box.launch_stage(12, 2, 5)
+        k1.record(stream)
+        k1.synchronize()
+        lineF_ms = k0.elapsed_time(k1) / 5
     fp64_peak = box.fp64_peak()
     mgalx, my, mgalz = GRID
     nkx = 2 * (mgalx // 3) // 2
@@ -750,7 +769,7 @@ def run_ours(args):
                     "frac": p2_gbs / hbm_peak, "peak_source": f"MEASURED_PEAKS.json ({hbm_src})",
                     "algorithmic_bytes_per_launch": p2_bytes},
             "traffic": traffic,
-            "line_kernels_ms": {"k_lineA": line_ms[0], "k_lineB": line_ms[1]},
+            "line_kernels_ms": {"k_lineA": line_ms[0], "k_lineB": line_ms[1], "k_lineF": lineF_ms},
         },
         "mixed_value": mixed["value"] if mixed else None,
         "mixed_speedup": mixed["speedup_vs_fp64"] if mixed else None,
@@ -798,9 +817,15 @@ def main():
                          "in [500, 2000] beyond the first)")
     ap.add_argument("--mixed", action="store_true",
                     help="profiling only (with --lite): the FP32-mixed precision form")
+    ap.add_argument("--line-form", default="auto", choices=["auto", "fused", "split"],
+                    help="profiling only (with --lite): the y-line kernels after the autotuner")
+    ap.add_argument("--line-segments", type=int, default=0,
+                    help="profiling only (with --lite): warps per y-line solve after the autotuner")
     args = ap.parse_args()
-    if (args.variant != "plain" or args.boxes != 1 or args.mixed) and not args.lite:
-        ap.error("--variant, --boxes and --mixed are for profiling runs (--lite)")
+    if (args.variant != "plain" or args.boxes != 1 or args.mixed or args.line_form != "auto"
+            or args.line_segments) and not args.lite:
+        ap.error("--variant, --boxes, --mixed, --line-form and --line-segments are for "
+                 "profiling runs (--lite)")
     global GRID
     GRID = GRIDS[args.grid]
     if args.warmup < 3:

@@ -253,8 +253,10 @@ int sb_kspace_get(sb_kspace *ks, int col, long off, long len, double *host);
 /* Measurement hooks (no counterpart in the reference; used by the benchmark).
  * sb_launch_stage enqueues `count` launches of one kernel of substep rk on the
  * handle's stream: stage 1..3 the plane stages, 4 the per-box phase tables,
- * 5 and 6 the two y-line kernels; with LES, 7..10 the four LES plane kernels
- * and 11 the LES y-line kernel.  The launches act on the current device state, so a
+ * 5 and 6 the two y-line kernels of the split form, 12 the fused y-line kernel
+ * (handles without temperature or y filter/dealiasing); with LES, 7..10 the four
+ * LES plane kernels and 11 the LES y-line kernel.  The launches act on the
+ * current device state, so a
  * run that used them must set the state again before stepping.
  * sb_fp64_peak measures the device's FP64 FMA throughput in TFLOP/s. */
 int sb_launch_stage(sb_handle *h, int stage, int rk, int count);
@@ -272,14 +274,23 @@ int sb_physical_fields(sb_handle *h, int member, unsigned mask, double *out);
  * columns per block of stages 1 and 3 (4 or 8), threads per block of stage 2
  * (the default or twice it) -- and the y-line tile, 1, 2 or 3 warps per line
  * solve (segments of the banded rows solved at once; each choice has its own
- * factor tables), keeps the fastest and re-captures the step graph.  choice
- * (may be NULL) receives cb1, cb3, t2; sb_get_tuning gives cb1, cb3, t2 and
- * the warps per line solve.  The state itself is not changed; call it after
- * sb_set_state and before sb_step.  sb_set_line_segments sets the warps per
- * line solve directly (1..3; my - 3 >= 6 rows per segment). */
+ * factor tables) in either form of the y-line stage (below), keeps the fastest
+ * and re-captures the step graph.  choice (may be NULL) receives cb1, cb3, t2;
+ * sb_get_tuning gives cb1, cb3, t2 and the warps per line solve.  The state
+ * itself is not changed; call it after sb_set_state and before sb_step.
+ * sb_set_line_segments sets the warps per line solve directly (1..3; my - 3 >=
+ * 6 rows per segment).
+ * sb_set_line_form chooses the y-line kernels of a substep: 1 (the default
+ * where available) one fused kernel that takes each group of lines through all
+ * its solves, 0 the split pair; form 1 needs a handle without temperature or y
+ * filter/dealiasing (otherwise error 1, and such handles always run form 0).
+ * sb_get_line_form gives the form the step graph uses.  Both forms compute the
+ * same step (bit for bit in FP64). */
 int sb_autotune(sb_handle *h, int *choice);
 int sb_get_tuning(sb_handle *h, int *out);
 int sb_set_line_segments(sb_handle *h, int nseg);
+int sb_set_line_form(sb_handle *h, int form);
+int sb_get_line_form(sb_handle *h, int *form);
 int sb_fp64_peak(sb_handle *h, double *tflops);
 
 /* Standalone y-line operators on device-resident complex lines.  Line data is

@@ -312,7 +312,7 @@ module shearbox_c
        real(c_double), intent(out) :: host(*)
      end function sb_kspace_get
 
-     ! tiles of the step (plane stages, warps per y-line solve)
+     ! tiles of the step (plane stages, warps per y-line solve, y-line form)
      integer(c_int) function sb_autotune(h, choice) bind(C, name="sb_autotune")
        import :: c_int, c_ptr
        type(c_ptr), value :: h
@@ -330,6 +330,19 @@ module shearbox_c
        type(c_ptr), value :: h
        integer(c_int), value :: nseg
      end function sb_set_line_segments
+
+     ! y-line kernels of a substep: 1 fused, 0 split
+     integer(c_int) function sb_set_line_form(h, form) bind(C, name="sb_set_line_form")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int), value :: form
+     end function sb_set_line_form
+
+     integer(c_int) function sb_get_line_form(h, form) bind(C, name="sb_get_line_form")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int), intent(out) :: form
+     end function sb_get_line_form
 
      ! getfil on the run's grid; info: pass a buffer of at least 584 bytes
      ! (sb_restart_info), flags = 1 keeps the vorticity of a changed Re

@@ -94,7 +94,8 @@ ABI_FUNCTIONS = [
     "sb_kspace_create", "sb_kspace_destroy", "sb_kspace_col", "sb_kspace_stream",
     "sb_kspace_sync", "sb_kspace_gram", "sb_kspace_update", "sb_kspace_transform",
     "sb_kspace_combine", "sb_kspace_perturb", "sb_kspace_fd", "sb_kspace_set", "sb_kspace_get",
-    "sb_read_restart_ex", "sb_get_tuning", "sb_set_line_segments",
+    "sb_read_restart_ex", "sb_get_tuning", "sb_set_line_segments", "sb_set_line_form",
+    "sb_get_line_form",
 ]
 
 _lib = None
@@ -148,6 +149,8 @@ def lib(auto_build: bool = False):
     L.sb_autotune.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     L.sb_get_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     L.sb_set_line_segments.argtypes = [vp, ctypes.c_int]
+    L.sb_set_line_form.argtypes = [vp, ctypes.c_int]
+    L.sb_get_line_form.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     L.sb_physical_fields.argtypes = [vp, ctypes.c_int, ctypes.c_uint, dp]
     L.sb_op_derivyc.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp,
                                 ctypes.c_long, vp, ctypes.c_long, dp, dp, vp]
@@ -352,21 +355,33 @@ class ShearBox:
         return dict(zip(names, out))
 
     def autotune(self) -> dict:
-        """Picks the fastest plane-stage tiles and y-line tile (warps per line
-        solve) on the current state (keep the state set before calling);
-        returns the choice."""
+        """Picks the fastest plane-stage tiles, y-line tile (warps per line
+        solve) and y-line form on the current state (keep the state set before
+        calling); returns the choice."""
         _check(lib().sb_autotune(self.h, None))
         return self.tuning()
 
     def tuning(self) -> dict:
-        """The current tiles (sb_get_tuning)."""
+        """The current tiles (sb_get_tuning) and y-line form
+        (sb_get_line_form: "fused" or "split")."""
         c = (ctypes.c_int * 4)()
         _check(lib().sb_get_tuning(self.h, c))
-        return {"p1_cols": c[0], "p3_cols": c[1], "p2_threads": c[2], "line_segments": c[3]}
+        f = ctypes.c_int(0)
+        _check(lib().sb_get_line_form(self.h, ctypes.byref(f)))
+        return {"p1_cols": c[0], "p3_cols": c[1], "p2_threads": c[2], "line_segments": c[3],
+                "line_form": "fused" if f.value else "split"}
 
     def set_line_segments(self, nseg: int):
         """Warps per y-line solve, 1..3 (sb_set_line_segments)."""
         _check(lib().sb_set_line_segments(self.h, int(nseg)))
+
+    def set_line_form(self, form: str):
+        """The y-line kernels of a substep: "fused" (one kernel; handles
+        without temperature or y filter/dealiasing) or "split"
+        (sb_set_line_form)."""
+        if form not in ("fused", "split"):
+            raise ValueError(f"line form {form!r}: 'fused' or 'split'")
+        _check(lib().sb_set_line_form(self.h, 1 if form == "fused" else 0))
 
     def statistics(self, member: int = 0) -> dict:
         """The hist accumulators of the last step call (sb_get_statistics):

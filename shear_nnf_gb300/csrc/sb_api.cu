@@ -348,6 +348,10 @@ static int capture_step(sb_handle *h) {
       if ((e = launch_tables(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
     }
     if (h->g.les && (e = launch_lineL(h->g, h->bf, h->st)) != cudaSuccess) break;
+    if (h->g.lform && line_fused_ok(h->g)) {
+      e = launch_lineF(h->g, h->bf, rk, h->st);
+      continue;
+    }
     if ((e = launch_lineA(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
     e = launch_lineB(h->g, h->bf, rk, h->st);
   }
@@ -535,6 +539,7 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
     g.slo[q] = plan.lo[q];
     g.shi[q] = plan.hi[q];
   }
+  g.lform = 1;  // the fused y-line kernel wherever the step allows it
   cudaError_t ce = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
   if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
@@ -1030,8 +1035,10 @@ void *sb_get_stream(sb_handle *h) { return h ? (void *)h->st : nullptr; }
 
 int sb_launch_stage(sb_handle *h, int stage, int rk, int count) {
   if (!h || count < 0) return fail(1, "bad argument");
-  if (stage < 1 || stage > 11 || rk < 1 || rk > 3) return fail(1, "stage 1..11, rk 1..3");
-  if (stage >= 7 && !h->g.les) return fail(1, "stages 7..11 need an LES handle");
+  if (stage < 1 || stage > 12 || rk < 1 || rk > 3) return fail(1, "stage 1..12, rk 1..3");
+  if (stage >= 7 && stage <= 11 && !h->g.les) return fail(1, "stages 7..11 need an LES handle");
+  if (stage == 12 && !line_fused_ok(h->g))
+    return fail(1, "stage 12 (fused y-line kernel) not available for this handle");
   for (int q = 0; q < count; q++) {
     cudaError_t e;
     if (stage <= 3)
@@ -1044,8 +1051,10 @@ int sb_launch_stage(sb_handle *h, int stage, int rk, int count) {
       e = launch_lineB(h->g, h->bf, rk, h->st);
     else if (stage <= 10)
       e = launch_les(h->g, h->bf, stage - 5, rk, h->st);
-    else
+    else if (stage == 11)
       e = launch_lineL(h->g, h->bf, h->st);
+    else
+      e = launch_lineF(h->g, h->bf, rk, h->st);
     if (e != cudaSuccess) return fail(3, "launch: %s", cudaGetErrorString(e));
   }
   return 0;
@@ -1163,31 +1172,39 @@ int sb_autotune(sb_handle *h, int *choice) {
   // tables), timed on whole captured steps -- the solves of a step differ in
   // kind and count per kernel, so no single kernel stands for them -- from a
   // snapshot of the state that is put back afterwards
-  int nseg = g.nseg;
+  int nseg = g.nseg, lform = g.lform;
   best = 1e30f;
   Snapshot snap;
   int rc = snap.take(h);
   for (int c : {1, 2, 3}) {
     if (rc || e != cudaSuccess) break;
     if ((g.my - 3) / c < 6) continue;
-    if ((rc = build_line_tables(h, c)) || (rc = capture_step(h))) break;
-    for (int q = 0; q < 3 && e == cudaSuccess; q++) {
-      if ((rc = snap.restore(h))) break;
-      if (q) cudaEventRecord(e0, st);
-      e = launch_step_call(h, 2);
-      if (q) cudaEventRecord(e1, st);
-      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-      float tq = 0.0f;
-      if (q && e == cudaSuccess) e = cudaEventElapsedTime(&tq, e0, e1);
-      if (q == 1) t = tq;
-      if (q == 2) t = t < tq ? t : tq;
+    if ((rc = build_line_tables(h, c))) break;
+    // both forms of the y-line stage where the fused one is available
+    for (int f = 1; f >= 0; f--) {
+      if (rc || e != cudaSuccess) break;
+      if (f == 1 && !line_fused_ok(g)) continue;
+      g.lform = f;
+      if ((rc = capture_step(h))) break;
+      for (int q = 0; q < 3 && e == cudaSuccess; q++) {
+        if ((rc = snap.restore(h))) break;
+        if (q) cudaEventRecord(e0, st);
+        e = launch_step_call(h, 2);
+        if (q) cudaEventRecord(e1, st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float tq = 0.0f;
+        if (q && e == cudaSuccess) e = cudaEventElapsedTime(&tq, e0, e1);
+        if (q == 1) t = tq;
+        if (q == 2) t = t < tq ? t : tq;
+      }
+      if (!rc && e == cudaSuccess && t < best) best = t, nseg = c, lform = f;
     }
-    if (!rc && e == cudaSuccess && t < best) best = t, nseg = c;
   }
   if (!rc) rc = snap.restore(h);
   snap.release();
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  g.lform = lform;
   if (rc) return rc;
   if (e != cudaSuccess) return fail(3, "autotune: %s", cudaGetErrorString(e));
   if (g.nseg != nseg && (rc = build_line_tables(h, nseg))) return rc;
@@ -1204,6 +1221,21 @@ int sb_set_line_segments(sb_handle *h, int nseg) {
   const int rc = build_line_tables(h, nseg);
   if (rc) return rc;
   return capture_step(h);
+}
+
+int sb_set_line_form(sb_handle *h, int form) {
+  if (!h) return fail(1, "null handle");
+  if (form != 0 && form != 1) return fail(1, "line form %d (0 split, 1 fused)", form);
+  if (form == 1 && !line_fused_ok(h->g))
+    return fail(1, "fused y-line kernel not available for this handle");
+  h->g.lform = form;
+  return capture_step(h);
+}
+
+int sb_get_line_form(sb_handle *h, int *form) {
+  if (!h || !form) return fail(1, "null argument");
+  *form = (h->g.lform && line_fused_ok(h->g)) ? 1 : 0;
+  return 0;
 }
 
 int sb_get_tuning(sb_handle *h, int *out) {

@@ -488,6 +488,10 @@ cudaError_t launch_finish(const Grid &g, const Bufs &bf, cudaStream_t st) {
   cudaError_t lineA_f32(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);           \
   cudaError_t lineB_f64(const Grid &g, const Bufs &bf, int mode, cudaStream_t st);         \
   cudaError_t lineB_f32(const Grid &g, const Bufs &bf, int mode, cudaStream_t st);         \
+  cudaError_t lineF_f64(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);           \
+  cudaError_t lineF_f32(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);           \
+  bool lineF_fits_f64(const Grid &g);                                                      \
+  bool lineF_fits_f32(const Grid &g);                                                      \
   cudaError_t lineL_f64(const Grid &g, const Bufs &bf, cudaStream_t st);                   \
   cudaError_t lineL_f32(const Grid &g, const Bufs &bf, cudaStream_t st);                   \
   cudaError_t meand1_f64(const Grid &g, const Bufs &bf, cudaStream_t st);                  \
@@ -531,6 +535,15 @@ cudaError_t launch_lineA(const Grid &g, const Bufs &bf, int rk, cudaStream_t st)
 }
 cudaError_t launch_lineB(const Grid &g, const Bufs &bf, int mode, cudaStream_t st) {
   SB_SEG_CALL(lineB, g, bf, mode, st)
+}
+cudaError_t launch_lineF(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  SB_SEG_CALL(lineF, g, bf, rk, st)
+}
+// the fused y-line kernel covers the plain step: no temperature, no y filter
+// or y dealiasing, and its block's shared memory fits
+bool line_fused_ok(const Grid &g) {
+  if (g.temp || g.ydeal) return false;
+  SB_SEG_CALL(lineF_fits, g)
 }
 cudaError_t launch_lineL(const Grid &g, const Bufs &bf, cudaStream_t st) {
   SB_SEG_CALL(lineL, g, bf, st)

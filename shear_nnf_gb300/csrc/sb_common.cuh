@@ -61,6 +61,7 @@ struct Grid {
   long field;            // doubles per field of one box   (plane*my)
   int nlines_pad;        // component lines per member, padded to whole warps
   int nseg, slo[4], shi[4];  // segments of the banded rows of the y-solves
+  int lform;             // y-line kernels of a substep: 0 k_lineA + k_lineB, 1 k_lineF
   int ngrp;              // groups of 16 lines per member in the y-line kernels
   // Smagorinsky LES (cross.f90:1291-1406): on/off, molecular viscosity kept,
   // (Cles * Deltag)^2, fields per z row of zbuf (6, or 10 with the model),

@@ -31,6 +31,10 @@ bool line_segments_supported(int nseg);
 size_t line_smem(const Grid &g);
 cudaError_t launch_lineA(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
 cudaError_t launch_lineB(const Grid &g, const Bufs &bf, int mode, cudaStream_t st);
+// the substep's y-line work in one kernel (k_lineF) in place of k_lineA +
+// k_lineB, where line_fused_ok(g)
+cudaError_t launch_lineF(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
+bool line_fused_ok(const Grid &g);
 cudaError_t launch_setconj(const Grid &g, const Bufs &bf, cudaStream_t st);
 cudaError_t launch_scalar(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
 cudaError_t launch_tables(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);

@@ -19,7 +19,10 @@
 // updates tb00; k_lineB role 1 adds the buoyancy gbeta lap(tb) to the phi
 // right-hand side and a third role updates tb.
 // The same k_lineB (mode 0) is the prologue of a cross call: v from phi on the
-// first step (cross.f90:408-426) and the first derivatives.  Forward
+// first step (cross.f90:408-426) and the first derivatives.  For the plain
+// step (no temperature, no y filter or y dealiasing) k_lineF does both
+// kernels' work in one launch, each block taking its 16 lines through all
+// the solves with two pipelines of warps; the handle chooses the form.  Forward
 // substitutions are kept in shared memory, one column per thread.  The
 // per-box kernels of the step (k_scalar, k_tables, k_finish) are in
 // sb_box.cu.
@@ -422,6 +425,258 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs 
   store_col(ys, ystr, (R *)bf.V + off, ps, L);
 }
 
+// ---------------------------------------------------------------------------
+// k_lineF: the y-line work of one substep in one kernel, for the plain step
+// (no temperature, no y filter or y dealiasing; an LES step qualifies, its
+// k_lineL runs before).  Per line, k_lineA's and k_lineB's work is a chain of
+// solves that never leaves the line, so one block can take 16 lines through
+// all of it with two pipelines of kSeg warps (pipeline 0: omega_y, pipeline
+// 1: phi), each doing one solve or one pointwise update per phase:
+//   phase  pipeline 0                             pipeline 1
+//   1      T = d/dy(dH1/dx + dH3/dz)              S = d2(phi)/dy2
+//   2      omega_y: hg + nu lap, RK3 update,      phi: hv - T + nu lap, RK3
+//          zeta store, remaps (d2 from Lv)        update, zeta store, remaps
+//   3      d(omega_y)/dy -> D                     v = lapcdy(phi) -> G
+//   4      d2(omega_y)/dy2 -> Lv                  dv/dy -> V
+// All warps of a block then carry the same work (the split kernels pair a
+// heavy role with a light one on the SM sub-partitions), and T and S stay in
+// shared memory, rounded to the storage type as k_lineA stores them, so the
+// step is the split kernels' step.  The mean block runs the mean lines on
+// pipeline 0 (nu u00'' and the mean update, then du00/dy for the next
+// substep).  Every phase passes the same block barriers on both pipelines
+// (two per solve, `seg_idle` where a pipeline has no solve, one after each
+// of phases 1-3); the pipeline branches are uniform per warp.
+__device__ __forceinline__ void seg_idle() {
+  __syncthreads();
+  __syncthreads();
+}
+
+// rk_update with the subtracted right-hand-side term and d2f/dy2 given per
+// row by functors (sub(h, i) returns h minus the term; d2(i) the derivative),
+// the same arithmetic
+template <typename R, class SubF, class D2F>
+__device__ __forceinline__ void rk_update_fn(const SubF &sub, const D2F &d2,
+                                             const R *__restrict__ rhs, R *__restrict__ f,
+                                             R *__restrict__ fwk, long ps, const LineThread &L,
+                                             int rk, double nuv, double k2, double Dt,
+                                             const double *__restrict__ mf1,
+                                             const double *__restrict__ mf2, long mfs) {
+  const R gk = (R)kGama[rk], zk = (R)kZeta[rk], dtr = (R)Dt;
+  const int c = L.c;
+#pragma unroll 2
+  for (int i = L.r0; i <= L.r1; i++) {
+    const int j = i - 1;
+    const long q = (long)j * ps;
+    const R fo = f[q];
+    R h = sub(rhs[q], i);
+    const double vis = -(k2 * (double)fo) + d2(i, q);
+    h = h + (R)(nuv * vis);
+    R wk = (rk == 0) ? gk * h : fwk[q] + gk * h;
+    const double fn = (double)(fo + dtr * wk);
+    const cd m2 = ldc2(mf2 + (long)j * mfs);
+    const double fnm = cmul_c(fn, __shfl_xor_sync(0xffffffffu, fn, 1), m2, c);
+    if (rk < 2) {
+      const cd m1 = ldc2(mf1 + (long)j * mfs);
+      const double wz = (double)(h * zk);
+      wk = (R)cmul_c(wz, __shfl_xor_sync(0xffffffffu, wz, 1), m1, c);
+    }
+    if (L.active) {
+      f[q] = (R)fnm;
+      fwk[q] = wk;
+    }
+  }
+}
+
+// block -> (member, group of 16 lines), the member's mean block last; warp ->
+// (pipeline, segment); lane -> (line of the group, component)
+__device__ __forceinline__ bool line_thread_f(const Grid &g, LineThread *L, int *pipe) {
+  const int per = g.ngrp + 1;
+  L->b = blockIdx.x / per;
+  if (L->b >= g.B) return false;
+  const int r = blockIdx.x - L->b * per;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  *pipe = w / kSeg;
+  L->role = *pipe;
+  L->mean = r >= g.ngrp;
+  L->s = w - *pipe * kSeg;
+  L->l = lane >> 1;
+  L->c = lane & 1;
+  const int nl = g.nkx * g.mz;
+  if (L->mean) {
+    L->lc = 0;
+    L->active = (L->l == 0);
+  } else {
+    L->lc = (long)r * 16 + L->l;
+    L->active = L->lc < nl;
+    if (!L->active) L->lc = nl - 1;
+  }
+  L->i = (int)(L->lc % g.nkx);
+  L->k = (int)(L->lc / g.nkx);
+  L->r0 = g.slo[L->s];
+  L->r1 = (L->s == kSeg - 1) ? g.my : g.shi[L->s];
+  return true;
+}
+
+#define SEG_SOLVE_P(U, PS, VIEW, SVIEW, TAIL, SHP, SHM, R0, R1, R2, R3, ANTI)                   \
+  solve_seg<kSeg>(U, PS, ys, ystr, N, VIEW, SVIEW, TAIL, SHP, SHM, L.c, L.s, L.l, g.slo, g.shi, \
+                  R0, R1, R2, R3, ANTI, &xch[pipe][0][0][0][0])
+
+template <typename R>
+__global__ void __launch_bounds__(64 * kSeg, 1) k_lineF(Grid g, Bufs bf, int rk1) {
+  __shared__ double xch[2][kSeg][16][2][SB_XS];
+  LineThread L;
+  int pipe = 0;
+  if (!line_thread_f(g, &L, &pipe)) return;  // whole blocks
+  Member &M = bf.mem[L.b];
+  if (M.halted) return;  // uniform per block
+  const int N = g.my, ystr = blockDim.x;
+  const int rk = rk1 - 1;
+  double *ys = ycol();
+  const FacView V1(bf.d1, 0), V2(bf.d2, 0);
+  const SegView W1(bf.d1, 0), W2(bf.d2, 0);
+  const double Dt = M.Deltat, nu = M.nu;
+  if (L.mean) {
+    R *mu = (R *)bf.mu + (long)L.b * 2 * N + L.c;
+    const cd one = mk(1.0, 0.0);
+    // phase 1: nu u00'' (visc3d(u00, rf0u, m=1, rk=0), cross.f90:666-672)
+    if (pipe == 0) {
+      const TailLoad T2{bf.tl2o + (long)L.b * g.nkx * SB_TAIL};
+      SEG_SOLVE_P(mu, 2, V2, W2, T2, one, one, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6], false);
+    } else {
+      seg_idle();
+    }
+    __syncthreads();
+    // phase 2: forcing, damping and the RK3 update of the mean profiles
+    // (cross.f90:622-626,703-723,753-756), k_lineA's mean block
+    if (pipe == 0) {
+      R *mwk = (R *)bf.mwk + (long)L.b * 2 * N + L.c;
+      const R *mrf = (const R *)bf.mrf + (long)L.b * 2 * N + L.c;
+      const R gk = (R)kGama[rk], zk = (R)kZeta[rk];
+      const bool damp = g.damp && L.c == 0;
+      const bool xf = g.force == -1 && L.c == 0;
+      for (int i = L.r0; i <= L.r1; i++) {
+        const int j = i - 1;
+        R rf0 = mrf[2 * j];
+        if (xf) rf0 = (R)((double)rf0 + g.xforce);
+        if (damp) {
+          const double y = (double)j * g.dy - 0.5 * g.Ly;
+          const double hw = 1.0 - (0.25 * (1.0 + tanh(6.0 * (g.damp_a - y) / g.lz + 3.0))) *
+                                      (1.0 + tanh(6.0 * (g.damp_a + y) / g.lz + 3.0));
+          rf0 = (R)((double)rf0 - g.damp_up * hw * (double)mu[2 * j]);
+        }
+        const R rf = rf0 + (R)(nu * (-(0.0 * (double)mu[2 * j]) + ys[(i - L.r0) * ystr]));
+        R wk = (rk == 0) ? gk * rf : mwk[2 * j] + gk * rf;
+        const R un = mu[2 * j] + (R)Dt * wk;
+        if (rk < 2) wk = rf * zk;
+        if (L.active) {
+          mu[2 * j] = un;
+          mwk[2 * j] = wk;
+        }
+      }
+    }
+    __syncthreads();
+    // phase 3: du00/dy, dw00/dy of the updated profiles (cross.f90:1186-1192)
+    if (pipe == 0) {
+      R *mdu = (R *)bf.mdu + (long)L.b * 2 * N + L.c;
+      const TailLoad T1{bf.tl1o + (long)L.b * g.nkx * SB_TAIL};
+      SEG_SOLVE_P(mu, 2, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true);
+      if (L.active)
+        for (int i = L.r0; i <= L.r1; i++) mdu[2 * (i - 1)] = (R)ys[(i - L.r0) * ystr];
+    } else {
+      seg_idle();
+    }
+    __syncthreads();
+    seg_idle();  // phase 4
+    return;
+  }
+  const long off = (long)L.b * g.field + 2 * L.lc + L.c;
+  const long ps = g.plane;
+  const int i = L.i, k = L.k;
+  const bool is00 = (i == 0 && k == 0);
+  const double a = g.alp * i;
+  const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
+  const double k2 = a * a + gz * gz;
+  const double *mf1 = bf.mf1 + (long)L.b * 2 * N * g.nkx + 2 * i;
+  const double *mf2 = bf.mf2 + (long)L.b * 2 * N * g.nkx + 2 * i;
+  {
+    // phases 1-2 at the phase of time t
+    const cd shp = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * i);
+    const cd shm = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
+    if (pipe == 0) {
+      // T = d/dy (dH1/dx + dH3/dz) (cross.f90:565-575)
+      const TailLoad T1{bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL};
+      SEG_SOLVE_P((const R *)bf.D + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
+                  g.rh1[6], true);
+      // the value k_lineA would store
+      for (int r = L.r0; r <= L.r1; r++)
+        ys[(r - L.r0) * ystr] = (double)(R)ys[(r - L.r0) * ystr];
+    } else {
+      // S = d2(phi)/dy2 for the viscous term of the phi equation (cross.f90:660)
+      const TailLoad T2{bf.tl2o + ((long)L.b * g.nkx + i) * SB_TAIL};
+      SEG_SOLVE_P((const R *)bf.phi + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4],
+                  g.rh2[5], g.rh2[6], false);
+      for (int r = L.r0; r <= L.r1; r++)
+        ys[(r - L.r0) * ystr] = (double)(R)ys[(r - L.r0) * ystr];
+    }
+  }
+  __syncthreads();
+  if (pipe == 0) {
+    // hg += nu lap(omega_y) (visc3d, cross.f90:659) with d2(omega_y)/dy2 of
+    // the substep's starting state, taken in phase 4 of the previous substep
+    // (or the prologue); RK3 update, zeta store, remaps (cross.f90:694-781)
+    const R *lv = (const R *)bf.Lv + off;
+    rk_update_fn<R>([](R h, int) { return h; },
+                    [lv](int, long q) { return (double)lv[q]; }, (const R *)bf.G + off,
+                    (R *)bf.vor + off, (R *)bf.vorwk + off, ps, L, rk, is00 ? 0.0 : nu, k2, Dt,
+                    mf1, mf2, 2 * g.nkx);
+  } else {
+    // hv - d/dy(dH1/dx + dH3/dz) + nu lap(phi), RK3 update, zeta store, remaps
+    // (cross.f90:607,660,694-781); T from pipeline 0's column of the same
+    // (segment, line, component)
+    const double *ys0 = ys - 32 * kSeg;
+    const int r0 = L.r0;
+    const double *yb = ys;
+    rk_update_fn<R>([ys0, r0, ystr](R h, int r) { return h - (R)ys0[(r - r0) * ystr]; },
+                    [yb, r0, ystr](int r, long) { return yb[(r - r0) * ystr]; },
+                    (const R *)bf.V + off, (R *)bf.phi + off, (R *)bf.phiwk + off, ps, L, rk,
+                    is00 ? 0.0 : M.nu, k2, Dt, mf1, mf2, 2 * g.nkx);
+  }
+  __syncthreads();  // whole updated lines are read below
+  // phases 3-4 at the phase of time t + c_k dt
+  const cd shp = ldc2(bf.sh_new + (long)L.b * 4 * g.nkx + 2 * i);
+  const cd shm = ldc2(bf.sh_new + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
+  const TailLoad T1{bf.tl1n + ((long)L.b * g.nkx + i) * SB_TAIL};
+  if (pipe == 0) {
+    // d(omega_y)/dy (cross.f90:440)
+    SEG_SOLVE_P((const R *)bf.vor + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
+                g.rh1[6], true);
+    store_col(ys, ystr, (R *)bf.D + off, ps, L);
+  } else {
+    // v = lapcdy(phi) (cross.f90:784-795); hg(0,0) keeps the value the
+    // nonlinear stage left (zero)
+    const FacView VH(bf.hz, L.lc);
+    const SegView WH(bf.hz, L.lc);
+    const TailMake TH{VH, shp, N};
+    SEG_SOLVE_P((const R *)bf.phi + off, ps, VH, WH, TH, shp, shm, g.pr2[3], g.pr2[4], g.pr2[5],
+                g.pr2[6], false);
+    if (!is00) store_col(ys, ystr, (R *)bf.G + off, ps, L);
+  }
+  __syncthreads();  // v of all segments is read below
+  if (pipe == 0) {
+    // d2(omega_y)/dy2 of the next substep's starting state (its visc3d,
+    // cross.f90:659)
+    const TailLoad T2{bf.tl2n + ((long)L.b * g.nkx + i) * SB_TAIL};
+    SEG_SOLVE_P((const R *)bf.vor + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
+                g.rh2[6], false);
+    store_col(ys, ystr, (R *)bf.Lv + off, ps, L);
+  } else {
+    // dv/dy (cross.f90:442)
+    SEG_SOLVE_P((const R *)bf.G + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
+                g.rh1[6], true);
+    store_col(ys, ystr, (R *)bf.V + off, ps, L);
+  }
+}
+
 // LES y-operators (iuse_LES, cross.f90:565-608,639-647), between k_tables and
 // k_lineA:
 //   role 0: hg += d(rhgc2)/dy                       (derivyc, -> G)
@@ -615,6 +870,17 @@ static size_t smem_of(const Grid &g) {
 // the exported launchers of this compilation (sb::seg<K>::name_f64/_f32)
 size_t SB_PSUF(line_smem)(const Grid &g) { return smem_of(g); }
 
+// k_lineF (two pipelines: twice the threads and columns of the split
+// kernels, two exchange areas) fits the device's shared memory per block
+bool SB_PSUF(lineF_fits)(const Grid &g) {
+  int dev = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return false;
+  const size_t xs = sizeof(double) * 2 * kSeg * 16 * 2 * SB_XS;
+  return 2 * smem_of(g) + xs <= (size_t)optin;
+}
+
 cudaError_t SB_PSUF(prepare_line)(const Grid &g) {
   typedef SbR R;
   const int sm = (int)smem_of(g);
@@ -625,6 +891,8 @@ cudaError_t SB_PSUF(prepare_line)(const Grid &g) {
   cudaFuncSetAttribute(k_lineL<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   cudaFuncSetAttribute(k_filter<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   cudaFuncSetAttribute(k_meand1<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  if (SB_PSUF(lineF_fits)(g))
+    cudaFuncSetAttribute(k_lineF<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * sm);
   return cudaGetLastError();
 }
 
@@ -645,6 +913,13 @@ cudaError_t SB_PSUF(lineB)(const Grid &g, const Bufs &bf, int mode, cudaStream_t
     k_lineB<R, true><<<nb, kLineT, smem_of(g), st>>>(g, bf, mode);
   else
     k_lineB<R, false><<<nb, kLineT, smem_of(g), st>>>(g, bf, mode);
+  return cudaGetLastError();
+}
+
+cudaError_t SB_PSUF(lineF)(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  typedef SbR R;
+  const unsigned nb = (unsigned)(g.B * (g.ngrp + 1));
+  k_lineF<R><<<nb, 2 * kLineT, 2 * smem_of(g), st>>>(g, bf, rk);
   return cudaGetLastError();
 }
 
