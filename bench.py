@@ -533,6 +533,8 @@ def run_ours(args):
         pp.update(les=1, les_visc=1, cs=0.1)
     elif args.variant == "temperature":
         pp.update(temperature=1, fkappa=LZ ** 2 / REZ / 0.7, bym=1.0, gbeta=0.5)
+    elif args.variant == "implicit":
+        pp.update(implicit_visc=1)
     p = sb.make_params(**pp)
     st0 = sb.seed_state(p, 3 + rank)
     nbox = args.boxes if args.lite else 1
@@ -579,6 +581,8 @@ def run_ours(args):
     # the spectra and plane sums of the statistics at substep 1, the
     # end-of-step kernel; LES adds 5 per substep; the fused y-line form runs
     # one line kernel per substep instead of two; + 4 entry launches
+    # (the implicit variant: k_hfac + k_lineI per substep in place of the two
+    # line kernels)
     per_step = (39 if args.variant == "les" else 24) - (3 if tuning.get("line_form") == "fused"
                                                          else 0)
     launches = per_step * args.steps + 4
@@ -810,8 +814,9 @@ def main():
     ap.add_argument("--no-temp", action="store_true", help="skip the temperature (crosst) leg")
     ap.add_argument("--lite", action="store_true",
                     help="profiling only: time the steps, skip e2e / CPU / per-kernel legs")
-    ap.add_argument("--variant", default="plain", choices=["plain", "les", "temperature"],
-                    help="profiling only (with --lite): step the LES or the temperature box")
+    ap.add_argument("--variant", default="plain",
+                    choices=["plain", "les", "temperature", "implicit"],
+                    help="profiling only (with --lite): step the LES, temperature or semi-implicit box")
     ap.add_argument("--boxes", type=int, default=1,
                     help="profiling only (with --lite): boxes in the batch (Re_z log-uniform "
                          "in [500, 2000] beyond the first)")

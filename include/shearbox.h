@@ -75,6 +75,12 @@ typedef struct sb_params {
                                   inertial force xforce to rf0u (cross.f90:610-624,
                                   crosst.f90:680-693) */
   double force_roll, xforce;   /* their amplitudes (initcr.f90:2103-2118) */
+  int implicit_visc;           /* 1: viscous terms semi-implicit, the reference's
+                                  explicit = 0 (cross.f90:797-989; hre3.dat keyword
+                                  explicit, initcr.f90:1976-1984): a Helmholtz solve
+                                  (d2/dy2 - k^2 - Re/(beta_k dt)) per line and
+                                  substep, no viscous time-step limit.  Needs les =
+                                  temperature = ydeal = 0 (error 2 otherwise). */
 } sb_params;
 
 /* Per-box status after sb_step (cross.f90 istop logic, 1683-1690, 2102-2115) */
@@ -255,7 +261,8 @@ int sb_kspace_get(sb_kspace *ks, int col, long off, long len, double *host);
  * handle's stream: stage 1..3 the plane stages, 4 the per-box phase tables,
  * 5 and 6 the two y-line kernels of the split form, 12 the fused y-line kernel
  * (handles without temperature or y filter/dealiasing); with LES, 7..10 the four
- * LES plane kernels and 11 the LES y-line kernel.  The launches act on the
+ * LES plane kernels and 11 the LES y-line kernel; with implicit_visc, 13 the
+ * factorisation of the substep's Helmholtz operators and 14 its y-line kernel.  The launches act on the
  * current device state, so a
  * run that used them must set the state again before stepping.
  * sb_fp64_peak measures the device's FP64 FMA throughput in TFLOP/s. */
@@ -284,8 +291,9 @@ int sb_physical_fields(sb_handle *h, int member, unsigned mask, double *out);
  * where available) one fused kernel that takes each group of lines through all
  * its solves, 0 the split pair; form 1 needs a handle without temperature or y
  * filter/dealiasing (otherwise error 1, and such handles always run form 0).
- * sb_get_line_form gives the form the step graph uses.  Both forms compute the
- * same step (bit for bit in FP64). */
+ * sb_get_line_form gives the form the step graph uses (2 for a handle with
+ * implicit_visc, whose substeps run the semi-implicit y-line kernel).  Both
+ * forms compute the same step (to the last bits in FP64). */
 int sb_autotune(sb_handle *h, int *choice);
 int sb_get_tuning(sb_handle *h, int *out);
 int sb_set_line_segments(sb_handle *h, int nseg);

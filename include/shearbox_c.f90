@@ -34,6 +34,7 @@ module shearbox_c
      real(c_double)  :: damp_up, damp_aa
      integer(c_int)  :: force
      real(c_double)  :: force_roll, xforce
+     integer(c_int)  :: implicit_visc
   end type sb_params
 
   type, bind(C) :: sb_status

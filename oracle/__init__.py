@@ -52,6 +52,7 @@ class OrcParams(ctypes.Structure):
         ("gbeta", ctypes.c_double),
         ("damping", ctypes.c_int), ("damp_up", ctypes.c_double), ("damp_aa", ctypes.c_double),
         ("force", ctypes.c_int), ("force_roll", ctypes.c_double), ("xforce", ctypes.c_double),
+        ("implicit_visc", ctypes.c_int),
     ]
 
 
@@ -154,11 +155,16 @@ class Oracle:
                  vbulk=0.0, fixed_dt=0.0, readflag=1, uprim=1.0, nhist=1,
                  etime=1e10, dumptime=1e10, dtimag=1e10, keep_laminar=0, les=0, les_visc=1,
                  cs=0.1, ydeal=0, temperature=0, fkappa=0.0, bym=0.0, gbeta=0.0, damping=0,
-                 damp_up=0.0, damp_aa=0.0, force=0, force_roll=0.0, xforce=0.0):
+                 damp_up=0.0, damp_aa=0.0, force=0, force_roll=0.0, xforce=0.0,
+                 implicit_visc=0):
+        if implicit_visc and (les or temperature):
+            # the reference stops on LES with explicit = 0 (initcr.f90:2179-2182);
+            # crosst's semi-implicit branch is not restated
+            raise ValueError("implicit_visc is for cross without LES or temperature")
         self.p = OrcParams(mgalx, my, mgalz, Re, alp, Ly, gam, s, chi, CFL, vbulk, fixed_dt,
                            readflag, uprim, nhist, etime, dumptime, dtimag, keep_laminar, les,
                            les_visc, cs, ydeal, temperature, fkappa, bym, gbeta, damping,
-                           damp_up, damp_aa, force, force_roll, xforce)
+                           damp_up, damp_aa, force, force_roll, xforce, implicit_visc)
         self.h = lib().orc_create(ctypes.byref(self.p))
         sz = (ctypes.c_int * 8)()
         lib().orc_sizes(self.h, sz)

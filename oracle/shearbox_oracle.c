@@ -1590,6 +1590,147 @@ static void moving_frame(ctx *c, double *vor, double *phi, double mtime) {
   free(sydt);
 }
 
+/* The semi-implicit viscous branch of one substep (explicit = 0,
+ * cross.f90:797-989): nonlinear terms by the low-storage RK3 as in the
+ * explicit branch, viscous terms by the Crank-Nicolson-like pair alpha_k
+ * (explicit part) and beta_k (implicit part), so that each substep solves
+ *   (d2/dy2 - k^2 - Re/(beta_k Dt)) f_new =
+ *       -Re/beta_k (gama_k h + zeta_{k-1} h_old + alpha_k nu lap f + f/Dt)
+ * per (kx, kz) line with the shear phase of t + c_k Dt.  hv, hg, rf0u, rf0w are
+ * the assembled right-hand sides; on return vorwk, phiwk, u00wk, w00wk hold the
+ * zeta stores of the next substep and hg holds v = lapcdy(phi). */
+static const double ALPHA[3] = {29.0 / 96.0, -3.0 / 40.0, 1.0 / 6.0};
+static const double IBETA[3] = {160.0 / 37.0, 24.0 / 5.0, 6.0};
+static void implicit_substep(ctx *c, int rkstep, double Deltat, double r1, double xoffb,
+                             double xofft, double u00b, double u00t, double *xwkb,
+                             double *xwkt, double *vor, double *phi, double *u00, double *w00,
+                             double *hv, double *hg, double *vorwk, double *phiwk,
+                             double *u00wk, double *w00wk, const double *rf0u,
+                             const double *rf0w, double *ddu, double *wk1dr, cplx *shwkb,
+                             cplx *shwkt) {
+  int my = c->my, nkx = c->nkx, mz = c->mz, mx1 = c->mx1;
+  size_t nfield = 2 * (size_t)my * nkx * mz;
+  double s = c->p.s, Re = c->p.Re;
+  double gk = GAMA[rkstep - 1], zk = ZETA[rkstep - 1];
+  /* (2) gama_k [hv, hg] -> [phiwk, vorwk] (cross.f90:800-811) */
+  if (rkstep == 1) {
+    for (size_t q = 0; q < nfield; q++) {
+      vorwk[q] = gk * hg[q];
+      phiwk[q] = gk * hv[q];
+    }
+  } else {
+    for (size_t q = 0; q < nfield; q++) {
+      vorwk[q] = vorwk[q] + gk * hg[q];
+      phiwk[q] = phiwk[q] + gk * hv[q];
+    }
+  }
+  /* (3) alpha_k nu lap [vor, phi] -> ++[vorwk, phiwk] with the phase of t
+   * (cross.f90:812-828) */
+  double fac = ALPHA[rkstep - 1] * (1.0 / Re);
+#pragma omp parallel for schedule(static)
+  for (int ik = 0; ik < nkx * mz; ik++) {
+    int i = ik % nkx, k = ik / nkx;
+    if (i != 0 || k != 0) {
+      ythread *t = &c->yt[my_thread()];
+      double rk = c->gam2[k] + c->alp2[i];
+      double *scr = ddu + 2 * (size_t)my * ik;
+      visc3d(c, t, PEN(vor, i, k), PEN(vorwk, i, k), scr, shwkt[i], shwkb[i], 2, rk, fac, 1);
+      visc3d(c, t, PEN(phi, i, k), PEN(phiwk, i, k), scr, shwkt[i], shwkb[i], 2, rk, fac, 0);
+    }
+  }
+  /* (2*, 3*) the mean profiles (cross.f90:830-845) */
+  if (rkstep == 1) {
+    for (int j = 0; j < my; j++) {
+      u00wk[j] = gk * rf0u[j];
+      w00wk[j] = gk * rf0w[j];
+    }
+  } else {
+    for (int j = 0; j < my; j++) {
+      u00wk[j] = u00wk[j] + gk * rf0u[j];
+      w00wk[j] = w00wk[j] + gk * rf0w[j];
+    }
+  }
+  cplx one = C(1.0, 0.0);
+  visc3d(c, &c->yt[0], u00, u00wk, wk1dr, one, one, 1, 0.0, fac, 0);
+  visc3d(c, &c->yt[0], w00, w00wk, wk1dr, one, one, 1, 0.0, fac, 0);
+  /* (4) + [vor, phi]/Dt, (6) times -Re/beta_k (cross.f90:847-867) */
+  for (size_t q = 0; q < nfield; q++) {
+    vorwk[q] = vorwk[q] + (1.0 / Deltat) * vor[q];
+    phiwk[q] = phiwk[q] + (1.0 / Deltat) * phi[q];
+  }
+  double fb = -Re * IBETA[rkstep - 1];
+  for (size_t q = 0; q < nfield; q++) {
+    vorwk[q] = fb * vorwk[q];
+    phiwk[q] = fb * phiwk[q];
+  }
+  for (int j = 0; j < my; j++) {
+    u00wk[j] = fb * (u00wk[j] + (1.0 / Deltat) * u00[j]);
+    w00wk[j] = fb * (w00wk[j] + (1.0 / Deltat) * w00[j]);
+  }
+  /* (7) shear-periodic boundary at t + c_k Dt (cross.f90:869-884) */
+  if (fabs(s) > 0.5) {
+    *xwkb = xoffb + r1 * u00b;
+    *xwkt = xofft + r1 * u00t;
+    for (int i = 0; i <= mx1; i++) {
+      double a = c->xalp_im[i];
+      shwkb[i] = C(cos((-a) * *xwkb), sin((-a) * *xwkb));
+      shwkt[i] = C(cos((-a) * *xwkt), sin((-a) * *xwkt));
+    }
+  }
+  /* (8) right-hand sides to the frame of t + c_k Dt, Helmholtz solves
+   * (cross.f90:886-925) */
+  {
+    double mf = (rkstep == 1) ? -(s * r1) : -(s * (CA[rkstep - 1] - CA[rkstep - 2]) * Deltat);
+    moving_frame(c, vorwk, phiwk, mf);
+  }
+  double dtr = Re / Deltat, dtr1 = dtr * IBETA[rkstep - 1];
+#pragma omp parallel for schedule(static)
+  for (int ik = 0; ik < nkx * mz; ik++) {
+    int i = ik % nkx, k = ik / nkx;
+    if (i != 0 || k != 0) {
+      double rk = c->gam2[k] + c->alp2[i], rk2 = dtr1 + rk;
+      lapcdy(c, &c->yt[my_thread()], PEN(vorwk, i, k), rk2, PEN(vor, i, k), shwkt[i], shwkb[i],
+             2);
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (int ik = 0; ik < nkx * mz; ik++) {
+    int i = ik % nkx, k = ik / nkx;
+    if (i != 0 || k != 0) {
+      double rk = c->gam2[k] + c->alp2[i], rk2 = dtr1 + rk;
+      lapcdy(c, &c->yt[my_thread()], PEN(phiwk, i, k), rk2, PEN(phi, i, k), shwkt[i], shwkb[i],
+             2);
+    }
+  }
+  /* (9) zeta stores (cross.f90:927-941) */
+  if (rkstep != 3) {
+    for (size_t q = 0; q < nfield; q++) {
+      vorwk[q] = zk * hg[q];
+      phiwk[q] = zk * hv[q];
+    }
+    double mf = (rkstep == 1) ? -(GAMA[0] * Deltat * s) : -((GAMA[1] + ZETA[0]) * Deltat * s);
+    moving_frame(c, vorwk, phiwk, mf);
+  }
+  /* v = lapcdy(phi) (cross.f90:942-956) */
+#pragma omp parallel for schedule(static)
+  for (int ik = 0; ik < nkx * mz; ik++) {
+    int i = ik % nkx, k = ik / nkx;
+    if (i != 0 || k != 0) {
+      double rk = c->gam2[k] + c->alp2[i];
+      lapcdy(c, &c->yt[my_thread()], PEN(phi, i, k), rk, PEN(hg, i, k), shwkt[i], shwkb[i], 2);
+    }
+  }
+  /* (8*, 9*) the mean profiles (cross.f90:960-975) */
+  lapcdy(c, &c->yt[0], u00wk, dtr1, u00, one, one, 1);
+  lapcdy(c, &c->yt[0], w00wk, dtr1, w00, one, one, 1);
+  if (rkstep != 3) {
+    for (int j = 0; j < my; j++) {
+      u00wk[j] = zk * rf0u[j];
+      w00wk[j] = zk * rf0w[j];
+    }
+  }
+}
+
 /* moving_frame_t (operators.f90:147-196): the same phase on one field */
 static void moving_frame_t(ctx *c, double *temp, double mtime) {
   int my = c->my, nkx = c->nkx, mz = c->mz;
@@ -1870,6 +2011,9 @@ static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00,
                      double *tb00, double *ptime, double *pxoffb, double *pxofft, int nstep,
                      double *trace, int *ntrace, int *pistop, double *pdeltat) {
   int my = c->my, nkx = c->nkx, mz = c->mz, mx1 = c->mx1;
+  /* the semi-implicit branch is restated for cross without LES
+   * (initcr.f90:2179-2182 stops there) */
+  if (c->p.implicit_visc && (c->p.les || tb != NULL)) return -1;
   size_t nfield = 2 * (size_t)my * nkx * mz; /* doubles per pencil field */
   size_t nplane = (size_t)nkx * mz;
   double s = c->p.s, Ly = c->p.Ly, Re = c->p.Re;
@@ -2144,7 +2288,8 @@ static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00,
               /* crosst.f90:1236-1257 */
               CFLk = CFL * c->cflkk * dt;
               if (CFLv > CFL) dt = (CFLk > CFLv) ? 1.0 / c->cflkk : 1.0 / c->cflvv;
-            } else if (CFLv > CFL) {
+            } else if (CFLv > CFL && !c->p.implicit_visc) {
+              /* the viscous limit of the explicit branch only (cross.f90:1669) */
               dt = 1.0 / c->cflvv;
             }
           }
@@ -2280,6 +2425,12 @@ static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00,
           rf0u[j] = rf0u[j] + txy00[j];
           rf0w[j] = rf0w[j] + tyz00[j];
         }
+      }
+      if (c->p.implicit_visc) {
+        implicit_substep(c, rkstep, Deltat, r1, xoffb, xofft, u00b, u00t, &xwkb, &xwkt, vor,
+                         phi, u00, w00, hv, hg, vorwk, phiwk, u00wk, w00wk, rf0u, rf0w, ddu,
+                         wk1dr, shwkb, shwkt);
+        continue;
       }
       if (!les || c->p.les_visc) {
 #pragma omp parallel for schedule(static)

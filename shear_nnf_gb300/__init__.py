@@ -43,6 +43,7 @@ class SbParams(ctypes.Structure):
         ("gbeta", ctypes.c_double),
         ("damping", ctypes.c_int), ("damp_up", ctypes.c_double), ("damp_aa", ctypes.c_double),
         ("force", ctypes.c_int), ("force_roll", ctypes.c_double), ("xforce", ctypes.c_double),
+        ("implicit_visc", ctypes.c_int),
     ]
 
 
@@ -215,11 +216,11 @@ def make_params(mgalx, my, mgalz, Re, alp, Ly, gam, s=1.0, chi=0.0, CFL=0.5, vbu
                 fixed_dt=0.0, readflag=1, uprim=1.0, nhist=1, etime=1e10, dumptime=1e10,
                 dtimag=1e10, keep_laminar=0, les=0, les_visc=1, cs=0.1, ydeal=0, temperature=0,
                 fkappa=0.0, bym=0.0, gbeta=0.0, damping=0, damp_up=0.0, damp_aa=0.0, force=0,
-                force_roll=0.0, xforce=0.0) -> SbParams:
+                force_roll=0.0, xforce=0.0, implicit_visc=0) -> SbParams:
     return SbParams(mgalx, my, mgalz, Re, alp, Ly, gam, s, chi, CFL, vbulk, fixed_dt, readflag,
                     uprim, nhist, etime, dumptime, dtimag, keep_laminar, les, les_visc, cs, ydeal,
                     temperature, fkappa, bym, gbeta, damping, damp_up, damp_aa, force,
-                    force_roll, xforce)
+                    force_roll, xforce, implicit_visc)
 
 
 def sizes(p: SbParams) -> dict:
@@ -369,7 +370,7 @@ class ShearBox:
         f = ctypes.c_int(0)
         _check(lib().sb_get_line_form(self.h, ctypes.byref(f)))
         return {"p1_cols": c[0], "p3_cols": c[1], "p2_threads": c[2], "line_segments": c[3],
-                "line_form": "fused" if f.value else "split"}
+                "line_form": ("split", "fused", "implicit")[f.value]}
 
     def set_line_segments(self, nseg: int):
         """Warps per y-line solve, 1..3 (sb_set_line_segments)."""
@@ -581,7 +582,7 @@ def params_from_restart(info: SbRestartInfo, **overrides) -> SbParams:
     """Step parameters recorded by a restart file: grid, Re, alp, Ly, gam, s, chi
     from the header and, with a footer, CFL, uprim, vbulk and the switches and
     parameters escru writes (ifix_dt with the Delta t as fixed_dt, iadd_force,
-    force_roll, xforce, iadd_damping, damp_aa, damp_up, iuse_LES, iadd_visc,
+    force_roll, xforce, iadd_damping, damp_aa, damp_up, iuse_LES, iadd_visc, explicit,
     Cles; readwrite.f90:1336-1398).  Keyword arguments override any of them
     (the hre2.dat/hre3.dat settings of the run that reads the file)."""
     kw = dict(mgalx=info.mgalx, my=info.my, mgalz=info.mgalz, Re=info.Re, alp=info.alp,
@@ -594,7 +595,8 @@ def params_from_restart(info: SbRestartInfo, **overrides) -> SbParams:
             if opt[1]:
                 kw["fixed_dt"] = prm[0]
             kw.update(force=opt[2], force_roll=prm[1], xforce=prm[2], damping=opt[5],
-                      damp_aa=prm[4], damp_up=prm[5], les=opt[6], les_visc=opt[7])
+                      damp_aa=prm[4], damp_up=prm[5], les=opt[6], les_visc=opt[7],
+                      implicit_visc=0 if opt[0] else 1)
             if opt[6]:
                 kw["cs"] = prm[6]
     kw.update(overrides)

@@ -21,7 +21,7 @@ UNITS = [("sb_kernels.cu", ["-DSB_FLOAT_TU=0"]), ("sb_kernels.cu", ["-DSB_FLOAT_
          # the y-line kernels once per (warps per line solve, precision)
          *[("sb_yline.cu", [f"-DSB_FLOAT_TU={f}", f"-DSB_KSEG={k}"]) for k in (1, 2, 3)
            for f in (0, 1)],
-         ("sb_box.cu", []),
+         ("sb_box.cu", []), ("sb_implicit.cu", []),
          ("sb_ops.cu", []), ("sb_noalloc.cu", []), ("sb_api.cu", []), ("sb_krylov.cu", []),
          # host set-up (coefficients, factorisations, the seeded field) without
          # fused multiply-adds: the same bits on x86 and Arm hosts

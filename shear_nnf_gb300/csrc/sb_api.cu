@@ -123,6 +123,12 @@ static int check_params(const sb_params *p) {
     return fail(2, "iadd_damping=%d not available (0, 1)", p->damping);
   if (p->force < -1 || p->force > 2)
     return fail(2, "iadd_force=%d not available (-1, 0, 1, 2)", p->force);
+  if (p->implicit_visc != 0 && p->implicit_visc != 1)
+    return fail(2, "implicit_visc=%d not available (0, 1)", p->implicit_visc);
+  // LES with explicit = 0 stops the reference (initcr.f90:2179-2182); the
+  // semi-implicit kernels cover the plain step
+  if (p->implicit_visc && (p->les || p->temperature || p->ydeal))
+    return fail(2, "implicit_visc needs les = temperature = ydeal = 0");
   if (!(p->Re != 0.0) || !(p->alp > 0) || !(p->gam > 0) || !(p->Ly > 0) || !(p->CFL > 0))
     return fail(1, "invalid physical parameters");
   return 0;
@@ -270,6 +276,27 @@ static int build_line_tables(sb_handle *h, int nseg) {
     }
     H.stride = nl;
   }
+  if (g.impl) {
+    // the semi-implicit Helmholtz tables, filled by k_hfac every substep:
+    // boxes x (lines + the mean line)
+    const size_t n = g.my, L = (size_t)g.B * (nl + 1);
+    Fac &I = bf.hi;
+    double *q[17];
+    const size_t cnt[17] = {n * L, n * L, n * L, n * L, n * L, n * L, n * L, n * L, 10 * L,
+                            n * L, n * L, n * L, n * L, n * L, n * L, 9 * (size_t)g.nseg * L,
+                            16 * n * L};
+    for (int t = 0; t < 17; t++)
+      if ((rc = dalloc(h, &q[t], cnt[t]))) return rc;
+    I.La = q[0]; I.Lb = q[1]; I.Lc = q[2]; I.Ddm1 = q[3]; I.Dd = q[4];
+    I.e = q[5]; I.f = q[6]; I.g = q[7]; I.sums = q[8];
+    for (int t = 0; t < 3; t++) {
+      I.hf[t] = q[9 + t];
+      I.hb[t] = q[12 + t];
+    }
+    I.ef = q[15];
+    I.rows = q[16];
+    I.stride = (long)L;
+  }
   if (prepare_line(g) != cudaSuccess)
     return fail(3, "line kernel attributes: %s", cudaGetErrorString(cudaGetLastError()));
   return 0;
@@ -336,6 +363,7 @@ static int capture_step(sb_handle *h) {
           (e = cudaStreamWaitEvent(h->side, h->ev_fork, 0)) != cudaSuccess ||
           (e = launch_scalar(h->g, h->bf, rk, h->side)) != cudaSuccess ||
           (e = launch_tables(h->g, h->bf, rk, h->side)) != cudaSuccess ||
+          (h->g.impl && (e = launch_hfac(h->g, h->bf, rk, h->side)) != cudaSuccess) ||
           (e = cudaEventRecord(h->ev_join, h->side)) != cudaSuccess ||
           (e = launch_plane(h->g, h->bf, 3, rk, h->st)) != cudaSuccess ||
           (e = cudaStreamWaitEvent(h->st, h->ev_join, 0)) != cudaSuccess)
@@ -348,6 +376,10 @@ static int capture_step(sb_handle *h) {
       if ((e = launch_tables(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
     }
     if (h->g.les && (e = launch_lineL(h->g, h->bf, h->st)) != cudaSuccess) break;
+    if (h->g.impl) {
+      e = launch_lineI(h->g, h->bf, rk, h->st);
+      continue;
+    }
     if (h->g.lform && line_fused_ok(h->g)) {
       e = launch_lineF(h->g, h->bf, rk, h->st);
       continue;
@@ -504,6 +536,7 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   g.cbl = les_cb(p->mgalz);
   g.ncbl = (g.nkx + g.cbl - 1) / g.cbl;
   g.ydeal = p->ydeal;
+  g.impl = p->implicit_visc ? 1 : 0;
   g.my23 = 2 * (p->my / 3);  // initcr.f90:207-210
   g.ny1 = ((g.my23 - 1) - 1) / 2;
   g.ny2 = p->my - g.ny1;
@@ -649,6 +682,10 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
   if ((rc = build_line_tables(h, g.nseg))) {
     sb_destroy(h);
     return rc;
+  }
+  if (g.impl && !line_implicit_ok(g)) {
+    sb_destroy(h);
+    return fail(2, "implicit_visc: my=%d too large for the semi-implicit y-line block", g.my);
   }
   h->mem_init.resize(B);
   for (size_t b = 0; b < B; b++) member_defaults(p, g, p->Re, &h->mem_init[b]);
@@ -1035,10 +1072,11 @@ void *sb_get_stream(sb_handle *h) { return h ? (void *)h->st : nullptr; }
 
 int sb_launch_stage(sb_handle *h, int stage, int rk, int count) {
   if (!h || count < 0) return fail(1, "bad argument");
-  if (stage < 1 || stage > 12 || rk < 1 || rk > 3) return fail(1, "stage 1..12, rk 1..3");
+  if (stage < 1 || stage > 14 || rk < 1 || rk > 3) return fail(1, "stage 1..14, rk 1..3");
   if (stage >= 7 && stage <= 11 && !h->g.les) return fail(1, "stages 7..11 need an LES handle");
   if (stage == 12 && !line_fused_ok(h->g))
     return fail(1, "stage 12 (fused y-line kernel) not available for this handle");
+  if (stage >= 13 && !h->g.impl) return fail(1, "stages 13, 14 need an implicit_visc handle");
   for (int q = 0; q < count; q++) {
     cudaError_t e;
     if (stage <= 3)
@@ -1053,8 +1091,12 @@ int sb_launch_stage(sb_handle *h, int stage, int rk, int count) {
       e = launch_les(h->g, h->bf, stage - 5, rk, h->st);
     else if (stage == 11)
       e = launch_lineL(h->g, h->bf, h->st);
-    else
+    else if (stage == 12)
       e = launch_lineF(h->g, h->bf, rk, h->st);
+    else if (stage == 13)
+      e = launch_hfac(h->g, h->bf, rk, h->st);
+    else
+      e = launch_lineI(h->g, h->bf, rk, h->st);
     if (e != cudaSuccess) return fail(3, "launch: %s", cudaGetErrorString(e));
   }
   return 0;
@@ -1234,7 +1276,7 @@ int sb_set_line_form(sb_handle *h, int form) {
 
 int sb_get_line_form(sb_handle *h, int *form) {
   if (!h || !form) return fail(1, "null argument");
-  *form = (h->g.lform && line_fused_ok(h->g)) ? 1 : 0;
+  *form = h->g.impl ? 2 : ((h->g.lform && line_fused_ok(h->g)) ? 1 : 0);
   return 0;
 }
 

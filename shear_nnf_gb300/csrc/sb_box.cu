@@ -270,7 +270,8 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
         // does (crosst.f90:1236-1257)
         const double CFLk = M.CFL * M.cflkk * dt;
         if (M.CFLv > M.CFL) dt = (CFLk > M.CFLv) ? 1.0 / M.cflkk : 1.0 / M.cflvv;
-      } else if (M.CFLv > M.CFL) {
+      } else if (M.CFLv > M.CFL && !g.impl) {
+        // the viscous limit of the explicit branch only (cross.f90:1669)
         dt = 1.0 / M.cflvv;
       }
     }
@@ -491,6 +492,8 @@ cudaError_t launch_finish(const Grid &g, const Bufs &bf, cudaStream_t st) {
   cudaError_t lineF_f64(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);           \
   cudaError_t lineF_f32(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);           \
   bool lineF_fits_f64(const Grid &g);                                                      \
+  cudaError_t lineI_f64(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);           \
+  cudaError_t lineI_f32(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);           \
   bool lineF_fits_f32(const Grid &g);                                                      \
   cudaError_t lineL_f64(const Grid &g, const Bufs &bf, cudaStream_t st);                   \
   cudaError_t lineL_f32(const Grid &g, const Bufs &bf, cudaStream_t st);                   \
@@ -542,9 +545,14 @@ cudaError_t launch_lineF(const Grid &g, const Bufs &bf, int rk, cudaStream_t st)
 // the fused y-line kernel covers the plain step: no temperature, no y filter
 // or y dealiasing, and its block's shared memory fits
 bool line_fused_ok(const Grid &g) {
-  if (g.temp || g.ydeal) return false;
+  if (g.temp || g.ydeal || g.impl) return false;
   SB_SEG_CALL(lineF_fits, g)
 }
+cudaError_t launch_lineI(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  SB_SEG_CALL(lineI, g, bf, rk, st)
+}
+// k_lineI has k_lineF's block (two pipelines): the same shared memory
+bool line_implicit_ok(const Grid &g) { SB_SEG_CALL(lineF_fits, g) }
 cudaError_t launch_lineL(const Grid &g, const Bufs &bf, cudaStream_t st) {
   SB_SEG_CALL(lineL, g, bf, st)
 }

@@ -62,6 +62,7 @@ struct Grid {
   int nlines_pad;        // component lines per member, padded to whole warps
   int nseg, slo[4], shi[4];  // segments of the banded rows of the y-solves
   int lform;             // y-line kernels of a substep: 0 k_lineA + k_lineB, 1 k_lineF
+  int impl;              // 1: semi-implicit viscous terms (explicit = 0): k_hfac + k_lineI
   int ngrp;              // groups of 16 lines per member in the y-line kernels
   // Smagorinsky LES (cross.f90:1291-1406): on/off, molecular viscosity kept,
   // (Cles * Deltag)^2, fields per z row of zbuf (6, or 10 with the model),
@@ -146,6 +147,8 @@ struct Bufs {
   const double *ginv;            // 1/g per kz  (g = gam * kz_signed; 0 at k=0)
   const double *kinv;            // 1/(alp2+gam2) per (k,i); 0 at (0,0)
   Fac d1, d2, hz;                // d/dy, d2/dy2, Helmholtz (per line)
+  Fac hi;                        // semi-implicit Helmholtz (k^2 + dtr1) per box and line,
+                                 // line slot nkx*mz the mean line; rebuilt every substep
   Fac flt;                       // left-hand side of the compact y-filter
   const double *twy;             // y-transform twiddles (iydealiasing 1, 2), factored form
   const float *twyf;

@@ -178,7 +178,7 @@ int sb_write_restart(const char *path, const sb_params *p, const double *vor, co
   flush();
   put_i32(r, 1742); put_i32(r, 9); put_i32(r, 13);  // irev (mod.f90:45), nopt, nparams
   flush();
-  const int opts[9] = {1, p->fixed_dt > 0 ? 1 : 0, p->force, 5, 0, p->damping,
+  const int opts[9] = {p->implicit_visc ? 0 : 1, p->fixed_dt > 0 ? 1 : 0, p->force, 5, 0, p->damping,
                        p->les ? 1 : 0, p->les_visc ? 1 : 0, 0};
   for (int q = 0; q < 9; q++) put_i32(r, opts[q]);
   flush();

@@ -35,6 +35,11 @@ cudaError_t launch_lineB(const Grid &g, const Bufs &bf, int mode, cudaStream_t s
 // k_lineB, where line_fused_ok(g)
 cudaError_t launch_lineF(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
 bool line_fused_ok(const Grid &g);
+// the semi-implicit viscous branch: factor tables of the substep (k_hfac)
+// and the y-line kernel (k_lineI)
+cudaError_t launch_hfac(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
+cudaError_t launch_lineI(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
+bool line_implicit_ok(const Grid &g);
 cudaError_t launch_setconj(const Grid &g, const Bufs &bf, cudaStream_t st);
 cudaError_t launch_scalar(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);
 cudaError_t launch_tables(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);

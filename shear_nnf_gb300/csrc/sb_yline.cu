@@ -677,6 +677,222 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineF(Grid g, Bufs bf, int rk1
   }
 }
 
+// ---------------------------------------------------------------------------
+// k_lineI: the y-line work of one substep of the semi-implicit viscous branch
+// (explicit = 0, cross.f90:797-989), for the plain step (no LES, temperature,
+// y filter or y dealiasing).  Same block layout as k_lineF (two pipelines of
+// kSeg warps on 16 lines), five phases:
+//   phase  pipeline 0 (omega_y)                 pipeline 1 (phi)
+//   1      T = d/dy(dH1/dx + dH3/dz)            S = d2(phi)/dy2
+//   2      right-hand side of the Helmholtz     the same for phi with
+//          equation (below) -> T buffer,        hv - T -> S buffer,
+//          zeta store -> vorwk                  zeta store -> phiwk
+//   3      omega_y = lapcdy(rhs, k^2 + dtr1)    phi = lapcdy(rhs, k^2 + dtr1)
+//   4      d(omega_y)/dy -> D                   v = lapcdy(phi, k^2) -> G
+//   5      d2(omega_y)/dy2 -> Lv                dv/dy -> V
+// with, per point (cross.f90:800-867, in this order),
+//   wk = [wk +] gama_k h;  wk += alpha_k nu (f'' - k^2 f);  wk += f/Dt;
+//   rhs = -Re ibeta_k wk,  moved to the frame of t + c_k Dt (moving_frame);
+// and the Helmholtz factors of k^2 + dtr1 (dtr1 = Re ibeta_k / Dt) built for
+// this substep by k_hfac.  The mean block (pipeline 0): nu u00'' in phase 1,
+// the mean right-hand side in phase 2 (through mdu), the real Helmholtz solve
+// of dtr1 in phase 3, du00/dy in phase 4.  The (0,0) line keeps its state
+// (cross.f90 skips it).
+__device__ __constant__ static const double kAlpha[3] = {29.0 / 96.0, -3.0 / 40.0, 1.0 / 6.0};
+__device__ __constant__ static const double kIbetaL[3] = {160.0 / 37.0, 24.0 / 5.0, 6.0};
+
+template <typename R>
+__global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1) {
+  __shared__ double xch[2][kSeg][16][2][SB_XS];
+  LineThread L;
+  int pipe = 0;
+  if (!line_thread_f(g, &L, &pipe)) return;  // whole blocks
+  Member &M = bf.mem[L.b];
+  if (M.halted) return;  // uniform per block
+  const int N = g.my, ystr = blockDim.x;
+  const int rk = rk1 - 1;
+  double *ys = ycol();
+  const FacView V1(bf.d1, 0), V2(bf.d2, 0);
+  const SegView W1(bf.d1, 0), W2(bf.d2, 0);
+  const double Dt = M.Deltat, nu = M.nu;
+  const double fa = kAlpha[rk] * nu, fb = -M.Re * kIbetaL[rk], rdt = 1.0 / Dt;
+  const R gk = (R)kGama[rk], zk = (R)kZeta[rk];
+  const int nl = g.nkx * g.mz;
+  const long hline0 = (long)L.b * (nl + 1);  // this box's first line of the implicit factors
+  if (L.mean) {
+    R *mu = (R *)bf.mu + (long)L.b * 2 * N + L.c;
+    R *mdu = (R *)bf.mdu + (long)L.b * 2 * N + L.c;
+    const cd one = mk(1.0, 0.0);
+    // phase 1: u00'' (visc3d(u00, u00wk, m=1, rk=0), cross.f90:842-845)
+    if (pipe == 0) {
+      const TailLoad T2{bf.tl2o + (long)L.b * g.nkx * SB_TAIL};
+      SEG_SOLVE_P(mu, 2, V2, W2, T2, one, one, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6], false);
+    } else {
+      seg_idle();
+    }
+    __syncthreads();
+    // phase 2: forcing, damping, the mean right-hand side -> mdu and the zeta
+    // store (cross.f90:622-626,830-867,972-975)
+    if (pipe == 0) {
+      R *mwk = (R *)bf.mwk + (long)L.b * 2 * N + L.c;
+      const R *mrf = (const R *)bf.mrf + (long)L.b * 2 * N + L.c;
+      const bool damp = g.damp && L.c == 0;
+      const bool xf = g.force == -1 && L.c == 0;
+      for (int i = L.r0; i <= L.r1; i++) {
+        const int j = i - 1;
+        R rf0 = mrf[2 * j];
+        if (xf) rf0 = (R)((double)rf0 + g.xforce);
+        if (damp) {
+          const double y = (double)j * g.dy - 0.5 * g.Ly;
+          const double hw = 1.0 - (0.25 * (1.0 + tanh(6.0 * (g.damp_a - y) / g.lz + 3.0))) *
+                                      (1.0 + tanh(6.0 * (g.damp_a + y) / g.lz + 3.0));
+          rf0 = (R)((double)rf0 - g.damp_up * hw * (double)mu[2 * j]);
+        }
+        const R wk = (rk == 0) ? gk * rf0 : mwk[2 * j] + gk * rf0;
+        double w = (double)wk;
+        w = w + fa * (-(0.0 * (double)mu[2 * j]) + ys[(i - L.r0) * ystr]);
+        const double rhs = fb * (w + rdt * (double)mu[2 * j]);
+        if (L.active) {
+          mdu[2 * j] = (R)rhs;
+          if (rk < 2) mwk[2 * j] = zk * rf0;
+        }
+      }
+    }
+    __syncthreads();
+    // phase 3: u00 = lapcdy(rhs, dtr1) (cross.f90:965-967), real lines
+    if (pipe == 0) {
+      const FacView VI(bf.hi, hline0 + nl);
+      const SegView WI(bf.hi, hline0 + nl);
+      const TailMake TI{VI, one, N};
+      SEG_SOLVE_P((const R *)mdu, 2, VI, WI, TI, one, one, g.pr2[3], g.pr2[4], g.pr2[5], g.pr2[6],
+                  false);
+      store_col(ys, ystr, mu, 2, L);
+    } else {
+      seg_idle();
+    }
+    __syncthreads();
+    // phase 4: du00/dy, dw00/dy of the new profiles (cross.f90:1186-1192)
+    if (pipe == 0) {
+      const TailLoad T1{bf.tl1o + (long)L.b * g.nkx * SB_TAIL};
+      SEG_SOLVE_P(mu, 2, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true);
+      store_col(ys, ystr, mdu, 2, L);
+    } else {
+      seg_idle();
+    }
+    __syncthreads();
+    seg_idle();  // phase 5
+    return;
+  }
+  const long off = (long)L.b * g.field + 2 * L.lc + L.c;
+  const long ps = g.plane;
+  const int i = L.i, k = L.k;
+  const bool is00 = (i == 0 && k == 0);
+  const double a = g.alp * i;
+  const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz);
+  const double k2 = gz * gz + a * a;
+  const double *mf1 = bf.mf1 + (long)L.b * 2 * N * g.nkx + 2 * i;
+  const double *mf2 = bf.mf2 + (long)L.b * 2 * N * g.nkx + 2 * i;
+  {
+    // phase 1 at the phase of time t
+    const cd shp = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * i);
+    const cd shm = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
+    if (pipe == 0) {
+      // T = d/dy (dH1/dx + dH3/dz) (cross.f90:565-575), as k_lineA stores it
+      const TailLoad T1{bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL};
+      SEG_SOLVE_P((const R *)bf.D + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
+                  g.rh1[6], true);
+      for (int r = L.r0; r <= L.r1; r++)
+        ys[(r - L.r0) * ystr] = (double)(R)ys[(r - L.r0) * ystr];
+    } else {
+      // S = d2(phi)/dy2 (visc3d, cross.f90:824)
+      const TailLoad T2{bf.tl2o + ((long)L.b * g.nkx + i) * SB_TAIL};
+      SEG_SOLVE_P((const R *)bf.phi + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4],
+                  g.rh2[5], g.rh2[6], false);
+    }
+  }
+  __syncthreads();
+  {
+    // phase 2: right-hand sides of the Helmholtz equations and the zeta
+    // stores (cross.f90:800-867,886-941); omega_y'' from Lv, taken at the end
+    // of the previous substep (or by the prologue)
+    const R *h0 = pipe ? (const R *)bf.V + off : (const R *)bf.G + off;
+    R *f = pipe ? (R *)bf.phi + off : (R *)bf.vor + off;
+    R *fwk = pipe ? (R *)bf.phiwk + off : (R *)bf.vorwk + off;
+    R *rhs_out = pipe ? (R *)bf.S + off : (R *)bf.T + off;
+    const R *lv = (const R *)bf.Lv + off;
+    const double *ys0 = ys - 32 * kSeg * pipe;  // pipeline 0's column (T)
+    const int c = L.c;
+#pragma unroll 2
+    for (int r = L.r0; r <= L.r1; r++) {
+      const int j = r - 1;
+      const long q = (long)j * ps;
+      R h = h0[q];
+      if (pipe) h = h - (R)ys0[(r - L.r0) * ystr];  // hv = hv - d/dy(...)
+      const R fo = f[q];
+      const R wk = (rk == 0) ? gk * h : fwk[q] + gk * h;
+      const double d2 = pipe ? ys[(r - L.r0) * ystr] : (double)lv[q];
+      double w = (double)wk;
+      if (!is00) w = w + fa * (-(k2 * (double)fo) + d2);
+      w = fb * (w + rdt * (double)fo);
+      const cd m2 = ldc2(mf2 + (long)j * 2 * g.nkx);
+      const double rm = cmul_c(w, __shfl_xor_sync(0xffffffffu, w, 1), m2, c);
+      double zs = 0.0;
+      if (rk < 2) {
+        const cd m1 = ldc2(mf1 + (long)j * 2 * g.nkx);
+        const double wz = (double)(zk * h);
+        zs = cmul_c(wz, __shfl_xor_sync(0xffffffffu, wz, 1), m1, c);
+      }
+      if (L.active) {
+        rhs_out[q] = (R)rm;
+        if (rk < 2) fwk[q] = (R)zs;
+      }
+    }
+  }
+  __syncthreads();
+  // phases 3-5 at the phase of time t + c_k dt
+  const cd shp = ldc2(bf.sh_new + (long)L.b * 4 * g.nkx + 2 * i);
+  const cd shm = ldc2(bf.sh_new + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
+  {
+    // phase 3: the Helmholtz solves (cross.f90:894-925)
+    const FacView VI(bf.hi, hline0 + L.lc);
+    const SegView WI(bf.hi, hline0 + L.lc);
+    const TailMake TI{VI, shp, N};
+    const R *src = pipe ? (const R *)bf.S + off : (const R *)bf.T + off;
+    SEG_SOLVE_P(src, ps, VI, WI, TI, shp, shm, g.pr2[3], g.pr2[4], g.pr2[5], g.pr2[6], false);
+    if (!is00) store_col(ys, ystr, pipe ? (R *)bf.phi + off : (R *)bf.vor + off, ps, L);
+  }
+  __syncthreads();  // whole updated lines are read below
+  const TailLoad T1{bf.tl1n + ((long)L.b * g.nkx + i) * SB_TAIL};
+  if (pipe == 0) {
+    // d(omega_y)/dy (cross.f90:440)
+    SEG_SOLVE_P((const R *)bf.vor + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
+                g.rh1[6], true);
+    store_col(ys, ystr, (R *)bf.D + off, ps, L);
+  } else {
+    // v = lapcdy(phi, k^2) (cross.f90:942-956); hg(0,0) keeps the value the
+    // nonlinear stage left (zero)
+    const FacView VH(bf.hz, L.lc);
+    const SegView WH(bf.hz, L.lc);
+    const TailMake TH{VH, shp, N};
+    SEG_SOLVE_P((const R *)bf.phi + off, ps, VH, WH, TH, shp, shm, g.pr2[3], g.pr2[4], g.pr2[5],
+                g.pr2[6], false);
+    if (!is00) store_col(ys, ystr, (R *)bf.G + off, ps, L);
+  }
+  __syncthreads();  // v of all segments is read below
+  if (pipe == 0) {
+    // d2(omega_y)/dy2 of the next substep's starting state
+    const TailLoad T2{bf.tl2n + ((long)L.b * g.nkx + i) * SB_TAIL};
+    SEG_SOLVE_P((const R *)bf.vor + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
+                g.rh2[6], false);
+    store_col(ys, ystr, (R *)bf.Lv + off, ps, L);
+  } else {
+    // dv/dy (cross.f90:442)
+    SEG_SOLVE_P((const R *)bf.G + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
+                g.rh1[6], true);
+    store_col(ys, ystr, (R *)bf.V + off, ps, L);
+  }
+}
+
 // LES y-operators (iuse_LES, cross.f90:565-608,639-647), between k_tables and
 // k_lineA:
 //   role 0: hg += d(rhgc2)/dy                       (derivyc, -> G)
@@ -891,8 +1107,10 @@ cudaError_t SB_PSUF(prepare_line)(const Grid &g) {
   cudaFuncSetAttribute(k_lineL<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   cudaFuncSetAttribute(k_filter<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   cudaFuncSetAttribute(k_meand1<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  if (SB_PSUF(lineF_fits)(g))
+  if (SB_PSUF(lineF_fits)(g)) {
     cudaFuncSetAttribute(k_lineF<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * sm);
+    cudaFuncSetAttribute(k_lineI<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * sm);
+  }
   return cudaGetLastError();
 }
 
@@ -920,6 +1138,13 @@ cudaError_t SB_PSUF(lineF)(const Grid &g, const Bufs &bf, int rk, cudaStream_t s
   typedef SbR R;
   const unsigned nb = (unsigned)(g.B * (g.ngrp + 1));
   k_lineF<R><<<nb, 2 * kLineT, 2 * smem_of(g), st>>>(g, bf, rk);
+  return cudaGetLastError();
+}
+
+cudaError_t SB_PSUF(lineI)(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
+  typedef SbR R;
+  const unsigned nb = (unsigned)(g.B * (g.ngrp + 1));
+  k_lineI<R><<<nb, 2 * kLineT, 2 * smem_of(g), st>>>(g, bf, rk);
   return cudaGetLastError();
 }
 
