@@ -26,6 +26,16 @@
 #pragma once
 #include <type_traits>
 
+// Build-time choice of the FP64 stage order where a length has a radix-2
+// factor: 0 (default) radix 3, 4, ..., 2 last; 1 the radix-2 stage second
+// (for 192 = 3*4*4*4 plan 1 splits one radix-4 stage into two radix-2
+// stages).  The FP64 instruction count per point is the same for both (a
+// radix-2 layer costs 3 per point in the factored form, a radix-4 stage 6);
+// the stages differ in shared-memory strides and barrier count.
+#ifndef SB_FFT_PLAN
+#define SB_FFT_PLAN 0
+#endif
+
 #include "sb_common.cuh"
 
 namespace sb {
@@ -313,18 +323,38 @@ __device__ __forceinline__ double2 *fft_batch_g(double2 *A, double2 *B,
     gstage4<64, 4, SIGN, M, T>(B, A, G); __syncthreads();
     gstage4<64, 16, SIGN, M, T>(A, B, G); __syncthreads();
     return B;
+  } else if constexpr (N == 96 && SB_FFT_PLAN == 1) {
+    gstage3<96, SIGN, M, T, GAP>(A, B); __syncthreads();
+    gstage2<96, 3, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<96, 6, SIGN, M, T>(A, B, G); __syncthreads();
+    gstage4<96, 24, SIGN, M, T>(B, A, G); __syncthreads();
+    return A;
   } else if constexpr (N == 96) {
     gstage3<96, SIGN, M, T, GAP>(A, B); __syncthreads();
     gstage4<96, 3, SIGN, M, T>(B, A, G); __syncthreads();
     gstage4<96, 12, SIGN, M, T>(A, B, G); __syncthreads();
     gstage2<96, 48, SIGN, M, T>(B, A, G); __syncthreads();
     return A;
+  } else if constexpr (N == 192 && SB_FFT_PLAN == 1) {
+    gstage3<192, SIGN, M, T, GAP>(A, B); __syncthreads();
+    gstage2<192, 3, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<192, 6, SIGN, M, T>(A, B, G); __syncthreads();
+    gstage4<192, 24, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage2<192, 96, SIGN, M, T>(A, B, G); __syncthreads();
+    return B;
   } else if constexpr (N == 192) {
     gstage3<192, SIGN, M, T, GAP>(A, B); __syncthreads();
     gstage4<192, 3, SIGN, M, T>(B, A, G); __syncthreads();
     gstage4<192, 12, SIGN, M, T>(A, B, G); __syncthreads();
     gstage4<192, 48, SIGN, M, T>(B, A, G); __syncthreads();
     return A;
+  } else if constexpr (N == 384 && SB_FFT_PLAN == 1) {
+    gstage3<384, SIGN, M, T, GAP>(A, B); __syncthreads();
+    gstage2<384, 3, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<384, 6, SIGN, M, T>(A, B, G); __syncthreads();
+    gstage4<384, 24, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<384, 96, SIGN, M, T>(A, B, G); __syncthreads();
+    return B;
   } else if constexpr (N == 384) {
     gstage3<384, SIGN, M, T, GAP>(A, B); __syncthreads();
     gstage4<384, 3, SIGN, M, T>(B, A, G); __syncthreads();
