@@ -187,9 +187,10 @@ static int upload_uniform(sb_handle *h, Fac *F, const double a[7], int n) {
 
 // The factor tables of the y-line solves for a segment plan of nseg warps per
 // line: d/dy and d2/dy2 (and the y-filter), each the same for every line, and
-// the Helmholtz operator (rh2 - k^2 pr2) per (kx, kz) line (lapcdy,
-// diffy_shear_hepta.f90:466-525; line (0,0) is never solved and gets a
-// harmless k^2 = 1).  Replaces the tables of an earlier plan.
+// the Helmholtz operator (rh2 - k^2 pr2) per (kx, kz >= 0) line (lapcdy,
+// diffy_shear_hepta.f90:466-525; the kz < 0 lines use the entry of -kz, the
+// same k^2; line (0,0) is never solved and gets a harmless k^2 = 1).
+// Replaces the tables of an earlier plan.
 static int build_line_tables(sb_handle *h, int nseg) {
   Grid &g = h->g;
   Bufs &bf = h->bf;
@@ -222,47 +223,50 @@ static int build_line_tables(sb_handle *h, int nseg) {
       (g.ydeal == 3 && (rc = upload_uniform(h, &bf.flt, flhs, g.my))))
     return rc;
   {
+    // lines (kx, kz) and (kx, -kz) share k^2 and so their factors: the table
+    // holds the kz >= 0 lines only (hz_line maps a line to its entry)
+    const int nlh = g.nkx * (g.nz + 1);
     const size_t n = g.my;
-    std::vector<double> La(n * nl), Lb(n * nl), Lc(n * nl), Dm(n * nl), Dd(n * nl), e(n * nl),
-        f(n * nl), gg(n * nl), sums(10 * (size_t)nl);
-    std::vector<double> hf[3], hb[3], ef(9 * (size_t)g.nseg * nl), rows(16 * n * nl);
+    std::vector<double> La(n * nlh), Lb(n * nlh), Lc(n * nlh), Dm(n * nlh), Dd(n * nlh), e(n * nlh),
+        f(n * nlh), gg(n * nlh), sums(10 * (size_t)nlh);
+    std::vector<double> hf[3], hb[3], ef(9 * (size_t)g.nseg * nlh), rows(16 * n * nlh);
     for (int t = 0; t < 3; t++) {
-      hf[t].assign(n * nl, 0.0);
-      hb[t].assign(n * nl, 0.0);
+      hf[t].assign(n * nlh, 0.0);
+      hb[t].assign(n * nlh, 0.0);
     }
     sbh::SegPlan plan;
     sbh::seg_plan(g.my, g.nseg, &plan);
     sbh::SegFac sfac;
     sbh::BaseFac bfac;
-    for (int k = 0; k < g.mz; k++)
+    for (int k = 0; k <= g.nz; k++)
       for (int i = 0; i < g.nkx; i++) {
         const size_t line = (size_t)k * g.nkx + i;
-        int kzs = (k <= g.nz) ? k : k - g.mz;
+        int kzs = k;
         double gz = g.gam * kzs, a = g.alp * i;
         double k2 = (i == 0 && k == 0) ? 1.0 : gz * gz + a * a;
         double lap[7];
         for (int d = 0; d < 7; d++) lap[d] = rh2[d] - k2 * co.pr2[d];
         sbh::base_factor(lap, g.my, &bfac);
         for (size_t q = 0; q < n; q++) {
-          La[q * nl + line] = bfac.La[q];
-          Lb[q * nl + line] = bfac.Lb[q];
-          Lc[q * nl + line] = bfac.Lc[q];
-          Dm[q * nl + line] = bfac.Ddm1[q];
-          Dd[q * nl + line] = bfac.Dd[q];
-          e[q * nl + line] = bfac.e[q];
-          f[q * nl + line] = bfac.f[q];
-          gg[q * nl + line] = bfac.g[q];
+          La[q * nlh + line] = bfac.La[q];
+          Lb[q * nlh + line] = bfac.Lb[q];
+          Lc[q * nlh + line] = bfac.Lc[q];
+          Dm[q * nlh + line] = bfac.Ddm1[q];
+          Dd[q * nlh + line] = bfac.Dd[q];
+          e[q * nlh + line] = bfac.e[q];
+          f[q * nlh + line] = bfac.f[q];
+          gg[q * nlh + line] = bfac.g[q];
         }
-        for (int q = 0; q < 6; q++) sums[(size_t)q * nl + line] = bfac.sums[q];
-        for (int q = 0; q < 4; q++) sums[(size_t)(6 + q) * nl + line] = lap[3 + q];
+        for (int q = 0; q < 6; q++) sums[(size_t)q * nlh + line] = bfac.sums[q];
+        for (int q = 0; q < 4; q++) sums[(size_t)(6 + q) * nlh + line] = lap[3 + q];
         sbh::seg_factor(bfac, g.my, plan, &sfac);
         for (int t = 0; t < 3; t++)
           for (size_t q = 0; q < n; q++) {
-            hf[t][q * nl + line] = sfac.hf[t][q];
-            hb[t][q * nl + line] = sfac.hb[t][q];
+            hf[t][q * nlh + line] = sfac.hf[t][q];
+            hb[t][q * nlh + line] = sfac.hb[t][q];
           }
-        for (size_t q = 0; q < sfac.ef.size(); q++) ef[q * nl + line] = sfac.ef[q];
-        pack_rows(bfac, sfac, n, nl, line, rows);
+        for (size_t q = 0; q < sfac.ef.size(); q++) ef[q * nlh + line] = sfac.ef[q];
+        pack_rows(bfac, sfac, n, nlh, line, rows);
       }
     Fac &H = bf.hz;
     if ((rc = upload(h, &H.La, La)) || (rc = upload(h, &H.Lb, Lb)) || (rc = upload(h, &H.Lc, Lc)) ||
@@ -274,7 +278,7 @@ static int build_line_tables(sb_handle *h, int nseg) {
         (rc = upload(h, &H.ef, ef)) || (rc = upload(h, &H.rows, rows))) {
       return rc;
     }
-    H.stride = nl;
+    H.stride = nlh;
   }
   if (g.impl) {
     // the semi-implicit Helmholtz tables, filled by k_hfac every substep:

@@ -106,6 +106,13 @@ __device__ __forceinline__ bool line_thread(const Grid &g, int roles, LineThread
   return true;
 }
 
+// the entry of line lc in the per-line Helmholtz table: the table holds the
+// kz >= 0 lines, (kx, -kz) has the k^2 of (kx, kz)
+__device__ __forceinline__ long hz_line(const Grid &g, long lc) {
+  const int i = (int)(lc % g.nkx), k = (int)(lc / g.nkx);
+  return (long)((k <= g.nz) ? k : g.mz - k) * g.nkx + i;
+}
+
 // one thread's column of the shared-memory buffer (its segment's rows)
 __device__ __forceinline__ double *ycol() {
   extern __shared__ double sm_y[];
@@ -406,8 +413,8 @@ __global__ void __launch_bounds__(32 * kSeg, SB_LINE_MINB) k_lineB(Grid g, Bufs 
   // v = lapcdy(phi) (cross.f90:784-795, first step: 408-426); hg(0,0) keeps
   // the value the nonlinear stage left (zero), or zero in the prologue
   {
-    const FacView VH(bf.hz, L.lc);
-    const SegView WH(bf.hz, L.lc);
+    const FacView VH(bf.hz, hz_line(g, L.lc));
+    const SegView WH(bf.hz, hz_line(g, L.lc));
     const TailMake TH{VH, shp, N};
     SEG_SOLVE((const R *)bf.phi + off, ps, VH, WH, TH, shp, shm, g.pr2[3], g.pr2[4], g.pr2[5],
               g.pr2[6], false);
@@ -654,8 +661,8 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineF(Grid g, Bufs bf, int rk1
   } else {
     // v = lapcdy(phi) (cross.f90:784-795); hg(0,0) keeps the value the
     // nonlinear stage left (zero)
-    const FacView VH(bf.hz, L.lc);
-    const SegView WH(bf.hz, L.lc);
+    const FacView VH(bf.hz, hz_line(g, L.lc));
+    const SegView WH(bf.hz, hz_line(g, L.lc));
     const TailMake TH{VH, shp, N};
     SEG_SOLVE_P((const R *)bf.phi + off, ps, VH, WH, TH, shp, shm, g.pr2[3], g.pr2[4], g.pr2[5],
                 g.pr2[6], false);
@@ -871,8 +878,8 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1
   } else {
     // v = lapcdy(phi, k^2) (cross.f90:942-956); hg(0,0) keeps the value the
     // nonlinear stage left (zero)
-    const FacView VH(bf.hz, L.lc);
-    const SegView WH(bf.hz, L.lc);
+    const FacView VH(bf.hz, hz_line(g, L.lc));
+    const SegView WH(bf.hz, hz_line(g, L.lc));
     const TailMake TH{VH, shp, N};
     SEG_SOLVE_P((const R *)bf.phi + off, ps, VH, WH, TH, shp, shm, g.pr2[3], g.pr2[4], g.pr2[5],
                 g.pr2[6], false);
