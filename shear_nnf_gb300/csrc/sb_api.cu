@@ -282,8 +282,8 @@ static int build_line_tables(sb_handle *h, int nseg) {
   }
   if (g.impl) {
     // the semi-implicit Helmholtz tables, filled by k_hfac every substep:
-    // boxes x (lines + the mean line)
-    const size_t n = g.my, L = (size_t)g.B * (nl + 1);
+    // boxes x (lines (kx, kz >= 0) + the mean line)
+    const size_t n = g.my, L = (size_t)g.B * (g.nkx * (g.nz + 1) + 1);
     Fac &I = bf.hi;
     double *q[17];
     const size_t cnt[17] = {n * L, n * L, n * L, n * L, n * L, n * L, n * L, n * L, 10 * L,

@@ -147,8 +147,8 @@ struct Bufs {
   const double *ginv;            // 1/g per kz  (g = gam * kz_signed; 0 at k=0)
   const double *kinv;            // 1/(alp2+gam2) per (k,i); 0 at (0,0)
   Fac d1, d2, hz;                // d/dy, d2/dy2, Helmholtz (per line)
-  Fac hi;                        // semi-implicit Helmholtz (k^2 + dtr1) per box and line,
-                                 // line slot nkx*mz the mean line; rebuilt every substep
+  Fac hi;                        // semi-implicit Helmholtz (k^2 + dtr1) per box and line
+                                 // (kx, kz >= 0), then the mean line; rebuilt every substep
   Fac flt;                       // left-hand side of the compact y-filter
   const double *twy;             // y-transform twiddles (iydealiasing 1, 2), factored form
   const float *twyf;

@@ -6,8 +6,8 @@
 // and for the mean profiles (d2/dy2 - dtr1) u00 = rhs (lapcdy(., rk2, .),
 // cross.f90:898-925,965-967).  Delta t follows the CFL rule per step and per
 // box, so the Helmholtz factorisations are rebuilt on the device every
-// substep, after k_tables: one warp per (box, line slot), slot nkx*mz is the
-// mean line.  The tables have the layout of the per-line Helmholtz tables of
+// substep, after k_tables, for the lines (kx, kz >= 0) of every box (a line
+// (kx, -kz) has the same k^2) and the mean line.  The tables have the layout of the per-line Helmholtz tables of
 // the explicit step (Fac with stride = boxes x (lines + 1)): the LDL^H base
 // with the shear phase factored out of the border rows (the steps of
 // base_factor in sb_host.cpp, after modChol7cyclic_cmplx,
@@ -37,7 +37,8 @@ __device__ __constant__ static const double kIbeta[3] = {160.0 / 37.0, 24.0 / 5.
 constexpr int kHfLines = 10;
 
 __global__ void __launch_bounds__(128) k_hfac(Grid g, Bufs bf, int rk) {
-  const int n = g.my, nl = g.nkx * g.mz, per = nl + 1;
+  // lines (kx, kz >= 0): (kx, -kz) has the same k^2; slot nl is the mean line
+  const int n = g.my, nl = g.nkx * (g.nz + 1), per = nl + 1;
   const long nslots = (long)g.B * per;
   const int lane = threadIdx.x & 31, part = lane / kHfLines, l = lane - part * kHfLines;
   const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -61,7 +62,7 @@ __global__ void __launch_bounds__(128) k_hfac(Grid g, Bufs bf, int rk) {
   double k2 = dtr1;
   if (lc < nl) {
     const int i = lc % g.nkx, k = lc / g.nkx;
-    const double gz = g.gam * ((k <= g.nz) ? k : k - g.mz), ax = g.alp * i;
+    const double gz = g.gam * k, ax = g.alp * i;
     if (i != 0 || k != 0) k2 = dtr1 + (gz * gz + ax * ax);
   }
   double a[7];
@@ -220,7 +221,7 @@ __global__ void __launch_bounds__(128) k_hfac(Grid g, Bufs bf, int rk) {
 }
 
 cudaError_t launch_hfac(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
-  const long warps = ((long)g.B * (g.nkx * g.mz + 1) + kHfLines - 1) / kHfLines;
+  const long warps = ((long)g.B * (g.nkx * (g.nz + 1) + 1) + kHfLines - 1) / kHfLines;
   const unsigned nb = (unsigned)((warps + 3) / 4);
   k_hfac<<<nb, 128, 0, st>>>(g, bf, rk - 1);
   return cudaGetLastError();

@@ -724,8 +724,9 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1
   const double Dt = M.Deltat, nu = M.nu;
   const double fa = kAlpha[rk] * nu, fb = -M.Re * kIbetaL[rk], rdt = 1.0 / Dt;
   const R gk = (R)kGama[rk], zk = (R)kZeta[rk];
-  const int nl = g.nkx * g.mz;
-  const long hline0 = (long)L.b * (nl + 1);  // this box's first line of the implicit factors
+  // this box's entries of the implicit factors: lines (kx, kz >= 0), then the mean line
+  const int nl = g.nkx * (g.nz + 1);
+  const long hline0 = (long)L.b * (nl + 1);
   if (L.mean) {
     R *mu = (R *)bf.mu + (long)L.b * 2 * N + L.c;
     R *mdu = (R *)bf.mdu + (long)L.b * 2 * N + L.c;
@@ -861,8 +862,8 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1
   const cd shm = ldc2(bf.sh_new + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
   {
     // phase 3: the Helmholtz solves (cross.f90:894-925)
-    const FacView VI(bf.hi, hline0 + L.lc);
-    const SegView WI(bf.hi, hline0 + L.lc);
+    const FacView VI(bf.hi, hline0 + hz_line(g, L.lc));
+    const SegView WI(bf.hi, hline0 + hz_line(g, L.lc));
     const TailMake TI{VI, shp, N};
     const R *src = pipe ? (const R *)bf.S + off : (const R *)bf.T + off;
     SEG_SOLVE_P(src, ps, VI, WI, TI, shp, shm, g.pr2[3], g.pr2[4], g.pr2[5], g.pr2[6], false);
