@@ -535,6 +535,8 @@ def run_ours(args):
         pp.update(temperature=1, fkappa=LZ ** 2 / REZ / 0.7, bym=1.0, gbeta=0.5)
     elif args.variant == "implicit":
         pp.update(implicit_visc=1)
+    elif args.variant == "implicit-temperature":
+        pp.update(implicit_visc=1, temperature=1, fkappa=LZ ** 2 / REZ / 0.7, bym=1.0, gbeta=0.5)
     p = sb.make_params(**pp)
     st0 = sb.seed_state(p, 3 + rank)
     nbox = args.boxes if args.lite else 1
@@ -585,6 +587,8 @@ def run_ours(args):
     # line kernels)
     per_step = (39 if args.variant == "les" else 24) - (3 if tuning.get("line_form") == "fused"
                                                          else 0)
+    if args.variant == "implicit-temperature":
+        per_step += 3  # the scalar's factor tables
     launches = per_step * args.steps + 4
     if args.lite:
         # profiling runs (ncu): the timed steps only, no side measurements
@@ -815,7 +819,7 @@ def main():
     ap.add_argument("--lite", action="store_true",
                     help="profiling only: time the steps, skip e2e / CPU / per-kernel legs")
     ap.add_argument("--variant", default="plain",
-                    choices=["plain", "les", "temperature", "implicit"],
+                    choices=["plain", "les", "temperature", "implicit", "implicit-temperature"],
                     help="profiling only (with --lite): step the LES, temperature or semi-implicit box")
     ap.add_argument("--boxes", type=int, default=1,
                     help="profiling only (with --lite): boxes in the batch (Re_z log-uniform "

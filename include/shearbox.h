@@ -75,12 +75,15 @@ typedef struct sb_params {
                                   inertial force xforce to rf0u (cross.f90:610-624,
                                   crosst.f90:680-693) */
   double force_roll, xforce;   /* their amplitudes (initcr.f90:2103-2118) */
-  int implicit_visc;           /* 1: viscous terms semi-implicit, the reference's
-                                  explicit = 0 (cross.f90:797-989; hre3.dat keyword
-                                  explicit, initcr.f90:1976-1984): a Helmholtz solve
-                                  (d2/dy2 - k^2 - Re/(beta_k dt)) per line and
-                                  substep, no viscous time-step limit.  Needs les =
-                                  temperature = ydeal = 0 (error 2 otherwise). */
+  int implicit_visc;           /* 1: viscous (and with the temperature, thermal)
+                                  terms semi-implicit, the reference's explicit = 0
+                                  (cross.f90:797-989, crosst.f90:916-1195; hre3.dat
+                                  keyword explicit, initcr.f90:1976-1984): a
+                                  Helmholtz solve (d2/dy2 - k^2 - Re/(beta_k dt))
+                                  per line and substep, no viscous time-step limit
+                                  (crosst: at most 6/CFL times it).  Needs les =
+                                  ydeal = 0 and, with the temperature, fkappa > 0
+                                  (error 2 otherwise). */
 } sb_params;
 
 /* Per-box status after sb_step (cross.f90 istop logic, 1683-1690, 2102-2115) */

@@ -157,10 +157,10 @@ class Oracle:
                  cs=0.1, ydeal=0, temperature=0, fkappa=0.0, bym=0.0, gbeta=0.0, damping=0,
                  damp_up=0.0, damp_aa=0.0, force=0, force_roll=0.0, xforce=0.0,
                  implicit_visc=0):
-        if implicit_visc and (les or temperature):
+        if implicit_visc and (les or (temperature and not fkappa > 0)):
             # the reference stops on LES with explicit = 0 (initcr.f90:2179-2182);
-            # crosst's semi-implicit branch is not restated
-            raise ValueError("implicit_visc is for cross without LES or temperature")
+            # crosst's semi-implicit branch divides by fkappa
+            raise ValueError("implicit_visc needs les = 0 (and fkappa > 0 with the temperature)")
         self.p = OrcParams(mgalx, my, mgalz, Re, alp, Ly, gam, s, chi, CFL, vbulk, fixed_dt,
                            readflag, uprim, nhist, etime, dumptime, dtimag, keep_laminar, les,
                            les_visc, cs, ydeal, temperature, fkappa, bym, gbeta, damping,

@@ -7,7 +7,9 @@
  * -ffp-contract=off) so that the oracle is deterministic on x86 and Arm.
  *
  * Restated parts:
- *   cross.f90:336-1029       RK3 step loop, explicit branch, iadd_mode=5
+ *   cross.f90:336-1029       RK3 step loop, explicit and semi-implicit (797-989)
+ *                            branches, iadd_mode=5; crosst.f90:916-1195 the
+ *                            semi-implicit branch with the scalar
  *   cross.f90:1127-1765      hvhg (non-LES)
  *   cross.f90:1773-2121      hist, flags 'f' and 'w' (UNER record)
  *   fou3D_thread.f:22-161    fourxz / fill00 / pack00 (FFTW semantics, own FFT)
@@ -1591,7 +1593,9 @@ static void moving_frame(ctx *c, double *vor, double *phi, double mtime) {
 }
 
 /* The semi-implicit viscous branch of one substep (explicit = 0,
- * cross.f90:797-989): nonlinear terms by the low-storage RK3 as in the
+ * cross.f90:797-989; with the scalar of crosst, crosst.f90:916-1195: the
+ * buoyancy stays explicit, tb diffuses semi-implicitly with fkappa in place of
+ * nu): nonlinear terms by the low-storage RK3 as in the
  * explicit branch, viscous terms by the Crank-Nicolson-like pair alpha_k
  * (explicit part) and beta_k (implicit part), so that each substep solves
  *   (d2/dy2 - k^2 - Re/(beta_k Dt)) f_new =
@@ -1599,6 +1603,7 @@ static void moving_frame(ctx *c, double *vor, double *phi, double mtime) {
  * per (kx, kz) line with the shear phase of t + c_k Dt.  hv, hg, rf0u, rf0w are
  * the assembled right-hand sides; on return vorwk, phiwk, u00wk, w00wk hold the
  * zeta stores of the next substep and hg holds v = lapcdy(phi). */
+static void moving_frame_t(ctx *c, double *temp, double mtime);
 static const double ALPHA[3] = {29.0 / 96.0, -3.0 / 40.0, 1.0 / 6.0};
 static const double IBETA[3] = {160.0 / 37.0, 24.0 / 5.0, 6.0};
 static void implicit_substep(ctx *c, int rkstep, double Deltat, double r1, double xoffb,
@@ -1607,22 +1612,44 @@ static void implicit_substep(ctx *c, int rkstep, double Deltat, double r1, doubl
                              double *hv, double *hg, double *vorwk, double *phiwk,
                              double *u00wk, double *w00wk, const double *rf0u,
                              const double *rf0w, double *ddu, double *wk1dr, cplx *shwkb,
-                             cplx *shwkt) {
+                             cplx *shwkt, double *tb, double *tb00, const double *ht,
+                             double *tbwk, double *tb00wk, const double *rf0tb) {
   int my = c->my, nkx = c->nkx, mz = c->mz, mx1 = c->mx1;
   size_t nfield = 2 * (size_t)my * nkx * mz;
   double s = c->p.s, Re = c->p.Re;
   double gk = GAMA[rkstep - 1], zk = ZETA[rkstep - 1];
-  /* (2) gama_k [hv, hg] -> [phiwk, vorwk] (cross.f90:800-811) */
+  const int temp = (tb != NULL);
+  const double fkappa = c->p.fkappa, gbeta = c->p.gbeta;
+  if (temp) {
+    /* crosst: the buoyancy gbeta lap(tb) into hv before the accumulation
+     * (crosst.f90:919-932) */
+#pragma omp parallel for schedule(static)
+    for (int ik = 0; ik < nkx * mz; ik++) {
+      int i = ik % nkx, k = ik / nkx;
+      if (i != 0 || k != 0) {
+        ythread *t = &c->yt[my_thread()];
+        double rk = c->gam2[k] + c->alp2[i];
+        double *scr = ddu + 2 * (size_t)my * ik;
+        visc3d(c, t, PEN(tb, i, k), PEN(hv, i, k), scr, shwkt[i], shwkb[i], 2, rk, gbeta, 1);
+      }
+    }
+  }
+  /* (2) gama_k [hv, hg] -> [phiwk, vorwk] (cross.f90:800-811; crosst.f90:934-952
+   * with gama_k ht -> tbwk) */
   if (rkstep == 1) {
     for (size_t q = 0; q < nfield; q++) {
       vorwk[q] = gk * hg[q];
       phiwk[q] = gk * hv[q];
     }
+    if (temp)
+      for (size_t q = 0; q < nfield; q++) tbwk[q] = gk * ht[q];
   } else {
     for (size_t q = 0; q < nfield; q++) {
       vorwk[q] = vorwk[q] + gk * hg[q];
       phiwk[q] = phiwk[q] + gk * hv[q];
     }
+    if (temp)
+      for (size_t q = 0; q < nfield; q++) tbwk[q] = tbwk[q] + gk * ht[q];
   }
   /* (3) alpha_k nu lap [vor, phi] -> ++[vorwk, phiwk] with the phase of t
    * (cross.f90:812-828) */
@@ -1636,37 +1663,54 @@ static void implicit_substep(ctx *c, int rkstep, double Deltat, double r1, doubl
       double *scr = ddu + 2 * (size_t)my * ik;
       visc3d(c, t, PEN(vor, i, k), PEN(vorwk, i, k), scr, shwkt[i], shwkb[i], 2, rk, fac, 1);
       visc3d(c, t, PEN(phi, i, k), PEN(phiwk, i, k), scr, shwkt[i], shwkb[i], 2, rk, fac, 0);
+      if (temp)
+        visc3d(c, t, PEN(tb, i, k), PEN(tbwk, i, k), scr, shwkt[i], shwkb[i], 2, rk,
+               ALPHA[rkstep - 1] * fkappa, 0);
     }
   }
-  /* (2*, 3*) the mean profiles (cross.f90:830-845) */
+  /* (2*, 3*) the mean profiles (cross.f90:830-845; crosst.f90:975-997) */
   if (rkstep == 1) {
     for (int j = 0; j < my; j++) {
       u00wk[j] = gk * rf0u[j];
       w00wk[j] = gk * rf0w[j];
     }
+    if (temp)
+      for (int j = 0; j < my; j++) tb00wk[j] = gk * rf0tb[j];
   } else {
     for (int j = 0; j < my; j++) {
       u00wk[j] = u00wk[j] + gk * rf0u[j];
       w00wk[j] = w00wk[j] + gk * rf0w[j];
     }
+    if (temp)
+      for (int j = 0; j < my; j++) tb00wk[j] = tb00wk[j] + gk * rf0tb[j];
   }
   cplx one = C(1.0, 0.0);
   visc3d(c, &c->yt[0], u00, u00wk, wk1dr, one, one, 1, 0.0, fac, 0);
   visc3d(c, &c->yt[0], w00, w00wk, wk1dr, one, one, 1, 0.0, fac, 0);
-  /* (4) + [vor, phi]/Dt, (6) times -Re/beta_k (cross.f90:847-867) */
+  if (temp)
+    visc3d(c, &c->yt[0], tb00, tb00wk, wk1dr, one, one, 1, 0.0, ALPHA[rkstep - 1] * fkappa, 0);
+  /* (4) + [vor, phi]/Dt, (6) times -Re/beta_k (cross.f90:847-867); the scalar
+   * with -1/(fkappa beta_k) (crosst.f90:999-1028) */
   for (size_t q = 0; q < nfield; q++) {
     vorwk[q] = vorwk[q] + (1.0 / Deltat) * vor[q];
     phiwk[q] = phiwk[q] + (1.0 / Deltat) * phi[q];
   }
+  if (temp)
+    for (size_t q = 0; q < nfield; q++) tbwk[q] = tbwk[q] + (1.0 / Deltat) * tb[q];
   double fb = -Re * IBETA[rkstep - 1];
+  double fbt = temp ? -(1.0 / fkappa) * IBETA[rkstep - 1] : 0.0;
   for (size_t q = 0; q < nfield; q++) {
     vorwk[q] = fb * vorwk[q];
     phiwk[q] = fb * phiwk[q];
   }
+  if (temp)
+    for (size_t q = 0; q < nfield; q++) tbwk[q] = fbt * tbwk[q];
   for (int j = 0; j < my; j++) {
     u00wk[j] = fb * (u00wk[j] + (1.0 / Deltat) * u00[j]);
     w00wk[j] = fb * (w00wk[j] + (1.0 / Deltat) * w00[j]);
   }
+  if (temp)
+    for (int j = 0; j < my; j++) tb00wk[j] = fbt * (tb00wk[j] + (1.0 / Deltat) * tb00[j]);
   /* (7) shear-periodic boundary at t + c_k Dt (cross.f90:869-884) */
   if (fabs(s) > 0.5) {
     *xwkb = xoffb + r1 * u00b;
@@ -1682,8 +1726,11 @@ static void implicit_substep(ctx *c, int rkstep, double Deltat, double r1, doubl
   {
     double mf = (rkstep == 1) ? -(s * r1) : -(s * (CA[rkstep - 1] - CA[rkstep - 2]) * Deltat);
     moving_frame(c, vorwk, phiwk, mf);
+    if (temp) moving_frame_t(c, tbwk, mf);
   }
   double dtr = Re / Deltat, dtr1 = dtr * IBETA[rkstep - 1];
+  /* crosst: dtrk = (1/fkappa)/Dt (crosst.f90:1976-1977) */
+  double dtr1k = temp ? ((1.0 / fkappa) / Deltat) * IBETA[rkstep - 1] : 0.0;
 #pragma omp parallel for schedule(static)
   for (int ik = 0; ik < nkx * mz; ik++) {
     int i = ik % nkx, k = ik / nkx;
@@ -1702,14 +1749,28 @@ static void implicit_substep(ctx *c, int rkstep, double Deltat, double r1, doubl
              2);
     }
   }
-  /* (9) zeta stores (cross.f90:927-941) */
+  if (temp) {
+#pragma omp parallel for schedule(static)
+    for (int ik = 0; ik < nkx * mz; ik++) {
+      int i = ik % nkx, k = ik / nkx;
+      if (i != 0 || k != 0) {
+        double rk = c->gam2[k] + c->alp2[i], rk2 = dtr1k + rk;
+        lapcdy(c, &c->yt[my_thread()], PEN(tbwk, i, k), rk2, PEN(tb, i, k), shwkt[i],
+               shwkb[i], 2);
+      }
+    }
+  }
+  /* (9) zeta stores (cross.f90:927-941; crosst.f90:1106-1125) */
   if (rkstep != 3) {
     for (size_t q = 0; q < nfield; q++) {
       vorwk[q] = zk * hg[q];
       phiwk[q] = zk * hv[q];
     }
+    if (temp)
+      for (size_t q = 0; q < nfield; q++) tbwk[q] = zk * ht[q];
     double mf = (rkstep == 1) ? -(GAMA[0] * Deltat * s) : -((GAMA[1] + ZETA[0]) * Deltat * s);
     moving_frame(c, vorwk, phiwk, mf);
+    if (temp) moving_frame_t(c, tbwk, mf);
   }
   /* v = lapcdy(phi) (cross.f90:942-956) */
 #pragma omp parallel for schedule(static)
@@ -1723,11 +1784,14 @@ static void implicit_substep(ctx *c, int rkstep, double Deltat, double r1, doubl
   /* (8*, 9*) the mean profiles (cross.f90:960-975) */
   lapcdy(c, &c->yt[0], u00wk, dtr1, u00, one, one, 1);
   lapcdy(c, &c->yt[0], w00wk, dtr1, w00, one, one, 1);
+  if (temp) lapcdy(c, &c->yt[0], tb00wk, dtr1k, tb00, one, one, 1);
   if (rkstep != 3) {
     for (int j = 0; j < my; j++) {
       u00wk[j] = zk * rf0u[j];
       w00wk[j] = zk * rf0w[j];
     }
+    if (temp)
+      for (int j = 0; j < my; j++) tb00wk[j] = zk * rf0tb[j];
   }
 }
 
@@ -2011,9 +2075,9 @@ static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00,
                      double *tb00, double *ptime, double *pxoffb, double *pxofft, int nstep,
                      double *trace, int *ntrace, int *pistop, double *pdeltat) {
   int my = c->my, nkx = c->nkx, mz = c->mz, mx1 = c->mx1;
-  /* the semi-implicit branch is restated for cross without LES
-   * (initcr.f90:2179-2182 stops there) */
-  if (c->p.implicit_visc && (c->p.les || tb != NULL)) return -1;
+  /* the semi-implicit branch is restated without LES (initcr.f90:2179-2182
+   * stops there); with the temperature it divides by fkappa */
+  if (c->p.implicit_visc && (c->p.les || (tb != NULL && !(c->p.fkappa > 0.0)))) return -1;
   size_t nfield = 2 * (size_t)my * nkx * mz; /* doubles per pencil field */
   size_t nplane = (size_t)nkx * mz;
   double s = c->p.s, Ly = c->p.Ly, Re = c->p.Re;
@@ -2285,9 +2349,15 @@ static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00,
             }
             CFLv = CFL * c->cflvv * dt;
             if (temp) {
-              /* crosst.f90:1236-1257 */
+              /* crosst.f90:1929-1968: explicit, dt within the viscous and
+               * thermal limits; semi-implicit, at most 6/CFL times them
+               * once CFLv exceeds 2 */
               CFLk = CFL * c->cflkk * dt;
-              if (CFLv > CFL) dt = (CFLk > CFLv) ? 1.0 / c->cflkk : 1.0 / c->cflvv;
+              if (!c->p.implicit_visc) {
+                if (CFLv > CFL) dt = (CFLk > CFLv) ? 1.0 / c->cflkk : 1.0 / c->cflvv;
+              } else if (CFLv > 2.0) {
+                dt = (CFLk > CFLv) ? 1.0 / c->cflkk / CFL * 6.0 : 1.0 / c->cflvv / CFL * 6.0;
+              }
             } else if (CFLv > CFL && !c->p.implicit_visc) {
               /* the viscous limit of the explicit branch only (cross.f90:1669) */
               dt = 1.0 / c->cflvv;
@@ -2429,7 +2499,7 @@ static int cross_run(ctx *c, double *vor, double *phi, double *u00, double *w00,
       if (c->p.implicit_visc) {
         implicit_substep(c, rkstep, Deltat, r1, xoffb, xofft, u00b, u00t, &xwkb, &xwkt, vor,
                          phi, u00, w00, hv, hg, vorwk, phiwk, u00wk, w00wk, rf0u, rf0w, ddu,
-                         wk1dr, shwkb, shwkt);
+                         wk1dr, shwkb, shwkt, tb, tb00, ht, tbwk, tb00wk, rf0tb);
         continue;
       }
       if (!les || c->p.les_visc) {

@@ -53,8 +53,9 @@ typedef struct orc_params {
                            * (cross.f90:610-624) */
   double force_roll, xforce; /* their amplitudes (initcr.f90:2103-2118) */
   int implicit_visc;      /* 1: viscous terms semi-implicit (explicit = 0,
-                           * cross.f90:797-989, initcr.f90:1976-1984); not with
-                           * LES (initcr.f90:2179) nor the temperature */
+                           * cross.f90:797-989, crosst.f90:916-1195,
+                           * initcr.f90:1976-1984); not with LES
+                           * (initcr.f90:2179), fkappa > 0 with the temperature */
 } orc_params;
 
 /* one .cfbin record per statistics step (cross.f90:2087):

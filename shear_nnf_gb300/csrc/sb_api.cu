@@ -127,8 +127,10 @@ static int check_params(const sb_params *p) {
     return fail(2, "implicit_visc=%d not available (0, 1)", p->implicit_visc);
   // LES with explicit = 0 stops the reference (initcr.f90:2179-2182); the
   // semi-implicit kernels cover the plain step
-  if (p->implicit_visc && (p->les || p->temperature || p->ydeal))
-    return fail(2, "implicit_visc needs les = temperature = ydeal = 0");
+  if (p->implicit_visc && (p->les || p->ydeal))
+    return fail(2, "implicit_visc needs les = ydeal = 0");
+  if (p->implicit_visc && p->temperature && !(p->fkappa > 0.0))
+    return fail(2, "implicit_visc with the temperature needs fkappa > 0");
   if (!(p->Re != 0.0) || !(p->alp > 0) || !(p->gam > 0) || !(p->Ly > 0) || !(p->CFL > 0))
     return fail(1, "invalid physical parameters");
   return 0;
@@ -300,6 +302,21 @@ static int build_line_tables(sb_handle *h, int nseg) {
     I.ef = q[15];
     I.rows = q[16];
     I.stride = (long)L;
+    if (g.temp) {
+      // the scalar's tables of crosst, same layout
+      Fac &K = bf.hit;
+      for (int t = 0; t < 17; t++)
+        if ((rc = dalloc(h, &q[t], cnt[t]))) return rc;
+      K.La = q[0]; K.Lb = q[1]; K.Lc = q[2]; K.Ddm1 = q[3]; K.Dd = q[4];
+      K.e = q[5]; K.f = q[6]; K.g = q[7]; K.sums = q[8];
+      for (int t = 0; t < 3; t++) {
+        K.hf[t] = q[9 + t];
+        K.hb[t] = q[12 + t];
+      }
+      K.ef = q[15];
+      K.rows = q[16];
+      K.stride = (long)L;
+    }
   }
   if (prepare_line(g) != cudaSuccess)
     return fail(3, "line kernel attributes: %s", cudaGetErrorString(cudaGetLastError()));

@@ -267,9 +267,14 @@ __global__ void __launch_bounds__(256) k_scalar(Grid g, Bufs bf, int rk) {
       M.CFLv = M.CFL * M.cflvv * dt;
       if (g.temp) {
         // the thermal-diffusion limit enters only where the viscous one
-        // does (crosst.f90:1236-1257)
+        // does (crosst.f90:1929-1968): explicit, within both limits;
+        // semi-implicit, at most 6/CFL times them once CFLv exceeds 2
         const double CFLk = M.CFL * M.cflkk * dt;
-        if (M.CFLv > M.CFL) dt = (CFLk > M.CFLv) ? 1.0 / M.cflkk : 1.0 / M.cflvv;
+        if (!g.impl) {
+          if (M.CFLv > M.CFL) dt = (CFLk > M.CFLv) ? 1.0 / M.cflkk : 1.0 / M.cflvv;
+        } else if (M.CFLv > 2.0) {
+          dt = (CFLk > M.CFLv) ? 1.0 / M.cflkk / M.CFL * 6.0 : 1.0 / M.cflvv / M.CFL * 6.0;
+        }
       } else if (M.CFLv > M.CFL && !g.impl) {
         // the viscous limit of the explicit branch only (cross.f90:1669)
         dt = 1.0 / M.cflvv;
@@ -492,6 +497,8 @@ cudaError_t launch_finish(const Grid &g, const Bufs &bf, cudaStream_t st) {
   cudaError_t lineF_f64(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);           \
   cudaError_t lineF_f32(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);           \
   bool lineF_fits_f64(const Grid &g);                                                      \
+  bool lineI_fits_f64(const Grid &g, int np);                                              \
+  bool lineI_fits_f32(const Grid &g, int np);                                              \
   cudaError_t lineI_f64(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);           \
   cudaError_t lineI_f32(const Grid &g, const Bufs &bf, int rk, cudaStream_t st);           \
   bool lineF_fits_f32(const Grid &g);                                                      \
@@ -551,8 +558,8 @@ bool line_fused_ok(const Grid &g) {
 cudaError_t launch_lineI(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
   SB_SEG_CALL(lineI, g, bf, rk, st)
 }
-// k_lineI has k_lineF's block (two pipelines): the same shared memory
-bool line_implicit_ok(const Grid &g) { SB_SEG_CALL(lineF_fits, g) }
+// k_lineI has k_lineF's block (two pipelines, three with the temperature)
+bool line_implicit_ok(const Grid &g) { SB_SEG_CALL(lineI_fits, g, g.temp ? 3 : 2) }
 cudaError_t launch_lineL(const Grid &g, const Bufs &bf, cudaStream_t st) {
   SB_SEG_CALL(lineL, g, bf, st)
 }

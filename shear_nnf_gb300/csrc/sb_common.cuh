@@ -149,6 +149,7 @@ struct Bufs {
   Fac d1, d2, hz;                // d/dy, d2/dy2, Helmholtz (per line)
   Fac hi;                        // semi-implicit Helmholtz (k^2 + dtr1) per box and line
                                  // (kx, kz >= 0), then the mean line; rebuilt every substep
+  Fac hit;                       // the same for the scalar of crosst (k^2 + dtr1k)
   Fac flt;                       // left-hand side of the compact y-filter
   const double *twy;             // y-transform twiddles (iydealiasing 1, 2), factored form
   const float *twyf;

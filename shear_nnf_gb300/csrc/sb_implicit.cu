@@ -36,7 +36,10 @@ __device__ __constant__ static const double kIbeta[3] = {160.0 / 37.0, 24.0 / 5.
 // same, so those rows are copied instead of recomputed.
 constexpr int kHfLines = 10;
 
-__global__ void __launch_bounds__(128) k_hfac(Grid g, Bufs bf, int rk) {
+// which = 0: the flow's operators (dtr1 = Re ibeta_k / Dt, tables bf.hi);
+// 1: the scalar's of crosst (dtr1k = ibeta_k / (fkappa Dt), crosst.f90:1976-1977,
+// tables bf.hit)
+__global__ void __launch_bounds__(128) k_hfac(Grid g, Bufs bf, int rk, int which) {
   // lines (kx, kz >= 0): (kx, -kz) has the same k^2; slot nl is the mean line
   const int n = g.my, nl = g.nkx * (g.nz + 1), per = nl + 1;
   const long nslots = (long)g.B * per;
@@ -49,7 +52,7 @@ __global__ void __launch_bounds__(128) k_hfac(Grid g, Bufs bf, int rk) {
   const Member &M = bf.mem[b];
   const bool wr = on && !M.halted;  // this lane writes
   const long stride = nslots;
-  Fac &F = bf.hi;
+  Fac &F = which ? bf.hit : bf.hi;
   double *La = const_cast<double *>(F.La), *Lb = const_cast<double *>(F.Lb),
          *Lc = const_cast<double *>(F.Lc), *Dd = const_cast<double *>(F.Dd),
          *Dm = const_cast<double *>(F.Ddm1), *E = const_cast<double *>(F.e),
@@ -58,7 +61,8 @@ __global__ void __launch_bounds__(128) k_hfac(Grid g, Bufs bf, int rk) {
          *rows = const_cast<double *>(F.rows);
   // the operator rh2 - k2 pr2 with k2 = kx^2 + kz^2 + dtr1 (dtr1 alone on the
   // mean line; the (0,0) line is never solved and gets the mean line's k2)
-  const double dtr1 = (M.Re / M.Deltat) * kIbeta[rk];
+  const double dtr1 = which ? ((1.0 / g.kappa) / M.Deltat) * kIbeta[rk]
+                            : (M.Re / M.Deltat) * kIbeta[rk];
   double k2 = dtr1;
   if (lc < nl) {
     const int i = lc % g.nkx, k = lc / g.nkx;
@@ -223,7 +227,8 @@ __global__ void __launch_bounds__(128) k_hfac(Grid g, Bufs bf, int rk) {
 cudaError_t launch_hfac(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
   const long warps = ((long)g.B * (g.nkx * (g.nz + 1) + 1) + kHfLines - 1) / kHfLines;
   const unsigned nb = (unsigned)((warps + 3) / 4);
-  k_hfac<<<nb, 128, 0, st>>>(g, bf, rk - 1);
+  k_hfac<<<nb, 128, 0, st>>>(g, bf, rk - 1, 0);
+  if (g.temp) k_hfac<<<nb, 128, 0, st>>>(g, bf, rk - 1, 1);
   return cudaGetLastError();
 }
 

@@ -686,31 +686,37 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineF(Grid g, Bufs bf, int rk1
 
 // ---------------------------------------------------------------------------
 // k_lineI: the y-line work of one substep of the semi-implicit viscous branch
-// (explicit = 0, cross.f90:797-989), for the plain step (no LES, temperature,
-// y filter or y dealiasing).  Same block layout as k_lineF (two pipelines of
-// kSeg warps on 16 lines), five phases:
-//   phase  pipeline 0 (omega_y)                 pipeline 1 (phi)
-//   1      T = d/dy(dH1/dx + dH3/dz)            S = d2(phi)/dy2
-//   2      right-hand side of the Helmholtz     the same for phi with
-//          equation (below) -> T buffer,        hv - T -> S buffer,
-//          zeta store -> vorwk                  zeta store -> phiwk
-//   3      omega_y = lapcdy(rhs, k^2 + dtr1)    phi = lapcdy(rhs, k^2 + dtr1)
-//   4      d(omega_y)/dy -> D                   v = lapcdy(phi, k^2) -> G
-//   5      d2(omega_y)/dy2 -> Lv                dv/dy -> V
-// with, per point (cross.f90:800-867, in this order),
+// (explicit = 0, cross.f90:797-989; crosst.f90:916-1195 with TEMP), without
+// LES, y filter or y dealiasing.  k_lineF's block (pipelines of kSeg warps on
+// 16 lines), with a third pipeline for the scalar tb under TEMP:
+//   phase  pipeline 0 (omega_y)         pipeline 1 (phi)          pipeline 2 (tb)
+//   1      T = d/dy(dH1/dx + dH3/dz)    S = d2(phi)/dy2           Lt = lap(tb)
+//   2      -                            -                         ht += d(-vT)/dy
+//   3      right-hand side -> T buf,    the same for phi with     the same for tb
+//          zeta store -> vorwk          hv - T + gbeta Lt         -> R2 buf
+//   4      omega_y = lapcdy(rhs,        phi = lapcdy(rhs,         tb = lapcdy(rhs,
+//          k^2 + dtr1)                  k^2 + dtr1)               k^2 + dtr1k)
+//   5      d(omega_y)/dy -> D           v = lapcdy(phi, k^2) -> G -
+//   6      d2(omega_y)/dy2 -> Lv        dv/dy -> V                -
+// (phase 2 and pipeline 2 only with TEMP), with, per point (cross.f90:800-867,
+// crosst.f90:934-1028, in this order),
 //   wk = [wk +] gama_k h;  wk += alpha_k nu (f'' - k^2 f);  wk += f/Dt;
-//   rhs = -Re ibeta_k wk,  moved to the frame of t + c_k Dt (moving_frame);
-// and the Helmholtz factors of k^2 + dtr1 (dtr1 = Re ibeta_k / Dt) built for
-// this substep by k_hfac.  The mean block (pipeline 0): nu u00'' in phase 1,
-// the mean right-hand side in phase 2 (through mdu), the real Helmholtz solve
-// of dtr1 in phase 3, du00/dy in phase 4.  The (0,0) line keeps its state
-// (cross.f90 skips it).
+//   rhs = -Re ibeta_k wk (tb: -ibeta_k/fkappa, diffusivity fkappa), moved to
+//   the frame of t + c_k Dt (moving_frame, moving_frame_t);
+// dtr1 = Re ibeta_k / Dt, dtr1k = ibeta_k / (fkappa Dt); the Helmholtz factors
+// of the substep come from k_hfac.  The mean block: u00, w00 on pipeline 0
+// (u00'' in phase 1, the right-hand side in phase 3 through mdu, the real
+// Helmholtz solve of dtr1 in phase 4, du00/dy in phase 5), tb00 on pipeline 2
+// (d(-vT00)/dy -> mtr in phase 1, tb00'' in phase 2, the right-hand side
+// through mtr in phase 3, the solve of dtr1k in phase 4).  The (0,0) line
+// keeps its state (cross.f90 and crosst.f90 skip it).
 __device__ __constant__ static const double kAlpha[3] = {29.0 / 96.0, -3.0 / 40.0, 1.0 / 6.0};
 __device__ __constant__ static const double kIbetaL[3] = {160.0 / 37.0, 24.0 / 5.0, 6.0};
 
-template <typename R>
-__global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1) {
-  __shared__ double xch[2][kSeg][16][2][SB_XS];
+template <typename R, bool TEMP>
+__global__ void __launch_bounds__((TEMP ? 96 : 64) * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1) {
+  constexpr int NP = TEMP ? 3 : 2;
+  __shared__ double xch[NP][kSeg][16][2][SB_XS];
   LineThread L;
   int pipe = 0;
   if (!line_thread_f(g, &L, &pipe)) return;  // whole blocks
@@ -723,6 +729,8 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1
   const SegView W1(bf.d1, 0), W2(bf.d2, 0);
   const double Dt = M.Deltat, nu = M.nu;
   const double fa = kAlpha[rk] * nu, fb = -M.Re * kIbetaL[rk], rdt = 1.0 / Dt;
+  const double fat = TEMP ? kAlpha[rk] * g.kappa : 0.0;
+  const double fbt = TEMP ? -(1.0 / g.kappa) * kIbetaL[rk] : 0.0;
   const R gk = (R)kGama[rk], zk = (R)kZeta[rk];
   // this box's entries of the implicit factors: lines (kx, kz >= 0), then the mean line
   const int nl = g.nkx * (g.nz + 1);
@@ -730,17 +738,34 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1
   if (L.mean) {
     R *mu = (R *)bf.mu + (long)L.b * 2 * N + L.c;
     R *mdu = (R *)bf.mdu + (long)L.b * 2 * N + L.c;
+    R *mt = TEMP ? (R *)bf.mt + (long)L.b * 2 * N + L.c : nullptr;
+    R *mtr = TEMP ? (R *)bf.mtr + (long)L.b * 2 * N + L.c : nullptr;
     const cd one = mk(1.0, 0.0);
-    // phase 1: u00'' (visc3d(u00, u00wk, m=1, rk=0), cross.f90:842-845)
+    const TailLoad T1{bf.tl1o + (long)L.b * g.nkx * SB_TAIL};
+    const TailLoad T2{bf.tl2o + (long)L.b * g.nkx * SB_TAIL};
+    // phase 1: u00'' (visc3d(u00, u00wk, m=1, rk=0), cross.f90:842-845);
+    // rf0tb = d(-vT_00)/dy from the (0,0) line of -vT (crosst.f90:642-645)
     if (pipe == 0) {
-      const TailLoad T2{bf.tl2o + (long)L.b * g.nkx * SB_TAIL};
       SEG_SOLVE_P(mu, 2, V2, W2, T2, one, one, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6], false);
+    } else if (TEMP && pipe == 2) {
+      const R *src = (const R *)bf.R2 + (long)L.b * g.field + L.c;
+      SEG_SOLVE_P(src, g.plane, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true);
+      if (L.active && L.c == 0)
+        for (int i = L.r0; i <= L.r1; i++) mtr[2 * (i - 1)] = (R)ys[(i - L.r0) * ystr];
     } else {
       seg_idle();
     }
     __syncthreads();
-    // phase 2: forcing, damping, the mean right-hand side -> mdu and the zeta
-    // store (cross.f90:622-626,830-867,972-975)
+    if constexpr (TEMP) {
+      // phase 2: tb00'' (visc3d(tb00, tb00wk, rk=0), crosst.f90:994-997)
+      if (pipe == 2)
+        SEG_SOLVE_P(mt, 2, V2, W2, T2, one, one, g.rh2[3], g.rh2[4], g.rh2[5], g.rh2[6], false);
+      else
+        seg_idle();
+      __syncthreads();
+    }
+    // phase 3: forcing, damping, the mean right-hand sides and the zeta stores
+    // (cross.f90:622-626,830-867,972-975; crosst.f90:975-1028,1163-1168)
     if (pipe == 0) {
       R *mwk = (R *)bf.mwk + (long)L.b * 2 * N + L.c;
       const R *mrf = (const R *)bf.mrf + (long)L.b * 2 * N + L.c;
@@ -765,9 +790,24 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1
           if (rk < 2) mwk[2 * j] = zk * rf0;
         }
       }
+    } else if (TEMP && pipe == 2 && L.c == 0) {
+      R *mtwk = (R *)bf.mtwk + (long)L.b * 2 * N;
+      for (int i = L.r0; i <= L.r1; i++) {
+        const int j = i - 1;
+        const R rf0 = mtr[2 * j];
+        const R wk = (rk == 0) ? gk * rf0 : mtwk[2 * j] + gk * rf0;
+        double w = (double)wk;
+        w = w + fat * (-(0.0 * (double)mt[2 * j]) + ys[(i - L.r0) * ystr]);
+        const double rhs = fbt * (w + rdt * (double)mt[2 * j]);
+        if (L.active) {
+          mtr[2 * j] = (R)rhs;
+          if (rk < 2) mtwk[2 * j] = zk * rf0;
+        }
+      }
     }
     __syncthreads();
-    // phase 3: u00 = lapcdy(rhs, dtr1) (cross.f90:965-967), real lines
+    // phase 4: u00 = lapcdy(rhs, dtr1) (cross.f90:965-967), tb00 =
+    // lapcdy(rhs, dtr1k) (crosst.f90:1158-1161), real lines
     if (pipe == 0) {
       const FacView VI(bf.hi, hline0 + nl);
       const SegView WI(bf.hi, hline0 + nl);
@@ -775,20 +815,27 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1
       SEG_SOLVE_P((const R *)mdu, 2, VI, WI, TI, one, one, g.pr2[3], g.pr2[4], g.pr2[5], g.pr2[6],
                   false);
       store_col(ys, ystr, mu, 2, L);
+    } else if (TEMP && pipe == 2) {
+      const FacView VK(bf.hit, hline0 + nl);
+      const SegView WK(bf.hit, hline0 + nl);
+      const TailMake TK{VK, one, N};
+      SEG_SOLVE_P((const R *)mtr, 2, VK, WK, TK, one, one, g.pr2[3], g.pr2[4], g.pr2[5],
+                  g.pr2[6], false);
+      if (L.active && L.c == 0)
+        for (int i = L.r0; i <= L.r1; i++) mt[2 * (i - 1)] = (R)ys[(i - L.r0) * ystr];
     } else {
       seg_idle();
     }
     __syncthreads();
-    // phase 4: du00/dy, dw00/dy of the new profiles (cross.f90:1186-1192)
+    // phase 5: du00/dy, dw00/dy of the new profiles (cross.f90:1186-1192)
     if (pipe == 0) {
-      const TailLoad T1{bf.tl1o + (long)L.b * g.nkx * SB_TAIL};
       SEG_SOLVE_P(mu, 2, V1, W1, T1, one, one, 0.0, g.rh1[4], g.rh1[5], g.rh1[6], true);
       store_col(ys, ystr, mdu, 2, L);
     } else {
       seg_idle();
     }
     __syncthreads();
-    seg_idle();  // phase 5
+    seg_idle();  // phase 6
     return;
   }
   const long off = (long)L.b * g.field + 2 * L.lc + L.c;
@@ -801,47 +848,89 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1
   const double *mf1 = bf.mf1 + (long)L.b * 2 * N * g.nkx + 2 * i;
   const double *mf2 = bf.mf2 + (long)L.b * 2 * N * g.nkx + 2 * i;
   {
-    // phase 1 at the phase of time t
+    // phases 1-2 at the phase of time t
     const cd shp = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * i);
     const cd shm = ldc2(bf.sh_old + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
+    const TailLoad T1{bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL};
+    const TailLoad T2{bf.tl2o + ((long)L.b * g.nkx + i) * SB_TAIL};
     if (pipe == 0) {
       // T = d/dy (dH1/dx + dH3/dz) (cross.f90:565-575), as k_lineA stores it
-      const TailLoad T1{bf.tl1o + ((long)L.b * g.nkx + i) * SB_TAIL};
       SEG_SOLVE_P((const R *)bf.D + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
                   g.rh1[6], true);
       for (int r = L.r0; r <= L.r1; r++)
         ys[(r - L.r0) * ystr] = (double)(R)ys[(r - L.r0) * ystr];
-    } else {
+    } else if (pipe == 1) {
       // S = d2(phi)/dy2 (visc3d, cross.f90:824)
-      const TailLoad T2{bf.tl2o + ((long)L.b * g.nkx + i) * SB_TAIL};
       SEG_SOLVE_P((const R *)bf.phi + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4],
                   g.rh2[5], g.rh2[6], false);
+    } else if (TEMP) {
+      // lap(tb) = d2(tb)/dy2 - k^2 tb, for the buoyancy of the phi equation and
+      // the diffusion of tb (crosst.f90:919-932,954-970)
+      SEG_SOLVE_P((const R *)bf.tb + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4],
+                  g.rh2[5], g.rh2[6], false);
+      if (L.active) {
+        const R *tb = (const R *)bf.tb + off;
+        R *lt = (R *)bf.Lt + off;
+        for (int r = L.r0; r <= L.r1; r++) {
+          const long q = (long)(r - 1) * ps;
+          lt[q] = (R)(-(k2 * (double)tb[q]) + ys[(r - L.r0) * ystr]);
+        }
+      }
+    }
+    __syncthreads();
+    if constexpr (TEMP) {
+      // phase 2: ht += d(-vT)/dy (crosst.f90:633-636,677)
+      if (pipe == 2) {
+        SEG_SOLVE_P((const R *)bf.R2 + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
+                    g.rh1[6], true);
+        if (L.active) {
+          R *ht = (R *)bf.Ht + off;
+          for (int r = L.r0; r <= L.r1; r++) {
+            const long q = (long)(r - 1) * ps;
+            ht[q] = ht[q] + (R)ys[(r - L.r0) * ystr];
+          }
+        }
+      } else {
+        seg_idle();
+      }
+      __syncthreads();
     }
   }
-  __syncthreads();
   {
-    // phase 2: right-hand sides of the Helmholtz equations and the zeta
-    // stores (cross.f90:800-867,886-941); omega_y'' from Lv, taken at the end
-    // of the previous substep (or by the prologue)
-    const R *h0 = pipe ? (const R *)bf.V + off : (const R *)bf.G + off;
-    R *f = pipe ? (R *)bf.phi + off : (R *)bf.vor + off;
-    R *fwk = pipe ? (R *)bf.phiwk + off : (R *)bf.vorwk + off;
-    R *rhs_out = pipe ? (R *)bf.S + off : (R *)bf.T + off;
+    // phase 3: right-hand sides of the Helmholtz equations and the zeta
+    // stores (cross.f90:800-867,886-941; crosst.f90:934-1028,1106-1125);
+    // omega_y'' from Lv, taken at the end of the previous substep (or by the
+    // prologue)
+    const R *h0 = pipe == 0 ? (const R *)bf.G + off
+                            : (pipe == 1 ? (const R *)bf.V + off : (const R *)bf.Ht + off);
+    R *f = pipe == 0 ? (R *)bf.vor + off : (pipe == 1 ? (R *)bf.phi + off : (R *)bf.tb + off);
+    R *fwk = pipe == 0 ? (R *)bf.vorwk + off
+                       : (pipe == 1 ? (R *)bf.phiwk + off : (R *)bf.tbwk + off);
+    R *rhs_out = pipe == 0 ? (R *)bf.T + off : (pipe == 1 ? (R *)bf.S + off : (R *)bf.R2 + off);
     const R *lv = (const R *)bf.Lv + off;
+    const R *lt = TEMP ? (const R *)bf.Lt + off : nullptr;
     const double *ys0 = ys - 32 * kSeg * pipe;  // pipeline 0's column (T)
+    const double fvis = pipe == 2 ? fat : fa, fscale = pipe == 2 ? fbt : fb;
     const int c = L.c;
 #pragma unroll 2
     for (int r = L.r0; r <= L.r1; r++) {
       const int j = r - 1;
       const long q = (long)j * ps;
       R h = h0[q];
-      if (pipe) h = h - (R)ys0[(r - L.r0) * ystr];  // hv = hv - d/dy(...)
+      if (pipe == 1) {
+        h = h - (R)ys0[(r - L.r0) * ystr];  // hv = hv - d/dy(...)
+        if (TEMP && !is00) h = h + (R)(g.gbeta * (double)lt[q]);  // buoyancy
+      }
       const R fo = f[q];
       const R wk = (rk == 0) ? gk * h : fwk[q] + gk * h;
-      const double d2 = pipe ? ys[(r - L.r0) * ystr] : (double)lv[q];
       double w = (double)wk;
-      if (!is00) w = w + fa * (-(k2 * (double)fo) + d2);
-      w = fb * (w + rdt * (double)fo);
+      if (!is00) {
+        const double lap = pipe == 0 ? -(k2 * (double)fo) + (double)lv[q]
+                                     : (pipe == 1 ? -(k2 * (double)fo) + ys[(r - L.r0) * ystr]
+                                                  : (double)lt[q]);
+        w = w + fvis * lap;
+      }
+      w = fscale * (w + rdt * (double)fo);
       const cd m2 = ldc2(mf2 + (long)j * 2 * g.nkx);
       const double rm = cmul_c(w, __shfl_xor_sync(0xffffffffu, w, 1), m2, c);
       double zs = 0.0;
@@ -857,17 +946,22 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1
     }
   }
   __syncthreads();
-  // phases 3-5 at the phase of time t + c_k dt
+  // phases 4-6 at the phase of time t + c_k dt
   const cd shp = ldc2(bf.sh_new + (long)L.b * 4 * g.nkx + 2 * i);
   const cd shm = ldc2(bf.sh_new + (long)L.b * 4 * g.nkx + 2 * (g.nkx + i));
   {
-    // phase 3: the Helmholtz solves (cross.f90:894-925)
-    const FacView VI(bf.hi, hline0 + hz_line(g, L.lc));
-    const SegView WI(bf.hi, hline0 + hz_line(g, L.lc));
+    // phase 4: the Helmholtz solves (cross.f90:894-925; crosst.f90:1094-1104)
+    const Fac &FI = pipe == 2 ? bf.hit : bf.hi;
+    const FacView VI(FI, hline0 + hz_line(g, L.lc));
+    const SegView WI(FI, hline0 + hz_line(g, L.lc));
     const TailMake TI{VI, shp, N};
-    const R *src = pipe ? (const R *)bf.S + off : (const R *)bf.T + off;
+    const R *src = pipe == 0 ? (const R *)bf.T + off
+                             : (pipe == 1 ? (const R *)bf.S + off : (const R *)bf.R2 + off);
     SEG_SOLVE_P(src, ps, VI, WI, TI, shp, shm, g.pr2[3], g.pr2[4], g.pr2[5], g.pr2[6], false);
-    if (!is00) store_col(ys, ystr, pipe ? (R *)bf.phi + off : (R *)bf.vor + off, ps, L);
+    if (!is00)
+      store_col(ys, ystr,
+                pipe == 0 ? (R *)bf.vor + off : (pipe == 1 ? (R *)bf.phi + off : (R *)bf.tb + off),
+                ps, L);
   }
   __syncthreads();  // whole updated lines are read below
   const TailLoad T1{bf.tl1n + ((long)L.b * g.nkx + i) * SB_TAIL};
@@ -876,7 +970,7 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1
     SEG_SOLVE_P((const R *)bf.vor + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
                 g.rh1[6], true);
     store_col(ys, ystr, (R *)bf.D + off, ps, L);
-  } else {
+  } else if (pipe == 1) {
     // v = lapcdy(phi, k^2) (cross.f90:942-956); hg(0,0) keeps the value the
     // nonlinear stage left (zero)
     const FacView VH(bf.hz, hz_line(g, L.lc));
@@ -885,6 +979,8 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1
     SEG_SOLVE_P((const R *)bf.phi + off, ps, VH, WH, TH, shp, shm, g.pr2[3], g.pr2[4], g.pr2[5],
                 g.pr2[6], false);
     if (!is00) store_col(ys, ystr, (R *)bf.G + off, ps, L);
+  } else {
+    seg_idle();
   }
   __syncthreads();  // v of all segments is read below
   if (pipe == 0) {
@@ -893,11 +989,13 @@ __global__ void __launch_bounds__(64 * kSeg, 1) k_lineI(Grid g, Bufs bf, int rk1
     SEG_SOLVE_P((const R *)bf.vor + off, ps, V2, W2, T2, shp, shm, g.rh2[3], g.rh2[4], g.rh2[5],
                 g.rh2[6], false);
     store_col(ys, ystr, (R *)bf.Lv + off, ps, L);
-  } else {
+  } else if (pipe == 1) {
     // dv/dy (cross.f90:442)
     SEG_SOLVE_P((const R *)bf.G + off, ps, V1, W1, T1, shp, shm, 0.0, g.rh1[4], g.rh1[5],
                 g.rh1[6], true);
     store_col(ys, ystr, (R *)bf.V + off, ps, L);
+  } else {
+    seg_idle();
   }
 }
 
@@ -1094,16 +1192,18 @@ static size_t smem_of(const Grid &g) {
 // the exported launchers of this compilation (sb::seg<K>::name_f64/_f32)
 size_t SB_PSUF(line_smem)(const Grid &g) { return smem_of(g); }
 
-// k_lineF (two pipelines: twice the threads and columns of the split
-// kernels, two exchange areas) fits the device's shared memory per block
-bool SB_PSUF(lineF_fits)(const Grid &g) {
+// a block of np pipelines (k_lineF, k_lineI: np times the threads and
+// columns of the split kernels, np exchange areas) fits the device's shared
+// memory per block
+bool SB_PSUF(lineI_fits)(const Grid &g, int np) {
   int dev = 0, optin = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
     return false;
-  const size_t xs = sizeof(double) * 2 * kSeg * 16 * 2 * SB_XS;
-  return 2 * smem_of(g) + xs <= (size_t)optin;
+  const size_t xs = sizeof(double) * np * kSeg * 16 * 2 * SB_XS;
+  return np * smem_of(g) + xs <= (size_t)optin;
 }
+bool SB_PSUF(lineF_fits)(const Grid &g) { return SB_PSUF(lineI_fits)(g, 2); }
 
 cudaError_t SB_PSUF(prepare_line)(const Grid &g) {
   typedef SbR R;
@@ -1117,8 +1217,10 @@ cudaError_t SB_PSUF(prepare_line)(const Grid &g) {
   cudaFuncSetAttribute(k_meand1<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   if (SB_PSUF(lineF_fits)(g)) {
     cudaFuncSetAttribute(k_lineF<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * sm);
-    cudaFuncSetAttribute(k_lineI<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * sm);
+    cudaFuncSetAttribute(k_lineI<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * sm);
   }
+  if (SB_PSUF(lineI_fits)(g, 3))
+    cudaFuncSetAttribute(k_lineI<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 3 * sm);
   return cudaGetLastError();
 }
 
@@ -1152,7 +1254,10 @@ cudaError_t SB_PSUF(lineF)(const Grid &g, const Bufs &bf, int rk, cudaStream_t s
 cudaError_t SB_PSUF(lineI)(const Grid &g, const Bufs &bf, int rk, cudaStream_t st) {
   typedef SbR R;
   const unsigned nb = (unsigned)(g.B * (g.ngrp + 1));
-  k_lineI<R><<<nb, 2 * kLineT, 2 * smem_of(g), st>>>(g, bf, rk);
+  if (g.temp)
+    k_lineI<R, true><<<nb, 3 * kLineT, 3 * smem_of(g), st>>>(g, bf, rk);
+  else
+    k_lineI<R, false><<<nb, 2 * kLineT, 2 * smem_of(g), st>>>(g, bf, rk);
   return cudaGetLastError();
 }
 

@@ -4,7 +4,8 @@ unidirectional mean flows) the branch is the scalar recurrence
     f_k (1 - beta_k Dt lam) = f_{k-1} (1 + alpha_k Dt lam)
 per substep, lam = -nu (k^2 + kappa^2) with kappa^2 the compact scheme's
 modified wavenumber of the y profile; the shear case follows the
-rapid-distortion solution like the explicit branch."""
+rapid-distortion solution like the explicit branch; crosst's branch adds the
+scalar (semi-implicit diffusion, explicit buoyancy)."""
 import numpy as np
 import pytest
 
@@ -114,9 +115,9 @@ def test_rdt_single_wave_implicit():
     assert np.abs(np.abs(v) / expected - 1).max() < 2e-5
 
 
-def test_implicit_refused_with_les_or_temperature():
+def test_implicit_refused_with_les_or_zero_diffusivity():
     pp = box_params(64, 32, 32, rez=1000.0)
-    for kw in ({"les": 1}, {"temperature": 1}):
+    for kw in ({"les": 1}, {"temperature": 1, "fkappa": 0.0}):
         with pytest.raises(ValueError):
             oracle.Oracle(**pp, **kw, implicit_visc=1)
 
@@ -136,3 +137,81 @@ def test_seeded_turbulence_close_to_explicit():
     for k in ("vor", "phi"):
         d = np.linalg.norm(out[0][k] - out[1][k]) / np.linalg.norm(out[0][k])
         assert 1e-12 < d < 1e-4, (k, d)
+
+
+# ---- crosst's semi-implicit branch (crosst.f90:916-1195)
+
+def _rest_scalar_recurrence(T, P, n, dt, kap, nu, k2, gb):
+    """Fluid at rest, one y-constant line (kx, 0): the scalar diffuses
+    semi-implicitly (fkappa), the buoyancy -gbeta k^2 T of the substep's start
+    drives phi as a nonlinear term (gama/zeta), phi's viscous term is
+    semi-implicit."""
+    gama, zeta = (8 / 15, 5 / 12, 3 / 4), (-17 / 60, -5 / 12, 0.0)
+    lt, lp = -kap * k2, -nu * k2
+    for _ in range(n):
+        hold = 0.0
+        for k in range(3):
+            h = -gb * k2 * T
+            extra = dt * (gama[k] * h + (zeta[k - 1] * hold if k else 0.0))
+            T, P = (T * (1 + ALPHA[k] * dt * lt) / (1 - BETA[k] * dt * lt),
+                    (P * (1 + ALPHA[k] * dt * lp) + extra) / (1 - BETA[k] * dt * lp))
+            hold = h
+    return T, P
+
+
+def test_rest_scalar_and_buoyancy_implicit():
+    """crosst at rest with implicit_visc: the line (kx=1, kz=0) follows the
+    semi-implicit recurrence of diffusion and buoyancy, at a step 10 times the
+    explicit thermal limit."""
+    from test_temperature_oracle import REST, BASE, _rest_state
+    kappa, gbeta, dt, n = 0.05, 0.7, 0.2, 6
+    o = oracle.Oracle(**dict(REST, fixed_dt=dt, fkappa=kappa, gbeta=gbeta), implicit_visc=1)
+    amp = 1e-7
+    st = _rest_state(o, amp, 0.0)
+    o.cross(st, n)
+    k2 = (BASE["alp"] * 1) ** 2
+    T_n, phi_n = _rest_scalar_recurrence(amp, 0.0, n, dt, kappa, 1.0 / BASE["Re"], k2, gbeta)
+    np.testing.assert_allclose(st["tb"][0, 1, :], T_n, rtol=1e-11, atol=0)
+    np.testing.assert_allclose(st["phi"][0, 1, :], phi_n, rtol=1e-9, atol=0)
+
+
+def test_rest_mean_scalar_implicit():
+    """tb00 = A cos(ky y) at rest decays with the implicit gain of fkappa and
+    the compact scheme's modified wavenumber (lapcdy(tb00wk, dtr1k),
+    crosst.f90:1158-1161)."""
+    from test_temperature_oracle import REST, _rest_state
+    kappa, dt, n = 0.05, 0.2, 6
+    o = oracle.Oracle(**dict(REST, fixed_dt=dt, fkappa=kappa, gbeta=0.7), implicit_visc=1)
+    st = _rest_state(o, 0.0, 0.3)
+    tb00_0 = st["tb00"].copy()
+    o.cross(st, n)
+    lam = kappa * o.derivyc(tb00_0, iord=2)[0] / tb00_0[0]
+    np.testing.assert_allclose(st["tb00"], _gain(lam, dt) ** n * tb00_0, rtol=1e-10, atol=1e-14)
+    assert np.all(st["tb"] == 0.0) and np.all(st["phi"] == 0.0)
+
+
+def test_crosst_implicit_close_to_explicit():
+    """Seeded turbulence with the scalar at a small step: the semi-implicit
+    crosst differs from the explicit one by the time-discretisation error of
+    the viscous and diffusive terms, except on the (0,0) line of tb, which the
+    explicit branch advances with ht(0,0) (crosst.f90:813-826) and the
+    semi-implicit one leaves alone (its solves skip (0,0),
+    crosst.f90:1094-1104)."""
+    import shear_nnf_gb300 as sb
+    pp = box_params(64, 32, 32, rez=1000.0, fixed_dt=0.002, temperature=1, fkappa=0.02,
+                    bym=1.0, gbeta=0.5)
+    st0 = sb.seed_state(sb.make_params(**pp), 3)
+    out = []
+    for imp in (0, 1):
+        o = oracle.Oracle(**pp, implicit_visc=imp)
+        st = {k: (v.copy() if hasattr(v, "copy") else v) for k, v in st0.items()}
+        o.cross(st, 10)
+        out.append(st)
+    for st in out:
+        assert np.all(np.isfinite(st["tb"]))
+    assert np.all(out[1]["tb"][0, 0] == 0.0) and np.abs(out[0]["tb"][0, 0]).max() > 0
+    for st in out:
+        st["tb"][0, 0] = 0.0
+    for k in ("vor", "phi", "tb", "tb00"):
+        d = np.linalg.norm(out[0][k] - out[1][k]) / np.linalg.norm(out[0][k])
+        assert 1e-12 < d < 1e-5, (k, d)
