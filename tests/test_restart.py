@@ -118,6 +118,20 @@ def test_params_from_restart(tmp_path):
             assert getattr(q, name) == pytest.approx(getattr(p, name), rel=1e-14, abs=1e-300), name
     r = sb.params_from_restart(info, Re=2.0, damping=0)
     assert r.Re == 2.0 and r.damping == 0 and r.force == 2
+    assert q.implicit_visc == 0
+
+
+def test_footer_records_the_integrator(tmp_path):
+    """The first footer switch is the reference's explicit flag: 1 for the
+    explicit branch, 0 for the semi-implicit one (implicit_visc)."""
+    st = sb.seed_state(sb.make_params(**box_params(64, 32, 32, 1000.0)), 2)
+    f = tmp_path / "i.bin"
+    for imp in (0, 1):
+        p = sb.make_params(**box_params(64, 32, 32, 1000.0), implicit_visc=imp)
+        sb.write_restart(f, p, st)
+        assert struct.unpack("<9i", _records(f)[-2])[0] == 1 - imp
+        _, info = sb.read_restart(f)
+        assert sb.params_from_restart(info).implicit_visc == imp
 
 
 @pytest.mark.parametrize("target", [(96, 32, 48), (48, 32, 32)])
