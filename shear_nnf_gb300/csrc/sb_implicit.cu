@@ -158,14 +158,41 @@ __global__ void __launch_bounds__(128) k_hfac(Grid g, Bufs bf, int rk, int which
     brow(1, b1, true);
     brow(2, b2 - l1 * dd1 * La[at(1)], true);
     brow(3, b3 - l2 * dd2 * Lb[at(2)] - l1 * dd1 * La[at(2)], true);
-#pragma unroll 4
-    for (int i = 4; i <= n - 6; i++) {
+    // The border rows decay geometrically along the band (a linear recurrence
+    // of the diagonally dominant factors): once the last three entries of
+    // every line of the warp are below 2^-64 of their largest (checked every
+    // fourth row), all further entries and their share of the sums lie below
+    // FP64 rounding and are written as zeros.
+    double lmax = fmax(fabs(l1), fmax(fabs(l2), fabs(l3)));
+    int i = 4;
+    bool cut = false;
+    for (; i <= n - 6; i++) {
       const long o = at(i - 1);
       brow(i, -(l3 * dd3 * Lc[o]) - l2 * dd2 * Lb[o] - l1 * dd1 * La[o], true);
+      if ((i & 3) == 3) {
+        lmax = fmax(lmax, fmax(fabs(l1), fmax(fabs(l2), fabs(l3))));
+        const double thr = lmax * 0x1p-64;
+        const bool small = !on || (fabs(l1) <= thr && fabs(l2) <= thr && fabs(l3) <= thr);
+        if (__all_sync(0xffffffffu, small)) {
+          cut = true;
+          i++;
+          break;
+        }
+      }
     }
-    for (int i = n - 5; i <= n - 4; i++) {
-      const long o = at(i - 1);
-      brow(i, -(l3 * dd3 * Lc[o]) - l2 * dd2 * Lb[o] - l1 * dd1 * La[o], i <= last);
+    if (cut) {
+      if (wr) {
+        double *Lp = part == 0 ? E : (part == 1 ? Fb : Gb);
+        for (int r = i; r <= last; r++) {
+          Lp[at(r - 1)] = 0.0;
+          rows[at(r - 1) * 16 + 3 + part] = 0.0;
+        }
+      }
+    } else {
+      for (i = n - 5; i <= n - 4; i++) {
+        const long o = at(i - 1);
+        brow(i, -(l3 * dd3 * Lc[o]) - l2 * dd2 * Lb[o] - l1 * dd1 * La[o], i <= last);
+      }
     }
     if (wr) {
       if (part == 0) {
@@ -188,9 +215,11 @@ __global__ void __launch_bounds__(128) k_hfac(Grid g, Bufs bf, int rk, int which
     double *hf = const_cast<double *>(F.hf[part]), *hb = const_cast<double *>(F.hb[part]);
     for (int sg = 0; sg < g.nseg; sg++) {
       const int lo = g.slo[sg], hi = g.shi[sg];
+      // the homogeneous solutions decay away from their unit start like the
+      // border rows: below 2^-64 over three rows, the rest is written as zeros
       double h1 = (t == 1), h2 = (t == 2), h3 = (t == 3), se = 0.0, sf = 0.0, sgs = 0.0;
-#pragma unroll 4
-      for (int i = lo; i <= hi; i++) {
+      int i = lo;
+      for (; i <= hi; i++) {
         const long o = at(i - 1);
         const double h = -Lc[o] * h3 - Lb[o] * h2 - La[o] * h1;
         se += E[o] * h;
@@ -201,7 +230,17 @@ __global__ void __launch_bounds__(128) k_hfac(Grid g, Bufs bf, int rk, int which
           rows[o * 16 + 8 + part] = h;
         }
         h3 = h2; h2 = h1; h1 = h;
+        if (((i - lo) & 3) == 3 && fabs(h1) <= 0x1p-64 && fabs(h2) <= 0x1p-64 &&
+            fabs(h3) <= 0x1p-64) {
+          i++;
+          break;
+        }
       }
+      if (wr)
+        for (; i <= hi; i++) {
+          hf[at(i - 1)] = 0.0;
+          rows[at(i - 1) * 16 + 8 + part] = 0.0;
+        }
       if (wr) {
         ef[at((sg * 3 + 0) * 3 + t - 1)] = se;
         ef[at((sg * 3 + 1) * 3 + t - 1)] = sf;
@@ -209,16 +248,26 @@ __global__ void __launch_bounds__(128) k_hfac(Grid g, Bufs bf, int rk, int which
       }
       if (sg < g.nseg - 1) {
         double g1 = (t == 1), g2 = (t == 2), g3 = (t == 3);
-#pragma unroll 4
-        for (int i = hi; i >= lo; i--) {
+        int ib = hi;
+        for (; ib >= lo; ib--) {
           // rows above n-3 hold zeros (at() of seg_factor)
-          const double v = -La[at(i)] * g1 - Lb[at(i + 1)] * g2 - Lc[at(i + 2)] * g3;
+          const double v = -La[at(ib)] * g1 - Lb[at(ib + 1)] * g2 - Lc[at(ib + 2)] * g3;
           if (wr) {
-            hb[at(i - 1)] = v;
-            rows[at(i - 1) * 16 + 12 + part] = v;
+            hb[at(ib - 1)] = v;
+            rows[at(ib - 1) * 16 + 12 + part] = v;
           }
           g3 = g2; g2 = g1; g1 = v;
+          if (((hi - ib) & 3) == 3 && fabs(g1) <= 0x1p-64 && fabs(g2) <= 0x1p-64 &&
+              fabs(g3) <= 0x1p-64) {
+            ib--;
+            break;
+          }
         }
+        if (wr)
+          for (; ib >= lo; ib--) {
+            hb[at(ib - 1)] = 0.0;
+            rows[at(ib - 1) * 16 + 12 + part] = 0.0;
+          }
       }
     }
   }
