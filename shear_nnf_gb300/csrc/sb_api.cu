@@ -113,7 +113,8 @@ static int check_params(const sb_params *p) {
   if (p->mgalx <= 0 || p->my <= 0 || p->mgalz <= 0)
     return fail(1, "mgalx grid error %d %d %d", p->mgalx, p->my, p->mgalz);  // initcr.f90:188
   if (!supported_grid(p->mgalx, p->mgalz))
-    return fail(1, "unsupported x/z grid %d x %d (transform lengths 32,48,64,96,192[,384])",
+    return fail(1, "unsupported x/z grid %d x %d (transform lengths 32,48,64,80,96,128,160,192,256 "
+                   "and for x also 320,384)",
                 p->mgalx, p->mgalz);
   if (p->mgalz % 2) return fail(1, "mgalz must be even");
   if (p->my < 16 || p->my > kMaxMy) return fail(1, "my=%d outside 16..%d", p->my, kMaxMy);

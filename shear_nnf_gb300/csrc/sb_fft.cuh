@@ -8,7 +8,7 @@
 // reversal).
 //
 // Two forms share the stage layout:
-//  * fft_batch_std: radix 4/2/3 stages, twiddles from a per-length table of
+//  * fft_batch_std: radix 4/2/3/5 stages, twiddles from a per-length table of
 //    e^{-2 pi i t/N} (FP32 storage and the standalone y operators);
 //  * the FP64 form (fft_batch on double2): GB300 issues one FP64 instruction per
 //    two lanes and cycle on each SM sub-partition, so FP64 instruction count is
@@ -66,6 +66,28 @@ __device__ __forceinline__ void butterfly(R2 *v) {
     v[2].x = a0.x - b0.x; v[2].y = a0.y - b0.y;
     v[1].x = a1.x + jb.x; v[1].y = a1.y + jb.y;
     v[3].x = a1.x - jb.x; v[3].y = a1.y - jb.y;
+  } else if constexpr (R == 5) {
+    // X_k = sum_n v_n w^(nk), w = exp(SIGN 2 pi i/5), from the sums and
+    // differences of the symmetric pairs (v1, v4), (v2, v3)
+    typedef decltype(v[0].x) T;
+    const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;  // cos(2pi/5), cos(4pi/5)
+    const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;   // sin(2pi/5), sin(4pi/5)
+    R2 t1, t2, t3, t4, a1, a2, b1, b2;
+    t1.x = v[1].x + v[4].x; t1.y = v[1].y + v[4].y;
+    t2.x = v[2].x + v[3].x; t2.y = v[2].y + v[3].y;
+    t3.x = v[1].x - v[4].x; t3.y = v[1].y - v[4].y;
+    t4.x = v[2].x - v[3].x; t4.y = v[2].y - v[3].y;
+    a1.x = v[0].x + c1 * t1.x + c2 * t2.x; a1.y = v[0].y + c1 * t1.y + c2 * t2.y;
+    a2.x = v[0].x + c2 * t1.x + c1 * t2.x; a2.y = v[0].y + c2 * t1.y + c1 * t2.y;
+    b1.x = s1 * t3.x + s2 * t4.x; b1.y = s1 * t3.y + s2 * t4.y;
+    b2.x = s2 * t3.x - s1 * t4.x; b2.y = s2 * t3.y - s1 * t4.y;
+    // i SIGN b = SIGN (-b.y, b.x)
+    const T sg = (SIGN < 0) ? (T)-1 : (T)1;
+    v[0].x = v[0].x + t1.x + t2.x; v[0].y = v[0].y + t1.y + t2.y;
+    v[1].x = a1.x - sg * b1.y; v[1].y = a1.y + sg * b1.x;
+    v[4].x = a1.x + sg * b1.y; v[4].y = a1.y - sg * b1.x;
+    v[2].x = a2.x - sg * b2.y; v[2].y = a2.y + sg * b2.x;
+    v[3].x = a2.x + sg * b2.y; v[3].y = a2.y - sg * b2.x;
   } else if constexpr (R == 3) {
     typedef decltype(v[0].x) T;
     const T s3 = (T)0.86602540378443864676;  // sin(pi/3)
@@ -131,6 +153,35 @@ __device__ __forceinline__ R2 *fft_batch_std(R2 *A, R2 *B, const R2 *__restrict_
     fft_stage<64, 4, 4, SIGN, M, T>(B, A, tw); __syncthreads();
     fft_stage<64, 16, 4, SIGN, M, T>(A, B, tw); __syncthreads();
     return B;
+  } else if constexpr (N == 80) {
+    fft_stage<80, 1, 5, SIGN, M, T>(A, B, tw); __syncthreads();
+    fft_stage<80, 5, 4, SIGN, M, T>(B, A, tw); __syncthreads();
+    fft_stage<80, 20, 4, SIGN, M, T>(A, B, tw); __syncthreads();
+    return B;
+  } else if constexpr (N == 128) {
+    fft_stage<128, 1, 4, SIGN, M, T>(A, B, tw); __syncthreads();
+    fft_stage<128, 4, 4, SIGN, M, T>(B, A, tw); __syncthreads();
+    fft_stage<128, 16, 4, SIGN, M, T>(A, B, tw); __syncthreads();
+    fft_stage<128, 64, 2, SIGN, M, T>(B, A, tw); __syncthreads();
+    return A;
+  } else if constexpr (N == 160) {
+    fft_stage<160, 1, 5, SIGN, M, T>(A, B, tw); __syncthreads();
+    fft_stage<160, 5, 4, SIGN, M, T>(B, A, tw); __syncthreads();
+    fft_stage<160, 20, 4, SIGN, M, T>(A, B, tw); __syncthreads();
+    fft_stage<160, 80, 2, SIGN, M, T>(B, A, tw); __syncthreads();
+    return A;
+  } else if constexpr (N == 256) {
+    fft_stage<256, 1, 4, SIGN, M, T>(A, B, tw); __syncthreads();
+    fft_stage<256, 4, 4, SIGN, M, T>(B, A, tw); __syncthreads();
+    fft_stage<256, 16, 4, SIGN, M, T>(A, B, tw); __syncthreads();
+    fft_stage<256, 64, 4, SIGN, M, T>(B, A, tw); __syncthreads();
+    return A;
+  } else if constexpr (N == 320) {
+    fft_stage<320, 1, 5, SIGN, M, T>(A, B, tw); __syncthreads();
+    fft_stage<320, 5, 4, SIGN, M, T>(B, A, tw); __syncthreads();
+    fft_stage<320, 20, 4, SIGN, M, T>(A, B, tw); __syncthreads();
+    fft_stage<320, 80, 4, SIGN, M, T>(B, A, tw); __syncthreads();
+    return A;
   } else if constexpr (N == 96) {
     fft_stage<96, 1, 4, SIGN, M, T>(A, B, tw); __syncthreads();
     fft_stage<96, 4, 4, SIGN, M, T>(B, A, tw); __syncthreads();
@@ -222,6 +273,26 @@ __device__ __forceinline__ void gstage3(const double2 *__restrict__ in, double2 
       dst[1] = make_double2(fma(s3, dy, hx), fma(-s3, dx, hy));
       dst[2] = make_double2(fma(-s3, dy, hx), fma(s3, dx, hy));
     }
+  }
+}
+
+// radix-5 stage without twiddles (first stage, Ns = 1): the 5-point DFT of
+// butterfly<5>, 36 FP64 instructions
+template <int N, int SIGN, int M, int T>
+__device__ __forceinline__ void gstage5_first(const double2 *__restrict__ in,
+                                              double2 *__restrict__ out) {
+  constexpr int NR = N / 5;
+  for (int bt = threadIdx.x; bt < M * NR; bt += T) {
+    const int m = bt / NR;
+    const int j = bt - m * NR;
+    const double2 *src = in + m * N;
+    double2 *dst = out + m * N + 5 * j;
+    double2 v[5];
+#pragma unroll
+    for (int r = 0; r < 5; r++) v[r] = src[j + r * NR];
+    butterfly<5, SIGN>(v);
+#pragma unroll
+    for (int r = 0; r < 5; r++) dst[r] = v[r];
   }
 }
 
@@ -323,6 +394,35 @@ __device__ __forceinline__ double2 *fft_batch_g(double2 *A, double2 *B,
     gstage4<64, 4, SIGN, M, T>(B, A, G); __syncthreads();
     gstage4<64, 16, SIGN, M, T>(A, B, G); __syncthreads();
     return B;
+  } else if constexpr (N == 80) {
+    gstage5_first<80, SIGN, M, T>(A, B); __syncthreads();
+    gstage4<80, 5, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<80, 20, SIGN, M, T>(A, B, G); __syncthreads();
+    return B;
+  } else if constexpr (N == 128) {
+    gstage4_first<128, SIGN, M, T>(A, B); __syncthreads();
+    gstage4<128, 4, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<128, 16, SIGN, M, T>(A, B, G); __syncthreads();
+    gstage2<128, 64, SIGN, M, T>(B, A, G); __syncthreads();
+    return A;
+  } else if constexpr (N == 160) {
+    gstage5_first<160, SIGN, M, T>(A, B); __syncthreads();
+    gstage4<160, 5, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<160, 20, SIGN, M, T>(A, B, G); __syncthreads();
+    gstage2<160, 80, SIGN, M, T>(B, A, G); __syncthreads();
+    return A;
+  } else if constexpr (N == 256) {
+    gstage4_first<256, SIGN, M, T>(A, B); __syncthreads();
+    gstage4<256, 4, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<256, 16, SIGN, M, T>(A, B, G); __syncthreads();
+    gstage4<256, 64, SIGN, M, T>(B, A, G); __syncthreads();
+    return A;
+  } else if constexpr (N == 320) {
+    gstage5_first<320, SIGN, M, T>(A, B); __syncthreads();
+    gstage4<320, 5, SIGN, M, T>(B, A, G); __syncthreads();
+    gstage4<320, 20, SIGN, M, T>(A, B, G); __syncthreads();
+    gstage4<320, 80, SIGN, M, T>(B, A, G); __syncthreads();
+    return A;
   } else if constexpr (N == 96 && SB_FFT_PLAN == 1) {
     gstage3<96, SIGN, M, T, GAP>(A, B); __syncthreads();
     gstage2<96, 3, SIGN, M, T>(B, A, G); __syncthreads();

@@ -1075,9 +1075,9 @@ bool plane3_fits(const Grid &g, int cb) {
 int plane_cb(int) { return 8; }
 int plane_t2_default(int mgalx) {
   switch (mgalx) {
-    case 32: case 48: return 64;
-    case 64: case 96: return 96;
-    case 192: return 128;
+    case 32: case 48: case 80: return 64;
+    case 64: case 96: case 128: return 96;
+    case 160: case 192: return 128;
     default: return 256;
   }
 }
@@ -1161,8 +1161,13 @@ static cudaError_t launch_plane_t(const Grid &g, const Bufs &bf, int stage, int 
       case 32: e = launch_p2_t<R, 32, 64>(g, bf, rk, st, prep); break;
       case 48: e = launch_p2_t<R, 48, 64>(g, bf, rk, st, prep); break;
       case 64: e = launch_p2_t<R, 64, 96>(g, bf, rk, st, prep); break;
+      case 80: e = launch_p2_t<R, 80, 64>(g, bf, rk, st, prep); break;
       case 96: e = launch_p2_t<R, 96, 96>(g, bf, rk, st, prep); break;
+      case 128: e = launch_p2_t<R, 128, 96>(g, bf, rk, st, prep); break;
+      case 160: e = launch_p2_t<R, 160, 128>(g, bf, rk, st, prep); break;
       case 192: e = launch_p2_t<R, 192, 128>(g, bf, rk, st, prep); break;
+      case 256: e = launch_p2_t<R, 256, 256>(g, bf, rk, st, prep); break;
+      case 320: e = launch_p2_t<R, 320, 256>(g, bf, rk, st, prep); break;
       case 384: e = launch_p2_t<R, 384, 256>(g, bf, rk, st, prep); break;
       default: return cudaErrorInvalidValue;
     }
@@ -1172,8 +1177,12 @@ static cudaError_t launch_plane_t(const Grid &g, const Bufs &bf, int stage, int 
     case 32: return launch_p13_cb<R, 32>(g, bf, rk, st, stage, prep);
     case 48: return launch_p13_cb<R, 48>(g, bf, rk, st, stage, prep);
     case 64: return launch_p13_cb<R, 64>(g, bf, rk, st, stage, prep);
+    case 80: return launch_p13_cb<R, 80>(g, bf, rk, st, stage, prep);
     case 96: return launch_p13_cb<R, 96>(g, bf, rk, st, stage, prep);
+    case 128: return launch_p13_cb<R, 128>(g, bf, rk, st, stage, prep);
+    case 160: return launch_p13_cb<R, 160>(g, bf, rk, st, stage, prep);
     case 192: return launch_p13_cb<R, 192>(g, bf, rk, st, stage, prep);
+    case 256: return launch_p13_cb<R, 256>(g, bf, rk, st, stage, prep);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -1225,7 +1234,12 @@ static cudaError_t launch_les_t(const Grid &g, const Bufs &bf, int stage, int rk
       case 48: e = launch_les_x<R, 48, 64>(g, bf, stage, rk, st, prep); break;
       case 64: e = launch_les_x<R, 64, 96>(g, bf, stage, rk, st, prep); break;
       case 96: e = launch_les_x<R, 96, 96>(g, bf, stage, rk, st, prep); break;
+      case 80: e = launch_les_x<R, 80, 64>(g, bf, stage, rk, st, prep); break;
+      case 128: e = launch_les_x<R, 128, 96>(g, bf, stage, rk, st, prep); break;
+      case 160: e = launch_les_x<R, 160, 128>(g, bf, stage, rk, st, prep); break;
       case 192: e = launch_les_x<R, 192, 128>(g, bf, stage, rk, st, prep); break;
+      case 256: e = launch_les_x<R, 256, 256>(g, bf, stage, rk, st, prep); break;
+      case 320: e = launch_les_x<R, 320, 256>(g, bf, stage, rk, st, prep); break;
       case 384: e = launch_les_x<R, 384, 256>(g, bf, stage, rk, st, prep); break;
       default: return cudaErrorInvalidValue;
     }
@@ -1235,8 +1249,12 @@ static cudaError_t launch_les_t(const Grid &g, const Bufs &bf, int stage, int rk
     case 32: return launch_les_z<R, 32, 4>(g, bf, stage, st, prep);
     case 48: return launch_les_z<R, 48, 4>(g, bf, stage, st, prep);
     case 64: return launch_les_z<R, 64, 4>(g, bf, stage, st, prep);
+    case 80: return launch_les_z<R, 80, 4>(g, bf, stage, st, prep);
     case 96: return launch_les_z<R, 96, 4>(g, bf, stage, st, prep);
+    case 128: return launch_les_z<R, 128, 4>(g, bf, stage, st, prep);
+    case 160: return launch_les_z<R, 160, 4>(g, bf, stage, st, prep);
     case 192: return launch_les_z<R, 192, 2>(g, bf, stage, st, prep);
+    case 256: return launch_les_z<R, 256, 2>(g, bf, stage, st, prep);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -1339,8 +1357,8 @@ cudaError_t fp64_peak(double *tflops, cudaStream_t st) {
 }
 
 bool supported_grid(int mgalx, int mgalz) {
-  const int xs[] = {32, 48, 64, 96, 192, 384};
-  const int zs[] = {32, 48, 64, 96, 192};
+  const int xs[] = {32, 48, 64, 80, 96, 128, 160, 192, 256, 320, 384};
+  const int zs[] = {32, 48, 64, 80, 96, 128, 160, 192, 256};
   bool okx = false, okz = false;
   for (int v : xs) okx |= (v == mgalx);
   for (int v : zs) okz |= (v == mgalz);
@@ -1466,8 +1484,13 @@ static cudaError_t launch_phys_r(const Grid &g, const Bufs &bf, unsigned mask, d
     case 32: return launch_phys_t<R, 32, 64>(g, bf, mask, out, st);
     case 48: return launch_phys_t<R, 48, 64>(g, bf, mask, out, st);
     case 64: return launch_phys_t<R, 64, 96>(g, bf, mask, out, st);
+    case 80: return launch_phys_t<R, 80, 64>(g, bf, mask, out, st);
     case 96: return launch_phys_t<R, 96, 96>(g, bf, mask, out, st);
+    case 128: return launch_phys_t<R, 128, 96>(g, bf, mask, out, st);
+    case 160: return launch_phys_t<R, 160, 128>(g, bf, mask, out, st);
     case 192: return launch_phys_t<R, 192, 128>(g, bf, mask, out, st);
+    case 256: return launch_phys_t<R, 256, 256>(g, bf, mask, out, st);
+    case 320: return launch_phys_t<R, 320, 256>(g, bf, mask, out, st);
     case 384: return launch_phys_t<R, 384, 256>(g, bf, mask, out, st);
     default: return cudaErrorInvalidValue;
   }

@@ -1,18 +1,19 @@
 """Twiddle tables of the transforms (host code, sb_fft_twiddles): the factored
 FP64 form e^{-2 pi i t/n} = (-i)^q c (1 + i tau) reconstructs the complex table,
 keeps c >= cos(pi/4) and |tau| <= 1, and its swap bits and signs follow q; a
-numpy model of the device's FP64 stages (radix 3 first, fused radix-4 and
-radix-2 pairs, the 2/3-gap radix-3 stage) on these tables equals the DFT for
-every supported length.  The device stages themselves are checked by the GPU
+numpy model of the device's FP64 stages (radix 3 or 5 first, fused radix-4
+and radix-2 pairs, the 2/3-gap radix-3 stage) on these tables equals the DFT
+for every supported length.  The device stages themselves are checked by the GPU
 parity tests."""
 import numpy as np
 import pytest
 
 import shear_nnf_gb300 as sb
 
-LENGTHS = (32, 48, 64, 96, 192, 384)
-PLANS = {32: [4, 4, 2], 48: [3, 4, 4], 64: [4, 4, 4], 96: [3, 4, 4, 2], 192: [3, 4, 4, 4],
-         384: [3, 4, 4, 4, 2]}
+LENGTHS = (32, 48, 64, 80, 96, 128, 160, 192, 256, 320, 384)
+PLANS = {32: [4, 4, 2], 48: [3, 4, 4], 64: [4, 4, 4], 80: [5, 4, 4], 96: [3, 4, 4, 2],
+         128: [4, 4, 4, 2], 160: [5, 4, 4, 2], 192: [3, 4, 4, 4], 256: [4, 4, 4, 4],
+         320: [5, 4, 4, 4], 384: [3, 4, 4, 4, 2]}
 
 
 def _factored(n):
@@ -58,6 +59,16 @@ def _stage(x, n, ns, r, sign, tab, gap):
             t1, d = v1 + v[2], v1 - v[2]
             h = v[0] - 0.5 * t1
             X = [v[0] + t1, h + s3 * (d.imag - 1j * d.real), h - s3 * (d.imag - 1j * d.real)]
+        elif ns == 1 and r == 5:
+            # the 5-point DFT of butterfly<5> from the symmetric pairs
+            c1, c2 = np.cos(2 * np.pi / 5), np.cos(4 * np.pi / 5)
+            s1, s2 = np.sin(2 * np.pi / 5), np.sin(4 * np.pi / 5)
+            t1, t2, t3, t4 = v[1] + v[4], v[2] + v[3], v[1] - v[4], v[2] - v[3]
+            a1, a2 = v[0] + c1 * t1 + c2 * t2, v[0] + c2 * t1 + c1 * t2
+            b1, b2 = s1 * t3 + s2 * t4, s2 * t3 - s1 * t4
+            sg = -1 if sign < 0 else 1
+            X = [v[0] + t1 + t2, a1 + 1j * sg * b1, a2 + 1j * sg * b2, a2 - 1j * sg * b2,
+                 a1 - 1j * sg * b1]
         elif ns == 1 and r == 4:
             a0, a1, b0, b1 = v[0] + v[2], v[0] - v[2], v[1] + v[3], v[1] - v[3]
             jb = -1j * b1 if sign < 0 else 1j * b1
