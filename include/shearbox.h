@@ -333,7 +333,7 @@ int sb_op_filterc(int my, int nlines, const double *u, long ldu, double *out, lo
 
 /* y-line transforms in place on device lines (FFTW conventions; forward,
  * iopt < 0, scaled by 1/my; backward, iopt > 0, unscaled), my in
- * {32, 48, 64, 96, 192, 384}:
+ * {32, 48, 64, 80, 96, 128, 160, 192, 256, 320, 384}:
  *   sb_op_cfty  complex lines, element (line, j) at c + 2*(j*ldc + line):
  *               cfty, cftdoublew.F:151-201
  *   sb_op_rfty  real lines of my + 2 rows, element (line, j) at c + j*ldc + line;

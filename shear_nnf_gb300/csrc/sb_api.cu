@@ -108,7 +108,8 @@ static int check_params(const sb_params *p) {
   if (p && (p->ydeal < 0 || p->ydeal > 3))
     return fail(2, "iydealiasing=%d not available (0..3)", p->ydeal);
   if (p && (p->ydeal == 1 || p->ydeal == 2) && !supported_ylen(p->my))
-    return fail(2, "iydealiasing=%d needs my in 32,48,64,96,192,384 (y transforms)", p->ydeal);
+    return fail(2, "iydealiasing=%d needs my in 32,48,64,80,96,128,160,192,256,320,384 "
+                   "(y transforms)", p->ydeal);
   if (!p) return fail(1, "null parameters");
   if (p->mgalx <= 0 || p->my <= 0 || p->mgalz <= 0)
     return fail(1, "mgalx grid error %d %d %d", p->mgalx, p->my, p->mgalz);  // initcr.f90:188

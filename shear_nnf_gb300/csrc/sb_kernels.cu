@@ -1283,8 +1283,13 @@ static cudaError_t launch_ydeal_r(const Grid &g, const Bufs &bf, int rk, cudaStr
     case 32: return launch_ydeal_t<R, 32>(g, bf, rk, st, prep);
     case 48: return launch_ydeal_t<R, 48>(g, bf, rk, st, prep);
     case 64: return launch_ydeal_t<R, 64>(g, bf, rk, st, prep);
+    case 80: return launch_ydeal_t<R, 80>(g, bf, rk, st, prep);
     case 96: return launch_ydeal_t<R, 96>(g, bf, rk, st, prep);
+    case 128: return launch_ydeal_t<R, 128>(g, bf, rk, st, prep);
+    case 160: return launch_ydeal_t<R, 160>(g, bf, rk, st, prep);
     case 192: return launch_ydeal_t<R, 192>(g, bf, rk, st, prep);
+    case 256: return launch_ydeal_t<R, 256>(g, bf, rk, st, prep);
+    case 320: return launch_ydeal_t<R, 320>(g, bf, rk, st, prep);
     case 384: return launch_ydeal_t<R, 384>(g, bf, rk, st, prep);
     default: return cudaErrorInvalidValue;
   }
@@ -1292,7 +1297,10 @@ static cudaError_t launch_ydeal_r(const Grid &g, const Bufs &bf, int rk, cudaStr
 
 #if !SB_FLOAT_TU
 bool supported_ylen(int my) {
-  return my == 32 || my == 48 || my == 64 || my == 96 || my == 192 || my == 384;
+  const int ys[] = {32, 48, 64, 80, 96, 128, 160, 192, 256, 320, 384};
+  for (int v : ys)
+    if (v == my) return true;
+  return false;
 }
 
 template <int MY>
@@ -1307,8 +1315,13 @@ cudaError_t launch_yop(int my, int nlines, double *c, long ldc, int iopt, int re
     case 32: return launch_yop_t<32>(nlines, c, ldc, iopt, real, st);
     case 48: return launch_yop_t<48>(nlines, c, ldc, iopt, real, st);
     case 64: return launch_yop_t<64>(nlines, c, ldc, iopt, real, st);
+    case 80: return launch_yop_t<80>(nlines, c, ldc, iopt, real, st);
     case 96: return launch_yop_t<96>(nlines, c, ldc, iopt, real, st);
+    case 128: return launch_yop_t<128>(nlines, c, ldc, iopt, real, st);
+    case 160: return launch_yop_t<160>(nlines, c, ldc, iopt, real, st);
     case 192: return launch_yop_t<192>(nlines, c, ldc, iopt, real, st);
+    case 256: return launch_yop_t<256>(nlines, c, ldc, iopt, real, st);
+    case 320: return launch_yop_t<320>(nlines, c, ldc, iopt, real, st);
     case 384: return launch_yop_t<384>(nlines, c, ldc, iopt, real, st);
     default: return cudaErrorInvalidValue;
   }

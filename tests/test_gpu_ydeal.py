@@ -12,7 +12,7 @@ from test_gpu_step import _field_errors, _run_both, _trace_error
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("my", [32, 48, 96, 192])
+@pytest.mark.parametrize("my", [32, 48, 80, 96, 128, 160, 192, 256, 320])
 def test_op_y_transforms(my):
     import torch
     import shear_nnf_gb300 as sb
@@ -58,7 +58,9 @@ def test_op_filterc(my):
 @pytest.mark.parametrize("grid,kw", [((64, 32, 32), {"ydeal": 1, "fixed_dt": 0.005}),
                                      ((96, 48, 48), {"ydeal": 1}),
                                      ((64, 32, 32), {"ydeal": 2, "fixed_dt": 0.005}),
-                                     ((96, 48, 48), {"ydeal": 2})])
+                                     ((96, 48, 48), {"ydeal": 2}),
+                                     ((64, 80, 32), {"ydeal": 1}),
+                                     ((64, 128, 64), {"ydeal": 2})])
 def test_ydeal_step(grid, kw):
     pp = box_params(*grid, rez=4000.0, **kw)
     st_o, tr_o, st_g, tr_g, status = _run_both(pp, 1)
