@@ -114,8 +114,8 @@ static int check_params(const sb_params *p) {
   if (p->mgalx <= 0 || p->my <= 0 || p->mgalz <= 0)
     return fail(1, "mgalx grid error %d %d %d", p->mgalx, p->my, p->mgalz);  // initcr.f90:188
   if (!supported_grid(p->mgalx, p->mgalz))
-    return fail(1, "unsupported x/z grid %d x %d (transform lengths 32,48,64,80,96,128,160,192,256 "
-                   "and for x also 320,384)",
+    return fail(1, "unsupported x/z grid %d x %d (transform lengths 32,48,64,80,96,128,160,192,256,"
+                   "384 and for x also 320)",
                 p->mgalx, p->mgalz);
   if (p->mgalz % 2) return fail(1, "mgalz must be even");
   if (p->my < 16 || p->my > kMaxMy) return fail(1, "my=%d outside 16..%d", p->my, kMaxMy);
@@ -125,6 +125,10 @@ static int check_params(const sb_params *p) {
     return fail(2, "iadd_damping=%d not available (0, 1)", p->damping);
   if (p->force < -1 || p->force > 2)
     return fail(2, "iadd_force=%d not available (-1, 0, 1, 2)", p->force);
+  // plane stage 3 holds 3 (6 with the temperature) columns of mgalz points
+  // in shared memory, at least 4 columns per block
+  if (p->temperature && p->mgalz > 256)
+    return fail(2, "itemperature=1 needs mgalz <= 256 (got %d)", p->mgalz);
   if (p->implicit_visc != 0 && p->implicit_visc != 1)
     return fail(2, "implicit_visc=%d not available (0, 1)", p->implicit_visc);
   // LES with explicit = 0 stops the reference (initcr.f90:2179-2182); the
@@ -644,7 +648,7 @@ int sb_create(const sb_params *p, int batch, int precision, sb_handle **out) {
     sb_destroy(h);
     return rc;
   }
-  if (g.temp && !plane3_fits(g, g.cb3)) {
+  if (!plane3_fits(g, g.cb3)) {
     g.cb3 = 4;
     g.ncb3 = (g.nkx + g.cb3 - 1) / g.cb3;
   }

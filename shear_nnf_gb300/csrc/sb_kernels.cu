@@ -1093,7 +1093,8 @@ static cudaError_t launch_p13(const Grid &g, const Bufs &bf, int rk, cudaStream_
   if (prep) {
     cudaFuncSetAttribute(k_p1<R, NZ, CB, T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
     cudaFuncSetAttribute(k_p1<R, NZ, CB, T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
-    cudaFuncSetAttribute(k_p3<R, NZ, CB, T3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+    if (sm3 <= kMaxSmem)  // plane3_fits keeps the step off the blocks that do not fit
+      cudaFuncSetAttribute(k_p3<R, NZ, CB, T3, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
     if (sm3t <= kMaxSmem)
       cudaFuncSetAttribute(k_p3<R, NZ, CB, T3, 6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3t);
     return cudaGetLastError();
@@ -1183,6 +1184,7 @@ static cudaError_t launch_plane_t(const Grid &g, const Bufs &bf, int stage, int 
     case 160: return launch_p13_cb<R, 160>(g, bf, rk, st, stage, prep);
     case 192: return launch_p13_cb<R, 192>(g, bf, rk, st, stage, prep);
     case 256: return launch_p13_cb<R, 256>(g, bf, rk, st, stage, prep);
+    case 384: return launch_p13_cb<R, 384>(g, bf, rk, st, stage, prep);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -1255,6 +1257,7 @@ static cudaError_t launch_les_t(const Grid &g, const Bufs &bf, int stage, int rk
     case 160: return launch_les_z<R, 160, 4>(g, bf, stage, st, prep);
     case 192: return launch_les_z<R, 192, 2>(g, bf, stage, st, prep);
     case 256: return launch_les_z<R, 256, 2>(g, bf, stage, st, prep);
+    case 384: return launch_les_z<R, 384, 2>(g, bf, stage, st, prep);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -1371,7 +1374,7 @@ cudaError_t fp64_peak(double *tflops, cudaStream_t st) {
 
 bool supported_grid(int mgalx, int mgalz) {
   const int xs[] = {32, 48, 64, 80, 96, 128, 160, 192, 256, 320, 384};
-  const int zs[] = {32, 48, 64, 80, 96, 128, 160, 192, 256};
+  const int zs[] = {32, 48, 64, 80, 96, 128, 160, 192, 256, 384};
   bool okx = false, okz = false;
   for (int v : xs) okx |= (v == mgalx);
   for (int v : zs) okz |= (v == mgalz);

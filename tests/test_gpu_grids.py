@@ -1,5 +1,6 @@
 """Transform lengths beyond the benchmark configurations: powers of two (128,
-256) and 5 x 2^k (80, 160, 320, with a radix-5 first stage), in x and z, against
+256), 5 x 2^k (80, 160, 320, with a radix-5 first stage) and mgalz = 384 (plane
+stage 3 with 4 columns per block), in x and z, against
 the oracle (whose mixed-radix FFT covers them): the step (FP64 one step and ten
 steps, the FP32-mixed form), the LES stages (their x and z transforms) and the
 physical fields (the x transform of convh5's fields)."""
@@ -12,7 +13,7 @@ from test_gpu_step import ONE_STEP, TRACE_TOL, _field_errors, _run_both, _trace_
 pytestmark = pytest.mark.gpu
 
 GRIDS = [(80, 32, 80), (128, 64, 128), (160, 48, 160), (256, 32, 256), (320, 32, 160),
-         (128, 48, 80)]
+         (128, 48, 80), (192, 32, 384)]
 
 
 @pytest.mark.parametrize("grid", GRIDS)
@@ -45,7 +46,7 @@ def test_mixed_close_to_fp64(grid):
         assert rel_l2(b[k], a[k]) < 1e-5, k
 
 
-@pytest.mark.parametrize("grid", [(128, 48, 128), (160, 48, 80)])
+@pytest.mark.parametrize("grid", [(128, 48, 128), (160, 48, 80), (96, 32, 384)])
 def test_les_one_step(grid):
     pp = box_params(*grid, rez=4000.0, les=1, les_visc=1, cs=0.1)
     st_o, tr_o, st_g, tr_g, status = _run_both(pp, 1)
@@ -67,3 +68,10 @@ def test_physical_fields():
     for k in names:
         err = np.linalg.norm(got[k] - ref[k]) / max(np.linalg.norm(ref[k]), 1e-300)
         assert err < 1e-12, (k, err)
+
+
+def test_temperature_refused_beyond_256_in_z():
+    import shear_nnf_gb300 as sb
+    p = sb.make_params(**box_params(96, 32, 384, rez=2000.0, temperature=1, fkappa=0.01))
+    with pytest.raises(sb.ShearBoxError):
+        sb.ShearBox(p)
