@@ -194,3 +194,48 @@ def test_crosst_mixed_close_to_fp64():
         out.append(s)
     err = {k: rel_l2(out[1][k], out[0][k]) for k in KEYS}
     assert max(err.values()) < 1e-4, err
+
+
+def test_crosst_batch_members_match_single_runs():
+    """Three crosst boxes with their own Reynolds numbers on the
+    three-pipeline line kernel equal the single-box runs."""
+    import shear_nnf_gb300 as sb
+    from test_gpu_temperature import KEYS, _temp
+    pp = _temp((64, 32, 32), 4000.0)
+    p = sb.make_params(**pp, implicit_visc=1)
+    lz = 2 * np.pi
+    res = [2000.0, 4000.0, 8000.0]
+    sts = [sb.seed_state(p, 30 + m) for m in range(3)]
+    box = sb.ShearBox(p, batch=3)
+    for m in range(3):
+        box.set_state(sts[m], m)
+        box.set_re(m, res[m] / lz ** 2)
+    box.step(8)
+    for m in range(3):
+        single = sb.ShearBox(sb.make_params(**dict(pp, Re=res[m] / lz ** 2), implicit_visc=1))
+        single.set_state(sts[m])
+        single.step(8)
+        a, b = box.get_state(m), single.get_state(0)
+        for k in KEYS:
+            assert rel_l2(a[k], b[k]) < 1e-13, (m, k)
+
+
+@pytest.mark.parametrize("temperature", [0, 1])
+def test_autotune_keeps_the_implicit_step(temperature):
+    import shear_nnf_gb300 as sb
+    from test_gpu_temperature import _temp
+    pp = _temp((64, 32, 32), 4000.0) if temperature else box_params(64, 32, 32, rez=4000.0)
+    p = sb.make_params(**pp, implicit_visc=1)
+    st0 = sb.seed_state(p, 12)
+    ref = sb.ShearBox(p)
+    a = copy_state(st0)
+    ref.cross(a, 5)
+    box = sb.ShearBox(p)
+    box.set_state(st0)
+    choice = box.autotune()
+    assert choice["line_form"] == "implicit"
+    b = copy_state(st0)
+    box.cross(b, 5)
+    tol = 1e-13 if choice["line_segments"] == ref.tuning()["line_segments"] else 1e-11
+    for k in ("vor", "phi", "u00", "w00"):
+        assert rel_l2(b[k], a[k]) < tol, k
