@@ -1,14 +1,16 @@
 // sb_implicit.cu -- factor tables of the semi-implicit viscous branch of cross
-// (explicit = 0, cross.f90:797-989).
+// and crosst (explicit = 0, cross.f90:797-989, crosst.f90:916-1195).
 //
 // That branch solves, per substep k and (kx, kz) line,
 //   (d2/dy2 - k^2 - dtr1) f_new = rhs,   dtr1 = Re ibeta_k / Delta t,
 // and for the mean profiles (d2/dy2 - dtr1) u00 = rhs (lapcdy(., rk2, .),
-// cross.f90:898-925,965-967).  Delta t follows the CFL rule per step and per
-// box, so the Helmholtz factorisations are rebuilt on the device every
-// substep, after k_tables, for the lines (kx, kz >= 0) of every box (a line
-// (kx, -kz) has the same k^2) and the mean line.  The tables have the layout of the per-line Helmholtz tables of
-// the explicit step (Fac with stride = boxes x (lines + 1)): the LDL^H base
+// cross.f90:898-925,965-967); crosst's scalar the same with dtr1k = ibeta_k /
+// (fkappa Delta t).  Delta t follows the CFL rule per step and per box, so the
+// Helmholtz factorisations are rebuilt on the device every substep, after
+// k_tables, for the lines (kx, kz >= 0) of every box (a line (kx, -kz) has the
+// same k^2) and the mean line.  The tables have the layout of the per-line
+// Helmholtz tables of the explicit step (Fac with stride = boxes x (lines +
+// 1)): the LDL^H base
 // with the shear phase factored out of the border rows (the steps of
 // base_factor in sb_host.cpp, after modChol7cyclic_cmplx,
 // diffy_shear_hepta.f90:578-755), the homogeneous solutions and border sums
