@@ -75,3 +75,35 @@ def test_temperature_refused_beyond_256_in_z():
     p = sb.make_params(**box_params(96, 32, 384, rez=2000.0, temperature=1, fkappa=0.01))
     with pytest.raises(sb.ShearBoxError):
         sb.ShearBox(p)
+
+
+@pytest.mark.parametrize("implicit", [0, 1])
+def test_shortest_lines(implicit):
+    """my = 16, the shortest y line (two segments of six banded rows), in
+    both integrators, ten steps against the oracle."""
+    import oracle
+    import shear_nnf_gb300 as sb
+    pp = box_params(32, 16, 32, rez=1000.0, fixed_dt=0.005)
+    p = sb.make_params(**pp, implicit_visc=implicit)
+    st0 = sb.seed_state(p, 8)
+    a, b = copy_state(st0), copy_state(st0)
+    oracle.Oracle(**pp, implicit_visc=implicit).cross(a, 10)
+    box = sb.ShearBox(p)
+    box.set_line_segments(2)
+    box.cross(b, 10)
+    for k in ("vor", "phi", "u00", "w00"):
+        assert rel_l2(b[k], a[k]) < 1e-11, k
+
+
+def test_longest_lines():
+    """my = 448, the longest y line: the fused block does not fit in shared
+    memory, so the split y-line kernels run (and the semi-implicit branch,
+    which needs the fused block, is refused)."""
+    import shear_nnf_gb300 as sb
+    pp = box_params(32, 448, 32, rez=1000.0, fixed_dt=0.002)
+    st_o, tr_o, st_g, tr_g, status = _run_both(pp, 1)
+    err = _field_errors(st_o, st_g)
+    assert max(err.values()) < ONE_STEP, err
+    assert sb.ShearBox(sb.make_params(**pp)).tuning()["line_form"] == "split"
+    with pytest.raises(sb.ShearBoxError):
+        sb.ShearBox(sb.make_params(**pp, implicit_visc=1))
