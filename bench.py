@@ -596,7 +596,11 @@ def run_ours(args):
             print(json.dumps({"metric": METRIC, "value": steps_per_s, "unit": "steps/s",
                               "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
                               "ms_per_step": ms_max / args.steps, "lite": True,
-                              "config": config({"grid": list(GRID), "tuning": tuning,
+                              "config": config({"workload": (
+                                  f"shearing box {GRID[0]}x{GRID[1]}x{GRID[2]}, {nbox} box(es), "
+                                  f"{'FP32-mixed' if args.mixed else 'FP64'} RK3 step, "
+                                  f"variant {args.variant} (profiling run)"),
+                                                "grid": list(GRID), "tuning": tuning,
                                                 "variant": args.variant, "boxes": nbox,
                                                 "precision": "mixed" if args.mixed else "fp64"}),
                               "gpu_launches": launches}))

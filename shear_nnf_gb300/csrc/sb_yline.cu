@@ -528,8 +528,18 @@ __device__ __forceinline__ bool line_thread_f(const Grid &g, LineThread *L, int 
   solve_seg<kSeg>(U, PS, ys, ystr, N, VIEW, SVIEW, TAIL, SHP, SHM, L.c, L.s, L.l, g.slo, g.shi, \
                   R0, R1, R2, R3, ANTI, &xch[pipe][0][0][0][0])
 
+// k_lineF: resident warps per SM the kernel is register-budgeted for (a
+// build-time knob; 0 leaves the registers to the compiler).  12 warps cap it
+// at 168 registers without spills (from 202-214): the 64-box 64x32x32 mixed
+// ensemble steps 2.3% faster (more lines in flight per SM), the one-box
+// 192x96x96 step is unchanged (its 253 blocks fit one wave either way), and
+// 16 warps (128 registers) spill and lose 4%.
+#ifndef SB_LINEF_WARPS
+#define SB_LINEF_WARPS 12
+#endif
 template <typename R>
-__global__ void __launch_bounds__(64 * kSeg, 1) k_lineF(Grid g, Bufs bf, int rk1) {
+__global__ void __launch_bounds__(64 * kSeg, SB_LINEF_WARPS / (2 * kSeg) > 0 ? SB_LINEF_WARPS / (2 * kSeg) : 1)
+    k_lineF(Grid g, Bufs bf, int rk1) {
   __shared__ double xch[2][kSeg][16][2][SB_XS];
   LineThread L;
   int pipe = 0;
