@@ -296,12 +296,21 @@ int sb_physical_fields(sb_handle *h, int member, unsigned mask, double *out);
  * filter/dealiasing (otherwise error 1, and such handles always run form 0).
  * sb_get_line_form gives the form the step graph uses (2 for a handle with
  * implicit_visc, whose substeps run the semi-implicit y-line kernel).  Both
- * forms compute the same step (to the last bits in FP64). */
+ * forms compute the same step (to the last bits in FP64).
+ * sb_set_side_branch chooses which side work of a substep the step graph runs
+ * as a branch concurrent with the plane stages: bit 0 the spectra of a
+ * statistics step (beside plane stages 1-2), bit 1 the per-box scalars and
+ * phase tables (beside plane stage 3; handles with LES always run these in
+ * order); a cleared bit runs that work on the main stream in order.  The
+ * default is 3 and sb_autotune picks the fastest mask; every mask computes the
+ * same step bit for bit.  sb_get_side_branch gives the mask in use. */
 int sb_autotune(sb_handle *h, int *choice);
 int sb_get_tuning(sb_handle *h, int *out);
 int sb_set_line_segments(sb_handle *h, int nseg);
 int sb_set_line_form(sb_handle *h, int form);
 int sb_get_line_form(sb_handle *h, int *form);
+int sb_set_side_branch(sb_handle *h, int mask);
+int sb_get_side_branch(sb_handle *h, int *mask);
 int sb_fp64_peak(sb_handle *h, double *tflops);
 
 /* Standalone y-line operators on device-resident complex lines.  Line data is

@@ -345,6 +345,19 @@ module shearbox_c
        integer(c_int), intent(out) :: form
      end function sb_get_line_form
 
+     ! side work run as concurrent graph branches: bit 0 spectra, bit 1 scalars
+     integer(c_int) function sb_set_side_branch(h, mask) bind(C, name="sb_set_side_branch")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int), value :: mask
+     end function sb_set_side_branch
+
+     integer(c_int) function sb_get_side_branch(h, mask) bind(C, name="sb_get_side_branch")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h
+       integer(c_int), intent(out) :: mask
+     end function sb_get_side_branch
+
      ! getfil on the run's grid; info: pass a buffer of at least 584 bytes
      ! (sb_restart_info), flags = 1 keeps the vorticity of a changed Re
      integer(c_int) function sb_read_restart_ex(path, p, flags, vor, phi, u00, w00, info) &

@@ -96,7 +96,7 @@ ABI_FUNCTIONS = [
     "sb_kspace_sync", "sb_kspace_gram", "sb_kspace_update", "sb_kspace_transform",
     "sb_kspace_combine", "sb_kspace_perturb", "sb_kspace_fd", "sb_kspace_set", "sb_kspace_get",
     "sb_read_restart_ex", "sb_get_tuning", "sb_set_line_segments", "sb_set_line_form",
-    "sb_get_line_form",
+    "sb_get_line_form", "sb_set_side_branch", "sb_get_side_branch",
 ]
 
 _lib = None
@@ -152,6 +152,8 @@ def lib(auto_build: bool = False):
     L.sb_set_line_segments.argtypes = [vp, ctypes.c_int]
     L.sb_set_line_form.argtypes = [vp, ctypes.c_int]
     L.sb_get_line_form.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+    L.sb_set_side_branch.argtypes = [vp, ctypes.c_int]
+    L.sb_get_side_branch.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     L.sb_physical_fields.argtypes = [vp, ctypes.c_int, ctypes.c_uint, dp]
     L.sb_op_derivyc.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int, vp,
                                 ctypes.c_long, vp, ctypes.c_long, dp, dp, vp]
@@ -369,8 +371,10 @@ class ShearBox:
         _check(lib().sb_get_tuning(self.h, c))
         f = ctypes.c_int(0)
         _check(lib().sb_get_line_form(self.h, ctypes.byref(f)))
+        m = ctypes.c_int(0)
+        _check(lib().sb_get_side_branch(self.h, ctypes.byref(m)))
         return {"p1_cols": c[0], "p3_cols": c[1], "p2_threads": c[2], "line_segments": c[3],
-                "line_form": ("split", "fused", "implicit")[f.value]}
+                "line_form": ("split", "fused", "implicit")[f.value], "side_branch": m.value}
 
     def set_line_segments(self, nseg: int):
         """Warps per y-line solve, 1..3 (sb_set_line_segments)."""
@@ -383,6 +387,12 @@ class ShearBox:
         if form not in ("fused", "split"):
             raise ValueError(f"line form {form!r}: 'fused' or 'split'")
         _check(lib().sb_set_line_form(self.h, 1 if form == "fused" else 0))
+
+    def set_side_branch(self, mask: int):
+        """Side work run as concurrent branches of the step graph: bit 0 the
+        spectra, bit 1 the scalars and tables; 0 runs all of it in order
+        (sb_set_side_branch)."""
+        _check(lib().sb_set_side_branch(self.h, int(mask)))
 
     def statistics(self, member: int = 0) -> dict:
         """The hist accumulators of the last step call (sb_get_statistics):

@@ -58,6 +58,10 @@ struct sb_handle {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // the spectra of a statistics step run beside plane stages 1-2
   cudaEvent_t ev_s0 = nullptr, ev_s1 = nullptr;
+  // which side work the step graph runs as a concurrent branch: bit 0 the
+  // spectra, bit 1 the scalars and tables (a cleared bit puts that work on
+  // the main stream in order)
+  int branch = 3;
   // the host copies of phi run on the side stream beside those of omega_y
   cudaEvent_t ev_c0 = nullptr, ev_c1 = nullptr;
   cudaGraphExec_t step_exec = nullptr;
@@ -370,7 +374,9 @@ static int capture_step(sb_handle *h) {
         ((e = launch_ydeal(h->g, h->bf, rk, h->st)) != cudaSuccess ||
          (e = launch_meand1(h->g, h->bf, h->st)) != cudaSuccess))
       break;
-    if (rk == 1 &&
+    const bool br_spec = (h->branch & 1) != 0, br_scal = (h->branch & 2) && !h->g.les;
+    if (rk == 1 && !br_spec && (e = launch_spectra(h->g, h->bf, h->st)) != cudaSuccess) break;
+    if (rk == 1 && br_spec &&
         ((e = cudaEventRecord(h->ev_s0, h->st)) != cudaSuccess ||
          (e = cudaStreamWaitEvent(h->side, h->ev_s0, 0)) != cudaSuccess ||
          (e = launch_spectra(h->g, h->bf, h->side)) != cudaSuccess ||
@@ -379,11 +385,12 @@ static int capture_step(sb_handle *h) {
     if ((e = launch_plane(h->g, h->bf, 1, rk, h->st)) != cudaSuccess) break;
     if ((e = launch_plane(h->g, h->bf, 2, rk, h->st)) != cudaSuccess) break;
     // plane stage 3 overwrites inputs of the spectra
-    if (rk == 1 && (e = cudaStreamWaitEvent(h->st, h->ev_s1, 0)) != cudaSuccess) break;
+    if (rk == 1 && br_spec && (e = cudaStreamWaitEvent(h->st, h->ev_s1, 0)) != cudaSuccess)
+      break;
     if (h->g.les)
       for (int q = 2; q <= 4 && e == cudaSuccess; q++) e = launch_les(h->g, h->bf, q, rk, h->st);
     if (e != cudaSuccess) break;
-    if (!h->g.les) {
+    if (br_scal) {
       // k_scalar needs stages 1-2 (statistics, |u| maxima) and k_tables needs
       // k_scalar: both run on a branch beside plane stage 3
       if ((e = cudaEventRecord(h->ev_fork, h->st)) != cudaSuccess ||
@@ -396,11 +403,13 @@ static int capture_step(sb_handle *h) {
           (e = cudaStreamWaitEvent(h->st, h->ev_join, 0)) != cudaSuccess)
         break;
     } else {
-      // with LES, k_scalar also takes the statistics of the LES stages
+      // in order on the main stream; with LES, k_scalar also takes the
+      // statistics of the LES stages
       if ((e = launch_plane(h->g, h->bf, 3, rk, h->st)) != cudaSuccess) break;
-      if ((e = launch_les(h->g, h->bf, 5, rk, h->st)) != cudaSuccess) break;
+      if (h->g.les && (e = launch_les(h->g, h->bf, 5, rk, h->st)) != cudaSuccess) break;
       if ((e = launch_scalar(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
       if ((e = launch_tables(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
+      if (h->g.impl && (e = launch_hfac(h->g, h->bf, rk, h->st)) != cudaSuccess) break;
     }
     if (h->g.les && (e = launch_lineL(h->g, h->bf, h->st)) != cudaSuccess) break;
     if (h->g.impl) {
@@ -1269,14 +1278,38 @@ int sb_autotune(sb_handle *h, int *choice) {
       if (!rc && e == cudaSuccess && t < best) best = t, nseg = c, lform = f;
     }
   }
+  // which side work runs as a concurrent graph branch, on the chosen tile:
+  // a branch that shares the SMs with short plane stages can cost more than
+  // it hides (measured: the FP32-mixed 192x96x96 step is 7% faster with the
+  // spectra in order, the FP64 step 1% slower)
+  g.lform = lform;
+  if (!rc && e == cudaSuccess && g.nseg != nseg) rc = build_line_tables(h, nseg);
+  int branch = h->branch;
+  best = 1e30f;
+  for (int m : {3, 2, 1, 0}) {
+    if (rc || e != cudaSuccess) break;
+    h->branch = m;
+    if ((rc = capture_step(h))) break;
+    for (int q = 0; q < 3 && e == cudaSuccess; q++) {
+      if ((rc = snap.restore(h))) break;
+      cudaEventRecord(e0, st);
+      e = launch_step_call(h, 4);
+      cudaEventRecord(e1, st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float tq = 0.0f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&tq, e0, e1);
+      if (q == 1) t = tq;
+      if (q == 2) t = t < tq ? t : tq;
+    }
+    if (!rc && e == cudaSuccess && t < best) best = t, branch = m;
+  }
+  h->branch = branch;
   if (!rc) rc = snap.restore(h);
   snap.release();
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  g.lform = lform;
   if (rc) return rc;
   if (e != cudaSuccess) return fail(3, "autotune: %s", cudaGetErrorString(e));
-  if (g.nseg != nseg && (rc = build_line_tables(h, nseg))) return rc;
   if (choice) {
     choice[0] = g.cb1;
     choice[1] = g.cb3;
@@ -1299,6 +1332,19 @@ int sb_set_line_form(sb_handle *h, int form) {
     return fail(1, "fused y-line kernel not available for this handle");
   h->g.lform = form;
   return capture_step(h);
+}
+
+int sb_set_side_branch(sb_handle *h, int mask) {
+  if (!h) return fail(1, "null handle");
+  if (mask < 0 || mask > 3) return fail(1, "side-branch mask %d (0..3)", mask);
+  h->branch = mask;
+  return capture_step(h);
+}
+
+int sb_get_side_branch(sb_handle *h, int *mask) {
+  if (!h || !mask) return fail(1, "null argument");
+  *mask = h->branch;
+  return 0;
 }
 
 int sb_get_line_form(sb_handle *h, int *form) {

@@ -218,8 +218,8 @@ __global__ void __launch_bounds__(T) k_p1(Grid g, Bufs bf, int rk) {
 // block's modes of the 11 hist quantities (up vp wp uvr uwr vwr o1p o2p o3p
 // o12p eps) and of tbp utbp vtbp wtbp, reduced per plane by k_hsum.  A block
 // takes 16 modes of a box; its 8 thread slices take every 8th plane; the
-// per-mode slices are added in a fixed order, the per-plane modes by a fixed
-// half-warp tree.  FP64 arithmetic whatever the storage precision.  Runs
+// per-mode slices are added in a fixed order, the per-plane modes in mode
+// order through shared memory.  FP64 arithmetic whatever the storage precision.  Runs
 // before the per-box scalars update Delta t: spl2 and splt carry the Delta t
 // of the previous step, as in hist 'f'.
 // ---------------------------------------------------------------------------
@@ -248,8 +248,11 @@ __global__ void __launch_bounds__(kSpecModes * kSpecSlices) k_spectra(Grid g, Bu
   const double cs = (i == 0 && k > nz) ? -1.0 : 1.0;
   const int nblk = gridDim.x;
   double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, tacc[4] = {0, 0, 0, 0};
-  // the same number of iterations on every slice (the half-warp shuffles
-  // below need every lane of the warp): planes past the last carry weight 0
+  // per-plane products of the 16 modes, double-buffered across iterations
+  constexpr int NQ = TEMP ? SB_NHIST_Q : 11;
+  __shared__ double tpart[2][kSpecSlices][NQ][kSpecModes + 1];
+  // the same number of iterations on every slice (the block barrier in the
+  // loop needs every thread): planes past the last carry weight 0
   const int niter = (g.my + kSpecSlices - 1) / kSpecSlices;
   for (int it = 0; it < niter; it++) {
     const int jr = sl + kSpecSlices * it;
@@ -331,22 +334,30 @@ __global__ void __launch_bounds__(kSpecModes * kSpecSlices) k_spectra(Grid g, Bu
       pq[14] = w * (u3x * tx + u3y * ty);
 #pragma unroll
       for (int f = 0; f < 4; f++) tacc[f] += pq[11 + f];
-    } else {
-#pragma unroll
-      for (int f = 11; f < SB_NHIST_Q; f++) pq[f] = 0.0;
     }
-    // the plane's partial over the block's 16 modes (the lanes of one half warp)
+    // the plane's partial over the block's 16 modes: the products go through
+    // shared memory and one thread per (slice, quantity) adds its 16 modes in
+    // order (15 FP64 adds per quantity, where a shuffle tree spends 4 adds on
+    // every lane)
+    double(*tp)[NQ][kSpecModes + 1] = tpart[it & 1];
 #pragma unroll
-    for (int f = 0; f < SB_NHIST_Q; f++) {
-      double x = pq[f];
-      for (int o = kSpecModes / 2; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-      pq[f] = x;
-    }
-    if (mi == 0 && jok) {
-      double *hp = bf.hpart + (((long)b * g.my + j) * nblk + blockIdx.x) * SB_NHIST_Q;
+    for (int f = 0; f < NQ; f++) tp[sl][f][mi] = pq[f];
+    __syncthreads();
+    if (threadIdx.x < kSpecSlices * NQ) {
+      const int s2 = threadIdx.x / NQ, f = threadIdx.x - s2 * NQ;
+      const int j2 = s2 + kSpecSlices * it;
+      if (j2 < g.my) {
+        double x = tp[s2][f][0];
 #pragma unroll
-      for (int f = 0; f < SB_NHIST_Q; f++) hp[f] = pq[f];
+        for (int m = 1; m < kSpecModes; m++) x += tp[s2][f][m];
+        double *hp = bf.hpart + (((long)b * g.my + j2) * nblk + blockIdx.x) * SB_NHIST_Q;
+        hp[f] = x;
+        if (!TEMP && f == 0)
+          for (int f2 = NQ; f2 < SB_NHIST_Q; f2++) hp[f2] = 0.0;
+      }
     }
+    // the next iteration writes the other buffer; the one after waits for this
+    // iteration's readers at the next barrier
   }
   __shared__ double red[kSpecSlices][12][kSpecModes];
 #pragma unroll

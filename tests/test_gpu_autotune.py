@@ -97,3 +97,36 @@ def test_fused_form_refused_where_unavailable():
         with pytest.raises(sb.ShearBoxError):
             box.set_line_form("fused")
         box.set_line_form("split")
+
+
+@pytest.mark.parametrize("prec,extra", [(0, {}), (1, {}), (0, {"implicit_visc": 1}),
+                                        (0, {"les": 1, "les_visc": 1, "cs": 0.1})])
+def test_side_branch_masks_compute_the_same_step(prec, extra):
+    """The spectra and the per-box scalars run as concurrent graph branches or
+    in order on the main stream (sb_set_side_branch): the same kernels on the
+    same inputs, so the state, the trace and the statistics agree bit for
+    bit; the autotuner's mask is one of the four."""
+    import shear_nnf_gb300 as sb
+    p = sb.make_params(**box_params(64, 32, 32, rez=1000.0, **extra))
+    st0 = sb.seed_state(p, 5)
+    out = {}
+    for mask in (3, 2, 1, 0):
+        box = sb.ShearBox(p, precision=prec)
+        box.set_side_branch(mask)
+        assert box.tuning()["side_branch"] == mask
+        s = copy_state(st0)
+        tr, _ = box.cross(s, 4)
+        out[mask] = (s, tr, box.statistics())
+    s3, tr3, st3 = out[3]
+    for mask in (2, 1, 0):
+        s, tr, stt = out[mask]
+        for k in ("vor", "phi", "u00", "w00"):
+            assert np.array_equal(s[k], s3[k]), (mask, k)
+        assert np.array_equal(tr, tr3), mask
+        for k, v in st3.items():
+            assert np.array_equal(np.asarray(stt[k]), np.asarray(v)), (mask, k)
+    box = sb.ShearBox(p, precision=prec)
+    with pytest.raises(sb.ShearBoxError):
+        box.set_side_branch(4)
+    box.set_state(st0)
+    assert box.autotune()["side_branch"] in (0, 1, 2, 3)
