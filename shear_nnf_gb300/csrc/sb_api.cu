@@ -100,7 +100,7 @@ static int dalloc(sb_handle *h, double **p, size_t n) {
   return 0;
 }
 static int upload(sb_handle *h, const double **dst, const std::vector<double> &v) {
-  double *p;
+  double *p = nullptr;
   int rc = dalloc(h, &p, v.size());
   if (rc) return rc;
   CK(cudaMemcpy(p, v.data(), sizeof(double) * v.size(), cudaMemcpyHostToDevice));
@@ -228,7 +228,6 @@ static int build_line_tables(sb_handle *h, int nseg) {
   double flhs[7], frhs[9];
   sbh::filter_coeffs(flhs, frhs);
   const double *rh2 = g.rh2;
-  const int nl = g.nkx * g.mz;
   int rc;
   if ((rc = upload_uniform(h, &bf.d1, co.pr1, g.my)) ||
       (rc = upload_uniform(h, &bf.d2, co.pr2, g.my)) ||
