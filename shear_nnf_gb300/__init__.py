@@ -145,6 +145,8 @@ def lib(auto_build: bool = False):
                                 dp, dp]
     L.sb_compact_coeffs.argtypes = [dp, dp, dp, dp]
     L.sb_last_error.restype = ctypes.c_char_p
+    L.sb_last_error.argtypes = []
+    L.sb_version.argtypes = []
     L.sb_launch_stage.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.sb_fp64_peak.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.sb_autotune.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]

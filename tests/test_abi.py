@@ -35,6 +35,33 @@ def test_python_wrapper_lists_the_header():
     assert sorted(sb.ABI_FUNCTIONS) == _declared()
 
 
+def _prototypes():
+    txt = open(os.path.join(ROOT, "include", "shearbox.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(sb_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", txt, flags=re.S):
+        args = " ".join(m.group(2).split())
+        out[m.group(1)] = [] if args in ("", "void") else [a.strip() for a in args.split(",")]
+    return out
+
+
+def test_python_argtypes_match_the_header():
+    """Every entry point the Python host binds has one ctypes argument type per
+    parameter of its prototype, pointers where the header has pointers."""
+    import shear_nnf_gb300 as sb
+    L = sb.lib()
+    protos = _prototypes()
+    assert sorted(protos) == sorted(sb.ABI_FUNCTIONS)
+    for name, params in protos.items():
+        at = getattr(L, name).argtypes
+        assert at is not None and len(at) == len(params), (name, params, at)
+        for decl, t in zip(params, at):
+            is_ptr = "*" in decl or "[" in decl  # array parameters are pointers
+            is_ctype_ptr = t in (ctypes.c_void_p, ctypes.c_char_p) or hasattr(t, "_type_") and \
+                isinstance(getattr(t, "_type_"), type) and issubclass(t, ctypes._Pointer)
+            assert is_ptr == bool(is_ctype_ptr), (name, decl, t)
+
+
 def test_sizes_follow_initcr():
     import shear_nnf_gb300 as sb
     for (gx, gy, gz), (mx, mz) in {(192, 96, 96): (128, 63), (64, 32, 32): (42, 19),
