@@ -268,6 +268,27 @@ module shearbox_c
        real(c_double), value :: alpha
      end function sb_kspace_update
 
+     ! cols b0..b0+p-1 <- (cols b0..) M in place, p <= 64, M p x p row-major
+     integer(c_int) function sb_kspace_transform(ks, r0, r1, b0, p, M) &
+          bind(C, name="sb_kspace_transform")
+       import :: c_int, c_long, c_ptr, c_double
+       type(c_ptr), value :: ks
+       integer(c_long), value :: r0, r1
+       integer(c_int), value :: b0, p
+       real(c_double), intent(in) :: M(*)
+     end function sb_kspace_transform
+
+     ! the space's CUDA stream and a blocking wait on it
+     type(c_ptr) function sb_kspace_stream(ks) bind(C, name="sb_kspace_stream")
+       import :: c_ptr
+       type(c_ptr), value :: ks
+     end function sb_kspace_stream
+
+     integer(c_int) function sb_kspace_sync(ks) bind(C, name="sb_kspace_sync")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: ks
+     end function sb_kspace_sync
+
      integer(c_int) function sb_kspace_combine(ks, r0, r1, dst, nsrc, src, coef) &
           bind(C, name="sb_kspace_combine")
        import :: c_int, c_long, c_ptr, c_double
@@ -369,6 +390,94 @@ module shearbox_c
        real(c_double), intent(out) :: vor(*), phi(*), u00(*), w00(*)
        type(c_ptr), value :: info
      end function sb_read_restart_ex
+
+     ! getfil of a file on the run's grid only (sb_read_restart_ex with flags 0)
+     integer(c_int) function sb_read_restart(path, p, vor, phi, u00, w00, info) &
+          bind(C, name="sb_read_restart")
+       import :: c_int, c_char, c_double, c_ptr, sb_params
+       character(kind=c_char), intent(in) :: path(*)   ! NUL-terminated
+       type(sb_params), intent(in) :: p
+       real(c_double), intent(out) :: vor(*), phi(*), u00(*), w00(*)
+       type(c_ptr), value :: info
+     end function sb_read_restart
+
+     ! the handle's CUDA stream (cudaStream_t) and a blocking wait on it
+     type(c_ptr) function sb_get_stream(h) bind(C, name="sb_get_stream")
+       import :: c_ptr
+       type(c_ptr), value :: h
+     end function sb_get_stream
+
+     integer(c_int) function sb_sync(h) bind(C, name="sb_sync")
+       import :: c_int, c_ptr
+       type(c_ptr), value :: h
+     end function sb_sync
+
+     ! y-line operators on DEVICE lines u, out (c_ptr of device memory, e.g.
+     ! from CUDA Fortran or an OpenACC host_data region), element (line, j) at
+     ! the complex u(line + j*ldu); shp, shm, k2 are host arrays of nlines
+     ! entries; stream is a cudaStream_t (c_null_ptr: the legacy stream)
+     ! derivyc (diffy_shear_hepta.f90:333-450), iord 1 or 2
+     integer(c_int) function sb_op_derivyc(my, Ly, iord, nlines, u, ldu, out, ldo, shp, shm, &
+          stream) bind(C, name="sb_op_derivyc")
+       import :: c_int, c_long, c_double, c_double_complex, c_ptr
+       integer(c_int), value :: my, iord, nlines
+       real(c_double), value :: Ly
+       type(c_ptr), value :: u, out, stream
+       integer(c_long), value :: ldu, ldo
+       complex(c_double_complex), intent(in) :: shp(*), shm(*)
+     end function sb_op_derivyc
+
+     ! the same without device allocation (fixed library scratch, error 6 when
+     ! the request does not fit)
+     integer(c_int) function sb_op_derivyc_noalloc(my, Ly, iord, nlines, u, ldu, out, ldo, &
+          shp, shm, stream) bind(C, name="sb_op_derivyc_noalloc")
+       import :: c_int, c_long, c_double, c_double_complex, c_ptr
+       integer(c_int), value :: my, iord, nlines
+       real(c_double), value :: Ly
+       type(c_ptr), value :: u, out, stream
+       integer(c_long), value :: ldu, ldo
+       complex(c_double_complex), intent(in) :: shp(*), shm(*)
+     end function sb_op_derivyc_noalloc
+
+     ! lapcdy (diffy_shear_hepta.f90:466-525): (d2/dy2 - k2) out = u
+     integer(c_int) function sb_op_lapcdy(my, Ly, nlines, u, ldu, out, ldo, k2, shp, shm, &
+          stream) bind(C, name="sb_op_lapcdy")
+       import :: c_int, c_long, c_double, c_double_complex, c_ptr
+       integer(c_int), value :: my, nlines
+       real(c_double), value :: Ly
+       type(c_ptr), value :: u, out, stream
+       integer(c_long), value :: ldu, ldo
+       real(c_double), intent(in) :: k2(*)
+       complex(c_double_complex), intent(in) :: shp(*), shm(*)
+     end function sb_op_lapcdy
+
+     ! filterc (filter_shear_hepta.f90:104-148)
+     integer(c_int) function sb_op_filterc(my, nlines, u, ldu, out, ldo, shp, stream) &
+          bind(C, name="sb_op_filterc")
+       import :: c_int, c_long, c_double_complex, c_ptr
+       integer(c_int), value :: my, nlines
+       type(c_ptr), value :: u, out, stream
+       integer(c_long), value :: ldu, ldo
+       complex(c_double_complex), intent(in) :: shp(*)
+     end function sb_op_filterc
+
+     ! cfty / rfty (cftdoublew.F:151-201, rftdoublew.F:133-158) in place on
+     ! device lines c; iopt < 0 forward (scaled by 1/my), > 0 backward
+     integer(c_int) function sb_op_cfty(my, nlines, c, ldc, iopt, stream) &
+          bind(C, name="sb_op_cfty")
+       import :: c_int, c_long, c_ptr
+       integer(c_int), value :: my, nlines, iopt
+       type(c_ptr), value :: c, stream
+       integer(c_long), value :: ldc
+     end function sb_op_cfty
+
+     integer(c_int) function sb_op_rfty(my, nlines, c, ldc, iopt, stream) &
+          bind(C, name="sb_op_rfty")
+       import :: c_int, c_long, c_ptr
+       integer(c_int), value :: my, nlines, iopt
+       type(c_ptr), value :: c, stream
+       integer(c_long), value :: ldc
+     end function sb_op_rfty
 
      integer(c_int) function sb_sizes(p, out) bind(C, name="sb_sizes")
        import :: c_int, sb_params

@@ -184,6 +184,21 @@ def test_fortran_interface_binds_exported_symbols(lib):
         assert n in declared and hasattr(lib, n), n
 
 
+def test_fortran_interfaces_match_the_prototypes():
+    """Each bind(C) interface has the header prototype's parameter count, and
+    every entry point is bound except the test and benchmark helpers."""
+    txt = re.sub(r"&\s*\n\s*&?", " ", _f90())
+    funcs = re.findall(r'function\s+(sb_[a-z0-9_]+)\s*\(([^)]*)\)\s*bind\(C,\s*'
+                       r'name="(sb_[a-z0-9_]+)"\)', txt, flags=re.I)
+    protos = _prototypes()
+    for fname, args, cname in funcs:
+        assert fname == cname and cname in protos, cname
+        assert len([a for a in args.split(",") if a.strip()]) == len(protos[cname]), cname
+    helpers = {"sb_compact_coeffs", "sb_fft_twiddles", "sb_fp64_peak", "sb_launch_stage",
+               "sb_seed_state"}
+    assert set(protos) - {c for _, _, c in funcs} == helpers
+
+
 def test_fortran_types_follow_the_c_structs():
     """The bind(C) derived types list the C struct members in order and type."""
     import shear_nnf_gb300 as sb
