@@ -10,7 +10,7 @@ import oracle
 from conftest import box_params, copy_state
 
 
-@pytest.mark.parametrize("n", [32, 48, 64, 96, 192, 384, 30])
+@pytest.mark.parametrize("n", [32, 48, 64, 80, 96, 128, 160, 192, 256, 320, 384, 30])
 def test_fft_matches_numpy(n):
     rng = np.random.default_rng(n)
     x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
@@ -26,7 +26,8 @@ def _full_spectrum(o, fou, mgalx, mgalz):
     return full
 
 
-@pytest.mark.parametrize("grid", [(64, 32), (96, 48), (192, 96)])
+@pytest.mark.parametrize("grid", [(64, 32), (96, 48), (192, 96), (80, 160), (320, 256),
+                                  (128, 384)])
 def test_fourxz_matches_numpy(grid):
     """fourxz with fill00/pack00 (fou3D_thread.f:22-161): unnormalised c2r, r2c
     scaled by 1/(mgalx*mgalz), 2/3-rule truncation."""
