@@ -172,22 +172,24 @@ def plane2_traffic():
     return None
 
 
-def cpu_baseline(nsteps_sample: int, threads: int):
-    """The C oracle on the host cores, a bounded sample of steps.  Loads only
-    the oracle: the seeded field comes from the oracle's own generator, which
-    the CPU tests hold bit-identical to the library's."""
+def cpu_baseline(nsteps_sample: int, threads: int, warmup: int = 1):
+    """The C oracle on the host cores, a bounded sample of steps after
+    `warmup` untimed ones.  Loads only the oracle: the seeded field comes from
+    the oracle's own generator, which the CPU tests hold bit-identical to the
+    library's."""
     import oracle
     oracle.set_threads(threads)
     pp = box_params()
     st = oracle.seed_state(seed=3, **pp)
     o = oracle.Oracle(**pp)
-    o.cross(st, 1)  # warm-up
+    o.cross(st, warmup)
     t0 = time.perf_counter()
     o.cross(st, nsteps_sample)
     dt = time.perf_counter() - t0
     return {"value": nsteps_sample / dt, "unit": "steps/s", "cores": threads, "kind": "port",
             "sample": f"{nsteps_sample} consecutive FP64 steps of the 192x96x96 box "
-                      f"(C oracle, OpenMP, {threads} threads), after 1 warm-up step",
+                      f"(C oracle, OpenMP, {threads} threads), after {warmup} warm-up "
+                      f"step{'s' if warmup != 1 else ''}",
             "seconds": dt}
 
 
@@ -197,7 +199,7 @@ def run_reference(args):
         return
     threads = os.cpu_count() or 1
     n = max(1, min(args.steps, 20))
-    res = cpu_baseline(n, threads)
+    res = cpu_baseline(n, threads, warmup=args.warmup)
     line = {"impl": "reference", "metric": METRIC, "value": res["value"], "unit": "steps/s",
             "n_gpus": args.gpus, "steps": n, "warmup": args.warmup,
             "ms_per_step": 1e3 / res["value"], "higher_is_better": True, "scaling": "weak",
