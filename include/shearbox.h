@@ -155,8 +155,9 @@ int sb_get_trace(sb_handle *h, int member, double *out, int max_records, int *nr
 int sb_cross(sb_handle *h, double *vor, double *phi, double *u00, double *w00, double *time,
              double *xoffb, double *xofft, int nstep, sb_status *st);
 
-/* Drop-in for crosst() (crosst.f90:3-5, explicit branch, iadd_mode 5): as
- * sb_cross with the scalar tb and its mean tb00; needs temperature = 1. */
+/* Drop-in for crosst() (crosst.f90:3-5, iadd_mode 5; the explicit branch, or
+ * the semi-implicit one with implicit_visc): as sb_cross with the scalar tb and
+ * its mean tb00; needs temperature = 1. */
 int sb_crosst(sb_handle *h, double *vor, double *phi, double *u00, double *w00, double *tb,
               double *tb00, double *time, double *xoffb, double *xofft, int nstep,
               sb_status *st);
