@@ -266,9 +266,9 @@ int sb_kspace_get(sb_kspace *ks, int col, long off, long len, double *host);
  * 5 and 6 the two y-line kernels of the split form, 12 the fused y-line kernel
  * (handles without temperature or y filter/dealiasing); with LES, 7..10 the four
  * LES plane kernels and 11 the LES y-line kernel; with implicit_visc, 13 the
- * factorisation of the substep's Helmholtz operators and 14 its y-line kernel.  The launches act on the
- * current device state, so a
- * run that used them must set the state again before stepping.
+ * factorisation of the substep's Helmholtz operators and 14 its y-line
+ * kernel.  The launches act on the current device state, so a run that used
+ * them must set the state again before stepping.
  * sb_fp64_peak measures the device's FP64 FMA throughput in TFLOP/s. */
 int sb_launch_stage(sb_handle *h, int stage, int rk, int count);
 
@@ -285,8 +285,9 @@ int sb_physical_fields(sb_handle *h, int member, unsigned mask, double *out);
  * columns per block of stages 1 and 3 (4 or 8), threads per block of stage 2
  * (the default or twice it) -- and the y-line tile, 1, 2 or 3 warps per line
  * solve (segments of the banded rows solved at once; each choice has its own
- * factor tables) in either form of the y-line stage (below), keeps the fastest
- * and re-captures the step graph.  choice (may be NULL) receives cb1, cb3, t2;
+ * factor tables) in either form of the y-line stage (below), then the side
+ * branch mask (sb_set_side_branch) on that tile, keeps the fastest and
+ * re-captures the step graph.  choice (may be NULL) receives cb1, cb3, t2;
  * sb_get_tuning gives cb1, cb3, t2 and the warps per line solve.  The state
  * itself is not changed; call it after sb_set_state and before sb_step.
  * sb_set_line_segments sets the warps per line solve directly (1..3; my - 3 >=
