@@ -217,3 +217,20 @@ def test_fortran_types_follow_the_c_structs():
     for tname, cls in (("sb_params", sb.SbParams), ("sb_status", sb.SbStatus)):
         assert [(n.lower(), t) for n, t in fields(tname)] == \
             [(n.lower(), t) for n, t in cls._fields_], tname
+
+
+def test_product_code_never_reaches_the_oracle():
+    """The package and its CUDA sources name no oracle module, library or
+    source: the oracle is test infrastructure only, and the product path has
+    no CPU fallback to route through it."""
+    pkg = os.path.join(ROOT, "shear_nnf_gb300")
+    hits = []
+    for d, _, files in os.walk(pkg):
+        if "_build" in d or "__pycache__" in d:
+            continue
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".cpp", ".h")):
+                txt = open(os.path.join(d, f), errors="replace").read()
+                if re.search(r"\boracle\b|liboracle|shearbox_oracle", txt, flags=re.I):
+                    hits.append(f)
+    assert hits == []
